@@ -1,0 +1,108 @@
+"""Build recipe and ctypes wrapper for the C restatement oracle (TEST INFRASTRUCTURE ONLY).
+
+``oracle/nsw6_oracle.c`` restates the reference's NSW6 step on the CPU; it is
+compiled here into ``oracle/_build/libnsw6_oracle[_omp].so``:
+
+  strict  -O2 -ffp-contract=off, serial: the checker used by the tests.
+  omp     -O3 -fopenmp: the multi-threaded CPU baseline ("port") of bench.py.
+
+Only tests, the golden-fixture script, ``__graft_entry__.smoke`` and the
+CPU-baseline leg of bench.py use this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+BUILD = HERE / "_build"
+if str(HERE.parent) not in sys.path:
+    sys.path.insert(0, str(HERE.parent))
+
+from nicam_kokkos_microphysics_gb300.state import MP_DRIVER_ARGS, region_shape  # noqa: E402
+
+VARIANTS = {
+    "strict": ["-O2", "-ffp-contract=off"],
+    "omp": ["-O3", "-ffp-contract=off", "-fopenmp"],
+}
+
+PARAM_NAMES = ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg", "ice_nuc", "kk_aut"]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in PARAM_NAMES]
+
+
+def lib_path(variant: str = "strict") -> Path:
+    return BUILD / ("libnsw6_oracle.so" if variant == "strict" else f"libnsw6_oracle_{variant}.so")
+
+
+def build(variant: str = "strict", force: bool = False) -> Path:
+    BUILD.mkdir(parents=True, exist_ok=True)
+    so = lib_path(variant)
+    src = [HERE / "nsw6_oracle.c", HERE / "nsw6_oracle.h", Path(__file__)]
+    if so.exists() and not force and all(so.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return so
+    cmd = ["gcc", "-std=c11", "-fPIC", "-shared", "-Wall", "-Wno-unused-variable",
+           *VARIANTS[variant], str(HERE / "nsw6_oracle.c"), "-o", str(so), "-lm"]
+    subprocess.run(cmd, check=True)
+    return so
+
+
+_LIBS: dict[str, ctypes.CDLL] = {}
+
+
+def load(variant: str = "strict", build_if_missing: bool = True) -> ctypes.CDLL:
+    lib = _LIBS.get(variant)
+    if lib is not None:
+        return lib
+    path = build(variant) if build_if_missing else lib_path(variant)
+    lib = ctypes.CDLL(str(path), mode=os.RTLD_LOCAL)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.nsw6o_default_params.argtypes = [ctypes.POINTER(Params)]
+    lib.nsw6o_mp_driver.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, ctypes.POINTER(Params),
+                                    ctypes.POINTER(ctypes.c_void_p), ctypes.c_double, ctypes.c_double,
+                                    ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+    lib.nsw6o_mp_driver.restype = ctypes.c_int
+    lib.nsw6o_max_threads.restype = ctypes.c_int
+    _LIBS[variant] = lib
+    return lib
+
+
+def default_params() -> dict[str, float]:
+    p = Params()
+    load().nsw6o_default_params(ctypes.byref(p))
+    return {n: getattr(p, n) for n in PARAM_NAMES}
+
+
+def mp_driver(reg: dict[str, np.ndarray], gz: np.ndarray, gzh: np.ndarray, dt: float, ct: float = 0.0,
+              params: dict[str, float] | None = None, variant: str = "strict", itelim: int = 100):
+    """Run the restated mp_driver in place on one region (per-region layout).
+
+    Returns (rc, status[4]) with rc 0 on success and 2 when the saturation
+    Newton iteration did not converge within ``itelim`` iterations.
+    """
+    lib = load(variant)
+    kall, gall = reg["rhog"].shape
+    p = Params()
+    lib.nsw6o_default_params(ctypes.byref(p))
+    for k, v in (params or {}).items():
+        setattr(p, k, float(v))
+    ptrs = (ctypes.c_void_p * len(MP_DRIVER_ARGS))()
+    for i, (name, kind, _) in enumerate(MP_DRIVER_ARGS):
+        a = reg[name]
+        if a.shape != region_shape(kind, kall, gall) or a.dtype != np.float64 or not a.flags.c_contiguous:
+            raise ValueError(f"argument {name}: bad shape/dtype {a.shape} {a.dtype}")
+        ptrs[i] = a.ctypes.data
+    gz = np.ascontiguousarray(gz, dtype=np.float64)
+    gzh = np.ascontiguousarray(gzh, dtype=np.float64)
+    st = (ctypes.c_int * 4)()
+    dp = ctypes.POINTER(ctypes.c_double)
+    rc = lib.nsw6o_mp_driver(gall, kall, gz.ctypes.data_as(dp), gzh.ctypes.data_as(dp), ctypes.byref(p), ptrs,
+                             float(dt), float(ct), int(itelim), st)
+    return rc, list(st)
