@@ -1,0 +1,338 @@
+#!/usr/bin/env python
+"""Benchmark of one NICAM NSW6 microphysics step on GB300.
+
+Workload (N=1): gall = 16900 (130 x 130 points), kall = 42, lall = 10 regions
+(7.1 M cells), dt = 60 s, FP64, seeded synthetic states (the NICAM snapshot the
+reference ships without is replaced by nicam_kokkos_microphysics_gb300.state).
+A step is one mp_driver call over all regions, in place, as the reference
+harness loops over SET_iteration (src/main.cpp:261-319).  The working set
+(about 3 GB) is far larger than the 129 MB L2, so no flush is needed between
+steps.
+
+Metric: cells per second per NSW6 step (gall * kall * lall / step time).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+For N > 1 (torchrun, one process per GPU) every rank steps its own lall
+regions (weak scaling, no collective on the data path); rank 0 prints the
+line with value = all cells / max step time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from nicam_kokkos_microphysics_gb300.state import (ARG_NAMES, MP_DRIVER_ARGS, StateSpec, batched_shape,  # noqa: E402
+                                                   make_state, region_view)
+
+METRIC = "cells/sec per NSW6 step (FP64)"
+UNIT = "cells/s"
+# Algorithmic bytes of one step per cell: 21 FP64 fields read and 28 written
+# (the minimum the step must touch, without read-for-ownership) plus ~3 B of
+# per-column outputs at kall = 42.
+ALGO_BYTES_PER_CELL = 49 * 8 + 3
+# Algorithmic bytes of the cell kernel per interior cell: it reads rhog,
+# rhogq(6), q(QV), tem, gsgam2 and writes rhog, rhoge, tem, rhogq(6), q(5),
+# re_liquid, re_cld.
+CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
+
+
+def env_rank():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def fp64_probe():
+    """FP64 pipe rate of this GPU (DFMA per second) from the throughput probe."""
+    import ctypes
+    from nicam_kokkos_microphysics_gb300 import _native
+    if not _native.PROBE_LIB.exists():
+        return None
+    lib = ctypes.CDLL(str(_native.PROBE_LIB))
+    lib.nsw6_probe_rate.restype = ctypes.c_double
+    lib.nsw6_probe_rate.argtypes = [ctypes.c_int, ctypes.c_int]
+    r = lib.nsw6_probe_rate(0, 4000)
+    return r if r > 0 else None
+
+
+# ----------------------------------------------------------------- CPU side
+def cpu_reference_sample(spec: StateSpec, steps: int, use_port: bool = False):
+    """Time the reference's CPU implementation on one region per step.
+
+    Uses the reference's own sources built with the OpenMP Kokkos shim
+    (oracle/_ref) when they are available, else the OpenMP build of the C
+    restatement.  Returns (cells/s, kind, threads, seconds per step list)."""
+    from oracle import build_ref, restatement
+    one = StateSpec(gall=spec.gall, kall=spec.kall, lall=1, seed=spec.seed, variant=spec.variant, dt=spec.dt)
+    st = make_state(one, out_fill=0.0)
+    reg = region_view(st, 0)
+    cells = one.gall * one.kall
+    times = []
+    if not use_port and build_ref.sources_available():
+        from oracle import ref
+        lib = ref.load(one.gall, one.kall, st["_gz"], st["_gzh"], variant="omp")
+        kind = "reference"
+        threads = os.cpu_count()
+        run = lambda: ref.mp_driver(lib, reg, one.dt)  # noqa: E731
+    else:
+        kind = "port"
+        lib = restatement.load("omp")
+        threads = lib.nsw6o_max_threads()
+        run = lambda: restatement.mp_driver(reg, st["_gz"], st["_gzh"], one.dt, variant="omp")  # noqa: E731
+    run()  # warm-up
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        run()
+        times.append(time.perf_counter() - t0)
+    med = statistics.median(times)
+    return cells / med, kind, threads, times
+
+
+def run_reference_arm(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    spec = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall, seed=args.seed, variant=args.variant)
+    total = max(args.warmup, 0)
+    v, kind, threads, times = cpu_reference_sample(spec, max(args.steps, 1) + 0 * total)
+    ms = statistics.median(times) * 1e3
+    line = {
+        "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NICAM-like state)",
+        "impl": "reference",
+        "config": {"workload": f"NSW6 step, gall={spec.gall} kall={spec.kall}, one region per step "
+                               f"(sample of lall={spec.lall})", "variant": spec.variant},
+        "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+                         "sample": f"{args.steps} steps x 1 region of {spec.gall}x{spec.kall} cells, median"},
+        "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ----------------------------------------------------------------- GPU side
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description="NSW6 step benchmark")
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--gall", type=int, default=16900)
+    ap.add_argument("--kall", type=int, default=42)
+    ap.add_argument("--lall", type=int, default=10)
+    ap.add_argument("--variant", default="standard", choices=["standard", "convective", "cold"])
+    ap.add_argument("--seed", type=int, default=1002)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference_arm(args)
+
+    import torch
+    rank, world, local = env_rank()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    from nicam_kokkos_microphysics_gb300 import mp_init
+
+    spec = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall, seed=args.seed + 7919 * rank,
+                     variant=args.variant)
+    st = make_state(spec, out_fill=0.0)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    dev = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
+    args_dev = [dev[n] for n in ARG_NAMES]
+    drv.set_sync_check(False)
+
+    def step():
+        drv.mp_driver_batched(spec.lall, *args_dev, dt=spec.dt, ct=0.0)
+
+    for _ in range(args.warmup):
+        step()
+    rc, cell = drv.last_error()
+    if rc != 0:
+        raise RuntimeError(f"warm-up step failed with status {rc} at {cell}")
+
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    drv.set_timing(True)
+    drv.read_timing()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    t_cell, t_col, nsteps = drv.read_timing()
+    drv.set_timing(False)
+    rc, cell = drv.last_error()
+    if rc != 0:
+        raise RuntimeError(f"timed steps failed with status {rc} at {cell}")
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    cells_rank = spec.cells
+    value = cells_rank * world / (ms * 1e-3)
+
+    # ---- end to end through the public API with host (pinned) buffers
+    e2e = None
+    if not args.no_e2e:
+        host = {}
+        for n in ARG_NAMES:
+            t = torch.empty(st[n].shape, dtype=torch.float64, pin_memory=True)
+            t.numpy()[...] = st[n]
+            host[n] = t.numpy()
+        from nicam_kokkos_microphysics_gb300._native import load as _load  # noqa: F401
+        import ctypes
+        kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
+        read_args = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "vx", "vy", "vz", "tem", "q",
+                     "gsgam2", "gsgam2h", "gam2", "gam2h", "ix", "iy", "iz", "jx", "jy", "jz", "z"]
+        write_args = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "rho", "tem", "pre", "q", "qd",
+                      "precip", "ISO1_precip", "ISO2_precip", "precip_rhoe", "precip_lh_heat", "precip_rhophi",
+                      "precip_rhokin", "re_liquid", "re_solid", "re_cld", "rctop", "rwtop", "tctop", "GDCLW",
+                      "GDCFRC", "GPREC"]
+        nbytes = lambda n: int(np.prod(batched_shape(kinds[n], spec.lall, spec.kall, spec.gall))) * 8  # noqa: E731
+        h2d = sum(nbytes(n) for n in read_args)
+        d2h = sum(nbytes(n) for n in write_args)
+        drv.run(host, dt=spec.dt)  # warm-up (allocates the staging buffers)
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            drv.run(host, dt=spec.dt)
+        dt_e2e = (time.perf_counter() - t0) / args.steps
+        if dist:
+            t = torch.tensor([dt_e2e], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt_e2e = float(t.item())
+        e2e = {"value": cells_rank * world / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": dt_e2e * 1e3}
+
+    # ---- roofline of the dominant kernel
+    peaks, src = measured_peaks()
+    n_int = spec.gall * (spec.kall - 2) * spec.lall
+    cell_ms = t_cell / max(nsteps, 1)
+    col_ms = t_col / max(nsteps, 1)
+    dfma = fp64_probe()
+    achieved_gbs = CELL_KERNEL_BYTES_PER_CELL * n_int / (cell_ms * 1e-3) / 1e9
+    roofline = {"kernel": "nsw6_cell_kernel", "bound": "hbm", "achieved": achieved_gbs,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
+                "traffic": None, "peak_source": f"{src} copy bandwidth",
+                "cell_kernel_ms": cell_ms, "column_kernel_ms": col_ms,
+                "fp64_fma_per_s_measured": dfma,
+                "note": "the cell kernel is FP64-pipe bound; the HBM fraction is reported for reference"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        v, kind, threads, times = cpu_reference_sample(spec, 3)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
+               "sample": f"3 steps x 1 region of {spec.gall}x{spec.kall} cells (median), OpenMP"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NICAM-like state)",
+        "config": {"workload": f"NSW6 FP64 step, gall={spec.gall} kall={spec.kall} lall={spec.lall} per GPU "
+                               f"({spec.cells} cells), dt={spec.dt}", "variant": spec.variant,
+                   "l2": "working set >> L2 (no flush needed)", "parallelism": f"regions x{world}"},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+        "gpu_launches": 2 * args.steps,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    drv.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

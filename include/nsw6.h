@@ -1,0 +1,162 @@
+/* nsw6.h - C ABI of the GB300-native NICAM NSW6 microphysics step.
+ *
+ * Drop-in for the reference's MP_DRIVER::mp_driver (Kokkos version,
+ * src/mod_mp_driver.h:71-124, src/mod_mp_driver.cpp:335-613) with
+ * MP_TYPE = "NSW6": same argument list, same order, same (gall, kall, lall)
+ * structure-of-arrays layout (C order, g fastest), FP64, updated in place.
+ * Pointers are CUDA device pointers unless a function says otherwise.
+ *
+ * The one-time set-up the reference performs through process globals
+ * (GRD_Setup mod_debug.cpp:92-187, CVW_CPW_Setup mod_debug.cpp:76-90,
+ * SATURATION_Setup mod_satadjust.cpp:24-47, mp_init/mp_nsw6_init
+ * mod_mp_driver.cpp:11-24 / mod_mp_nsw6.cpp:276-434) is held in an opaque
+ * handle instead, so several grids can coexist in one process.
+ *
+ * Error convention: every function returns an nsw6_status (0 = success).
+ * The device never traps: a saturation-adjustment Newton iteration that does
+ * not converge (the reference calls Kokkos::abort, mod_satadjust.cpp:883-891)
+ * is recorded in a device status word and reported as NSW6_ERR_NOCONV or
+ * NSW6_ERR_NAN; nsw6_last_error() gives the first failing cell.
+ *
+ * Threading: a handle is not re-entrant; calls on one handle must not overlap.
+ * All work of a call is issued on the handle's CUDA stream.
+ */
+#ifndef NSW6_H
+#define NSW6_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSW6_ABI_VERSION 1
+
+typedef enum nsw6_status {
+  NSW6_OK = 0,
+  NSW6_ERR_BAD_ARG = 1,      /* null pointer, bad size, region out of range          */
+  NSW6_ERR_CUDA = 2,         /* a CUDA runtime call failed                           */
+  NSW6_ERR_NOCONV = 3,       /* satadjust Newton hit the iteration limit             */
+  NSW6_ERR_NAN = 4,          /* satadjust produced a non-finite temperature          */
+  NSW6_ERR_UNSUPPORTED = 5   /* configuration not implemented                        */
+} nsw6_status;
+
+/* Tunable NSW6 scheme parameters (GlobalParams, src/mod_mp_nsw6.h:16-123,
+ * values as set by mp_nsw6_init).  Differentiable parameters of the
+ * tangent-linear/adjoint entry points follow this order. */
+typedef struct nsw6_params {
+  double beta_saut;   /* ice->snow autoconversion rate      [1/s]  mod_mp_nsw6.cpp:287-294, used :1162 */
+  double qicrt_saut;  /* ice->snow autoconversion threshold [kg/kg] mod_mp_nsw6.h:87, used :1163       */
+  double Cr;          /* rain fall-speed coefficient               mod_mp_nsw6.h:27, used :1076         */
+  double Cs;          /* snow fall-speed coefficient               mod_mp_nsw6.h:28, used :1077         */
+  double Cg;          /* graupel fall-speed coefficient            mod_mp_nsw6.cpp:337, used :1078      */
+  double ice_nuc;     /* ice nucleation coefficient of Qi0         literal at mod_mp_nsw6.cpp:1083      */
+  double kk_aut;      /* KK2000 warm-rain autoconversion rate      literal at mod_mp_nsw6.cpp:1156      */
+} nsw6_params;
+
+typedef struct nsw6_handle nsw6_handle;
+
+/* Fills *p with the values of the reference configuration. */
+void nsw6_default_params(nsw6_params* p);
+
+/* Creates a handle for regions of gall columns and kall levels (5 <= kall <=
+ * 160; kmin = 1, kmax = kall-2, as include/problemsize.h:62-79) and up to lall_max regions
+ * per batched call.  gz/gzh are the full-level and interface heights [kall]
+ * in HOST memory (the contents of GRD_gz.dat / GRD_gzh.dat read by
+ * GRD_Input_vgrid, mod_debug.cpp:189-195).  Allocates all device workspace;
+ * no later call allocates.  Uses the current CUDA device. */
+int nsw6_create(nsw6_handle** h, int gall, int kall, int lall_max, const double* gz, const double* gzh);
+int nsw6_destroy(nsw6_handle* h);
+
+int nsw6_set_params(nsw6_handle* h, const nsw6_params* p);
+int nsw6_get_params(const nsw6_handle* h, nsw6_params* p);
+
+/* Stream (cudaStream_t, may be 0) on which all work of the handle runs. */
+int nsw6_set_stream(nsw6_handle* h, void* stream);
+
+/* When sync_check is non-zero (the default) every mp_driver call waits for
+ * its work and returns the device status (like the reference, whose
+ * mp_driver ends with Kokkos::fence).  When zero, calls return after
+ * enqueueing; read the status with nsw6_last_error. */
+int nsw6_set_sync_check(nsw6_handle* h, int sync_check);
+
+/* Newton iteration limit of the saturation adjustment (reference: itelim = 100,
+ * mod_satadjust.cpp:809). */
+int nsw6_set_itelim(nsw6_handle* h, int itelim);
+
+/* Per-kernel timing with CUDA events recorded on the handle's stream around
+ * each kernel of every step (0 = off, the default). */
+int nsw6_set_timing(nsw6_handle* h, int on);
+
+/* Synchronises and returns the kernel time accumulated since the previous
+ * read, in milliseconds: t[0] cell kernel, t[1] column kernel (n >= 2), and
+ * the number of steps timed.  Resets the accumulators. */
+int nsw6_read_timing(nsw6_handle* h, double* t, int n, int* steps);
+
+/* Synchronises the handle's stream and returns the status of the work issued
+ * since the previous call; *k, *g, *l and *iters (any may be NULL) give the
+ * first failing cell.  Clears the device status word. */
+int nsw6_last_error(nsw6_handle* h, int* k, int* g, int* l, int* iters);
+
+const char* nsw6_strerror(int status);
+
+/* One NSW6 step on one region: replaces MP_DRIVER::mp_driver
+ * (src/mod_mp_driver.cpp:335-388), same arguments in the same order.
+ * 2-D fields are [kall][gall], tracer fields [6][kall][gall] (QV QC QR QI QS
+ * QG), precip/ISO1_precip/ISO2_precip [2][gall], precip_rhoe..precip_rhokin
+ * and ix..jz [gall], rctop/rwtop/tctop [1][gall].  w, unccn, frhoge_af,
+ * frhogqv_af, frhoge_rad, rhogqke, zh, ct and CBMFX are accepted and unused,
+ * as in the reference. */
+int mp_driver(nsw6_handle* h, int l_region,
+              double* rhog, double* rhogvx, double* rhogvy, double* rhogvz, double* rhogw, double* rhoge,
+              double* rhogq,
+              const double* vx, const double* vy, const double* vz, const double* w, const double* unccn,
+              double* rho, double* tem, double* pre,
+              double* q, double* qd,
+              double* precip, double* ISO1_precip, double* ISO2_precip,
+              double* precip_rhoe, double* precip_lh_heat, double* precip_rhophi, double* precip_rhokin,
+              double* re_liquid, double* re_solid, double* re_cld,
+              double* rctop, double* rwtop, double* tctop,
+              const double* frhoge_af, const double* frhogqv_af, const double* frhoge_rad, const double* rhogqke,
+              const double* gsgam2, const double* gsgam2h, const double* gam2, const double* gam2h,
+              const double* ix, const double* iy, const double* iz,
+              const double* jx, const double* jy, const double* jz,
+              const double* z, const double* zh,
+              double dt, double ct,
+              double* GDCLW, double* GDCFRC, double* GPREC, const double* CBMFX);
+
+/* All lall regions in one launch sequence, arrays in the reference harness's
+ * all-regions layout (src/main.cpp:19-90): [lall][kall][gall] fields,
+ * [lall][6][kall][gall] tracers, [2][lall][gall] precipitation (the
+ * precip_mp layout with ADM_KNONE = 1), [lall][gall] column fields and
+ * [lall][1][gall] cloud-top fields.  The cross-column reductions of the
+ * sedimentation scheme (vadv1d_prep, mod_vadv1d.cpp:316-353) stay per region,
+ * so the result equals lall mp_driver calls. */
+int mp_driver_batched(nsw6_handle* h, int lall,
+                      double* rhog, double* rhogvx, double* rhogvy, double* rhogvz, double* rhogw, double* rhoge,
+                      double* rhogq,
+                      const double* vx, const double* vy, const double* vz, const double* w, const double* unccn,
+                      double* rho, double* tem, double* pre,
+                      double* q, double* qd,
+                      double* precip, double* ISO1_precip, double* ISO2_precip,
+                      double* precip_rhoe, double* precip_lh_heat, double* precip_rhophi, double* precip_rhokin,
+                      double* re_liquid, double* re_solid, double* re_cld,
+                      double* rctop, double* rwtop, double* tctop,
+                      const double* frhoge_af, const double* frhogqv_af, const double* frhoge_rad,
+                      const double* rhogqke,
+                      const double* gsgam2, const double* gsgam2h, const double* gam2, const double* gam2h,
+                      const double* ix, const double* iy, const double* iz,
+                      const double* jx, const double* jy, const double* jz,
+                      const double* z, const double* zh,
+                      double dt, double ct,
+                      double* GDCLW, double* GDCFRC, double* GPREC, const double* CBMFX);
+
+/* Same as mp_driver_batched with the 50 array arguments passed as an array
+ * of pointers in the reference order (args[0] = rhog ... args[49] = CBMFX).
+ * When `host` is non-zero the pointers are HOST memory: the call copies the
+ * inputs to device workspace, runs the step and copies the outputs back
+ * (synchronous).  This is the entry point a ctypes/cffi/FFI binding uses. */
+int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSW6_H */

@@ -1,0 +1,219 @@
+"""GB300-native NICAM NSW6 microphysics step.
+
+Python mirror of the reference's driver interface (src/mod_mp_driver.h):
+
+* ``mp_init(MP_TYPE, gall, kall, gz, gzh, lall_max=1)`` replaces the set-up
+  sequence GRD_Setup / CVW_CPW_Setup / SATURATION_Setup / mp_init of the
+  reference harness (src/main.cpp:177-189) and returns an :class:`MPDriver`.
+  Like the reference (mod_mp_driver.cpp:11-24) it accepts only "NSW6".
+* ``MPDriver.mp_driver(l_region, rhog, ..., dt, ct, GDCLW, GDCFRC, GPREC,
+  CBMFX)`` takes the reference's 50 array arguments in the reference's order
+  (float64 CUDA tensors, updated in place) and runs one NSW6 step on one
+  region through the C ABI of ``include/nsw6.h``.
+* ``MPDriver.mp_driver_batched(lall, ...)`` does the same for ``lall``
+  regions stored in the all-regions layout of the reference harness.
+* ``MPDriver.run(state, dt)`` takes a dict keyed by the reference argument
+  names; numpy (host) arrays go through the host-memory entry point.
+
+All compute runs in the CUDA library built from ``csrc/``; when it is missing
+the import of this API fails with an explicit error.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Any
+
+import numpy as np
+
+from . import _native
+from .state import ARG_NAMES, MP_DRIVER_ARGS, batched_shape, region_shape
+
+__all__ = ["MPDriver", "mp_init", "NSW6Error", "PARAM_NAMES", "default_params"]
+
+PARAM_NAMES = ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg", "ice_nuc", "kk_aut"]
+
+NSW6_OK, NSW6_ERR_BAD_ARG, NSW6_ERR_CUDA, NSW6_ERR_NOCONV, NSW6_ERR_NAN = 0, 1, 2, 3, 4
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in PARAM_NAMES]
+
+
+class NSW6Error(RuntimeError):
+    def __init__(self, code: int, msg: str, cell: tuple[int, int, int, int] | None = None):
+        super().__init__(f"nsw6 error {code}: {msg}" + (f" (k={cell[0]} g={cell[1]} l={cell[2]} iters={cell[3]})"
+                                                        if cell else ""))
+        self.code = code
+        self.cell = cell
+
+
+def default_params() -> dict[str, float]:
+    lib = _native.load()
+    p = _Params()
+    lib.nsw6_default_params(ctypes.byref(p))
+    return {n: getattr(p, n) for n in PARAM_NAMES}
+
+
+def _check(rc: int, lib, handle=None) -> None:
+    if rc == NSW6_OK:
+        return
+    cell = None
+    msg = lib.nsw6_strerror(rc).decode()
+    raise NSW6Error(rc, msg, cell)
+
+
+class MPDriver:
+    """One NSW6 configuration on one grid: owns the device workspace."""
+
+    def __init__(self, gall: int, kall: int, gz, gzh, lall_max: int = 1, params: dict | None = None):
+        self._lib = _native.load()
+        self.gall, self.kall, self.lall_max = int(gall), int(kall), int(lall_max)
+        gz = np.ascontiguousarray(gz, dtype=np.float64)
+        gzh = np.ascontiguousarray(gzh, dtype=np.float64)
+        if gz.shape != (self.kall,) or gzh.shape != (self.kall,):
+            raise ValueError("gz and gzh must have kall elements")
+        h = ctypes.c_void_p()
+        rc = self._lib.nsw6_create(ctypes.byref(h), self.gall, self.kall, self.lall_max,
+                                   gz.ctypes.data, gzh.ctypes.data)
+        _check(rc, self._lib)
+        self._h = h
+        if params:
+            self.set_params(**params)
+
+    # ------------------------------------------------------------ lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.nsw6_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ------------------------------------------------------------ settings
+    def get_params(self) -> dict[str, float]:
+        p = _Params()
+        _check(self._lib.nsw6_get_params(self._h, ctypes.byref(p)), self._lib)
+        return {n: getattr(p, n) for n in PARAM_NAMES}
+
+    def set_params(self, **kw: float) -> None:
+        cur = self.get_params()
+        for k, v in kw.items():
+            if k not in cur:
+                raise KeyError(f"unknown NSW6 parameter {k!r}")
+            cur[k] = float(v)
+        p = _Params(**cur)
+        _check(self._lib.nsw6_set_params(self._h, ctypes.byref(p)), self._lib)
+
+    def set_itelim(self, itelim: int) -> None:
+        _check(self._lib.nsw6_set_itelim(self._h, int(itelim)), self._lib)
+
+    def set_sync_check(self, on: bool) -> None:
+        _check(self._lib.nsw6_set_sync_check(self._h, int(bool(on))), self._lib)
+
+    def set_stream(self, stream: Any) -> None:
+        """cudaStream_t as int, or a torch.cuda.Stream."""
+        ptr = getattr(stream, "cuda_stream", stream)
+        _check(self._lib.nsw6_set_stream(self._h, ctypes.c_void_p(int(ptr or 0))), self._lib)
+
+    def set_timing(self, on: bool) -> None:
+        _check(self._lib.nsw6_set_timing(self._h, int(bool(on))), self._lib)
+
+    def read_timing(self) -> tuple[float, float, int]:
+        """(cell kernel ms, column kernel ms, steps) accumulated since the last read."""
+        t = (ctypes.c_double * 2)()
+        n = ctypes.c_int()
+        _check(self._lib.nsw6_read_timing(self._h, t, 2, ctypes.byref(n)), self._lib)
+        return t[0], t[1], n.value
+
+    def last_error(self) -> tuple[int, tuple[int, int, int, int]]:
+        k, g, l, it = (ctypes.c_int() for _ in range(4))
+        rc = self._lib.nsw6_last_error(self._h, ctypes.byref(k), ctypes.byref(g), ctypes.byref(l), ctypes.byref(it))
+        return rc, (k.value, g.value, l.value, it.value)
+
+    def _raise_status(self, rc: int) -> None:
+        if rc == NSW6_OK:
+            return
+        raise NSW6Error(rc, self._lib.nsw6_strerror(rc).decode())
+
+    # ------------------------------------------------------------ calls
+    def _device_ptrs(self, args, shapes) -> list[int]:
+        import torch
+        ptrs = []
+        for (name, _, _), a, shp in zip(MP_DRIVER_ARGS, args, shapes):
+            if not isinstance(a, torch.Tensor):
+                raise TypeError(f"{name}: expected a CUDA tensor, got {type(a).__name__}")
+            if a.device.type != "cuda" or a.dtype != torch.float64 or not a.is_contiguous():
+                raise ValueError(f"{name}: expected a contiguous float64 CUDA tensor")
+            if tuple(a.shape) != tuple(shp):
+                raise ValueError(f"{name}: expected shape {tuple(shp)}, got {tuple(a.shape)}")
+            ptrs.append(a.data_ptr())
+        return ptrs
+
+    def _use_torch_stream(self) -> None:
+        import torch
+        self.set_stream(torch.cuda.current_stream().cuda_stream)
+
+    def mp_driver(self, l_region: int, *args, dt: float | None = None, ct: float = 0.0):
+        """Reference argument order: 46 arrays, dt, ct, 4 arrays (mod_mp_driver.h:71-124)."""
+        arrays, dt, ct = _split_args(args, dt, ct)
+        shapes = [region_shape(kind, self.kall, self.gall) for _, kind, _ in MP_DRIVER_ARGS]
+        ptrs = self._device_ptrs(arrays, shapes)
+        self._use_torch_stream()
+        rc = self._lib.mp_driver(self._h, int(l_region), *ptrs[:46], float(dt), float(ct), *ptrs[46:])
+        self._raise_status(rc)
+
+    def mp_driver_batched(self, lall: int, *args, dt: float | None = None, ct: float = 0.0):
+        arrays, dt, ct = _split_args(args, dt, ct)
+        shapes = [batched_shape(kind, lall, self.kall, self.gall) for _, kind, _ in MP_DRIVER_ARGS]
+        ptrs = self._device_ptrs(arrays, shapes)
+        self._use_torch_stream()
+        rc = self._lib.mp_driver_batched(self._h, int(lall), *ptrs[:46], float(dt), float(ct), *ptrs[46:])
+        self._raise_status(rc)
+
+    def run(self, state: dict, dt: float, ct: float = 0.0, lall: int | None = None) -> None:
+        """Run one step in place on a dict keyed by the reference argument names.
+
+        Arrays are in the all-regions layout (see ``state.batched_shape``).
+        CUDA tensors run on the device; numpy arrays go through the host entry
+        point, which copies inputs in and outputs back inside the call.
+        """
+        first = state[ARG_NAMES[0]]
+        if lall is None:
+            lall = first.shape[0]
+        if isinstance(first, np.ndarray):
+            ptrs = (ctypes.c_void_p * len(ARG_NAMES))()
+            for i, (name, kind, _) in enumerate(MP_DRIVER_ARGS):
+                a = state[name]
+                if a.shape != batched_shape(kind, lall, self.kall, self.gall) or a.dtype != np.float64 \
+                        or not a.flags.c_contiguous:
+                    raise ValueError(f"{name}: expected contiguous float64 array of shape "
+                                     f"{batched_shape(kind, lall, self.kall, self.gall)}")
+                ptrs[i] = a.ctypes.data
+            rc = self._lib.mp_driver_argv(self._h, int(lall), ptrs, float(dt), float(ct), 1)
+            self._raise_status(rc)
+            return
+        self.mp_driver_batched(lall, *[state[n] for n in ARG_NAMES], dt=dt, ct=ct)
+
+    def run_argv(self, lall: int, ptrs: list[int], dt: float, ct: float = 0.0, host: bool = False) -> int:
+        """Raw entry point: 50 pointers in reference order; returns the status code."""
+        arr = (ctypes.c_void_p * len(ARG_NAMES))(*ptrs)
+        return self._lib.mp_driver_argv(self._h, int(lall), arr, float(dt), float(ct), int(host))
+
+
+def _split_args(args, dt, ct):
+    """Accept either (46 arrays, dt, ct, 4 arrays) or 50 arrays with dt/ct keywords."""
+    if len(args) == 52:
+        return list(args[:46]) + list(args[48:]), float(args[46]), float(args[47])
+    if len(args) == 50 and dt is not None:
+        return list(args), float(dt), float(ct)
+    raise TypeError("expected the 50 mp_driver arrays with dt and ct in the reference order")
+
+
+def mp_init(MP_TYPE: str, gall: int, kall: int, gz, gzh, lall_max: int = 1, params: dict | None = None) -> MPDriver:
+    """Set up the microphysics driver (mod_mp_driver.cpp:11-24): only "NSW6" exists."""
+    if MP_TYPE != "NSW6":
+        raise ValueError(f"mp_init: NOT appropriate type. Type: {MP_TYPE}")
+    return MPDriver(gall, kall, gz, gzh, lall_max=lall_max, params=params)

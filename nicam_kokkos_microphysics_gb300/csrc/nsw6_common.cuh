@@ -1,0 +1,131 @@
+// Shared definitions of the GB300 NSW6 kernels: physical constants, the scheme
+// constant block passed to every kernel, launch geometry and small helpers.
+#pragma once
+
+#include <cstdint>
+
+#ifndef __CUDACC__
+#define __host__
+#define __device__
+#define __forceinline__ inline
+#endif
+
+namespace nsw6 {
+
+// ------------------------------------------------------------------ constants
+// include/problemsize.h:86-135 and private module constants.
+constexpr double PI = 3.141592653589793;
+constexpr double EPS = 2.220446E-16;
+constexpr double UNDEF = -9.9999E+30;
+constexpr double GRAV = 9.79764;
+constexpr double RDRY = 287.04;
+constexpr double CVDRY = 717.56;
+constexpr double RVAP = 461.46;
+constexpr double CL = 4218.0;
+constexpr double PSAT0 = 610.7;
+constexpr double LHV0 = 2501000.0;
+constexpr double LHS0 = 2834000.0;
+constexpr double LHF0 = 333000.0;
+constexpr double PSTD = 101325.0;
+constexpr double TEM00 = 273.15;
+constexpr double DWATR = 1000.0;
+constexpr double TEM_MIN = 10.0;   // mod_satadjust.cpp:6
+constexpr double DENS00 = 1.28;    // mod_mp_nsw6.cpp:8
+constexpr int NQ = 6;
+constexpr int I_QV = 0, I_QC = 1, I_QR = 2, I_QI = 3, I_QS = 4, I_QG = 5;
+
+// Tile geometry.  The cell kernel gives one CTA CELL_TG columns x all interior
+// levels; the column kernel one CTA 16 (kall <= 64) or 8 columns x all levels.
+constexpr int CELL_TG = 32;
+constexpr int CELL_THREADS = 256;
+constexpr int MAX_KALL = 160;
+
+// Scheme constants: mp_nsw6_init (mod_mp_nsw6.cpp:276-434) with the settings it
+// hard-wires, the effective-radius constants of mp_nsw6_new::init
+// (mod_mp_nsw6.cpp:506-517) and SATURATION_Setup (mod_satadjust.cpp:24-47).
+// Built once on the host (same libm as the oracle) and passed by value.
+struct Consts {
+  double Ar, As, Ag, Cr, Cs, Cg, N0r, N0s, N0g;
+  double GAM_1br, GAM_2br, GAM_3br, GAM_3dr, GAM_6dr, GAM_1brdr, GAM_5dr_h;
+  double GAM_1bs, GAM_2bs, GAM_3bs, GAM_3ds, GAM_1bsds, GAM_5ds_h;
+  double GAM_1bg, GAM_3dg, GAM_1bgdg, GAM_5dg_h;
+  double Esi, Egs, gamma_sacr, gamma_gacs, mi;
+  double beta_saut, gamma_saut, qicrt_saut;
+  double A_frz, B_frz, mi40, mi50, Ri50;
+  double Nc_ihtr, Di_max, Di_a, ln10;
+  double coef_a[10], coef_b[10];
+  double Nc_def, coef_dgam, coef_xf;
+  double ice_nuc, kk_aut;
+  double LovR_liq, LovR_ice, RTEM00;
+  double dtemp_criteria;
+  // derived products that appear verbatim in the reference expressions
+  double log_mi50, log_mi40;
+  double Dc_berry, pow_Nc_m179;
+};
+
+// Per-level grid metrics (GRD_Setup, mod_debug.cpp:92-187), device copy laid
+// out as [field][kall].
+enum GridField {
+  GF_GZ, GF_GZH, GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH, GF_AFACT, GF_BFACT, GF_CFACT, GF_DFACT, GF_GZSHIFT, GF_COUNT
+};
+
+// Argument positions of mp_driver (mod_mp_driver.h:71-124).
+enum Arg {
+  A_rhog, A_rhogvx, A_rhogvy, A_rhogvz, A_rhogw, A_rhoge, A_rhogq, A_vx, A_vy, A_vz, A_w,
+  A_unccn, A_rho, A_tem, A_pre, A_q, A_qd, A_precip, A_ISO1, A_ISO2, A_precip_rhoe,
+  A_precip_lh_heat, A_precip_rhophi, A_precip_rhokin, A_re_liquid, A_re_solid, A_re_cld,
+  A_rctop, A_rwtop, A_tctop, A_frhoge_af, A_frhogqv_af, A_frhoge_rad, A_rhogqke, A_gsgam2,
+  A_gsgam2h, A_gam2, A_gam2h, A_ix, A_iy, A_iz, A_jx, A_jy, A_jz, A_z, A_zh, A_GDCLW,
+  A_GDCFRC, A_GPREC, A_CBMFX, A_COUNT
+};
+
+// Device status word: first failure wins.
+struct DevStatus {
+  int code;   // 0 ok, NSW6_ERR_NOCONV, NSW6_ERR_NAN
+  int k, g, l, iters;
+};
+
+// Problem description handed to the kernels.  Array pointers follow the
+// all-regions layout; per-region calls use lall = 1.
+struct Problem {
+  int gall, kall, kmin, kmax, lall;
+  double dt, dt2, dt3;   // dt, pow(dt,2), pow(dt,3) as vadv1d_prep forms them (mod_vadv1d.cpp:265-266)
+  int itelim;
+  const double* grid;          // [GF_COUNT][kall]
+  double* const* a;            // not used on device
+  // field bases
+  double *rhog, *rhogvx, *rhogvy, *rhogvz, *rhogw, *rhoge, *rhogq;
+  const double *vx, *vy, *vz;
+  double *rho, *tem, *pre, *q, *qd;
+  double *precip, *iso1, *iso2;          // [2][lall][gall]
+  double *precip_rhoe, *precip_lh_heat, *precip_rhophi, *precip_rhokin;   // [lall][gall]
+  double *re_liquid, *re_solid, *re_cld;
+  double *rctop, *rwtop, *tctop;         // [lall][1][gall]
+  const double *gsgam2, *gsgam2h, *gam2, *gam2h;
+  const double *ix, *iy, *iz, *jx, *jy, *jz;
+  const double* z;
+  double *GDCLW, *GDCFRC, *GPREC;
+  // workspace
+  double* zdis;                // [lall][6][kall][gall]: zdis0 (QR,QS,QG) then zdis0h (QR,QS,QG)
+  unsigned long long* zmax;    // [lall][6][kall] ordered keys, reset to 0
+  unsigned long long* zmin;    // [lall][6][kall] ordered keys, reset to ~0
+  DevStatus* status;
+};
+
+__host__ __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }  // Kokkos::min
+__host__ __device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }  // Kokkos::max
+
+// Order-preserving map double -> uint64 (total order, -0 < +0), used for exact
+// atomic max/min of the per-level departure-distance extrema.
+__host__ __device__ __forceinline__ unsigned long long order_key(double v) {
+  union { double d; unsigned long long u; } c;
+  c.d = v;
+  return (c.u >> 63) ? ~c.u : (c.u | 0x8000000000000000ull);
+}
+__host__ __device__ __forceinline__ double key_value(unsigned long long k) {
+  union { double d; unsigned long long u; } c;
+  c.u = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  return c.d;
+}
+
+}  // namespace nsw6

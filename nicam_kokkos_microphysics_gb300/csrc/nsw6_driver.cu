@@ -1,0 +1,568 @@
+// Host driver and C ABI of the GB300 NSW6 step (see include/nsw6.h).
+//
+// Replaces MP_DRIVER::mp_init / mp_driver (src/mod_mp_driver.cpp:11-24,
+// 335-613) and the set-up routines the reference runs through globals:
+// GRD_Setup (mod_debug.cpp:92-187), SATURATION_Setup (mod_satadjust.cpp:24-47)
+// and mp_nsw6_init (mod_mp_nsw6.cpp:276-434).  All device memory a step needs
+// is allocated in nsw6_create; a step enqueues two memsets and two kernels.
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+
+#include <cuda_runtime.h>
+
+#include "../../include/nsw6.h"
+#include "nsw6_common.cuh"
+
+namespace nsw6 {
+cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev);
+}
+
+using namespace nsw6;
+
+struct nsw6_handle {
+  int gall = 0, kall = 0, lall_max = 0;
+  nsw6_params params{};
+  Consts C{};
+  double* d_grid = nullptr;
+  double* d_zdis = nullptr;
+  unsigned long long* d_zmax = nullptr;
+  unsigned long long* d_zmin = nullptr;
+  DevStatus* d_status = nullptr;
+  cudaStream_t stream = nullptr;
+  int sync_check = 1;
+  int itelim = 100;
+  // device staging of the 50 arguments for host-memory calls (allocated by the
+  // first such call)
+  double* d_stage = nullptr;
+  size_t stage_count = 0;
+  // kernel timing: a ring of event triples folded into the sums when full
+  int timing = 0;
+  static constexpr int kRing = 64;
+  cudaEvent_t ev[kRing][3] = {};
+  int ev_used = 0;
+  double t_sum[2] = {0.0, 0.0};
+  int t_steps = 0;
+};
+
+namespace {
+
+// MISC_gammafunc, mod_debug.cpp:332-361.
+double gammafunc(double xx) {
+  static const double coef[6] = {+76.18009172947146, -86.50532032941677, +24.01409824083091,
+                                 -1.231739572450155, +0.1208650973866179E-2, -0.5395239384953E-5};
+  double x = xx, y = x, tmp = x + 5.5;
+  tmp = tmp - (x + 0.5) * std::log(tmp);
+  double ser = 1.000000000190015;
+  for (int j = 0; j < 6; ++j) {
+    y += 1;
+    ser += coef[j] / y;
+  }
+  return std::exp(-tmp + std::log(2.5066282746310005 * ser / x));
+}
+
+// mp_nsw6_init (mod_mp_nsw6.cpp:276-434) with its hard-wired choices (Roh and
+// Satoh 2014 snow, explicit ice generation, KK2000 autoconversion,
+// beta_gaut = 0), GlobalParams defaults (mod_mp_nsw6.h:16-123), the
+// effective-radius constants of mp_nsw6_new::init (:506-517) and
+// SATURATION_Setup with EIN_TYPE = "SIMPLE" (mod_satadjust.cpp:24-47).
+Consts make_consts(const nsw6_params& p) {
+  Consts c;
+  std::memset(&c, 0, sizeof(c));
+  const double rho_s = 100.0, rho_g = 400.0;
+  const double Br = 3.0, Bs = 2.0, Bg = 3.0, Dr = 0.50, Ds = 0.25, Dg = 0.50;
+  (void)rho_s;
+  c.N0r = 8.E+6;
+  c.N0s = 3.E+6;
+  c.N0g = 4.0E+8;
+  c.Ar = PI * DWATR / 6.0;
+  c.As = 0.069;
+  c.Ag = PI * rho_g / 6.0;
+  c.Esi = 0.25;
+  c.Egs = 0.0;
+  c.gamma_sacr = 6.0E-2;
+  c.gamma_gacs = 90.E-3;
+  c.mi = 4.19E-13;
+  c.beta_saut = p.beta_saut;
+  c.gamma_saut = 6.0E-2;
+  c.qicrt_saut = p.qicrt_saut;
+  c.A_frz = 0.66;
+  c.B_frz = 100.0;
+  c.mi40 = 2.46E-10;
+  c.mi50 = 4.80E-10;
+  c.Ri50 = 5.E-5;
+  c.Nc_ihtr = 300.0;
+  c.Di_max = 500.E-6;
+  c.Di_a = 11.9;
+  c.Cr = p.Cr;
+  c.Cs = p.Cs;
+  c.Cg = p.Cg;
+  c.GAM_1br = gammafunc(1.0 + Br);
+  c.GAM_2br = gammafunc(2.0 + Br);
+  c.GAM_3br = gammafunc(3.0 + Br);
+  c.GAM_3dr = gammafunc(3.0 + Dr);
+  c.GAM_6dr = gammafunc(6.0 + Dr);
+  c.GAM_1brdr = gammafunc(1.0 + Br + Dr);
+  c.GAM_5dr_h = gammafunc(0.5 * (5.0 + Dr));
+  c.GAM_1bs = gammafunc(1.0 + Bs);
+  c.GAM_2bs = gammafunc(2.0 + Bs);
+  c.GAM_3bs = gammafunc(3.0 + Bs);
+  c.GAM_3ds = gammafunc(3.0 + Ds);
+  c.GAM_1bsds = gammafunc(1.0 + Bs + Ds);
+  c.GAM_5ds_h = gammafunc(0.5 * (5.0 + Ds));
+  c.GAM_1bg = gammafunc(1.0 + Bg);
+  c.GAM_3dg = gammafunc(3.0 + Dg);
+  c.GAM_1bgdg = gammafunc(1.0 + Bg + Dg);
+  c.GAM_5dg_h = gammafunc(0.5 * (5.0 + Dg));
+  c.ln10 = std::log(10.0);
+  static const double ca[10] = {5.065339, -0.062659, -3.032362, 0.029469, -0.000285,
+                                0.31255, 0.000204, 0.003199, 0.0, -0.015952};
+  static const double cb[10] = {0.476221, -0.015896, 0.165977, 0.007468, -0.000141,
+                                0.060366, 0.000079, 0.000594, 0.0, -0.003577};
+  std::memcpy(c.coef_a, ca, sizeof(ca));
+  std::memcpy(c.coef_b, cb, sizeof(cb));
+  c.Nc_def = 50.0;
+  {
+    const double Dc = 0.146 - 5.964E-2 * std::log(c.Nc_def / 2000.0);
+    const double dgamma_a = 0.1444 / (Dc * Dc);
+    const double GAM_dgam = gammafunc(dgamma_a);
+    const double GAM_dgam23 = gammafunc(dgamma_a + 2.0 / 3.0);
+    c.coef_dgam = GAM_dgam23 / GAM_dgam * std::pow(dgamma_a, (-2.0 / 3.0));
+    c.coef_xf = 3.0 / 4.0 / PI / DWATR;
+    c.Dc_berry = Dc;
+  }
+  c.ice_nuc = p.ice_nuc;
+  c.kk_aut = p.kk_aut;
+  c.LovR_liq = LHV0 / RVAP;
+  c.LovR_ice = LHS0 / RVAP;
+  c.RTEM00 = 1.0 / TEM00;
+  c.dtemp_criteria = std::pow(10.0, (double)(-(15 + 1) / 2));
+  c.log_mi50 = std::log(c.mi50);
+  c.log_mi40 = std::log(c.mi40);
+  c.pow_Nc_m179 = std::pow(c.Nc_def, -1.79);
+  return c;
+}
+
+// GRD_Setup, mod_debug.cpp:92-187, plus GRD_gz_shift (mod_precip_transport.cpp:698-709).
+void make_grid(int K, const double* gz, const double* gzh, double* out /* [GF_COUNT][K] */) {
+  std::memset(out, 0, sizeof(double) * GF_COUNT * (size_t)K);
+  double* g_gz = out + GF_GZ * K;
+  double* g_gzh = out + GF_GZH * K;
+  double* dgz = out + GF_DGZ * K;
+  double* dgzh = out + GF_DGZH * K;
+  double* rdgz = out + GF_RDGZ * K;
+  double* rdgzh = out + GF_RDGZH * K;
+  double* af = out + GF_AFACT * K;
+  double* bf = out + GF_BFACT * K;
+  double* cf = out + GF_CFACT * K;
+  double* df = out + GF_DFACT * K;
+  double* gzs = out + GF_GZSHIFT * K;
+  const int kmin = 1, kmax = K - 2;
+  for (int k = 0; k < K; ++k) {
+    g_gz[k] = gz[k];
+    g_gzh[k] = gzh[k];
+  }
+  for (int k = kmin - 1; k <= kmax; ++k) dgz[k] = g_gzh[k + 1] - g_gzh[k];
+  dgz[kmax + 1] = dgz[kmax];
+  for (int k = kmin; k <= kmax + 1; ++k) dgzh[k] = g_gz[k] - g_gz[k - 1];
+  dgzh[kmin - 1] = dgzh[kmin];
+  for (int k = 0; k < K; ++k) {
+    rdgz[k] = 1.0 / dgz[k];
+    rdgzh[k] = 1.0 / dgzh[k];
+  }
+  for (int k = kmin; k <= kmax + 1; ++k) af[k] = (g_gzh[k] - g_gz[k - 1]) / (g_gz[k] - g_gz[k - 1]);
+  af[kmin - 1] = 1.0;
+  for (int k = 0; k < K; ++k) bf[k] = 1.0 - af[k];
+  for (int k = kmin; k <= kmax; ++k) cf[k] = (g_gz[k] - g_gzh[k]) / (g_gzh[k + 1] - g_gzh[k]);
+  cf[kmin - 1] = 1.0;
+  cf[kmax + 1] = 0.0;
+  for (int k = 0; k < K; ++k) df[k] = 1.0 - cf[k];
+  for (int k = kmin; k <= kmax + 1; ++k) gzs[k] = g_gz[k - 1];
+}
+
+// Elements per region of each mp_driver argument (reference order).
+size_t arg_region_elems(int a, int K, int G) {
+  switch (a) {
+    case A_rhogq:
+    case A_q:
+      return (size_t)NQ * K * G;
+    case A_precip:
+    case A_ISO1:
+    case A_ISO2:
+      return 2 * (size_t)G;
+    case A_precip_rhoe:
+    case A_precip_lh_heat:
+    case A_precip_rhophi:
+    case A_precip_rhokin:
+    case A_rctop:
+    case A_rwtop:
+    case A_tctop:
+    case A_ix:
+    case A_iy:
+    case A_iz:
+    case A_jx:
+    case A_jy:
+    case A_jz:
+      return (size_t)G;
+    default:
+      return (size_t)K * G;
+  }
+}
+
+// Arguments the step reads (copied to the device by host-memory calls) and
+// writes (copied back).
+bool arg_is_read(int a) {
+  switch (a) {
+    case A_rhog: case A_rhogvx: case A_rhogvy: case A_rhogvz: case A_rhogw: case A_rhoge: case A_rhogq:
+    case A_vx: case A_vy: case A_vz: case A_tem: case A_q: case A_gsgam2: case A_gsgam2h: case A_gam2:
+    case A_gam2h: case A_ix: case A_iy: case A_iz: case A_jx: case A_jy: case A_jz: case A_z:
+      return true;
+    default:
+      return false;
+  }
+}
+bool arg_is_written(int a) {
+  switch (a) {
+    case A_rhog: case A_rhogvx: case A_rhogvy: case A_rhogvz: case A_rhogw: case A_rhoge: case A_rhogq:
+    case A_rho: case A_tem: case A_pre: case A_q: case A_qd: case A_precip: case A_ISO1: case A_ISO2:
+    case A_precip_rhoe: case A_precip_lh_heat: case A_precip_rhophi: case A_precip_rhokin: case A_re_liquid:
+    case A_re_solid: case A_re_cld: case A_rctop: case A_rwtop: case A_tctop: case A_GDCLW: case A_GDCFRC:
+    case A_GPREC:
+      return true;
+    default:
+      return false;
+  }
+}
+
+int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem& P) {
+  if (!h || lall < 1 || lall > h->lall_max || !a) return NSW6_ERR_BAD_ARG;
+  if (!(dt > 0.0) || !std::isfinite(dt)) return NSW6_ERR_BAD_ARG;
+  for (int i = 0; i < A_COUNT; ++i) {
+    if (arg_is_read(i) || arg_is_written(i)) {
+      if (!a[i]) return NSW6_ERR_BAD_ARG;
+    }
+  }
+  std::memset(&P, 0, sizeof(P));
+  P.gall = h->gall;
+  P.kall = h->kall;
+  P.kmin = 1;
+  P.kmax = h->kall - 2;
+  P.lall = lall;
+  P.dt = dt;
+  P.dt2 = std::pow(dt, 2);
+  P.dt3 = std::pow(dt, 3);
+  P.itelim = h->itelim;
+  P.grid = h->d_grid;
+  P.rhog = a[A_rhog];
+  P.rhogvx = a[A_rhogvx];
+  P.rhogvy = a[A_rhogvy];
+  P.rhogvz = a[A_rhogvz];
+  P.rhogw = a[A_rhogw];
+  P.rhoge = a[A_rhoge];
+  P.rhogq = a[A_rhogq];
+  P.vx = a[A_vx];
+  P.vy = a[A_vy];
+  P.vz = a[A_vz];
+  P.rho = a[A_rho];
+  P.tem = a[A_tem];
+  P.pre = a[A_pre];
+  P.q = a[A_q];
+  P.qd = a[A_qd];
+  P.precip = a[A_precip];
+  P.iso1 = a[A_ISO1];
+  P.iso2 = a[A_ISO2];
+  P.precip_rhoe = a[A_precip_rhoe];
+  P.precip_lh_heat = a[A_precip_lh_heat];
+  P.precip_rhophi = a[A_precip_rhophi];
+  P.precip_rhokin = a[A_precip_rhokin];
+  P.re_liquid = a[A_re_liquid];
+  P.re_solid = a[A_re_solid];
+  P.re_cld = a[A_re_cld];
+  P.rctop = a[A_rctop];
+  P.rwtop = a[A_rwtop];
+  P.tctop = a[A_tctop];
+  P.gsgam2 = a[A_gsgam2];
+  P.gsgam2h = a[A_gsgam2h];
+  P.gam2 = a[A_gam2];
+  P.gam2h = a[A_gam2h];
+  P.ix = a[A_ix];
+  P.iy = a[A_iy];
+  P.iz = a[A_iz];
+  P.jx = a[A_jx];
+  P.jy = a[A_jy];
+  P.jz = a[A_jz];
+  P.z = a[A_z];
+  P.GDCLW = a[A_GDCLW];
+  P.GDCFRC = a[A_GDCFRC];
+  P.GPREC = a[A_GPREC];
+  P.zdis = h->d_zdis;
+  P.zmax = h->d_zmax;
+  P.zmin = h->d_zmin;
+  P.status = h->d_status;
+  return NSW6_OK;
+}
+
+// Adds the elapsed times of the recorded event triples to the sums.
+int fold_timing(nsw6_handle* h) {
+  if (h->ev_used == 0) return NSW6_OK;
+  if (cudaEventSynchronize(h->ev[h->ev_used - 1][2]) != cudaSuccess) return NSW6_ERR_CUDA;
+  for (int i = 0; i < h->ev_used; ++i) {
+    float a = 0.f, b = 0.f;
+    cudaEventElapsedTime(&a, h->ev[i][0], h->ev[i][1]);
+    cudaEventElapsedTime(&b, h->ev[i][1], h->ev[i][2]);
+    h->t_sum[0] += a;
+    h->t_sum[1] += b;
+  }
+  h->t_steps += h->ev_used;
+  h->ev_used = 0;
+  return NSW6_OK;
+}
+
+cudaEvent_t* next_events(nsw6_handle* h) {
+  if (!h->timing) return nullptr;
+  if (h->ev_used == nsw6_handle::kRing && fold_timing(h) != NSW6_OK) return nullptr;
+  cudaEvent_t* e = h->ev[h->ev_used];
+  if (!e[0]) {
+    for (int j = 0; j < 3; ++j)
+      if (cudaEventCreate(&e[j]) != cudaSuccess) return nullptr;
+  }
+  ++h->ev_used;
+  return e;
+}
+
+int finish(nsw6_handle* h, cudaError_t launch) {
+  if (launch != cudaSuccess) return NSW6_ERR_CUDA;
+  if (!h->sync_check) return NSW6_OK;
+  return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
+}
+
+int run(nsw6_handle* h, int lall, double* const* a, double dt) {
+  Problem P;
+  int rc = fill_problem(h, lall, a, dt, P);
+  if (rc != NSW6_OK) return rc;
+  return finish(h, launch_step(P, h->C, h->stream, next_events(h)));
+}
+
+}  // namespace
+
+extern "C" {
+
+void nsw6_default_params(nsw6_params* p) {
+  if (!p) return;
+  p->beta_saut = 5.0E-3;
+  p->qicrt_saut = 0.0;
+  p->Cr = 130.0;
+  p->Cs = 4.84;
+  p->Cg = std::sqrt((4.0 * 400.0 * GRAV) / (3.0 * DENS00 * 0.6));
+  p->ice_nuc = 4.92E-11;
+  p->kk_aut = 1350.0;
+}
+
+int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const double* gz, const double* gzh) {
+  if (!out || gall < 1 || kall < 5 || kall > MAX_KALL || lall_max < 1 || !gz || !gzh) return NSW6_ERR_BAD_ARG;
+  *out = nullptr;
+  nsw6_handle* h = new (std::nothrow) nsw6_handle();
+  if (!h) return NSW6_ERR_BAD_ARG;
+  h->gall = gall;
+  h->kall = kall;
+  h->lall_max = lall_max;
+  nsw6_default_params(&h->params);
+  h->C = make_consts(h->params);
+  double* hgrid = (double*)std::malloc(sizeof(double) * GF_COUNT * (size_t)kall);
+  make_grid(kall, gz, gzh, hgrid);
+  const size_t KG = (size_t)kall * gall;
+  const size_t nkey = (size_t)lall_max * 6 * kall;
+  bool ok = cudaMalloc(&h->d_grid, sizeof(double) * GF_COUNT * kall) == cudaSuccess &&
+            cudaMalloc(&h->d_zdis, sizeof(double) * 6 * KG * lall_max) == cudaSuccess &&
+            cudaMalloc(&h->d_zmax, sizeof(unsigned long long) * nkey) == cudaSuccess &&
+            cudaMalloc(&h->d_zmin, sizeof(unsigned long long) * nkey) == cudaSuccess &&
+            cudaMalloc(&h->d_status, sizeof(DevStatus)) == cudaSuccess &&
+            cudaMemcpy(h->d_grid, hgrid, sizeof(double) * GF_COUNT * kall, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemset(h->d_status, 0, sizeof(DevStatus)) == cudaSuccess;
+  std::free(hgrid);
+  if (!ok) {
+    nsw6_destroy(h);
+    return NSW6_ERR_CUDA;
+  }
+  *out = h;
+  return NSW6_OK;
+}
+
+int nsw6_destroy(nsw6_handle* h) {
+  if (!h) return NSW6_OK;
+  cudaFree(h->d_grid);
+  cudaFree(h->d_zdis);
+  cudaFree(h->d_zmax);
+  cudaFree(h->d_zmin);
+  cudaFree(h->d_status);
+  cudaFree(h->d_stage);
+  for (auto& tri : h->ev)
+    for (auto& e : tri)
+      if (e) cudaEventDestroy(e);
+  delete h;
+  return NSW6_OK;
+}
+
+int nsw6_set_params(nsw6_handle* h, const nsw6_params* p) {
+  if (!h || !p) return NSW6_ERR_BAD_ARG;
+  h->params = *p;
+  h->C = make_consts(h->params);
+  return NSW6_OK;
+}
+
+int nsw6_get_params(const nsw6_handle* h, nsw6_params* p) {
+  if (!h || !p) return NSW6_ERR_BAD_ARG;
+  *p = h->params;
+  return NSW6_OK;
+}
+
+int nsw6_set_stream(nsw6_handle* h, void* stream) {
+  if (!h) return NSW6_ERR_BAD_ARG;
+  h->stream = (cudaStream_t)stream;
+  return NSW6_OK;
+}
+
+int nsw6_set_sync_check(nsw6_handle* h, int sync_check) {
+  if (!h) return NSW6_ERR_BAD_ARG;
+  h->sync_check = sync_check;
+  return NSW6_OK;
+}
+
+int nsw6_set_itelim(nsw6_handle* h, int itelim) {
+  if (!h || itelim < 1) return NSW6_ERR_BAD_ARG;
+  h->itelim = itelim;
+  return NSW6_OK;
+}
+
+int nsw6_set_timing(nsw6_handle* h, int on) {
+  if (!h) return NSW6_ERR_BAD_ARG;
+  h->timing = on;
+  return NSW6_OK;
+}
+
+int nsw6_read_timing(nsw6_handle* h, double* t, int n, int* steps) {
+  if (!h || !t || n < 2) return NSW6_ERR_BAD_ARG;
+  const int rc = fold_timing(h);
+  if (rc != NSW6_OK) return rc;
+  t[0] = h->t_sum[0];
+  t[1] = h->t_sum[1];
+  if (steps) *steps = h->t_steps;
+  h->t_sum[0] = h->t_sum[1] = 0.0;
+  h->t_steps = 0;
+  return NSW6_OK;
+}
+
+int nsw6_last_error(nsw6_handle* h, int* k, int* g, int* l, int* iters) {
+  if (!h) return NSW6_ERR_BAD_ARG;
+  DevStatus st;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (cudaMemcpy(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (st.code != 0 && cudaMemset(h->d_status, 0, sizeof(DevStatus)) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (k) *k = st.k;
+  if (g) *g = st.g;
+  if (l) *l = st.l;
+  if (iters) *iters = st.iters;
+  return st.code;
+}
+
+const char* nsw6_strerror(int status) {
+  switch (status) {
+    case NSW6_OK: return "success";
+    case NSW6_ERR_BAD_ARG: return "bad argument";
+    case NSW6_ERR_CUDA: return "CUDA runtime error";
+    case NSW6_ERR_NOCONV: return "saturation adjustment did not converge";
+    case NSW6_ERR_NAN: return "saturation adjustment produced a non-finite temperature";
+    case NSW6_ERR_UNSUPPORTED: return "unsupported configuration";
+    default: return "unknown status";
+  }
+}
+
+int mp_driver(nsw6_handle* h, int l_region, double* rhog, double* rhogvx, double* rhogvy, double* rhogvz,
+              double* rhogw, double* rhoge, double* rhogq, const double* vx, const double* vy, const double* vz,
+              const double* w, const double* unccn, double* rho, double* tem, double* pre, double* q, double* qd,
+              double* precip, double* ISO1_precip, double* ISO2_precip, double* precip_rhoe,
+              double* precip_lh_heat, double* precip_rhophi, double* precip_rhokin, double* re_liquid,
+              double* re_solid, double* re_cld, double* rctop, double* rwtop, double* tctop,
+              const double* frhoge_af, const double* frhogqv_af, const double* frhoge_rad, const double* rhogqke,
+              const double* gsgam2, const double* gsgam2h, const double* gam2, const double* gam2h,
+              const double* ix, const double* iy, const double* iz, const double* jx, const double* jy,
+              const double* jz, const double* z, const double* zh, double dt, double ct, double* GDCLW,
+              double* GDCFRC, double* GPREC, const double* CBMFX) {
+  (void)l_region;
+  (void)ct;
+  double* a[A_COUNT] = {rhog, rhogvx, rhogvy, rhogvz, rhogw, rhoge, rhogq,
+                        (double*)vx, (double*)vy, (double*)vz, (double*)w, (double*)unccn,
+                        rho, tem, pre, q, qd, precip, ISO1_precip, ISO2_precip,
+                        precip_rhoe, precip_lh_heat, precip_rhophi, precip_rhokin,
+                        re_liquid, re_solid, re_cld, rctop, rwtop, tctop,
+                        (double*)frhoge_af, (double*)frhogqv_af, (double*)frhoge_rad, (double*)rhogqke,
+                        (double*)gsgam2, (double*)gsgam2h, (double*)gam2, (double*)gam2h,
+                        (double*)ix, (double*)iy, (double*)iz, (double*)jx, (double*)jy, (double*)jz,
+                        (double*)z, (double*)zh, GDCLW, GDCFRC, GPREC, (double*)CBMFX};
+  return run(h, 1, a, dt);
+}
+
+int mp_driver_batched(nsw6_handle* h, int lall, double* rhog, double* rhogvx, double* rhogvy, double* rhogvz,
+                      double* rhogw, double* rhoge, double* rhogq, const double* vx, const double* vy,
+                      const double* vz, const double* w, const double* unccn, double* rho, double* tem, double* pre,
+                      double* q, double* qd, double* precip, double* ISO1_precip, double* ISO2_precip,
+                      double* precip_rhoe, double* precip_lh_heat, double* precip_rhophi, double* precip_rhokin,
+                      double* re_liquid, double* re_solid, double* re_cld, double* rctop, double* rwtop,
+                      double* tctop, const double* frhoge_af, const double* frhogqv_af, const double* frhoge_rad,
+                      const double* rhogqke, const double* gsgam2, const double* gsgam2h, const double* gam2,
+                      const double* gam2h, const double* ix, const double* iy, const double* iz, const double* jx,
+                      const double* jy, const double* jz, const double* z, const double* zh, double dt, double ct,
+                      double* GDCLW, double* GDCFRC, double* GPREC, const double* CBMFX) {
+  (void)ct;
+  double* a[A_COUNT] = {rhog, rhogvx, rhogvy, rhogvz, rhogw, rhoge, rhogq,
+                        (double*)vx, (double*)vy, (double*)vz, (double*)w, (double*)unccn,
+                        rho, tem, pre, q, qd, precip, ISO1_precip, ISO2_precip,
+                        precip_rhoe, precip_lh_heat, precip_rhophi, precip_rhokin,
+                        re_liquid, re_solid, re_cld, rctop, rwtop, tctop,
+                        (double*)frhoge_af, (double*)frhogqv_af, (double*)frhoge_rad, (double*)rhogqke,
+                        (double*)gsgam2, (double*)gsgam2h, (double*)gam2, (double*)gam2h,
+                        (double*)ix, (double*)iy, (double*)iz, (double*)jx, (double*)jy, (double*)jz,
+                        (double*)z, (double*)zh, GDCLW, GDCFRC, GPREC, (double*)CBMFX};
+  return run(h, lall, a, dt);
+}
+
+int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int host) {
+  (void)ct;
+  if (!h || !args || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
+  if (!host) return run(h, lall, args, dt);
+
+  const int K = h->kall, G = h->gall;
+  size_t need = 0;
+  for (int i = 0; i < A_COUNT; ++i) need += arg_region_elems(i, K, G) * (size_t)h->lall_max;
+  if (!h->d_stage) {
+    if (cudaMalloc(&h->d_stage, sizeof(double) * need) != cudaSuccess) return NSW6_ERR_CUDA;
+    h->stage_count = need;
+  }
+  double* dev[A_COUNT];
+  size_t offs = 0;
+  for (int i = 0; i < A_COUNT; ++i) {
+    dev[i] = h->d_stage + offs;
+    offs += arg_region_elems(i, K, G) * (size_t)h->lall_max;
+  }
+  for (int i = 0; i < A_COUNT; ++i) {
+    if ((arg_is_read(i) || arg_is_written(i)) && !args[i]) return NSW6_ERR_BAD_ARG;
+    if (!arg_is_read(i)) continue;
+    const size_t bytes = sizeof(double) * arg_region_elems(i, K, G) * (size_t)lall;
+    if (cudaMemcpyAsync(dev[i], args[i], bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+  }
+  Problem P;
+  int rc = fill_problem(h, lall, dev, dt, P);
+  if (rc != NSW6_OK) return rc;
+  if (launch_step(P, h->C, h->stream, next_events(h)) != cudaSuccess) return NSW6_ERR_CUDA;
+  for (int i = 0; i < A_COUNT; ++i) {
+    if (!arg_is_written(i)) continue;
+    const size_t bytes = sizeof(double) * arg_region_elems(i, K, G) * (size_t)lall;
+    if (cudaMemcpyAsync(args[i], dev[i], bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+  }
+  return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
+}
+
+}  // extern "C"

@@ -1,0 +1,711 @@
+// GB300 (sm_103a) kernels of one NSW6 microphysics step, FP64.
+//
+// Two kernels per step (plus two memsets of the extrema buffers):
+//
+//  nsw6_cell_kernel    one CTA = CELL_TG columns x all interior levels of one
+//                      region.  Per cell: negative filter, saturation values,
+//                      Bergeron parameters, the NSW6 process rates, the
+//                      RHOGQ/RHOGE/TEM updates and the fall speeds.  Then, per
+//                      column, the sedimentation departure distances of
+//                      vadv1d_prep for QR/QS/QG on full and half levels and
+//                      their per-level extrema, reduced over the region with
+//                      exact order-preserving 64-bit atomics.
+//
+//  nsw6_column_kernel  one CTA = COL_TG columns x all levels, column state in
+//                      shared memory.  Departure cells, the 24 flux integrals of
+//                      vadv1d_getflux_new, the transport tendencies, surface
+//                      precipitation, the KIN2EIN energy correction, the final
+//                      thermodynamic state, the saturation adjustment (Newton
+//                      on T) and the closing negative filter.
+//
+// The only coupling between columns, the per-level max/min of the departure
+// distance over a region (mod_vadv1d.cpp:316-353), is what separates the two
+// kernels.
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "nsw6_cell.cuh"
+#include "nsw6_common.cuh"
+
+namespace nsw6 {
+
+constexpr int ERR_NOCONV = 3;
+constexpr int ERR_NAN = 4;
+
+__device__ __forceinline__ void record_error(DevStatus* st, int code, int k, int g, int l, int iters) {
+  if (atomicCAS(&st->code, 0, code) == 0) {
+    st->k = k;
+    st->g = g;
+    st->l = l;
+    st->iters = iters;
+  }
+}
+
+// ------------------------------------------------------------------ kernel 1
+__global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Consts C) {
+  extern __shared__ double sm[];
+  const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const int l = blockIdx.y;
+  const int g0 = blockIdx.x * CELL_TG;
+  const size_t KG = (size_t)K * G;
+  const size_t off = (size_t)l * KG;
+  const size_t offq = (size_t)l * NQ * KG;
+  double* vts = sm;                      // [3][K][CELL_TG] fall speeds of QR, QS, QG
+  double* grid = sm + 3 * K * CELL_TG;   // [GF_COUNT][K]
+
+  for (int c = threadIdx.x; c < 3 * K * CELL_TG; c += blockDim.x) vts[c] = 0.0;
+  for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) grid[c] = P.grid[c];
+  __syncthreads();
+
+  const int nlev = kmax - kmin + 1;
+  for (int c = threadIdx.x; c < nlev * CELL_TG; c += blockDim.x) {
+    const int k = kmin + c / CELL_TG;
+    const int gx = c % CELL_TG;
+    const int g = g0 + gx;
+    if (g >= G) continue;
+    const size_t i = off + (size_t)k * G + g;
+    const size_t iq = offq + (size_t)k * G + g;
+    CellIn in;
+    in.rhog = P.rhog[i];
+    in.tem = P.tem[i];
+    in.gsgam2 = P.gsgam2[i];
+    in.q0 = P.q[iq];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) in.rhogq[n] = P.rhogq[iq + (size_t)n * KG];
+    CellOut o;
+    nsw6_cell(C, P.dt, in, o);
+    P.rhog[i] = o.rhog;
+    P.rhoge[i] = o.rhoge;
+    P.tem[i] = o.tem;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) P.rhogq[iq + (size_t)n * KG] = o.rhogq[n];
+#pragma unroll
+    for (int n = 1; n < 6; ++n) P.q[iq + (size_t)n * KG] = o.q[n];
+    P.re_liquid[i] = o.rceff;
+    P.re_cld[i] = o.rceff_cld;
+    vts[(0 * K + k) * CELL_TG + gx] = o.Vt[0];  // QR
+    vts[(1 * K + k) * CELL_TG + gx] = o.Vt[2];  // QS
+    vts[(2 * K + k) * CELL_TG + gx] = o.Vt[3];  // QG
+    if (k == kmax) {
+      // The reference writes the cloud-top scalars from every level in parallel
+      // (mod_mp_nsw6.cpp:1579-1592); the sequential order, in which the top
+      // interior level is written last, is used.  TagUpdateCLD, :710-726.
+      const size_t ic = (size_t)l * G + g;
+      P.rctop[ic] = o.rctop;
+      P.tctop[ic] = o.tctop;
+      const double sw = (0.5 + copysign(0.5, o.tctop - TEM00));
+      P.rwtop[ic] = (sw)*o.rctop + (1.0 - sw) * UNDEF;
+    }
+  }
+  __syncthreads();
+
+  // Departure distances (vadv1d_prep) and their per-level region extrema.
+  // Row s = t + 3*half: t = QR, QS, QG; half = 0 full levels (mkmin = kmin,
+  // dz = dgz), 1 half levels (mkmin = kmin+1, dz = dgzh, wp = Vtermh).
+  const double* dgz = grid + GF_DGZ * K;
+  const double* dgzh = grid + GF_DGZH * K;
+  for (int c = threadIdx.x; c < 6 * K * CELL_TG; c += blockDim.x) {
+    const int s = c / (K * CELL_TG);
+    const int rem = c - s * K * CELL_TG;
+    const int k = rem / CELL_TG;
+    const int gx = rem % CELL_TG;
+    const int t = s % 3;
+    const int half = s / 3;
+    const int mkmin = half ? kmin + 1 : kmin;
+    if (k < mkmin || k > kmax) continue;  // uniform across the warp (CELL_TG == 32)
+    const int g = g0 + gx;
+    const bool valid = g < G;
+    const double* col = vts + t * K * CELL_TG + gx;
+    double z = 0.0;
+    if (valid) {
+      if (!half) {
+        auto wp = [&](int j) { return col[j * CELL_TG]; };
+        z = vadv_zdis(wp, dgz, k, mkmin, kmax, P.dt, P.dt2, P.dt3);
+      } else {
+        // Vtermh, mod_precip_transport.cpp:847-861
+        auto wp = [&](int j) {
+          return (j >= kmin + 1 && j <= kmax - 1) ? 0.5 * (col[j * CELL_TG] + col[(j - 1) * CELL_TG]) : 0.0;
+        };
+        z = vadv_zdis(wp, dgzh, k, mkmin, kmax, P.dt, P.dt2, P.dt3);
+      }
+      P.zdis[((size_t)l * 6 + s) * KG + (size_t)k * G + g] = z;
+    }
+    // NaN never wins the reference's comparisons, so it is left out
+    unsigned long long kmx = (valid && z == z) ? order_key(z) : 0ull;
+    unsigned long long kmn = (valid && z == z) ? order_key(z) : ~0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long a = __shfl_xor_sync(0xffffffffu, kmx, o);
+      const unsigned long long b = __shfl_xor_sync(0xffffffffu, kmn, o);
+      kmx = a > kmx ? a : kmx;
+      kmn = b < kmn ? b : kmn;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      const size_t e = ((size_t)l * 6 + s) * K + k;
+      if (kmx != 0ull) atomicMax(&P.zmax[e], kmx);
+      if (kmn != ~0ull) atomicMin(&P.zmin[e], kmn);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ kernel 2
+// Shared-memory field slots, each [K][COL_TG] doubles.
+enum ColSlot {
+  S_KINH, S_KINV, S_DRHOE, S_DRHOPHI, S_DKINH, S_DKINV, S_DRHOGU, S_DRHOGV, S_DRHOGW,
+  S_DQR, S_DQS, S_DQG, S_RHOF, S_F, S_RGS, S_BASE, S_VI, S_VJ, S_COUNT
+};
+
+struct ColumnShared {
+  double* f;         // [S_COUNT][K][COL_TG]
+  double* grid;      // [GF_COUNT][K]
+  double* colacc;    // [6][COL_TG]: precip0, precip1, lh_heat, rhoe, rhophi, rhokin
+  int* bmin;         // [6][K]
+  int* bmax;         // [6][K]
+  unsigned char* kc; // [K][COL_TG]
+};
+
+// Departure cell of vadv1d_prep for one cell (mod_vadv1d.cpp:355-389).  The
+// sign tests of the reference's copysign products are exact comparisons.
+__device__ __forceinline__ int departure_cell(const double* zh, int k, double zdis, int bmn, int bmx, int mkmin,
+                                              int mkmax) {
+  int kc;
+  if (bmn == k && bmx == k) {
+    kc = k;
+  } else {
+    kc = 0;
+    const double dep = zh[k] - zdis;
+    for (int k2 = bmn; k2 <= bmx; ++k2) {
+      const double s1 = copysign(1.0, dep - zh[k2]);
+      const double s2 = copysign(1.0, zh[k2 + 1] - dep);
+      const int tmp = (int)((double)k2 * s1 * s2);
+      kc = kc > tmp ? kc : tmp;
+    }
+  }
+  if (kc == 0) kc = mkmin;
+  if (kc == mkmax + 1) kc = mkmax;
+  return kc;
+}
+
+// Flux integral of vadv1d_getflux_new for one cell (mod_vadv1d.cpp:410-449),
+// including its small-value filter.  As in the reference's Kokkos lambda
+// (size_t level index), the (k-1)-k2 and k2-k factors are evaluated unsigned
+// and never negative, so the weight is +dz(k2) above the departure cell and
+// -dz(k2) below it.
+template <int TG>
+__device__ __forceinline__ double flux_integral(const double* rhof_col, const double* dz, int k, int kc,
+                                                double zdis0, int bmn, int bmx) {
+  double f = 0.0, zdis = zdis0;
+  if (!(bmn == k && bmx == k)) {
+    for (int k2 = bmn; k2 <= bmx; ++k2) {
+      const double f1 = (double)(k2 - (kc + 1));
+      const double f4 = (double)((kc - 1) - k2);
+      const double fact =
+          dz[k2] * 0.25 * ((copysign(1.0, f1) + 1.0) * 2.0 - 2.0 * (copysign(1.0, f4) + 1.0));
+      f = f + rhof_col[k2 * TG] * fact;
+      zdis = zdis0 - fact;
+    }
+  }
+  f = f + rhof_col[kc * TG] * zdis;
+  return f * (0.5 + copysign(0.5, fabs(f) - EPS));
+}
+
+template <int COL_TG>
+__global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
+  extern __shared__ double smraw[];
+  const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const int l = blockIdx.y;
+  const int g0 = blockIdx.x * COL_TG;
+  const size_t KG = (size_t)K * G;
+  const size_t off = (size_t)l * KG;
+  const size_t offq = (size_t)l * NQ * KG;
+  const int ncell = K * COL_TG;
+  const double dt = P.dt;
+
+  ColumnShared S;
+  S.f = smraw;
+  S.grid = S.f + (size_t)S_COUNT * ncell;
+  S.colacc = S.grid + GF_COUNT * K;
+  S.bmin = reinterpret_cast<int*>(S.colacc + 6 * COL_TG);
+  S.bmax = S.bmin + 6 * K;
+  S.kc = reinterpret_cast<unsigned char*>(S.bmax + 6 * K);
+  auto F = [&](int slot) { return S.f + (size_t)slot * ncell; };
+
+  for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) S.grid[c] = P.grid[c];
+  for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) S.colacc[c] = 0.0;
+  __syncthreads();
+  const double* gzh = S.grid + GF_GZH * K;
+  const double* gzs = S.grid + GF_GZSHIFT * K;
+  const double* dgz = S.grid + GF_DGZ * K;
+  const double* dgzh = S.grid + GF_DGZH * K;
+  const double* rdgz = S.grid + GF_RDGZ * K;
+  const double* rdgzh = S.grid + GF_RDGZH * K;
+  const double* afact = S.grid + GF_AFACT * K;
+  const double* bfact = S.grid + GF_BFACT * K;
+  const double* cfact = S.grid + GF_CFACT * K;
+  const double* dfact = S.grid + GF_DFACT * K;
+
+  // ---- kcell_min/max per level from the region extrema (mod_vadv1d.cpp:316-353)
+  for (int c = threadIdx.x; c < 6 * K; c += blockDim.x) {
+    const int s = c / K, k = c % K;
+    const int half = s / 3;
+    const int mkmin = half ? kmin + 1 : kmin;
+    const double* zh = half ? gzs : gzh;
+    int bmn = k, bmx = k;
+    if (k >= mkmin && k <= kmax) {
+      const size_t e = ((size_t)l * 6 + s) * K + k;
+      const unsigned long long kx = P.zmax[e], kn = P.zmin[e];
+      double zzmax = DBL_MIN, zzmin = DBL_MIN;
+      if (kx != 0ull) {
+        const double v = key_value(kx);
+        zzmax = v > zzmax ? v : zzmax;
+      }
+      if (kn != ~0ull) {
+        const double v = key_value(kn);
+        zzmin = v < zzmin ? v : zzmin;
+      }
+      if (zzmax > 0.0) {
+        for (int k2 = k; k2 >= mkmin; --k2)
+          if ((zh[k2] <= zh[k] - zzmax) && (zh[k2 + 1] > zh[k] - zzmax)) {
+            bmn = k2;
+            break;
+          }
+      }
+      if (zzmin < 0.0) {
+        for (int k2 = k; k2 <= kmax; ++k2)
+          if ((zh[k2] <= zh[k] - zzmin) && (zh[k2 + 1] > zh[k] - zzmin)) {
+            bmx = k2;
+            break;
+          }
+      }
+    }
+    S.bmin[c] = bmn;
+    S.bmax[c] = bmx;
+  }
+
+  // ---- metric factors, kinetic energy, zeroed accumulators
+  //      (mod_precip_transport.cpp:715-770, cnvvar_rhogkin_in mod_debug.cpp:269-330)
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+    const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    for (int s = S_KINH; s <= S_DQG; ++s) F(s)[c] = 0.0;
+    F(S_RGS)[c] = 0.0;
+    F(S_VI)[c] = 0.0;
+    F(S_VJ)[c] = 0.0;
+    if (g >= G) continue;
+    const size_t i = off + (size_t)k * G + g;
+    const size_t ic = (size_t)l * G + g;
+    const bool interior = (k >= kmin && k <= kmax);
+    if (interior) F(S_RGS)[c] = P.gam2[i] / P.gsgam2[i];
+    const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
+    F(S_VI)[c] = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
+    F(S_VJ)[c] = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
+    if (interior) {
+      const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
+      F(S_KINH)[c] = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / P.rhog[i];
+    }
+    if (k >= kmin + 1 && k <= kmax) {
+      const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
+      const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
+      const double rw = P.rhogw[i];
+      F(S_KINV)[c] = 0.5 * (rw * rw) / (c2w0 * P.rhog[i] + c2w1 * P.rhog[i - G]);
+    }
+  }
+  __syncthreads();
+
+  // ---- sedimentation of QR, QS, QG (mod_precip_transport.cpp:767-955)
+  const int tracer[3] = {I_QR, I_QS, I_QG};
+  for (int t = 0; t < 3; ++t) {
+    const int nq = tracer[t];
+    const double* zdis0 = P.zdis + ((size_t)l * 6 + t) * KG;
+    const double* zdis0h = P.zdis + ((size_t)l * 6 + 3 + t) * KG;
+    const int* bmn_f = S.bmin + t * K;
+    const int* bmx_f = S.bmax + t * K;
+    const int* bmn_h = S.bmin + (3 + t) * K;
+    const int* bmx_h = S.bmax + (3 + t) * K;
+    const double* rhogq_n = P.rhogq + offq + (size_t)nq * KG;
+    const double* q_n = P.q + offq + (size_t)nq * KG;
+
+    // departure cells (full levels) and rhoq = rhogq * rgs
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+      const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+      if (g >= G) continue;
+      const size_t i = (size_t)k * G + g;
+      F(S_BASE)[c] = rhogq_n[i] * F(S_RGS)[c];
+      if (k >= kmin && k <= kmax) S.kc[c] = (unsigned char)departure_cell(gzh, k, zdis0[off + i], bmn_f[k], bmx_f[k], kmin, kmax);
+    }
+    __syncthreads();
+
+    for (int f = 0; f < 6; ++f) {
+      // flux source: q, e, phi, kin_h, u, v (mod_precip_transport.cpp:776-808)
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+        double r = 0.0;
+        if (g < G) {
+          const size_t i = off + (size_t)k * G + g;
+          const double b = F(S_BASE)[c];
+          switch (f) {
+            case 0: r = b; break;
+            case 1: r = b * CVDRY * P.tem[i]; break;
+            case 2: r = b * GRAV * P.z[i]; break;
+            case 3: r = q_n[i - off] * F(S_RGS)[c] * F(S_KINH)[c]; break;
+            case 4: r = b * F(S_VI)[c]; break;
+            default: r = b * F(S_VJ)[c]; break;
+          }
+        }
+        F(S_RHOF)[c] = r;
+      }
+      __syncthreads();
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+        double fl = 0.0;
+        if (g < G && k >= kmin && k <= kmax)
+          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[off + (size_t)k * G + g], bmn_f[k], bmx_f[k]);
+        F(S_F)[c] = fl;
+      }
+      __syncthreads();
+      // flux divergence and surface fluxes (mod_precip_transport.cpp:782-842, 900-954)
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+        if (g >= G || k < kmin || k > kmax) continue;
+        const double fk = F(S_F)[c], fk1 = F(S_F)[c + COL_TG];
+        const double d = (fk1 - fk) * rdgz[k];
+        switch (f) {
+          case 0:
+            F(S_DQR + t)[c] = -d;
+            if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + (-fk / dt);
+            break;
+          case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - d; break;
+          case 2: F(S_DRHOPHI)[c] = F(S_DRHOPHI)[c] - d; break;
+          case 3: F(S_DKINH)[c] = F(S_DKINH)[c] - d; break;
+          case 4: F(S_DRHOGU)[c] = F(S_DRHOGU)[c] - d; break;
+          default: F(S_DRHOGV)[c] = F(S_DRHOGV)[c] - d; break;
+        }
+        if (k == kmin) {
+          double* acc = S.colacc;
+          switch (f) {
+            case 0:
+              if (nq == I_QR) {
+                acc[0 * COL_TG + gx] = acc[0 * COL_TG + gx] - fk / dt;
+              } else {
+                acc[1 * COL_TG + gx] = acc[1 * COL_TG + gx] - fk / dt;
+                acc[2 * COL_TG + gx] = acc[2 * COL_TG + gx] + fk * LHF0 / dt;
+              }
+              break;
+            case 1: acc[3 * COL_TG + gx] = acc[3 * COL_TG + gx] - fk / dt; break;
+            case 2: acc[4 * COL_TG + gx] = acc[4 * COL_TG + gx] - fk / dt; break;
+            case 3: acc[5 * COL_TG + gx] = acc[5 * COL_TG + gx] - fk / dt; break;
+            default: break;
+          }
+        }
+      }
+      __syncthreads();
+    }
+
+    // half levels: departure cells and qh (mod_precip_transport.cpp:845-882)
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+      const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+      double qh = 0.0;
+      if (g < G && k >= kmin + 1 && k <= kmax) {
+        const size_t i = off + (size_t)k * G + g;
+        qh = 0.5 * (q_n[i - off] + q_n[i - off - G]) * (P.gam2h[i] / P.gsgam2h[i]);
+        S.kc[c] = (unsigned char)departure_cell(gzs, k, zdis0h[i], bmn_h[k], bmx_h[k], kmin + 1, kmax);
+      }
+      F(S_BASE)[c] = qh;
+      F(S_RHOF)[c] = qh * F(S_KINV)[c];
+    }
+    __syncthreads();
+    for (int w = 0; w < 2; ++w) {
+      // vertical kinetic energy (w = 0) and momentum w (w = 1); the reference
+      // passes the full-level kcell_max as the upper bound (:890, :892)
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+        double fl = 0.0;
+        if (g < G && k >= kmin + 1 && k <= kmax)
+          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgzh, k, S.kc[c], zdis0h[off + (size_t)k * G + g], bmn_h[k], bmx_f[k]);
+        F(S_F)[c] = fl;
+      }
+      __syncthreads();
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+        if (g < G && k >= kmin + 1 && k <= kmax) {
+          const double d = (F(S_F)[c] - F(S_F)[c - COL_TG]) * rdgzh[k];
+          if (w == 0) F(S_DKINV)[c] = F(S_DKINV)[c] - d;
+          else F(S_DRHOGW)[c] = F(S_DRHOGW)[c] - d;
+        }
+        if (w == 0) {
+          double r = 0.0;
+          if (g < G && k >= kmin + 1 && k <= kmax) r = F(S_BASE)[c] * P.rhogw[off + (size_t)k * G + g];
+          F(S_RHOF)[c] = r;
+        }
+      }
+      __syncthreads();
+    }
+  }
+
+  // ---- apply the tendencies (mod_precip_transport.cpp:956-989)
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+    const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    if (g >= G) continue;
+    const size_t i = off + (size_t)k * G + g;
+    const size_t ic = (size_t)l * G + g;
+    const size_t iq = offq + (size_t)k * G + g;
+    const double dqr = F(S_DQR)[c], dqs = F(S_DQS)[c], dqg = F(S_DQG)[c];
+    double rhoge = P.rhoge[i] + F(S_DRHOE)[c] + F(S_DRHOPHI)[c];
+    F(S_KINH)[c] = F(S_KINH)[c] + F(S_DKINH)[c];
+    F(S_KINV)[c] = F(S_KINV)[c] + F(S_DKINV)[c];
+    const double du = F(S_DRHOGU)[c], dv = F(S_DRHOGV)[c];
+    P.rhogvx[i] = P.rhogvx[i] + du * P.ix[ic] + dv * P.jx[ic];
+    P.rhogvy[i] = P.rhogvy[i] + du * P.iy[ic] + dv * P.jy[ic];
+    P.rhogvz[i] = P.rhogvz[i] + du * P.iz[ic] + dv * P.jz[ic];
+    const double rw = P.rhogw[i] + F(S_DRHOGW)[c];
+    P.rhogw[i] = rw;
+    F(S_DRHOGW)[c] = rw;
+    // tracers in order QV..QG; QV, QC and QI add exact zeros
+    double rhog = P.rhog[i];
+    const double zz = P.z[i];
+    P.rhogq[iq + (size_t)I_QV * KG] = P.rhogq[iq + (size_t)I_QV * KG] + 0.0;
+    P.rhogq[iq + (size_t)I_QC * KG] = P.rhogq[iq + (size_t)I_QC * KG] + 0.0;
+    P.rhogq[iq + (size_t)I_QR * KG] = P.rhogq[iq + (size_t)I_QR * KG] + dqr;
+    rhog = rhog + dqr;
+    rhoge = rhoge - dqr * GRAV * zz;
+    P.rhogq[iq + (size_t)I_QI * KG] = P.rhogq[iq + (size_t)I_QI * KG] + 0.0;
+    P.rhogq[iq + (size_t)I_QS * KG] = P.rhogq[iq + (size_t)I_QS * KG] + dqs;
+    rhog = rhog + dqs;
+    rhoge = rhoge - dqs * GRAV * zz;
+    P.rhogq[iq + (size_t)I_QG * KG] = P.rhogq[iq + (size_t)I_QG * KG] + dqg;
+    rhog = rhog + dqg;
+    rhoge = rhoge - dqg * GRAV * zz;
+    P.rhog[i] = rhog;
+    P.rhoge[i] = rhoge;
+    F(S_RHOF)[c] = rhog;
+  }
+  __syncthreads();
+
+  // ---- KIN2EIN (mod_precip_transport.cpp:991-1011): tmp2 and the vertical
+  //      kinetic energy of the updated state
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+    const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    F(S_DRHOE)[c] = 0.0;
+    F(S_DRHOPHI)[c] = 0.0;
+    if (g >= G) continue;
+    const size_t i = off + (size_t)k * G + g;
+    if (k >= kmin && k <= kmax) {
+      const double w2c0 = cfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
+      const double w2c1 = dfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
+      F(S_DRHOE)[c] = F(S_KINH)[c] + (w2c0 * F(S_KINV)[c + COL_TG] + w2c1 * F(S_KINV)[c]);
+    }
+    if (k >= kmin + 1 && k <= kmax) {
+      const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
+      const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
+      const double rw = F(S_DRHOGW)[c];
+      F(S_DRHOPHI)[c] = 0.5 * (rw * rw) / (c2w0 * F(S_RHOF)[c] + c2w1 * F(S_RHOF)[c - COL_TG]);
+    }
+  }
+  __syncthreads();
+
+  // ---- per cell: KIN2EIN, final thermodynamics, saturation adjustment,
+  //      negative filter, outputs
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+    const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    if (g >= G) continue;
+    const size_t i = off + (size_t)k * G + g;
+    const size_t iq = offq + (size_t)k * G + g;
+    const bool interior = (k >= kmin && k <= kmax);
+    const double rhog = F(S_RHOF)[c];
+    double rhoge = P.rhoge[i];
+    if (interior) {
+      const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
+      const double tmp_h = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / rhog;
+      const double w2c0 = cfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
+      const double w2c1 = dfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
+      const double tmp = tmp_h + (w2c0 * F(S_DRHOPHI)[c + COL_TG] + w2c1 * F(S_DRHOPHI)[c]);
+      rhoge = rhoge + (F(S_DRHOE)[c] - tmp);
+    }
+    double rq[6], q[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) rq[n] = P.rhogq[iq + (size_t)n * KG];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) q[n] = rq[n] / rhog;
+    const double gsg = P.gsgam2[i];
+    double rho = rhog / gsg;
+    const double ein = rhoge / rhog;
+    double qd = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qd = qd - q[n];
+    // THRMDYN_tempre, mod_thrmdyn.cpp:137-180
+    double cvt = 0.0, qdl = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) {
+      cvt = cvt + q[n] * CVDRY;
+      qdl = qdl - q[n];
+    }
+    cvt = cvt + qdl * CVDRY;
+    double tem = ein / cvt;
+    double pre = rho * tem * (qdl * RDRY + q[I_QV] * RVAP);
+
+    // SATURATION_adjustment, ice_adjust = false (mod_satadjust.cpp:274-362)
+    const double ein_moist = rhoge / rhog + q[I_QV] * LHV0;
+    const double qsum = q[I_QV] + q[I_QC];
+    q[I_QV] = qsum;
+    q[I_QC] = 0.0;
+    double cvtot = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+    const double rho_l = rhog / gsg;
+    tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
+    if (interior) {
+      // satadjust_liq, mod_satadjust.cpp:771-896
+      double qd_l = 1.0;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
+      double rtem = 1.0 / (dmax(tem, TEM_MIN));
+      double psat = PSAT0 * exp(C.LovR_liq * (C.RTEM00 - rtem));
+      double qsat = psat / (rho_l * RVAP * tem);
+      if (qsum - qsat > EPS) {
+        bool converged = false;
+        int ite;
+        for (ite = 0; ite < P.itelim; ++ite) {
+          rtem = 1.0 / (dmax(tem, TEM_MIN));
+          psat = PSAT0 * exp(C.LovR_liq * (C.RTEM00 - rtem));
+          qsat = psat / (rho_l * RVAP * tem);
+          q[I_QV] = qsat;
+          q[I_QC] = qsum - qsat;
+          double cv = qd_l * CVDRY;
+#pragma unroll
+          for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
+          const double emoist_new = tem * cv + q[I_QV] * LHV0;
+          // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
+          // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
+          const double dqsat_dT = (C.LovR_liq / (tem * tem)) * qsat;
+          const double demoist_dT = cv + dqsat_dT * LHV0;
+          const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+          tem = tem - dtemp;
+          if (fabs(dtemp) < C.dtemp_criteria) {
+            converged = true;
+            break;
+          }
+          if (tem * 0.0 != 0.0) break;
+        }
+        if (!converged) record_error(P.status, (tem * 0.0 != 0.0) ? ERR_NAN : ERR_NOCONV, k, g, l, ite);
+      }
+    }
+    rq[I_QV] = rhog * q[I_QV];
+    rq[I_QC] = rhog * q[I_QC];
+    cvtot = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+    rhoge = rhog * tem * cvtot;
+
+    // negative_filter (mod_mp_nsw6.cpp:1770-1831), interior levels
+    double rhog_o = rhog;
+    if (interior) {
+      double diffq = 0.0;
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) {
+        diffq += rq[n];
+        rq[n] = dmax(rq[n], 0.0);
+      }
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) diffq -= rq[n];
+      rq[I_QV] += diffq;
+      diffq = rq[I_QV];
+      rq[I_QV] = dmax(rq[I_QV], 0.0);
+      diffq -= rq[I_QV];
+      rhog_o = rhog * (1.0 - diffq);
+      rho = rhog_o / gsg;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) q[n] = rq[n] / rhog_o;
+      double qdf = 1.0;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
+      double cva = qdf * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
+      rhoge = tem * rhog_o * cva;
+      pre = rho * (qdf * RDRY + q[I_QV] * RVAP) * tem;
+    }
+
+    P.rhog[i] = rhog_o;
+    P.rhoge[i] = rhoge;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      P.rhogq[iq + (size_t)n * KG] = rq[n];
+      P.q[iq + (size_t)n * KG] = q[n];
+    }
+    P.rho[i] = rho;
+    P.tem[i] = tem;
+    P.pre[i] = pre;
+    P.qd[i] = qd;
+    // mp_driver epilogue (mod_mp_driver.cpp:555-612, MP_DIV_NUM = 1)
+    P.re_solid[i] = 20.0E-6;
+    P.GDCLW[i] = 0.0;
+    P.GDCFRC[i] = 0.0;
+    if (!interior) {
+      P.GPREC[i] = 0.0;
+      P.re_liquid[i] = 0.0;
+      P.re_cld[i] = 0.0;
+    }
+    if (k == kmin) {
+      const size_t ic = (size_t)l * G + g;
+      const size_t r0 = (size_t)l * G + g, r1 = ((size_t)P.lall + l) * G + g;
+      const double* acc = S.colacc;
+      P.precip[r0] = 0.0 + acc[0 * COL_TG + gx];
+      P.precip[r1] = 0.0 + acc[1 * COL_TG + gx];
+      P.iso1[r0] = 0.0;
+      P.iso1[r1] = 0.0;
+      P.iso2[r0] = 0.0;
+      P.iso2[r1] = 0.0;
+      P.precip_lh_heat[ic] = 0.0 + acc[2 * COL_TG + gx];
+      P.precip_rhoe[ic] = 0.0 + acc[3 * COL_TG + gx];
+      P.precip_rhophi[ic] = 0.0 + acc[4 * COL_TG + gx];
+      P.precip_rhokin[ic] = 0.0 + acc[5 * COL_TG + gx];
+    }
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+size_t cell_smem_bytes(int K) { return sizeof(double) * (size_t)(3 * K * CELL_TG + GF_COUNT * K); }
+
+int column_tile(int K) { return K <= 64 ? 16 : 8; }
+
+size_t column_smem_bytes(int K) {
+  const int TG = column_tile(K);
+  return sizeof(double) * ((size_t)S_COUNT * K * TG + GF_COUNT * K + 6 * TG) + sizeof(int) * 12 * K +
+         (size_t)K * TG + 16;
+}
+
+int column_threads(int K) {
+  const int ncell = K * column_tile(K);
+  const int passes = (ncell + 255) / 256;
+  int per = (ncell + passes - 1) / passes;
+  per = (per + 31) / 32 * 32;
+  return per > 256 ? 256 : per;
+}
+
+cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev) {
+  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  cudaError_t e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  const size_t s1 = cell_smem_bytes(P.kall);
+  const size_t s2 = column_smem_bytes(P.kall);
+  static bool attr_done = false;
+  if (!attr_done) {
+    cudaFuncSetAttribute(nsw6_cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    attr_done = true;
+  }
+  dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
+  if (ev) cudaEventRecord(ev[0], stream);
+  nsw6_cell_kernel<<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  if (ev) cudaEventRecord(ev[1], stream);
+  const int tg = column_tile(P.kall);
+  dim3 g2((P.gall + tg - 1) / tg, P.lall);
+  if (tg == 16) nsw6_column_kernel<16><<<g2, column_threads(P.kall), s2, stream>>>(P, C);
+  else nsw6_column_kernel<8><<<g2, column_threads(P.kall), s2, stream>>>(P, C);
+  if (ev) cudaEventRecord(ev[2], stream);
+  return cudaGetLastError();
+}
+
+}  // namespace nsw6

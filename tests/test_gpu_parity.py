@@ -1,0 +1,188 @@
+"""GPU parity tests: the sm_103a NSW6 step against the oracle.
+
+Pass criterion for every output field and every cell: |gpu - oracle| <=
+1e-20 + 1e-11 * |oracle| (relative 1e-11, absolute floor 1e-20 for near-zero
+mixing ratios).  Each test also prints the reference's own statistic (signed
+max/min/sum of the difference, mod_debug.cpp:363-410).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_files
+from nicam_kokkos_microphysics_gb300.state import (ARG_NAMES, MP_DRIVER_ARGS, OUTPUT_NAMES, StateSpec, make_state,
+                                                   region_shape, region_view)
+from oracle import restatement
+from _parity import compare, summary
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def run_gpu(reg: dict, gz, gzh, dt: float, params: dict | None = None, itelim: int | None = None) -> dict:
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    kall, gall = reg["rhog"].shape
+    drv = mp_init("NSW6", gall, kall, gz, gzh, params=params)
+    if itelim is not None:
+        drv.set_itelim(itelim)
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in reg.items()}
+    drv.mp_driver(0, *[t[n] for n in ARG_NAMES], dt=dt, ct=0.0)
+    torch.cuda.synchronize()
+    out = {k: v.cpu().numpy() for k, v in t.items()}
+    drv.close()
+    return out
+
+
+def run_oracle(reg: dict, gz, gzh, dt: float, params: dict | None = None) -> dict:
+    want = {k: v.copy() for k, v in reg.items()}
+    rc, st = restatement.mp_driver(want, gz, gzh, dt, params=params)
+    assert rc == 0, st
+    return want
+
+
+def assert_parity(got: dict, want: dict, label: str):
+    stats = compare(got, want, OUTPUT_NAMES)
+    print(f"\n[{label}]\n" + summary(stats))
+    bad = {n: s for n, s in stats.items() if s["n_bad"]}
+    assert not bad, f"{label}: fields outside 1e-11 relative: {sorted(bad)}\n" + summary(stats)
+
+
+def load_golden(path):
+    z = np.load(path)
+    kall, gall = z["in_rhog"].shape
+    reg = {}
+    for name, kind, _ in MP_DRIVER_ARGS:
+        key = f"in_{name}"
+        reg[name] = z[key].copy() if key in z else np.full(region_shape(kind, kall, gall), np.nan)
+    out = {n: z[f"out_{n}"] for n in OUTPUT_NAMES}
+    return reg, out, z["gz"], z["gzh"], float(z["dt"])
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: p.stem)
+def test_gpu_matches_reference_golden(path):
+    reg, out, gz, gzh, dt = load_golden(path)
+    got = run_gpu(reg, gz, gzh, dt)
+    assert_parity(got, out, path.stem)
+    for n in OUTPUT_NAMES:
+        assert np.isfinite(got[n]).all(), f"{n} not fully written"
+
+
+@pytest.mark.parametrize("variant,seed", [("standard", 1001), ("convective", 1002), ("cold", 1003)])
+def test_gpu_matches_oracle_full_region(variant, seed):
+    """One full benchmark region: gall = 16900 (130 x 130), kall = 42."""
+    spec = StateSpec(gall=16900, kall=42, lall=1, seed=seed, variant=variant)
+    st = make_state(spec, out_fill=np.nan)
+    reg = region_view(st, 0)
+    want = run_oracle(reg, st["_gz"], st["_gzh"], spec.dt)
+    got = run_gpu(reg, st["_gz"], st["_gzh"], spec.dt)
+    assert_parity(got, want, f"{variant} 16900x42")
+
+
+@pytest.mark.parametrize("gall,kall", [(1, 42), (17, 42), (33, 12), (31, 5), (250, 7), (64, 96)])
+def test_gpu_ragged_and_small_shapes(gall, kall):
+    spec = StateSpec(gall=gall, kall=kall, lall=1, seed=gall * 1000 + kall, variant="convective")
+    st = make_state(spec, out_fill=np.nan)
+    reg = region_view(st, 0)
+    want = run_oracle(reg, st["_gz"], st["_gzh"], spec.dt)
+    got = run_gpu(reg, st["_gz"], st["_gzh"], spec.dt)
+    assert_parity(got, want, f"{gall}x{kall}")
+
+
+def test_gpu_changed_parameters():
+    p = {"beta_saut": 7.5e-3, "qicrt_saut": 1.0e-6, "Cr": 120.0, "Cs": 5.1, "Cg": 70.0, "ice_nuc": 6.0e-11,
+         "kk_aut": 1500.0}
+    spec = StateSpec(gall=500, kall=42, lall=1, seed=77, variant="cold")
+    st = make_state(spec, out_fill=np.nan)
+    reg = region_view(st, 0)
+    want = run_oracle(reg, st["_gz"], st["_gzh"], spec.dt, params=p)
+    got = run_gpu(reg, st["_gz"], st["_gzh"], spec.dt, params=p)
+    assert_parity(got, want, "changed parameters")
+
+
+def test_gpu_batched_equals_per_region():
+    """All regions in one call equal one call per region, bit for bit; the
+    region-wide reductions stay per region."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=700, kall=42, lall=3, seed=31, variant="convective")
+    st = make_state(spec, out_fill=np.nan)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    tb = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    drv.mp_driver_batched(spec.lall, *[tb[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    torch.cuda.synchronize()
+    for l in range(spec.lall):
+        reg = region_view(st, l)
+        tr = {n: torch.from_numpy(reg[n]).cuda() for n in ARG_NAMES}
+        drv.mp_driver(l, *[tr[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        torch.cuda.synchronize()
+        for name, kind, intent in MP_DRIVER_ARGS:
+            if intent == "in":
+                continue
+            b = tb[name].cpu().numpy()
+            b = b[:, l] if kind == "2g" else b[l]
+            r = tr[name].cpu().numpy()
+            assert np.array_equal(b.view(np.int64), r.view(np.int64)), (name, l)
+    drv.close()
+
+
+def test_gpu_host_entry_equals_device_entry():
+    """The host-memory entry point (copies inside the call) gives the device result."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=300, kall=42, lall=2, seed=5, variant="standard")
+    st = make_state(spec, out_fill=np.nan)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=2)
+    host = {n: st[n].copy() for n in ARG_NAMES}
+    drv.run(host, dt=spec.dt)
+    dev = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    drv.run(dev, dt=spec.dt)
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        assert np.array_equal(host[n].view(np.int64), dev[n].cpu().numpy().view(np.int64)), n
+    drv.close()
+
+
+def test_gpu_deterministic():
+    reg, out, gz, gzh, dt = load_golden(golden_files()[1])
+    a = run_gpu(reg, gz, gzh, dt)
+    b = run_gpu(reg, gz, gzh, dt)
+    for n in OUTPUT_NAMES:
+        assert np.array_equal(a[n].view(np.int64), b[n].view(np.int64)), n
+
+
+def test_gpu_nonconvergence_is_reported_not_trapped():
+    """An iteration limit of 1 leaves saturated cells unconverged: the call
+    returns NSW6_ERR_NOCONV with the failing cell, and the device stays usable."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import NSW6Error
+    reg, out, gz, gzh, dt = load_golden(golden_files()[0])
+    with pytest.raises(NSW6Error) as ei:
+        run_gpu(reg, gz, gzh, dt, itelim=1)
+    assert ei.value.code == 3
+    got = run_gpu(reg, gz, gzh, dt)
+    assert_parity(got, out, "after error")
+    torch.cuda.synchronize()
+
+
+def test_gpu_rejects_bad_arguments():
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=32, kall=12, lall=1, seed=1)
+    st = make_state(spec, out_fill=0.0)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"])
+    t = {n: torch.from_numpy(v).cuda() for n, v in region_view(st, 0).items()}
+    args = [t[n] for n in ARG_NAMES]
+    with pytest.raises(ValueError):
+        drv.mp_driver(0, *args[:-1], torch.zeros(3, device="cuda", dtype=torch.float64), dt=60.0, ct=0.0)
+    with pytest.raises(ValueError):
+        mp_init("NDW6", 32, 12, st["_gz"], st["_gzh"])
+    assert drv.run_argv(2, [a.data_ptr() for a in args], 60.0) == 1  # lall above lall_max
+    drv.close()
