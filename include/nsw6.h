@@ -82,6 +82,16 @@ int nsw6_set_sync_check(nsw6_handle* h, int sync_check);
  * mod_satadjust.cpp:809). */
 int nsw6_set_itelim(nsw6_handle* h, int itelim);
 
+/* Transcendental functions of the step: 0 (default) table-driven FP64
+ * exp/log/pow written for this library (about one unit in the last place),
+ * 1 the CUDA math library.  Both agree with the reference to the stated
+ * tolerance; mode 1 exists to separate their effects in checks. */
+int nsw6_set_math(nsw6_handle* h, int mode);
+
+/* Evaluates the step's table-driven exp (fn 0), log (fn 1) or pow (fn 2,
+ * x^y) on n device-resident inputs, for accuracy checks. */
+int nsw6_eval_math(nsw6_handle* h, int fn, const double* x, const double* y, double* out, int n);
+
 /* Per-kernel timing with CUDA events recorded on the handle's stream around
  * each kernel of every step (0 = off, the default). */
 int nsw6_set_timing(nsw6_handle* h, int on);

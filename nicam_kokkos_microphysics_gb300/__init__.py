@@ -118,6 +118,18 @@ class MPDriver:
         ptr = getattr(stream, "cuda_stream", stream)
         _check(self._lib.nsw6_set_stream(self._h, ctypes.c_void_p(int(ptr or 0))), self._lib)
 
+    def set_math(self, mode: int) -> None:
+        """0: table-driven exp/log/pow (default), 1: CUDA math library."""
+        _check(self._lib.nsw6_set_math(self._h, int(mode)), self._lib)
+
+    def eval_math(self, fn: int, x, y=None):
+        """Evaluate the table-driven exp (0), log (1) or pow (2) on CUDA tensors."""
+        import torch
+        out = torch.empty_like(x)
+        yp = y.data_ptr() if y is not None else None
+        _check(self._lib.nsw6_eval_math(self._h, int(fn), x.data_ptr(), yp, out.data_ptr(), x.numel()), self._lib)
+        return out
+
     def set_timing(self, on: bool) -> None:
         _check(self._lib.nsw6_set_timing(self._h, int(bool(on))), self._lib)
 

@@ -98,6 +98,8 @@ def load() -> ctypes.CDLL:
     lib.nsw6_set_itelim.argtypes = [vp, c_int]
     lib.nsw6_last_error.argtypes = [vp] + [ctypes.POINTER(c_int)] * 4
     lib.nsw6_set_timing.argtypes = [vp, c_int]
+    lib.nsw6_set_math.argtypes = [vp, c_int]
+    lib.nsw6_eval_math.argtypes = [vp, c_int, vp, vp, vp, c_int]
     lib.nsw6_read_timing.argtypes = [vp, ctypes.POINTER(c_double), c_int, ctypes.POINTER(c_int)]
     lib.nsw6_strerror.argtypes = [c_int]
     lib.nsw6_strerror.restype = ctypes.c_char_p

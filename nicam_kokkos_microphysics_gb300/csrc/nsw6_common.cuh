@@ -61,6 +61,12 @@ struct Consts {
   // derived products that appear verbatim in the reference expressions
   double log_mi50, log_mi40;
   double Dc_berry, pow_Nc_m179;
+  // constant factors of the process rates folded on the host (nsw6_cell.cuh)
+  double K_rlmdr, K_rlmdg, rAs, K_vtr, K_vts, K_vtg;
+  double K_sacw, K_gacw, K_raci, K_saci, K_iacr, K_sacr, K_2gam2br, K_gacr, K_g13, K_g22, K_racs;
+  double K_aut, rLHF0, K_ventr1, K_ventr2, K_revp, K_ihtr, K_vents2, K_2pi, K_clf, K_ventg1, K_ventg2;
+  double K_gdep, K_gfrz, K_xf, K_r2c, K_r2r;
+  double roh_a[28], roh_b[28];   // per snow moment: ln10*loga and b as cubics in tems
 };
 
 // Per-level grid metrics (GRD_Setup, mod_debug.cpp:92-187), device copy laid
@@ -90,8 +96,11 @@ struct DevStatus {
 struct Problem {
   int gall, kall, kmin, kmax, lall;
   double dt, dt2, dt3;   // dt, pow(dt,2), pow(dt,3) as vadv1d_prep forms them (mod_vadv1d.cpp:265-266)
+  double rdt;            // 1 / dt
   int itelim;
+  int math_lib;                // 0 table-driven transcendentals, 1 CUDA libm
   const double* grid;          // [GF_COUNT][kall]
+  const double* fmtab;         // fast-math tables (nsw6_fastmath.cuh)
   double* const* a;            // not used on device
   // field bases
   double *rhog, *rhogvx, *rhogvy, *rhogvz, *rhogw, *rhoge, *rhogq;

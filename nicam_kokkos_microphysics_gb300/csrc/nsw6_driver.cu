@@ -14,9 +14,12 @@
 
 #include "../../include/nsw6.h"
 #include "nsw6_common.cuh"
+#include "nsw6_fastmath.cuh"
 
 namespace nsw6 {
 cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev);
+cudaError_t launch_math(int fn, const double* x, const double* y, double* out, int n, const double* fmtab,
+                        cudaStream_t stream);
 }
 
 using namespace nsw6;
@@ -26,6 +29,7 @@ struct nsw6_handle {
   nsw6_params params{};
   Consts C{};
   double* d_grid = nullptr;
+  double* d_fmtab = nullptr;
   double* d_zdis = nullptr;
   unsigned long long* d_zmax = nullptr;
   unsigned long long* d_zmin = nullptr;
@@ -33,6 +37,7 @@ struct nsw6_handle {
   cudaStream_t stream = nullptr;
   int sync_check = 1;
   int itelim = 100;
+  int math_lib = 0;   // 0: table-driven exp/log/pow, 1: CUDA libm
   // device staging of the 50 arguments for host-memory calls (allocated by the
   // first such call)
   double* d_stage = nullptr;
@@ -141,7 +146,79 @@ Consts make_consts(const nsw6_params& p) {
   c.log_mi50 = std::log(c.mi50);
   c.log_mi40 = std::log(c.mi40);
   c.pow_Nc_m179 = std::pow(c.Nc_def, -1.79);
+
+  // folded constant factors (nsw6_cell.cuh); GAM = GAM_2 = 1, GAM_3 = 2,
+  // Esw = Egw = Eri = Esr = Egr = 1 (mod_mp_nsw6.h:58-67, mp_nsw6_init :345-356)
+  const double GAM = 1.0, GAM_2 = 1.0, GAM_3 = 2.0;
+  c.K_rlmdr = 1.0 / (c.Ar * c.N0r * c.GAM_1br);
+  c.K_rlmdg = 1.0 / (c.Ag * c.N0g * c.GAM_1bg);
+  c.rAs = 1.0 / c.As;
+  c.K_vtr = -c.Cr * c.GAM_1brdr / c.GAM_1br;
+  c.K_vts = -c.Cs;
+  c.K_vtg = -c.Cg * c.GAM_1bgdg / c.GAM_1bg;
+  c.K_sacw = 0.25 * PI * c.Cs;
+  c.K_gacw = 0.25 * PI * c.N0g * c.Cg * c.GAM_3dg;
+  c.K_raci = 0.25 * PI * c.N0r * c.Cr * c.GAM_3dr;
+  c.K_saci = 0.25 * PI * c.Cs;
+  c.K_iacr = c.Ar / c.mi * 0.25 * PI * c.N0r * c.Cr * c.GAM_6dr;
+  c.K_sacr = c.Ar * 0.25 * PI * c.N0r;
+  c.K_2gam2br = 2.0 * c.GAM_2br;
+  c.K_gacr = c.Ar * 0.25 * PI * c.N0g * c.N0r;
+  c.K_g13 = c.GAM_1br * GAM_3;
+  c.K_g22 = 2.0 * c.GAM_2br * GAM_2;
+  c.K_racs = c.As * 0.25 * PI * c.N0r;
+  c.K_aut = c.kk_aut * c.pow_Nc_m179;
+  c.rLHF0 = 1.0 / LHF0;
+  c.K_ventr1 = 0.78 * GAM_2;
+  c.K_ventr2 = 0.27 * c.GAM_5dr_h;
+  c.K_revp = 2.0 * PI * c.N0r;
+  c.K_ihtr = c.B_frz / (DWATR * (c.Nc_ihtr * 1.0E+6));
+  c.K_vents2 = 0.39 * std::sqrt(c.Cs);
+  c.K_2pi = 2.0 * PI;
+  c.K_clf = CL / LHF0;
+  c.K_ventg1 = 0.78 * GAM_2;
+  c.K_ventg2 = 0.27 * c.GAM_5dg_h;
+  c.K_gdep = 2.0 * PI * c.N0g;
+  c.K_gfrz = 2.0 * PI * c.N0r * 60.0 * c.B_frz * c.Ar;
+  c.K_xf = 1.0E-9 / c.Nc_def;
+  c.K_r2c = c.coef_dgam * (c.Nc_def * 1.0E+6);
+  c.K_r2r = 0.25 * c.N0r * GAM_3;
+  (void)GAM;
+  // Roh and Satoh (2014) moments (mod_mp_nsw6.cpp:994-1057): loga(nm, t) and
+  // b(nm, t) expanded as cubics in t = tems for nm = 0, 1, 2, 3, 4, 2.25, 1.625
+  static const double nms[7] = {0.0, 1.0, 2.0, 3.0, 4.0, 2.25, 1.625};
+  for (int i = 0; i < 7; ++i) {
+    const double nm = nms[i];
+    const double* A = c.coef_a;
+    const double* B = c.coef_b;
+    const double ea[4] = {A[0] + nm * (A[2] + nm * (A[5] + nm * A[9])), A[1] + nm * (A[3] + nm * A[7]),
+                          A[4] + nm * A[6], A[8]};
+    const double eb[4] = {B[0] + nm * (B[2] + nm * (B[5] + nm * B[9])), B[1] + nm * (B[3] + nm * B[7]),
+                          B[4] + nm * B[6], B[8]};
+    for (int j = 0; j < 4; ++j) {
+      c.roh_a[4 * i + j] = c.ln10 * ea[j];
+      c.roh_b[4 * i + j] = eb[j];
+    }
+  }
   return c;
+}
+
+// Fast-math tables (nsw6_fastmath.cuh), computed in extended precision:
+// [0,256) 2^(j/256); [256,512) 1/c_j; [512,768) -log(1/c_j), where c_j is the
+// centre of the j-th of 256 mantissa intervals of [0.75, 1.5).
+void build_fastmath_tables(double* t) {
+  for (int j = 0; j < FM_EXP_N; ++j) t[j] = (double)exp2l((long double)j / 256.0L);
+  for (int j = 0; j < FM_LOG_N; ++j) {
+    unsigned long long lo_bits = 0x3FE8000000000000ull + ((unsigned long long)j << 44);
+    unsigned long long hi_bits = lo_bits + (1ull << 44);
+    double mlo, mhi;
+    std::memcpy(&mlo, &lo_bits, 8);
+    std::memcpy(&mhi, &hi_bits, 8);
+    const long double cj = 0.5L * ((long double)mlo + (long double)mhi);
+    const double ic = (double)(1.0L / cj);
+    t[FM_EXP_N + j] = ic;
+    t[FM_EXP_N + FM_LOG_N + j] = (double)(-logl((long double)ic));
+  }
 }
 
 // GRD_Setup, mod_debug.cpp:92-187, plus GRD_gz_shift (mod_precip_transport.cpp:698-709).
@@ -254,6 +331,9 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.dt3 = std::pow(dt, 3);
   P.itelim = h->itelim;
   P.grid = h->d_grid;
+  P.fmtab = h->d_fmtab;
+  P.rdt = 1.0 / dt;
+  P.math_lib = h->math_lib;
   P.rhog = a[A_rhog];
   P.rhogvx = a[A_rhogvx];
   P.rhogvy = a[A_rhogvy];
@@ -369,8 +449,10 @@ int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const doubl
   h->lall_max = lall_max;
   nsw6_default_params(&h->params);
   h->C = make_consts(h->params);
-  double* hgrid = (double*)std::malloc(sizeof(double) * GF_COUNT * (size_t)kall);
+  double* hgrid = (double*)std::malloc(sizeof(double) * (GF_COUNT * (size_t)kall + FM_TABLE_DOUBLES));
   make_grid(kall, gz, gzh, hgrid);
+  double* htab = hgrid + GF_COUNT * (size_t)kall;
+  build_fastmath_tables(htab);
   const size_t KG = (size_t)kall * gall;
   const size_t nkey = (size_t)lall_max * 6 * kall;
   bool ok = cudaMalloc(&h->d_grid, sizeof(double) * GF_COUNT * kall) == cudaSuccess &&
@@ -378,6 +460,8 @@ int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const doubl
             cudaMalloc(&h->d_zmax, sizeof(unsigned long long) * nkey) == cudaSuccess &&
             cudaMalloc(&h->d_zmin, sizeof(unsigned long long) * nkey) == cudaSuccess &&
             cudaMalloc(&h->d_status, sizeof(DevStatus)) == cudaSuccess &&
+            cudaMalloc(&h->d_fmtab, sizeof(double) * FM_TABLE_DOUBLES) == cudaSuccess &&
+            cudaMemcpy(h->d_fmtab, htab, sizeof(double) * FM_TABLE_DOUBLES, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(h->d_grid, hgrid, sizeof(double) * GF_COUNT * kall, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemset(h->d_status, 0, sizeof(DevStatus)) == cudaSuccess;
   std::free(hgrid);
@@ -392,6 +476,7 @@ int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const doubl
 int nsw6_destroy(nsw6_handle* h) {
   if (!h) return NSW6_OK;
   cudaFree(h->d_grid);
+  cudaFree(h->d_fmtab);
   cudaFree(h->d_zdis);
   cudaFree(h->d_zmax);
   cudaFree(h->d_zmin);
@@ -433,6 +518,18 @@ int nsw6_set_itelim(nsw6_handle* h, int itelim) {
   if (!h || itelim < 1) return NSW6_ERR_BAD_ARG;
   h->itelim = itelim;
   return NSW6_OK;
+}
+
+int nsw6_set_math(nsw6_handle* h, int mode) {
+  if (!h || mode < 0 || mode > 1) return NSW6_ERR_BAD_ARG;
+  h->math_lib = mode;
+  return NSW6_OK;
+}
+
+int nsw6_eval_math(nsw6_handle* h, int fn, const double* x, const double* y, double* out, int n) {
+  if (!h || fn < 0 || fn > 2 || n < 0 || !x || !out || (fn == 2 && !y)) return NSW6_ERR_BAD_ARG;
+  if (launch_math(fn, x, y, out, n, h->d_fmtab, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  return cudaStreamSynchronize(h->stream) == cudaSuccess ? NSW6_OK : NSW6_ERR_CUDA;
 }
 
 int nsw6_set_timing(nsw6_handle* h, int on) {

@@ -26,6 +26,7 @@
 
 #include "nsw6_cell.cuh"
 #include "nsw6_common.cuh"
+#include "nsw6_fastmath.cuh"
 
 namespace nsw6 {
 
@@ -42,6 +43,18 @@ __device__ __forceinline__ void record_error(DevStatus* st, int code, int k, int
 }
 
 // ------------------------------------------------------------------ kernel 1
+template <class M>
+__device__ __forceinline__ M make_math(const double* tab);
+template <>
+__device__ __forceinline__ FastMath make_math<FastMath>(const double* tab) {
+  return FastMath{tab, tab + FM_EXP_N, tab + FM_EXP_N + FM_LOG_N};
+}
+template <>
+__device__ __forceinline__ LibMath make_math<LibMath>(const double*) {
+  return LibMath{};
+}
+
+template <class M>
 __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Consts C) {
   extern __shared__ double sm[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
@@ -52,10 +65,13 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
   const size_t offq = (size_t)l * NQ * KG;
   double* vts = sm;                      // [3][K][CELL_TG] fall speeds of QR, QS, QG
   double* grid = sm + 3 * K * CELL_TG;   // [GF_COUNT][K]
+  double* tab = grid + GF_COUNT * K;     // [FM_TABLE_DOUBLES]
 
   for (int c = threadIdx.x; c < 3 * K * CELL_TG; c += blockDim.x) vts[c] = 0.0;
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) grid[c] = P.grid[c];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
+  const M mth = make_math<M>(tab);
 
   const int nlev = kmax - kmin + 1;
   for (int c = threadIdx.x; c < nlev * CELL_TG; c += blockDim.x) {
@@ -73,7 +89,7 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
 #pragma unroll
     for (int n = 0; n < 6; ++n) in.rhogq[n] = P.rhogq[iq + (size_t)n * KG];
     CellOut o;
-    nsw6_cell(C, P.dt, in, o);
+    nsw6_cell(C, mth, P.dt, P.rdt, in, o);
     P.rhog[i] = o.rhog;
     P.rhoge[i] = o.rhoge;
     P.tem[i] = o.tem;
@@ -83,9 +99,9 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
     for (int n = 1; n < 6; ++n) P.q[iq + (size_t)n * KG] = o.q[n];
     P.re_liquid[i] = o.rceff;
     P.re_cld[i] = o.rceff_cld;
-    vts[(0 * K + k) * CELL_TG + gx] = o.Vt[0];  // QR
-    vts[(1 * K + k) * CELL_TG + gx] = o.Vt[2];  // QS
-    vts[(2 * K + k) * CELL_TG + gx] = o.Vt[3];  // QG
+    vts[(0 * K + k) * CELL_TG + gx] = o.Vtr;
+    vts[(1 * K + k) * CELL_TG + gx] = o.Vts;
+    vts[(2 * K + k) * CELL_TG + gx] = o.Vtg;
     if (k == kmax) {
       // The reference writes the cloud-top scalars from every level in parallel
       // (mod_mp_nsw6.cpp:1579-1592); the sequential order, in which the top
@@ -209,7 +225,7 @@ __device__ __forceinline__ double flux_integral(const double* rhof_col, const do
   return f * (0.5 + copysign(0.5, fabs(f) - EPS));
 }
 
-template <int COL_TG>
+template <int COL_TG, class M>
 __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   extern __shared__ double smraw[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
@@ -228,11 +244,15 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   S.bmin = reinterpret_cast<int*>(S.colacc + 6 * COL_TG);
   S.bmax = S.bmin + 6 * K;
   S.kc = reinterpret_cast<unsigned char*>(S.bmax + 6 * K);
+  double* tab = reinterpret_cast<double*>(
+      (reinterpret_cast<uintptr_t>(S.kc + (size_t)K * COL_TG) + 15) & ~(uintptr_t)15);
   auto F = [&](int slot) { return S.f + (size_t)slot * ncell; };
 
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) S.grid[c] = P.grid[c];
   for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) S.colacc[c] = 0.0;
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
+  const M mth = make_math<M>(tab);
   const double* gzh = S.grid + GF_GZH * K;
   const double* gzs = S.grid + GF_GZSHIFT * K;
   const double* dgz = S.grid + GF_DGZ * K;
@@ -315,6 +335,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   const int tracer[3] = {I_QR, I_QS, I_QG};
   for (int t = 0; t < 3; ++t) {
     const int nq = tracer[t];
+    // departure distances of this region: [6][K][G] rows t (full) and 3 + t (half)
     const double* zdis0 = P.zdis + ((size_t)l * 6 + t) * KG;
     const double* zdis0h = P.zdis + ((size_t)l * 6 + 3 + t) * KG;
     const int* bmn_f = S.bmin + t * K;
@@ -330,7 +351,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       if (g >= G) continue;
       const size_t i = (size_t)k * G + g;
       F(S_BASE)[c] = rhogq_n[i] * F(S_RGS)[c];
-      if (k >= kmin && k <= kmax) S.kc[c] = (unsigned char)departure_cell(gzh, k, zdis0[off + i], bmn_f[k], bmx_f[k], kmin, kmax);
+      if (k >= kmin && k <= kmax) S.kc[c] = (unsigned char)departure_cell(gzh, k, zdis0[i], bmn_f[k], bmx_f[k], kmin, kmax);
     }
     __syncthreads();
 
@@ -358,7 +379,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
         double fl = 0.0;
         if (g < G && k >= kmin && k <= kmax)
-          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[off + (size_t)k * G + g], bmn_f[k], bmx_f[k]);
+          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[(size_t)k * G + g], bmn_f[k], bmx_f[k]);
         F(S_F)[c] = fl;
       }
       __syncthreads();
@@ -407,7 +428,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       if (g < G && k >= kmin + 1 && k <= kmax) {
         const size_t i = off + (size_t)k * G + g;
         qh = 0.5 * (q_n[i - off] + q_n[i - off - G]) * (P.gam2h[i] / P.gsgam2h[i]);
-        S.kc[c] = (unsigned char)departure_cell(gzs, k, zdis0h[i], bmn_h[k], bmx_h[k], kmin + 1, kmax);
+        S.kc[c] = (unsigned char)departure_cell(gzs, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
       }
       F(S_BASE)[c] = qh;
       F(S_RHOF)[c] = qh * F(S_KINV)[c];
@@ -420,7 +441,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
         double fl = 0.0;
         if (g < G && k >= kmin + 1 && k <= kmax)
-          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgzh, k, S.kc[c], zdis0h[off + (size_t)k * G + g], bmn_h[k], bmx_f[k]);
+          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgzh, k, S.kc[c], zdis0h[(size_t)k * G + g], bmn_h[k], bmx_f[k]);
         F(S_F)[c] = fl;
       }
       __syncthreads();
@@ -523,11 +544,13 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     double rq[6], q[6];
 #pragma unroll
     for (int n = 0; n < 6; ++n) rq[n] = P.rhogq[iq + (size_t)n * KG];
+    const double rrhog = 1.0 / rhog;
 #pragma unroll
-    for (int n = 0; n < 6; ++n) q[n] = rq[n] / rhog;
+    for (int n = 0; n < 6; ++n) q[n] = rq[n] * rrhog;
     const double gsg = P.gsgam2[i];
-    double rho = rhog / gsg;
-    const double ein = rhoge / rhog;
+    const double rgsg = 1.0 / gsg;
+    double rho = rhog * rgsg;
+    const double ein = rhoge * rrhog;
     double qd = 1.0;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) qd = qd - q[n];
@@ -543,30 +566,31 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     double pre = rho * tem * (qdl * RDRY + q[I_QV] * RVAP);
 
     // SATURATION_adjustment, ice_adjust = false (mod_satadjust.cpp:274-362)
-    const double ein_moist = rhoge / rhog + q[I_QV] * LHV0;
+    const double ein_moist = ein + q[I_QV] * LHV0;
     const double qsum = q[I_QV] + q[I_QC];
     q[I_QV] = qsum;
     q[I_QC] = 0.0;
     double cvtot = qd * CVDRY;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
-    const double rho_l = rhog / gsg;
+    const double rho_l = rho;
     tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
     if (interior) {
       // satadjust_liq, mod_satadjust.cpp:771-896
       double qd_l = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
+      const double rrhor = 1.0 / (rho_l * RVAP);
       double rtem = 1.0 / (dmax(tem, TEM_MIN));
-      double psat = PSAT0 * exp(C.LovR_liq * (C.RTEM00 - rtem));
-      double qsat = psat / (rho_l * RVAP * tem);
+      double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      double qsat = psat * rrhor * rtem;
       if (qsum - qsat > EPS) {
         bool converged = false;
         int ite;
         for (ite = 0; ite < P.itelim; ++ite) {
           rtem = 1.0 / (dmax(tem, TEM_MIN));
-          psat = PSAT0 * exp(C.LovR_liq * (C.RTEM00 - rtem));
-          qsat = psat / (rho_l * RVAP * tem);
+          psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+          qsat = psat * rrhor * rtem;
           q[I_QV] = qsat;
           q[I_QC] = qsum - qsat;
           double cv = qd_l * CVDRY;
@@ -575,7 +599,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
           const double emoist_new = tem * cv + q[I_QV] * LHV0;
           // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
           // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
-          const double dqsat_dT = (C.LovR_liq / (tem * tem)) * qsat;
+          const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
           const double demoist_dT = cv + dqsat_dT * LHV0;
           const double dtemp = (emoist_new - ein_moist) / demoist_dT;
           tem = tem - dtemp;
@@ -611,9 +635,10 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       rq[I_QV] = dmax(rq[I_QV], 0.0);
       diffq -= rq[I_QV];
       rhog_o = rhog * (1.0 - diffq);
-      rho = rhog_o / gsg;
+      rho = rhog_o * rgsg;
+      const double rro = 1.0 / rhog_o;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n) q[n] = rq[n] / rhog_o;
+      for (int n = 1; n <= 5; ++n) q[n] = rq[n] * rro;
       double qdf = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
@@ -662,15 +687,38 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   }
 }
 
+// ------------------------------------------------------------------ math check
+// Evaluates the step's table-driven transcendentals on n inputs:
+// fn 0 exp(x), 1 log(x), 2 pow(x, y).
+__global__ void nsw6_math_kernel(int fn, const double* x, const double* y, double* out, int n, const double* fmtab) {
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = fmtab[c];
+  __syncthreads();
+  const FastMath m = make_math<FastMath>(tab);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = x[i];
+    out[i] = fn == 0 ? m.exp(v) : fn == 1 ? m.log(v) : m.pow(v, y[i]);
+  }
+}
+
+cudaError_t launch_math(int fn, const double* x, const double* y, double* out, int n, const double* fmtab,
+                        cudaStream_t stream) {
+  const int blocks = n <= 0 ? 1 : (n + 255) / 256 > 1024 ? 1024 : (n + 255) / 256;
+  nsw6_math_kernel<<<blocks, 256, 0, stream>>>(fn, x, y, out, n, fmtab);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ launchers
-size_t cell_smem_bytes(int K) { return sizeof(double) * (size_t)(3 * K * CELL_TG + GF_COUNT * K); }
+size_t cell_smem_bytes(int K) {
+  return sizeof(double) * (size_t)(3 * K * CELL_TG + GF_COUNT * K + FM_TABLE_DOUBLES);
+}
 
 int column_tile(int K) { return K <= 64 ? 16 : 8; }
 
 size_t column_smem_bytes(int K) {
   const int TG = column_tile(K);
-  return sizeof(double) * ((size_t)S_COUNT * K * TG + GF_COUNT * K + 6 * TG) + sizeof(int) * 12 * K +
-         (size_t)K * TG + 16;
+  return sizeof(double) * ((size_t)S_COUNT * K * TG + GF_COUNT * K + 6 * TG + FM_TABLE_DOUBLES) +
+         sizeof(int) * 12 * K + (size_t)K * TG + 16;
 }
 
 int column_threads(int K) {
@@ -691,19 +739,29 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   const size_t s2 = column_smem_bytes(P.kall);
   static bool attr_done = false;
   if (!attr_done) {
-    cudaFuncSetAttribute(nsw6_cell_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(nsw6_cell_kernel<FastMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(nsw6_cell_kernel<LibMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<16, FastMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<8, FastMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<16, LibMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<8, LibMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     attr_done = true;
   }
   dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
   if (ev) cudaEventRecord(ev[0], stream);
-  nsw6_cell_kernel<<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  if (P.math_lib) nsw6_cell_kernel<LibMath><<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  else nsw6_cell_kernel<FastMath><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   if (ev) cudaEventRecord(ev[1], stream);
   const int tg = column_tile(P.kall);
   dim3 g2((P.gall + tg - 1) / tg, P.lall);
-  if (tg == 16) nsw6_column_kernel<16><<<g2, column_threads(P.kall), s2, stream>>>(P, C);
-  else nsw6_column_kernel<8><<<g2, column_threads(P.kall), s2, stream>>>(P, C);
+  const int nt = column_threads(P.kall);
+  if (tg == 16) {
+    if (P.math_lib) nsw6_column_kernel<16, LibMath><<<g2, nt, s2, stream>>>(P, C);
+    else nsw6_column_kernel<16, FastMath><<<g2, nt, s2, stream>>>(P, C);
+  } else {
+    if (P.math_lib) nsw6_column_kernel<8, LibMath><<<g2, nt, s2, stream>>>(P, C);
+    else nsw6_column_kernel<8, FastMath><<<g2, nt, s2, stream>>>(P, C);
+  }
   if (ev) cudaEventRecord(ev[2], stream);
   return cudaGetLastError();
 }
