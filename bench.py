@@ -47,6 +47,9 @@ ALGO_BYTES_PER_CELL = 49 * 8 + 3
 # rhogq(6), q(QV), tem, gsgam2 and writes rhog, rhoge, tem, rhogq(6), q(5),
 # re_liquid, re_cld.
 CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
+# DRAM bytes (read + write) per interior cell of the cell kernel, from the ncu
+# capture of one 16900 x 42 region (profiles/nsw6_cell_kernel_16900x42.md).
+CELL_KERNEL_TRAFFIC_PER_CELL = 170.5
 
 
 def env_rank():
@@ -115,8 +118,11 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def fp64_probe():
-    """FP64 pipe rate of this GPU (DFMA per second) from the throughput probe."""
+def fp64_rates():
+    """Measured FP64 rates of this GPU (throughput probe): DFMA per second and
+    the op weights of the CUDA FP64 functions in FP64 flop equivalents (an FMA
+    counts 2, so weight = 2 x DFMA rate / function rate, less the additions
+    and multiplications the probe loop wraps around each call)."""
     import ctypes
     from nicam_kokkos_microphysics_gb300 import _native
     if not _native.PROBE_LIB.exists():
@@ -124,8 +130,35 @@ def fp64_probe():
     lib = ctypes.CDLL(str(_native.PROBE_LIB))
     lib.nsw6_probe_rate.restype = ctypes.c_double
     lib.nsw6_probe_rate.argtypes = [ctypes.c_int, ctypes.c_int]
-    r = lib.nsw6_probe_rate(0, 4000)
-    return r if r > 0 else None
+    r = {n: lib.nsw6_probe_rate(i, it) for i, (n, it) in
+         enumerate([("dfma", 4000), ("dadd", 4000), ("dmul", 4000), ("div", 1000), ("sqrt", 1000),
+                    ("exp", 500), ("log", 500), ("pow", 250)])}
+    if min(r.values()) <= 0:
+        return None
+    extra = {"div": 0, "sqrt": 1, "exp": 2, "log": 1, "pow": 1}
+    w = {"add": 1.0, "mul": 1.0, "cmp": 1.0}
+    for k, e in extra.items():
+        w[k] = 2.0 * (r["dfma"] / r[k] - e)
+    return {"dfma_per_s": r["dfma"], "peak_tflops": 2.0 * r["dfma"] / 1e12, "weights": w, "rates": r}
+
+
+def algorithmic_work(spec: StateSpec, st: dict, weights: dict) -> dict:
+    """FP64 work per cell of the reference algorithm on region 0 of the state,
+    counted by the operation-counting build of the oracle (integer powers as
+    products), weighted with the measured op weights."""
+    from oracle import restatement
+    reg = region_view(st, 0)
+    c = restatement.count_ops(reg, st["_gz"], st["_gzh"], spec.dt)
+    n_int = spec.gall * (spec.kall - 2)
+    n_all = spec.gall * spec.kall
+
+    def work(ph):
+        return sum(c[ph][k] * weights[k] for k in c[ph])
+
+    return {"cell_per_interior_cell": (work("cell") + work("zdis")) / n_int,
+            "column_per_cell": work("column") / n_all,
+            "counts_per_interior_cell": {k: (c["cell"][k] + c["zdis"][k]) / n_int for k in c["cell"]},
+            "column_counts_per_cell": {k: c["column"][k] / n_all for k in c["column"]}}
 
 
 # ----------------------------------------------------------------- CPU side
@@ -217,6 +250,7 @@ def main(argv=None) -> int:
     spec = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall, seed=args.seed + 7919 * rank,
                      variant=args.variant)
     st = make_state(spec, out_fill=0.0)
+    st0 = {k: v.copy() for k, v in st.items()}
     drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
     dev = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
     args_dev = [dev[n] for n in ARG_NAMES]
@@ -296,19 +330,36 @@ def main(argv=None) -> int:
         e2e = {"value": cells_rank * world / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": dt_e2e * 1e3}
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of the dominant kernel (the cell kernel: FP64-pipe bound)
     peaks, src = measured_peaks()
     n_int = spec.gall * (spec.kall - 2) * spec.lall
     cell_ms = t_cell / max(nsteps, 1)
     col_ms = t_col / max(nsteps, 1)
-    dfma = fp64_probe()
-    achieved_gbs = CELL_KERNEL_BYTES_PER_CELL * n_int / (cell_ms * 1e-3) / 1e9
-    roofline = {"kernel": "nsw6_cell_kernel", "bound": "hbm", "achieved": achieved_gbs,
-                "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved_gbs / peaks["hbm_gbs"],
-                "traffic": None, "peak_source": f"{src} copy bandwidth",
-                "cell_kernel_ms": cell_ms, "column_kernel_ms": col_ms,
-                "fp64_fma_per_s_measured": dfma,
-                "note": "the cell kernel is FP64-pipe bound; the HBM fraction is reported for reference"}
+    rates = fp64_rates()
+    hbm_gbs = CELL_KERNEL_BYTES_PER_CELL * n_int / (cell_ms * 1e-3) / 1e9
+    roofline = {"kernel": "nsw6_cell_kernel", "cell_kernel_ms": cell_ms, "column_kernel_ms": col_ms,
+                "hbm": {"achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                        "frac": hbm_gbs / peaks["hbm_gbs"], "peak_source": f"{src} copy bandwidth"}}
+    if rates:
+        aw = algorithmic_work(spec, st0, rates["weights"])
+        flops = aw["cell_per_interior_cell"] * n_int
+        achieved = flops / (cell_ms * 1e-3) / 1e12
+        col_flops = aw["column_per_cell"] * spec.cells
+        roofline.update({
+            "bound": "fp64", "achieved": achieved, "peak": rates["peak_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / rates["peak_tflops"], "traffic": CELL_KERNEL_TRAFFIC_PER_CELL * n_int,
+            "peak_source": "measured in this run: FP64 FMA throughput probe (MEASURED_PEAKS.json has no FP64 peak)",
+            "work_per_interior_cell": aw["cell_per_interior_cell"],
+            "work_definition": "reference operations counted on this state (integer powers as products), "
+                               "weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by measured cost",
+            "op_weights": rates["weights"],
+            "column_kernel": {"achieved": col_flops / (col_ms * 1e-3) / 1e12,
+                              "frac": col_flops / (col_ms * 1e-3) / 1e12 / rates["peak_tflops"],
+                              "work_per_cell": aw["column_per_cell"]},
+        })
+    else:
+        roofline.update({"bound": "hbm", "achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": hbm_gbs / peaks["hbm_gbs"], "traffic": None})
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -151,9 +151,9 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
   const double Vts = C.K_vts * rho_fact * RMOMs_Vt;
   const double Vtg = C.K_vtg * rho_fact * RLMDg_dg;
 
-  // nucleation, :1080-1085; Qi0 = ice_nuc * Ni0^1.33 / dens
-  const double Ni0 = dmax(mth.exp(-0.1 * temc), 1.0) * 1000.0;
-  const double Qi0 = C.ice_nuc * mth.pow(Ni0, 1.33) * Rdens;
+  // nucleation, :1080-1085: Ni0 = max(exp(-0.1 temc), 1) * 1000 and
+  // Qi0 = ice_nuc * Ni0^1.33 / dens, with log(Ni0) = ln 1000 + max(-0.1 temc, 0)
+  const double Qi0 = C.ice_nuc * mth.exp(1.33 * (C.ln1000 + dmax(-0.1 * temc, 0.0))) * Rdens;
   double Pigen = dmax(dmin(Qi0 - qi, qv - qsati), 0.0) * rdt;
 
   // accretion, :1087-1145
@@ -345,22 +345,27 @@ __device__ __forceinline__ double vadv_wh(const WP& wp, int j, int mkmin, int mk
 }
 
 // Departure distance zdis(k) of vadv1d_prep for k in [mkmin, mkmax]
-// (mod_vadv1d.cpp:284-302), in the reference's evaluation order: it decides
-// the departure cells and the region-wide bounds, so it is kept exact.
+// (mod_vadv1d.cpp:284-302):
+//   zdis = dt w - dt^2/2 w (w+ - w-)/(dz- + dz) + dt^3/6 w (r^2 + w c),
+//   r = (w+ - w-)/(dz- + dz),  c = 2 ((w+ - w)/dz - (w - w-)/dz-)/(dz- + dz),
+// evaluated with the per-level reciprocals rdz = 1/dz and rdzs = 1/(dz- + dz)
+// instead of divisions.  zdis only decides which layer the departure point
+// lies in (an ulp-level change matters only within an ulp of an interface)
+// and scales the flux of the departure layer.
 template <class WP>
-__device__ __forceinline__ double vadv_zdis(const WP& wp, const double* dz, int k, int mkmin, int mkmax, double dt,
-                                           double dt2, double dt3) {
+__device__ __forceinline__ double vadv_zdis(const WP& wp, const double* rdz, const double* rdzs, int k, int mkmin,
+                                           int mkmax, double dt, double hdt2, double sdt3) {
   if (k == mkmin) {
     const double w0 = vadv_wh(wp, mkmin, mkmin, mkmax), wpp = vadv_wh(wp, mkmin + 1, mkmin, mkmax);
-    return dt * w0 - dt2 * w0 * (wpp - w0) / dz[mkmin] / 2.0;
+    return __fma_rn(-hdt2 * w0, (wpp - w0) * rdz[mkmin], dt * w0);
   }
   const double wm = vadv_wh(wp, k - 1, mkmin, mkmax);
   const double w0 = vadv_wh(wp, k, mkmin, mkmax);
   const double wpp = vadv_wh(wp, k + 1, mkmin, mkmax);
-  const double dzs = dz[k - 1] + dz[k];
-  const double r = (wpp - wm) / dzs;
-  return dt * w0 - dt2 * w0 * (wpp - wm) / dzs / 2.0 +
-         dt3 * w0 * (r * r + w0 * (((wpp - w0) / dz[k] - (w0 - wm) / dz[k - 1]) / dzs * 2.0)) / 6.0;
+  const double r = (wpp - wm) * rdzs[k];
+  const double c = 2.0 * rdzs[k] * __fma_rn(wpp - w0, rdz[k], -(w0 - wm) * rdz[k - 1]);
+  const double t3 = sdt3 * w0 * __fma_rn(w0, c, r * r);
+  return __fma_rn(-hdt2 * w0, r, __fma_rn(dt, w0, t3));
 }
 
 }  // namespace nsw6

@@ -67,12 +67,15 @@ struct Consts {
   double K_aut, rLHF0, K_ventr1, K_ventr2, K_revp, K_ihtr, K_vents2, K_2pi, K_clf, K_ventg1, K_ventg2;
   double K_gdep, K_gfrz, K_xf, K_r2c, K_r2r;
   double roh_a[28], roh_b[28];   // per snow moment: ln10*loga and b as cubics in tems
+  double ln1000;
 };
 
 // Per-level grid metrics (GRD_Setup, mod_debug.cpp:92-187), device copy laid
 // out as [field][kall].
 enum GridField {
-  GF_GZ, GF_GZH, GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH, GF_AFACT, GF_BFACT, GF_CFACT, GF_DFACT, GF_GZSHIFT, GF_COUNT
+  GF_GZ, GF_GZH, GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH, GF_AFACT, GF_BFACT, GF_CFACT, GF_DFACT, GF_GZSHIFT,
+  GF_RDZS, GF_RDZSH,   // 1 / (dgz(k-1) + dgz(k)) and 1 / (dgzh(k-1) + dgzh(k)), k >= 1
+  GF_COUNT
 };
 
 // Argument positions of mp_driver (mod_mp_driver.h:71-124).
@@ -96,6 +99,7 @@ struct DevStatus {
 struct Problem {
   int gall, kall, kmin, kmax, lall;
   double dt, dt2, dt3;   // dt, pow(dt,2), pow(dt,3) as vadv1d_prep forms them (mod_vadv1d.cpp:265-266)
+  double hdt2, sdt3;     // dt^2 / 2 and dt^3 / 6
   double rdt;            // 1 / dt
   int itelim;
   int math_lib;                // 0 table-driven transcendentals, 1 CUDA libm

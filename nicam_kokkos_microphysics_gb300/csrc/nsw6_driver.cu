@@ -146,6 +146,7 @@ Consts make_consts(const nsw6_params& p) {
   c.log_mi50 = std::log(c.mi50);
   c.log_mi40 = std::log(c.mi40);
   c.pow_Nc_m179 = std::pow(c.Nc_def, -1.79);
+  c.ln1000 = std::log(1000.0);
 
   // folded constant factors (nsw6_cell.cuh); GAM = GAM_2 = 1, GAM_3 = 2,
   // Esw = Egw = Eri = Esr = Egr = 1 (mod_mp_nsw6.h:58-67, mp_nsw6_init :345-356)
@@ -256,6 +257,12 @@ void make_grid(int K, const double* gz, const double* gzh, double* out /* [GF_CO
   cf[kmax + 1] = 0.0;
   for (int k = 0; k < K; ++k) df[k] = 1.0 - cf[k];
   for (int k = kmin; k <= kmax + 1; ++k) gzs[k] = g_gz[k - 1];
+  double* rdzs = out + GF_RDZS * K;
+  double* rdzsh = out + GF_RDZSH * K;
+  for (int k = 1; k < K; ++k) {
+    rdzs[k] = 1.0 / (dgz[k - 1] + dgz[k]);
+    rdzsh[k] = 1.0 / (dgzh[k - 1] + dgzh[k]);
+  }
 }
 
 // Elements per region of each mp_driver argument (reference order).
@@ -329,6 +336,8 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.dt = dt;
   P.dt2 = std::pow(dt, 2);
   P.dt3 = std::pow(dt, 3);
+  P.hdt2 = P.dt2 / 2.0;
+  P.sdt3 = P.dt3 / 6.0;
   P.itelim = h->itelim;
   P.grid = h->d_grid;
   P.fmtab = h->d_fmtab;

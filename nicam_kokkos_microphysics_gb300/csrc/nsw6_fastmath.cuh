@@ -68,6 +68,10 @@ struct FastMath {
       lo = 0.0;
       return ::log(x);
     }
+    if (fabs(x - 1.0) < NEAR1) {  // x - 1 is exact here (Sterbenz)
+      lo = 0.0;
+      return log1p_near1(x - 1.0);
+    }
     const long long u = bits - 0x3FE8000000000000ll;       // relative to 0.75
     const long long e = u >> 52;                            // arithmetic shift
     const int j = (int)((u >> 44) & (FM_LOG_N - 1));
@@ -86,6 +90,20 @@ struct FastMath {
     return hi;
   }
 
+  // Near x = 1 the table split cancels; log(x) = log1p(f) with f = x - 1 is
+  // evaluated directly as f + f^2 (-1/2 + f (1/3 + ... + f (-1/8))), whose
+  // truncation error is below 2e-18 relative for |f| < 1/128.
+  static constexpr double NEAR1 = 0.0078125;
+  __device__ __forceinline__ static double log1p_near1(double f) {
+    double q = __fma_rn(f, -1.2500000000000000e-01, 1.4285714285714285e-01);
+    q = __fma_rn(q, f, -1.6666666666666666e-01);
+    q = __fma_rn(q, f, 2.0e-01);
+    q = __fma_rn(q, f, -0.25);
+    q = __fma_rn(q, f, 3.3333333333333331e-01);
+    q = __fma_rn(q, f, -0.5);
+    return __fma_rn(q, __dmul_rn(f, f), f);
+  }
+
   // log1p(r) = r - r^2/2 + r^3/3 - r^4/4 + r^5/5 - r^6/6 for |r| < 2e-3.
   __device__ __forceinline__ static double log1p_poly(double r) {
     double q = __fma_rn(r, -1.6666666666666666e-01, 2.0e-01);
@@ -99,6 +117,7 @@ struct FastMath {
   __device__ __forceinline__ double log(double x) const {
     const long long bits = __double_as_longlong(x);
     if (!(x >= 2.2250738585072014e-308 && x < 1.7976931348623157e308)) return ::log(x);
+    if (fabs(x - 1.0) < NEAR1) return log1p_near1(x - 1.0);
     const long long u = bits - 0x3FE8000000000000ll;
     const long long e = u >> 52;
     const int j = (int)((u >> 44) & (FM_LOG_N - 1));

@@ -118,8 +118,10 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
   // Departure distances (vadv1d_prep) and their per-level region extrema.
   // Row s = t + 3*half: t = QR, QS, QG; half = 0 full levels (mkmin = kmin,
   // dz = dgz), 1 half levels (mkmin = kmin+1, dz = dgzh, wp = Vtermh).
-  const double* dgz = grid + GF_DGZ * K;
-  const double* dgzh = grid + GF_DGZH * K;
+  const double* rdgz = grid + GF_RDGZ * K;
+  const double* rdgzh = grid + GF_RDGZH * K;
+  const double* rdzs = grid + GF_RDZS * K;
+  const double* rdzsh = grid + GF_RDZSH * K;
   for (int c = threadIdx.x; c < 6 * K * CELL_TG; c += blockDim.x) {
     const int s = c / (K * CELL_TG);
     const int rem = c - s * K * CELL_TG;
@@ -136,13 +138,13 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
     if (valid) {
       if (!half) {
         auto wp = [&](int j) { return col[j * CELL_TG]; };
-        z = vadv_zdis(wp, dgz, k, mkmin, kmax, P.dt, P.dt2, P.dt3);
+        z = vadv_zdis(wp, rdgz, rdzs, k, mkmin, kmax, P.dt, P.hdt2, P.sdt3);
       } else {
         // Vtermh, mod_precip_transport.cpp:847-861
         auto wp = [&](int j) {
           return (j >= kmin + 1 && j <= kmax - 1) ? 0.5 * (col[j * CELL_TG] + col[(j - 1) * CELL_TG]) : 0.0;
         };
-        z = vadv_zdis(wp, dgzh, k, mkmin, kmax, P.dt, P.dt2, P.dt3);
+        z = vadv_zdis(wp, rdgzh, rdzsh, k, mkmin, kmax, P.dt, P.hdt2, P.sdt3);
       }
       P.zdis[((size_t)l * 6 + s) * KG + (size_t)k * G + g] = z;
     }
@@ -181,7 +183,9 @@ struct ColumnShared {
 };
 
 // Departure cell of vadv1d_prep for one cell (mod_vadv1d.cpp:355-389).  The
-// sign tests of the reference's copysign products are exact comparisons.
+// reference's tmp = k2 * copysign(1, dep - zh(k2)) * copysign(1, zh(k2+1) - dep)
+// is k2 when both signs agree and -k2 otherwise; the sign of a difference of
+// two doubles is their comparison, so the test is exact integer logic.
 __device__ __forceinline__ int departure_cell(const double* zh, int k, double zdis, int bmn, int bmx, int mkmin,
                                               int mkmax) {
   int kc;
@@ -191,9 +195,9 @@ __device__ __forceinline__ int departure_cell(const double* zh, int k, double zd
     kc = 0;
     const double dep = zh[k] - zdis;
     for (int k2 = bmn; k2 <= bmx; ++k2) {
-      const double s1 = copysign(1.0, dep - zh[k2]);
-      const double s2 = copysign(1.0, zh[k2 + 1] - dep);
-      const int tmp = (int)((double)k2 * s1 * s2);
+      const bool s1 = dep >= zh[k2];
+      const bool s2 = zh[k2 + 1] >= dep;
+      const int tmp = (s1 == s2) ? k2 : -k2;
       kc = kc > tmp ? kc : tmp;
     }
   }
@@ -203,26 +207,24 @@ __device__ __forceinline__ int departure_cell(const double* zh, int k, double zd
 }
 
 // Flux integral of vadv1d_getflux_new for one cell (mod_vadv1d.cpp:410-449),
-// including its small-value filter.  As in the reference's Kokkos lambda
-// (size_t level index), the (k-1)-k2 and k2-k factors are evaluated unsigned
-// and never negative, so the weight is +dz(k2) above the departure cell and
-// -dz(k2) below it.
+// including its small-value filter |f| < EPS -> 0.  In the reference's Kokkos
+// lambda the level index is a size_t, so its (k-1)-k2 and k2-k factors are
+// evaluated unsigned and never negative; the weight of layer k2 is then
+// fact = dz(k2) * 0.25 * ((sign(k2-kc-1)+1) * 2 - 2 * (sign(kc-1-k2)+1)),
+// i.e. +dz(k2) above the departure cell, -dz(k2) below it and 0 at it, and
+// zdis = zdis0 - fact of the last layer k2 = bmx.
 template <int TG>
 __device__ __forceinline__ double flux_integral(const double* rhof_col, const double* dz, int k, int kc,
                                                 double zdis0, int bmn, int bmx) {
   double f = 0.0, zdis = zdis0;
   if (!(bmn == k && bmx == k)) {
     for (int k2 = bmn; k2 <= bmx; ++k2) {
-      const double f1 = (double)(k2 - (kc + 1));
-      const double f4 = (double)((kc - 1) - k2);
-      const double fact =
-          dz[k2] * 0.25 * ((copysign(1.0, f1) + 1.0) * 2.0 - 2.0 * (copysign(1.0, f4) + 1.0));
-      f = f + rhof_col[k2 * TG] * fact;
-      zdis = zdis0 - fact;
+      if (k2 != kc) f = __fma_rn(rhof_col[k2 * TG], k2 > kc ? dz[k2] : -dz[k2], f);
     }
+    if (bmx != kc) zdis = zdis0 - (bmx > kc ? dz[bmx] : -dz[bmx]);
   }
-  f = f + rhof_col[kc * TG] * zdis;
-  return f * (0.5 + copysign(0.5, fabs(f) - EPS));
+  f = __fma_rn(rhof_col[kc * TG], zdis, f);
+  return fabs(f) >= EPS ? f : 0.0;
 }
 
 template <int COL_TG, class M>
@@ -544,13 +546,15 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     double rq[6], q[6];
 #pragma unroll
     for (int n = 0; n < 6; ++n) rq[n] = P.rhogq[iq + (size_t)n * KG];
-    const double rrhog = 1.0 / rhog;
+    // These quotients keep the reference's exact divisions: the saturation
+    // adjustment forms qc = qsum - qsat from them, a difference of nearly
+    // equal numbers in which one unit in the last place of qsum is already a
+    // relative error of 1e-11 when qc is small.
 #pragma unroll
-    for (int n = 0; n < 6; ++n) q[n] = rq[n] * rrhog;
+    for (int n = 0; n < 6; ++n) q[n] = rq[n] / rhog;
     const double gsg = P.gsgam2[i];
-    const double rgsg = 1.0 / gsg;
-    double rho = rhog * rgsg;
-    const double ein = rhoge * rrhog;
+    double rho = rhog / gsg;
+    const double ein = rhoge / rhog;
     double qd = 1.0;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) qd = qd - q[n];
@@ -580,17 +584,16 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       double qd_l = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
-      const double rrhor = 1.0 / (rho_l * RVAP);
       double rtem = 1.0 / (dmax(tem, TEM_MIN));
       double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-      double qsat = psat * rrhor * rtem;
+      double qsat = psat / (rho_l * RVAP * tem);
       if (qsum - qsat > EPS) {
         bool converged = false;
         int ite;
         for (ite = 0; ite < P.itelim; ++ite) {
           rtem = 1.0 / (dmax(tem, TEM_MIN));
           psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-          qsat = psat * rrhor * rtem;
+          qsat = psat / (rho_l * RVAP * tem);
           q[I_QV] = qsat;
           q[I_QC] = qsum - qsat;
           double cv = qd_l * CVDRY;
@@ -635,10 +638,9 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       rq[I_QV] = dmax(rq[I_QV], 0.0);
       diffq -= rq[I_QV];
       rhog_o = rhog * (1.0 - diffq);
-      rho = rhog_o * rgsg;
-      const double rro = 1.0 / rhog_o;
+      rho = rhog_o / gsg;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n) q[n] = rq[n] * rro;
+      for (int n = 1; n <= 5; ++n) q[n] = rq[n] / rhog_o;
       double qdf = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];

@@ -25,6 +25,7 @@ from __future__ import annotations
 import argparse
 import concurrent.futures as cf
 import os
+import platform
 import re
 import shutil
 import subprocess
@@ -54,6 +55,9 @@ REF_UNITS = [
 VARIANT_FLAGS = {
     "strict": ["-O2", "-ffp-contract=off"],
     "omp": ["-O3", "-fopenmp", "-DNSW6_SHIM_OPENMP"],
+    # fused multiply-add contraction, as the reference's GPU (nvcc) and -Ofast
+    # builds compile it: measures the reference's own build-to-build spread
+    "fma": ["-O2", "-ffp-contract=fast"] + (["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []),
 }
 
 

@@ -13,6 +13,15 @@
 #include <stdlib.h>
 #include <string.h>
 
+/* Phase markers for the operation-counting build (oracle/opcount.cpp); empty
+ * otherwise.  Phase 1: negative filter, saturation values, process rates and
+ * cell updates (the GPU cell kernel); phase 2: transport, saturation
+ * adjustment and closing filter (the GPU column kernel); phase 3: the
+ * departure distances of vadv1d_prep (computed in the GPU cell kernel). */
+#ifndef NSW6O_PHASE
+#define NSW6O_PHASE(n)
+#endif
+
 #ifdef _OPENMP
 #include <omp.h>
 #define OMP_FOR _Pragma("omp parallel for schedule(static)")
@@ -819,6 +828,7 @@ static void vadv1d_prep(const dims_t* D, int mkmin, int mkmax, const double* dz,
                         const double* wp, double* zdis, int* kcell, int* kcell_max, int* kcell_min, double dt,
                         double* wh) {
   const int G = D->G, K = D->K;
+  NSW6O_PHASE(3);
   const double dt2 = pow(dt, 2);
   const double dt3 = pow(dt, 3);
   memset(wh, 0, sizeof(double) * D->N);
@@ -848,6 +858,7 @@ static void vadv1d_prep(const dims_t* D, int mkmin, int mkmax, const double* dz,
     zdis[IX(mkmax + 1, g)] = dt * wh[IX(mkmax + 1, g)] -
                              dt2 * wh[IX(mkmax + 1, g)] * (wh[IX(mkmax + 1, g)] - wh[IX(mkmax, g)]) / dz[mkmax] / 2.0;
   }
+  NSW6O_PHASE(2);
   for (int k = 0; k < K; ++k) {
     for (int g = 0; g < G; ++g) kcell[IX(k, g)] = k;
     kcell_min[k] = k;
@@ -997,6 +1008,7 @@ int nsw6o_mp_driver(int gall, int kall, const double* gz_in, const double* gzh_i
   for (int g = 0; g < G; ++g) precip_rhoe[g] = precip_lh_heat[g] = precip_rhophi[g] = precip_rhokin[g] = 0.0;
 
   /* ---- mp_nsw6_new::init, mod_mp_nsw6.cpp:439-518 */
+  NSW6O_PHASE(1);
   negative_filter(D, rhog, rhoge, rhogq, rho, tem, pre, q, gsgam2, qdw, cvw);
   for (size_t i = 0; i < N; ++i) Nc[i] = C.Nc_def;  /* TagAerosolF, :681-684 */
   psat_fn(D, &C, tem, psatl, C.CPovR_liq, C.LovR_liq);
@@ -1069,6 +1081,7 @@ int nsw6o_mp_driver(int gall, int kall, const double* gz_in, const double* gzh_i
   }
 
   /* ---- precip_transport_new, mod_precip_transport.cpp:573-1087 */
+  NSW6O_PHASE(2);
   {
     double *rhogkin = zalloc(N), *rhogkin_h = zalloc(N), *rhogkin_v = zalloc(N);
     double *rhoq = zalloc(N), *rhoeq = zalloc(N), *rhophiq = zalloc(N), *rhokin_h = zalloc(N);
@@ -1343,6 +1356,7 @@ int nsw6o_mp_driver(int gall, int kall, const double* gz_in, const double* gzh_i
 
   negative_filter(D, rhog, rhoge, rhogq, rho, tem, pre, q, gsgam2, qdw, cvw);
 
+  NSW6O_PHASE(0);
   /* ---- mp_driver epilogue, mod_mp_driver.cpp:555-612 (MP_DIV_NUM = 1) */
   for (size_t i = 0; i < N; ++i) re_solid[i] = 20.0E-6;
   const double fraction_mp = 1.0 / (double)1;

@@ -32,6 +32,8 @@ VARIANTS = {
 }
 
 PARAM_NAMES = ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg", "ice_nuc", "kk_aut"]
+OP_NAMES = ["add", "mul", "div", "sqrt", "exp", "log", "pow", "cmp"]
+PHASES = ["setup", "cell", "column", "zdis"]
 
 
 class Params(ctypes.Structure):
@@ -52,6 +54,40 @@ def build(variant: str = "strict", force: bool = False) -> Path:
            *VARIANTS[variant], str(HERE / "nsw6_oracle.c"), "-o", str(so), "-lm"]
     subprocess.run(cmd, check=True)
     return so
+
+
+def build_opcount(force: bool = False) -> Path:
+    """Operation-counting build (oracle/opcount.cpp)."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    so = BUILD / "libnsw6_opcount.so"
+    src = [HERE / "opcount.cpp", HERE / "nsw6_oracle.c", HERE / "nsw6_oracle.h"]
+    if so.exists() and not force and all(so.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return so
+    subprocess.run(["g++", "-std=c++17", "-O1", "-fPIC", "-shared", "-w", f"-I{HERE}", str(HERE / "opcount.cpp"),
+                    "-o", str(so)], check=True)
+    return so
+
+
+def count_ops(reg: dict[str, np.ndarray], gz: np.ndarray, gzh: np.ndarray, dt: float) -> dict:
+    """Per-phase counts of the reference algorithm's FP64 operations for one
+    step on one region (the arrays are updated in place)."""
+    lib = ctypes.CDLL(str(build_opcount()), mode=os.RTLD_LOCAL)
+    dp = ctypes.POINTER(ctypes.c_double)
+    lib.nsw6o_count_ops.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, ctypes.POINTER(ctypes.c_void_p),
+                                    ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
+    kall, gall = reg["rhog"].shape
+    p = np.array([default_params()[n] for n in PARAM_NAMES])
+    ptrs = (ctypes.c_void_p * len(MP_DRIVER_ARGS))()
+    for i, (name, _, _) in enumerate(MP_DRIVER_ARGS):
+        ptrs[i] = reg[name].ctypes.data
+    out = (ctypes.c_longlong * (4 * 8))()
+    gz = np.ascontiguousarray(gz, dtype=np.float64)
+    gzh = np.ascontiguousarray(gzh, dtype=np.float64)
+    rc = lib.nsw6o_count_ops(gall, kall, gz.ctypes.data_as(dp), gzh.ctypes.data_as(dp), p.ctypes.data_as(dp), ptrs,
+                             float(dt), out)
+    res = {ph: {op: int(out[i * 8 + j]) for j, op in enumerate(OP_NAMES)} for i, ph in enumerate(PHASES)}
+    res["rc"] = rc
+    return res
 
 
 _LIBS: dict[str, ctypes.CDLL] = {}
