@@ -31,6 +31,18 @@
 
 namespace nsw6 {
 
+// a / b rounded to nearest, given rb = 1 / b rounded to nearest: one product
+// and Markstein's correction step (r = a - q b is exact in an FMA, and q + r rb
+// rounds to the correctly rounded quotient).  Three FP64 instructions where a
+// division costs several times more; used where the reference divides by a
+// value the cell reuses, so that near-total consumption of a species leaves
+// the same residue as in the reference.
+__device__ __forceinline__ double div_rn(double a, double b, double rb) {
+  const double q = a * rb;
+  const double r = __fma_rn(-q, b, a);
+  return __fma_rn(r, rb, q);
+}
+
 struct CellIn {
   double rhog, tem, gsgam2, q0;
   double rhogq[6];
@@ -69,7 +81,7 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
   double qn[6];
   qn[0] = in.q0;
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) qn[n] = rq[n] * rrhog;
+  for (int n = 1; n <= 5; ++n) qn[n] = div_rn(rq[n], rhog, rrhog);
   double qd = 1.0;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) qd = qd - qn[n];
@@ -101,8 +113,8 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
   const double delta1 = (qr >= 1.0E-4) ? 1.0 : 0.0;
   const double delta2 = (1.0E-4 >= qr && 1.0E-4 >= qs) ? 1.0 : 0.0;
   const double spsati = (Sice >= 1.0) ? 1.0 : 0.0;
-  const double dqv_dt = qv * rdt, dqc_dt = qc * rdt, dqr_dt = qr * rdt;
-  const double dqi_dt = qi * rdt, dqs_dt = qs * rdt, dqg_dt = qg * rdt;
+  const double dqv_dt = div_rn(qv, dt, rdt), dqc_dt = div_rn(qc, dt, rdt), dqr_dt = div_rn(qr, dt, rdt);
+  const double dqi_dt = div_rn(qi, dt, rdt), dqs_dt = div_rn(qs, dt, rdt), dqg_dt = div_rn(qg, dt, rdt);
 
   // rain slope parameter, :953-967
   const double RLMDr = (qr >= 1.0E-12) ? sqrt(sqrt(dens * qr * C.K_rlmdr)) : 0.0;
@@ -285,14 +297,13 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
   qs_t = dmax(qs_t, -dqs_dt);
   qg_t = dmax(qg_t, -dqg_dt);
   const double qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
-  const double rdt_g = rhog * dt;
   double drq[6];
-  drq[0] = qv_t * rdt_g;
-  drq[1] = qc_t * rdt_g;
-  drq[2] = qr_t * rdt_g;
-  drq[3] = qi_t * rdt_g;
-  drq[4] = qs_t * rdt_g;
-  drq[5] = qg_t * rdt_g;
+  drq[0] = rhog * qv_t * dt;
+  drq[1] = rhog * qc_t * dt;
+  drq[2] = rhog * qr_t * dt;
+  drq[3] = rhog * qi_t * dt;
+  drq[4] = rhog * qs_t * dt;
+  drq[5] = rhog * qg_t * dt;
   o.Vtr = Vtr;
   o.Vts = Vts;
   o.Vtg = Vtg;
@@ -320,7 +331,7 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
   rhoge = rhoge - LHV0 * drq[I_QV] + LHF0 * drq[I_QI] + LHF0 * drq[I_QS] + LHF0 * drq[I_QG];
   o.q[0] = qn[0];
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) o.q[n] = rq[n] * rrhog;
+  for (int n = 1; n <= 5; ++n) o.q[n] = div_rn(rq[n], rhog, rrhog);
   double qd2 = 1.0;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) qd2 = qd2 - o.q[n];

@@ -205,10 +205,17 @@ Consts make_consts(const nsw6_params& p) {
 }
 
 // Fast-math tables (nsw6_fastmath.cuh), computed in extended precision:
-// [0,256) 2^(j/256); [256,512) 1/c_j; [512,768) -log(1/c_j), where c_j is the
-// centre of the j-th of 256 mantissa intervals of [0.75, 1.5).
+// [0,256) 2^(j/256) rounded; [256,512) its relative rounding error;
+// [512,768) 1/c_j; [768,1024) -log(1/c_j), where c_j is the centre of the j-th
+// of 256 mantissa intervals of [0.75, 1.5).
 void build_fastmath_tables(double* t) {
-  for (int j = 0; j < FM_EXP_N; ++j) t[j] = (double)exp2l((long double)j / 256.0L);
+  for (int j = 0; j < FM_EXP_N; ++j) {
+    const long double v = exp2l((long double)j / 256.0L);
+    t[j] = (double)v;
+    t[FM_EXP_N + j] = (double)(v / (long double)t[j] - 1.0L);
+  }
+  double* ic_t = t + 2 * FM_EXP_N;
+  double* lc_t = ic_t + FM_LOG_N;
   for (int j = 0; j < FM_LOG_N; ++j) {
     unsigned long long lo_bits = 0x3FE8000000000000ull + ((unsigned long long)j << 44);
     unsigned long long hi_bits = lo_bits + (1ull << 44);
@@ -217,8 +224,8 @@ void build_fastmath_tables(double* t) {
     std::memcpy(&mhi, &hi_bits, 8);
     const long double cj = 0.5L * ((long double)mlo + (long double)mhi);
     const double ic = (double)(1.0L / cj);
-    t[FM_EXP_N + j] = ic;
-    t[FM_EXP_N + FM_LOG_N + j] = (double)(-logl((long double)ic));
+    ic_t[j] = ic;
+    lc_t[j] = (double)(-logl((long double)ic));
   }
 }
 

@@ -9,18 +9,19 @@
 //
 //   exp(x) = 2^m * 2^(j/256) * exp(r),  x = (256 m + j) ln2/256 + r,
 //            |r| <= ln2/512, exp(r) - 1 by its degree-4 Taylor polynomial
-//            (truncation error < 4e-17), 2^(j/256) from a 256-entry table;
+//            (truncation error < 4e-17), 2^(j/256) = T_j (1 + d_j) from two
+//            256-entry tables (T_j rounded, d_j its relative rounding error);
 //   log(x) = e ln2 + log(c_j) + log1p(r),  x = 2^e m, m in [0.75, 1.5),
 //            r = m / c_j - 1 with |r| < 2e-3, log1p(r) by its degree-6
 //            Taylor polynomial, 1/c_j and -log(1/c_j) from 256-entry tables.
 //
-// Both are accurate to about one unit in the last place; arguments outside
+// Both are accurate to about half a unit in the last place; arguments outside
 // the fast range (non-normal, huge, negative log arguments) fall back to the
 // CUDA math library.  pow(x, y) = exp(y log x) carries the rounding error of
 // y*log(x) (computed with a fused multiply-add) into exp through exp(h + l) =
 // exp(h)(1 + l), which keeps it within a few units in the last place.
 //
-// The tables (6 KB) are built on the host in extended precision and staged
+// The tables (8 KB) are built on the host in extended precision and staged
 // in shared memory by every CTA.
 #pragma once
 
@@ -30,14 +31,15 @@ namespace nsw6 {
 
 constexpr int FM_EXP_N = 256;
 constexpr int FM_LOG_N = 256;
-constexpr int FM_TABLE_DOUBLES = FM_EXP_N + 2 * FM_LOG_N;
+constexpr int FM_TABLE_DOUBLES = 2 * FM_EXP_N + 2 * FM_LOG_N;
 
 struct FastMath {
-  const double* exp_t;    // [256]: 2^(j/256)
+  const double* exp_t;    // [256]: 2^(j/256) rounded
+  const double* exp_d;    // [256]: 2^(j/256) / exp_t[j] - 1
   const double* log_ic;   // [256]: 1 / c_j (rounded)
   const double* log_c;    // [256]: -log(log_ic[j])
 
-  // exp with |relative error| ~ 1 ulp; slow path outside [-708, 709].
+  // exp within about half an ulp; slow path outside (-708, 708).
   __device__ __forceinline__ double exp(double x) const {
     if (!(fabs(x) < 708.0)) return ::exp(x);
     const double shift = 6755399441055744.0;               // 1.5 * 2^52
@@ -55,7 +57,7 @@ struct FastMath {
     double p = __fma_rn(r, 4.1666666666666664e-02, 1.6666666666666666e-01);
     p = __fma_rn(p, r, 0.5);
     p = __fma_rn(p, r, 1.0);
-    p = __dmul_rn(p, r);
+    p = __fma_rn(p, r, exp_d[j]);   // exp(r) (1 + d_j) - 1, dropping d_j (exp(r) - 1) < 2e-19
     const long long tb = __double_as_longlong(exp_t[j]) + ((long long)m << 52);
     const double s = __longlong_as_double(tb);
     return __fma_rn(s, p, s);
@@ -113,18 +115,11 @@ struct FastMath {
     return __fma_rn(q, __dmul_rn(r, r), r);
   }
 
-  // log(x) to about one ulp (the low-order correction of log_hl is dropped).
+  // log(x) = hi + lo of log_hl, rounded once: within about half an ulp.
   __device__ __forceinline__ double log(double x) const {
-    const long long bits = __double_as_longlong(x);
-    if (!(x >= 2.2250738585072014e-308 && x < 1.7976931348623157e308)) return ::log(x);
-    if (fabs(x - 1.0) < NEAR1) return log1p_near1(x - 1.0);
-    const long long u = bits - 0x3FE8000000000000ll;
-    const long long e = u >> 52;
-    const int j = (int)((u >> 44) & (FM_LOG_N - 1));
-    const double m = __longlong_as_double(bits - (e << 52));
-    const double r = __fma_rn(m, log_ic[j], -1.0);
-    const double a = __fma_rn((double)e, 0.6931471805599453, log_c[j]);
-    return __dadd_rn(a, log1p_poly(r));
+    double lo;
+    const double hi = log_hl(x, lo);
+    return __dadd_rn(hi, lo);
   }
 
   // x^y for x >= 0 (the only use here); x == 0 gives 0 for y > 0.

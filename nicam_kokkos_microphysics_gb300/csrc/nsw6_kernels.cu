@@ -47,7 +47,7 @@ template <class M>
 __device__ __forceinline__ M make_math(const double* tab);
 template <>
 __device__ __forceinline__ FastMath make_math<FastMath>(const double* tab) {
-  return FastMath{tab, tab + FM_EXP_N, tab + FM_EXP_N + FM_LOG_N};
+  return FastMath{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
 }
 template <>
 __device__ __forceinline__ LibMath make_math<LibMath>(const double*) {
