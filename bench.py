@@ -49,7 +49,12 @@ ALGO_BYTES_PER_CELL = 49 * 8 + 3
 CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
 # DRAM bytes (read + write) per interior cell of the cell kernel, from the ncu
 # capture of one 16900 x 42 region (profiles/nsw6_cell_kernel_16900x42.md).
-CELL_KERNEL_TRAFFIC_PER_CELL = 170.5
+CELL_KERNEL_TRAFFIC_PER_CELL = 170.0
+# FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
+# divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
+# the throughput probe (csrc/nsw6_probe.cu) and frozen here.
+OP_WEIGHTS = {"add": 1.0, "mul": 1.0, "cmp": 1.0, "div": 15.0, "sqrt": 15.2, "exp": 30.0, "log": 58.4,
+              "pow": 173.8}
 
 
 def env_rank():
@@ -341,7 +346,7 @@ def main(argv=None) -> int:
                 "hbm": {"achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                         "frac": hbm_gbs / peaks["hbm_gbs"], "peak_source": f"{src} copy bandwidth"}}
     if rates:
-        aw = algorithmic_work(spec, st0, rates["weights"])
+        aw = algorithmic_work(spec, st0, OP_WEIGHTS)
         flops = aw["cell_per_interior_cell"] * n_int
         achieved = flops / (cell_ms * 1e-3) / 1e12
         col_flops = aw["column_per_cell"] * spec.cells
@@ -351,8 +356,9 @@ def main(argv=None) -> int:
             "peak_source": "measured in this run: FP64 FMA throughput probe (MEASURED_PEAKS.json has no FP64 peak)",
             "work_per_interior_cell": aw["cell_per_interior_cell"],
             "work_definition": "reference operations counted on this state (integer powers as products), "
-                               "weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by measured cost",
-            "op_weights": rates["weights"],
+                               "weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by their frozen measured cost",
+            "op_weights": OP_WEIGHTS,
+            "op_weights_this_run": rates["weights"],
             "column_kernel": {"achieved": col_flops / (col_ms * 1e-3) / 1e12,
                               "frac": col_flops / (col_ms * 1e-3) / 1e12 / rates["peak_tflops"],
                               "work_per_cell": aw["column_per_cell"]},
