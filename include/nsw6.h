@@ -36,7 +36,8 @@ typedef enum nsw6_status {
   NSW6_ERR_CUDA = 2,         /* a CUDA runtime call failed                           */
   NSW6_ERR_NOCONV = 3,       /* satadjust Newton hit the iteration limit             */
   NSW6_ERR_NAN = 4,          /* satadjust produced a non-finite temperature          */
-  NSW6_ERR_UNSUPPORTED = 5   /* configuration not implemented                        */
+  NSW6_ERR_UNSUPPORTED = 5,  /* configuration not implemented                        */
+  NSW6_ERR_TOO_LARGE = 6     /* region larger than mp_driver_noalloc's fixed scratch */
 } nsw6_status;
 
 /* Tunable NSW6 scheme parameters (GlobalParams, src/mod_mp_nsw6.h:16-123,
@@ -165,6 +166,48 @@ int mp_driver_batched(nsw6_handle* h, int lall,
  * inputs to device workspace, runs the step and copies the outputs back
  * (synchronous).  This is the entry point a ctypes/cffi/FFI binding uses. */
 int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int host);
+
+/* ---------------------------------------------------------------------------
+ * mp_driver_noalloc: one NSW6 step on one region that allocates nothing.
+ *
+ * No counterpart in the reference (its mp_driver allocates some 45 temporary
+ * Views on every call, src/mod_mp_driver.cpp:394-418).  It is for callers that
+ * must not call cudaMalloc / cudaFree, or any routine that allocates device
+ * memory, inside their time loop: cudaMalloc and cudaFree synchronise the
+ * whole device and stall every other stream, and in a process where another
+ * allocator (a framework's caching allocator, a fixed memory pool) already
+ * holds the device memory a fresh cudaMalloc can fail mid-run.  Such a caller
+ * cannot create an nsw6_handle, which allocates its workspace.
+ *
+ * The workspace is a fixed file-scope device array inside the library (about
+ * 100 MB, present on every device the library is loaded on).  Limits: kall in
+ * [5, 160] and gall * kall <= NSW6_NOALLOC_MAX_CELLS; larger regions return
+ * NSW6_ERR_TOO_LARGE before anything is issued.
+ *
+ * gz, gzh: HOST arrays of kall heights (the contents of GRD_gz.dat /
+ * GRD_gzh.dat).  params: NULL for the defaults.  args: the 50 arrays of one
+ * region in the reference order (args[0] = rhog ... args[49] = CBMFX), CUDA
+ * device pointers, per-region layout as for mp_driver.  stream: a
+ * cudaStream_t (NULL = the default stream).  The call issues its work on
+ * `stream`, then synchronises it and returns the step's status
+ * (NSW6_ERR_NOCONV / NSW6_ERR_NAN as mp_driver).
+ *
+ * Set-up: the first call on each device looks up the scratch array's device
+ * address (cudaGetSymbolAddress, which may load the library's device code);
+ * make that first call before any stream capture begins.
+ *
+ * Zero state: nothing has to be zero before a call.  Each call writes the grid
+ * metrics and fast-math tables into the scratch, resets the status word to 0
+ * and the departure-distance extrema keys to 0 / all ones, and every
+ * departure distance the step reads is written by the same call first.
+ *
+ * Concurrency: all calls in the process share one scratch array per device.
+ * Calls that overlap in time (from several host threads, or on several streams
+ * of one device without ordering between them) race on it and give wrong
+ * results; serialise them. */
+#define NSW6_NOALLOC_MAX_CELLS 2097152
+int mp_driver_noalloc(int gall, int kall, const double* gz, const double* gzh, const nsw6_params* params,
+                      double* const* args, double dt, double ct, void* stream);
 
 #ifdef __cplusplus
 }

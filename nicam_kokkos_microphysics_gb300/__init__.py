@@ -28,7 +28,7 @@ import numpy as np
 from . import _native
 from .state import ARG_NAMES, MP_DRIVER_ARGS, batched_shape, region_shape
 
-__all__ = ["MPDriver", "mp_init", "NSW6Error", "PARAM_NAMES", "default_params"]
+__all__ = ["MPDriver", "mp_init", "mp_driver_noalloc", "NSW6Error", "PARAM_NAMES", "default_params"]
 
 PARAM_NAMES = ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg", "ice_nuc", "kk_aut"]
 
@@ -229,3 +229,36 @@ def mp_init(MP_TYPE: str, gall: int, kall: int, gz, gzh, lall_max: int = 1, para
     if MP_TYPE != "NSW6":
         raise ValueError(f"mp_init: NOT appropriate type. Type: {MP_TYPE}")
     return MPDriver(gall, kall, gz, gzh, lall_max=lall_max, params=params)
+
+
+def mp_driver_noalloc(gall: int, kall: int, gz, gzh, *args, dt: float | None = None, ct: float = 0.0,
+                      params: dict | None = None) -> None:
+    """One NSW6 step on one region through ``mp_driver_noalloc`` of the C ABI,
+    which allocates no device memory (its workspace is a fixed array inside the
+    library; regions up to 2,097,152 cells and kall <= 160).  Arguments as
+    ``MPDriver.mp_driver`` without the region index; runs on torch's current
+    stream and returns after the step has finished."""
+    import torch
+    lib = _native.load()
+    arrays, dt, ct = _split_args(args, dt, ct)
+    shapes = [region_shape(kind, kall, gall) for _, kind, _ in MP_DRIVER_ARGS]
+    ptrs = (ctypes.c_void_p * len(ARG_NAMES))()
+    for i, ((name, _, _), a, shp) in enumerate(zip(MP_DRIVER_ARGS, arrays, shapes)):
+        if not isinstance(a, torch.Tensor) or a.device.type != "cuda" or a.dtype != torch.float64 \
+                or not a.is_contiguous() or tuple(a.shape) != tuple(shp):
+            raise ValueError(f"{name}: expected a contiguous float64 CUDA tensor of shape {tuple(shp)}")
+        ptrs[i] = a.data_ptr()
+    gz = np.ascontiguousarray(gz, dtype=np.float64)
+    gzh = np.ascontiguousarray(gzh, dtype=np.float64)
+    if gz.shape != (kall,) or gzh.shape != (kall,):
+        raise ValueError("gz and gzh must hold kall heights")
+    p = None
+    if params is not None:
+        p = _Params()
+        lib.nsw6_default_params(ctypes.byref(p))
+        for k, v in params.items():
+            setattr(p, k, float(v))
+    rc = lib.mp_driver_noalloc(int(gall), int(kall), gz.ctypes.data, gzh.ctypes.data,
+                               ctypes.addressof(p) if p is not None else None, ptrs, float(dt), float(ct),
+                               torch.cuda.current_stream().cuda_stream)
+    _check(rc, lib)

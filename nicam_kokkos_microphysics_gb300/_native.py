@@ -106,6 +106,7 @@ def load() -> ctypes.CDLL:
     lib.mp_driver_argv.argtypes = [vp, c_int, ctypes.POINTER(vp), c_double, c_double, c_int]
     lib.mp_driver.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.mp_driver_batched.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
+    lib.mp_driver_noalloc.argtypes = [c_int, c_int, vp, vp, vp, ctypes.POINTER(vp), c_double, c_double, vp]
     _lib = lib
     return lib
 

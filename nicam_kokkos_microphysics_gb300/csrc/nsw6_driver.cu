@@ -587,6 +587,8 @@ const char* nsw6_strerror(int status) {
     case NSW6_ERR_NOCONV: return "saturation adjustment did not converge";
     case NSW6_ERR_NAN: return "saturation adjustment produced a non-finite temperature";
     case NSW6_ERR_UNSUPPORTED: return "unsupported configuration";
+    case NSW6_ERR_TOO_LARGE:
+      return "region too large for mp_driver_noalloc (needs 5 <= kall <= 160 and gall * kall <= 2097152)";
     default: return "unknown status";
   }
 }
@@ -679,3 +681,88 @@ int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, dou
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------- mp_driver_noalloc
+// Fixed scratch of mp_driver_noalloc, in doubles; every slot starts on a
+// 256-byte boundary.  The departure distances take 6 doubles per cell.
+namespace {
+constexpr size_t NA_STATUS = 0;                                   // DevStatus (256 B slot)
+constexpr size_t NA_ZMAX = NA_STATUS + 32;                        // [6][MAX_KALL] uint64 keys
+constexpr size_t NA_ZMIN = NA_ZMAX + 6 * MAX_KALL;                // [6][MAX_KALL] uint64 keys
+constexpr size_t NA_GRID = NA_ZMIN + 6 * MAX_KALL;                // [GF_COUNT][MAX_KALL]
+constexpr size_t NA_FMTAB = NA_GRID + (size_t)GF_COUNT * MAX_KALL; // [FM_TABLE_DOUBLES]
+constexpr size_t NA_ZDIS = ((NA_FMTAB + FM_TABLE_DOUBLES + 31) / 32) * 32;  // [6][kall][gall]
+constexpr size_t NA_TOTAL = NA_ZDIS + 6 * (size_t)NSW6_NOALLOC_MAX_CELLS;
+static_assert(NA_ZMAX % 32 == 0 && NA_ZMIN % 32 == 0 && NA_GRID % 32 == 0 && NA_FMTAB % 32 == 0,
+              "scratch slots must stay 256-byte aligned");
+static_assert(sizeof(DevStatus) <= 32 * sizeof(double), "status slot too small");
+
+static __device__ __align__(256) double g_noalloc_scratch[NA_TOTAL];
+
+constexpr int NA_MAX_DEVICES = 64;
+double* g_noalloc_ptr[NA_MAX_DEVICES] = {};
+
+// Device address of the scratch on the current device, looked up once.
+int noalloc_scratch(double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (dev < 0 || dev >= NA_MAX_DEVICES) return NSW6_ERR_UNSUPPORTED;
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return NSW6_ERR_CUDA;
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return NSW6_OK;
+}
+}  // namespace
+
+extern "C" int mp_driver_noalloc(int gall, int kall, const double* gz, const double* gzh,
+                                 const nsw6_params* params, double* const* args, double dt, double ct,
+                                 void* stream) {
+  (void)ct;
+  if (!gz || !gzh || !args) return NSW6_ERR_BAD_ARG;
+  if (gall < 1 || kall < 5) return NSW6_ERR_BAD_ARG;
+  if (kall > MAX_KALL || (long long)gall * kall > NSW6_NOALLOC_MAX_CELLS) return NSW6_ERR_TOO_LARGE;
+  double* base = nullptr;
+  int rc = noalloc_scratch(&base);
+  if (rc != NSW6_OK) return rc;
+
+  // A handle on the stack whose workspace pointers are slots of the scratch.
+  nsw6_handle h;
+  h.gall = gall;
+  h.kall = kall;
+  h.lall_max = 1;
+  if (params) h.params = *params;
+  else nsw6_default_params(&h.params);
+  h.C = make_consts(h.params);
+  h.d_grid = base + NA_GRID;
+  h.d_fmtab = base + NA_FMTAB;
+  h.d_zdis = base + NA_ZDIS;
+  h.d_zmax = reinterpret_cast<unsigned long long*>(base + NA_ZMAX);
+  h.d_zmin = reinterpret_cast<unsigned long long*>(base + NA_ZMIN);
+  h.d_status = reinterpret_cast<DevStatus*>(base + NA_STATUS);
+  h.stream = static_cast<cudaStream_t>(stream);
+
+  Problem P;
+  rc = fill_problem(&h, 1, args, dt, P);
+  if (rc != NSW6_OK) return rc;
+
+  // Grid metrics and fast-math tables, computed on the host stack and copied
+  // into the scratch (pageable source: the copy has consumed it on return).
+  double hbuf[GF_COUNT * MAX_KALL + FM_TABLE_DOUBLES];
+  make_grid(kall, gz, gzh, hbuf);
+  build_fastmath_tables(hbuf + GF_COUNT * MAX_KALL);
+  if (cudaMemcpyAsync(h.d_grid, hbuf, sizeof(double) * GF_COUNT * (size_t)kall, cudaMemcpyHostToDevice,
+                      h.stream) != cudaSuccess ||
+      cudaMemcpyAsync(h.d_fmtab, hbuf + GF_COUNT * MAX_KALL, sizeof(double) * FM_TABLE_DOUBLES,
+                      cudaMemcpyHostToDevice, h.stream) != cudaSuccess ||
+      cudaMemsetAsync(h.d_status, 0, sizeof(DevStatus), h.stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  if (launch_step(P, h.C, h.stream, nullptr) != cudaSuccess) return NSW6_ERR_CUDA;
+  DevStatus st;
+  if (cudaMemcpyAsync(&st, h.d_status, sizeof(st), cudaMemcpyDeviceToHost, h.stream) != cudaSuccess ||
+      cudaStreamSynchronize(h.stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  return st.code;
+}
