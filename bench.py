@@ -38,6 +38,7 @@ from nicam_kokkos_microphysics_gb300.state import (ARG_NAMES, MP_DRIVER_ARGS, St
                                                    make_state, region_view)
 
 METRIC = "cells/sec per NSW6 step (FP64)"
+METRIC_MIXED = "cells/sec per NSW6 step (mixed precision)"
 UNIT = "cells/s"
 # Algorithmic bytes of one step per cell: 21 FP64 fields read and 28 written
 # (the minimum the step must touch, without read-for-ownership) plus ~3 B of
@@ -50,6 +51,9 @@ CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
 # DRAM bytes (read + write) per interior cell of the cell kernel, from the ncu
 # capture of one 16900 x 42 region (profiles/nsw6_cell_kernel_16900x42.md).
 CELL_KERNEL_TRAFFIC_PER_CELL = 170.0
+# DRAM bytes (read + write) per cell of the column kernel, same capture
+# (profiles/nsw6_column_kernel_16900x42.md).
+COLUMN_KERNEL_TRAFFIC_PER_CELL = 381.0
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (csrc/nsw6_probe.cu) and frozen here.
@@ -222,6 +226,132 @@ def run_reference_arm(args):
     return 0
 
 
+# Fields whose error the mixed path reports, and the reduction that gives it:
+# per field, max |mixed - fp64| / max |fp64| (field-normalised maximum) and
+# the mean over cells with |fp64| >= 1e-3 max |fp64| of the per-cell relative
+# error; tracers per species.
+MIXED_FIELDS = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "q", "tem", "precip",
+                "precip_rhoe", "precip_lh_heat", "GPREC"]
+SPECIES = ["QV", "QC", "QR", "QI", "QS", "QG"]
+
+
+def field_errors(a, b) -> dict:
+    import torch
+    d = (a - b).abs()
+    bmax = b.abs().max()
+    sig = b.abs() >= 1e-3 * bmax
+    rel = d[sig] / b.abs()[sig]
+    return {"max_rel_field": float(d.max() / bmax) if bmax > 0 else 0.0,
+            "mean_rel": float(rel.mean()) if rel.numel() else 0.0,
+            "max_rel_cell": float(rel.max()) if rel.numel() else 0.0}
+
+
+def mixed_vs_fp64(drv, spec: StateSpec, st0: dict) -> dict:
+    """One step of the FP64 path and one of the mixed path from the same state."""
+    import torch
+    ref = {n: torch.from_numpy(st0[n]).cuda() for n in ARG_NAMES}
+    mix = {n: t.clone() for n, t in ref.items()}
+    drv.set_precision("fp64")
+    drv.mp_driver_batched(spec.lall, *[ref[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.set_precision("mixed")
+    drv.mp_driver_batched(spec.lall, *[mix[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    torch.cuda.synchronize()
+    out = {}
+    for n in MIXED_FIELDS:
+        a, b = mix[n], ref[n]
+        if n in ("rhogq", "q"):
+            for s, sp in enumerate(SPECIES):
+                out[f"{n}[{sp}]"] = field_errors(a[:, s], b[:, s])
+        else:
+            out[n] = field_errors(a, b)
+    return out
+
+
+def run_adjoint_bench(args) -> int:
+    """Adjoint / forward time of one step (mp_driver_adjoint around the state,
+    seeded with the loss sum (precip)^2 + column QC), or, with --window N, of
+    the window gradient of the accumulated surface precipitation (forward in
+    --precision, per-step checkpoints, FP64 adjoint)."""
+    import torch
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    from nicam_kokkos_microphysics_gb300.window import window_forward, window_gradient
+    gall = args.gall if args.gall != 16900 or args.window else 4096
+    lall = args.lall if args.window else 1
+    spec = StateSpec(gall=gall, kall=args.kall, lall=lall, seed=args.seed, variant=args.variant)
+    st = make_state(spec, out_fill=0.0)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    x0 = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
+    sampler = ClockSampler(0)
+    line = {"n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded NICAM-like state)", "unit": "ratio", "gpu_launches": None}
+    if args.window:
+        for _ in range(max(1, args.warmup // 3)):
+            window_gradient(drv, spec.lall, x0, 2, spec.dt, precision=args.precision)
+        torch.cuda.reset_peak_memory_stats()
+        sampler.start()
+        res = window_gradient(drv, spec.lall, x0, args.window, spec.dt, precision=args.precision)
+        clocks = sampler.stop()
+        # forward alone, without checkpoints, for the ratio
+        xs = {n: t.clone() for n, t in x0.items()}
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        window_forward(drv, spec.lall, xs, args.window, spec.dt, args.precision)
+        torch.cuda.synchronize()
+        t_plain = time.perf_counter() - t0
+        line.update({
+            "metric": "adjoint/forward time ratio, window gradient of accumulated surface precipitation",
+            "value": res["t_adjoint"] / t_plain, "steps": args.window, "warmup": args.warmup,
+            "ms_per_step": res["t_adjoint"] * 1e3 / args.window,
+            "config": {"workload": f"{args.window}-step window, gall={spec.gall} kall={spec.kall} lall={spec.lall}, "
+                                   f"dt={spec.dt}, forward {args.precision}, FP64 adjoint, per-step checkpoints",
+                       "variant": spec.variant},
+            "forward_ms": t_plain * 1e3, "forward_with_checkpoints_ms": res["t_forward"] * 1e3,
+            "adjoint_ms": res["t_adjoint"] * 1e3, "peak_device_bytes": res["peak_bytes"],
+            "J": res["J"], "dJ_dparams": res["dparams"].tolist(), "clocks": clocks,
+            "gpu_launches": args.window * 2 + args.window * 3,
+        })
+    else:
+        dev = {n: t.clone() for n, t in x0.items()}
+        kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
+        for _ in range(args.warmup):
+            y = {n: t.clone() for n, t in x0.items()}
+            drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        y = {n: t.clone() for n, t in x0.items()}
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(args.steps):
+            drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        e1.record()
+        torch.cuda.synchronize()
+        t_fwd = e0.elapsed_time(e1) / args.steps
+        bar = {n: torch.zeros(batched_shape(kinds[n], spec.lall, spec.kall, spec.gall), dtype=torch.float64,
+                              device="cuda") for n in ARG_NAMES}
+        drv.adjoint(spec.lall, dev, {n: b.clone() for n, b in bar.items()}, dt=spec.dt)   # warm-up, tape sizing
+        torch.cuda.reset_peak_memory_stats()
+        sampler.start()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            b = {n: t.clone() for n, t in bar.items()}
+            b["precip"].fill_(1.0)
+            b["rhogq"][:, 1] = 1.0
+            drv.adjoint(spec.lall, dev, b, dt=spec.dt)
+        torch.cuda.synchronize()
+        t_adj = (time.perf_counter() - t0) / args.steps * 1e3
+        clocks = sampler.stop()
+        line.update({
+            "metric": "adjoint/forward time ratio of one NSW6 step", "value": t_adj / t_fwd, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_adj,
+            "config": {"workload": f"adjoint of one FP64 step, gall={spec.gall} kall={spec.kall} lall={spec.lall}, "
+                                   f"dt={spec.dt}", "variant": spec.variant},
+            "forward_ms": t_fwd, "adjoint_ms": t_adj, "clocks": clocks, "gpu_launches": 4 * args.steps,
+        })
+    print(json.dumps(line), flush=True)
+    drv.close()
+    return 0
+
+
 # ----------------------------------------------------------------- GPU side
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description="NSW6 step benchmark")
@@ -236,7 +366,15 @@ def main(argv=None) -> int:
     ap.add_argument("--seed", type=int, default=1002)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="plain FP64 step, or FP32 process rates with FP64 budgets, flux sums and Newton")
+    ap.add_argument("--adjoint", action="store_true",
+                    help="time the adjoint step against the forward step (default workload 4096 x 42, one region)")
+    ap.add_argument("--window", type=int, default=0,
+                    help="with --adjoint: gradient over a window of this many steps with per-step checkpoints")
     args = ap.parse_args(argv)
+    if args.adjoint:
+        return run_adjoint_bench(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -257,6 +395,7 @@ def main(argv=None) -> int:
     st = make_state(spec, out_fill=0.0)
     st0 = {k: v.copy() for k, v in st.items()}
     drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    drv.set_precision(args.precision)
     dev = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
     args_dev = [dev[n] for n in ARG_NAMES]
     drv.set_sync_check(False)
@@ -335,37 +474,49 @@ def main(argv=None) -> int:
         e2e = {"value": cells_rank * world / dt_e2e, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": dt_e2e * 1e3}
 
-    # ---- roofline of the dominant kernel (the cell kernel: FP64-pipe bound)
+    # ---- mixed precision: error of one step against the FP64 path on the same state
+    mixed_error = None
+    if args.precision == "mixed":
+        mixed_error = mixed_vs_fp64(drv, spec, st0)
+
+    # ---- roofline of the dominant kernel
     peaks, src = measured_peaks()
     n_int = spec.gall * (spec.kall - 2) * spec.lall
     cell_ms = t_cell / max(nsteps, 1)
     col_ms = t_col / max(nsteps, 1)
     rates = fp64_rates()
-    hbm_gbs = CELL_KERNEL_BYTES_PER_CELL * n_int / (cell_ms * 1e-3) / 1e9
-    roofline = {"kernel": "nsw6_cell_kernel", "cell_kernel_ms": cell_ms, "column_kernel_ms": col_ms,
-                "hbm": {"achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                        "frac": hbm_gbs / peaks["hbm_gbs"], "peak_source": f"{src} copy bandwidth"}}
+    hbm_cell = CELL_KERNEL_BYTES_PER_CELL * n_int / (cell_ms * 1e-3) / 1e9
+    hbm = {"cell_kernel_gbs": hbm_cell, "cell_kernel_frac": hbm_cell / peaks["hbm_gbs"], "peak": peaks["hbm_gbs"],
+           "unit": "GB/s", "peak_source": f"{src} copy bandwidth"}
+    roofline = {"cell_kernel_ms": cell_ms, "column_kernel_ms": col_ms, "hbm": hbm}
     if rates:
         aw = algorithmic_work(spec, st0, OP_WEIGHTS)
-        flops = aw["cell_per_interior_cell"] * n_int
-        achieved = flops / (cell_ms * 1e-3) / 1e12
+        cell_flops = aw["cell_per_interior_cell"] * n_int
         col_flops = aw["column_per_cell"] * spec.cells
+        cell = {"achieved": cell_flops / (cell_ms * 1e-3) / 1e12, "work_per_interior_cell": aw["cell_per_interior_cell"],
+                "traffic": CELL_KERNEL_TRAFFIC_PER_CELL * n_int}
+        col = {"achieved": col_flops / (col_ms * 1e-3) / 1e12, "work_per_cell": aw["column_per_cell"],
+               "traffic": COLUMN_KERNEL_TRAFFIC_PER_CELL * spec.cells}
+        for d in (cell, col):
+            d["frac"] = d["achieved"] / rates["peak_tflops"]
+        top, other, names = (cell, col, ("nsw6_cell_kernel", "nsw6_column_kernel")) if cell_ms >= col_ms else \
+            (col, cell, ("nsw6_column_kernel", "nsw6_cell_kernel"))
         roofline.update({
-            "bound": "fp64", "achieved": achieved, "peak": rates["peak_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / rates["peak_tflops"], "traffic": CELL_KERNEL_TRAFFIC_PER_CELL * n_int,
+            "kernel": names[0], "bound": "fp64", "achieved": top["achieved"], "peak": rates["peak_tflops"],
+            "unit": "TFLOP/s", "frac": top["frac"], "traffic": top["traffic"],
             "peak_source": "measured in this run: FP64 FMA throughput probe (MEASURED_PEAKS.json has no FP64 peak)",
-            "work_per_interior_cell": aw["cell_per_interior_cell"],
-            "work_definition": "reference operations counted on this state (integer powers as products), "
-                               "weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by their frozen measured cost",
+            "work_definition": "FP64 operations of the reference algorithm counted on this state (integer powers "
+                               "as products), weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by their frozen "
+                               "measured cost",
             "op_weights": OP_WEIGHTS,
             "op_weights_this_run": rates["weights"],
-            "column_kernel": {"achieved": col_flops / (col_ms * 1e-3) / 1e12,
-                              "frac": col_flops / (col_ms * 1e-3) / 1e12 / rates["peak_tflops"],
-                              "work_per_cell": aw["column_per_cell"]},
+            names[1]: other,
         })
+        roofline.update({"work_per_unit": top.get("work_per_interior_cell", top.get("work_per_cell"))})
     else:
-        roofline.update({"bound": "hbm", "achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": hbm_gbs / peaks["hbm_gbs"], "traffic": None})
+        roofline.update({"kernel": "nsw6_cell_kernel", "bound": "hbm", "achieved": hbm_cell,
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": hbm_cell / peaks["hbm_gbs"],
+                         "traffic": None})
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -373,16 +524,20 @@ def main(argv=None) -> int:
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
                "sample": f"3 steps x 1 region of {spec.gall}x{spec.kall} cells (median), OpenMP"}
 
+    mixed = args.precision == "mixed"
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NICAM-like state)",
-        "config": {"workload": f"NSW6 FP64 step, gall={spec.gall} kall={spec.kall} lall={spec.lall} per GPU "
-                               f"({spec.cells} cells), dt={spec.dt}", "variant": spec.variant,
+        "metric": METRIC_MIXED if mixed else METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic (seeded NICAM-like state)",
+        "config": {"workload": f"NSW6 {'mixed-precision' if mixed else 'FP64'} step, gall={spec.gall} "
+                               f"kall={spec.kall} lall={spec.lall} per GPU ({spec.cells} cells), dt={spec.dt}",
+                   "variant": spec.variant, "precision": args.precision,
                    "l2": "working set >> L2 (no flush needed)", "parallelism": f"regions x{world}"},
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": 2 * args.steps,
     }
+    if mixed_error is not None:
+        line["mixed_error_vs_fp64"] = mixed_error
     if rank == 0:
         print(json.dumps(line), flush=True)
     drv.close()

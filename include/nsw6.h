@@ -93,6 +93,17 @@ int nsw6_set_math(nsw6_handle* h, int mode);
  * x^y) on n device-resident inputs, for accuracy checks. */
 int nsw6_eval_math(nsw6_handle* h, int fn, const double* x, const double* y, double* out, int n);
 
+/* Precision of the step for every entry point of this handle: 0 (default) the
+ * plain FP64 step; 1 the mixed-precision step: saturation values, process
+ * rates, limiters, tendencies, fall speeds, effective radii and departure
+ * distances in FP32, while the negative filter, the tracer and internal-
+ * energy budgets, the flux sums of the transport and the saturation-
+ * adjustment Newton iteration with its vapour pressure stay FP64; 2 the FP64
+ * step evaluated one column per thread by the code the tangent-linear and
+ * adjoint kernels are built from (bitwise equal to 0; for checking them).  No
+ * counterpart in the reference (FP64 only). */
+int nsw6_set_precision(nsw6_handle* h, int mode);
+
 /* Per-kernel timing with CUDA events recorded on the handle's stream around
  * each kernel of every step (0 = off, the default). */
 int nsw6_set_timing(nsw6_handle* h, int on);
@@ -134,6 +145,27 @@ int mp_driver(nsw6_handle* h, int l_region,
               double dt, double ct,
               double* GDCLW, double* GDCFRC, double* GPREC, const double* CBMFX);
 
+/* mp_driver in the mixed precision of nsw6_set_precision(h, 1), for this call
+ * only; same arguments. */
+int mp_driver_mixed(nsw6_handle* h, int l_region,
+                    double* rhog, double* rhogvx, double* rhogvy, double* rhogvz, double* rhogw, double* rhoge,
+                    double* rhogq,
+                    const double* vx, const double* vy, const double* vz, const double* w, const double* unccn,
+                    double* rho, double* tem, double* pre,
+                    double* q, double* qd,
+                    double* precip, double* ISO1_precip, double* ISO2_precip,
+                    double* precip_rhoe, double* precip_lh_heat, double* precip_rhophi, double* precip_rhokin,
+                    double* re_liquid, double* re_solid, double* re_cld,
+                    double* rctop, double* rwtop, double* tctop,
+                    const double* frhoge_af, const double* frhogqv_af, const double* frhoge_rad,
+                    const double* rhogqke,
+                    const double* gsgam2, const double* gsgam2h, const double* gam2, const double* gam2h,
+                    const double* ix, const double* iy, const double* iz,
+                    const double* jx, const double* jy, const double* jz,
+                    const double* z, const double* zh,
+                    double dt, double ct,
+                    double* GDCLW, double* GDCFRC, double* GPREC, const double* CBMFX);
+
 /* All lall regions in one launch sequence, arrays in the reference harness's
  * all-regions layout (src/main.cpp:19-90): [lall][kall][gall] fields,
  * [lall][6][kall][gall] tracers, [2][lall][gall] precipitation (the
@@ -166,6 +198,45 @@ int mp_driver_batched(nsw6_handle* h, int lall,
  * inputs to device workspace, runs the step and copies the outputs back
  * (synchronous).  This is the entry point a ctypes/cffi/FFI binding uses. */
 int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int host);
+
+/* nsteps consecutive steps of mp_driver_argv (device pointers) on the same
+ * arrays, the state evolving in place as in the reference harness's
+ * SET_iteration loop (src/main.cpp:261-319).  The step (two memsets and the
+ * two kernels) is captured once into a CUDA graph on a stream of the handle
+ * and replayed nsteps times on the handle's stream; the graph is kept and
+ * re-captured when the arrays, lall, dt, the parameters or the precision /
+ * math / itelim settings change.  The status word is checked once, after the
+ * last step.  No counterpart in the reference. */
+int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int nsteps);
+
+/* ---------------------------------------------------------------------------
+ * Tangent-linear and adjoint steps (no counterpart in the reference).
+ *
+ * Both linearise the FP64 step around the state `args` (the 50 arrays of
+ * mp_driver_argv, device pointers, all-regions layout, lall regions).  The
+ * derivatives follow the branch each switch and limiter takes; the departure
+ * cells and flux-integral bounds of the sedimentation are held fixed; the
+ * saturation-adjustment temperature is differentiated implicitly at its
+ * converged value.  Parameters are the seven of nsw6_params in their order
+ * (beta_saut, qicrt_saut, Cr, Cs, Cg, ice_nuc, kk_aut).  kall <= 48.
+ *
+ * mp_driver_tlm: advances `args` by one step (the FP64 step, evaluated one
+ *   column per thread) and maps the tangents in `targs` (50 device pointers,
+ *   same layouts; on entry dx, on exit dy) : dy = (dM/dx) dx + (dM/dp) dp,
+ *   with dparams[7] a host array (NULL: no parameter tangent).
+ *
+ * mp_driver_adjoint: `args` is the state BEFORE the step and is not changed.
+ *   `aargs` (50 device pointers): on entry the adjoints of the step's outputs,
+ *   on exit the adjoints of its inputs -- replaced for the arguments the step
+ *   both reads and writes, added to for the arguments it only reads, zero for
+ *   the arguments it only writes.  dparams[7] (host, may be NULL): the
+ *   parameters' adjoint is added to it.  The tapes are sized by a first pass
+ *   and kept in the handle (about 32 bytes per recorded operation for up to
+ *   8192 columns at a time). */
+int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
+                  double dt, double ct);
+int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
+                      double dt, double ct);
 
 /* ---------------------------------------------------------------------------
  * mp_driver_noalloc: one NSW6 step on one region that allocates nothing.

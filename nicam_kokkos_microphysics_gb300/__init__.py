@@ -118,6 +118,14 @@ class MPDriver:
         ptr = getattr(stream, "cuda_stream", stream)
         _check(self._lib.nsw6_set_stream(self._h, ctypes.c_void_p(int(ptr or 0))), self._lib)
 
+    def set_precision(self, mode: int | str) -> None:
+        """0 / "fp64": the plain FP64 step (default); 1 / "mixed": FP32 process
+        rates with FP64 budgets, flux sums and saturation adjustment; 2 /
+        "serial": the FP64 step one column per thread, by the code of the
+        derivative kernels (for checking them)."""
+        m = {"fp64": 0, "mixed": 1, "serial": 2}.get(mode, mode) if isinstance(mode, str) else int(mode)
+        _check(self._lib.nsw6_set_precision(self._h, int(m)), self._lib)
+
     def set_math(self, mode: int) -> None:
         """0: table-driven exp/log/pow (default), 1: CUDA math library."""
         _check(self._lib.nsw6_set_math(self._h, int(mode)), self._lib)
@@ -177,6 +185,15 @@ class MPDriver:
         rc = self._lib.mp_driver(self._h, int(l_region), *ptrs[:46], float(dt), float(ct), *ptrs[46:])
         self._raise_status(rc)
 
+    def mp_driver_mixed(self, l_region: int, *args, dt: float | None = None, ct: float = 0.0):
+        """mp_driver in mixed precision for this call (C ABI mp_driver_mixed)."""
+        arrays, dt, ct = _split_args(args, dt, ct)
+        shapes = [region_shape(kind, self.kall, self.gall) for _, kind, _ in MP_DRIVER_ARGS]
+        ptrs = self._device_ptrs(arrays, shapes)
+        self._use_torch_stream()
+        rc = self._lib.mp_driver_mixed(self._h, int(l_region), *ptrs[:46], float(dt), float(ct), *ptrs[46:])
+        self._raise_status(rc)
+
     def mp_driver_batched(self, lall: int, *args, dt: float | None = None, ct: float = 0.0):
         arrays, dt, ct = _split_args(args, dt, ct)
         shapes = [batched_shape(kind, lall, self.kall, self.gall) for _, kind, _ in MP_DRIVER_ARGS]
@@ -208,6 +225,50 @@ class MPDriver:
             self._raise_status(rc)
             return
         self.mp_driver_batched(lall, *[state[n] for n in ARG_NAMES], dt=dt, ct=ct)
+
+    def mp_driver_steps(self, lall: int, state: dict, nsteps: int, dt: float, ct: float = 0.0) -> None:
+        """nsteps steps in place on ``state`` (CUDA tensors keyed by the
+        argument names, all-regions layout) from one captured CUDA graph."""
+        self._use_torch_stream()
+        rc = self._lib.mp_driver_steps(self._h, int(lall), self._ptr_array(state, lall), float(dt), float(ct),
+                                       int(nsteps))
+        self._raise_status(rc)
+
+    # ------------------------------------------------------- derivatives
+    def _ptr_array(self, state: dict, lall: int):
+        import torch
+        arr = (ctypes.c_void_p * len(ARG_NAMES))()
+        for i, (name, kind, _) in enumerate(MP_DRIVER_ARGS):
+            t = state[name]
+            shp = batched_shape(kind, lall, self.kall, self.gall)
+            if not isinstance(t, torch.Tensor) or t.device.type != "cuda" or t.dtype != torch.float64 \
+                    or not t.is_contiguous() or tuple(t.shape) != tuple(shp):
+                raise ValueError(f"{name}: expected a contiguous float64 CUDA tensor of shape {tuple(shp)}")
+            arr[i] = t.data_ptr()
+        return arr
+
+    def tlm(self, lall: int, state: dict, tangent: dict, dparams=None, dt: float = 60.0, ct: float = 0.0) -> None:
+        """Tangent-linear step (C ABI mp_driver_tlm): advances ``state`` by one
+        FP64 step and maps ``tangent`` (same keys and shapes) in place; dparams:
+        7 parameter tangents or None."""
+        self._use_torch_stream()
+        dp = None
+        if dparams is not None:
+            dp = (ctypes.c_double * 7)(*[float(v) for v in dparams])
+        rc = self._lib.mp_driver_tlm(self._h, int(lall), self._ptr_array(state, lall), self._ptr_array(tangent, lall),
+                                     dp, float(dt), float(ct))
+        self._raise_status(rc)
+
+    def adjoint(self, lall: int, state: dict, adjoint: dict, dt: float = 60.0, ct: float = 0.0) -> np.ndarray:
+        """Adjoint step (C ABI mp_driver_adjoint) around ``state`` (unchanged):
+        ``adjoint`` holds the output adjoints on entry and the input adjoints on
+        exit; returns the adjoint of the 7 parameters."""
+        self._use_torch_stream()
+        dp = (ctypes.c_double * 7)()
+        rc = self._lib.mp_driver_adjoint(self._h, int(lall), self._ptr_array(state, lall),
+                                         self._ptr_array(adjoint, lall), dp, float(dt), float(ct))
+        self._raise_status(rc)
+        return np.array(dp[:], dtype=np.float64)
 
     def run_argv(self, lall: int, ptrs: list[int], dt: float, ct: float = 0.0, host: bool = False) -> int:
         """Raw entry point: 50 pointers in reference order; returns the status code."""

@@ -19,8 +19,8 @@ INCLUDE = PKG.parent / "include"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libnsw6_gb300.so"
 
-SOURCES = ["nsw6_kernels.cu", "nsw6_driver.cu"]
-HEADERS = ["nsw6_common.cuh", "nsw6_cell.cuh"]
+SOURCES = ["nsw6_kernels.cu", "nsw6_deriv.cu", "nsw6_driver.cu"]
+HEADERS = ["nsw6_common.cuh", "nsw6_cell.cuh", "nsw6_fastmath.cuh", "nsw6_ad.cuh", "nsw6_column_step.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false keeps every product and sum separately rounded, as the
 # reference's arithmetic is written; fused operations are spelled out
@@ -44,15 +44,27 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the translation units in parallel, then link the library."""
     if not force and not _stale():
         return LIB
+    import concurrent.futures as cf
     LIBDIR.mkdir(parents=True, exist_ok=True)
+    objdir = LIBDIR / "obj"
+    objdir.mkdir(exist_ok=True)
+    compile_flags = [f for f in NVCC_FLAGS if f != "-shared"]
+
+    def compile_one(src: str) -> Path:
+        obj = objdir / (Path(src).stem + ".o")
+        cmd = [nvcc(), *ARCH, *compile_flags, "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        subprocess.run(cmd, check=True)
+        return obj
+
+    with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
     tmp = LIB.with_suffix(".so.tmp")
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-I", str(INCLUDE),
-           *[str(CSRC / s) for s in SOURCES], "-o", str(tmp)]
-    if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-    subprocess.run(cmd, check=True)
+    subprocess.run([nvcc(), *ARCH, "-shared", *[str(o) for o in objs], "-o", str(tmp)], check=True)
     os.replace(tmp, LIB)
     return LIB
 
@@ -106,6 +118,11 @@ def load() -> ctypes.CDLL:
     lib.mp_driver_argv.argtypes = [vp, c_int, ctypes.POINTER(vp), c_double, c_double, c_int]
     lib.mp_driver.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.mp_driver_batched.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
+    lib.mp_driver_mixed.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
+    lib.nsw6_set_precision.argtypes = [vp, c_int]
+    lib.mp_driver_steps.argtypes = [vp, c_int, ctypes.POINTER(vp), c_double, c_double, c_int]
+    lib.mp_driver_tlm.argtypes = [vp, c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), vp, c_double, c_double]
+    lib.mp_driver_adjoint.argtypes = [vp, c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), vp, c_double, c_double]
     lib.mp_driver_noalloc.argtypes = [c_int, c_int, vp, vp, vp, ctypes.POINTER(vp), c_double, c_double, vp]
     _lib = lib
     return lib

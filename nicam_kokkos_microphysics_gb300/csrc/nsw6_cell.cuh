@@ -43,286 +43,387 @@ __device__ __forceinline__ double div_rn(double a, double b, double rb) {
   return __fma_rn(r, rb, q);
 }
 
-struct CellIn {
-  double rhog, tem, gsgam2, q0;
-  double rhogq[6];
+template <class D>
+struct CellInT {
+  D rhog, tem, gsgam2, q0;
+  D rhogq[6];
 };
 
-struct CellOut {
-  double rhog, rhoge, tem;
-  double rhogq[6];
-  double q[6];
-  double Vtr, Vts, Vtg;
-  double rceff, rceff_cld, rctop, tctop;
+template <class D>
+struct CellOutT {
+  D rhog, rhoge, tem;
+  D rhogq[6];
+  D q[6];
+  D Vtr, Vts, Vtg;
+  D rceff, rceff_cld, rctop, tctop;
 };
+using CellIn = CellInT<double>;
+using CellOut = CellOutT<double>;
 
-template <class M>
-__device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double dt, double rdt, const CellIn& in,
-                                          CellOut& o) {
+// Scalar helpers overloaded on the precision of the process rates (FP64 in
+// the plain path, FP32 in the mixed path).
+__device__ __forceinline__ double fmaR(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float fmaR(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double sqrtR(double x) { return sqrt(x); }
+__device__ __forceinline__ float sqrtR(float x) { return sqrtf(x); }
+__device__ __forceinline__ double fabsR(double x) { return fabs(x); }
+__device__ __forceinline__ float fabsR(float x) { return fabsf(x); }
+__device__ __forceinline__ float dmin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float dmax(float a, float b) { return (a < b) ? b : a; }
+// x * f for a switch value f in {0, 1} (the reference's iceflg, delta1,
+// delta2, spsati): x, or the zero x * 0 gives (a zero with the sign of x),
+// selected without an FP64 multiplication.
+__device__ __forceinline__ double sel(bool on, double x) { return on ? x : copysign(0.0, x); }
+__device__ __forceinline__ float sel(bool on, float x) { return on ? x : copysignf(0.0f, x); }
+
+// q / dt of the rates: the correctly rounded quotient in FP64 (the reference
+// divides), a product with 1/dt in FP32.
+__device__ __forceinline__ double per_dt(double q, double dt, double rdt) { return div_rn(q, dt, rdt); }
+__device__ __forceinline__ float per_dt(float q, float, float rdt) { return q * rdt; }
+
+// R = double: the plain FP64 step.  R = float (the mixed path): saturation
+// values, process rates, limiters, tendencies, fall speeds and effective radii
+// in FP32; the negative filter, the tracer and internal-energy budgets
+// (rhogq += drhogq, rhoge) and the temperature update stay FP64.
+//
+// D is the type of the state and budget arithmetic: double in both paths; the
+// tangent-linear and adjoint kernels instantiate R = D with their derivative
+// types (nsw6_ad.cuh).
+template <class M, class R, class D = double>
+__device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, double dt, double rdt,
+                                          const CellInT<D>& in, CellOutT<D>& o) {
+  constexpr bool kMixed = sizeof(R) == sizeof(float);
+  const R dtR = R(dt), rdtR = R(rdt);
   // ---- negative_filter, mod_mp_nsw6.cpp:1770-1831
-  double rq[6];
+  D rq[6];
 #pragma unroll
   for (int n = 0; n < 6; ++n) rq[n] = in.rhogq[n];
-  double diffq = 0.0;
+  D diffq = D(0.0);
 #pragma unroll
   for (int n = 2; n <= 5; ++n) {
     diffq += rq[n];
-    rq[n] = dmax(rq[n], 0.0);
+    rq[n] = dmax(rq[n], D(0.0));
   }
 #pragma unroll
   for (int n = 2; n <= 5; ++n) diffq -= rq[n];
   rq[I_QV] += diffq;
   diffq = rq[I_QV];
-  rq[I_QV] = dmax(rq[I_QV], 0.0);
+  rq[I_QV] = dmax(rq[I_QV], D(0.0));
   diffq -= rq[I_QV];
-  const double rhog = in.rhog * (1.0 - diffq);
-  const double rrhog = 1.0 / rhog;
-  const double dens = rhog / in.gsgam2;
-  double qn[6];
+  const D rhog = in.rhog * (1.0 - diffq);
+  const D rrhog = 1.0 / rhog;
+  const D dens = rhog / in.gsgam2;
+  D qn[6];
   qn[0] = in.q0;
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) qn[n] = div_rn(rq[n], rhog, rrhog);
-  double qd = 1.0;
+  for (int n = 1; n <= 5; ++n) qn[n] = kMixed ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
+  D qd = D(1.0);
 #pragma unroll
   for (int n = 1; n <= 5; ++n) qd = qd - qn[n];
-  double cv = qd * CVDRY;
+  D cv = qd * CVDRY;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) cv = cv + qn[n] * CVDRY;
-  const double temp = in.tem;
-  double rhoge = temp * rhog * cv;
-  const double pre = dens * (qd * RDRY + qn[0] * RVAP) * temp;
+  const D temp = in.tem;
+  D rhoge = temp * rhog * cv;
+  const R pre = R(dens * (qd * RDRY + qn[0] * RVAP) * temp);
 
   // ---- psat / qsat (CPovR = 0 under EIN_TYPE "SIMPLE": the power term is 1)
-  const double rtem = 1.0 / dmax(temp, TEM_MIN);
-  const double psatl = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-  const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
-  const double rdrt = 1.0 / (dens * RVAP * temp);
-  const double qsatl = psatl * rdrt;
-  const double qsati = psati * rdrt;
+  const R tempR = R(temp), densR = R(dens);
+  const R rtem = R(1.0) / dmax(tempR, R(TEM_MIN));
+  const R psatl = R(PSAT0) * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+  const R psati = R(PSAT0) * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
+  const R rdrt = R(1.0) / (densR * R(RVAP) * tempR);
+  const R qsatl = psatl * rdrt;
+  const R qsati = psati * rdrt;
 
   // ---- TagBigLoop, mod_mp_nsw6.cpp:902-1594
-  const double qv = dmax(qn[0], 0.0), qc = dmax(qn[1], 0.0), qr = dmax(qn[2], 0.0);
-  const double qi = dmax(qn[3], 0.0), qs = dmax(qn[4], 0.0), qg = dmax(qn[5], 0.0);
-  const double Sliq = qv / dmax(qsatl, EPS);
-  const double Sice = qv / dmax(qsati, EPS);
-  const double Rdens = 1.0 / dens;
-  const double rho_fact = sqrt(DENS00 * Rdens);
-  const double temc = temp - TEM00;
-  const bool warm = !(temc < 0.0);  // iceflg = 0.5 - copysign(0.5, temc) == 0
-  const double iceflg = warm ? 0.0 : 1.0;
-  const double delta1 = (qr >= 1.0E-4) ? 1.0 : 0.0;
-  const double delta2 = (1.0E-4 >= qr && 1.0E-4 >= qs) ? 1.0 : 0.0;
-  const double spsati = (Sice >= 1.0) ? 1.0 : 0.0;
-  const double dqv_dt = div_rn(qv, dt, rdt), dqc_dt = div_rn(qc, dt, rdt), dqr_dt = div_rn(qr, dt, rdt);
-  const double dqi_dt = div_rn(qi, dt, rdt), dqs_dt = div_rn(qs, dt, rdt), dqg_dt = div_rn(qg, dt, rdt);
+  const R Z = R(0.0), ONE = R(1.0);
+  const R qv = dmax(R(qn[0]), Z), qc = dmax(R(qn[1]), Z), qr = dmax(R(qn[2]), Z);
+  const R qi = dmax(R(qn[3]), Z), qs = dmax(R(qn[4]), Z), qg = dmax(R(qn[5]), Z);
+  const R Sliq = qv / dmax(qsatl, R(EPS));
+  const R Sice = qv / dmax(qsati, R(EPS));
+  const R Rdens = ONE / densR;
+  const R rho_fact = sqrtR(R(DENS00) * Rdens);
+  const R temc = tempR - R(TEM00);
+  const bool warm = !(temc < Z);  // iceflg = 0.5 - copysign(0.5, temc) == 0
+  const bool d1 = (qr >= R(1.0E-4));                          // delta1
+  const bool d2 = (R(1.0E-4) >= qr && R(1.0E-4) >= qs);       // delta2
+  const bool sps = (Sice >= ONE);                              // spsati
+  const R dqv_dt = per_dt(qv, dtR, rdtR), dqc_dt = per_dt(qc, dtR, rdtR), dqr_dt = per_dt(qr, dtR, rdtR);
+  const R dqi_dt = per_dt(qi, dtR, rdtR), dqs_dt = per_dt(qs, dtR, rdtR), dqg_dt = per_dt(qg, dtR, rdtR);
+
+  // The blocks of a species that is absent are skipped: every quantity they
+  // would compute is then exactly zero (the reference evaluates them with a
+  // zero slope parameter or moment), which is what the initial values hold.
+  // The cell kernel groups cells by species so that whole warps skip them.
 
   // rain slope parameter, :953-967
-  const double RLMDr = (qr >= 1.0E-12) ? sqrt(sqrt(dens * qr * C.K_rlmdr)) : 0.0;
-  const double RLMDr_dr = sqrt(RLMDr);
-  const double RLMDr_2 = RLMDr * RLMDr;
-  const double RLMDr_3 = RLMDr_2 * RLMDr;
-  const double RLMDr_1br = RLMDr_2 * RLMDr_2;
-  const double RLMDr_2br = RLMDr_1br * RLMDr;
-  const double RLMDr_3br = RLMDr_3 * RLMDr_3;
-  const double RLMDr_7 = RLMDr_3br * RLMDr;
-  const double RLMDr_3dr = RLMDr_3 * RLMDr_dr;
-  const double RLMDr_5dr = RLMDr_2br * RLMDr_dr;
-  const double RLMDr_6dr = RLMDr_3br * RLMDr_dr;
+  const bool rain = (qr >= R(1.0E-12));
+  R RLMDr = Z, RLMDr_dr = Z, RLMDr_2 = Z, RLMDr_3 = Z, RLMDr_1br = Z, RLMDr_2br = Z, RLMDr_3br = Z, RLMDr_7 = Z;
+  R RLMDr_3dr = Z, RLMDr_5dr = Z, RLMDr_6dr = Z;
+  if (rain) {
+    RLMDr = sqrtR(sqrtR(densR * qr * C.K_rlmdr));
+    RLMDr_dr = sqrtR(RLMDr);
+    RLMDr_2 = RLMDr * RLMDr;
+    RLMDr_3 = RLMDr_2 * RLMDr;
+    RLMDr_1br = RLMDr_2 * RLMDr_2;
+    RLMDr_2br = RLMDr_1br * RLMDr;
+    RLMDr_3br = RLMDr_3 * RLMDr_3;
+    RLMDr_7 = RLMDr_3br * RLMDr;
+    RLMDr_3dr = RLMDr_3 * RLMDr_dr;
+    RLMDr_5dr = RLMDr_2br * RLMDr_dr;
+    RLMDr_6dr = RLMDr_3br * RLMDr_dr;
+  }
 
   // Roh and Satoh (2014) snow moments, :994-1057.  Each moment is
   // 10^loga * Xs2^b = exp(ln10 * loga + log(Xs2) * b), with loga and b
   // polynomials in tems whose coefficients per moment are folded on the host.
-  const double Xs2 = dens * qs * C.rAs;
-  const bool snow = (Xs2 >= 1.0E-12);
-  const double tems = dmin(-0.1, temc);
-  const double logX = snow ? mth.log(Xs2) : 0.0;
-  double mom[7];  // MOMs_0, MOMs_1, MOMs_0bs, MOMs_1bs, MOMs_2bs, MOMs_2ds (= nm 2.25), MOMs_5ds_h
+  const R Xs2 = densR * qs * C.rAs;
+  const bool snow = (Xs2 >= R(1.0E-12));
+  R mom[7] = {Z, Z, Z, Z, Z, Z, Z};  // MOMs_0, _1, _0bs, _1bs, _2bs, _2ds (= nm 2.25), _5ds_h
+  R RMOMs_Vt = Z;
+  if (snow) {
+    const R tems = dmin(R(-0.1), temc);
+    const R logX = mth.log(Xs2);
 #pragma unroll
-  for (int i = 0; i < 7; ++i) {
-    const double* a = C.roh_a + 4 * i;
-    const double* b = C.roh_b + 4 * i;
-    const double la = __fma_rn(__fma_rn(__fma_rn(a[3], tems, a[2]), tems, a[1]), tems, a[0]);
-    const double lb = __fma_rn(__fma_rn(__fma_rn(b[3], tems, b[2]), tems, b[1]), tems, b[0]);
-    mom[i] = snow ? mth.exp(__fma_rn(logX, lb, la)) : 0.0;
+    for (int i = 0; i < 7; ++i) {
+      const R* a = C.roh_a + 4 * i;
+      const R* b = C.roh_b + 4 * i;
+      const R la = fmaR(fmaR(fmaR(a[3], tems, a[2]), tems, a[1]), tems, a[0]);
+      const R lb = fmaR(fmaR(fmaR(b[3], tems, b[2]), tems, b[1]), tems, b[0]);
+      mom[i] = mth.exp(fmaR(logX, lb, la));
+    }
+    RMOMs_Vt = mom[5] / mom[2];
   }
-  const double MOMs_0 = mom[0], MOMs_1 = mom[1], MOMs_2 = Xs2;
-  const double MOMs_0bs = mom[2], MOMs_1bs = mom[3], MOMs_2bs = mom[4], MOMs_2ds = mom[5];
-  const double MOMs_5ds_h = mom[6];
-  const double RMOMs_Vt = snow ? mom[5] / MOMs_0bs : 0.0;
+  const R MOMs_0 = mom[0], MOMs_1 = mom[1], MOMs_2 = Xs2;
+  const R MOMs_0bs = mom[2], MOMs_1bs = mom[3], MOMs_2bs = mom[4], MOMs_2ds = mom[5];
+  const R MOMs_5ds_h = mom[6];
 
   // graupel slope parameter, :1059-1066
-  const double RLMDg = (qg >= 1.0E-12) ? sqrt(sqrt(dens * qg * C.K_rlmdg)) : 0.0;
-  const double RLMDg_dg = sqrt(RLMDg);
-  const double RLMDg_2 = RLMDg * RLMDg;
-  const double RLMDg_3 = RLMDg_2 * RLMDg;
-  const double RLMDg_3dg = RLMDg_3 * RLMDg_dg;
-  const double RLMDg_5dg = RLMDg_3 * RLMDg_2 * RLMDg_dg;
+  const bool graupel = (qg >= R(1.0E-12));
+  R RLMDg = Z, RLMDg_dg = Z, RLMDg_2 = Z, RLMDg_3 = Z, RLMDg_3dg = Z, RLMDg_5dg = Z;
+  if (graupel) {
+    RLMDg = sqrtR(sqrtR(densR * qg * C.K_rlmdg));
+    RLMDg_dg = sqrtR(RLMDg);
+    RLMDg_2 = RLMDg * RLMDg;
+    RLMDg_3 = RLMDg_2 * RLMDg;
+    RLMDg_3dg = RLMDg_3 * RLMDg_dg;
+    RLMDg_5dg = RLMDg_3 * RLMDg_2 * RLMDg_dg;
+  }
 
   // terminal velocity, :1072-1078
-  const double Vtr = C.K_vtr * rho_fact * RLMDr_dr;
-  const double Vts = C.K_vts * rho_fact * RMOMs_Vt;
-  const double Vtg = C.K_vtg * rho_fact * RLMDg_dg;
+  const R Vtr = C.K_vtr * rho_fact * RLMDr_dr;
+  const R Vts = C.K_vts * rho_fact * RMOMs_Vt;
+  const R Vtg = C.K_vtg * rho_fact * RLMDg_dg;
 
   // nucleation, :1080-1085: Ni0 = max(exp(-0.1 temc), 1) * 1000 and
   // Qi0 = ice_nuc * Ni0^1.33 / dens, with log(Ni0) = ln 1000 + max(-0.1 temc, 0)
-  const double Qi0 = C.ice_nuc * mth.exp(1.33 * (C.ln1000 + dmax(-0.1 * temc, 0.0))) * Rdens;
-  double Pigen = dmax(dmin(Qi0 - qi, qv - qsati), 0.0) * rdt;
+  const R Qi0 = C.ice_nuc * mth.exp(R(1.33) * (C.ln1000 + dmax(R(-0.1) * temc, Z))) * Rdens;
+  R Pigen = dmax(dmin(Qi0 - qi, qv - qsati), Z) * rdtR;
 
   // accretion, :1087-1145
-  const double Esi_mod = dmin(C.Esi, C.Esi * mth.exp(C.gamma_sacr * temc));
-  const double qcqr = qc * qr;
-  double Pracw = (qcqr >= 1.0E-12) ? 67.0 * mth.pow(qcqr, 1.15) : 0.0;
-  const double fr = rho_fact;
-  double Psacw = qc * C.K_sacw * MOMs_2ds * fr;
-  double Pgacw = qc * C.K_gacw * RLMDg_3dg * fr;
-  double Praci = qi * C.K_raci * RLMDr_3dr * fr;
-  double Psaci = qi * C.K_saci * Esi_mod * MOMs_2ds * fr;
-  double Piacr = qi * C.K_iacr * RLMDr_6dr * fr;
-  const double dvrs = fabs(Vtr - Vts);
-  double Psacr = C.K_sacr * Rdens * dvrs *
-                 (C.GAM_1br * RLMDr_1br * MOMs_2 + C.K_2gam2br * RLMDr_2br * MOMs_1 + C.GAM_3br * RLMDr_3br * MOMs_0);
-  double Pgacr = C.K_gacr * Rdens * fabs(Vtg - Vtr) *
-                 (C.K_g13 * RLMDr_1br * RLMDg_3 + C.K_g22 * RLMDr_2br * RLMDg_2 + C.GAM_3br * RLMDr_3br * RLMDg);
-  double Pracs = C.K_racs * Rdens * dvrs * (2.0 * MOMs_0bs * RLMDr_3 + 2.0 * MOMs_1bs * RLMDr_2 + MOMs_2bs * RLMDr);
+  // Esi_mod and betai, :1089, :1162: min(E, E exp(0.06 temc)) is E when temc >= 0
+  // (exp >= 1 there) and E >= 0; both use the same exponential when
+  // gamma_sacr == gamma_saut (both 6e-2 in this configuration).
+  R Esi_mod = C.Esi, betai = C.beta_saut;
+  if (!(warm && C.Esi >= Z && C.beta_saut >= Z)) {
+    const R eg = mth.exp(C.gamma_sacr * temc);
+    const R eb = (C.gamma_saut == C.gamma_sacr) ? eg : mth.exp(C.gamma_saut * temc);
+    Esi_mod = dmin(C.Esi, C.Esi * eg);
+    betai = dmin(C.beta_saut, C.beta_saut * eb);
+  }
+  const R qcqr = qc * qr;
+  R Pracw = Z;
+  if (qcqr >= R(1.0E-12)) Pracw = R(67.0) * mth.pow(qcqr, R(1.15));
+  const R fr = rho_fact;
+  R Psacw = qc * C.K_sacw * MOMs_2ds * fr;
+  R Pgacw = qc * C.K_gacw * RLMDg_3dg * fr;
+  R Praci = qi * C.K_raci * RLMDr_3dr * fr;
+  R Psaci = qi * C.K_saci * Esi_mod * MOMs_2ds * fr;
+  R Piacr = qi * C.K_iacr * RLMDr_6dr * fr;
+  const R dvrs = fabsR(Vtr - Vts);
+  R Psacr = C.K_sacr * Rdens * dvrs *
+            (C.GAM_1br * RLMDr_1br * MOMs_2 + C.K_2gam2br * RLMDr_2br * MOMs_1 + C.GAM_3br * RLMDr_3br * MOMs_0);
+  R Pgacr = C.K_gacr * Rdens * fabsR(Vtg - Vtr) *
+            (C.K_g13 * RLMDr_1br * RLMDg_3 + C.K_g22 * RLMDr_2br * RLMDg_2 + C.GAM_3br * RLMDr_3br * RLMDg);
+  R Pracs = C.K_racs * Rdens * dvrs * (R(2.0) * MOMs_0bs * RLMDr_3 + R(2.0) * MOMs_1bs * RLMDr_2 + MOMs_2bs * RLMDr);
 
   // autoconversion, :1147-1172 (KK2000; only the second Praut_kk assignment is live)
-  const double rhoqc = dens * qc * 1000.0;
-  double Praut = C.K_aut * mth.pow(qc, 2.47);
-  const double betai = dmin(C.beta_saut, C.beta_saut * mth.exp(C.gamma_saut * temc));
-  double Psaut = dmax(betai * (qi - C.qicrt_saut), 0.0);
+  const R rhoqc = densR * qc * R(1000.0);
+  R Praut = Z;   // K_aut * pow(0, 2.47) = 0
+  if (qc > Z) Praut = C.K_aut * mth.pow(qc, R(2.47));
+  R Psaut = dmax(betai * (qi - C.qicrt_saut), Z);
 
   // evaporation, sublimation, melting and freezing, :1174-1247
-  const double Ka = (2.428E-2 + 7.47E-5 * temc);
-  const double KdD = (2.222E-5 + 1.37E-7 * temc) * PSTD / pre * dens;   // Kd * dens
-  const double rNu = dens / (1.718E-5 + 5.28E-8 * temc);                // 1 / Nu
-  const double rKaT = 1.0 / (Ka * temp);
-  const double xl = KdD * qsatl, xi = KdD * qsati;
-  const double Glv = xl / (LHV0 * rKaT * (C.LovR_liq * rtem - 1.0) * xl + 1.0);
-  const double Giv = xi / (LHS0 * rKaT * (C.LovR_ice * rtem - 1.0) * xi + 1.0);
-  const double Gil = Ka * temc * C.rLHF0;
-  const double ventr = C.K_ventr1 * RLMDr_2 + C.K_ventr2 * sqrt(C.Cr * fr * rNu * RLMDr_5dr);
-  double Prevp = C.K_revp * Rdens * (1.0 - dmin(Sliq, 1.0)) * Glv * ventr;
-  const double rhoqi = dmax(dens * qi, EPS);
-  const double XNi = dmin(dmax(5.38E+7 * mth.pow(rhoqi, 0.75), 1.0E+3), 1.0E+6);
-  const double XMi = rhoqi / XNi;
-  const double Di = dmin(C.Di_a * sqrt(XMi), C.Di_max);
-  double tmp = 4.0 * Di * XNi * Rdens * (Sice - 1.0) * Giv;
-  double Pidep = spsati * tmp;
-  double Pisub = (1.0 - spsati) * (-tmp);
-  const bool below40 = (temc + 40.0 < 0.0);
-  double Pihom = below40 ? dqc_dt : 0.0;
-  const double efrz = mth.exp(-C.A_frz * temc) - 1.0;
-  double Pihtr = (!below40 && !warm) ? dens * (qc * qc) * C.K_ihtr * efrz : 0.0;
-  double Pimlt = warm ? dqi_dt : 0.0;
-  const double vents = 0.65 * MOMs_1 + C.K_vents2 * sqrt(fr * rNu) * MOMs_5ds_h;
-  tmp = C.K_2pi * Rdens * (Sice - 1.0) * Giv * vents;
-  double Psdep = spsati * tmp;
-  double Pssub = (1.0 - spsati) * (-tmp);
-  double Psmlt = dmax(C.K_2pi * Rdens * Gil * vents + C.K_clf * temc * (Psacw + Psacr), 0.0);
-  const double ventg = C.K_ventg1 * RLMDg_2 + C.K_ventg2 * sqrt(C.Cg * fr * rNu * RLMDg_5dg);
-  tmp = C.K_gdep * Rdens * (Sice - 1.0) * Giv * ventg;
-  double Pgdep = spsati * tmp;
-  double Pgsub = (1.0 - spsati) * (-tmp);
-  double Pgmlt = dmax(C.K_gdep * Rdens * Gil * ventg + C.K_clf * temc * (Pgacw + Pgacr), 0.0);
-  double Pgfrz = C.K_gfrz * Rdens * efrz * RLMDr_7;
+  const R Ka = (R(2.428E-2) + R(7.47E-5) * temc);
+  const R KdD = (R(2.222E-5) + R(1.37E-7) * temc) * R(PSTD) / pre * densR;   // Kd * dens
+  const R rNu = densR / (R(1.718E-5) + R(5.28E-8) * temc);                 // 1 / Nu
+  const R rKaT = ONE / (Ka * tempR);
+  const R xi = KdD * qsati;
+  const R Giv = xi / (R(LHS0) * rKaT * (C.LovR_ice * rtem - ONE) * xi + ONE);
+  const R Gil = Ka * temc * C.rLHF0;
+  R Prevp = Z;
+  if (rain) {
+    const R xl = KdD * qsatl;
+    const R Glv = xl / (R(LHV0) * rKaT * (C.LovR_liq * rtem - ONE) * xl + ONE);
+    const R ventr = C.K_ventr1 * RLMDr_2 + C.K_ventr2 * sqrtR(C.Cr * fr * rNu * RLMDr_5dr);
+    Prevp = C.K_revp * Rdens * (ONE - dmin(Sliq, ONE)) * Glv * ventr;
+  }
+  const R rhoqi = dmax(densR * qi, R(EPS));
+  // with no ice, rhoqi = EPS and XNi, Di take the constant values folded on the host
+  R XNi = C.XNi_eps, Di = C.Di_eps;
+  if (rhoqi > R(EPS)) {
+    XNi = dmin(dmax(R(5.38E+7) * mth.pow(rhoqi, R(0.75)), R(1.0E+3)), R(1.0E+6));
+    const R XMi = rhoqi / XNi;
+    Di = dmin(C.Di_a * sqrtR(XMi), C.Di_max);
+  }
+  R tmp = R(4.0) * Di * XNi * Rdens * (Sice - ONE) * Giv;
+  R Pidep = sel(sps, tmp);
+  R Pisub = sel(!sps, -tmp);
+  const bool below40 = (temc + R(40.0) < Z);
+  R Pihom = below40 ? dqc_dt : Z;
+  const R efrz = mth.exp(-C.A_frz * temc) - ONE;
+  R Pihtr = (!below40 && !warm) ? densR * (qc * qc) * C.K_ihtr * efrz : Z;
+  R Pimlt = warm ? dqi_dt : Z;
+  const R vents = R(0.65) * MOMs_1 + C.K_vents2 * sqrtR(fr * rNu) * MOMs_5ds_h;
+  tmp = C.K_2pi * Rdens * (Sice - ONE) * Giv * vents;
+  R Psdep = sel(sps, tmp);
+  R Pssub = sel(!sps, -tmp);
+  R Psmlt = dmax(C.K_2pi * Rdens * Gil * vents + C.K_clf * temc * (Psacw + Psacr), Z);
+  const R ventg = C.K_ventg1 * RLMDg_2 + C.K_ventg2 * sqrtR(C.Cg * fr * rNu * RLMDg_5dg);
+  tmp = C.K_gdep * Rdens * (Sice - ONE) * Giv * ventg;
+  R Pgdep = sel(sps, tmp);
+  R Pgsub = sel(!sps, -tmp);
+  R Pgmlt = dmax(C.K_gdep * Rdens * Gil * ventg + C.K_clf * temc * (Pgacw + Pgacr), Z);
+  R Pgfrz = C.K_gfrz * Rdens * efrz * RLMDr_7;
 
   // limiters, :1249-1296 (iceflg selects; sw_expice = 1; Psfw = Psfi = Pgaut = Pgaci = Pgacs = 0)
-  Pigen = dmin(Pigen, dqv_dt) * iceflg;
-  Pidep = dmin(Pidep, dqv_dt) * iceflg;
-  Psdep = dmin(Psdep, dqv_dt) * iceflg;
-  Pgdep = dmin(Pgdep, dqv_dt) * iceflg;
-  Pracw = Pracw + Psacw * (1.0 - iceflg) + Pgacw * (1.0 - iceflg);
+  const bool cold = !warm;   // iceflg == 1
+  Pigen = sel(cold, dmin(Pigen, dqv_dt));
+  Pidep = sel(cold, dmin(Pidep, dqv_dt));
+  Psdep = sel(cold, dmin(Psdep, dqv_dt));
+  Pgdep = sel(cold, dmin(Pgdep, dqv_dt));
+  Pracw = Pracw + sel(warm, Psacw) + sel(warm, Pgacw);
   Praut = dmin(Praut, dqc_dt);
   Pracw = dmin(Pracw, dqc_dt);
-  Pihom = dmin(Pihom, dqc_dt) * iceflg;
-  Pihtr = dmin(Pihtr, dqc_dt) * iceflg;
-  Psacw = dmin(Psacw, dqc_dt) * iceflg;
-  Pgacw = dmin(Pgacw, dqc_dt) * iceflg;
+  Pihom = sel(cold, dmin(Pihom, dqc_dt));
+  Pihtr = sel(cold, dmin(Pihtr, dqc_dt));
+  Psacw = sel(cold, dmin(Psacw, dqc_dt));
+  Pgacw = sel(cold, dmin(Pgacw, dqc_dt));
   Prevp = dmin(Prevp, dqr_dt);
-  Piacr = dmin(Piacr, dqr_dt) * iceflg;
-  Psacr = dmin(Psacr, dqr_dt) * iceflg;
-  Pgacr = dmin(Pgacr, dqr_dt) * iceflg;
-  Pgfrz = dmin(Pgfrz, dqr_dt) * iceflg;
-  Pisub = dmin(Pisub, dqi_dt) * iceflg;
-  Pimlt = dmin(Pimlt, dqi_dt) * (1.0 - iceflg);
-  Psaut = dmin(Psaut, dqi_dt) * iceflg;
-  Praci = dmin(Praci, dqi_dt) * iceflg;
-  Psaci = dmin(Psaci, dqi_dt) * iceflg;
-  Pssub = dmin(Pssub, dqs_dt) * iceflg;
-  Psmlt = dmin(Psmlt, dqs_dt) * (1.0 - iceflg);
-  Pracs = dmin(Pracs, dqs_dt) * iceflg;
-  Pgsub = dmin(Pgsub, dqg_dt) * iceflg;
-  Pgmlt = dmin(Pgmlt, dqg_dt) * (1.0 - iceflg);
-  double Piacr_s = (1.0 - delta1) * Piacr;
-  double Piacr_g = delta1 * Piacr;
-  double Praci_s = (1.0 - delta1) * Praci;
-  double Praci_g = delta1 * Praci;
-  double Psacr_s = delta2 * Psacr;
-  double Psacr_g = (1.0 - delta2) * Psacr;
-  Pracs = (1.0 - delta2) * Pracs;
+  Piacr = sel(cold, dmin(Piacr, dqr_dt));
+  Psacr = sel(cold, dmin(Psacr, dqr_dt));
+  Pgacr = sel(cold, dmin(Pgacr, dqr_dt));
+  Pgfrz = sel(cold, dmin(Pgfrz, dqr_dt));
+  Pisub = sel(cold, dmin(Pisub, dqi_dt));
+  Pimlt = sel(warm, dmin(Pimlt, dqi_dt));
+  Psaut = sel(cold, dmin(Psaut, dqi_dt));
+  Praci = sel(cold, dmin(Praci, dqi_dt));
+  Psaci = sel(cold, dmin(Psaci, dqi_dt));
+  Pssub = sel(cold, dmin(Pssub, dqs_dt));
+  Psmlt = sel(warm, dmin(Psmlt, dqs_dt));
+  Pracs = sel(cold, dmin(Pracs, dqs_dt));
+  Pgsub = sel(cold, dmin(Pgsub, dqg_dt));
+  Pgmlt = sel(warm, dmin(Pgmlt, dqg_dt));
+  R Piacr_s = sel(!d1, Piacr);
+  R Piacr_g = sel(d1, Piacr);
+  R Praci_s = sel(!d1, Praci);
+  R Praci_g = sel(d1, Praci);
+  R Psacr_s = sel(d2, Psacr);
+  R Psacr_g = sel(!d2, Psacr);
+  Pracs = sel(!d2, Pracs);
 
   // loss limiters, :1298-1477: fac = 1 when production >= loss - EPS,
   // else min(-dq/dt / net, 1) (the reference's (net - fac_sw) is net there)
-  auto limiter = [&](double net, double dq) {
-    return (net + EPS >= 0.0) ? 1.0 : dmin(-dq / net, 1.0);
+  auto limiter = [&](R net, R dq) {
+    return (net + R(EPS) >= Z) ? ONE : dmin(-dq / net, ONE);
   };
-  double fac;
+  // scaling by fac = 1 is exact and skipped
+  R fac;
   fac = limiter(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw, dqc_dt);  // [QC]
-  Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Pgacw *= fac;
+  if (fac != ONE) {
+    Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Pgacw *= fac;
+  }
   fac = limiter(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g, dqi_dt);  // [QI]
-  Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
-  Praci_s *= fac; Psaci *= fac; Praci_g *= fac;
+  if (fac != ONE) {
+    Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
+    Praci_s *= fac; Psaci *= fac; Praci_g *= fac;
+  }
   fac = limiter(+Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz,
                 dqr_dt);  // [QR]
-  Praut *= fac; Pracw *= fac; Psmlt *= fac; Pgmlt *= fac; Prevp *= fac; Piacr_s *= fac; Psacr_s *= fac;
-  Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac;
+  if (fac != ONE) {
+    Praut *= fac; Pracw *= fac; Psmlt *= fac; Pgmlt *= fac; Prevp *= fac; Piacr_s *= fac; Psacr_s *= fac;
+    Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac;
+  }
   fac = limiter(+Prevp + Pisub + Pssub + Pgsub - Pigen - Pidep - Psdep - Pgdep, dqv_dt);  // [QV]
-  Prevp *= fac; Pisub *= fac; Pssub *= fac; Pgsub *= fac; Pigen *= fac; Pidep *= fac; Psdep *= fac; Pgdep *= fac;
+  if (fac != ONE) {
+    Prevp *= fac; Pisub *= fac; Pssub *= fac; Pgsub *= fac; Pigen *= fac; Pidep *= fac; Psdep *= fac; Pgdep *= fac;
+  }
   fac = limiter(+Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs, dqs_dt);  // [QS]
-  Psdep *= fac; Psacw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac; Psaci *= fac;
-  Pssub *= fac; Psmlt *= fac; Pracs *= fac;
+  if (fac != ONE) {
+    Psdep *= fac; Psacw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac; Psaci *= fac;
+    Pssub *= fac; Psmlt *= fac; Pracs *= fac;
+  }
   fac = limiter(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt, dqg_dt);  // [QG]
-  Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
-  Pracs *= fac; Pgsub *= fac; Pgmlt *= fac;
+  if (fac != ONE) {
+    Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
+    Pracs *= fac; Pgsub *= fac; Pgmlt *= fac;
+  }
 
   // tendencies, :1479-1559
-  double qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;
-  double qr_t = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;
-  double qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;
-  double qs_t = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
-  double qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
+  R qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;
+  R qr_t = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;
+  R qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;
+  R qs_t = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
+  R qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
   qc_t = dmax(qc_t, -dqc_dt);
   qr_t = dmax(qr_t, -dqr_dt);
   qi_t = dmax(qi_t, -dqi_dt);
   qs_t = dmax(qs_t, -dqs_dt);
   qg_t = dmax(qg_t, -dqg_dt);
-  const double qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
-  double drq[6];
-  drq[0] = rhog * qv_t * dt;
-  drq[1] = rhog * qc_t * dt;
-  drq[2] = rhog * qr_t * dt;
-  drq[3] = rhog * qi_t * dt;
-  drq[4] = rhog * qs_t * dt;
-  drq[5] = rhog * qg_t * dt;
-  o.Vtr = Vtr;
-  o.Vts = Vts;
-  o.Vtg = Vtg;
+  const R qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
+  D drq[6];
+  drq[0] = rhog * D(qv_t) * dt;
+  drq[1] = rhog * D(qc_t) * dt;
+  drq[2] = rhog * D(qr_t) * dt;
+  drq[3] = rhog * D(qi_t) * dt;
+  drq[4] = rhog * D(qs_t) * dt;
+  drq[5] = rhog * D(qg_t) * dt;
+  if (kMixed) {
+    // A species whose loss reached its whole content leaves exactly nothing
+    // (the FP64 path leaves a rounding residue of the same size as the
+    // reference's; FP32 rates would leave one 10^9 times larger), and the
+    // vapour takes the balance so that total water stays exact.
+    const R qt[6] = {qv_t, qc_t, qr_t, qi_t, qs_t, qg_t};
+    const R lim[6] = {dqv_dt, dqc_dt, dqr_dt, dqi_dt, dqs_dt, dqg_dt};
+    D sum = D(0.0);
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) {
+      if (qt[n] <= -lim[n] && lim[n] > Z) drq[n] = -rq[n];
+      sum += drq[n];
+    }
+    drq[0] = -sum;
+  }
+  o.Vtr = D(Vtr);
+  o.Vts = D(Vts);
+  o.Vtg = D(Vtg);
 
   // effective radius and cloud top, :1566-1592
   {
-    const double r2_min = 1.0E-10, q_min = 1.0E-5;
-    const double rf_qc = mth.pow(C.coef_xf * (rhoqc * C.K_xf) + EPS, 0.33333333);
-    const double r2_qc = C.K_r2c * (rf_qc * rf_qc);
-    const double r2_qr = C.K_r2r * RLMDr_3;
-    const double r3_qc = C.coef_xf * dens * qc;
-    const double r3_qr = C.coef_xf * dens * qr;
-    const double r2 = r2_qc + r2_qr;
+    const R r2_min = R(1.0E-10), q_min = R(1.0E-5);
+    const R rf_qc = mth.pow(C.coef_xf * (rhoqc * C.K_xf) + R(EPS), R(0.33333333));
+    const R r2_qc = C.K_r2c * (rf_qc * rf_qc);
+    const R r2_qr = C.K_r2r * RLMDr_3;
+    const R r3_qc = C.coef_xf * densR * qc;
+    const R r3_qr = C.coef_xf * densR * qr;
+    const R r2 = r2_qc + r2_qr;
     const bool big = (r2 >= r2_min);
-    o.rceff = big ? (r3_qc + r3_qr) / r2 : 0.0;
+    const R rceff = big ? (r3_qc + r3_qr) / r2 : Z;
     const bool top = !big && ((qc + qr) >= q_min);
-    o.rctop = top ? o.rceff : UNDEF;
-    o.tctop = top ? temp : UNDEF;
-    o.rceff_cld = (r2_qc >= r2_min) ? r3_qc / r2_qc : 0.0;
+    o.rceff = D(rceff);
+    o.rctop = top ? D(rceff) : D(UNDEF);
+    o.tctop = top ? temp : D(UNDEF);
+    o.rceff_cld = (r2_qc >= r2_min) ? D(r3_qc / r2_qc) : D(0.0);
   }
 
   // ---- TagUpdateRHOGQ / RHOGE / MassConc / TEM, mod_mp_nsw6.cpp:692-744
@@ -332,10 +433,10 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
   o.q[0] = qn[0];
 #pragma unroll
   for (int n = 1; n <= 5; ++n) o.q[n] = div_rn(rq[n], rhog, rrhog);
-  double qd2 = 1.0;
+  D qd2 = D(1.0);
 #pragma unroll
   for (int n = 1; n <= 5; ++n) qd2 = qd2 - o.q[n];
-  double cva = qd2 * CVDRY;
+  D cva = qd2 * CVDRY;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) cva = cva + o.q[n] * CVDRY;
   o.tem = rhoge / (rhog * cva);
@@ -347,9 +448,9 @@ __device__ __forceinline__ void nsw6_cell(const Consts& C, const M& mth, double 
 
 // Half-level velocity wh(j) of vadv1d_prep (mod_vadv1d.cpp:270-282) for a column
 // accessor wp(j).
-template <class WP>
-__device__ __forceinline__ double vadv_wh(const WP& wp, int j, int mkmin, int mkmax) {
-  if (j >= mkmin + 1 && j <= mkmax) return 0.5 * (wp(j - 1) + wp(j));
+template <class R, class WP>
+__device__ __forceinline__ R vadv_wh(const WP& wp, int j, int mkmin, int mkmax) {
+  if (j >= mkmin + 1 && j <= mkmax) return R(0.5) * (wp(j - 1) + wp(j));
   if (j == mkmin) return wp(mkmin);
   if (j == mkmin - 1) return wp(mkmin - 1);
   return wp(mkmax);  // j == mkmax + 1
@@ -363,20 +464,20 @@ __device__ __forceinline__ double vadv_wh(const WP& wp, int j, int mkmin, int mk
 // instead of divisions.  zdis only decides which layer the departure point
 // lies in (an ulp-level change matters only within an ulp of an interface)
 // and scales the flux of the departure layer.
-template <class WP>
-__device__ __forceinline__ double vadv_zdis(const WP& wp, const double* rdz, const double* rdzs, int k, int mkmin,
-                                           int mkmax, double dt, double hdt2, double sdt3) {
+template <class R, class G, class WP>
+__device__ __forceinline__ R vadv_zdis(const WP& wp, const G* rdz, const G* rdzs, int k, int mkmin, int mkmax, R dt,
+                                       R hdt2, R sdt3) {
   if (k == mkmin) {
-    const double w0 = vadv_wh(wp, mkmin, mkmin, mkmax), wpp = vadv_wh(wp, mkmin + 1, mkmin, mkmax);
-    return __fma_rn(-hdt2 * w0, (wpp - w0) * rdz[mkmin], dt * w0);
+    const R w0 = vadv_wh<R>(wp, mkmin, mkmin, mkmax), wpp = vadv_wh<R>(wp, mkmin + 1, mkmin, mkmax);
+    return fmaR(-hdt2 * w0, (wpp - w0) * rdz[mkmin], dt * w0);
   }
-  const double wm = vadv_wh(wp, k - 1, mkmin, mkmax);
-  const double w0 = vadv_wh(wp, k, mkmin, mkmax);
-  const double wpp = vadv_wh(wp, k + 1, mkmin, mkmax);
-  const double r = (wpp - wm) * rdzs[k];
-  const double c = 2.0 * rdzs[k] * __fma_rn(wpp - w0, rdz[k], -(w0 - wm) * rdz[k - 1]);
-  const double t3 = sdt3 * w0 * __fma_rn(w0, c, r * r);
-  return __fma_rn(-hdt2 * w0, r, __fma_rn(dt, w0, t3));
+  const R wm = vadv_wh<R>(wp, k - 1, mkmin, mkmax);
+  const R w0 = vadv_wh<R>(wp, k, mkmin, mkmax);
+  const R wpp = vadv_wh<R>(wp, k + 1, mkmin, mkmax);
+  const R r = (wpp - wm) * rdzs[k];
+  const R c = R(2.0) * rdzs[k] * fmaR(wpp - w0, rdz[k], -(w0 - wm) * rdz[k - 1]);
+  const R t3 = sdt3 * w0 * fmaR(w0, c, r * r);
+  return fmaR(-hdt2 * w0, r, fmaR(dt, w0, t3));
 }
 
 }  // namespace nsw6

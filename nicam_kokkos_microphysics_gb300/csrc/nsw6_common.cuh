@@ -43,32 +43,48 @@ constexpr int MAX_KALL = 160;
 // Scheme constants: mp_nsw6_init (mod_mp_nsw6.cpp:276-434) with the settings it
 // hard-wires, the effective-radius constants of mp_nsw6_new::init
 // (mod_mp_nsw6.cpp:506-517) and SATURATION_Setup (mod_satadjust.cpp:24-47).
-// Built once on the host (same libm as the oracle) and passed by value.
-struct Consts {
-  double Ar, As, Ag, Cr, Cs, Cg, N0r, N0s, N0g;
-  double GAM_1br, GAM_2br, GAM_3br, GAM_3dr, GAM_6dr, GAM_1brdr, GAM_5dr_h;
-  double GAM_1bs, GAM_2bs, GAM_3bs, GAM_3ds, GAM_1bsds, GAM_5ds_h;
-  double GAM_1bg, GAM_3dg, GAM_1bgdg, GAM_5dg_h;
-  double Esi, Egs, gamma_sacr, gamma_gacs, mi;
-  double beta_saut, gamma_saut, qicrt_saut;
-  double A_frz, B_frz, mi40, mi50, Ri50;
-  double Nc_ihtr, Di_max, Di_a, ln10;
-  double coef_a[10], coef_b[10];
-  double Nc_def, coef_dgam, coef_xf;
-  double ice_nuc, kk_aut;
-  double LovR_liq, LovR_ice, RTEM00;
-  double dtemp_criteria;
+// Built once on the host (same libm as the oracle) and passed by value; the
+// mixed-precision path gets an FP32 copy (ConstsT<float>, member by member).
+template <class R>
+struct ConstsT {
+  R Ar, As, Ag, Cr, Cs, Cg, N0r, N0s, N0g;
+  R GAM_1br, GAM_2br, GAM_3br, GAM_3dr, GAM_6dr, GAM_1brdr, GAM_5dr_h;
+  R GAM_1bs, GAM_2bs, GAM_3bs, GAM_3ds, GAM_1bsds, GAM_5ds_h;
+  R GAM_1bg, GAM_3dg, GAM_1bgdg, GAM_5dg_h;
+  R Esi, Egs, gamma_sacr, gamma_gacs, mi;
+  R beta_saut, gamma_saut, qicrt_saut;
+  R A_frz, B_frz, mi40, mi50, Ri50;
+  R Nc_ihtr, Di_max, Di_a, ln10;
+  R coef_a[10], coef_b[10];
+  R Nc_def, coef_dgam, coef_xf;
+  R ice_nuc, kk_aut;
+  R LovR_liq, LovR_ice, RTEM00;
+  R dtemp_criteria;
   // derived products that appear verbatim in the reference expressions
-  double log_mi50, log_mi40;
-  double Dc_berry, pow_Nc_m179;
+  R log_mi50, log_mi40;
+  R Dc_berry, pow_Nc_m179;
   // constant factors of the process rates folded on the host (nsw6_cell.cuh)
-  double K_rlmdr, K_rlmdg, rAs, K_vtr, K_vts, K_vtg;
-  double K_sacw, K_gacw, K_raci, K_saci, K_iacr, K_sacr, K_2gam2br, K_gacr, K_g13, K_g22, K_racs;
-  double K_aut, rLHF0, K_ventr1, K_ventr2, K_revp, K_ihtr, K_vents2, K_2pi, K_clf, K_ventg1, K_ventg2;
-  double K_gdep, K_gfrz, K_xf, K_r2c, K_r2r;
-  double roh_a[28], roh_b[28];   // per snow moment: ln10*loga and b as cubics in tems
-  double ln1000;
+  R K_rlmdr, K_rlmdg, rAs, K_vtr, K_vts, K_vtg;
+  R K_sacw, K_gacw, K_raci, K_saci, K_iacr, K_sacr, K_2gam2br, K_gacr, K_g13, K_g22, K_racs;
+  R K_aut, rLHF0, K_ventr1, K_ventr2, K_revp, K_ihtr, K_vents2, K_2pi, K_clf, K_ventg1, K_ventg2;
+  R K_gdep, K_gfrz, K_xf, K_r2c, K_r2r;
+  R roh_a[28], roh_b[28];   // per snow moment: ln10*loga and b as cubics in tems
+  R ln1000;
+  R XNi_eps, Di_eps;   // ice number and diameter at the floor rhoqi = EPS (no ice)
 };
+using Consts = ConstsT<double>;
+using ConstsF = ConstsT<float>;
+static_assert(sizeof(Consts) == 2 * sizeof(ConstsF), "ConstsT must hold scalars only");
+
+// Member-by-member FP32 copy of the scheme constants (both layouts are plain
+// arrays of their scalar type in the same order).
+inline ConstsF consts_to_float(const Consts& c) {
+  ConstsF f;
+  const double* src = reinterpret_cast<const double*>(&c);
+  float* dst = reinterpret_cast<float*>(&f);
+  for (size_t i = 0; i < sizeof(Consts) / sizeof(double); ++i) dst[i] = (float)src[i];
+  return f;
+}
 
 // Per-level grid metrics (GRD_Setup, mod_debug.cpp:92-187), device copy laid
 // out as [field][kall].
@@ -103,6 +119,7 @@ struct Problem {
   double rdt;            // 1 / dt
   int itelim;
   int math_lib;                // 0 table-driven transcendentals, 1 CUDA libm
+  int mixed;                   // 0 plain FP64 step, 1 mixed precision (FP32 process rates)
   const double* grid;          // [GF_COUNT][kall]
   const double* fmtab;         // fast-math tables (nsw6_fastmath.cuh)
   double* const* a;            // not used on device
@@ -124,6 +141,35 @@ struct Problem {
   unsigned long long* zmin;    // [lall][6][kall] ordered keys, reset to ~0
   DevStatus* status;
 };
+
+// The 50 mp_driver array arguments of one call, in the reference order.
+struct ArgPtrs {
+  double* a[A_COUNT];
+};
+
+// Per-thread tapes of the adjoint kernel, interleaved over nslot threads:
+// operands pa/pb, partial derivatives da/db and adjoints of cap entries each.
+struct TapeMem {
+  int* pa;
+  int* pb;
+  double* da;
+  double* db;
+  double* adj;
+  int nslot, cap, count_only;
+};
+
+// Comparisons of doubles on the integer pipe (the FP64 pipe is the scarce one
+// on GB300): for non-NaN a and b, a >= b exactly when cmp_key(a) >=
+// cmp_key(b), with -0 and +0 equal.
+__device__ __forceinline__ long long cmp_key(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == (long long)0x8000000000000000ULL) b = 0;
+  return b < 0 ? (b ^ 0x7fffffffffffffffLL) : b;
+}
+__device__ __forceinline__ bool is_nan_bits(double x) {
+  return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+constexpr long long EPS_BITS = 0x3caffffff4178da3LL;   // bit pattern of EPS = 2.220446E-16
 
 __host__ __device__ __forceinline__ double dmin(double a, double b) { return (b < a) ? b : a; }  // Kokkos::min
 __host__ __device__ __forceinline__ double dmax(double a, double b) { return (a < b) ? b : a; }  // Kokkos::max

@@ -1,0 +1,273 @@
+// Derivative kernels of the NSW6 step: the serial-column FP64 step (the
+// forward of the derivative kernels, checked bit for bit against the
+// production kernels), the tangent-linear step and the adjoint step.
+//
+// One thread walks one whole column (nsw6_column_step.cuh).  The region-wide
+// bounds of the flux integrals come from the departure-distance extrema of the
+// same state, computed beforehand by the production cell kernel on a copy.
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "nsw6_column_step.cuh"
+
+namespace nsw6 {
+
+namespace {
+
+__device__ __forceinline__ void record_error_d(DevStatus* st, int code, int k, int g, int l, int iters) {
+  if (atomicCAS(&st->code, 0, code) == 0) {
+    st->k = k;
+    st->g = g;
+    st->l = l;
+    st->iters = iters;
+  }
+}
+
+// Index helpers for the all-regions layout.
+struct Lay {
+  int K, G, lall;
+  __device__ __forceinline__ size_t f(int l, int k, int g) const { return ((size_t)l * K + k) * G + g; }
+  __device__ __forceinline__ size_t t(int l, int n, int k, int g) const {
+    return (((size_t)l * NQ + n) * K + k) * G + g;
+  }
+  __device__ __forceinline__ size_t c(int l, int g) const { return (size_t)l * G + g; }
+  __device__ __forceinline__ size_t p(int r, int l, int g) const { return ((size_t)r * lall + l) * G + g; }
+};
+
+// Visits every (argument, index, state slot) the step reads.
+template <class T, class V>
+__device__ __forceinline__ void for_inputs(ColState<T>& s, const Lay& L, int l, int g, const V& v) {
+  for (int k = 0; k < L.K; ++k) {
+    const size_t i = L.f(l, k, g);
+    v(A_rhog, i, s.rhog[k]);
+    v(A_rhoge, i, s.rhoge[k]);
+    v(A_rhogvx, i, s.rhogvx[k]);
+    v(A_rhogvy, i, s.rhogvy[k]);
+    v(A_rhogvz, i, s.rhogvz[k]);
+    v(A_rhogw, i, s.rhogw[k]);
+    v(A_tem, i, s.tem[k]);
+    v(A_vx, i, s.vx[k]);
+    v(A_vy, i, s.vy[k]);
+    v(A_vz, i, s.vz[k]);
+    v(A_gsgam2, i, s.gsgam2[k]);
+    v(A_gsgam2h, i, s.gsgam2h[k]);
+    v(A_gam2, i, s.gam2[k]);
+    v(A_gam2h, i, s.gam2h[k]);
+    v(A_z, i, s.z[k]);
+    for (int n = 0; n < NQ; ++n) {
+      const size_t iq = L.t(l, n, k, g);
+      v(A_rhogq, iq, s.rhogq[n][k]);
+      v(A_q, iq, s.q[n][k]);
+    }
+  }
+  const size_t ic = L.c(l, g);
+  v(A_ix, ic, s.ix);
+  v(A_iy, ic, s.iy);
+  v(A_iz, ic, s.iz);
+  v(A_jx, ic, s.jx);
+  v(A_jy, ic, s.jy);
+  v(A_jz, ic, s.jz);
+}
+
+// Visits every (argument, index, value) the step writes; constant outputs are
+// passed as T constants.
+template <class T, class V>
+__device__ __forceinline__ void for_outputs(ColState<T>& s, const Lay& L, int l, int g, const V& v) {
+  for (int k = 0; k < L.K; ++k) {
+    const size_t i = L.f(l, k, g);
+    v(A_rhog, i, s.rhog[k]);
+    v(A_rhogvx, i, s.rhogvx[k]);
+    v(A_rhogvy, i, s.rhogvy[k]);
+    v(A_rhogvz, i, s.rhogvz[k]);
+    v(A_rhogw, i, s.rhogw[k]);
+    v(A_rhoge, i, s.rhoge[k]);
+    v(A_rho, i, s.rho[k]);
+    v(A_tem, i, s.tem[k]);
+    v(A_pre, i, s.pre[k]);
+    v(A_qd, i, s.qd[k]);
+    v(A_re_liquid, i, s.re_liquid[k]);
+    v(A_re_cld, i, s.re_cld[k]);
+    v(A_GPREC, i, s.GPREC[k]);
+    T c0 = T(20.0E-6), z0 = T(0.0), z1 = T(0.0);
+    v(A_re_solid, i, c0);
+    v(A_GDCLW, i, z0);
+    v(A_GDCFRC, i, z1);
+    for (int n = 0; n < NQ; ++n) {
+      const size_t iq = L.t(l, n, k, g);
+      v(A_rhogq, iq, s.rhogq[n][k]);
+      v(A_q, iq, s.q[n][k]);
+    }
+  }
+  const size_t ic = L.c(l, g);
+  v(A_precip, L.p(0, l, g), s.precip0);
+  v(A_precip, L.p(1, l, g), s.precip1);
+  T z2 = T(0.0), z3 = T(0.0), z4 = T(0.0), z5 = T(0.0);
+  v(A_ISO1, L.p(0, l, g), z2);
+  v(A_ISO1, L.p(1, l, g), z3);
+  v(A_ISO2, L.p(0, l, g), z4);
+  v(A_ISO2, L.p(1, l, g), z5);
+  v(A_precip_rhoe, ic, s.p_rhoe);
+  v(A_precip_lh_heat, ic, s.lh_heat);
+  v(A_precip_rhophi, ic, s.p_rhophi);
+  v(A_precip_rhokin, ic, s.p_rhokin);
+  v(A_rctop, ic, s.rctop);
+  v(A_rwtop, ic, s.rwtop);
+  v(A_tctop, ic, s.tctop);
+}
+
+// Shared-memory set-up common to the derivative kernels: the grid block and
+// the fast-math tables.
+__device__ __forceinline__ void stage(const Problem& P, double* grid, double* tab) {
+  for (int c = threadIdx.x; c < GF_COUNT * P.kall; c += blockDim.x) grid[c] = P.grid[c];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  __syncthreads();
+}
+
+}  // namespace
+
+// ---- serial-column FP64 step: the derivative kernels' forward, in place
+__global__ void __launch_bounds__(AD_THREADS) nsw6_serial_kernel(Problem P, Consts C, ArgPtrs x) {
+  __shared__ double grid[GF_COUNT * KA];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  stage(P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const Lay L{P.kall, P.gall, P.lall};
+  const int l = blockIdx.y;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= P.gall) return;
+  ColState<double> s;
+  ColWork<double> w;
+  for_inputs(s, L, l, g, [&](int a, size_t i, double& d) { d = x.a[a][i]; });
+  int bmn[6][KA], bmx[6][KA];
+  column_bounds(grid + GF_GZH * P.kall, grid + GF_GZSHIFT * P.kall, P.kall, P.kmin, P.kmax,
+                P.zmax + (size_t)l * 6 * P.kall, P.zmin + (size_t)l * 6 * P.kall, bmn, bmx);
+  int err = 0, ek = 0, eit = 0;
+  column_step<double, FastMath>(C, C, fm, fm, grid, P.kall, P.dt, P.rdt, P.hdt2, P.sdt3, P.itelim, bmn, bmx, s, w,
+                                &err, &ek, &eit);
+  if (err) record_error_d(P.status, err, ek, g, l, eit);
+  for_outputs(s, L, l, g, [&](int a, size_t i, double& d) { x.a[a][i] = d; });
+}
+
+// ---- tangent-linear step: x <- M(x), dx <- M'(x) dx (+ M_p dp)
+__global__ void __launch_bounds__(AD_THREADS) nsw6_tlm_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs dx,
+                                                              const double* params, const double* dparams) {
+  __shared__ double grid[GF_COUNT * KA];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  stage(P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const ADMath<Dual> mth{fm};
+  const Lay L{P.kall, P.gall, P.lall};
+  const int l = blockIdx.y;
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= P.gall) return;
+  Dual p[7];
+  for (int i = 0; i < 7; ++i) p[i] = Dual(params[i], dparams ? dparams[i] : 0.0);
+  ConstsT<Dual> CT;
+  consts_with_params(C, p, CT);
+  ColState<Dual> s;
+  ColWork<Dual> w;
+  for_inputs(s, L, l, g, [&](int a, size_t i, Dual& d) { d = Dual(x.a[a][i], dx.a[a][i]); });
+  int bmn[6][KA], bmx[6][KA];
+  column_bounds(grid + GF_GZH * P.kall, grid + GF_GZSHIFT * P.kall, P.kall, P.kmin, P.kmax,
+                P.zmax + (size_t)l * 6 * P.kall, P.zmin + (size_t)l * 6 * P.kall, bmn, bmx);
+  int err = 0, ek = 0, eit = 0;
+  column_step<Dual, ADMath<Dual>>(CT, C, mth, fm, grid, P.kall, P.dt, P.rdt, P.hdt2, P.sdt3, P.itelim, bmn, bmx, s,
+                                  w, &err, &ek, &eit);
+  if (err) record_error_d(P.status, err, ek, g, l, eit);
+  for_outputs(s, L, l, g, [&](int a, size_t i, Dual& d) {
+    x.a[a][i] = d.v;
+    dx.a[a][i] = d.d;
+  });
+}
+
+// ---- adjoint step: xb <- M'(x)^T xb (inputs), pbar += M_p^T xb
+// On entry xb holds the adjoints of the step's outputs; on exit the adjoints
+// of its inputs: replaced for arguments that are read and written, added for
+// arguments only read, zero for arguments only written.
+__global__ void __launch_bounds__(AD_THREADS) nsw6_adjoint_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
+                                                                  TapeMem tm, const double* params, double* pbar,
+                                                                  int* tape_max) {
+  __shared__ double grid[GF_COUNT * KA];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  __shared__ double red[7][AD_THREADS];
+  stage(P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const ADMath<RVar> mth{fm};
+  const Lay L{P.kall, P.gall, P.lall};
+  Tape& t = tape();
+  t.pa = tm.pa;
+  t.pb = tm.pb;
+  t.da = tm.da;
+  t.db = tm.db;
+  t.adj = tm.adj;
+  t.nslot = tm.nslot;
+  t.slot = blockIdx.x * blockDim.x + threadIdx.x;
+  t.cap = tm.cap;
+  double pacc[7] = {0, 0, 0, 0, 0, 0, 0};
+  const int ncol = P.lall * P.gall;
+  for (int col = t.slot; col < ncol; col += t.nslot) {
+    const int l = col / P.gall, g = col % P.gall;
+    t.n = 0;
+    t.overflow = 0;
+    t.count_only = tm.count_only;
+    RVar p[7];
+    for (int i = 0; i < 7; ++i) p[i] = leaf(params[i]);
+    ConstsT<RVar> CT;
+    consts_with_params(C, p, CT);
+    ColState<RVar> s;
+    for_inputs(s, L, l, g, [&](int a, size_t i, RVar& d) { d = leaf(x.a[a][i]); });
+    ColState<RVar> s_in = s;
+    ColWork<RVar> w;
+    int bmn[6][KA], bmx[6][KA];
+    column_bounds(grid + GF_GZH * P.kall, grid + GF_GZSHIFT * P.kall, P.kall, P.kmin, P.kmax,
+                  P.zmax + (size_t)l * 6 * P.kall, P.zmin + (size_t)l * 6 * P.kall, bmn, bmx);
+    int err = 0, ek = 0, eit = 0;
+    column_step<RVar, ADMath<RVar>>(CT, C, mth, fm, grid, P.kall, P.dt, P.rdt, P.hdt2, P.sdt3, P.itelim, bmn, bmx,
+                                    s, w, &err, &ek, &eit);
+    if (err) record_error_d(P.status, err, ek, g, l, eit);
+    atomicMax(tape_max, t.overflow ? t.cap + 1 : t.n);
+    if (t.overflow || t.count_only) continue;   // sizing pass, or reported through tape_max
+    for (int e = 0; e < t.n; ++e) t.adj[(size_t)e * t.nslot + t.slot] = 0.0;
+    for_outputs(s, L, l, g, [&](int a, size_t i, RVar& d) {
+      if (d.id >= 0) adj_of(d) += xb.a[a][i];
+    });
+    tape_reverse();
+    // written-only arguments: their adjoint is consumed
+    for_outputs(s, L, l, g, [&](int a, size_t i, RVar&) { xb.a[a][i] = 0.0; });
+    // read arguments: added (to zero for the ones also written: replaced)
+    for_inputs(s_in, L, l, g, [&](int a, size_t i, RVar& d) {
+      if (d.id >= 0) xb.a[a][i] += adj_of(d);
+    });
+    for (int i = 0; i < 7; ++i) pacc[i] += adj_of(p[i]);
+  }
+  for (int i = 0; i < 7; ++i) red[i][threadIdx.x] = pacc[i];
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double sum = 0.0;
+    for (int j = 0; j < (int)blockDim.x; ++j) sum += red[threadIdx.x][j];
+    atomicAdd(&pbar[threadIdx.x], sum);
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+cudaError_t launch_serial(const Problem& P, const Consts& C, const ArgPtrs& x, cudaStream_t stream) {
+  dim3 grid((P.gall + AD_THREADS - 1) / AD_THREADS, P.lall);
+  nsw6_serial_kernel<<<grid, AD_THREADS, 0, stream>>>(P, C, x);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tlm(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx, const double* params,
+                       const double* dparams, cudaStream_t stream) {
+  dim3 grid((P.gall + AD_THREADS - 1) / AD_THREADS, P.lall);
+  nsw6_tlm_kernel<<<grid, AD_THREADS, 0, stream>>>(P, C, x, dx, params, dparams);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const TapeMem& tm,
+                           const double* params, double* pbar, int* tape_max, cudaStream_t stream) {
+  const int blocks = tm.nslot / AD_THREADS;
+  nsw6_adjoint_kernel<<<blocks, AD_THREADS, 0, stream>>>(P, C, x, xb, tm, params, pbar, tape_max);
+  return cudaGetLastError();
+}
+
+}  // namespace nsw6

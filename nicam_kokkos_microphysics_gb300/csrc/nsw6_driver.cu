@@ -5,6 +5,7 @@
 // GRD_Setup (mod_debug.cpp:92-187), SATURATION_Setup (mod_satadjust.cpp:24-47)
 // and mp_nsw6_init (mod_mp_nsw6.cpp:276-434).  All device memory a step needs
 // is allocated in nsw6_create; a step enqueues two memsets and two kernels.
+#include <algorithm>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -18,6 +19,16 @@
 
 namespace nsw6 {
 cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev);
+cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t stream);
+cudaError_t launch_prepare();
+cudaError_t launch_serial(const Problem& P, const Consts& C, const ArgPtrs& x, cudaStream_t stream);
+cudaError_t launch_tlm(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx, const double* params,
+                       const double* dparams, cudaStream_t stream);
+cudaError_t launch_adjoint(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const TapeMem& tm,
+                           const double* params, double* pbar, int* tape_max, cudaStream_t stream);
+constexpr int DERIV_MAX_KALL = 48;   // KA of nsw6_column_step.cuh
+constexpr int DERIV_THREADS = 128;   // AD_THREADS of nsw6_ad.cuh
+constexpr int ADJ_MAX_SLOTS = 8192;  // threads of one adjoint launch (each with its own tape)
 cudaError_t launch_math(int fn, const double* x, const double* y, double* out, int n, const double* fmtab,
                         cudaStream_t stream);
 }
@@ -38,6 +49,20 @@ struct nsw6_handle {
   int sync_check = 1;
   int itelim = 100;
   int math_lib = 0;   // 0: table-driven exp/log/pow, 1: CUDA libm
+  int mixed = 0;      // 0: plain FP64 step, 1: mixed precision, 2: serial-column FP64 (derivative forward)
+  // derivative kernels: parameters, their adjoint, the tape-size counter and the tapes
+  double* d_dparam = nullptr;    // [16]: params [0,7), tangents [8,15)
+  double* d_pbar = nullptr;      // [8]
+  int* d_tmax = nullptr;
+  TapeMem tape{};
+  size_t tape_bytes = 0;
+  // captured step graph of mp_driver_steps and what it was captured for
+  cudaStream_t cap_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  double* graph_args[A_COUNT] = {};
+  int graph_lall = 0, graph_mixed = -1, graph_math = -1, graph_itelim = 0;
+  double graph_dt = 0.0;
+  nsw6_params graph_params{};
   // device staging of the 50 arguments for host-memory calls (allocated by the
   // first such call)
   double* d_stage = nullptr;
@@ -147,6 +172,10 @@ Consts make_consts(const nsw6_params& p) {
   c.log_mi40 = std::log(c.mi40);
   c.pow_Nc_m179 = std::pow(c.Nc_def, -1.79);
   c.ln1000 = std::log(1000.0);
+  // mod_mp_nsw6.cpp:1205-1208 at rhoqi = max(dens * qi, EPS) = EPS: the number
+  // 5.38e7 EPS^0.75 is far below the floor 1e3, so XNi = 1e3 exactly
+  c.XNi_eps = std::min(std::max(5.38E+7 * std::pow(EPS, 0.75), 1.0E+3), 1.0E+6);
+  c.Di_eps = std::min(c.Di_a * std::sqrt(EPS / c.XNi_eps), c.Di_max);
 
   // folded constant factors (nsw6_cell.cuh); GAM = GAM_2 = 1, GAM_3 = 2,
   // Esw = Egw = Eri = Esr = Egr = 1 (mod_mp_nsw6.h:58-67, mp_nsw6_init :345-356)
@@ -350,6 +379,7 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.fmtab = h->d_fmtab;
   P.rdt = 1.0 / dt;
   P.math_lib = h->math_lib;
+  P.mixed = h->mixed;
   P.rhog = a[A_rhog];
   P.rhogvx = a[A_rhogvx];
   P.rhogvy = a[A_rhogvy];
@@ -433,7 +463,75 @@ int finish(nsw6_handle* h, cudaError_t launch) {
   return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
 }
 
+// Device staging area for all 50 arguments of lall_max regions (the host
+// entry copies through it; the derivative kernels' pre-pass runs on it).
+int ensure_stage(nsw6_handle* h, double** dev) {
+  const int K = h->kall, G = h->gall;
+  size_t need = 0;
+  for (int i = 0; i < A_COUNT; ++i) need += arg_region_elems(i, K, G) * (size_t)h->lall_max;
+  if (!h->d_stage) {
+    if (cudaMalloc(&h->d_stage, sizeof(double) * need) != cudaSuccess) return NSW6_ERR_CUDA;
+    h->stage_count = need;
+  }
+  size_t offs = 0;
+  for (int i = 0; i < A_COUNT; ++i) {
+    dev[i] = h->d_stage + offs;
+    offs += arg_region_elems(i, K, G) * (size_t)h->lall_max;
+  }
+  return NSW6_OK;
+}
+
+// Region extrema of the departure distances of state a (into d_zmax/d_zmin):
+// the FP64 cell kernel on a copy of the fields it updates.
+int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
+  double* dev[A_COUNT];
+  int rc = ensure_stage(h, dev);
+  if (rc != NSW6_OK) return rc;
+  double* pa[A_COUNT];
+  for (int i = 0; i < A_COUNT; ++i) pa[i] = dev[i];
+  const int copy[4] = {A_rhog, A_tem, A_q, A_rhogq};
+  for (int c = 0; c < 4; ++c) {
+    const int i = copy[c];
+    if (!a[i]) return NSW6_ERR_BAD_ARG;
+    const size_t bytes = sizeof(double) * arg_region_elems(i, h->kall, h->gall) * (size_t)lall;
+    if (cudaMemcpyAsync(dev[i], a[i], bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+  }
+  pa[A_gsgam2] = a[A_gsgam2];
+  Problem P;
+  rc = fill_problem(h, lall, pa, dt, P);
+  if (rc != NSW6_OK) return rc;
+  return launch_cell_only(P, h->C, h->stream) == cudaSuccess ? NSW6_OK : NSW6_ERR_CUDA;
+}
+
+int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b) {
+  if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
+  if (h->kall > DERIV_MAX_KALL) return NSW6_ERR_UNSUPPORTED;
+  for (int i = 0; i < A_COUNT; ++i)
+    if ((arg_is_read(i) || arg_is_written(i)) && (!a[i] || !b[i])) return NSW6_ERR_BAD_ARG;
+  if (!h->d_dparam) {
+    if (cudaMalloc(&h->d_dparam, sizeof(double) * 16) != cudaSuccess ||
+        cudaMalloc(&h->d_pbar, sizeof(double) * 8) != cudaSuccess ||
+        cudaMalloc(&h->d_tmax, sizeof(int)) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+  }
+  return NSW6_OK;
+}
+
+int run_serial(nsw6_handle* h, int lall, double* const* a, double dt) {
+  if (h->kall > DERIV_MAX_KALL) return NSW6_ERR_UNSUPPORTED;
+  int rc = deriv_prepass(h, lall, a, dt);
+  if (rc != NSW6_OK) return rc;
+  Problem P;
+  rc = fill_problem(h, lall, a, dt, P);
+  if (rc != NSW6_OK) return rc;
+  ArgPtrs x;
+  for (int i = 0; i < A_COUNT; ++i) x.a[i] = a[i];
+  return finish(h, launch_serial(P, h->C, x, h->stream));
+}
+
 int run(nsw6_handle* h, int lall, double* const* a, double dt) {
+  if (h->mixed == 2) return run_serial(h, lall, a, dt);
   Problem P;
   int rc = fill_problem(h, lall, a, dt, P);
   if (rc != NSW6_OK) return rc;
@@ -497,7 +595,13 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_zmax);
   cudaFree(h->d_zmin);
   cudaFree(h->d_status);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   cudaFree(h->d_stage);
+  cudaFree(h->d_dparam);
+  cudaFree(h->d_pbar);
+  cudaFree(h->d_tmax);
+  cudaFree(h->tape.pa);
   for (auto& tri : h->ev)
     for (auto& e : tri)
       if (e) cudaEventDestroy(e);
@@ -539,6 +643,12 @@ int nsw6_set_itelim(nsw6_handle* h, int itelim) {
 int nsw6_set_math(nsw6_handle* h, int mode) {
   if (!h || mode < 0 || mode > 1) return NSW6_ERR_BAD_ARG;
   h->math_lib = mode;
+  return NSW6_OK;
+}
+
+int nsw6_set_precision(nsw6_handle* h, int mode) {
+  if (!h || mode < 0 || mode > 2) return NSW6_ERR_BAD_ARG;
+  h->mixed = mode;
   return NSW6_OK;
 }
 
@@ -618,6 +728,29 @@ int mp_driver(nsw6_handle* h, int l_region, double* rhog, double* rhogvx, double
   return run(h, 1, a, dt);
 }
 
+int mp_driver_mixed(nsw6_handle* h, int l_region, double* rhog, double* rhogvx, double* rhogvy, double* rhogvz,
+                    double* rhogw, double* rhoge, double* rhogq, const double* vx, const double* vy,
+                    const double* vz, const double* w, const double* unccn, double* rho, double* tem, double* pre,
+                    double* q, double* qd, double* precip, double* ISO1_precip, double* ISO2_precip,
+                    double* precip_rhoe, double* precip_lh_heat, double* precip_rhophi, double* precip_rhokin,
+                    double* re_liquid, double* re_solid, double* re_cld, double* rctop, double* rwtop,
+                    double* tctop, const double* frhoge_af, const double* frhogqv_af, const double* frhoge_rad,
+                    const double* rhogqke, const double* gsgam2, const double* gsgam2h, const double* gam2,
+                    const double* gam2h, const double* ix, const double* iy, const double* iz, const double* jx,
+                    const double* jy, const double* jz, const double* z, const double* zh, double dt, double ct,
+                    double* GDCLW, double* GDCFRC, double* GPREC, const double* CBMFX) {
+  if (!h) return NSW6_ERR_BAD_ARG;
+  const int saved = h->mixed;
+  h->mixed = 1;
+  const int rc = mp_driver(h, l_region, rhog, rhogvx, rhogvy, rhogvz, rhogw, rhoge, rhogq, vx, vy, vz, w, unccn,
+                           rho, tem, pre, q, qd, precip, ISO1_precip, ISO2_precip, precip_rhoe, precip_lh_heat,
+                           precip_rhophi, precip_rhokin, re_liquid, re_solid, re_cld, rctop, rwtop, tctop,
+                           frhoge_af, frhogqv_af, frhoge_rad, rhogqke, gsgam2, gsgam2h, gam2, gam2h, ix, iy, iz,
+                           jx, jy, jz, z, zh, dt, ct, GDCLW, GDCFRC, GPREC, CBMFX);
+  h->mixed = saved;
+  return rc;
+}
+
 int mp_driver_batched(nsw6_handle* h, int lall, double* rhog, double* rhogvx, double* rhogvy, double* rhogvz,
                       double* rhogw, double* rhoge, double* rhogq, const double* vx, const double* vy,
                       const double* vz, const double* w, const double* unccn, double* rho, double* tem, double* pre,
@@ -677,6 +810,149 @@ int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, dou
     if (cudaMemcpyAsync(args[i], dev[i], bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
       return NSW6_ERR_CUDA;
   }
+  return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
+}
+
+int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int nsteps) {
+  (void)ct;
+  if (!h || !args || lall < 1 || lall > h->lall_max || nsteps < 0) return NSW6_ERR_BAD_ARG;
+  if (h->mixed == 2) {   // the serial-column check path: plain calls
+    for (int i = 0; i < nsteps; ++i) {
+      const int rc = run(h, lall, args, dt);
+      if (rc != NSW6_OK) return rc;
+    }
+    return NSW6_OK;
+  }
+  Problem P;
+  int rc = fill_problem(h, lall, args, dt, P);
+  if (rc != NSW6_OK) return rc;
+  bool same = h->graph && h->graph_lall == lall && h->graph_dt == dt && h->graph_mixed == h->mixed &&
+              h->graph_math == h->math_lib && h->graph_itelim == h->itelim &&
+              std::memcmp(&h->graph_params, &h->params, sizeof(nsw6_params)) == 0;
+  for (int i = 0; same && i < A_COUNT; ++i) same = h->graph_args[i] == args[i];
+  if (!same) {
+    if (h->graph) {
+      cudaGraphExecDestroy(h->graph);
+      h->graph = nullptr;
+    }
+    if (!h->cap_stream && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+    if (launch_prepare() != cudaSuccess) return NSW6_ERR_CUDA;
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return NSW6_ERR_CUDA;
+    const cudaError_t le = launch_step(P, h->C, h->cap_stream, nullptr);
+    const cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &g);
+    if (le != cudaSuccess || ce != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      return NSW6_ERR_CUDA;
+    }
+    const cudaError_t ie = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) {
+      h->graph = nullptr;
+      return NSW6_ERR_CUDA;
+    }
+    for (int i = 0; i < A_COUNT; ++i) h->graph_args[i] = args[i];
+    h->graph_lall = lall;
+    h->graph_dt = dt;
+    h->graph_mixed = h->mixed;
+    h->graph_math = h->math_lib;
+    h->graph_itelim = h->itelim;
+    h->graph_params = h->params;
+  }
+  for (int i = 0; i < nsteps; ++i)
+    if (cudaGraphLaunch(h->graph, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  return finish(h, cudaSuccess);
+}
+
+int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
+                  double dt, double ct) {
+  (void)ct;
+  int rc = deriv_check(h, lall, args, targs);
+  if (rc != NSW6_OK) return rc;
+  rc = deriv_prepass(h, lall, args, dt);
+  if (rc != NSW6_OK) return rc;
+  Problem P;
+  rc = fill_problem(h, lall, args, dt, P);
+  if (rc != NSW6_OK) return rc;
+  double hp[16] = {};
+  std::memcpy(hp, &h->params, sizeof(double) * 7);
+  if (dparams) std::memcpy(hp + 8, dparams, sizeof(double) * 7);
+  if (cudaMemcpyAsync(h->d_dparam, hp, sizeof(hp), cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  ArgPtrs x, dx;
+  for (int i = 0; i < A_COUNT; ++i) {
+    x.a[i] = args[i];
+    dx.a[i] = targs[i];
+  }
+  rc = finish(h, launch_tlm(P, h->C, x, dx, h->d_dparam, h->d_dparam + 8, h->stream));
+  if (!h->sync_check && rc == NSW6_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  return rc;
+}
+
+int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
+                      double dt, double ct) {
+  (void)ct;
+  int rc = deriv_check(h, lall, args, aargs);
+  if (rc != NSW6_OK) return rc;
+  rc = deriv_prepass(h, lall, args, dt);
+  if (rc != NSW6_OK) return rc;
+  Problem P;
+  rc = fill_problem(h, lall, args, dt, P);
+  if (rc != NSW6_OK) return rc;
+  if (cudaMemcpyAsync(h->d_dparam, &h->params, sizeof(double) * 7, cudaMemcpyHostToDevice, h->stream) !=
+      cudaSuccess)
+    return NSW6_ERR_CUDA;
+  ArgPtrs x, xb;
+  for (int i = 0; i < A_COUNT; ++i) {
+    x.a[i] = args[i];
+    xb.a[i] = aargs[i];
+  }
+  const long long ncol = (long long)lall * h->gall;
+  long long slots = ((ncol + DERIV_THREADS - 1) / DERIV_THREADS) * DERIV_THREADS;
+  if (slots > ADJ_MAX_SLOTS) slots = ADJ_MAX_SLOTS;
+  const int nslot = (int)slots;
+  // sizing pass: the tape length of the longest column
+  int tmax = 0;
+  TapeMem cnt{};
+  cnt.nslot = nslot;
+  cnt.count_only = 1;
+  if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+      launch_adjoint(P, h->C, x, xb, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&tmax, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  const size_t per = sizeof(int) * 2 + sizeof(double) * 3;
+  const size_t need = per * (size_t)tmax * (size_t)nslot;
+  if (need > h->tape_bytes || h->tape.nslot != nslot || h->tape.cap < tmax) {
+    cudaFree(h->tape.pa);
+    h->tape = TapeMem{};
+    h->tape_bytes = 0;
+    char* base = nullptr;
+    if (cudaMalloc(&base, need) != cudaSuccess) return NSW6_ERR_CUDA;
+    const size_t n = (size_t)tmax * nslot;
+    h->tape.pa = reinterpret_cast<int*>(base);
+    h->tape.pb = h->tape.pa + n;
+    h->tape.da = reinterpret_cast<double*>(base + sizeof(int) * 2 * n);
+    h->tape.db = h->tape.da + n;
+    h->tape.adj = h->tape.db + n;
+    h->tape.nslot = nslot;
+    h->tape.cap = tmax;
+    h->tape_bytes = need;
+  }
+  h->tape.count_only = 0;
+  double pb[8] = {};
+  int tmax2 = 0;
+  if (cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+      launch_adjoint(P, h->C, x, xb, h->tape, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(pb, h->d_pbar, sizeof(double) * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&tmax2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  if (tmax2 > h->tape.cap) return NSW6_ERR_UNSUPPORTED;
+  if (dparams)
+    for (int i = 0; i < 7; ++i) dparams[i] += pb[i];
   return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
 }
 

@@ -134,6 +134,14 @@ struct FastMath {
   }
 };
 
+// FP32 transcendentals of the mixed-precision path (CUDA's expf / logf /
+// powf, within 2 ulp of FP32).
+struct FloatMath {
+  __device__ __forceinline__ float exp(float x) const { return ::expf(x); }
+  __device__ __forceinline__ float log(float x) const { return ::logf(x); }
+  __device__ __forceinline__ float pow(float x, float y) const { return ::powf(x, y); }
+};
+
 // Same interface on top of the CUDA math library (used to separate the
 // effects of the fast transcendentals from everything else).
 struct LibMath {

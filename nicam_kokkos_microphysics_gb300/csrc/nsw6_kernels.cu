@@ -53,9 +53,22 @@ template <>
 __device__ __forceinline__ LibMath make_math<LibMath>(const double*) {
   return LibMath{};
 }
+template <>
+__device__ __forceinline__ FloatMath make_math<FloatMath>(const double*) {
+  return FloatMath{};
+}
 
-template <class M>
-__global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Consts C) {
+// Shared memory of the cell kernel: fall speeds [3][K][CELL_TG] (type R), the
+// grid block [GF_COUNT][K] and the fast-math tables (doubles), and for R =
+// float FP32 copies of the four reciprocal rows the departure distances use.
+template <class R>
+__host__ __device__ constexpr size_t cell_vts_doubles(int K) {
+  return (3 * (size_t)K * CELL_TG * sizeof(R) + sizeof(double) - 1) / sizeof(double);
+}
+
+template <class M, class R>
+__global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, ConstsT<R> C) {
+  constexpr bool kMixed = sizeof(R) == sizeof(float);
   extern __shared__ double sm[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
   const int l = blockIdx.y;
@@ -63,18 +76,65 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
   const size_t KG = (size_t)K * G;
   const size_t off = (size_t)l * KG;
   const size_t offq = (size_t)l * NQ * KG;
-  double* vts = sm;                      // [3][K][CELL_TG] fall speeds of QR, QS, QG
-  double* grid = sm + 3 * K * CELL_TG;   // [GF_COUNT][K]
-  double* tab = grid + GF_COUNT * K;     // [FM_TABLE_DOUBLES]
+  R* vts = reinterpret_cast<R*>(sm);                   // [3][K][CELL_TG] fall speeds of QR, QS, QG
+  double* grid = sm + cell_vts_doubles<R>(K);          // [GF_COUNT][K]
+  double* tab = grid + GF_COUNT * K;                   // [FM_TABLE_DOUBLES]
+  float* gridf = reinterpret_cast<float*>(tab + FM_TABLE_DOUBLES);  // [4][K], mixed only
+  unsigned short* perm = reinterpret_cast<unsigned short*>(gridf + 4 * K);  // [nlev * CELL_TG], FP64 only
+  unsigned char* key = reinterpret_cast<unsigned char*>(perm + (K - 2) * CELL_TG);
+  __shared__ int bucket[33];
 
-  for (int c = threadIdx.x; c < 3 * K * CELL_TG; c += blockDim.x) vts[c] = 0.0;
+  for (int c = threadIdx.x; c < 3 * K * CELL_TG; c += blockDim.x) vts[c] = R(0.0);
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) grid[c] = P.grid[c];
-  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  if (!kMixed)
+    for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  if (kMixed) {
+    const int rows[4] = {GF_RDGZ, GF_RDGZH, GF_RDZS, GF_RDZSH};
+    for (int c = threadIdx.x; c < 4 * K; c += blockDim.x) gridf[c] = (float)P.grid[rows[c / K] * K + c % K];
+  }
   __syncthreads();
   const M mth = make_math<M>(tab);
 
   const int nlev = kmax - kmin + 1;
-  for (int c = threadIdx.x; c < nlev * CELL_TG; c += blockDim.x) {
+  const int ncell = nlev * CELL_TG;
+  // FP64: the tile's cells are grouped by the hydrometeors they hold (snow,
+  // rain, graupel, ice, cloud water: the blocks nsw6_cell skips when a species
+  // is absent), so that warps are uniform and skip those blocks together.  The
+  // order only decides which thread computes which cell.
+  int nvalid = ncell;
+  if (!kMixed) {
+    for (int c = threadIdx.x; c < 33; c += blockDim.x) bucket[c] = 0;
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+      const int k = kmin + c / CELL_TG;
+      const int g = g0 + c % CELL_TG;
+      int kk = 32;   // columns past the region's end go last
+      if (g < G) {
+        const size_t iq = offq + (size_t)k * G + g;
+        kk = (P.rhogq[iq + (size_t)I_QS * KG] > 0.0 ? 16 : 0) | (P.rhogq[iq + (size_t)I_QR * KG] > 0.0 ? 8 : 0) |
+             (P.rhogq[iq + (size_t)I_QG * KG] > 0.0 ? 4 : 0) | (P.rhogq[iq + (size_t)I_QI * KG] > 0.0 ? 2 : 0) |
+             (P.rhogq[iq + (size_t)I_QC * KG] > 0.0 ? 1 : 0);
+      }
+      key[c] = (unsigned char)kk;
+      atomicAdd(&bucket[kk], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = 0;
+      for (int b = 0; b < 33; ++b) {
+        const int n = bucket[b];
+        bucket[b] = run;
+        run += n;
+      }
+    }
+    __syncthreads();
+    nvalid = bucket[32];   // cells of columns inside the region
+    __syncthreads();
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) perm[atomicAdd(&bucket[key[c]], 1)] = (unsigned short)c;
+    __syncthreads();
+  }
+  for (int j = threadIdx.x; j < nvalid; j += blockDim.x) {
+    const int c = kMixed ? j : perm[j];
     const int k = kmin + c / CELL_TG;
     const int gx = c % CELL_TG;
     const int g = g0 + gx;
@@ -99,9 +159,9 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
     for (int n = 1; n < 6; ++n) P.q[iq + (size_t)n * KG] = o.q[n];
     P.re_liquid[i] = o.rceff;
     P.re_cld[i] = o.rceff_cld;
-    vts[(0 * K + k) * CELL_TG + gx] = o.Vtr;
-    vts[(1 * K + k) * CELL_TG + gx] = o.Vts;
-    vts[(2 * K + k) * CELL_TG + gx] = o.Vtg;
+    vts[(0 * K + k) * CELL_TG + gx] = R(o.Vtr);
+    vts[(1 * K + k) * CELL_TG + gx] = R(o.Vts);
+    vts[(2 * K + k) * CELL_TG + gx] = R(o.Vtg);
     if (k == kmax) {
       // The reference writes the cloud-top scalars from every level in parallel
       // (mod_mp_nsw6.cpp:1579-1592); the sequential order, in which the top
@@ -118,10 +178,22 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
   // Departure distances (vadv1d_prep) and their per-level region extrema.
   // Row s = t + 3*half: t = QR, QS, QG; half = 0 full levels (mkmin = kmin,
   // dz = dgz), 1 half levels (mkmin = kmin+1, dz = dgzh, wp = Vtermh).
-  const double* rdgz = grid + GF_RDGZ * K;
-  const double* rdgzh = grid + GF_RDGZH * K;
-  const double* rdzs = grid + GF_RDZS * K;
-  const double* rdzsh = grid + GF_RDZSH * K;
+  const R* rdgz;
+  const R* rdgzh;
+  const R* rdzs;
+  const R* rdzsh;
+  if constexpr (kMixed) {
+    rdgz = gridf;
+    rdgzh = gridf + K;
+    rdzs = gridf + 2 * K;
+    rdzsh = gridf + 3 * K;
+  } else {
+    rdgz = grid + GF_RDGZ * K;
+    rdgzh = grid + GF_RDGZH * K;
+    rdzs = grid + GF_RDZS * K;
+    rdzsh = grid + GF_RDZSH * K;
+  }
+  const R dtR = R(P.dt), hdt2R = R(P.hdt2), sdt3R = R(P.sdt3);
   for (int c = threadIdx.x; c < 6 * K * CELL_TG; c += blockDim.x) {
     const int s = c / (K * CELL_TG);
     const int rem = c - s * K * CELL_TG;
@@ -133,18 +205,18 @@ __global__ void __launch_bounds__(CELL_THREADS) nsw6_cell_kernel(Problem P, Cons
     if (k < mkmin || k > kmax) continue;  // uniform across the warp (CELL_TG == 32)
     const int g = g0 + gx;
     const bool valid = g < G;
-    const double* col = vts + t * K * CELL_TG + gx;
+    const R* col = vts + t * K * CELL_TG + gx;
     double z = 0.0;
     if (valid) {
       if (!half) {
         auto wp = [&](int j) { return col[j * CELL_TG]; };
-        z = vadv_zdis(wp, rdgz, rdzs, k, mkmin, kmax, P.dt, P.hdt2, P.sdt3);
+        z = double(vadv_zdis<R>(wp, rdgz, rdzs, k, mkmin, kmax, dtR, hdt2R, sdt3R));
       } else {
         // Vtermh, mod_precip_transport.cpp:847-861
         auto wp = [&](int j) {
-          return (j >= kmin + 1 && j <= kmax - 1) ? 0.5 * (col[j * CELL_TG] + col[(j - 1) * CELL_TG]) : 0.0;
+          return (j >= kmin + 1 && j <= kmax - 1) ? R(0.5) * (col[j * CELL_TG] + col[(j - 1) * CELL_TG]) : R(0.0);
         };
-        z = vadv_zdis(wp, rdgzh, rdzsh, k, mkmin, kmax, P.dt, P.hdt2, P.sdt3);
+        z = double(vadv_zdis<R>(wp, rdgzh, rdzsh, k, mkmin, kmax, dtR, hdt2R, sdt3R));
       }
       P.zdis[((size_t)l * 6 + s) * KG + (size_t)k * G + g] = z;
     }
@@ -186,17 +258,23 @@ struct ColumnShared {
 // reference's tmp = k2 * copysign(1, dep - zh(k2)) * copysign(1, zh(k2+1) - dep)
 // is k2 when both signs agree and -k2 otherwise; the sign of a difference of
 // two doubles is their comparison, so the test is exact integer logic.
-__device__ __forceinline__ int departure_cell(const double* zh, int k, double zdis, int bmn, int bmx, int mkmin,
-                                              int mkmax) {
+//
+// The comparisons run on the integer pipe: zk holds cmp_key of the interface
+// heights zh, and for non-NaN doubles a >= b exactly when their keys compare
+// so; a NaN departure point makes every comparison false, as in the reference.
+__device__ __forceinline__ int departure_cell(const double* zh, const long long* zk, int k, double zdis, int bmn,
+                                              int bmx, int mkmin, int mkmax) {
   int kc;
   if (bmn == k && bmx == k) {
     kc = k;
   } else {
     kc = 0;
     const double dep = zh[k] - zdis;
+    const long long dk = cmp_key(dep);
+    const bool nan = is_nan_bits(dep);
     for (int k2 = bmn; k2 <= bmx; ++k2) {
-      const bool s1 = dep >= zh[k2];
-      const bool s2 = zh[k2 + 1] >= dep;
+      const bool s1 = !nan && dk >= zk[k2];
+      const bool s2 = !nan && zk[k2 + 1] >= dk;
       const int tmp = (s1 == s2) ? k2 : -k2;
       kc = kc > tmp ? kc : tmp;
     }
@@ -224,10 +302,32 @@ __device__ __forceinline__ double flux_integral(const double* rhof_col, const do
     if (bmx != kc) zdis = zdis0 - (bmx > kc ? dz[bmx] : -dz[bmx]);
   }
   f = __fma_rn(rhof_col[kc * TG], zdis, f);
-  return fabs(f) >= EPS ? f : 0.0;
+  // |f| >= EPS on the integer pipe (NaN fails, as the comparison does)
+  const long long ab = __double_as_longlong(f) & 0x7fffffffffffffffLL;
+  return (ab >= EPS_BITS && ab <= 0x7ff0000000000000LL) ? f : 0.0;
 }
 
-template <int COL_TG, class M>
+// FP32 flux integral of the mixed path (momentum fluxes), same form.
+template <int TG>
+__device__ __forceinline__ float flux_integral_f(const float* rhof_col, const float* dz, int k, int kc, float zdis0,
+                                                 int bmn, int bmx) {
+  float f = 0.0f, zdis = zdis0;
+  if (!(bmn == k && bmx == k)) {
+    for (int k2 = bmn; k2 <= bmx; ++k2) {
+      if (k2 != kc) f = __fmaf_rn(rhof_col[k2 * TG], k2 > kc ? dz[k2] : -dz[k2], f);
+    }
+    if (bmx != kc) zdis = zdis0 - (bmx > kc ? dz[bmx] : -dz[bmx]);
+  }
+  f = __fmaf_rn(rhof_col[kc * TG], zdis, f);
+  return fabsf(f) >= (float)EPS ? f : 0.0f;
+}
+
+// MIX: the mixed-precision step: the momentum fluxes of the sedimentation (u,
+// v and w, full and half levels) are integrated and accumulated in FP32, and
+// the quotients of the final state use a plain reciprocal; the mass, energy
+// and kinetic-energy fluxes, their sums and the saturation adjustment stay
+// FP64.
+template <int COL_TG, class M, bool MIX>
 __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   extern __shared__ double smraw[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
@@ -248,9 +348,20 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   S.kc = reinterpret_cast<unsigned char*>(S.bmax + 6 * K);
   double* tab = reinterpret_cast<double*>(
       (reinterpret_cast<uintptr_t>(S.kc + (size_t)K * COL_TG) + 15) & ~(uintptr_t)15);
+  long long* zkey = reinterpret_cast<long long*>(tab + FM_TABLE_DOUBLES);   // [2][K]: cmp_key of gzh, gzshift
+  float* gf = reinterpret_cast<float*>(zkey + 2 * K);   // MIX: dgz, dgzh, rdgz, rdgzh in FP32
   auto F = [&](int slot) { return S.f + (size_t)slot * ncell; };
+  // FP32 views of slots (MIX): the flux source and flux of the momentum
+  // passes, and the momentum accumulators
+  auto FF = [&](int slot) { return reinterpret_cast<float*>(S.f + (size_t)slot * ncell); };
 
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) S.grid[c] = P.grid[c];
+  for (int c = threadIdx.x; c < 2 * K; c += blockDim.x)
+    zkey[c] = cmp_key(P.grid[(c < K ? GF_GZH : GF_GZSHIFT) * K + c % K]);
+  if (MIX) {
+    const int rows[4] = {GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH};
+    for (int c = threadIdx.x; c < 4 * K; c += blockDim.x) gf[c] = (float)P.grid[rows[c / K] * K + c % K];
+  }
   for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) S.colacc[c] = 0.0;
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
@@ -353,11 +464,41 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       if (g >= G) continue;
       const size_t i = (size_t)k * G + g;
       F(S_BASE)[c] = rhogq_n[i] * F(S_RGS)[c];
-      if (k >= kmin && k <= kmax) S.kc[c] = (unsigned char)departure_cell(gzh, k, zdis0[i], bmn_f[k], bmx_f[k], kmin, kmax);
+      if (k >= kmin && k <= kmax)
+        S.kc[c] = (unsigned char)departure_cell(gzh, zkey, k, zdis0[i], bmn_f[k], bmx_f[k], kmin, kmax);
     }
     __syncthreads();
 
     for (int f = 0; f < 6; ++f) {
+      if (MIX && f >= 4) {
+        // momentum fluxes in FP32
+        float* rf = FF(S_RHOF);
+        float* ff = FF(S_F);
+        float* acc = FF(f == 4 ? S_DRHOGU : S_DRHOGV);
+        const float* dgzf = gf;
+        const float* rdgzf = gf + 2 * K;
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int gx = c % COL_TG, g = g0 + gx;
+          rf[c] = (g < G) ? (float)(F(S_BASE)[c] * F(f == 4 ? S_VI : S_VJ)[c]) : 0.0f;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          float fl = 0.0f;
+          if (g < G && k >= kmin && k <= kmax)
+            fl = flux_integral_f<COL_TG>(rf + gx, dgzf, k, S.kc[c], (float)zdis0[(size_t)k * G + g], bmn_f[k],
+                                         bmx_f[k]);
+          ff[c] = fl;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          if (g >= G || k < kmin || k > kmax) continue;
+          acc[c] = acc[c] - (ff[c + COL_TG] - ff[c]) * rdgzf[k];
+        }
+        __syncthreads();
+        continue;
+      }
       // flux source: q, e, phi, kin_h, u, v (mod_precip_transport.cpp:776-808)
       for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
         const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
@@ -430,13 +571,36 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       if (g < G && k >= kmin + 1 && k <= kmax) {
         const size_t i = off + (size_t)k * G + g;
         qh = 0.5 * (q_n[i - off] + q_n[i - off - G]) * (P.gam2h[i] / P.gsgam2h[i]);
-        S.kc[c] = (unsigned char)departure_cell(gzs, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
+        S.kc[c] = (unsigned char)departure_cell(gzs, zkey + K, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
       }
       F(S_BASE)[c] = qh;
       F(S_RHOF)[c] = qh * F(S_KINV)[c];
     }
     __syncthreads();
     for (int w = 0; w < 2; ++w) {
+      if (MIX && w == 1) {
+        // momentum w in FP32 (its source was written as FP32 by the w = 0 pass)
+        const float* rf = FF(S_RHOF);
+        float* ff = FF(S_F);
+        float* acc = FF(S_DRHOGW);
+        const float* dgzhf = gf + K;
+        const float* rdgzhf = gf + 3 * K;
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          float fl = 0.0f;
+          if (g < G && k >= kmin + 1 && k <= kmax)
+            fl = flux_integral_f<COL_TG>(rf + gx, dgzhf, k, S.kc[c], (float)zdis0h[(size_t)k * G + g], bmn_h[k],
+                                         bmx_f[k]);
+          ff[c] = fl;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          if (g < G && k >= kmin + 1 && k <= kmax) acc[c] = acc[c] - (ff[c] - ff[c - COL_TG]) * rdgzhf[k];
+        }
+        __syncthreads();
+        continue;
+      }
       // vertical kinetic energy (w = 0) and momentum w (w = 1); the reference
       // passes the full-level kcell_max as the upper bound (:890, :892)
       for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
@@ -457,7 +621,8 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         if (w == 0) {
           double r = 0.0;
           if (g < G && k >= kmin + 1 && k <= kmax) r = F(S_BASE)[c] * P.rhogw[off + (size_t)k * G + g];
-          F(S_RHOF)[c] = r;
+          if (MIX) FF(S_RHOF)[c] = (float)r;
+          else F(S_RHOF)[c] = r;
         }
       }
       __syncthreads();
@@ -475,13 +640,14 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     double rhoge = P.rhoge[i] + F(S_DRHOE)[c] + F(S_DRHOPHI)[c];
     F(S_KINH)[c] = F(S_KINH)[c] + F(S_DKINH)[c];
     F(S_KINV)[c] = F(S_KINV)[c] + F(S_DKINV)[c];
-    const double du = F(S_DRHOGU)[c], dv = F(S_DRHOGV)[c];
+    const double du = MIX ? (double)FF(S_DRHOGU)[c] : F(S_DRHOGU)[c];
+    const double dv = MIX ? (double)FF(S_DRHOGV)[c] : F(S_DRHOGV)[c];
     P.rhogvx[i] = P.rhogvx[i] + du * P.ix[ic] + dv * P.jx[ic];
     P.rhogvy[i] = P.rhogvy[i] + du * P.iy[ic] + dv * P.jy[ic];
     P.rhogvz[i] = P.rhogvz[i] + du * P.iz[ic] + dv * P.jz[ic];
-    const double rw = P.rhogw[i] + F(S_DRHOGW)[c];
+    const double rw = P.rhogw[i] + (MIX ? (double)FF(S_DRHOGW)[c] : F(S_DRHOGW)[c]);
     P.rhogw[i] = rw;
-    F(S_DRHOGW)[c] = rw;
+    if (!MIX) F(S_DRHOGW)[c] = rw;   // MIX: the FP32 view of this slot is still being read
     // tracers in order QV..QG; QV, QC and QI add exact zeros
     double rhog = P.rhog[i];
     const double zz = P.z[i];
@@ -512,14 +678,15 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     if (g >= G) continue;
     const size_t i = off + (size_t)k * G + g;
     if (k >= kmin && k <= kmax) {
-      const double w2c0 = cfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
-      const double w2c1 = dfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
+      const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
+      const double w2c0 = div_rn(cfact[k] * P.gsgam2[i], gh, rgh);
+      const double w2c1 = div_rn(dfact[k] * P.gsgam2[i], gh, rgh);
       F(S_DRHOE)[c] = F(S_KINH)[c] + (w2c0 * F(S_KINV)[c + COL_TG] + w2c1 * F(S_KINV)[c]);
     }
     if (k >= kmin + 1 && k <= kmax) {
       const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
       const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
-      const double rw = F(S_DRHOGW)[c];
+      const double rw = MIX ? P.rhogw[i] : F(S_DRHOGW)[c];
       F(S_DRHOPHI)[c] = 0.5 * (rw * rw) / (c2w0 * F(S_RHOF)[c] + c2w1 * F(S_RHOF)[c - COL_TG]);
     }
   }
@@ -534,27 +701,32 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     const size_t iq = offq + (size_t)k * G + g;
     const bool interior = (k >= kmin && k <= kmax);
     const double rhog = F(S_RHOF)[c];
+    // Quotients by a shared denominator are formed from one reciprocal with a
+    // Markstein correction step (div_rn): correctly rounded, as the reference's
+    // divisions, at a third of the cost.
+    const double rrhog = 1.0 / rhog;
     double rhoge = P.rhoge[i];
     if (interior) {
       const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
-      const double tmp_h = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / rhog;
-      const double w2c0 = cfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
-      const double w2c1 = dfact[k] * P.gsgam2[i] / P.gsgam2h[i + G];
+      const double tmp_h = div_rn(0.5 * (rvx * rvx + rvy * rvy + rvz * rvz), rhog, rrhog);
+      const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
+      const double w2c0 = div_rn(cfact[k] * P.gsgam2[i], gh, rgh);
+      const double w2c1 = div_rn(dfact[k] * P.gsgam2[i], gh, rgh);
       const double tmp = tmp_h + (w2c0 * F(S_DRHOPHI)[c + COL_TG] + w2c1 * F(S_DRHOPHI)[c]);
       rhoge = rhoge + (F(S_DRHOE)[c] - tmp);
     }
     double rq[6], q[6];
 #pragma unroll
     for (int n = 0; n < 6; ++n) rq[n] = P.rhogq[iq + (size_t)n * KG];
-    // These quotients keep the reference's exact divisions: the saturation
-    // adjustment forms qc = qsum - qsat from them, a difference of nearly
-    // equal numbers in which one unit in the last place of qsum is already a
-    // relative error of 1e-11 when qc is small.
+    // These quotients must be correctly rounded: the saturation adjustment
+    // forms qc = qsum - qsat from them, a difference of nearly equal numbers
+    // in which one unit in the last place of qsum is already a relative error
+    // of 1e-11 when qc is small.
 #pragma unroll
-    for (int n = 0; n < 6; ++n) q[n] = rq[n] / rhog;
+    for (int n = 0; n < 6; ++n) q[n] = MIX ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
     const double gsg = P.gsgam2[i];
     double rho = rhog / gsg;
-    const double ein = rhoge / rhog;
+    const double ein = MIX ? rhoge * rrhog : div_rn(rhoge, rhog, rrhog);
     double qd = 1.0;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) qd = qd - q[n];
@@ -639,8 +811,9 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       diffq -= rq[I_QV];
       rhog_o = rhog * (1.0 - diffq);
       rho = rhog_o / gsg;
+      const double rrhog_o = 1.0 / rhog_o;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n) q[n] = rq[n] / rhog_o;
+      for (int n = 1; n <= 5; ++n) q[n] = MIX ? rq[n] * rrhog_o : div_rn(rq[n], rhog_o, rrhog_o);
       double qdf = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
@@ -711,8 +884,11 @@ cudaError_t launch_math(int fn, const double* x, const double* y, double* out, i
 }
 
 // ------------------------------------------------------------------ launchers
-size_t cell_smem_bytes(int K) {
-  return sizeof(double) * (size_t)(3 * K * CELL_TG + GF_COUNT * K + FM_TABLE_DOUBLES);
+size_t cell_smem_bytes(int K, bool mixed) {
+  const size_t vts = mixed ? cell_vts_doubles<float>(K) : cell_vts_doubles<double>(K);
+  // fall speeds, grid, tables, the FP32 reciprocal rows, the cell order and keys
+  return sizeof(double) * (vts + (size_t)GF_COUNT * K + FM_TABLE_DOUBLES) + sizeof(float) * 4 * K +
+         (sizeof(unsigned short) + 1) * (size_t)(K - 2) * CELL_TG;
 }
 
 int column_tile(int K) { return K <= 64 ? 16 : 8; }
@@ -720,7 +896,7 @@ int column_tile(int K) { return K <= 64 ? 16 : 8; }
 size_t column_smem_bytes(int K) {
   const int TG = column_tile(K);
   return sizeof(double) * ((size_t)S_COUNT * K * TG + GF_COUNT * K + 6 * TG + FM_TABLE_DOUBLES) +
-         sizeof(int) * 12 * K + (size_t)K * TG + 16;
+         sizeof(int) * 12 * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 4 * K;
 }
 
 int column_threads(int K) {
@@ -731,38 +907,72 @@ int column_threads(int K) {
   return per > 256 ? 256 : per;
 }
 
-cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev) {
+// The cell kernel alone (FP64): used on a copy of a state to obtain the
+// region extrema of the departure distances for the derivative kernels.
+cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t stream) {
   const size_t nkey = (size_t)P.lall * 6 * P.kall;
   cudaError_t e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  const size_t s1 = cell_smem_bytes(P.kall);
-  const size_t s2 = column_smem_bytes(P.kall);
+  cudaFuncSetAttribute(nsw6_cell_kernel<FastMath, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
+  nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, cell_smem_bytes(P.kall, false), stream>>>(P, C);
+  return cudaGetLastError();
+}
+
+// Opt-in shared-memory limits of the step kernels (once per process; before
+// any stream capture of a step).
+cudaError_t launch_prepare() {
   static bool attr_done = false;
   if (!attr_done) {
-    cudaFuncSetAttribute(nsw6_cell_kernel<FastMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(nsw6_cell_kernel<LibMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<16, FastMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<8, FastMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<16, LibMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<8, LibMath>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaFuncSetAttribute(nsw6_cell_kernel<FastMath, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(nsw6_cell_kernel<LibMath, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(nsw6_cell_kernel<FloatMath, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<16, FastMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<8, FastMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<16, LibMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<8, LibMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<16, FastMath, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
+    cudaFuncSetAttribute(nsw6_column_kernel<8, FastMath, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         227 * 1024);
     attr_done = true;
   }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev) {
+  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  cudaError_t e = launch_prepare();
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
+  if (e != cudaSuccess) return e;
+  const size_t s1 = cell_smem_bytes(P.kall, P.mixed != 0);
+  const size_t s2 = column_smem_bytes(P.kall);
   dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
   if (ev) cudaEventRecord(ev[0], stream);
-  if (P.math_lib) nsw6_cell_kernel<LibMath><<<g1, CELL_THREADS, s1, stream>>>(P, C);
-  else nsw6_cell_kernel<FastMath><<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  if (P.mixed) nsw6_cell_kernel<FloatMath, float><<<g1, CELL_THREADS, s1, stream>>>(P, consts_to_float(C));
+  else if (P.math_lib) nsw6_cell_kernel<LibMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  else nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   if (ev) cudaEventRecord(ev[1], stream);
   const int tg = column_tile(P.kall);
   dim3 g2((P.gall + tg - 1) / tg, P.lall);
   const int nt = column_threads(P.kall);
   if (tg == 16) {
-    if (P.math_lib) nsw6_column_kernel<16, LibMath><<<g2, nt, s2, stream>>>(P, C);
-    else nsw6_column_kernel<16, FastMath><<<g2, nt, s2, stream>>>(P, C);
+    if (P.mixed) nsw6_column_kernel<16, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
+    else if (P.math_lib) nsw6_column_kernel<16, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
+    else nsw6_column_kernel<16, FastMath, false><<<g2, nt, s2, stream>>>(P, C);
   } else {
-    if (P.math_lib) nsw6_column_kernel<8, LibMath><<<g2, nt, s2, stream>>>(P, C);
-    else nsw6_column_kernel<8, FastMath><<<g2, nt, s2, stream>>>(P, C);
+    if (P.mixed) nsw6_column_kernel<8, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
+    else if (P.math_lib) nsw6_column_kernel<8, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
+    else nsw6_column_kernel<8, FastMath, false><<<g2, nt, s2, stream>>>(P, C);
   }
   if (ev) cudaEventRecord(ev[2], stream);
   return cudaGetLastError();

@@ -19,6 +19,7 @@
 #include <string>
 
 #include "problemsize.h"
+#include "data_io.h"
 #include "mod_debug.h"
 #include "mod_satadjust.h"
 #include "mod_mp_driver.h"
@@ -167,6 +168,25 @@ int nsw6ref_mp_driver(int l_region, double* const* a, double dt, double ct) {
                        v2(46), v2(47), v2(48), v2(49));           // GDCLW GDCFRC GPREC CBMFX
   const int n = Kokkos::shim::abort_count().load() - before;
   return n == 0 ? 0 : 10 + n;
+}
+
+// The reference's own snapshot readers (src/data_io.cpp), for checking the
+// package's snapshot module against them: out receives the file's contents in
+// the harness's array layout (ADM_lall = 1 in these builds).
+void nsw6ref_read_1d(const char* fname, double* out) {
+  DATA_IO::read_data_1d(fname, out);
+}
+void nsw6ref_read_2d(const char* fname, double* out) {
+  DATA_IO::read_data_2d(fname, reinterpret_cast<double(*)[ADM_gall_in]>(out));
+}
+void nsw6ref_read_3d(const char* fname, double* out) {
+  DATA_IO::read_data_3d(fname, reinterpret_cast<double(*)[ADM_kall][ADM_gall_in]>(out));
+}
+void nsw6ref_read_4d(const char* fname, double* out) {
+  DATA_IO::read_data_4d(fname, reinterpret_cast<double(*)[TRC_VMAX][ADM_kall][ADM_gall_in]>(out));
+}
+void nsw6ref_read_precip(const char* fname, double* out) {
+  DATA_IO::read_data_4d(fname, reinterpret_cast<double(*)[ADM_lall][ADM_KNONE][ADM_gall_in]>(out));
 }
 
 }  // extern "C"

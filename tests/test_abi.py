@@ -45,3 +45,14 @@ def test_bad_arguments_rejected(lib):
     assert lib.nsw6_create(ctypes.byref(h), 0, 42, 1, gz, gz) == 1
     assert lib.nsw6_create(ctypes.byref(h), 10, 3, 1, gz, gz) == 1
     assert lib.mp_driver_argv(None, 1, None, ctypes.c_double(60.0), ctypes.c_double(0.0), 0) == 1
+
+
+def test_eps_bit_pattern_matches_eps():
+    """The integer-pipe |f| >= EPS test of the column kernel uses EPS's bit pattern."""
+    import re
+    import struct
+    from nicam_kokkos_microphysics_gb300 import _native
+    text = (_native.CSRC / "nsw6_common.cuh").read_text()
+    eps = float(re.search(r"constexpr double EPS = ([0-9.Ee+-]+);", text).group(1))
+    bits = int(re.search(r"constexpr long long EPS_BITS = (0x[0-9a-fA-F]+)LL;", text).group(1), 16)
+    assert struct.unpack("<q", struct.pack("<d", eps))[0] == bits

@@ -1,0 +1,256 @@
+"""Tangent-linear and adjoint steps (mp_driver_tlm / mp_driver_adjoint).
+
+* their forward, the FP64 step evaluated one column per thread, equals the
+  production kernels bit for bit;
+* adjoint dot-product test: <ybar, TLM dx> = <ADJ ybar, dx> + <pbar, dp>;
+* the gradient of the loss L = sum_g (precip_rain + precip_solid)^2 +
+  sum_{g,k} rhogq[QC] dgz(k) (surface precipitation and column-integrated
+  cloud water) with respect to state components and the seven NSW6 parameters
+  against FP64 central finite differences of the production step (relative
+  step 1e-6), at points away from the scheme's switches: a point is used when
+  the differences with steps h and h/4 agree (no switch flips in between).
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from nicam_kokkos_microphysics_gb300.autograd import READ_NAMES, WRITE_NAMES
+from nicam_kokkos_microphysics_gb300.state import ARG_NAMES, OUTPUT_NAMES, StateSpec, make_state, vertical_grid
+
+pytestmark = pytest.mark.gpu
+PARAMS = ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg", "ice_nuc", "kk_aut"]
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _setup(gall=4096, kall=42, lall=1, seed=2024, variant="standard"):
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=gall, kall=kall, lall=lall, seed=seed, variant=variant)
+    st = make_state(spec, out_fill=0.0)
+    drv = mp_init("NSW6", gall, kall, st["_gz"], st["_gzh"], lall_max=lall)
+    x0 = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    return torch, drv, spec, st, x0
+
+
+def _clone(d):
+    return {k: v.clone() for k, v in d.items()}
+
+
+@pytest.mark.parametrize("variant,gall,kall", [("standard", 500, 42), ("convective", 500, 42), ("cold", 300, 42),
+                                               ("convective", 129, 12)])
+def test_serial_forward_bitwise_equals_production(variant, gall, kall):
+    torch, drv, spec, st, x0 = _setup(gall, kall, 2, 11, variant)
+    a, b = _clone(x0), _clone(x0)
+    drv.mp_driver_batched(spec.lall, *[a[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.set_precision("serial")
+    drv.mp_driver_batched(spec.lall, *[b[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        assert torch.equal(a[n], b[n]), n
+    drv.close()
+
+
+def test_adjoint_dot_product():
+    torch, drv, spec, st, x0 = _setup(1024, 42, 1, 77, "convective")
+    g = torch.Generator(device="cuda").manual_seed(5)
+    dx = {n: torch.zeros_like(v) for n, v in x0.items()}
+    for n in READ_NAMES:
+        dx[n] = 1e-3 * x0[n].abs().mean() * torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64)
+    dp = np.array([1e-5, 1e-7, 1.0, 0.05, 0.5, 1e-13, 10.0])
+    ybar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    for n in WRITE_NAMES:
+        ybar[n] = torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64) / \
+            (x0[n].abs().mean() + 1e-30)
+    # TLM
+    x, t = _clone(x0), _clone(dx)
+    drv.tlm(spec.lall, x, t, dparams=dp, dt=spec.dt)
+    lhs = sum(float((ybar[n] * t[n]).sum()) for n in WRITE_NAMES)
+    # adjoint
+    bar = _clone(ybar)
+    pbar = drv.adjoint(spec.lall, _clone(x0), bar, dt=spec.dt)
+    rhs = sum(float((bar[n] * dx[n]).sum()) for n in READ_NAMES) + float(np.dot(pbar, dp))
+    print(f"\ndot-product test: <ybar, J dx> = {lhs:.17e}, <J^T ybar, dx> = {rhs:.17e}, "
+          f"rel diff {abs(lhs - rhs) / abs(lhs):.2e}")
+    assert abs(lhs - rhs) <= 1e-11 * abs(lhs)
+    # the TLM's forward is the FP64 step
+    y = _clone(x0)
+    drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    for n in OUTPUT_NAMES:
+        assert torch.equal(y[n], x[n]), n
+    drv.close()
+
+
+def _loss_terms(torch, spec):
+    gz, gzh = vertical_grid(spec.kall)
+    dgz = torch.tensor(np.diff(gzh, append=gzh[-1] + (gzh[-1] - gzh[-2])), dtype=torch.float64, device="cuda")
+    w = torch.zeros(spec.kall, dtype=torch.float64, device="cuda")
+    w[1:spec.kall - 1] = dgz[1:spec.kall - 1]
+    return w
+
+
+def _loss(torch, y, w):
+    p = y["precip"][0] + y["precip"][1]
+    return float((p * p).sum() + (y["rhogq"][:, 1] * w[None, :, None]).sum())
+
+
+def _loss_diff(torch, yp, ym, w):
+    """L(yp) - L(ym) summed term by term (no cancellation against the total)."""
+    pp = yp["precip"][0] + yp["precip"][1]
+    pm = ym["precip"][0] + ym["precip"][1]
+    return float(((pp - pm) * (pp + pm)).sum() + ((yp["rhogq"][:, 1] - ym["rhogq"][:, 1]) * w[None, :, None]).sum())
+
+
+def test_gradient_against_finite_differences():
+    torch, drv, spec, st, x0 = _setup(4096, 42, 1, 2024, "standard")
+    w = _loss_terms(torch, spec)
+
+    def forward(x):
+        y = _clone(x)
+        drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        return y
+
+    y0 = forward(x0)
+    bar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    bar["precip"] = 2.0 * (y0["precip"][0] + y0["precip"][1]).unsqueeze(0).expand_as(y0["precip"]).contiguous()
+    bar["rhogq"][:, 1] = w[None, :, None].expand(spec.lall, spec.kall, spec.gall)
+    pbar = drv.adjoint(spec.lall, _clone(x0), bar, dt=spec.dt)
+
+    def fd(setter, h):
+        xp, xm = _clone(x0), _clone(x0)
+        setter(xp, +h)
+        setter(xm, -h)
+        return _loss_diff(torch, forward(xp), forward(xm), w) / (2 * h)
+
+    rng = np.random.default_rng(3)
+    # columns with rain reaching the surface, where the loss is sensitive
+    prc = (y0["precip"][0, 0] + y0["precip"][1, 0]).abs().cpu().numpy()
+    cols = rng.choice(np.argsort(prc)[-400:], 16, replace=False)
+    checked = skipped = unresolved = 0
+    worst = 0.0
+    fields = (("tem", lambda k, g: (0, k, g), None), ("q", lambda k, g: (0, 0, k, g), 0),
+              ("rhogq", lambda k, g: (0, 2, k, g), 2), ("rhog", lambda k, g: (0, k, g), None))
+    for g in cols:
+        for name, idx, nq in fields:
+            # the level where the loss is most sensitive to this field
+            gcol = bar[name][0, :, g] if nq is None else bar[name][0, nq, :, g]
+            k = int(gcol[1:spec.kall - 1].abs().argmax()) + 1
+            ix = idx(k, int(g))
+            x = float(x0[name][ix])
+            h = 1e-6 * abs(x)
+            adj = float(bar[name][ix])
+            if h == 0.0:   # a zero value has no relative step
+                unresolved += 1
+                continue
+
+            def setter(xx, d, name=name, ix=ix):
+                xx[name][ix] += d
+
+            # rounding noise of the difference of this column's loss terms
+            pcol = float((y0["precip"][0, 0, g] + y0["precip"][1, 0, g]) ** 2)
+            qcol = float((y0["rhogq"][0, 1, :, g].abs() * w).sum())
+            noise = 4e-16 * (pcol + qcol) / h
+            if abs(adj) < 1e4 * noise:   # a 1e-6 relative step cannot resolve this derivative
+                unresolved += 1
+                continue
+            a1, a2 = fd(setter, h), fd(setter, h / 4)
+            scale = max(abs(a1), abs(adj), 1e-300)
+            if abs(a1 - a2) > 1e-6 * scale:   # a switch flips between the FD points
+                skipped += 1
+                continue
+            checked += 1
+            err = abs(adj - a1) / scale
+            worst = max(worst, err)
+            print(f"  d L / d {name}{ix}: adjoint {adj:+.10e}  FD {a1:+.10e}  rel {err:.1e}")
+            assert err <= 1e-6, (name, ix, adj, a1)
+    # the seven parameters
+    Ltot = float((y0["precip"][0] + y0["precip"][1]).pow(2).sum() + (y0["rhogq"][:, 1].abs() * w[None, :, None]).sum())
+    base = drv.get_params()
+    for i, pn in enumerate(PARAMS):
+        p0 = base[pn]
+        h = 1e-6 * abs(p0) if p0 != 0 else 1e-9   # qicrt_saut is 0: an absolute step of 1e-9 kg/kg
+        if abs(pbar[i]) < 1e4 * 4e-16 * Ltot / h:
+            unresolved += 1
+            continue
+
+        def yp(v):
+            drv.set_params(**{pn: v})
+            out = forward(x0)
+            drv.set_params(**{pn: p0})
+            return out
+
+        a1 = _loss_diff(torch, yp(p0 + h), yp(p0 - h), w) / (2 * h)
+        a2 = _loss_diff(torch, yp(p0 + h / 4), yp(p0 - h / 4), w) / (h / 2)
+        scale = max(abs(a1), abs(pbar[i]), 1e-300)
+        if abs(a1 - a2) > 1e-6 * scale:
+            skipped += 1
+            continue
+        checked += 1
+        err = abs(pbar[i] - a1) / scale
+        worst = max(worst, err)
+        print(f"  d L / d {pn}: adjoint {pbar[i]:+.10e}  FD {a1:+.10e}  rel {err:.1e}")
+        assert err <= 1e-6, (pn, pbar[i], a1)
+    print(f"\ngradient vs FD: {checked} components checked, {skipped} next to a switch, {unresolved} below the "
+          f"resolution of the step, worst rel err {worst:.2e}")
+    assert checked >= 20
+    drv.close()
+
+
+def test_window_gradient_against_finite_differences():
+    """Three-step window with checkpoints: gradient of the accumulated surface
+    precipitation with respect to the initial temperature and vapour and the
+    parameters, against term-wise central differences of the FP64 window."""
+    torch, drv, spec, st, x0 = _setup(512, 42, 1, 99, "convective")
+    from nicam_kokkos_microphysics_gb300.window import window_gradient
+    nsteps = 3
+    res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision="fp64")
+    bar, pbar = res["grad"], res["dparams"]
+
+    def precip_series(x):
+        y = _clone(x)
+        out = []
+        for _ in range(nsteps):
+            drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+            out.append((y["precip"][0] + y["precip"][1]).clone())
+        return out
+
+    def dJ(xp, xm):
+        sp, sm = precip_series(xp), precip_series(xm)
+        return float(sum((a - b).sum() for a, b in zip(sp, sm))) * spec.dt
+
+    y1 = _clone(x0)
+    drv.mp_driver_batched(spec.lall, *[y1[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    prc = (y1["precip"][0, 0] + y1["precip"][1, 0]).abs().cpu().numpy()
+    rng = np.random.default_rng(8)
+    checked = skipped = 0
+    for g in rng.choice(np.argsort(prc)[-64:], 8, replace=False):
+        for name, nq in (("tem", None), ("q", 0)):
+            gcol = bar[name][0, :, g] if nq is None else bar[name][0, nq, :, g]
+            k = int(gcol[1:spec.kall - 1].abs().argmax()) + 1   # the most sensitive level
+            ix = (0, k, int(g)) if nq is None else (0, nq, k, int(g))
+            h = 1e-6 * abs(float(x0[name][ix]))
+            vals = []
+            for hh in (h, h / 4):
+                xp, xm = _clone(x0), _clone(x0)
+                xp[name][ix] += hh
+                xm[name][ix] -= hh
+                vals.append(dJ(xp, xm) / (2 * hh))
+            adj = float(bar[name][ix])
+            scale = max(abs(vals[0]), abs(adj), 1e-300)
+            if abs(vals[0] - vals[1]) > 1e-6 * scale or scale < 1e-25:
+                skipped += 1
+                continue
+            checked += 1
+            err = abs(adj - vals[0]) / scale
+            print(f"  window dJ/d{name}{ix}: adjoint {adj:+.10e} FD {vals[0]:+.10e} rel {err:.1e}")
+            assert err <= 1e-6, (name, ix, adj, vals[0])
+    print(f"\nwindow gradient: {checked} checked, {skipped} next to a switch; J = {res['J']:.6e}; "
+          f"forward {res['t_forward'] * 1e3:.1f} ms, adjoint {res['t_adjoint'] * 1e3:.1f} ms")
+    assert checked >= 6
+    drv.close()

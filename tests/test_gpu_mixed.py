@@ -1,0 +1,89 @@
+"""Mixed-precision step (FP32 process rates; FP64 budgets, flux sums and
+saturation adjustment) against the FP64 path on full 130 x 130 regions.
+
+Targets: surface precipitation within 1e-5 and hydrometeor mixing ratios
+within 1e-4 relative error, measured per field as max |mixed - fp64| /
+max |fp64| and as the mean per-cell relative error over cells holding at
+least 1e-3 of the field's maximum.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from nicam_kokkos_microphysics_gb300.state import ARG_NAMES, OUTPUT_NAMES, StateSpec, make_state, region_view
+
+pytestmark = pytest.mark.gpu
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def errors(a: np.ndarray, b: np.ndarray) -> tuple[float, float]:
+    d = np.abs(a - b)
+    bmax = np.abs(b).max()
+    if bmax == 0:
+        return float(d.max()), 0.0
+    sig = np.abs(b) >= 1e-3 * bmax
+    return float(d.max() / bmax), float((d[sig] / np.abs(b[sig])).mean())
+
+
+def run_both(spec):
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    st = make_state(spec, out_fill=0.0)
+    reg = region_view(st, 0)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"])
+    a = {n: torch.from_numpy(np.ascontiguousarray(reg[n])).cuda() for n in ARG_NAMES}
+    b = {n: t.clone() for n, t in a.items()}
+    drv.mp_driver(0, *[a[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.mp_driver_mixed(0, *[b[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    torch.cuda.synchronize()
+    drv.close()
+    return ({n: a[n].cpu().numpy() for n in OUTPUT_NAMES}, {n: b[n].cpu().numpy() for n in OUTPUT_NAMES})
+
+
+@pytest.mark.parametrize("variant,seed", [("standard", 1001), ("convective", 1002), ("cold", 1003)])
+def test_mixed_within_targets(variant, seed):
+    fp64, mixed = run_both(StateSpec(gall=16900, kall=42, lall=1, seed=seed, variant=variant))
+    lines = []
+    for n in OUTPUT_NAMES:
+        assert np.isfinite(mixed[n]).all(), n
+    for s, sp in enumerate(["QC", "QR", "QI", "QS", "QG"], start=1):
+        mx, mean = errors(mixed["q"][s], fp64["q"][s])
+        lines.append(f"q[{sp}] max {mx:.2e} mean {mean:.2e}")
+        assert mx <= 1e-4 and mean <= 1e-4, lines[-1]
+    mx, mean = errors(mixed["precip"], fp64["precip"])
+    lines.append(f"precip max {mx:.2e} mean {mean:.2e}")
+    assert mx <= 1e-5 and mean <= 1e-5, lines[-1]
+    for n in ("rhog", "rhoge", "tem", "rhogvx", "rhogw"):
+        mx, mean = errors(mixed[n], fp64[n])
+        lines.append(f"{n} max {mx:.2e} mean {mean:.2e}")
+        assert mx <= 1e-5, lines[-1]
+    print(f"\n[{variant}] " + "; ".join(lines))
+
+
+def test_mixed_entry_equals_precision_switch():
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=700, kall=42, lall=1, seed=5, variant="convective")
+    st = make_state(spec, out_fill=0.0)
+    reg = region_view(st, 0)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"])
+    a = {n: torch.from_numpy(np.ascontiguousarray(reg[n])).cuda() for n in ARG_NAMES}
+    b = {n: t.clone() for n, t in a.items()}
+    c = {n: t.clone() for n, t in a.items()}
+    drv.mp_driver_mixed(0, *[a[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.set_precision("mixed")
+    drv.mp_driver(0, *[b[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.set_precision("fp64")
+    drv.mp_driver(0, *[c[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        assert torch.equal(a[n], b[n]), n
+    assert not torch.equal(a["rhogq"], c["rhogq"])
+    drv.close()

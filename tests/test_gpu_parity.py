@@ -205,3 +205,26 @@ def test_gpu_libm_mode_matches_oracle():
     got = {k: v.cpu().numpy() for k, v in t.items()}
     drv.close()
     assert_parity(got, want, "libm mode, convective 16900x42")
+
+
+def test_gpu_graph_steps_equal_repeated_calls():
+    """mp_driver_steps (one captured CUDA graph replayed) equals repeated
+    mp_driver_batched calls bit for bit, and re-captures for new arrays."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=900, kall=42, lall=2, seed=44, variant="convective")
+    st = make_state(spec, out_fill=np.nan)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    a = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    b = {n: t.clone() for n, t in a.items()}
+    c = {n: t.clone() for n, t in a.items()}
+    for _ in range(3):
+        drv.mp_driver_batched(spec.lall, *[a[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.mp_driver_steps(spec.lall, b, 2, dt=spec.dt)
+    drv.mp_driver_steps(spec.lall, b, 1, dt=spec.dt)
+    drv.mp_driver_steps(spec.lall, c, 3, dt=spec.dt)   # other arrays: a new graph
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        assert torch.equal(a[n], b[n]), n
+        assert torch.equal(a[n], c[n]), n
+    drv.close()
