@@ -464,20 +464,28 @@ __device__ __forceinline__ R vadv_wh(const WP& wp, int j, int mkmin, int mkmax) 
 // instead of divisions.  zdis only decides which layer the departure point
 // lies in (an ulp-level change matters only within an ulp of an interface)
 // and scales the flux of the departure layer.
-template <class R, class G, class WP>
-__device__ __forceinline__ R vadv_zdis(const WP& wp, const G* rdz, const G* rdzs, int k, int mkmin, int mkmax, R dt,
-                                       R hdt2, R sdt3) {
+// The same from the half-level velocities wh(j) themselves (an accessor).
+template <class R, class G, class WH>
+__device__ __forceinline__ R vadv_zdis_wh(const WH& wh, const G* rdz, const G* rdzs, int k, int mkmin, R dt, R hdt2,
+                                          R sdt3) {
   if (k == mkmin) {
-    const R w0 = vadv_wh<R>(wp, mkmin, mkmin, mkmax), wpp = vadv_wh<R>(wp, mkmin + 1, mkmin, mkmax);
+    const R w0 = wh(mkmin), wpp = wh(mkmin + 1);
     return fmaR(-hdt2 * w0, (wpp - w0) * rdz[mkmin], dt * w0);
   }
-  const R wm = vadv_wh<R>(wp, k - 1, mkmin, mkmax);
-  const R w0 = vadv_wh<R>(wp, k, mkmin, mkmax);
-  const R wpp = vadv_wh<R>(wp, k + 1, mkmin, mkmax);
+  const R wm = wh(k - 1);
+  const R w0 = wh(k);
+  const R wpp = wh(k + 1);
   const R r = (wpp - wm) * rdzs[k];
   const R c = R(2.0) * rdzs[k] * fmaR(wpp - w0, rdz[k], -(w0 - wm) * rdz[k - 1]);
   const R t3 = sdt3 * w0 * fmaR(w0, c, r * r);
   return fmaR(-hdt2 * w0, r, fmaR(dt, w0, t3));
+}
+
+template <class R, class G, class WP>
+__device__ __forceinline__ R vadv_zdis(const WP& wp, const G* rdz, const G* rdzs, int k, int mkmin, int mkmax, R dt,
+                                       R hdt2, R sdt3) {
+  auto wh = [&](int j) { return vadv_wh<R>(wp, j, mkmin, mkmax); };
+  return vadv_zdis_wh<R>(wh, rdz, rdzs, k, mkmin, dt, hdt2, sdt3);
 }
 
 }  // namespace nsw6

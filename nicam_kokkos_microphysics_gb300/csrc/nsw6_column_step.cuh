@@ -84,9 +84,7 @@ __device__ __forceinline__ T flux_integral_t(const T* rhof, const double* dz, in
                                              int bmx) {
   T f = T(0.0), zdis = zdis0;
   if (!(bmn == k && bmx == k)) {
-    for (int k2 = bmn; k2 <= bmx; ++k2) {
-      if (k2 != kc) f = fmaR(rhof[k2], T(k2 > kc ? dz[k2] : -dz[k2]), f);
-    }
+    for (int k2 = bmn; k2 <= bmx; ++k2) f = fmaR(rhof[k2], T(k2 > kc ? dz[k2] : (k2 < kc ? -dz[k2] : 0.0)), f);
     if (bmx != kc) zdis = zdis0 - T(bmx > kc ? dz[bmx] : -dz[bmx]);
   }
   f = fmaR(rhof[kc], zdis, f);
@@ -230,29 +228,12 @@ __device__ __forceinline__ int satadjust_t(const Consts& C, const FastMath& fm, 
   return 0;
 }
 
-// The whole step of one column.  gr: the grid block [GF_COUNT][K] (doubles).
-// mth: exp/log/pow of T.  C: FP64 constants (values), CT: the same as T (with
-// the parameter derivatives).  status: first error of the column.
+// The cell phase of one column: nsw6_cell on every interior level (as
+// nsw6_cell_kernel), leaving the fall speeds in w.vt.
 template <class T, class M>
-__device__ void column_step(const ConstsT<T>& CT, const Consts& C, const M& mth, const FastMath& fm,
-                            const double* gr, int K, double dt, double rdt, double hdt2, double sdt3, int itelim,
-                            const int (*bmn)[KA], const int (*bmx)[KA], ColState<T>& s, ColWork<T>& w, int* err,
-                            int* err_k, int* err_it) {
+__device__ void column_cell_phase(const ConstsT<T>& CT, const M& mth, int K, double dt, double rdt,
+                                  ColState<T>& s, ColWork<T>& w) {
   const int kmin = 1, kmax = K - 2;
-  const double* gzh = gr + GF_GZH * K;
-  const double* gzs = gr + GF_GZSHIFT * K;
-  const double* dgz = gr + GF_DGZ * K;
-  const double* dgzh = gr + GF_DGZH * K;
-  const double* rdgz = gr + GF_RDGZ * K;
-  const double* rdgzh = gr + GF_RDGZH * K;
-  const double* afact = gr + GF_AFACT * K;
-  const double* bfact = gr + GF_BFACT * K;
-  const double* cfact = gr + GF_CFACT * K;
-  const double* dfact = gr + GF_DFACT * K;
-  const double* rdzs = gr + GF_RDZS * K;
-  const double* rdzsh = gr + GF_RDZSH * K;
-
-  // ---- cell physics, interior levels (nsw6_cell_kernel)
   for (int t = 0; t < 3; ++t)
     for (int k = 0; k < K; ++k) w.vt[t][k] = T(0.0);
   for (int k = kmin; k <= kmax; ++k) {
@@ -284,6 +265,48 @@ __device__ void column_step(const ConstsT<T>& CT, const Consts& C, const M& mth,
       s.rwtop = sw * o.rctop + (1.0 - sw) * UNDEF;
     }
   }
+}
+
+// The column phase: departure distances from the fall speeds in w.vt,
+// transport, KIN2EIN, thermodynamics, saturation adjustment and the closing
+// filter (as nsw6_column_kernel).  gr: the grid block [GF_COUNT][K].
+template <class T>
+__device__ void column_transport_phase(const Consts& C, const FastMath& fm, const double* gr, int K, double dt,
+                                       double hdt2, double sdt3, int itelim, const int (*bmn)[KA],
+                                       const int (*bmx)[KA], ColState<T>& s, ColWork<T>& w, int* err, int* err_k,
+                                       int* err_it);
+
+// The whole step of one column.  mth: exp/log/pow of T.  C: FP64 constants
+// (values), CT: the same as T (with the parameter derivatives).  err: first
+// error of the column.
+template <class T, class M>
+__device__ void column_step(const ConstsT<T>& CT, const Consts& C, const M& mth, const FastMath& fm,
+                            const double* gr, int K, double dt, double rdt, double hdt2, double sdt3, int itelim,
+                            const int (*bmn)[KA], const int (*bmx)[KA], ColState<T>& s, ColWork<T>& w, int* err,
+                            int* err_k, int* err_it) {
+  column_cell_phase<T, M>(CT, mth, K, dt, rdt, s, w);
+  column_transport_phase<T>(C, fm, gr, K, dt, hdt2, sdt3, itelim, bmn, bmx, s, w, err, err_k, err_it);
+}
+
+template <class T>
+__device__ void column_transport_phase(const Consts& C, const FastMath& fm, const double* gr, int K, double dt,
+                                       double hdt2, double sdt3, int itelim, const int (*bmn)[KA],
+                                       const int (*bmx)[KA], ColState<T>& s, ColWork<T>& w, int* err, int* err_k,
+                                       int* err_it) {
+  const int kmin = 1, kmax = K - 2;
+  const double* gzh = gr + GF_GZH * K;
+  const double* gzs = gr + GF_GZSHIFT * K;
+  const double* dgz = gr + GF_DGZ * K;
+  const double* dgzh = gr + GF_DGZH * K;
+  const double* rdgz = gr + GF_RDGZ * K;
+  const double* rdgzh = gr + GF_RDGZH * K;
+  const double* afact = gr + GF_AFACT * K;
+  const double* bfact = gr + GF_BFACT * K;
+  const double* cfact = gr + GF_CFACT * K;
+  const double* dfact = gr + GF_DFACT * K;
+  const double* rdzs = gr + GF_RDZS * K;
+  const double* rdzsh = gr + GF_RDZSH * K;
+
   // ---- departure distances (vadv1d_prep)
   for (int r = 0; r < 6; ++r) {
     const int t = r % 3, half = r / 3;

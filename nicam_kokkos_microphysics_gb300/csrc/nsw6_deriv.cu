@@ -180,20 +180,59 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_tlm_kernel(Problem P, Consts 
   });
 }
 
-// ---- adjoint step: xb <- M'(x)^T xb (inputs), pbar += M_p^T xb
-// On entry xb holds the adjoints of the step's outputs; on exit the adjoints
-// of its inputs: replaced for arguments that are read and written, added for
-// arguments only read, zero for arguments only written.
-__global__ void __launch_bounds__(AD_THREADS) nsw6_adjoint_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
-                                                                  TapeMem tm, const double* params, double* pbar,
-                                                                  int* tape_max) {
-  __shared__ double grid[GF_COUNT * KA];
+// ------------------------------------------------------------------ adjoint in stages
+// The adjoint step runs in three kernels so that the cell physics, which is
+// local to a cell, is differentiated with one thread per cell:
+//   1. nsw6_adj_cellfwd_kernel  (per cell)    the FP64 cell phase, its outputs Y;
+//   2. nsw6_adj_column_kernel   (per column)  the adjoint of the column phase
+//      around Y: adjoints of the step's inputs it reads directly (into xb) and
+//      of the cell phase's outputs (YB);
+//   3. nsw6_adj_cell_kernel     (per cell)    the adjoint of the cell phase:
+//      adjoints of the cell inputs (into xb) and of the parameters.
+// Y / YB layout: [ADJ_NF][lall][kall][gall], fields below.
+enum AdjField {
+  Y_RHOG, Y_RHOGE, Y_TEM, Y_RHOGQ, Y_Q = Y_RHOGQ + 6,   // Y_Q + n - 1 for q[n], n = 1..5
+  Y_VT = Y_Q + 5, Y_RE = Y_VT + 3, Y_RECLD, Y_RCTOP, Y_TCTOP, ADJ_NF
+};
+
+__global__ void __launch_bounds__(256) nsw6_adj_cellfwd_kernel(Problem P, Consts C, ArgPtrs x, double* Y) {
   __shared__ double tab[FM_TABLE_DOUBLES];
-  __shared__ double red[7][AD_THREADS];
-  stage(P, grid, tab);
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  __syncthreads();
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
-  const ADMath<RVar> mth{fm};
   const Lay L{P.kall, P.gall, P.lall};
+  const size_t NC = (size_t)P.lall * P.kall * P.gall;
+  const int nint = P.kmax - P.kmin + 1;
+  const size_t ncell = (size_t)P.lall * nint * P.gall;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % P.gall);
+    const int k = P.kmin + (int)((c / P.gall) % nint);
+    const int l = (int)(c / ((size_t)P.gall * nint));
+    const size_t i = L.f(l, k, g);
+    CellIn in;
+    in.rhog = x.a[A_rhog][i];
+    in.tem = x.a[A_tem][i];
+    in.gsgam2 = x.a[A_gsgam2][i];
+    in.q0 = x.a[A_q][L.t(l, 0, k, g)];
+    for (int n = 0; n < 6; ++n) in.rhogq[n] = x.a[A_rhogq][L.t(l, n, k, g)];
+    CellOut o;
+    nsw6_cell(C, fm, P.dt, P.rdt, in, o);
+    Y[Y_RHOG * NC + i] = o.rhog;
+    Y[Y_RHOGE * NC + i] = o.rhoge;
+    Y[Y_TEM * NC + i] = o.tem;
+    for (int n = 0; n < 6; ++n) Y[(Y_RHOGQ + n) * NC + i] = o.rhogq[n];
+    for (int n = 1; n < 6; ++n) Y[(Y_Q + n - 1) * NC + i] = o.q[n];
+    Y[(Y_VT + 0) * NC + i] = o.Vtr;
+    Y[(Y_VT + 1) * NC + i] = o.Vts;
+    Y[(Y_VT + 2) * NC + i] = o.Vtg;
+    Y[Y_RE * NC + i] = o.rceff;
+    Y[Y_RECLD * NC + i] = o.rceff_cld;
+    Y[Y_RCTOP * NC + i] = o.rctop;
+    Y[Y_TCTOP * NC + i] = o.tctop;
+  }
+}
+
+__device__ __forceinline__ void tape_bind(const TapeMem& tm) {
   Tape& t = tape();
   t.pa = tm.pa;
   t.pb = tm.pb;
@@ -203,44 +242,172 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_adjoint_kernel(Problem P, Con
   t.nslot = tm.nslot;
   t.slot = blockIdx.x * blockDim.x + threadIdx.x;
   t.cap = tm.cap;
-  double pacc[7] = {0, 0, 0, 0, 0, 0, 0};
+  t.count_only = tm.count_only;
+}
+
+__global__ void __launch_bounds__(AD_THREADS) nsw6_adj_column_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
+                                                                     const double* Y, double* YB, TapeMem tm,
+                                                                     int* tape_max) {
+  __shared__ double grid[GF_COUNT * KA];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  stage(P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const Lay L{P.kall, P.gall, P.lall};
+  const size_t NC = (size_t)P.lall * P.kall * P.gall;
+  tape_bind(tm);
+  Tape& t = tape();
   const int ncol = P.lall * P.gall;
   for (int col = t.slot; col < ncol; col += t.nslot) {
     const int l = col / P.gall, g = col % P.gall;
     t.n = 0;
     t.overflow = 0;
-    t.count_only = tm.count_only;
-    RVar p[7];
-    for (int i = 0; i < 7; ++i) p[i] = leaf(params[i]);
-    ConstsT<RVar> CT;
-    consts_with_params(C, p, CT);
     ColState<RVar> s;
-    for_inputs(s, L, l, g, [&](int a, size_t i, RVar& d) { d = leaf(x.a[a][i]); });
-    ColState<RVar> s_in = s;
     ColWork<RVar> w;
+    // direct inputs and the halo levels from x; interior state from the cell phase's outputs Y
+    for_inputs(s, L, l, g, [&](int a, size_t i, RVar& d) { d = leaf(x.a[a][i]); });
+    for (int k = P.kmin; k <= P.kmax; ++k) {
+      const size_t i = L.f(l, k, g);
+      s.rhog[k] = leaf(Y[Y_RHOG * NC + i]);
+      s.rhoge[k] = leaf(Y[Y_RHOGE * NC + i]);
+      s.tem[k] = leaf(Y[Y_TEM * NC + i]);
+      for (int n = 0; n < 6; ++n) s.rhogq[n][k] = leaf(Y[(Y_RHOGQ + n) * NC + i]);
+      for (int n = 1; n < 6; ++n) s.q[n][k] = leaf(Y[(Y_Q + n - 1) * NC + i]);
+      for (int v = 0; v < 3; ++v) w.vt[v][k] = leaf(Y[(Y_VT + v) * NC + i]);
+    }
+    for (int v = 0; v < 3; ++v) {
+      w.vt[v][0] = RVar(0.0);
+      w.vt[v][P.kall - 1] = RVar(0.0);
+    }
+    ColState<RVar> s_in = s;
+    ColWork<RVar> w_in;
+    for (int v = 0; v < 3; ++v)
+      for (int k = 0; k < P.kall; ++k) w_in.vt[v][k] = w.vt[v][k];
+    // outputs of the cell phase only: constants here, their adjoints go to YB
+    for (int k = 0; k < P.kall; ++k) {
+      s.re_liquid[k] = RVar(0.0);
+      s.re_cld[k] = RVar(0.0);
+    }
+    s.rctop = s.tctop = s.rwtop = RVar(0.0);
     int bmn[6][KA], bmx[6][KA];
     column_bounds(grid + GF_GZH * P.kall, grid + GF_GZSHIFT * P.kall, P.kall, P.kmin, P.kmax,
                   P.zmax + (size_t)l * 6 * P.kall, P.zmin + (size_t)l * 6 * P.kall, bmn, bmx);
     int err = 0, ek = 0, eit = 0;
-    column_step<RVar, ADMath<RVar>>(CT, C, mth, fm, grid, P.kall, P.dt, P.rdt, P.hdt2, P.sdt3, P.itelim, bmn, bmx,
-                                    s, w, &err, &ek, &eit);
+    column_transport_phase<RVar>(C, fm, grid, P.kall, P.dt, P.hdt2, P.sdt3, P.itelim, bmn, bmx, s, w, &err, &ek,
+                                 &eit);
     if (err) record_error_d(P.status, err, ek, g, l, eit);
     atomicMax(tape_max, t.overflow ? t.cap + 1 : t.n);
-    if (t.overflow || t.count_only) continue;   // sizing pass, or reported through tape_max
+    if (t.overflow || t.count_only) continue;
     for (int e = 0; e < t.n; ++e) t.adj[(size_t)e * t.nslot + t.slot] = 0.0;
+    // output adjoints of the cell phase's own outputs, passed on to the cell adjoint
+    const size_t ic = L.c(l, g);
+    for (int k = P.kmin; k <= P.kmax; ++k) {
+      const size_t i = L.f(l, k, g);
+      YB[Y_RE * NC + i] = xb.a[A_re_liquid][i];
+      YB[Y_RECLD * NC + i] = xb.a[A_re_cld][i];
+      YB[Y_RCTOP * NC + i] = 0.0;
+      YB[Y_TCTOP * NC + i] = 0.0;
+    }
+    {
+      // rwtop = sw rctop + (1 - sw) UNDEF with sw from tctop (TagUpdateCLD)
+      const size_t i = L.f(l, P.kmax, g);
+      const double sw = (0.5 + copysign(0.5, Y[Y_TCTOP * NC + i] - TEM00));
+      YB[Y_RCTOP * NC + i] = xb.a[A_rctop][ic] + sw * xb.a[A_rwtop][ic];
+      YB[Y_TCTOP * NC + i] = xb.a[A_tctop][ic];
+    }
     for_outputs(s, L, l, g, [&](int a, size_t i, RVar& d) {
       if (d.id >= 0) adj_of(d) += xb.a[a][i];
     });
     tape_reverse();
-    // written-only arguments: their adjoint is consumed
     for_outputs(s, L, l, g, [&](int a, size_t i, RVar&) { xb.a[a][i] = 0.0; });
-    // read arguments: added (to zero for the ones also written: replaced)
+    // interior state and fall speeds: to YB; everything else (direct inputs,
+    // halo levels, the caller's q[QV]): added to xb
+    for (int k = P.kmin; k <= P.kmax; ++k) {
+      const size_t i = L.f(l, k, g);
+      auto put = [&](int f, RVar& d) {
+        YB[f * NC + i] = d.id >= 0 ? adj_of(d) : 0.0;
+        d.id = -1;   // not added to xb below
+      };
+      put(Y_RHOG, s_in.rhog[k]);
+      put(Y_RHOGE, s_in.rhoge[k]);
+      put(Y_TEM, s_in.tem[k]);
+      for (int n = 0; n < 6; ++n) put(Y_RHOGQ + n, s_in.rhogq[n][k]);
+      for (int n = 1; n < 6; ++n) put(Y_Q + n - 1, s_in.q[n][k]);
+      for (int v = 0; v < 3; ++v) put(Y_VT + v, w_in.vt[v][k]);
+    }
     for_inputs(s_in, L, l, g, [&](int a, size_t i, RVar& d) {
       if (d.id >= 0) xb.a[a][i] += adj_of(d);
     });
-    for (int i = 0; i < 7; ++i) pacc[i] += adj_of(p[i]);
   }
-  for (int i = 0; i < 7; ++i) red[i][threadIdx.x] = pacc[i];
+}
+
+__global__ void __launch_bounds__(AD_THREADS) nsw6_adj_cell_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
+                                                                   const double* YB, TapeMem tm,
+                                                                   const double* params, double* pbar,
+                                                                   int* tape_max) {
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  __shared__ double red[7][AD_THREADS];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  __syncthreads();
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const ADMath<RVar> mth{fm};
+  const Lay L{P.kall, P.gall, P.lall};
+  const size_t NC = (size_t)P.lall * P.kall * P.gall;
+  const int nint = P.kmax - P.kmin + 1;
+  const long long ncell = (long long)P.lall * nint * P.gall;
+  tape_bind(tm);
+  Tape& t = tape();
+  double pacc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long long c = t.slot; c < ncell; c += t.nslot) {
+    const int g = (int)(c % P.gall);
+    const int k = P.kmin + (int)((c / P.gall) % nint);
+    const int l = (int)(c / ((long long)P.gall * nint));
+    const size_t i = L.f(l, k, g);
+    t.n = 0;
+    t.overflow = 0;
+    RVar p[7];
+    for (int j = 0; j < 7; ++j) p[j] = leaf(params[j]);
+    ConstsT<RVar> CT;
+    consts_with_params(C, p, CT);
+    CellInT<RVar> in;
+    in.rhog = leaf(x.a[A_rhog][i]);
+    in.tem = leaf(x.a[A_tem][i]);
+    in.gsgam2 = leaf(x.a[A_gsgam2][i]);
+    in.q0 = leaf(x.a[A_q][L.t(l, 0, k, g)]);
+    for (int n = 0; n < 6; ++n) in.rhogq[n] = leaf(x.a[A_rhogq][L.t(l, n, k, g)]);
+    CellOutT<RVar> o;
+    nsw6_cell<ADMath<RVar>, RVar, RVar>(CT, mth, P.dt, P.rdt, in, o);
+    atomicMax(tape_max, t.overflow ? t.cap + 1 : t.n);
+    if (t.overflow || t.count_only) continue;
+    for (int e = 0; e < t.n; ++e) t.adj[(size_t)e * t.nslot + t.slot] = 0.0;
+    auto seed = [&](const RVar& d, int f) {
+      if (d.id >= 0) adj_of(d) += YB[f * NC + i];
+    };
+    seed(o.rhog, Y_RHOG);
+    seed(o.rhoge, Y_RHOGE);
+    seed(o.tem, Y_TEM);
+    for (int n = 0; n < 6; ++n) seed(o.rhogq[n], Y_RHOGQ + n);
+    for (int n = 1; n < 6; ++n) seed(o.q[n], Y_Q + n - 1);
+    seed(o.Vtr, Y_VT + 0);
+    seed(o.Vts, Y_VT + 1);
+    seed(o.Vtg, Y_VT + 2);
+    seed(o.rceff, Y_RE);
+    seed(o.rceff_cld, Y_RECLD);
+    if (k == P.kmax) {
+      seed(o.rctop, Y_RCTOP);
+      seed(o.tctop, Y_TCTOP);
+    }
+    tape_reverse();
+    auto add = [&](const RVar& d, int a, size_t idx) {
+      if (d.id >= 0) xb.a[a][idx] += adj_of(d);
+    };
+    add(in.rhog, A_rhog, i);
+    add(in.tem, A_tem, i);
+    add(in.gsgam2, A_gsgam2, i);
+    add(in.q0, A_q, L.t(l, 0, k, g));
+    for (int n = 0; n < 6; ++n) add(in.rhogq[n], A_rhogq, L.t(l, n, k, g));
+    for (int j = 0; j < 7; ++j) pacc[j] += adj_of(p[j]);
+  }
+  for (int j = 0; j < 7; ++j) red[j][threadIdx.x] = pacc[j];
   __syncthreads();
   if (threadIdx.x < 7) {
     double sum = 0.0;
@@ -263,11 +430,27 @@ cudaError_t launch_tlm(const Problem& P, const Consts& C, const ArgPtrs& x, cons
   return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const TapeMem& tm,
-                           const double* params, double* pbar, int* tape_max, cudaStream_t stream) {
-  const int blocks = tm.nslot / AD_THREADS;
-  nsw6_adjoint_kernel<<<blocks, AD_THREADS, 0, stream>>>(P, C, x, xb, tm, params, pbar, tape_max);
+constexpr int ADJ_NFIELDS = ADJ_NF;
+
+cudaError_t launch_adj_cellfwd(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, cudaStream_t stream) {
+  nsw6_adj_cellfwd_kernel<<<152 * 4, 256, 0, stream>>>(P, C, x, Y);
   return cudaGetLastError();
 }
+
+cudaError_t launch_adj_column(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* Y,
+                              double* YB, const TapeMem& tm, int* tape_max, cudaStream_t stream) {
+  nsw6_adj_column_kernel<<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, Y, YB, tm, tape_max);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
+                            const TapeMem& tm, const double* params, double* pbar, int* tape_max,
+                            cudaStream_t stream) {
+  nsw6_adj_cell_kernel<<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, YB, tm, params, pbar,
+                                                                         tape_max);
+  return cudaGetLastError();
+}
+
+int adj_nfields() { return ADJ_NFIELDS; }
 
 }  // namespace nsw6

@@ -24,11 +24,17 @@ cudaError_t launch_prepare();
 cudaError_t launch_serial(const Problem& P, const Consts& C, const ArgPtrs& x, cudaStream_t stream);
 cudaError_t launch_tlm(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx, const double* params,
                        const double* dparams, cudaStream_t stream);
-cudaError_t launch_adjoint(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const TapeMem& tm,
-                           const double* params, double* pbar, int* tape_max, cudaStream_t stream);
+cudaError_t launch_adj_cellfwd(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, cudaStream_t stream);
+cudaError_t launch_adj_column(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* Y,
+                              double* YB, const TapeMem& tm, int* tape_max, cudaStream_t stream);
+cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
+                            const TapeMem& tm, const double* params, double* pbar, int* tape_max,
+                            cudaStream_t stream);
+int adj_nfields();
 constexpr int DERIV_MAX_KALL = 48;   // KA of nsw6_column_step.cuh
 constexpr int DERIV_THREADS = 128;   // AD_THREADS of nsw6_ad.cuh
-constexpr int ADJ_MAX_SLOTS = 8192;  // threads of one adjoint launch (each with its own tape)
+constexpr int ADJ_COL_SLOTS = 8192;    // threads of the column adjoint (each with its own tape)
+constexpr int ADJ_CELL_SLOTS = 32768;  // threads of the cell adjoint
 cudaError_t launch_math(int fn, const double* x, const double* y, double* out, int n, const double* fmtab,
                         cudaStream_t stream);
 }
@@ -54,8 +60,11 @@ struct nsw6_handle {
   double* d_dparam = nullptr;    // [16]: params [0,7), tangents [8,15)
   double* d_pbar = nullptr;      // [8]
   int* d_tmax = nullptr;
-  TapeMem tape{};
+  TapeMem tape{};        // column-adjoint tapes
   size_t tape_bytes = 0;
+  TapeMem ctape{};       // cell-adjoint tapes
+  size_t ctape_bytes = 0;
+  double* d_Y = nullptr;   // cell-phase outputs and their adjoints [2][nfields][lall_max][kall][gall]
   // captured step graph of mp_driver_steps and what it was captured for
   cudaStream_t cap_stream = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -602,6 +611,8 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_pbar);
   cudaFree(h->d_tmax);
   cudaFree(h->tape.pa);
+  cudaFree(h->ctape.pa);
+  cudaFree(h->d_Y);
   for (auto& tri : h->ev)
     for (auto& e : tri)
       if (e) cudaEventDestroy(e);
@@ -890,6 +901,28 @@ int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* 
   return rc;
 }
 
+// (Re)allocates a set of interleaved tapes: nslot threads x cap entries.
+int ensure_tape(TapeMem& t, size_t& bytes, int nslot, int cap) {
+  const size_t per = sizeof(int) * 2 + sizeof(double) * 3;
+  const size_t need = per * (size_t)cap * (size_t)nslot;
+  if (t.pa && need <= bytes && t.nslot == nslot && t.cap >= cap) return NSW6_OK;
+  cudaFree(t.pa);
+  t = TapeMem{};
+  bytes = 0;
+  char* base = nullptr;
+  if (cudaMalloc(&base, need) != cudaSuccess) return NSW6_ERR_CUDA;
+  const size_t n = (size_t)cap * nslot;
+  t.pa = reinterpret_cast<int*>(base);
+  t.pb = t.pa + n;
+  t.da = reinterpret_cast<double*>(base + sizeof(int) * 2 * n);
+  t.db = t.da + n;
+  t.adj = t.db + n;
+  t.nslot = nslot;
+  t.cap = cap;
+  bytes = need;
+  return NSW6_OK;
+}
+
 int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
                       double dt, double ct) {
   (void)ct;
@@ -908,49 +941,51 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
     x.a[i] = args[i];
     xb.a[i] = aargs[i];
   }
-  const long long ncol = (long long)lall * h->gall;
-  long long slots = ((ncol + DERIV_THREADS - 1) / DERIV_THREADS) * DERIV_THREADS;
-  if (slots > ADJ_MAX_SLOTS) slots = ADJ_MAX_SLOTS;
-  const int nslot = (int)slots;
-  // sizing pass: the tape length of the longest column
-  int tmax = 0;
+  const size_t NC = (size_t)h->lall_max * h->kall * h->gall;
+  if (!h->d_Y && cudaMalloc(&h->d_Y, sizeof(double) * 2 * adj_nfields() * NC) != cudaSuccess) return NSW6_ERR_CUDA;
+  // the all-regions layout of Y for this call's lall
+  const size_t NCl = (size_t)lall * h->kall * h->gall;
+  double* Y = h->d_Y;
+  double* YB = h->d_Y + (size_t)adj_nfields() * NCl;
+  auto round_slots = [](long long n, int maxs) {
+    long long s = ((n + DERIV_THREADS - 1) / DERIV_THREADS) * DERIV_THREADS;
+    return (int)(s > maxs ? maxs : s);
+  };
+  const int ncol_slots = round_slots((long long)lall * h->gall, ADJ_COL_SLOTS);
+  const int ncell_slots = round_slots((long long)lall * (h->kall - 2) * h->gall, ADJ_CELL_SLOTS);
+  if (launch_adj_cellfwd(P, h->C, x, Y, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  // sizing passes: the longest tape of each stage
+  int tcol = 0, tcell = 0;
   TapeMem cnt{};
-  cnt.nslot = nslot;
   cnt.count_only = 1;
+  cnt.nslot = ncol_slots;
   if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-      launch_adjoint(P, h->C, x, xb, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(&tmax, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      launch_adj_column(P, h->C, x, xb, Y, YB, cnt, h->d_tmax, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&tcol, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  cnt.nslot = ncell_slots;
+  if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+      launch_adj_cell(P, h->C, x, xb, YB, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&tcell, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
       cudaStreamSynchronize(h->stream) != cudaSuccess)
     return NSW6_ERR_CUDA;
-  const size_t per = sizeof(int) * 2 + sizeof(double) * 3;
-  const size_t need = per * (size_t)tmax * (size_t)nslot;
-  if (need > h->tape_bytes || h->tape.nslot != nslot || h->tape.cap < tmax) {
-    cudaFree(h->tape.pa);
-    h->tape = TapeMem{};
-    h->tape_bytes = 0;
-    char* base = nullptr;
-    if (cudaMalloc(&base, need) != cudaSuccess) return NSW6_ERR_CUDA;
-    const size_t n = (size_t)tmax * nslot;
-    h->tape.pa = reinterpret_cast<int*>(base);
-    h->tape.pb = h->tape.pa + n;
-    h->tape.da = reinterpret_cast<double*>(base + sizeof(int) * 2 * n);
-    h->tape.db = h->tape.da + n;
-    h->tape.adj = h->tape.db + n;
-    h->tape.nslot = nslot;
-    h->tape.cap = tmax;
-    h->tape_bytes = need;
-  }
+  if ((rc = ensure_tape(h->tape, h->tape_bytes, ncol_slots, tcol)) != NSW6_OK) return rc;
+  if ((rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, tcell)) != NSW6_OK) return rc;
   h->tape.count_only = 0;
+  h->ctape.count_only = 0;
   double pb[8] = {};
-  int tmax2 = 0;
+  int t1 = 0, t2 = 0;
   if (cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-      launch_adjoint(P, h->C, x, xb, h->tape, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
+      launch_adj_column(P, h->C, x, xb, Y, YB, h->tape, h->d_tmax, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&t1, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+      launch_adj_cell(P, h->C, x, xb, YB, h->ctape, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
+      cudaMemcpyAsync(&t2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
       cudaMemcpyAsync(pb, h->d_pbar, sizeof(double) * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(&tmax2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
       cudaStreamSynchronize(h->stream) != cudaSuccess)
     return NSW6_ERR_CUDA;
-  if (tmax2 > h->tape.cap) return NSW6_ERR_UNSUPPORTED;
+  if (t1 > h->tape.cap || t2 > h->ctape.cap) return NSW6_ERR_UNSUPPORTED;
   if (dparams)
     for (int i = 0; i < 7; ++i) dparams[i] += pb[i];
   return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);

@@ -82,6 +82,8 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
   float* gridf = reinterpret_cast<float*>(tab + FM_TABLE_DOUBLES);  // [4][K], mixed only
   unsigned short* perm = reinterpret_cast<unsigned short*>(gridf + 4 * K);  // [nlev * CELL_TG], FP64 only
   unsigned char* key = reinterpret_cast<unsigned char*>(perm + (K - 2) * CELL_TG);
+  R* whs = reinterpret_cast<R*>(                                          // [K][CELL_TG] half-level velocities
+      (reinterpret_cast<uintptr_t>(key + (K - 2) * CELL_TG) + 15) & ~(uintptr_t)15);
   __shared__ int bucket[33];
 
   for (int c = threadIdx.x; c < 3 * K * CELL_TG; c += blockDim.x) vts[c] = R(0.0);
@@ -194,30 +196,41 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
     rdzsh = grid + GF_RDZSH * K;
   }
   const R dtR = R(P.dt), hdt2R = R(P.hdt2), sdt3R = R(P.sdt3);
-  for (int c = threadIdx.x; c < 6 * K * CELL_TG; c += blockDim.x) {
-    const int s = c / (K * CELL_TG);
-    const int rem = c - s * K * CELL_TG;
-    const int k = rem / CELL_TG;
-    const int gx = rem % CELL_TG;
+  // one row at a time: its half-level velocities wh(j) first (each is used by
+  // three departure distances), then the distances
+  for (int s = 0; s < 6; ++s) {
     const int t = s % 3;
     const int half = s / 3;
     const int mkmin = half ? kmin + 1 : kmin;
+    for (int c = threadIdx.x; c < K * CELL_TG; c += blockDim.x) {
+      const int j = c / CELL_TG, gx = c % CELL_TG;
+      if (j < mkmin - 1 || j > kmax + 1) continue;
+      const R* col = vts + t * K * CELL_TG + gx;
+      R v;
+      if (!half) {
+        auto wp = [&](int jj) { return col[jj * CELL_TG]; };
+        v = vadv_wh<R>(wp, j, mkmin, kmax);
+      } else {
+        // Vtermh, mod_precip_transport.cpp:847-861
+        auto wp = [&](int jj) {
+          return (jj >= kmin + 1 && jj <= kmax - 1) ? R(0.5) * (col[jj * CELL_TG] + col[(jj - 1) * CELL_TG]) : R(0.0);
+        };
+        v = vadv_wh<R>(wp, j, mkmin, kmax);
+      }
+      whs[c] = v;
+    }
+    __syncthreads();
+  for (int c = threadIdx.x; c < K * CELL_TG; c += blockDim.x) {
+    const int k = c / CELL_TG;
+    const int gx = c % CELL_TG;
     if (k < mkmin || k > kmax) continue;  // uniform across the warp (CELL_TG == 32)
     const int g = g0 + gx;
     const bool valid = g < G;
-    const R* col = vts + t * K * CELL_TG + gx;
     double z = 0.0;
     if (valid) {
-      if (!half) {
-        auto wp = [&](int j) { return col[j * CELL_TG]; };
-        z = double(vadv_zdis<R>(wp, rdgz, rdzs, k, mkmin, kmax, dtR, hdt2R, sdt3R));
-      } else {
-        // Vtermh, mod_precip_transport.cpp:847-861
-        auto wp = [&](int j) {
-          return (j >= kmin + 1 && j <= kmax - 1) ? R(0.5) * (col[j * CELL_TG] + col[(j - 1) * CELL_TG]) : R(0.0);
-        };
-        z = double(vadv_zdis<R>(wp, rdgzh, rdzsh, k, mkmin, kmax, dtR, hdt2R, sdt3R));
-      }
+      auto wh = [&](int j) { return whs[j * CELL_TG + gx]; };
+      z = half ? double(vadv_zdis_wh<R>(wh, rdgzh, rdzsh, k, mkmin, dtR, hdt2R, sdt3R))
+               : double(vadv_zdis_wh<R>(wh, rdgz, rdzs, k, mkmin, dtR, hdt2R, sdt3R));
       P.zdis[((size_t)l * 6 + s) * KG + (size_t)k * G + g] = z;
     }
     // NaN never wins the reference's comparisons, so it is left out
@@ -235,6 +248,8 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
       if (kmx != 0ull) atomicMax(&P.zmax[e], kmx);
       if (kmn != ~0ull) atomicMin(&P.zmin[e], kmn);
     }
+  }
+    __syncthreads();
   }
 }
 
@@ -296,9 +311,10 @@ __device__ __forceinline__ double flux_integral(const double* rhof_col, const do
                                                 double zdis0, int bmn, int bmx) {
   double f = 0.0, zdis = zdis0;
   if (!(bmn == k && bmx == k)) {
-    for (int k2 = bmn; k2 <= bmx; ++k2) {
-      if (k2 != kc) f = __fma_rn(rhof_col[k2 * TG], k2 > kc ? dz[k2] : -dz[k2], f);
-    }
+    // the departure cell's own weight is 0 (the reference multiplies by it):
+    // adding rhof(kc) * 0 leaves f unchanged and keeps every lane busy
+    for (int k2 = bmn; k2 <= bmx; ++k2)
+      f = __fma_rn(rhof_col[k2 * TG], k2 > kc ? dz[k2] : (k2 < kc ? -dz[k2] : 0.0), f);
     if (bmx != kc) zdis = zdis0 - (bmx > kc ? dz[bmx] : -dz[bmx]);
   }
   f = __fma_rn(rhof_col[kc * TG], zdis, f);
@@ -313,9 +329,8 @@ __device__ __forceinline__ float flux_integral_f(const float* rhof_col, const fl
                                                  int bmn, int bmx) {
   float f = 0.0f, zdis = zdis0;
   if (!(bmn == k && bmx == k)) {
-    for (int k2 = bmn; k2 <= bmx; ++k2) {
-      if (k2 != kc) f = __fmaf_rn(rhof_col[k2 * TG], k2 > kc ? dz[k2] : -dz[k2], f);
-    }
+    for (int k2 = bmn; k2 <= bmx; ++k2)
+      f = __fmaf_rn(rhof_col[k2 * TG], k2 > kc ? dz[k2] : (k2 < kc ? -dz[k2] : 0.0f), f);
     if (bmx != kc) zdis = zdis0 - (bmx > kc ? dz[bmx] : -dz[bmx]);
   }
   f = __fmaf_rn(rhof_col[kc * TG], zdis, f);
@@ -693,10 +708,22 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   __syncthreads();
 
   // ---- per cell: KIN2EIN, final thermodynamics, saturation adjustment,
-  //      negative filter, outputs
-  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+  //      negative filter, outputs.  The saturation-adjustment Newton
+  //      iteration runs only in saturated cells; to keep warps full they are
+  //      queued (pass A), iterated together (pass B) and finished (pass C),
+  //      the queue living in slots that are dead by now.  Pass C recomputes
+  //      the cell's state exactly as pass A did and takes the Newton result.
+  const int QE_TEM = S_KINH, QE_EIN = S_KINV, QE_QSUM = S_DKINH, QE_RHOL = S_DKINV, QE_QDL = S_DQR;
+  const int QE_Q2 = S_DQS, QE_Q3 = S_DQG, QE_Q4 = S_F, QE_Q5 = S_RGS, QE_C = S_BASE;
+  const int QE_TOUT = S_VI, QE_QV = S_VJ, QE_QC = S_DRHOGU;
+  __shared__ int nqueue;
+  if (threadIdx.x == 0) nqueue = 0;
+  __syncthreads();
+
+  // mode 0: returns true when the cell was queued for the Newton iteration;
+  // mode 1: finishes a queued cell with the result (tres, qvres, qcres)
+  auto final_cell = [&](int c, int mode, double tres, double qvres, double qcres) -> bool {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-    if (g >= G) continue;
     const size_t i = off + (size_t)k * G + g;
     const size_t iq = offq + (size_t)k * G + g;
     const bool interior = (k >= kmin && k <= kmax);
@@ -751,40 +778,31 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
     const double rho_l = rho;
     tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
-    if (interior) {
-      // satadjust_liq, mod_satadjust.cpp:771-896
+    if (mode == 1) {
+      tem = tres;
+      q[I_QV] = qvres;
+      q[I_QC] = qcres;
+    } else if (interior) {
+      // satadjust_liq, mod_satadjust.cpp:771-896: is the cell saturated?
       double qd_l = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
-      double rtem = 1.0 / (dmax(tem, TEM_MIN));
-      double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-      double qsat = psat / (rho_l * RVAP * tem);
+      const double rtem = 1.0 / (dmax(tem, TEM_MIN));
+      const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      const double qsat = psat / (rho_l * RVAP * tem);
       if (qsum - qsat > EPS) {
-        bool converged = false;
-        int ite;
-        for (ite = 0; ite < P.itelim; ++ite) {
-          rtem = 1.0 / (dmax(tem, TEM_MIN));
-          psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-          qsat = psat / (rho_l * RVAP * tem);
-          q[I_QV] = qsat;
-          q[I_QC] = qsum - qsat;
-          double cv = qd_l * CVDRY;
-#pragma unroll
-          for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
-          const double emoist_new = tem * cv + q[I_QV] * LHV0;
-          // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
-          // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
-          const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
-          const double demoist_dT = cv + dqsat_dT * LHV0;
-          const double dtemp = (emoist_new - ein_moist) / demoist_dT;
-          tem = tem - dtemp;
-          if (fabs(dtemp) < C.dtemp_criteria) {
-            converged = true;
-            break;
-          }
-          if (tem * 0.0 != 0.0) break;
-        }
-        if (!converged) record_error(P.status, (tem * 0.0 != 0.0) ? ERR_NAN : ERR_NOCONV, k, g, l, ite);
+        const int e = atomicAdd(&nqueue, 1);
+        F(QE_TEM)[e] = tem;
+        F(QE_EIN)[e] = ein_moist;
+        F(QE_QSUM)[e] = qsum;
+        F(QE_RHOL)[e] = rho_l;
+        F(QE_QDL)[e] = qd_l;
+        F(QE_Q2)[e] = q[2];
+        F(QE_Q3)[e] = q[3];
+        F(QE_Q4)[e] = q[4];
+        F(QE_Q5)[e] = q[5];
+        F(QE_C)[e] = (double)c;
+        return true;
       }
     }
     rq[I_QV] = rhog * q[I_QV];
@@ -844,6 +862,14 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       P.re_liquid[i] = 0.0;
       P.re_cld[i] = 0.0;
     }
+    return false;
+  };
+
+  // pass A: every cell; saturated interior cells are queued
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+    const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    if (g >= G) continue;
+    final_cell(c, 0, 0.0, 0.0, 0.0);
     if (k == kmin) {
       const size_t ic = (size_t)l * G + g;
       const size_t r0 = (size_t)l * G + g, r1 = ((size_t)P.lall + l) * G + g;
@@ -860,6 +886,57 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       P.precip_rhokin[ic] = 0.0 + acc[5 * COL_TG + gx];
     }
   }
+  __syncthreads();
+
+  // pass B: the Newton iteration of the queued cells, warps full
+  const int nq = nqueue;
+  for (int e = threadIdx.x; e < nq; e += blockDim.x) {
+    double tem = F(QE_TEM)[e];
+    const double ein_moist = F(QE_EIN)[e], qsum = F(QE_QSUM)[e], rho_l = F(QE_RHOL)[e], qd_l = F(QE_QDL)[e];
+    double q[6];
+    q[0] = qsum;
+    q[1] = 0.0;
+    q[2] = F(QE_Q2)[e];
+    q[3] = F(QE_Q3)[e];
+    q[4] = F(QE_Q4)[e];
+    q[5] = F(QE_Q5)[e];
+    bool converged = false;
+    int ite;
+    for (ite = 0; ite < P.itelim; ++ite) {
+      const double rtem = 1.0 / (dmax(tem, TEM_MIN));
+      const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      const double qsat = psat / (rho_l * RVAP * tem);
+      q[I_QV] = qsat;
+      q[I_QC] = qsum - qsat;
+      double cv = qd_l * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
+      const double emoist_new = tem * cv + q[I_QV] * LHV0;
+      // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
+      // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
+      const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
+      const double demoist_dT = cv + dqsat_dT * LHV0;
+      const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+      tem = tem - dtemp;
+      if (fabs(dtemp) < C.dtemp_criteria) {
+        converged = true;
+        break;
+      }
+      if (tem * 0.0 != 0.0) break;
+    }
+    if (!converged) {
+      const int c = (int)F(QE_C)[e];
+      record_error(P.status, (tem * 0.0 != 0.0) ? ERR_NAN : ERR_NOCONV, c / COL_TG, g0 + c % COL_TG, l, ite);
+    }
+    F(QE_TOUT)[e] = tem;
+    F(QE_QV)[e] = q[I_QV];
+    F(QE_QC)[e] = q[I_QC];
+  }
+  __syncthreads();
+
+  // pass C: finish the queued cells
+  for (int e = threadIdx.x; e < nq; e += blockDim.x)
+    final_cell((int)F(QE_C)[e], 1, F(QE_TOUT)[e], F(QE_QV)[e], F(QE_QC)[e]);
 }
 
 // ------------------------------------------------------------------ math check
@@ -888,7 +965,8 @@ size_t cell_smem_bytes(int K, bool mixed) {
   const size_t vts = mixed ? cell_vts_doubles<float>(K) : cell_vts_doubles<double>(K);
   // fall speeds, grid, tables, the FP32 reciprocal rows, the cell order and keys
   return sizeof(double) * (vts + (size_t)GF_COUNT * K + FM_TABLE_DOUBLES) + sizeof(float) * 4 * K +
-         (sizeof(unsigned short) + 1) * (size_t)(K - 2) * CELL_TG;
+         (sizeof(unsigned short) + 1) * (size_t)(K - 2) * CELL_TG + 16 +
+         (mixed ? sizeof(float) : sizeof(double)) * (size_t)K * CELL_TG;
 }
 
 int column_tile(int K) { return K <= 64 ? 16 : 8; }
@@ -907,6 +985,8 @@ int column_threads(int K) {
   return per > 256 ? 256 : per;
 }
 
+cudaError_t launch_prepare();
+
 // The cell kernel alone (FP64): used on a copy of a state to obtain the
 // region extrema of the departure distances for the derivative kernels.
 cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t stream) {
@@ -915,35 +995,47 @@ cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t str
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  cudaFuncSetAttribute(nsw6_cell_kernel<FastMath, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  e = launch_prepare();
+  if (e != cudaSuccess) return e;
   dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
   nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, cell_smem_bytes(P.kall, false), stream>>>(P, C);
   return cudaGetLastError();
 }
 
+// Raises a kernel's dynamic shared-memory limit to what the device allows a
+// block beside the kernel's own static shared memory.
+template <class Kernel>
+static cudaError_t raise_smem_limit(Kernel k, int optin) {
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, k);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes);
+}
+
 // Opt-in shared-memory limits of the step kernels (once per process; before
 // any stream capture of a step).
 cudaError_t launch_prepare() {
-  static bool attr_done = false;
-  if (!attr_done) {
-    cudaFuncSetAttribute(nsw6_cell_kernel<FastMath, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(nsw6_cell_kernel<LibMath, double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(nsw6_cell_kernel<FloatMath, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<16, FastMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<8, FastMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<16, LibMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<8, LibMath, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<16, FastMath, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    cudaFuncSetAttribute(nsw6_column_kernel<8, FastMath, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         227 * 1024);
-    attr_done = true;
+  static cudaError_t done = cudaErrorNotReady;
+  if (done == cudaErrorNotReady) {
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    const cudaError_t r[] = {
+        e,
+        raise_smem_limit(nsw6_cell_kernel<FastMath, double>, optin),
+        raise_smem_limit(nsw6_cell_kernel<LibMath, double>, optin),
+        raise_smem_limit(nsw6_cell_kernel<FloatMath, float>, optin),
+        raise_smem_limit(nsw6_column_kernel<16, FastMath, false>, optin),
+        raise_smem_limit(nsw6_column_kernel<8, FastMath, false>, optin),
+        raise_smem_limit(nsw6_column_kernel<16, LibMath, false>, optin),
+        raise_smem_limit(nsw6_column_kernel<8, LibMath, false>, optin),
+        raise_smem_limit(nsw6_column_kernel<16, FastMath, true>, optin),
+        raise_smem_limit(nsw6_column_kernel<8, FastMath, true>, optin)};
+    done = cudaSuccess;
+    for (cudaError_t x : r)
+      if (x != cudaSuccess) done = x;
   }
-  return cudaGetLastError();
+  return done;
 }
 
 cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev) {
