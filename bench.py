@@ -48,12 +48,11 @@ ALGO_BYTES_PER_CELL = 49 * 8 + 3
 # rhogq(6), q(QV), tem, gsgam2 and writes rhog, rhoge, tem, rhogq(6), q(5),
 # re_liquid, re_cld.
 CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
-# DRAM bytes (read + write) per interior cell of the cell kernel, from the ncu
-# capture of one 16900 x 42 region (profiles/nsw6_cell_kernel_16900x42.md).
-CELL_KERNEL_TRAFFIC_PER_CELL = 170.0
-# DRAM bytes (read + write) per cell of the column kernel, same capture
-# (profiles/nsw6_column_kernel_16900x42.md).
-COLUMN_KERNEL_TRAFFIC_PER_CELL = 381.0
+# DRAM bytes (read + write) per interior cell of the cell kernel and per cell of
+# the column kernel, from ncu captures (--set full) of each kernel on one
+# 16900 x 42 region; traffic grows in proportion to cells.
+CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 215.5, "mixed": 172.9}
+COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 379.1, "mixed": 401.0}
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (csrc/nsw6_probe.cu) and frozen here.
@@ -506,9 +505,9 @@ def main(argv=None) -> int:
         cell_flops = aw["cell_per_interior_cell"] * n_int
         col_flops = aw["column_per_cell"] * spec.cells
         cell = {"achieved": cell_flops / (cell_ms * 1e-3) / 1e12, "work_per_interior_cell": aw["cell_per_interior_cell"],
-                "traffic": CELL_KERNEL_TRAFFIC_PER_CELL * n_int}
+                "traffic": CELL_KERNEL_TRAFFIC_PER_CELL[args.precision] * n_int}
         col = {"achieved": col_flops / (col_ms * 1e-3) / 1e12, "work_per_cell": aw["column_per_cell"],
-               "traffic": COLUMN_KERNEL_TRAFFIC_PER_CELL * spec.cells}
+               "traffic": COLUMN_KERNEL_TRAFFIC_PER_CELL[args.precision] * spec.cells}
         for d in (cell, col):
             d["frac"] = d["achieved"] / rates["peak_tflops"]
         top, other, names = (cell, col, ("nsw6_cell_kernel", "nsw6_column_kernel")) if cell_ms >= col_ms else \
