@@ -70,6 +70,39 @@ int nsw6_destroy(nsw6_handle* h);
 int nsw6_set_params(nsw6_handle* h, const nsw6_params* p);
 int nsw6_get_params(const nsw6_handle* h, nsw6_params* p);
 
+/* Scheme switches of NSW6 that the reference selects in mp_nsw6_init
+ * (mod_mp_nsw6.cpp:276-434) and in globals (mod_mp_nsw6.cpp:127-132,
+ * problemsize.cpp:39).  1 = on; nsw6_default_options gives the reference's
+ * configuration {1, 1, 1, 0, 0, 0}. */
+typedef struct nsw6_options {
+  int roh2014;          /* Roh and Satoh (2014) snow (Roh_flag): its moments and N0g, As, Bs, Esi, Egi,
+                           Egs (:345-357); 0 = the classic snow moments (:975-992) and the
+                           GlobalParams values (mod_mp_nsw6.h:16-123)                              */
+  int explicit_icegen;  /* OPT_EXPLICIT_ICEGEN: Pigen, Pidep, Pihom, Pihtr, Pisub, Pimlt and the
+                           liquid saturation adjustment; 0 = Bergeron process (:1239-1247,
+                           Bergeron_param :1834-1890) and the mixed-phase adjustment
+                           satadjust_all (mod_satadjust.cpp:620-769) between 233.16 K and 273.16 K
+                           (:648-661).  roh2014 = 1 forces it on, as mp_nsw6_init does.            */
+  int kk2000;           /* qr_aut_acc_type "KK2000"; 0 = Berry (1968) autoconversion and the
+                           original accretion (:1091-1099, :1145-1160)                              */
+  int qi_sediment;      /* precip_transport_type "4WATER": cloud ice sediments with its fall speed
+                           Vti (:1073-1075); 0 = "3WATER"                                          */
+  int kin2kin;          /* PRCIP_TRN_ECORRECT "KIN2KIN": the transported kinetic energy rescales the
+                           momentum (mod_precip_transport.cpp:1012-1068); 0 = "KIN2EIN"           */
+  int aerosol_indirect; /* OPT_INDIR: cloud number max(unccn 1e-6, Nc_def) per cell (:676-679); the
+                           unccn argument is then read                                             */
+} nsw6_options;
+
+void nsw6_default_options(nsw6_options* o);
+
+/* Selects the scheme switches for the following calls of the handle.  Any
+ * non-default switch runs the FP64 step in the kernels built with the
+ * switched branches; with one set, mp_driver_mixed, nsw6_set_precision(h, 1
+ * or 2), nsw6_set_math(h, 1), mp_driver_tlm and mp_driver_adjoint return
+ * NSW6_ERR_UNSUPPORTED. */
+int nsw6_set_options(nsw6_handle* h, const nsw6_options* o);
+int nsw6_get_options(const nsw6_handle* h, nsw6_options* o);
+
 /* Stream (cudaStream_t, may be 0) on which all work of the handle runs. */
 int nsw6_set_stream(nsw6_handle* h, void* stream);
 

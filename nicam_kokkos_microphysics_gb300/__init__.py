@@ -28,15 +28,22 @@ import numpy as np
 from . import _native
 from .state import ARG_NAMES, MP_DRIVER_ARGS, batched_shape, region_shape
 
-__all__ = ["MPDriver", "mp_init", "mp_driver_noalloc", "NSW6Error", "PARAM_NAMES", "default_params"]
+__all__ = ["MPDriver", "mp_init", "mp_driver_noalloc", "NSW6Error", "PARAM_NAMES", "OPTION_NAMES", "default_params",
+           "default_options"]
 
 PARAM_NAMES = ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg", "ice_nuc", "kk_aut"]
+# Scheme switches of nsw6_options (include/nsw6.h), in its order.
+OPTION_NAMES = ["roh2014", "explicit_icegen", "kk2000", "qi_sediment", "kin2kin", "aerosol_indirect"]
 
 NSW6_OK, NSW6_ERR_BAD_ARG, NSW6_ERR_CUDA, NSW6_ERR_NOCONV, NSW6_ERR_NAN = 0, 1, 2, 3, 4
 
 
 class _Params(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in PARAM_NAMES]
+
+
+class _Options(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in OPTION_NAMES]
 
 
 class NSW6Error(RuntimeError):
@@ -54,6 +61,14 @@ def default_params() -> dict[str, float]:
     return {n: getattr(p, n) for n in PARAM_NAMES}
 
 
+def default_options() -> dict[str, int]:
+    """The reference's scheme configuration (nsw6_default_options)."""
+    lib = _native.load()
+    o = _Options()
+    lib.nsw6_default_options(ctypes.byref(o))
+    return {n: getattr(o, n) for n in OPTION_NAMES}
+
+
 def _check(rc: int, lib, handle=None) -> None:
     if rc == NSW6_OK:
         return
@@ -65,7 +80,8 @@ def _check(rc: int, lib, handle=None) -> None:
 class MPDriver:
     """One NSW6 configuration on one grid: owns the device workspace."""
 
-    def __init__(self, gall: int, kall: int, gz, gzh, lall_max: int = 1, params: dict | None = None):
+    def __init__(self, gall: int, kall: int, gz, gzh, lall_max: int = 1, params: dict | None = None,
+                 options: dict | None = None):
         self._lib = _native.load()
         self.gall, self.kall, self.lall_max = int(gall), int(kall), int(lall_max)
         gz = np.ascontiguousarray(gz, dtype=np.float64)
@@ -79,6 +95,8 @@ class MPDriver:
         self._h = h
         if params:
             self.set_params(**params)
+        if options:
+            self.set_options(**options)
 
     # ------------------------------------------------------------ lifetime
     def close(self) -> None:
@@ -106,6 +124,22 @@ class MPDriver:
             cur[k] = float(v)
         p = _Params(**cur)
         _check(self._lib.nsw6_set_params(self._h, ctypes.byref(p)), self._lib)
+
+    def get_options(self) -> dict[str, int]:
+        o = _Options()
+        _check(self._lib.nsw6_get_options(self._h, ctypes.byref(o)), self._lib)
+        return {n: getattr(o, n) for n in OPTION_NAMES}
+
+    def set_options(self, **kw: int) -> None:
+        """Scheme switches (nsw6_options): roh2014, explicit_icegen, kk2000,
+        qi_sediment, kin2kin, aerosol_indirect; unnamed ones keep their value."""
+        cur = self.get_options()
+        for k, v in kw.items():
+            if k not in cur:
+                raise KeyError(f"unknown NSW6 option {k!r}")
+            cur[k] = int(v)
+        o = _Options(**cur)
+        _check(self._lib.nsw6_set_options(self._h, ctypes.byref(o)), self._lib)
 
     def set_itelim(self, itelim: int) -> None:
         _check(self._lib.nsw6_set_itelim(self._h, int(itelim)), self._lib)
@@ -285,11 +319,12 @@ def _split_args(args, dt, ct):
     raise TypeError("expected the 50 mp_driver arrays with dt and ct in the reference order")
 
 
-def mp_init(MP_TYPE: str, gall: int, kall: int, gz, gzh, lall_max: int = 1, params: dict | None = None) -> MPDriver:
+def mp_init(MP_TYPE: str, gall: int, kall: int, gz, gzh, lall_max: int = 1, params: dict | None = None,
+            options: dict | None = None) -> MPDriver:
     """Set up the microphysics driver (mod_mp_driver.cpp:11-24): only "NSW6" exists."""
     if MP_TYPE != "NSW6":
         raise ValueError(f"mp_init: NOT appropriate type. Type: {MP_TYPE}")
-    return MPDriver(gall, kall, gz, gzh, lall_max=lall_max, params=params)
+    return MPDriver(gall, kall, gz, gzh, lall_max=lall_max, params=params, options=options)
 
 
 def mp_driver_noalloc(gall: int, kall: int, gz, gzh, *args, dt: float | None = None, ct: float = 0.0,

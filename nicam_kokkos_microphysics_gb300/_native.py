@@ -120,6 +120,10 @@ def load() -> ctypes.CDLL:
     lib.mp_driver_batched.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.mp_driver_mixed.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.nsw6_set_precision.argtypes = [vp, c_int]
+    lib.nsw6_default_options.argtypes = [vp]
+    lib.nsw6_default_options.restype = None
+    lib.nsw6_set_options.argtypes = [vp, vp]
+    lib.nsw6_get_options.argtypes = [vp, vp]
     lib.mp_driver_steps.argtypes = [vp, c_int, ctypes.POINTER(vp), c_double, c_double, c_int]
     lib.mp_driver_tlm.argtypes = [vp, c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), vp, c_double, c_double]
     lib.mp_driver_adjoint.argtypes = [vp, c_int, ctypes.POINTER(vp), ctypes.POINTER(vp), vp, c_double, c_double]

@@ -24,6 +24,15 @@
 //    nsw6_fastmath.cuh) in production, LibMath (CUDA's libm) for checks.
 //
 // Removing the dead terms is exact except for the sign of zero results.
+//
+// With OPT = true the same function also evaluates the branches that the
+// scheme switches select (ConstsT::opt_*, nsw6_options): the classic snow
+// moments (:975-992), the Bergeron terms with Bergeron_param
+// (:1239-1247, :1834-1890), Berry autoconversion and the original accretion
+// (:1091-1099, :1145-1160), the graupel accretion of ice and snow (:1116,
+// :1136-1140), the ice fall speed (:1073-1075) and the cloud number from the
+// CCN input (:676-679); each term enters the limiters and tendencies at the
+// reference's position.
 #pragma once
 
 #include "nsw6_common.cuh"
@@ -47,6 +56,7 @@ template <class D>
 struct CellInT {
   D rhog, tem, gsgam2, q0;
   D rhogq[6];
+  D unccn;   // read only with the aerosol-indirect switch
 };
 
 template <class D>
@@ -54,7 +64,7 @@ struct CellOutT {
   D rhog, rhoge, tem;
   D rhogq[6];
   D q[6];
-  D Vtr, Vts, Vtg;
+  D Vtr, Vts, Vtg, Vti;   // Vti only with OPT
   D rceff, rceff_cld, rctop, tctop;
 };
 using CellIn = CellInT<double>;
@@ -89,7 +99,7 @@ __device__ __forceinline__ float per_dt(float q, float, float rdt) { return q * 
 // D is the type of the state and budget arithmetic: double in both paths; the
 // tangent-linear and adjoint kernels instantiate R = D with their derivative
 // types (nsw6_ad.cuh).
-template <class M, class R, class D = double>
+template <class M, class R, class D = double, bool OPT = false>
 __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, double dt, double rdt,
                                           const CellInT<D>& in, CellOutT<D>& o) {
   constexpr bool kMixed = sizeof(R) == sizeof(float);
@@ -179,9 +189,32 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   // 10^loga * Xs2^b = exp(ln10 * loga + log(Xs2) * b), with loga and b
   // polynomials in tems whose coefficients per moment are folded on the host.
   const R Xs2 = densR * qs * C.rAs;
-  const bool snow = (Xs2 >= R(1.0E-12));
+  const bool roh = !OPT || C.opt_roh != Z;
+  const bool snow = roh && (Xs2 >= R(1.0E-12));
   R mom[7] = {Z, Z, Z, Z, Z, Z, Z};  // MOMs_0, _1, _0bs, _1bs, _2bs, _2ds (= nm 2.25), _5ds_h
   R RMOMs_Vt = Z;
+  R MOMs_2 = Xs2;
+  if constexpr (OPT) {
+    // classic moments of the snow size distribution, :975-992, with
+    // RLMDs = (dens qs / (As N0s GAM_1bs))^(1/4) and integer powers as products
+    if (!roh) {
+      MOMs_2 = Z;
+      if (qs >= R(1.0E-12)) {
+        const R s1 = sqrtR(sqrtR(densR * qs * C.K_rlmds));
+        const R ds = sqrtR(sqrtR(s1));
+        const R s2 = s1 * s1, s3 = s2 * s1, s4 = s2 * s2, s5 = s4 * s1, s6 = s3 * s3;
+        mom[0] = C.K_m0 * s1;
+        mom[1] = C.K_m1 * s2;
+        MOMs_2 = C.K_m2 * s3;
+        mom[2] = C.K_m0bs * s4;
+        mom[3] = C.K_m1bs * s5;
+        mom[4] = C.K_m2bs * s6;
+        mom[5] = C.K_m2ds * (s3 * ds);
+        mom[6] = C.K_m5dsh * sqrtR(s5 * ds);
+        RMOMs_Vt = C.K_rmomvt * ds;
+      }
+    }
+  }
   if (snow) {
     const R tems = dmin(R(-0.1), temc);
     const R logX = mth.log(Xs2);
@@ -195,7 +228,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     }
     RMOMs_Vt = mom[5] / mom[2];
   }
-  const R MOMs_0 = mom[0], MOMs_1 = mom[1], MOMs_2 = Xs2;
+  const R MOMs_0 = mom[0], MOMs_1 = mom[1];
   const R MOMs_0bs = mom[2], MOMs_1bs = mom[3], MOMs_2bs = mom[4], MOMs_2ds = mom[5];
   const R MOMs_5ds_h = mom[6];
 
@@ -215,6 +248,16 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   const R Vtr = C.K_vtr * rho_fact * RLMDr_dr;
   const R Vts = C.K_vts * rho_fact * RMOMs_Vt;
   const R Vtg = C.K_vtg * rho_fact * RLMDg_dg;
+  R Vti = Z;
+  if constexpr (OPT) {
+    // :1073-1075 with sw_constVti = 0 (CONST_Vti is UNDEF)
+    if (C.opt_qised != Z && qi >= R(1.0E-8)) Vti = R(-3.29) * mth.exp(mth.log(densR * qi) * R(0.16));
+  }
+  // cloud number (TagAerosolT / TagAerosolF, :676-684)
+  R Nc = C.Nc_def;
+  if constexpr (OPT) {
+    if (C.opt_indir != Z) Nc = dmax(R(in.unccn) * R(1.0E-6), C.Nc_def);
+  }
 
   // nucleation, :1080-1085: Ni0 = max(exp(-0.1 temc), 1) * 1000 and
   // Qi0 = ice_nuc * Ni0^1.33 / dens, with log(Ni0) = ln 1000 + max(-0.1 temc, 0)
@@ -232,10 +275,15 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     Esi_mod = dmin(C.Esi, C.Esi * eg);
     betai = dmin(C.beta_saut, C.beta_saut * eb);
   }
+  const bool kk = !OPT || C.opt_kk != Z;
+  const R fr = rho_fact;
   const R qcqr = qc * qr;
   R Pracw = Z;
-  if (qcqr >= R(1.0E-12)) Pracw = R(67.0) * mth.pow(qcqr, R(1.15));
-  const R fr = rho_fact;
+  if (kk) {
+    if (qcqr >= R(1.0E-12)) Pracw = R(67.0) * mth.pow(qcqr, R(1.15));
+  } else {
+    Pracw = qc * C.K_raci * RLMDr_3dr * fr;   // Pracw_orig (Erw = Eri = 1)
+  }
   R Psacw = qc * C.K_sacw * MOMs_2ds * fr;
   R Pgacw = qc * C.K_gacw * RLMDg_3dg * fr;
   R Praci = qi * C.K_raci * RLMDr_3dr * fr;
@@ -247,11 +295,32 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   R Pgacr = C.K_gacr * Rdens * fabsR(Vtg - Vtr) *
             (C.K_g13 * RLMDr_1br * RLMDg_3 + C.K_g22 * RLMDr_2br * RLMDg_2 + C.GAM_3br * RLMDr_3br * RLMDg);
   R Pracs = C.K_racs * Rdens * dvrs * (R(2.0) * MOMs_0bs * RLMDr_3 + R(2.0) * MOMs_1bs * RLMDr_2 + MOMs_2bs * RLMDr);
+  R Pgaci = Z, Pgacs = Z;   // Egi = Egs = 0 unless OPT
+  if constexpr (OPT) {
+    Pgaci = qi * C.K_gaci * RLMDg_3dg * fr;
+    R Egs_mod = C.Egs;
+    if (!(warm && C.Egs >= Z)) Egs_mod = dmin(C.Egs, C.Egs * mth.exp(C.gamma_gacs * temc));
+    Pgacs = C.K_gacs * Rdens * Egs_mod * fabsR(Vtg - Vts) *
+            (R(2.0) * MOMs_0bs * RLMDg_3 + R(2.0) * MOMs_1bs * RLMDg_2 + MOMs_2bs * RLMDg);
+  }
 
   // autoconversion, :1147-1172 (KK2000; only the second Praut_kk assignment is live)
   const R rhoqc = densR * qc * R(1000.0);
   R Praut = Z;   // K_aut * pow(0, 2.47) = 0
-  if (qc > Z) Praut = C.K_aut * mth.pow(qc, R(2.47));
+  if (kk) {
+    R K_aut = C.K_aut;
+    if constexpr (OPT) {
+      if (C.opt_indir != Z) K_aut = C.kk_aut * mth.pow(Nc, R(-1.79));
+    }
+    if (qc > Z) Praut = K_aut * mth.pow(qc, R(2.47));
+  } else {
+    // Berry (1968), :1145-1147
+    R Dc = C.Dc_berry;
+    if constexpr (OPT) {
+      if (C.opt_indir != Z) Dc = R(0.146) - R(5.964E-2) * mth.log(Nc / R(2000.0));
+    }
+    Praut = Rdens * R(1.67E-5) * rhoqc * rhoqc / (R(5.0) + R(3.66E-2) * Nc / (Dc * rhoqc + R(EPS)));
+  }
   R Psaut = dmax(betai * (qi - C.qicrt_saut), Z);
 
   // evaporation, sublimation, melting and freezing, :1174-1247
@@ -297,32 +366,58 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   R Pgmlt = dmax(C.K_gdep * Rdens * Gil * ventg + C.K_clf * temc * (Pgacw + Pgacr), Z);
   R Pgfrz = C.K_gfrz * Rdens * efrz * RLMDr_7;
 
-  // limiters, :1249-1296 (iceflg selects; sw_expice = 1; Psfw = Psfi = Pgaut = Pgaci = Pgacs = 0)
+  // Bergeron process (:1239-1247) with Bergeron_param (:1834-1890); it
+  // contributes only when sw_bergeron = 1 (-30 <= temc <= 0, sw_expice = 0)
+  // and iceflg = 1 (temc < 0)
+  const bool expice = !OPT || C.opt_expice != Z;
   const bool cold = !warm;   // iceflg == 1
-  Pigen = sel(cold, dmin(Pigen, dqv_dt));
-  Pidep = sel(cold, dmin(Pidep, dqv_dt));
+  R Psfw = Z, Psfi = Z;
+  if constexpr (OPT) {
+    if (!expice && cold && !(temc + R(30.0) < Z)) {
+      const R tb = dmin(dmax(temc, R(-30.99)), Z);
+      const int it = int(-tb);
+      const R fact = -(tb + R(it - 1));
+      const R a2 = (ONE - fact) * C.berg_a2[it] + fact * C.berg_a2[it + 1];
+      const R ma2 = ONE - a2;
+      const R a1 = ((ONE - fact) * C.berg_a1[it] + fact * C.berg_a1[it + 1]) * mth.pow(R(1.0E-3), ma2);
+      const R dt1 = (mth.exp(C.log_mi50 * ma2) - mth.exp(C.log_mi40 * ma2)) / (a1 * ma2);
+      const R Ni50 = qi * dtR / (C.mi50 * dt1);
+      Psfw = Ni50 * (a1 * mth.pow(C.mi50, a2) + C.K_berg_w * densR * qc);
+      Psfi = qi / dt1;
+    }
+  }
+
+  // limiters, :1249-1296 (iceflg selects; sw_expice = 1 unless OPT; Pgaut = 0)
+  Pigen = sel(cold && expice, dmin(Pigen, dqv_dt));
+  Pidep = sel(cold && expice, dmin(Pidep, dqv_dt));
   Psdep = sel(cold, dmin(Psdep, dqv_dt));
   Pgdep = sel(cold, dmin(Pgdep, dqv_dt));
   Pracw = Pracw + sel(warm, Psacw) + sel(warm, Pgacw);
   Praut = dmin(Praut, dqc_dt);
   Pracw = dmin(Pracw, dqc_dt);
-  Pihom = sel(cold, dmin(Pihom, dqc_dt));
-  Pihtr = sel(cold, dmin(Pihtr, dqc_dt));
+  Pihom = sel(cold && expice, dmin(Pihom, dqc_dt));
+  Pihtr = sel(cold && expice, dmin(Pihtr, dqc_dt));
   Psacw = sel(cold, dmin(Psacw, dqc_dt));
+  if constexpr (OPT) Psfw = sel(cold, dmin(Psfw, dqc_dt));
   Pgacw = sel(cold, dmin(Pgacw, dqc_dt));
   Prevp = dmin(Prevp, dqr_dt);
   Piacr = sel(cold, dmin(Piacr, dqr_dt));
   Psacr = sel(cold, dmin(Psacr, dqr_dt));
   Pgacr = sel(cold, dmin(Pgacr, dqr_dt));
   Pgfrz = sel(cold, dmin(Pgfrz, dqr_dt));
-  Pisub = sel(cold, dmin(Pisub, dqi_dt));
-  Pimlt = sel(warm, dmin(Pimlt, dqi_dt));
+  Pisub = sel(cold && expice, dmin(Pisub, dqi_dt));
+  Pimlt = sel(warm && expice, dmin(Pimlt, dqi_dt));
   Psaut = sel(cold, dmin(Psaut, dqi_dt));
   Praci = sel(cold, dmin(Praci, dqi_dt));
   Psaci = sel(cold, dmin(Psaci, dqi_dt));
+  if constexpr (OPT) {
+    Psfi = sel(cold, dmin(Psfi, dqi_dt));
+    Pgaci = sel(cold, dmin(Pgaci, dqi_dt));
+  }
   Pssub = sel(cold, dmin(Pssub, dqs_dt));
   Psmlt = sel(warm, dmin(Psmlt, dqs_dt));
   Pracs = sel(cold, dmin(Pracs, dqs_dt));
+  if constexpr (OPT) Pgacs = dmin(Pgacs, dqs_dt);
   Pgsub = sel(cold, dmin(Pgsub, dqg_dt));
   Pgmlt = sel(warm, dmin(Pgmlt, dqg_dt));
   R Piacr_s = sel(!d1, Piacr);
@@ -340,14 +435,27 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   };
   // scaling by fac = 1 is exact and skipped
   R fac;
-  fac = limiter(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw, dqc_dt);  // [QC]
-  if (fac != ONE) {
-    Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Pgacw *= fac;
-  }
-  fac = limiter(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g, dqi_dt);  // [QI]
-  if (fac != ONE) {
-    Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
-    Praci_s *= fac; Psaci *= fac; Praci_g *= fac;
+  if constexpr (!OPT) {
+    fac = limiter(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw, dqc_dt);  // [QC]
+    if (fac != ONE) {
+      Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Pgacw *= fac;
+    }
+    fac = limiter(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g, dqi_dt);  // [QI]
+    if (fac != ONE) {
+      Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
+      Praci_s *= fac; Psaci *= fac; Praci_g *= fac;
+    }
+  } else {
+    fac = limiter(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Psfw - Pgacw, dqc_dt);  // [QC]
+    if (fac != ONE) {
+      Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Psfw *= fac; Pgacw *= fac;
+    }
+    fac = limiter(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Psfi - Praci_g - Pgaci,
+                  dqi_dt);  // [QI]
+    if (fac != ONE) {
+      Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
+      Praci_s *= fac; Psaci *= fac; Psfi *= fac; Praci_g *= fac; Pgaci *= fac;
+    }
   }
   fac = limiter(+Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz,
                 dqr_dt);  // [QR]
@@ -359,23 +467,47 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   if (fac != ONE) {
     Prevp *= fac; Pisub *= fac; Pssub *= fac; Pgsub *= fac; Pigen *= fac; Pidep *= fac; Psdep *= fac; Pgdep *= fac;
   }
-  fac = limiter(+Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs, dqs_dt);  // [QS]
-  if (fac != ONE) {
-    Psdep *= fac; Psacw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac; Psaci *= fac;
-    Pssub *= fac; Psmlt *= fac; Pracs *= fac;
-  }
-  fac = limiter(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt, dqg_dt);  // [QG]
-  if (fac != ONE) {
-    Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
-    Pracs *= fac; Pgsub *= fac; Pgmlt *= fac;
+  if constexpr (!OPT) {
+    fac = limiter(+Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs, dqs_dt);  // [QS]
+    if (fac != ONE) {
+      Psdep *= fac; Psacw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac; Psaci *= fac;
+      Pssub *= fac; Psmlt *= fac; Pracs *= fac;
+    }
+    fac = limiter(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt, dqg_dt);  // [QG]
+    if (fac != ONE) {
+      Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
+      Pracs *= fac; Pgsub *= fac; Pgmlt *= fac;
+    }
+  } else {
+    fac = limiter(+Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs -
+                      Pgacs,
+                  dqs_dt);  // [QS]
+    if (fac != ONE) {
+      Psdep *= fac; Psacw *= fac; Psfw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac;
+      Psaci *= fac; Psfi *= fac; Pssub *= fac; Psmlt *= fac; Pracs *= fac; Pgacs *= fac;
+    }
+    fac = limiter(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt,
+                  dqg_dt);  // [QG]
+    if (fac != ONE) {
+      Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
+      Pgaci *= fac; Pracs *= fac; Pgacs *= fac; Pgsub *= fac; Pgmlt *= fac;
+    }
   }
 
   // tendencies, :1479-1559
-  R qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;
-  R qr_t = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;
-  R qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;
-  R qs_t = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
-  R qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
+  R qc_t, qr_t, qi_t, qs_t, qg_t;
+  qr_t = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;
+  if constexpr (!OPT) {
+    qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;
+    qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;
+    qs_t = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
+    qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
+  } else {
+    qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Psfw - Pgacw;
+    qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Psfi - Praci_g - Pgaci;
+    qs_t = +Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs - Pgacs;
+    qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt;
+  }
   qc_t = dmax(qc_t, -dqc_dt);
   qr_t = dmax(qr_t, -dqr_dt);
   qi_t = dmax(qi_t, -dqi_dt);
@@ -407,12 +539,20 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   o.Vtr = D(Vtr);
   o.Vts = D(Vts);
   o.Vtg = D(Vtg);
+  o.Vti = D(Vti);
 
   // effective radius and cloud top, :1566-1592
   {
     const R r2_min = R(1.0E-10), q_min = R(1.0E-5);
-    const R rf_qc = mth.pow(C.coef_xf * (rhoqc * C.K_xf) + R(EPS), R(0.33333333));
-    const R r2_qc = C.K_r2c * (rf_qc * rf_qc);
+    R K_xf = C.K_xf, K_r2c = C.K_r2c;
+    if constexpr (OPT) {
+      if (C.opt_indir != Z) {
+        K_xf = R(1.0E-9) / Nc;
+        K_r2c = C.coef_dgam * (Nc * R(1.0E+6));
+      }
+    }
+    const R rf_qc = mth.pow(C.coef_xf * (rhoqc * K_xf) + R(EPS), R(0.33333333));
+    const R r2_qc = K_r2c * (rf_qc * rf_qc);
     const R r2_qr = C.K_r2r * RLMDr_3;
     const R r3_qc = C.coef_xf * densR * qc;
     const R r3_qr = C.coef_xf * densR * qr;

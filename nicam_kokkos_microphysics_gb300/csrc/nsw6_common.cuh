@@ -71,6 +71,21 @@ struct ConstsT {
   R roh_a[28], roh_b[28];   // per snow moment: ln10*loga and b as cubics in tems
   R ln1000;
   R XNi_eps, Di_eps;   // ice number and diameter at the floor rhoqi = EPS (no ice)
+  // Scheme switches (1 = on) and the constants only the switched branches use
+  // (the kernels instantiated with OPT = true read them; nsw6_options):
+  //   opt_roh     Roh and Satoh (2014) snow moments (0: the classic moments)
+  //   opt_expice  explicit ice generation (0: Bergeron terms, no Pigen/Pidep/
+  //               Pihom/Pihtr/Pisub/Pimlt, mixed-phase saturation adjustment)
+  //   opt_kk      KK2000 warm rain (0: Berry autoconversion, orig. accretion)
+  //   opt_qised   QI sediments ("4WATER")
+  //   opt_kin2kin kinetic-energy correction of the transport (0: KIN2EIN)
+  //   opt_indir   cloud number from the CCN input (aerosol indirect effect)
+  R opt_roh, opt_expice, opt_kk, opt_qised, opt_kin2kin, opt_indir;
+  R Egi, K_gaci, K_gacs;                         // graupel-ice / graupel-snow accretion
+  R K_rlmds, K_m0, K_m1, K_m2, K_m0bs, K_m1bs, K_m2bs, K_m2ds, K_m5dsh, K_rmomvt;   // classic snow moments
+  R berg_a1[32], berg_a2[32];                    // Bergeron_param tables
+  R K_berg_w;                                    // PI Eiw Ri50^2 vti50
+  R sat_ulimit, sat_llimit;                      // SATURATION_Setrange of the mixed-phase adjustment
 };
 using Consts = ConstsT<double>;
 using ConstsF = ConstsT<float>;
@@ -120,6 +135,7 @@ struct Problem {
   int itelim;
   int math_lib;                // 0 table-driven transcendentals, 1 CUDA libm
   int mixed;                   // 0 plain FP64 step, 1 mixed precision (FP32 process rates)
+  int opt;                     // 1: the kernels with the scheme switches (FP64, FastMath)
   const double* grid;          // [GF_COUNT][kall]
   const double* fmtab;         // fast-math tables (nsw6_fastmath.cuh)
   double* const* a;            // not used on device
@@ -131,14 +147,18 @@ struct Problem {
   double *precip_rhoe, *precip_lh_heat, *precip_rhophi, *precip_rhokin;   // [lall][gall]
   double *re_liquid, *re_solid, *re_cld;
   double *rctop, *rwtop, *tctop;         // [lall][1][gall]
+  const double* unccn;         // read by the aerosol-indirect switch only
   const double *gsgam2, *gsgam2h, *gam2, *gam2h;
   const double *ix, *iy, *iz, *jx, *jy, *jz;
   const double* z;
   double *GDCLW, *GDCFRC, *GPREC;
   // workspace
-  double* zdis;                // [lall][6][kall][gall]: zdis0 (QR,QS,QG) then zdis0h (QR,QS,QG)
-  unsigned long long* zmax;    // [lall][6][kall] ordered keys, reset to 0
-  unsigned long long* zmin;    // [lall][6][kall] ordered keys, reset to ~0
+  // Sedimenting tracers: ntr = 3 (QR, QS, QG) or 4 with QI sedimentation
+  // (QR, QI, QS, QG), in the reference's tracer order.
+  int ntr;
+  double* zdis;                // [lall][2 ntr][kall][gall]: zdis0 per tracer, then zdis0h per tracer
+  unsigned long long* zmax;    // [lall][2 ntr][kall] ordered keys, reset to 0
+  unsigned long long* zmin;    // [lall][2 ntr][kall] ordered keys, reset to ~0
   DevStatus* status;
 };
 

@@ -44,6 +44,8 @@ using namespace nsw6;
 struct nsw6_handle {
   int gall = 0, kall = 0, lall_max = 0;
   nsw6_params params{};
+  nsw6_options opts{1, 1, 1, 0, 0, 0};
+  int opt_active = 0;   // a switch differs from the reference configuration
   Consts C{};
   double* d_grid = nullptr;
   double* d_fmtab = nullptr;
@@ -72,6 +74,7 @@ struct nsw6_handle {
   int graph_lall = 0, graph_mixed = -1, graph_math = -1, graph_itelim = 0;
   double graph_dt = 0.0;
   nsw6_params graph_params{};
+  nsw6_options graph_opts{};
   // device staging of the 50 arguments for host-memory calls (allocated by the
   // first such call)
   double* d_stage = nullptr;
@@ -84,6 +87,8 @@ struct nsw6_handle {
   double t_sum[2] = {0.0, 0.0};
   int t_steps = 0;
 };
+
+extern "C" void nsw6_default_options(nsw6_options* o);
 
 namespace {
 
@@ -106,20 +111,23 @@ double gammafunc(double xx) {
 // beta_gaut = 0), GlobalParams defaults (mod_mp_nsw6.h:16-123), the
 // effective-radius constants of mp_nsw6_new::init (:506-517) and
 // SATURATION_Setup with EIN_TYPE = "SIMPLE" (mod_satadjust.cpp:24-47).
-Consts make_consts(const nsw6_params& p) {
+Consts make_consts(const nsw6_params& p, const nsw6_options& o) {
   Consts c;
   std::memset(&c, 0, sizeof(c));
   const double rho_s = 100.0, rho_g = 400.0;
-  const double Br = 3.0, Bs = 2.0, Bg = 3.0, Dr = 0.50, Ds = 0.25, Dg = 0.50;
-  (void)rho_s;
+  // Roh_flag (mod_mp_nsw6.cpp:345-357) changes N0g, As, Bs, Esi, Egi, Egs from
+  // their GlobalParams values (mod_mp_nsw6.h:16-123)
+  const bool roh = o.roh2014 != 0;
+  const double Br = 3.0, Bs = roh ? 2.0 : 3.0, Bg = 3.0, Dr = 0.50, Ds = 0.25, Dg = 0.50;
   c.N0r = 8.E+6;
   c.N0s = 3.E+6;
-  c.N0g = 4.0E+8;
+  c.N0g = roh ? 4.0E+8 : 4.E+6;
   c.Ar = PI * DWATR / 6.0;
-  c.As = 0.069;
+  c.As = roh ? 0.069 : PI * rho_s / 6.0;
   c.Ag = PI * rho_g / 6.0;
-  c.Esi = 0.25;
-  c.Egs = 0.0;
+  c.Esi = roh ? 0.25 : 1.0;
+  c.Egi = roh ? 0.0 : 0.1;
+  c.Egs = roh ? 0.0 : 1.0;
   c.gamma_sacr = 6.0E-2;
   c.gamma_gacs = 90.E-3;
   c.mi = 4.19E-13;
@@ -222,7 +230,6 @@ Consts make_consts(const nsw6_params& p) {
   c.K_xf = 1.0E-9 / c.Nc_def;
   c.K_r2c = c.coef_dgam * (c.Nc_def * 1.0E+6);
   c.K_r2r = 0.25 * c.N0r * GAM_3;
-  (void)GAM;
   // Roh and Satoh (2014) moments (mod_mp_nsw6.cpp:994-1057): loga(nm, t) and
   // b(nm, t) expanded as cubics in t = tems for nm = 0, 1, 2, 3, 4, 2.25, 1.625
   static const double nms[7] = {0.0, 1.0, 2.0, 3.0, 4.0, 2.25, 1.625};
@@ -239,7 +246,48 @@ Consts make_consts(const nsw6_params& p) {
       c.roh_b[4 * i + j] = eb[j];
     }
   }
+  // the switches and the constants of the switched branches (nsw6_cell.cuh)
+  c.opt_roh = roh ? 1.0 : 0.0;
+  c.opt_expice = (roh || o.explicit_icegen) ? 1.0 : 0.0;   // mp_nsw6_init forces it with Roh_flag
+  c.opt_kk = o.kk2000 ? 1.0 : 0.0;
+  c.opt_qised = o.qi_sediment ? 1.0 : 0.0;
+  c.opt_kin2kin = o.kin2kin ? 1.0 : 0.0;
+  c.opt_indir = o.aerosol_indirect ? 1.0 : 0.0;
+  c.K_gaci = 0.25 * PI * c.Egi * c.N0g * c.Cg * c.GAM_3dg;
+  c.K_gacs = c.As * 0.25 * PI * c.N0g;
+  c.K_rlmds = 1.0 / (c.As * c.N0s * c.GAM_1bs);
+  c.K_m0 = c.N0s * GAM;
+  c.K_m1 = c.N0s * GAM_2;
+  c.K_m2 = c.N0s * GAM_3;
+  c.K_m0bs = c.N0s * c.GAM_1bs;
+  c.K_m1bs = c.N0s * c.GAM_2bs;
+  c.K_m2bs = c.N0s * c.GAM_3bs;
+  c.K_m2ds = c.N0s * c.GAM_3ds;
+  c.K_m5dsh = c.N0s * c.GAM_5ds_h;
+  c.K_rmomvt = c.GAM_1bsds / c.GAM_1bs;
+  // Bergeron_param tables (mod_mp_nsw6.cpp:1845-1861)
+  static const double a1t[32] = {0.0001E-7, 0.7939E-7, 0.7841E-6, 0.3369E-5, 0.4336E-5, 0.5285E-5, 0.3728E-5,
+                                 0.1852E-5, 0.2991E-6, 0.4248E-6, 0.7434E-6, 0.1812E-5, 0.4394E-5, 0.9145E-5,
+                                 0.1725E-4, 0.3348E-4, 0.1725E-4, 0.9175E-5, 0.4412E-5, 0.2252E-5, 0.9115E-6,
+                                 0.4876E-6, 0.3473E-6, 0.4758E-6, 0.6306E-6, 0.8573E-6, 0.7868E-6, 0.7192E-6,
+                                 0.6513E-6, 0.5956E-6, 0.5333E-6, 0.4834E-6};
+  static const double a2t[32] = {0.0100, 0.4006, 0.4831, 0.5320, 0.5307, 0.5319, 0.5249, 0.4888,
+                                 0.3849, 0.4047, 0.4318, 0.4771, 0.5183, 0.5463, 0.5651, 0.5813,
+                                 0.5655, 0.5478, 0.5203, 0.4906, 0.4447, 0.4126, 0.3960, 0.4149,
+                                 0.4320, 0.4506, 0.4483, 0.4460, 0.4433, 0.4413, 0.4382, 0.4361};
+  std::memcpy(c.berg_a1, a1t, sizeof(a1t));
+  std::memcpy(c.berg_a2, a2t, sizeof(a2t));
+  const double Eiw = 1.0, vti50 = 1.0;
+  c.K_berg_w = PI * Eiw * c.Ri50 * c.Ri50 * vti50;
+  c.sat_ulimit = 273.16;   // SATURATION_Setrange of the ice_adjust branch, :657-658
+  c.sat_llimit = 233.16;
   return c;
+}
+
+Consts make_consts(const nsw6_params& p) {
+  nsw6_options o;
+  nsw6_default_options(&o);
+  return make_consts(p, o);
 }
 
 // Fast-math tables (nsw6_fastmath.cuh), computed in extended precision:
@@ -389,6 +437,11 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.rdt = 1.0 / dt;
   P.math_lib = h->math_lib;
   P.mixed = h->mixed;
+  P.opt = h->opt_active;
+  P.ntr = h->opts.qi_sediment ? 4 : 3;
+  if (h->opt_active && (h->mixed != 0 || h->math_lib != 0)) return NSW6_ERR_UNSUPPORTED;
+  if (h->opts.aerosol_indirect && !a[A_unccn]) return NSW6_ERR_BAD_ARG;
+  P.unccn = a[A_unccn];
   P.rhog = a[A_rhog];
   P.rhogvx = a[A_rhogvx];
   P.rhogvy = a[A_rhogvy];
@@ -515,7 +568,7 @@ int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
 
 int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b) {
   if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
-  if (h->kall > DERIV_MAX_KALL) return NSW6_ERR_UNSUPPORTED;
+  if (h->kall > DERIV_MAX_KALL || h->opt_active) return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
     if ((arg_is_read(i) || arg_is_written(i)) && (!a[i] || !b[i])) return NSW6_ERR_BAD_ARG;
   if (!h->d_dparam) {
@@ -528,7 +581,7 @@ int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b) {
 }
 
 int run_serial(nsw6_handle* h, int lall, double* const* a, double dt) {
-  if (h->kall > DERIV_MAX_KALL) return NSW6_ERR_UNSUPPORTED;
+  if (h->kall > DERIV_MAX_KALL || h->opt_active) return NSW6_ERR_UNSUPPORTED;
   int rc = deriv_prepass(h, lall, a, dt);
   if (rc != NSW6_OK) return rc;
   Problem P;
@@ -577,9 +630,11 @@ int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const doubl
   double* htab = hgrid + GF_COUNT * (size_t)kall;
   build_fastmath_tables(htab);
   const size_t KG = (size_t)kall * gall;
-  const size_t nkey = (size_t)lall_max * 6 * kall;
+  // departure distances and extrema: 2 rows per sedimenting tracer, up to 4
+  // tracers with QI sedimentation
+  const size_t nkey = (size_t)lall_max * 8 * kall;
   bool ok = cudaMalloc(&h->d_grid, sizeof(double) * GF_COUNT * kall) == cudaSuccess &&
-            cudaMalloc(&h->d_zdis, sizeof(double) * 6 * KG * lall_max) == cudaSuccess &&
+            cudaMalloc(&h->d_zdis, sizeof(double) * 8 * KG * lall_max) == cudaSuccess &&
             cudaMalloc(&h->d_zmax, sizeof(unsigned long long) * nkey) == cudaSuccess &&
             cudaMalloc(&h->d_zmin, sizeof(unsigned long long) * nkey) == cudaSuccess &&
             cudaMalloc(&h->d_status, sizeof(DevStatus)) == cudaSuccess &&
@@ -623,7 +678,37 @@ int nsw6_destroy(nsw6_handle* h) {
 int nsw6_set_params(nsw6_handle* h, const nsw6_params* p) {
   if (!h || !p) return NSW6_ERR_BAD_ARG;
   h->params = *p;
-  h->C = make_consts(h->params);
+  h->C = make_consts(h->params, h->opts);
+  return NSW6_OK;
+}
+
+void nsw6_default_options(nsw6_options* o) {
+  if (!o) return;
+  o->roh2014 = 1;
+  o->explicit_icegen = 1;
+  o->kk2000 = 1;
+  o->qi_sediment = 0;
+  o->kin2kin = 0;
+  o->aerosol_indirect = 0;
+}
+
+int nsw6_set_options(nsw6_handle* h, const nsw6_options* o) {
+  if (!h || !o) return NSW6_ERR_BAD_ARG;
+  const int v[6] = {o->roh2014, o->explicit_icegen, o->kk2000, o->qi_sediment, o->kin2kin, o->aerosol_indirect};
+  for (int x : v)
+    if (x != 0 && x != 1) return NSW6_ERR_BAD_ARG;
+  h->opts = *o;
+  h->opts.explicit_icegen = (o->roh2014 || o->explicit_icegen) ? 1 : 0;
+  nsw6_options d;
+  nsw6_default_options(&d);
+  h->opt_active = std::memcmp(&h->opts, &d, sizeof(d)) != 0;
+  h->C = make_consts(h->params, h->opts);
+  return NSW6_OK;
+}
+
+int nsw6_get_options(const nsw6_handle* h, nsw6_options* o) {
+  if (!h || !o) return NSW6_ERR_BAD_ARG;
+  *o = h->opts;
   return NSW6_OK;
 }
 
@@ -839,7 +924,8 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
   if (rc != NSW6_OK) return rc;
   bool same = h->graph && h->graph_lall == lall && h->graph_dt == dt && h->graph_mixed == h->mixed &&
               h->graph_math == h->math_lib && h->graph_itelim == h->itelim &&
-              std::memcmp(&h->graph_params, &h->params, sizeof(nsw6_params)) == 0;
+              std::memcmp(&h->graph_params, &h->params, sizeof(nsw6_params)) == 0 &&
+              std::memcmp(&h->graph_opts, &h->opts, sizeof(nsw6_options)) == 0;
   for (int i = 0; same && i < A_COUNT; ++i) same = h->graph_args[i] == args[i];
   if (!same) {
     if (h->graph) {
@@ -870,6 +956,7 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
     h->graph_math = h->math_lib;
     h->graph_itelim = h->itelim;
     h->graph_params = h->params;
+    h->graph_opts = h->opts;
   }
   for (int i = 0; i < nsteps; ++i)
     if (cudaGraphLaunch(h->graph, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;

@@ -58,17 +58,23 @@ __device__ __forceinline__ FloatMath make_math<FloatMath>(const double*) {
   return FloatMath{};
 }
 
-// Shared memory of the cell kernel: fall speeds [3][K][CELL_TG] (type R), the
-// grid block [GF_COUNT][K] and the fast-math tables (doubles), and for R =
-// float FP32 copies of the four reciprocal rows the departure distances use.
+// Shared memory of the cell kernel: fall speeds [ntr][K][CELL_TG] (type R; 3
+// sedimenting tracers, 4 in the kernel with the scheme switches), the grid
+// block [GF_COUNT][K] and the fast-math tables (doubles), and for R = float
+// FP32 copies of the four reciprocal rows the departure distances use.
 template <class R>
-__host__ __device__ constexpr size_t cell_vts_doubles(int K) {
-  return (3 * (size_t)K * CELL_TG * sizeof(R) + sizeof(double) - 1) / sizeof(double);
+__host__ __device__ constexpr size_t cell_vts_doubles(int K, int nv = 3) {
+  return (nv * (size_t)K * CELL_TG * sizeof(R) + sizeof(double) - 1) / sizeof(double);
 }
 
-template <class M, class R>
+// OPT: the kernel with the scheme switches (FP64 only): the switched branches
+// of nsw6_cell, the CCN input, and the ice fall speed with its departure
+// distances when QI sediments.
+template <class M, class R, bool OPT = false>
 __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, ConstsT<R> C) {
   constexpr bool kMixed = sizeof(R) == sizeof(float);
+  constexpr int NV = OPT ? 4 : 3;            // fall-speed rows in shared memory
+  const int ntr = OPT ? P.ntr : 3;          // sedimenting tracers of this call
   extern __shared__ double sm[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
   const int l = blockIdx.y;
@@ -76,8 +82,8 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
   const size_t KG = (size_t)K * G;
   const size_t off = (size_t)l * KG;
   const size_t offq = (size_t)l * NQ * KG;
-  R* vts = reinterpret_cast<R*>(sm);                   // [3][K][CELL_TG] fall speeds of QR, QS, QG
-  double* grid = sm + cell_vts_doubles<R>(K);          // [GF_COUNT][K]
+  R* vts = reinterpret_cast<R*>(sm);                   // [ntr][K][CELL_TG] fall speeds, tracer order
+  double* grid = sm + cell_vts_doubles<R>(K, NV);      // [GF_COUNT][K]
   double* tab = grid + GF_COUNT * K;                   // [FM_TABLE_DOUBLES]
   float* gridf = reinterpret_cast<float*>(tab + FM_TABLE_DOUBLES);  // [4][K], mixed only
   unsigned short* perm = reinterpret_cast<unsigned short*>(gridf + 4 * K);  // [nlev * CELL_TG], FP64 only
@@ -86,7 +92,7 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
       (reinterpret_cast<uintptr_t>(key + (K - 2) * CELL_TG) + 15) & ~(uintptr_t)15);
   __shared__ int bucket[33];
 
-  for (int c = threadIdx.x; c < 3 * K * CELL_TG; c += blockDim.x) vts[c] = R(0.0);
+  for (int c = threadIdx.x; c < NV * K * CELL_TG; c += blockDim.x) vts[c] = R(0.0);
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) grid[c] = P.grid[c];
   if (!kMixed)
     for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
@@ -150,8 +156,9 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
     in.q0 = P.q[iq];
 #pragma unroll
     for (int n = 0; n < 6; ++n) in.rhogq[n] = P.rhogq[iq + (size_t)n * KG];
+    in.unccn = OPT ? P.unccn[i] : 0.0;
     CellOut o;
-    nsw6_cell(C, mth, P.dt, P.rdt, in, o);
+    nsw6_cell<M, R, double, OPT>(C, mth, P.dt, P.rdt, in, o);
     P.rhog[i] = o.rhog;
     P.rhoge[i] = o.rhoge;
     P.tem[i] = o.tem;
@@ -161,9 +168,11 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
     for (int n = 1; n < 6; ++n) P.q[iq + (size_t)n * KG] = o.q[n];
     P.re_liquid[i] = o.rceff;
     P.re_cld[i] = o.rceff_cld;
+    // tracer order of the transport: QR, (QI,) QS, QG
     vts[(0 * K + k) * CELL_TG + gx] = R(o.Vtr);
-    vts[(1 * K + k) * CELL_TG + gx] = R(o.Vts);
-    vts[(2 * K + k) * CELL_TG + gx] = R(o.Vtg);
+    if (ntr == 4) vts[(1 * K + k) * CELL_TG + gx] = R(o.Vti);
+    vts[((ntr - 2) * K + k) * CELL_TG + gx] = R(o.Vts);
+    vts[((ntr - 1) * K + k) * CELL_TG + gx] = R(o.Vtg);
     if (k == kmax) {
       // The reference writes the cloud-top scalars from every level in parallel
       // (mod_mp_nsw6.cpp:1579-1592); the sequential order, in which the top
@@ -178,8 +187,9 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
   __syncthreads();
 
   // Departure distances (vadv1d_prep) and their per-level region extrema.
-  // Row s = t + 3*half: t = QR, QS, QG; half = 0 full levels (mkmin = kmin,
-  // dz = dgz), 1 half levels (mkmin = kmin+1, dz = dgzh, wp = Vtermh).
+  // Row s = t + ntr*half: t = the sedimenting tracer; half = 0 full levels
+  // (mkmin = kmin, dz = dgz), 1 half levels (mkmin = kmin+1, dz = dgzh,
+  // wp = Vtermh).
   const R* rdgz;
   const R* rdgzh;
   const R* rdzs;
@@ -198,9 +208,10 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
   const R dtR = R(P.dt), hdt2R = R(P.hdt2), sdt3R = R(P.sdt3);
   // one row at a time: its half-level velocities wh(j) first (each is used by
   // three departure distances), then the distances
-  for (int s = 0; s < 6; ++s) {
-    const int t = s % 3;
-    const int half = s / 3;
+  const int nrow = 2 * ntr;
+  for (int s = 0; s < nrow; ++s) {
+    const int t = s % ntr;
+    const int half = s / ntr;
     const int mkmin = half ? kmin + 1 : kmin;
     for (int c = threadIdx.x; c < K * CELL_TG; c += blockDim.x) {
       const int j = c / CELL_TG, gx = c % CELL_TG;
@@ -231,7 +242,7 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
       auto wh = [&](int j) { return whs[j * CELL_TG + gx]; };
       z = half ? double(vadv_zdis_wh<R>(wh, rdgzh, rdzsh, k, mkmin, dtR, hdt2R, sdt3R))
                : double(vadv_zdis_wh<R>(wh, rdgz, rdzs, k, mkmin, dtR, hdt2R, sdt3R));
-      P.zdis[((size_t)l * 6 + s) * KG + (size_t)k * G + g] = z;
+      P.zdis[((size_t)l * nrow + s) * KG + (size_t)k * G + g] = z;
     }
     // NaN never wins the reference's comparisons, so it is left out
     unsigned long long kmx = (valid && z == z) ? order_key(z) : 0ull;
@@ -244,7 +255,7 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
       kmn = b < kmn ? b : kmn;
     }
     if ((threadIdx.x & 31) == 0) {
-      const size_t e = ((size_t)l * 6 + s) * K + k;
+      const size_t e = ((size_t)l * nrow + s) * K + k;
       if (kmx != 0ull) atomicMax(&P.zmax[e], kmx);
       if (kmn != ~0ull) atomicMin(&P.zmin[e], kmn);
     }
@@ -255,17 +266,20 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
 
 // ------------------------------------------------------------------ kernel 2
 // Shared-memory field slots, each [K][COL_TG] doubles.
+// S_DQI (the tendency of sedimenting QI) exists in the kernel with the scheme
+// switches only.
 enum ColSlot {
   S_KINH, S_KINV, S_DRHOE, S_DRHOPHI, S_DKINH, S_DKINV, S_DRHOGU, S_DRHOGV, S_DRHOGW,
-  S_DQR, S_DQS, S_DQG, S_RHOF, S_F, S_RGS, S_BASE, S_VI, S_VJ, S_COUNT
+  S_DQR, S_DQS, S_DQG, S_RHOF, S_F, S_RGS, S_BASE, S_VI, S_VJ, S_COUNT,
+  S_DQI = S_COUNT, S_COUNT_OPT
 };
 
 struct ColumnShared {
-  double* f;         // [S_COUNT][K][COL_TG]
+  double* f;         // [S_COUNT (S_COUNT_OPT)][K][COL_TG]
   double* grid;      // [GF_COUNT][K]
   double* colacc;    // [6][COL_TG]: precip0, precip1, lh_heat, rhoe, rhophi, rhokin
-  int* bmin;         // [6][K]
-  int* bmax;         // [6][K]
+  int* bmin;         // [2 ntr][K] (room for 8 rows with the switches)
+  int* bmax;         // [2 ntr][K]
   unsigned char* kc; // [K][COL_TG]
 };
 
@@ -342,10 +356,21 @@ __device__ __forceinline__ float flux_integral_f(const float* rhof_col, const fl
 // the quotients of the final state use a plain reciprocal; the mass, energy
 // and kinetic-energy fluxes, their sums and the saturation adjustment stay
 // FP64.
-template <int COL_TG, class M, bool MIX>
+//
+// OPT: the kernel with the scheme switches (FP64): QI sedimentation (4
+// tracers), the KIN2KIN kinetic-energy correction (mod_precip_transport.cpp:
+// 1012-1068) and the mixed-phase saturation adjustment (satadjust_all,
+// mod_satadjust.cpp:620-769).
+template <int COL_TG, class M, bool MIX, bool OPT = false>
 __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   extern __shared__ double smraw[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  constexpr int NSLOT = OPT ? S_COUNT_OPT : S_COUNT;
+  constexpr int NROW_MAX = OPT ? 8 : 6;
+  const int ntr = OPT ? P.ntr : 3;
+  const int nrow = 2 * ntr;
+  const bool kin2kin = OPT && C.opt_kin2kin != 0.0;
+  const bool ice_adj = OPT && C.opt_expice == 0.0;
   const int l = blockIdx.y;
   const int g0 = blockIdx.x * COL_TG;
   const size_t KG = (size_t)K * G;
@@ -356,11 +381,11 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
 
   ColumnShared S;
   S.f = smraw;
-  S.grid = S.f + (size_t)S_COUNT * ncell;
+  S.grid = S.f + (size_t)NSLOT * ncell;
   S.colacc = S.grid + GF_COUNT * K;
   S.bmin = reinterpret_cast<int*>(S.colacc + 6 * COL_TG);
-  S.bmax = S.bmin + 6 * K;
-  S.kc = reinterpret_cast<unsigned char*>(S.bmax + 6 * K);
+  S.bmax = S.bmin + NROW_MAX * K;
+  S.kc = reinterpret_cast<unsigned char*>(S.bmax + NROW_MAX * K);
   double* tab = reinterpret_cast<double*>(
       (reinterpret_cast<uintptr_t>(S.kc + (size_t)K * COL_TG) + 15) & ~(uintptr_t)15);
   long long* zkey = reinterpret_cast<long long*>(tab + FM_TABLE_DOUBLES);   // [2][K]: cmp_key of gzh, gzshift
@@ -393,14 +418,14 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   const double* dfact = S.grid + GF_DFACT * K;
 
   // ---- kcell_min/max per level from the region extrema (mod_vadv1d.cpp:316-353)
-  for (int c = threadIdx.x; c < 6 * K; c += blockDim.x) {
+  for (int c = threadIdx.x; c < nrow * K; c += blockDim.x) {
     const int s = c / K, k = c % K;
-    const int half = s / 3;
+    const int half = s / ntr;
     const int mkmin = half ? kmin + 1 : kmin;
     const double* zh = half ? gzs : gzh;
     int bmn = k, bmx = k;
     if (k >= mkmin && k <= kmax) {
-      const size_t e = ((size_t)l * 6 + s) * K + k;
+      const size_t e = ((size_t)l * nrow + s) * K + k;
       const unsigned long long kx = P.zmax[e], kn = P.zmin[e];
       double zzmax = DBL_MIN, zzmin = DBL_MIN;
       if (kx != 0ull) {
@@ -435,6 +460,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     for (int s = S_KINH; s <= S_DQG; ++s) F(s)[c] = 0.0;
+    if (OPT) F(S_DQI)[c] = 0.0;
     F(S_RGS)[c] = 0.0;
     F(S_VI)[c] = 0.0;
     F(S_VJ)[c] = 0.0;
@@ -460,16 +486,17 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   __syncthreads();
 
   // ---- sedimentation of QR, QS, QG (mod_precip_transport.cpp:767-955)
-  const int tracer[3] = {I_QR, I_QS, I_QG};
-  for (int t = 0; t < 3; ++t) {
-    const int nq = tracer[t];
-    // departure distances of this region: [6][K][G] rows t (full) and 3 + t (half)
-    const double* zdis0 = P.zdis + ((size_t)l * 6 + t) * KG;
-    const double* zdis0h = P.zdis + ((size_t)l * 6 + 3 + t) * KG;
+  // tracers in the reference's order (QI sediments with "4WATER")
+  for (int t = 0; t < ntr; ++t) {
+    const int nq = ntr == 4 ? (t == 0 ? I_QR : t == 1 ? I_QI : t == 2 ? I_QS : I_QG) : (t == 0 ? I_QR : t == 1 ? I_QS : I_QG);
+    const int dqs_slot = nq == I_QR ? S_DQR : nq == I_QS ? S_DQS : nq == I_QG ? S_DQG : S_DQI;
+    // departure distances of this region: [2 ntr][K][G] rows t (full) and ntr + t (half)
+    const double* zdis0 = P.zdis + ((size_t)l * nrow + t) * KG;
+    const double* zdis0h = P.zdis + ((size_t)l * nrow + ntr + t) * KG;
     const int* bmn_f = S.bmin + t * K;
     const int* bmx_f = S.bmax + t * K;
-    const int* bmn_h = S.bmin + (3 + t) * K;
-    const int* bmx_h = S.bmax + (3 + t) * K;
+    const int* bmn_h = S.bmin + (ntr + t) * K;
+    const int* bmx_h = S.bmax + (ntr + t) * K;
     const double* rhogq_n = P.rhogq + offq + (size_t)nq * KG;
     const double* q_n = P.q + offq + (size_t)nq * KG;
 
@@ -549,7 +576,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         const double d = (fk1 - fk) * rdgz[k];
         switch (f) {
           case 0:
-            F(S_DQR + t)[c] = -d;
+            F(dqs_slot)[c] = -d;
             if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + (-fk / dt);
             break;
           case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - d; break;
@@ -671,7 +698,14 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     P.rhogq[iq + (size_t)I_QR * KG] = P.rhogq[iq + (size_t)I_QR * KG] + dqr;
     rhog = rhog + dqr;
     rhoge = rhoge - dqr * GRAV * zz;
-    P.rhogq[iq + (size_t)I_QI * KG] = P.rhogq[iq + (size_t)I_QI * KG] + 0.0;
+    if (OPT && ntr == 4) {
+      const double dqi = F(S_DQI)[c];
+      P.rhogq[iq + (size_t)I_QI * KG] = P.rhogq[iq + (size_t)I_QI * KG] + dqi;
+      rhog = rhog + dqi;
+      rhoge = rhoge - dqi * GRAV * zz;
+    } else {
+      P.rhogq[iq + (size_t)I_QI * KG] = P.rhogq[iq + (size_t)I_QI * KG] + 0.0;
+    }
     P.rhogq[iq + (size_t)I_QS * KG] = P.rhogq[iq + (size_t)I_QS * KG] + dqs;
     rhog = rhog + dqs;
     rhoge = rhoge - dqs * GRAV * zz;
@@ -684,9 +718,44 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   }
   __syncthreads();
 
+  // ---- KIN2KIN (mod_precip_transport.cpp:1012-1068), with the switch: the
+  //      momentum is rescaled so that the kinetic energy carried by the
+  //      transport is kept, horizontal on [kmin, kmax], vertical on
+  //      [kmin, kmax+1] (where the carried energy is zero at kmin and kmax+1)
+  if (kin2kin) {
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+      const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+      if (g >= G || k < kmin || k > kmax + 1) continue;
+      const size_t i = off + (size_t)k * G + g;
+      const double rhog = F(S_RHOF)[c];
+      if (k <= kmax) {
+        const double kin_h0 = F(S_KINH)[c] / rhog;
+        double vx_t = P.rhogvx[i] / rhog, vy_t = P.rhogvy[i] / rhog, vz_t = P.rhogvz[i] / rhog;
+        const double kin_h = 0.5 * (vx_t * vx_t + vy_t * vy_t + vz_t * vz_t);
+        if (kin_h > 1.0E-20) {
+          const double r = sqrt(fabs(kin_h0 / kin_h));
+          vx_t = vx_t * r;
+          vy_t = vy_t * r;
+          vz_t = vz_t * r;
+        }
+        P.rhogvx[i] = vx_t * rhog;
+        P.rhogvy[i] = vy_t * rhog;
+        P.rhogvz[i] = vz_t * rhog;
+      }
+      const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
+      const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
+      const double rhogh = c2w0 * rhog + c2w1 * F(S_RHOF)[c - COL_TG];
+      const double kin_v0 = F(S_KINV)[c] / rhogh;
+      double w_t = P.rhogw[i] / rhogh;
+      const double kin_v = 0.5 * (w_t * w_t);
+      if (kin_v > 1.0E-20) w_t = w_t * sqrt(fabs(kin_v0 / kin_v));
+      P.rhogw[i] = w_t * rhogh;
+    }
+  }
+
   // ---- KIN2EIN (mod_precip_transport.cpp:991-1011): tmp2 and the vertical
   //      kinetic energy of the updated state
-  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+  for (int c = threadIdx.x; c < ncell && !kin2kin; c += blockDim.x) {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     F(S_DRHOE)[c] = 0.0;
     F(S_DRHOPHI)[c] = 0.0;
@@ -715,14 +784,14 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   //      the cell's state exactly as pass A did and takes the Newton result.
   const int QE_TEM = S_KINH, QE_EIN = S_KINV, QE_QSUM = S_DKINH, QE_RHOL = S_DKINV, QE_QDL = S_DQR;
   const int QE_Q2 = S_DQS, QE_Q3 = S_DQG, QE_Q4 = S_F, QE_Q5 = S_RGS, QE_C = S_BASE;
-  const int QE_TOUT = S_VI, QE_QV = S_VJ, QE_QC = S_DRHOGU;
+  const int QE_TOUT = S_VI, QE_QV = S_VJ, QE_QC = S_DRHOGU, QE_QI = S_DRHOGV;
   __shared__ int nqueue;
   if (threadIdx.x == 0) nqueue = 0;
   __syncthreads();
 
   // mode 0: returns true when the cell was queued for the Newton iteration;
   // mode 1: finishes a queued cell with the result (tres, qvres, qcres)
-  auto final_cell = [&](int c, int mode, double tres, double qvres, double qcres) -> bool {
+  auto final_cell = [&](int c, int mode, double tres, double qvres, double qcres, double qires) -> bool {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     const size_t i = off + (size_t)k * G + g;
     const size_t iq = offq + (size_t)k * G + g;
@@ -733,7 +802,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     // divisions, at a third of the cost.
     const double rrhog = 1.0 / rhog;
     double rhoge = P.rhoge[i];
-    if (interior) {
+    if (interior && !kin2kin) {
       const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
       const double tmp_h = div_rn(0.5 * (rvx * rvx + rvy * rvy + rvz * rvz), rhog, rrhog);
       const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
@@ -768,9 +837,17 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     double tem = ein / cvt;
     double pre = rho * tem * (qdl * RDRY + q[I_QV] * RVAP);
 
-    // SATURATION_adjustment, ice_adjust = false (mod_satadjust.cpp:274-362)
-    const double ein_moist = ein + q[I_QV] * LHV0;
-    const double qsum = q[I_QV] + q[I_QC];
+    // SATURATION_adjustment (mod_satadjust.cpp:274-362): ice_adjust = false,
+    // or true with the switch (cloud ice joins the adjustment)
+    double ein_moist, qsum;
+    if (ice_adj) {
+      ein_moist = ein + q[I_QV] * LHV0 - q[I_QI] * LHF0;
+      qsum = q[I_QV] + q[I_QC] + q[I_QI];
+      q[I_QI] = 0.0;
+    } else {
+      ein_moist = ein + q[I_QV] * LHV0;
+      qsum = q[I_QV] + q[I_QC];
+    }
     q[I_QV] = qsum;
     q[I_QC] = 0.0;
     double cvtot = qd * CVDRY;
@@ -782,13 +859,21 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       tem = tres;
       q[I_QV] = qvres;
       q[I_QC] = qcres;
+      if (ice_adj) q[I_QI] = qires;
     } else if (interior) {
-      // satadjust_liq, mod_satadjust.cpp:771-896: is the cell saturated?
+      // satadjust_liq (mod_satadjust.cpp:771-896) or satadjust_all
+      // (:620-769): is the cell saturated?
       double qd_l = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
       const double rtem = 1.0 / (dmax(tem, TEM_MIN));
-      const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      if (ice_adj) {
+        const double alpha =
+            dmin(dmax((tem - C.sat_llimit) / (C.sat_ulimit - C.sat_llimit), 0.0), 1.0);
+        const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
+        psat = psat * alpha + psati * (1.0 - alpha);
+      }
       const double qsat = psat / (rho_l * RVAP * tem);
       if (qsum - qsat > EPS) {
         const int e = atomicAdd(&nqueue, 1);
@@ -807,6 +892,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     }
     rq[I_QV] = rhog * q[I_QV];
     rq[I_QC] = rhog * q[I_QC];
+    if (ice_adj) rq[I_QI] = rhog * q[I_QI];
     cvtot = qd * CVDRY;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
@@ -869,7 +955,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     if (g >= G) continue;
-    final_cell(c, 0, 0.0, 0.0, 0.0);
+    final_cell(c, 0, 0.0, 0.0, 0.0, 0.0);
     if (k == kmin) {
       const size_t ic = (size_t)l * G + g;
       const size_t r0 = (size_t)l * G + g, r1 = ((size_t)P.lall + l) * G + g;
@@ -902,27 +988,65 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     q[5] = F(QE_Q5)[e];
     bool converged = false;
     int ite;
-    for (ite = 0; ite < P.itelim; ++ite) {
-      const double rtem = 1.0 / (dmax(tem, TEM_MIN));
-      const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-      const double qsat = psat / (rho_l * RVAP * tem);
-      q[I_QV] = qsat;
-      q[I_QC] = qsum - qsat;
-      double cv = qd_l * CVDRY;
+    if (ice_adj) {
+      // satadjust_all, mod_satadjust.cpp:686-754 (CPovR = CVovR = 0, all CVW = CVdry)
+      const double UL = C.sat_ulimit, LL = C.sat_llimit;
+      for (ite = 0; ite < P.itelim; ++ite) {
+        const double alpha = dmin(dmax((tem - LL) / (UL - LL), 0.0), 1.0);
+        const double rtem = 1.0 / (dmax(tem, TEM_MIN));
+        const double psatl = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+        const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
+        const double psat = psatl * alpha + psati * (1.0 - alpha);
+        const double qsatl = psatl / (rho_l * RVAP * tem);
+        const double qsati = psati / (rho_l * RVAP * tem);
+        const double qsat = psat / (rho_l * RVAP * tem);
+        q[I_QV] = qsat;
+        q[I_QC] = (qsum - qsat) * alpha;
+        q[I_QI] = (qsum - qsat) * (1.0 - alpha);
+        double cv = qd_l * CVDRY;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
-      const double emoist_new = tem * cv + q[I_QV] * LHV0;
-      // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
-      // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
-      const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
-      const double demoist_dT = cv + dqsat_dT * LHV0;
-      const double dtemp = (emoist_new - ein_moist) / demoist_dT;
-      tem = tem - dtemp;
-      if (fabs(dtemp) < C.dtemp_criteria) {
-        converged = true;
-        break;
+        for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
+        const double emoist_new = tem * cv + q[I_QV] * LHV0 - q[I_QI] * LHF0;
+        const double dalpha_dT = (!(UL - tem < 0.0) && !(tem - LL < 0.0)) ? 1.0 / (UL - LL) : 0.0;
+        const double t2 = tem * tem;
+        const double dqsatl_dT = (C.LovR_liq / t2) * qsatl;
+        const double dqsati_dT = (C.LovR_ice / t2) * qsati;
+        const double dqsat_dT = qsatl * dalpha_dT + dqsatl_dT * alpha - qsati * dalpha_dT + dqsati_dT * (1.0 - alpha);
+        const double dqc_dT = (qsum - qsat) * dalpha_dT - dqsat_dT * alpha;
+        const double dqi_dT = -(qsum - qsat) * dalpha_dT - dqsat_dT * (1.0 - alpha);
+        const double dcv_dT = dqsat_dT * CVDRY + dqc_dT * CVDRY + dqi_dT * CVDRY;
+        const double demoist_dT = tem * dcv_dT + cv + dqsat_dT * LHV0 - dqi_dT * LHF0;
+        const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+        tem = tem - dtemp;
+        if (fabs(dtemp) < C.dtemp_criteria) {
+          converged = true;
+          break;
+        }
+        if (tem * 0.0 != 0.0) break;
       }
-      if (tem * 0.0 != 0.0) break;
+    } else {
+      for (ite = 0; ite < P.itelim; ++ite) {
+        const double rtem = 1.0 / (dmax(tem, TEM_MIN));
+        const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+        const double qsat = psat / (rho_l * RVAP * tem);
+        q[I_QV] = qsat;
+        q[I_QC] = qsum - qsat;
+        double cv = qd_l * CVDRY;
+#pragma unroll
+        for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
+        const double emoist_new = tem * cv + q[I_QV] * LHV0;
+        // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
+        // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
+        const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
+        const double demoist_dT = cv + dqsat_dT * LHV0;
+        const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+        tem = tem - dtemp;
+        if (fabs(dtemp) < C.dtemp_criteria) {
+          converged = true;
+          break;
+        }
+        if (tem * 0.0 != 0.0) break;
+      }
     }
     if (!converged) {
       const int c = (int)F(QE_C)[e];
@@ -931,12 +1055,13 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     F(QE_TOUT)[e] = tem;
     F(QE_QV)[e] = q[I_QV];
     F(QE_QC)[e] = q[I_QC];
+    if (ice_adj) F(QE_QI)[e] = q[I_QI];
   }
   __syncthreads();
 
   // pass C: finish the queued cells
   for (int e = threadIdx.x; e < nq; e += blockDim.x)
-    final_cell((int)F(QE_C)[e], 1, F(QE_TOUT)[e], F(QE_QV)[e], F(QE_QC)[e]);
+    final_cell((int)F(QE_C)[e], 1, F(QE_TOUT)[e], F(QE_QV)[e], F(QE_QC)[e], ice_adj ? F(QE_QI)[e] : 0.0);
 }
 
 // ------------------------------------------------------------------ math check
@@ -961,8 +1086,8 @@ cudaError_t launch_math(int fn, const double* x, const double* y, double* out, i
 }
 
 // ------------------------------------------------------------------ launchers
-size_t cell_smem_bytes(int K, bool mixed) {
-  const size_t vts = mixed ? cell_vts_doubles<float>(K) : cell_vts_doubles<double>(K);
+size_t cell_smem_bytes(int K, bool mixed, bool opt) {
+  const size_t vts = mixed ? cell_vts_doubles<float>(K) : cell_vts_doubles<double>(K, opt ? 4 : 3);
   // fall speeds, grid, tables, the FP32 reciprocal rows, the cell order and keys
   return sizeof(double) * (vts + (size_t)GF_COUNT * K + FM_TABLE_DOUBLES) + sizeof(float) * 4 * K +
          (sizeof(unsigned short) + 1) * (size_t)(K - 2) * CELL_TG + 16 +
@@ -971,10 +1096,12 @@ size_t cell_smem_bytes(int K, bool mixed) {
 
 int column_tile(int K) { return K <= 64 ? 16 : 8; }
 
-size_t column_smem_bytes(int K) {
+size_t column_smem_bytes(int K, bool opt) {
   const int TG = column_tile(K);
-  return sizeof(double) * ((size_t)S_COUNT * K * TG + GF_COUNT * K + 6 * TG + FM_TABLE_DOUBLES) +
-         sizeof(int) * 12 * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 4 * K;
+  const size_t nslot = opt ? S_COUNT_OPT : S_COUNT;
+  const size_t nrow = opt ? 8 : 6;
+  return sizeof(double) * (nslot * K * TG + GF_COUNT * K + 6 * TG + FM_TABLE_DOUBLES) +
+         sizeof(int) * 2 * nrow * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 4 * K;
 }
 
 int column_threads(int K) {
@@ -990,7 +1117,7 @@ cudaError_t launch_prepare();
 // The cell kernel alone (FP64): used on a copy of a state to obtain the
 // region extrema of the departure distances for the derivative kernels.
 cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t stream) {
-  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  const size_t nkey = (size_t)P.lall * 2 * P.ntr * P.kall;
   cudaError_t e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
@@ -998,7 +1125,10 @@ cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t str
   e = launch_prepare();
   if (e != cudaSuccess) return e;
   dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
-  nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, cell_smem_bytes(P.kall, false), stream>>>(P, C);
+  if (P.opt)
+    nsw6_cell_kernel<FastMath, double, true><<<g1, CELL_THREADS, cell_smem_bytes(P.kall, false, true), stream>>>(P, C);
+  else
+    nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, cell_smem_bytes(P.kall, false, false), stream>>>(P, C);
   return cudaGetLastError();
 }
 
@@ -1025,6 +1155,9 @@ cudaError_t launch_prepare() {
         raise_smem_limit(nsw6_cell_kernel<FastMath, double>, optin),
         raise_smem_limit(nsw6_cell_kernel<LibMath, double>, optin),
         raise_smem_limit(nsw6_cell_kernel<FloatMath, float>, optin),
+        raise_smem_limit(nsw6_cell_kernel<FastMath, double, true>, optin),
+        raise_smem_limit(nsw6_column_kernel<16, FastMath, false, true>, optin),
+        raise_smem_limit(nsw6_column_kernel<8, FastMath, false, true>, optin),
         raise_smem_limit(nsw6_column_kernel<16, FastMath, false>, optin),
         raise_smem_limit(nsw6_column_kernel<8, FastMath, false>, optin),
         raise_smem_limit(nsw6_column_kernel<16, LibMath, false>, optin),
@@ -1039,18 +1172,20 @@ cudaError_t launch_prepare() {
 }
 
 cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev) {
-  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  const size_t nkey = (size_t)P.lall * 2 * P.ntr * P.kall;
   cudaError_t e = launch_prepare();
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
-  const size_t s1 = cell_smem_bytes(P.kall, P.mixed != 0);
-  const size_t s2 = column_smem_bytes(P.kall);
+  const bool opt = P.opt != 0;
+  const size_t s1 = cell_smem_bytes(P.kall, P.mixed != 0, opt);
+  const size_t s2 = column_smem_bytes(P.kall, opt);
   dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
   if (ev) cudaEventRecord(ev[0], stream);
-  if (P.mixed) nsw6_cell_kernel<FloatMath, float><<<g1, CELL_THREADS, s1, stream>>>(P, consts_to_float(C));
+  if (opt) nsw6_cell_kernel<FastMath, double, true><<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  else if (P.mixed) nsw6_cell_kernel<FloatMath, float><<<g1, CELL_THREADS, s1, stream>>>(P, consts_to_float(C));
   else if (P.math_lib) nsw6_cell_kernel<LibMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   else nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   if (ev) cudaEventRecord(ev[1], stream);
@@ -1058,11 +1193,13 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   dim3 g2((P.gall + tg - 1) / tg, P.lall);
   const int nt = column_threads(P.kall);
   if (tg == 16) {
-    if (P.mixed) nsw6_column_kernel<16, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
+    if (opt) nsw6_column_kernel<16, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
+    else if (P.mixed) nsw6_column_kernel<16, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.math_lib) nsw6_column_kernel<16, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
     else nsw6_column_kernel<16, FastMath, false><<<g2, nt, s2, stream>>>(P, C);
   } else {
-    if (P.mixed) nsw6_column_kernel<8, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
+    if (opt) nsw6_column_kernel<8, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
+    else if (P.mixed) nsw6_column_kernel<8, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.math_lib) nsw6_column_kernel<8, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
     else nsw6_column_kernel<8, FastMath, false><<<g2, nt, s2, stream>>>(P, C);
   }

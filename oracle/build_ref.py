@@ -15,6 +15,14 @@ against Kokkos >= 4.6.1, which is not installed.  This recipe
 Variants:
   strict  serial shim, -O2 -ffp-contract=off: the deterministic oracle.
   omp     OpenMP shim, -O3 -fopenmp: the reference's Kokkos-OpenMP CPU build.
+  fma     contraction on: the reference's own build-to-build spread.
+  opt     as strict, with the two scheme choices that mp_nsw6_init assigns from
+          literals (Roh_flag = true, qr_aut_acc_type = "KK2000",
+          src/mod_mp_nsw6.cpp:291-292) turned into variables the driver sets,
+          so that the switches mp_nsw6_init and precip_transport_new read
+          (Roh_flag, OPT_EXPLICIT_ICEGEN, qr_aut_acc_type, OPT_INDIR,
+          precip_transport_type, PRCIP_TRN_ECORRECT) can all be flipped; with
+          the defaults it computes exactly what strict computes.
 
 When the reference tree is absent (on a machine that only received the
 repository), the copy already in ``oracle/_ref/src`` is used if present.
@@ -58,7 +66,23 @@ VARIANT_FLAGS = {
     # fused multiply-add contraction, as the reference's GPU (nvcc) and -Ofast
     # builds compile it: measures the reference's own build-to-build spread
     "fma": ["-O2", "-ffp-contract=fast"] + (["-mfma"] if platform.machine() in ("x86_64", "AMD64") else []),
+    "opt": ["-O2", "-ffp-contract=off", "-DNSW6REF_OPTIONS"],
 }
+
+# The literal assignments of mp_nsw6_init that the "opt" variant replaces.
+OPT_PATCHES = [
+    ("    Roh_flag = true;\n", "    Roh_flag = nsw6ref_opt_roh;\n"),
+    ('    qr_aut_acc_type = "KK2000";\n', '    qr_aut_acc_type = nsw6ref_opt_kk2000 ? "KK2000" : "Default";\n'),
+]
+OPT_DECL = "extern bool nsw6ref_opt_roh;\nextern bool nsw6ref_opt_kk2000;\n"
+
+
+def patched_nsw6(text: str) -> str:
+    for a, b in OPT_PATCHES:
+        if text.count(a) != 1:
+            raise RuntimeError(f"mod_mp_nsw6.cpp: expected one occurrence of {a.strip()!r}")
+        text = text.replace(a, b)
+    return OPT_DECL + text
 
 
 def sources_available() -> bool:
@@ -117,13 +141,20 @@ def build(gall: int, kall: int, variant: str = "strict", jobs: int | None = None
         if not tgt.exists() or tgt.read_text() != text:
             tgt.write_text(text)
 
+    units = [src / "src" / u for u in REF_UNITS] + [HERE / "ref_driver.cpp"]
+    if variant == "opt":
+        psrc = bdir / "mod_mp_nsw6.cpp"
+        text = patched_nsw6((src / "src" / "mod_mp_nsw6.cpp").read_text())
+        if not psrc.exists() or psrc.read_text() != text:
+            psrc.write_text(text)
+        units = [psrc if u.name == "mod_mp_nsw6.cpp" else u for u in units]
+
     so = bdir / "libnsw6ref.so"
-    deps = [src / "src" / u for u in REF_UNITS] + [HERE / "ref_driver.cpp", SHIM / "Kokkos_Core.hpp", Path(__file__)]
+    deps = units + [SHIM / "Kokkos_Core.hpp", Path(__file__)]
     if so.exists() and not force and all(so.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return so
 
-    flags = ["g++", "-std=c++17", "-fPIC", "-w", f"-I{inc}", f"-I{SHIM}"] + VARIANT_FLAGS[variant]
-    units = [src / "src" / u for u in REF_UNITS] + [HERE / "ref_driver.cpp"]
+    flags = ["g++", "-std=c++17", "-fPIC", "-w", f"-I{inc}", f"-I{src / 'src'}", f"-I{SHIM}"] + VARIANT_FLAGS[variant]
 
     def compile_one(u: Path) -> Path:
         obj = bdir / (u.stem + ".o")

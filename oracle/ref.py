@@ -29,14 +29,25 @@ def available() -> bool:
     return build_ref.sources_available()
 
 
+# Scheme switches in the order of nsw6ref_set_options (oracle/ref_driver.cpp)
+# and of nsw6_options (include/nsw6.h), with the reference's defaults.
+OPTION_NAMES = ["roh2014", "explicit_icegen", "kk2000", "qi_sediment", "kin2kin", "aerosol_indirect"]
+DEFAULT_OPTIONS = {"roh2014": 1, "explicit_icegen": 1, "kk2000": 1, "qi_sediment": 0, "kin2kin": 0,
+                   "aerosol_indirect": 0}
+
+
 def load(gall: int, kall: int, gz: np.ndarray, gzh: np.ndarray, variant: str = "strict",
-         build: bool = True) -> ctypes.CDLL:
+         build: bool = True, options: dict | None = None) -> ctypes.CDLL:
     """Load (building if needed) the reference compiled for (gall, kall) and run its set-up.
 
     The reference keeps its grid and parameters in process globals, so one
     library instance serves one (gall, kall) grid; loading twice with a
-    different grid re-runs the set-up.
+    different grid re-runs the set-up.  ``options`` (the "opt" variant only)
+    sets the scheme switches before the set-up; missing keys take the
+    reference's defaults.
     """
+    if options is not None and variant != "opt":
+        raise ValueError("scheme options need the 'opt' build of the reference")
     key = (gall, kall, variant)
     lib = _LIBS.get(key)
     if lib is None:
@@ -47,7 +58,13 @@ def load(gall: int, kall: int, gz: np.ndarray, gzh: np.ndarray, variant: str = "
                                           ctypes.c_double, ctypes.c_double]
         lib.nsw6ref_set_params.argtypes = [ctypes.POINTER(ctypes.c_double)]
         lib.nsw6ref_get_params.argtypes = [ctypes.POINTER(ctypes.c_double)]
+        lib.nsw6ref_set_options.argtypes = [ctypes.POINTER(ctypes.c_int)]
         _LIBS[key] = lib
+    if variant == "opt":
+        o = dict(DEFAULT_OPTIONS, **(options or {}))
+        arr = (ctypes.c_int * len(OPTION_NAMES))(*[int(o[n]) for n in OPTION_NAMES])
+        if lib.nsw6ref_set_options(arr) != 0:
+            raise RuntimeError("reference build without scheme switches")
     gz = np.ascontiguousarray(gz, dtype=np.float64)
     gzh = np.ascontiguousarray(gzh, dtype=np.float64)
     dp = ctypes.POINTER(ctypes.c_double)

@@ -26,6 +26,18 @@
 
 using namespace PROBLEM_SIZE;
 
+#ifdef NSW6REF_OPTIONS
+// Scheme switches of the "opt" build (oracle/build_ref.py): the two choices
+// mp_nsw6_init assigns from literals read these variables instead, and the
+// others are the reference's own globals (src/mod_mp_nsw6.cpp:127-132,
+// src/problemsize.cpp:39).
+bool nsw6ref_opt_roh = true;
+bool nsw6ref_opt_kk2000 = true;
+extern std::string precip_transport_type;
+extern bool OPT_EXPLICIT_ICEGEN;
+extern bool OPT_INDIR;
+#endif
+
 namespace {
 
 struct CoutSilencer {
@@ -95,6 +107,11 @@ int nsw6ref_setup(const double* gz, const double* gzh) {
   DEBUG::GRD_Setup();
   DEBUG::CVW_CPW_Setup();
   SATADJUST::SATURATION_Setup();
+  // mp_nsw6_init assigns some members of the global para only in its
+  // Roh_flag branch (mod_mp_nsw6.cpp:345-357); start from the GlobalParams
+  // defaults, as a fresh process does, so that a set-up does not inherit the
+  // values of an earlier one.
+  para = GlobalParams();
   MP_DRIVER::mp_init(MP_TYPE);
 
   int rc = chdir(cwd);
@@ -121,6 +138,30 @@ int nsw6ref_set_params(const double* p) {
   para.Cs = p[3];
   para.Cg = p[4];
   return 0;
+}
+
+// Scheme switches (the "opt" build only; they take effect at the next
+// nsw6ref_setup, whose mp_init runs mp_nsw6_init):
+//   o[0] Roh_flag (Roh and Satoh 2014 snow settings, mod_mp_nsw6.cpp:345-357)
+//   o[1] OPT_EXPLICIT_ICEGEN (mp_nsw6_init forces it on when Roh_flag is set)
+//   o[2] KK2000 warm rain (1) or Berry (0), mod_mp_nsw6.cpp:374-387
+//   o[3] precip_transport_type "4WATER" (1) or "3WATER" (0)
+//   o[4] PRCIP_TRN_ECORRECT "KIN2KIN" (1) or "KIN2EIN" (0)
+//   o[5] OPT_INDIR (cloud number from unccn)
+// Returns 1 in builds without the switches.
+int nsw6ref_set_options(const int* o) {
+#ifdef NSW6REF_OPTIONS
+  nsw6ref_opt_roh = o[0] != 0;
+  OPT_EXPLICIT_ICEGEN = o[1] != 0;
+  nsw6ref_opt_kk2000 = o[2] != 0;
+  precip_transport_type = o[3] ? "4WATER" : "3WATER";
+  PRCIP_TRN_ECORRECT = o[4] ? "KIN2KIN" : "KIN2EIN";
+  OPT_INDIR = o[5] != 0;
+  return 0;
+#else
+  (void)o;
+  return 1;
+#endif
 }
 
 int nsw6ref_get_params(double* p) {

@@ -21,6 +21,11 @@ def golden_files():
     return sorted(GOLDEN.glob("golden_*.npz"))
 
 
+def options_files():
+    """Fixtures of the reference with non-default scheme switches."""
+    return sorted(GOLDEN.glob("options_*.npz"))
+
+
 @pytest.fixture(scope="session")
 def cuda_available():
     import torch

@@ -7,6 +7,8 @@
 """
 from __future__ import annotations
 
+from pathlib import Path
+
 import numpy as np
 import pytest
 
@@ -124,3 +126,35 @@ def test_reference_own_build_spread(variant, seed):
     print(f"\nreference fma vs strict, {variant}: {thr} threshold cells\n" + summary(stats))
     assert all(s["n_bad"] == 0 for s in stats.values())
     assert passes(stats)
+
+
+@needs_ref
+@pytest.mark.parametrize("variant,seed", [("standard", 201), ("cold", 202)])
+def test_reference_switch_build_equals_strict_at_defaults(variant, seed):
+    """The "opt" build (switch assignments of mp_nsw6_init turned into
+    variables) computes exactly what the unmodified build computes when the
+    switches hold the reference's values."""
+    spec = StateSpec(gall=40, kall=42, lall=1, seed=seed, variant=variant)
+    st = make_state(spec, out_fill=np.nan)
+    r1 = region_view(st, 0)
+    r2 = {k: v.copy() for k, v in r1.items()}
+    assert ref.mp_driver(ref.load(40, 42, st["_gz"], st["_gzh"]), r1, spec.dt) == 0
+    assert ref.mp_driver(ref.load(40, 42, st["_gz"], st["_gzh"], variant="opt", options={}), r2, spec.dt) == 0
+    for n in OUTPUT_NAMES:
+        assert np.array_equal(r1[n].view(np.int64), r2[n].view(np.int64)), n
+
+
+@needs_ref
+@pytest.mark.parametrize("path", sorted((Path(__file__).parent / "golden").glob("options_*.npz")),
+                         ids=lambda p: p.stem)
+def test_reference_reproduces_options_fixture(path):
+    """Each switch fixture is what the reference's "opt" build gives for its
+    switches, bit for bit."""
+    z = np.load(path)
+    reg, out, gz, gzh, dt = load_golden(path)
+    kall, gall = reg["rhog"].shape
+    opts = {n: int(v) for n, v in zip(ref.OPTION_NAMES, z["options"])}
+    lib = ref.load(gall, kall, gz, gzh, variant="opt", options=opts)
+    assert ref.mp_driver(lib, reg, dt) == 0
+    for n in OUTPUT_NAMES:
+        assert np.array_equal(np.asarray(reg[n]).view(np.int64), np.asarray(out[n]).view(np.int64)), n
