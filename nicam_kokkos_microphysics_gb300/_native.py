@@ -19,7 +19,7 @@ INCLUDE = PKG.parent / "include"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libnsw6_gb300.so"
 
-SOURCES = ["nsw6_kernels.cu", "nsw6_deriv.cu", "nsw6_driver.cu"]
+SOURCES = ["nsw6_kernels.cu", "nsw6_deriv.cu", "nsw6_adjoint.cu", "nsw6_driver.cu"]
 HEADERS = ["nsw6_common.cuh", "nsw6_cell.cuh", "nsw6_fastmath.cuh", "nsw6_ad.cuh", "nsw6_column_step.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false keeps every product and sum separately rounded, as the

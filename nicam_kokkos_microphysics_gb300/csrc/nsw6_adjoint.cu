@@ -1,0 +1,882 @@
+// Level-parallel adjoint of the column phase of the NSW6 step.
+//
+// The column phase (everything after the per-cell physics: departure
+// distances, the transport of QR, QS, QG, KIN2EIN, thermodynamics, the
+// saturation adjustment and the closing negative filter) is split at the
+// points where a value computed at one level is read at another, into four
+// per-cell stages:
+//
+//   S1  departure distances (vadv1d_prep, mod_vadv1d.cpp:231-391) from the
+//       fall speeds, the kinetic energies and the 24 flux sources
+//       (mod_precip_transport.cpp:767-900) of one cell;
+//   S2  one flux integral of vadv1d_getflux_new (mod_vadv1d.cpp:393-450) of
+//       one cell (a work item per cell and flux);
+//   S3  the flux divergences, surface fluxes and the application of the
+//       tendencies (mod_precip_transport.cpp:782-989) of one cell;
+//   S4  KIN2EIN (:991-1011), the final thermodynamic state, the saturation
+//       adjustment (mod_satadjust.cpp:274-362, 771-896) and the negative filter
+//       of one cell.
+//
+// Each stage is a function of one cell written over the scalar type T, its
+// inputs read through an accessor.  The forward kernels (T = double) store the
+// stage outputs; the adjoint kernels (T = RVar) re-record one cell's stage on a
+// short per-thread tape, seed its outputs with their adjoints, sweep the tape
+// and add the adjoints of its inputs, wherever they live (another level, the
+// cell phase's outputs, the caller's arrays), with atomic additions.  Every
+// cell of every column runs in parallel, where the serial column adjoint gave
+// one thread a whole column.
+//
+// The arithmetic is that of the serial column step (nsw6_column_step.cuh),
+// which reproduces the production kernels bit for bit; discrete choices
+// (departure cells, flux bounds, the small-flux filter, limiter branches) are
+// held at the forward's values and the Newton temperature is differentiated
+// implicitly, as there.
+#include <cfloat>
+#include <cuda_runtime.h>
+
+#include "nsw6_column_step.cuh"
+
+namespace nsw6 {
+
+// Cell-phase output fields (Y / YB layout of nsw6_deriv.cu).
+enum AdjFieldS {
+  YS_RHOG, YS_RHOGE, YS_TEM, YS_RHOGQ, YS_Q = YS_RHOGQ + 6, YS_VT = YS_Q + 5, YS_RE = YS_VT + 3, YS_RECLD,
+  YS_RCTOP, YS_TCTOP
+};
+
+// Work fields of the staged column adjoint: [NWF][lall][kall][gall].
+enum WorkField {
+  W_ZDIS = 0,                  // 6 departure distances (QR, QS, QG full; QR, QS, QG half)
+  W_KINH = 6, W_KINV,          // kinetic energies of the transport's input state
+  W_RHOF = 8,                  // 24 flux sources, tracer t, flux j: W_RHOF + 8 t + j (j < 6 full, 6..7 half)
+  W_F = W_RHOF + 24,           // 24 fluxes, same order
+  W_RHOG_N = W_F + 24, W_RHOGE_N, W_RVX_N, W_RVY_N, W_RVZ_N, W_RW_N,
+  W_RQ_N,                      // 6 tracers
+  W_KINH_N = W_RQ_N + 6, W_KINV_N,
+  NWF
+};
+
+// Seeds (output adjoints) of the column phase, copied from the caller's
+// adjoint arrays before any input adjoint is added there: [NSF][lall][kall][gall]
+// then the six column outputs [6][lall][gall].
+enum SeedField {
+  SF_RHOG, SF_RHOGE, SF_RVX, SF_RVY, SF_RVZ, SF_RW, SF_RHO, SF_TEM, SF_PRE, SF_QD, SF_GPREC,
+  SF_RQ, SF_Q = SF_RQ + 6, NSF = SF_Q + 6
+};
+enum SeedColumn { SC_PRECIP0, SC_PRECIP1, SC_LH, SC_RHOE, SC_RHOPHI, SC_RHOKIN, NSC };
+
+constexpr int STAGE_THREADS = AD_THREADS;
+constexpr int MAX_LEAVES = 96;
+constexpr int ERR_ADJ_CAPACITY = 5;   // a tape or the leaf log of a stage overflowed (NSW6_ERR_UNSUPPORTED)
+
+namespace {
+
+struct LayS {
+  int K, G, lall;
+  __device__ __forceinline__ size_t f(int l, int k, int g) const { return ((size_t)l * K + k) * G + g; }
+  __device__ __forceinline__ size_t t(int l, int n, int k, int g) const {
+    return (((size_t)l * NQ + n) * K + k) * G + g;
+  }
+  __device__ __forceinline__ size_t c(int l, int g) const { return (size_t)l * G + g; }
+  __device__ __forceinline__ size_t p(int r, int l, int g) const { return ((size_t)r * lall + l) * G + g; }
+};
+
+__device__ __forceinline__ void record_err(DevStatus* st, int code, int k, int g, int l, int iters) {
+  if (atomicCAS(&st->code, 0, code) == 0) {
+    st->k = k;
+    st->g = g;
+    st->l = l;
+    st->iters = iters;
+  }
+}
+
+// Everything a stage reads, and where the adjoints of what it reads go.
+struct StageIO {
+  Problem P;
+  LayS L;
+  size_t NC;
+  ArgPtrs x, xb;
+  const double* Y;
+  double* YB;
+  double* W;
+  double* WB;
+  const double* SB;     // seeds [NSF][NC] then [NSC][lall][gall]
+  const int* bnd;       // flux bounds [lall][2][6][kall]: bmn then bmx
+};
+
+// Where a leaf's adjoint is added.
+enum LeafKind { LK_W = 0, LK_Y = 1, LK_X = 2 };
+
+struct LeafLog {
+  int n, overflow;
+  int code[MAX_LEAVES];
+  int id[MAX_LEAVES];
+  size_t idx[MAX_LEAVES];
+};
+
+// Input accessor.  T = double: the stored values.  T = RVar: a new leaf per
+// read, logged with the place its adjoint belongs to.
+template <class T>
+struct In;
+
+template <>
+struct In<double> {
+  const StageIO& io;
+  int l, g;
+  __device__ double w(int f, int kk) const { return io.W[f * io.NC + io.L.f(l, kk, g)]; }
+  __device__ double y(int f, int kk) const { return io.Y[f * io.NC + io.L.f(l, kk, g)]; }
+  __device__ double x(int a, size_t i) const { return io.x.a[a][i]; }
+};
+
+template <>
+struct In<RVar> {
+  const StageIO& io;
+  int l, g;
+  LeafLog* log;
+  __device__ RVar put(int kind, int f, size_t i, double v) const {
+    const RVar r = leaf(v);
+    if (r.id < 0) return r;   // tape full: the stage reports the overflow
+    if (log->n >= MAX_LEAVES) {
+      log->overflow = 1;
+      return r;
+    }
+    log->code[log->n] = kind * 4096 + f;
+    log->id[log->n] = r.id;
+    log->idx[log->n] = i;
+    ++log->n;
+    return r;
+  }
+  __device__ RVar w(int f, int kk) const {
+    const size_t i = io.L.f(l, kk, g);
+    return put(LK_W, f, i, io.W[f * io.NC + i]);
+  }
+  __device__ RVar y(int f, int kk) const {
+    const size_t i = io.L.f(l, kk, g);
+    return put(LK_Y, f, i, io.Y[f * io.NC + i]);
+  }
+  __device__ RVar x(int a, size_t i) const { return put(LK_X, a, i, io.x.a[a][i]); }
+};
+
+// State fields the column phase reads: the cell phase's output at interior
+// levels, the caller's array at the halo levels.
+template <class T>
+__device__ __forceinline__ T st_rhog(const In<T>& in, int kk) {
+  return (kk >= in.io.P.kmin && kk <= in.io.P.kmax) ? in.y(YS_RHOG, kk) : in.x(A_rhog, in.io.L.f(in.l, kk, in.g));
+}
+template <class T>
+__device__ __forceinline__ T st_rhoge(const In<T>& in, int kk) {
+  return (kk >= in.io.P.kmin && kk <= in.io.P.kmax) ? in.y(YS_RHOGE, kk) : in.x(A_rhoge, in.io.L.f(in.l, kk, in.g));
+}
+template <class T>
+__device__ __forceinline__ T st_tem(const In<T>& in, int kk) {
+  return (kk >= in.io.P.kmin && kk <= in.io.P.kmax) ? in.y(YS_TEM, kk) : in.x(A_tem, in.io.L.f(in.l, kk, in.g));
+}
+template <class T>
+__device__ __forceinline__ T st_rhogq(const In<T>& in, int n, int kk) {
+  return (kk >= in.io.P.kmin && kk <= in.io.P.kmax) ? in.y(YS_RHOGQ + n, kk)
+                                                      : in.x(A_rhogq, in.io.L.t(in.l, n, kk, in.g));
+}
+template <class T>
+__device__ __forceinline__ T st_q(const In<T>& in, int n, int kk) {   // n >= 1
+  return (kk >= in.io.P.kmin && kk <= in.io.P.kmax) ? in.y(YS_Q + n - 1, kk)
+                                                      : in.x(A_q, in.io.L.t(in.l, n, kk, in.g));
+}
+template <class T>
+__device__ __forceinline__ T xf(const In<T>& in, int a, int kk) {
+  return in.x(a, in.io.L.f(in.l, kk, in.g));
+}
+template <class T>
+__device__ __forceinline__ T xc(const In<T>& in, int a) {
+  return in.x(a, in.io.L.c(in.l, in.g));
+}
+
+// ------------------------------------------------------------------ stages
+// S1: departure distances, kinetic energies and flux sources of cell (l, k, g).
+template <class T, class O>
+__device__ void stage1(const In<T>& in, const double* gr, int k, const O& out) {
+  const Problem& P = in.io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const double* rdgz = gr + GF_RDGZ * K;
+  const double* rdgzh = gr + GF_RDGZH * K;
+  const double* rdzs = gr + GF_RDZS * K;
+  const double* rdzsh = gr + GF_RDZSH * K;
+  const double* afact = gr + GF_AFACT * K;
+  const double* bfact = gr + GF_BFACT * K;
+  const bool interior = (k >= kmin && k <= kmax);
+  // fall speeds at levels k-3 .. k+1 (zero outside the interior)
+  T vt[3][5];
+  for (int t = 0; t < 3; ++t)
+    for (int j = 0; j < 5; ++j) {
+      const int kk = k - 3 + j;
+      vt[t][j] = (interior && kk >= kmin && kk <= kmax) ? in.y(YS_VT + t, kk) : T(0.0);
+    }
+  for (int r = 0; r < 6; ++r) {
+    const int t = r % 3, half = r / 3;
+    const int mkmin = half ? kmin + 1 : kmin;
+    T z = T(0.0);
+    if (k >= mkmin && k <= kmax) {
+      auto col = [&](int j) { return vt[t][j - k + 3]; };
+      if (!half) {
+        auto wp = [&](int j) { return col(j); };
+        z = vadv_zdis<T>(wp, rdgz, rdzs, k, mkmin, kmax, T(P.dt), T(P.hdt2), T(P.sdt3));
+      } else {
+        auto wp = [&](int j) { return (j >= kmin + 1 && j <= kmax - 1) ? T(0.5) * (col(j) + col(j - 1)) : T(0.0); };
+        z = vadv_zdis<T>(wp, rdgzh, rdzsh, k, mkmin, kmax, T(P.dt), T(P.hdt2), T(P.sdt3));
+      }
+    }
+    out(W_ZDIS + r, z);
+  }
+  // metric factors and kinetic energy (mod_precip_transport.cpp:715-770)
+  T rgs = T(0.0), kinh = T(0.0), kinv = T(0.0);
+  if (interior) rgs = xf(in, A_gam2, k) / xf(in, A_gsgam2, k);
+  const T vx = xf(in, A_vx, k), vy = xf(in, A_vy, k), vz = xf(in, A_vz, k);
+  const T vi = vx * xc(in, A_ix) + vy * xc(in, A_iy) + vz * xc(in, A_iz);
+  const T vj = vx * xc(in, A_jx) + vy * xc(in, A_jy) + vz * xc(in, A_jz);
+  if (interior) {
+    const T rvx = xf(in, A_rhogvx, k), rvy = xf(in, A_rhogvy, k), rvz = xf(in, A_rhogvz, k);
+    kinh = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / st_rhog(in, k);
+  }
+  const bool hk = (k >= kmin + 1 && k <= kmax);
+  T rw = T(0.0);
+  if (hk) {
+    const T gh = xf(in, A_gsgam2h, k);
+    const T c2w0 = afact[k] / xf(in, A_gsgam2, k) * gh;
+    const T c2w1 = bfact[k] / xf(in, A_gsgam2, k - 1) * gh;
+    rw = xf(in, A_rhogw, k);
+    kinv = 0.5 * (rw * rw) / (c2w0 * st_rhog(in, k) + c2w1 * st_rhog(in, k - 1));
+  }
+  out(W_KINH, kinh);
+  out(W_KINV, kinv);
+  // flux sources of QR, QS, QG (mod_precip_transport.cpp:776-808, 864-882)
+  const int tracer[3] = {I_QR, I_QS, I_QG};
+  const T tem = interior ? st_tem(in, k) : T(0.0);
+  const T zz = interior ? xf(in, A_z, k) : T(0.0);
+  T rgsh = T(0.0);
+  if (hk) rgsh = xf(in, A_gam2h, k) / xf(in, A_gsgam2h, k);
+  for (int t = 0; t < 3; ++t) {
+    const int nq = tracer[t];
+    T base = T(0.0), qn = T(0.0);
+    if (interior) {
+      base = st_rhogq(in, nq, k) * rgs;
+      qn = st_q(in, nq, k);
+    }
+    out(W_RHOF + 8 * t + 0, base);
+    out(W_RHOF + 8 * t + 1, base * CVDRY * tem);
+    out(W_RHOF + 8 * t + 2, base * GRAV * zz);
+    out(W_RHOF + 8 * t + 3, qn * rgs * kinh);
+    out(W_RHOF + 8 * t + 4, base * vi);
+    out(W_RHOF + 8 * t + 5, base * vj);
+    T qh = T(0.0), h1 = T(0.0);
+    if (hk) {
+      qh = 0.5 * (qn + st_q(in, nq, k - 1)) * rgsh;
+      h1 = qh * rw;
+    }
+    out(W_RHOF + 8 * t + 6, qh * kinv);
+    out(W_RHOF + 8 * t + 7, h1);
+  }
+}
+
+// S2: flux j (tracer j / 8, source j % 8) of cell (l, k, g).
+template <class T>
+__device__ T stage2(const In<T>& in, const double* gr, int k, int j) {
+  const Problem& P = in.io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const int t = j / 8, f = j % 8;
+  const bool full = f < 6;
+  const int mkmin = full ? kmin : kmin + 1;
+  if (k < mkmin || k > kmax) return T(0.0);
+  const int r = full ? t : 3 + t;
+  const int* bmn = in.io.bnd + ((size_t)in.l * 2 + 0) * 6 * K;
+  const int* bmx = in.io.bnd + ((size_t)in.l * 2 + 1) * 6 * K;
+  // the integral's range: the half levels use the full-level kcell_max
+  // (mod_precip_transport.cpp:890, 892)
+  const int lo = bmn[r * K + k];
+  const int hi = bmx[t * K + k];
+  const double* zh = gr + (full ? GF_GZH : GF_GZSHIFT) * K;
+  const double* dz = gr + (full ? GF_DGZ : GF_DGZH) * K;
+  const double zv = in.io.W[(W_ZDIS + r) * in.io.NC + in.io.L.f(in.l, k, in.g)];
+  const int kc = departure_cell_t(zh, k, zv, lo, bmx[r * K + k], mkmin, kmax);
+  const int src = W_RHOF + 8 * t + f;
+  T acc = T(0.0);
+  T zdis = in.w(W_ZDIS + r, k);
+  if (!(lo == k && hi == k)) {
+    for (int k2 = lo; k2 <= hi; ++k2)
+      acc = fmaR(in.w(src, k2), T(k2 > kc ? dz[k2] : (k2 < kc ? -dz[k2] : 0.0)), acc);
+    if (hi != kc) zdis = zdis - T(hi > kc ? dz[hi] : -dz[hi]);
+  }
+  acc = fmaR(in.w(src, kc), zdis, acc);
+  return fabsR(acc) >= T(EPS) ? acc : T(0.0);
+}
+
+// S3: divergences, surface fluxes and the updated state of cell (l, k, g).
+// o(field, value) for the work fields; fin(seed field, value) for the caller's
+// outputs written here (rhogvx/y/z, rhogw, GPREC); col(seed column, value) for
+// the surface outputs (k = kmin).
+template <class T, class O, class F, class Cc>
+__device__ void stage3(const In<T>& in, const double* gr, int k, const O& o, const F& fin, const Cc& col) {
+  const Problem& P = in.io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const double* rdgz = gr + GF_RDGZ * K;
+  const double* rdgzh = gr + GF_RDGZH * K;
+  const double dt = P.dt;
+  const bool interior = (k >= kmin && k <= kmax);
+  const bool hk = (k >= kmin + 1 && k <= kmax);
+  T dq[3] = {T(0.0), T(0.0), T(0.0)};
+  T drhoe = T(0.0), drhophi = T(0.0), dkinh = T(0.0), dkinv = T(0.0), du = T(0.0), dv = T(0.0), dw = T(0.0);
+  T acc[6] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
+  const int tracer[3] = {I_QR, I_QS, I_QG};
+  for (int t = 0; t < 3; ++t) {
+    const int nq = tracer[t];
+    if (interior) {
+      for (int f = 0; f < 6; ++f) {
+        const T fk = in.w(W_F + 8 * t + f, k), fk1 = in.w(W_F + 8 * t + f, k + 1);
+        const T d = (fk1 - fk) * rdgz[k];
+        switch (f) {
+          case 0:
+            dq[t] = -d;
+            if (nq == I_QR) fin(SF_GPREC, 0.0 + (-fk / dt));
+            break;
+          case 1: drhoe = drhoe - d; break;
+          case 2: drhophi = drhophi - d; break;
+          case 3: dkinh = dkinh - d; break;
+          case 4: du = du - d; break;
+          default: dv = dv - d; break;
+        }
+        if (k == kmin) {
+          switch (f) {
+            case 0:
+              if (nq == I_QR) {
+                acc[0] = acc[0] - fk / dt;
+              } else {
+                acc[1] = acc[1] - fk / dt;
+                acc[2] = acc[2] + fk * LHF0 / dt;
+              }
+              break;
+            case 1: acc[3] = acc[3] - fk / dt; break;
+            case 2: acc[4] = acc[4] - fk / dt; break;
+            case 3: acc[5] = acc[5] - fk / dt; break;
+            default: break;
+          }
+        }
+      }
+    }
+    if (hk) {
+      for (int w = 0; w < 2; ++w) {
+        const T d = (in.w(W_F + 8 * t + 6 + w, k) - in.w(W_F + 8 * t + 6 + w, k - 1)) * rdgzh[k];
+        if (w == 0) dkinv = dkinv - d;
+        else dw = dw - d;
+      }
+    }
+  }
+  if (k == kmin) {
+    col(SC_PRECIP0, 0.0 + acc[0]);
+    col(SC_PRECIP1, 0.0 + acc[1]);
+    col(SC_LH, 0.0 + acc[2]);
+    col(SC_RHOE, 0.0 + acc[3]);
+    col(SC_RHOPHI, 0.0 + acc[4]);
+    col(SC_RHOKIN, 0.0 + acc[5]);
+  }
+  // apply the tendencies (mod_precip_transport.cpp:956-989)
+  T rhoge = st_rhoge(in, k) + drhoe + drhophi;
+  o(W_KINH_N, in.w(W_KINH, k) + dkinh);
+  o(W_KINV_N, in.w(W_KINV, k) + dkinv);
+  const T ix = xc(in, A_ix), iy = xc(in, A_iy), iz = xc(in, A_iz);
+  const T jx = xc(in, A_jx), jy = xc(in, A_jy), jz = xc(in, A_jz);
+  const T rvx = xf(in, A_rhogvx, k) + du * ix + dv * jx;
+  const T rvy = xf(in, A_rhogvy, k) + du * iy + dv * jy;
+  const T rvz = xf(in, A_rhogvz, k) + du * iz + dv * jz;
+  const T rw = xf(in, A_rhogw, k) + dw;
+  o(W_RVX_N, rvx);
+  o(W_RVY_N, rvy);
+  o(W_RVZ_N, rvz);
+  o(W_RW_N, rw);
+  fin(SF_RVX, rvx);
+  fin(SF_RVY, rvy);
+  fin(SF_RVZ, rvz);
+  fin(SF_RW, rw);
+  T rhog = st_rhog(in, k);
+  const T zz = xf(in, A_z, k);
+  o(W_RQ_N + I_QV, st_rhogq(in, I_QV, k) + 0.0);
+  o(W_RQ_N + I_QC, st_rhogq(in, I_QC, k) + 0.0);
+  o(W_RQ_N + I_QR, st_rhogq(in, I_QR, k) + dq[0]);
+  rhog = rhog + dq[0];
+  rhoge = rhoge - dq[0] * GRAV * zz;
+  o(W_RQ_N + I_QI, st_rhogq(in, I_QI, k) + 0.0);
+  o(W_RQ_N + I_QS, st_rhogq(in, I_QS, k) + dq[1]);
+  rhog = rhog + dq[1];
+  rhoge = rhoge - dq[1] * GRAV * zz;
+  o(W_RQ_N + I_QG, st_rhogq(in, I_QG, k) + dq[2]);
+  rhog = rhog + dq[2];
+  rhoge = rhoge - dq[2] * GRAV * zz;
+  o(W_RHOG_N, rhog);
+  o(W_RHOGE_N, rhoge);
+}
+
+// Vertical kinetic energy of the updated state at half level j.
+template <class T>
+__device__ __forceinline__ T kinv_new(const In<T>& in, const double* gr, int j) {
+  const Problem& P = in.io.P;
+  const int K = P.kall;
+  if (!(j >= P.kmin + 1 && j <= P.kmax)) return T(0.0);
+  const double* afact = gr + GF_AFACT * K;
+  const double* bfact = gr + GF_BFACT * K;
+  const T gh = xf(in, A_gsgam2h, j);
+  const T c2w0 = afact[j] / xf(in, A_gsgam2, j) * gh;
+  const T c2w1 = bfact[j] / xf(in, A_gsgam2, j - 1) * gh;
+  const T rw = in.w(W_RW_N, j);
+  return 0.5 * (rw * rw) / (c2w0 * in.w(W_RHOG_N, j) + c2w1 * in.w(W_RHOG_N, j - 1));
+}
+
+// S4: KIN2EIN, thermodynamics, saturation adjustment and negative filter of
+// cell (l, k, g); fin(seed field, value) for each output.  Returns the Newton
+// status (0, or 3 / 4 with *iters).
+template <class T, class F>
+__device__ int stage4(const In<T>& in, const Consts& C, const double* gr, const FastMath& fm, int k, const F& fin,
+                      int* iters) {
+  const Problem& P = in.io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const double* cfact = gr + GF_CFACT * K;
+  const double* dfact = gr + GF_DFACT * K;
+  const bool interior = (k >= kmin && k <= kmax);
+  const T rhog = in.w(W_RHOG_N, k);
+  const T rrhog = 1.0 / rhog;
+  T rhoge = in.w(W_RHOGE_N, k);
+  const T gsg = xf(in, A_gsgam2, k);
+  if (interior) {
+    // KIN2EIN (mod_precip_transport.cpp:991-1011): the transported kinetic
+    // energy tmp2 less that of the updated state
+    const T gh = xf(in, A_gsgam2h, k + 1), rgh = 1.0 / gh;
+    const T w2c0 = div_rn(cfact[k] * gsg, gh, rgh);
+    const T w2c1 = div_rn(dfact[k] * gsg, gh, rgh);
+    const T tmp2 = in.w(W_KINH_N, k) + (w2c0 * in.w(W_KINV_N, k + 1) + w2c1 * in.w(W_KINV_N, k));
+    const T rvx = in.w(W_RVX_N, k), rvy = in.w(W_RVY_N, k), rvz = in.w(W_RVZ_N, k);
+    const T tmp_h = div_rn(0.5 * (rvx * rvx + rvy * rvy + rvz * rvz), rhog, rrhog);
+    const T tmp = tmp_h + (w2c0 * kinv_new(in, gr, k + 1) + w2c1 * kinv_new(in, gr, k));
+    rhoge = rhoge + (tmp2 - tmp);
+  }
+  T rq[6], q[6];
+#pragma unroll
+  for (int n = 0; n < 6; ++n) rq[n] = in.w(W_RQ_N + n, k);
+#pragma unroll
+  for (int n = 0; n < 6; ++n) q[n] = div_rn(rq[n], rhog, rrhog);
+  T rho = rhog / gsg;
+  const T ein = div_rn(rhoge, rhog, rrhog);
+  T qd = T(1.0);
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) qd = qd - q[n];
+  T cvt = T(0.0), qdl = T(1.0);
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) {
+    cvt = cvt + q[n] * CVDRY;
+    qdl = qdl - q[n];
+  }
+  cvt = cvt + qdl * CVDRY;
+  T tem = ein / cvt;
+  T pre = rho * tem * (qdl * RDRY + q[I_QV] * RVAP);
+  const T ein_moist = ein + q[I_QV] * LHV0;
+  const T qsum = q[I_QV] + q[I_QC];
+  q[I_QV] = qsum;
+  q[I_QC] = T(0.0);
+  T cvtot = qd * CVDRY;
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+  const T rho_l = rho;
+  tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
+  int rc = 0;
+  if (interior) rc = satadjust_t(C, fm, P.itelim, ein_moist, qsum, rho_l, q, tem, iters);
+  rq[I_QV] = rhog * q[I_QV];
+  rq[I_QC] = rhog * q[I_QC];
+  cvtot = qd * CVDRY;
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+  rhoge = rhog * tem * cvtot;
+  T rhog_o = rhog;
+  if (interior) {
+    // negative_filter (mod_mp_nsw6.cpp:1770-1831)
+    T diffq = T(0.0);
+#pragma unroll
+    for (int n = 2; n <= 5; ++n) {
+      diffq += rq[n];
+      rq[n] = dmax(rq[n], T(0.0));
+    }
+#pragma unroll
+    for (int n = 2; n <= 5; ++n) diffq -= rq[n];
+    rq[I_QV] += diffq;
+    diffq = rq[I_QV];
+    rq[I_QV] = dmax(rq[I_QV], T(0.0));
+    diffq -= rq[I_QV];
+    rhog_o = rhog * (1.0 - diffq);
+    rho = rhog_o / gsg;
+    const T rrhog_o = 1.0 / rhog_o;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) q[n] = div_rn(rq[n], rhog_o, rrhog_o);
+    T qdf = T(1.0);
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
+    T cva = qdf * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
+    rhoge = tem * rhog_o * cva;
+    pre = rho * (qdf * RDRY + q[I_QV] * RVAP) * tem;
+  }
+  fin(SF_RHOG, rhog_o);
+  fin(SF_RHOGE, rhoge);
+#pragma unroll
+  for (int n = 0; n < 6; ++n) {
+    fin(SF_RQ + n, rq[n]);
+    fin(SF_Q + n, q[n]);
+  }
+  fin(SF_RHO, rho);
+  fin(SF_TEM, tem);
+  fin(SF_PRE, pre);
+  fin(SF_QD, qd);
+  return rc;
+}
+
+__device__ __forceinline__ void stage_smem(const Problem& P, double* grid, double* tab) {
+  for (int c = threadIdx.x; c < GF_COUNT * P.kall; c += blockDim.x) grid[c] = P.grid[c];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  __syncthreads();
+}
+
+__device__ __forceinline__ void tape_bind_s(const TapeMem& tm) {
+  Tape& t = tape();
+  t.pa = tm.pa;
+  t.pb = tm.pb;
+  t.da = tm.da;
+  t.db = tm.db;
+  t.adj = tm.adj;
+  t.nslot = tm.nslot;
+  t.slot = blockIdx.x * blockDim.x + threadIdx.x;
+  t.cap = tm.cap;
+  t.count_only = 0;
+}
+
+// Starts a new record on the calling thread's tape.
+__device__ __forceinline__ void tape_begin(LeafLog& lg) {
+  Tape& t = tape();
+  t.n = 0;
+  t.overflow = 0;
+  lg.n = 0;
+  lg.overflow = 0;
+}
+
+// Zeroes the adjoints of the recorded entries (after seeding nothing yet).
+__device__ __forceinline__ void tape_clear_adj() {
+  Tape& t = tape();
+  for (int e = 0; e < t.n; ++e) t.adj[(size_t)e * t.nslot + t.slot] = 0.0;
+}
+
+__device__ __forceinline__ void seed(const RVar& v, double g) {
+  if (v.id >= 0 && g != 0.0) adj_of(v) += g;
+}
+
+// Adds the adjoints of the logged leaves to where their values came from.
+__device__ __forceinline__ void scatter(const StageIO& io, const LeafLog& lg) {
+  for (int e = 0; e < lg.n; ++e) {
+    const double g = adj_of(RVar(0.0, lg.id[e]));
+    if (g == 0.0) continue;
+    const int kind = lg.code[e] / 4096, f = lg.code[e] % 4096;
+    double* dst = kind == LK_W ? io.WB + f * io.NC : kind == LK_Y ? io.YB + f * io.NC : io.xb.a[f];
+    atomicAdd(dst + lg.idx[e], g);
+  }
+}
+
+// Reports a stage whose tape or leaf log ran out of room.
+__device__ __forceinline__ bool stage_overflow(const StageIO& io, const LeafLog& lg, int k, int g, int l) {
+  if (tape().overflow || lg.overflow) {
+    record_err(io.P.status, ERR_ADJ_CAPACITY, k, g, l, tape().n);
+    return true;
+  }
+  return false;
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(STAGE_THREADS) adj_bounds_kernel(Problem P, int* bnd) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * P.kall; c += blockDim.x) grid[c] = P.grid[c];
+  __syncthreads();
+  const int l = blockIdx.x;
+  const int K = P.kall;
+  if (threadIdx.x == 0) {
+    int bmn[6][KA], bmx[6][KA];
+    column_bounds(grid + GF_GZH * K, grid + GF_GZSHIFT * K, K, P.kmin, P.kmax, P.zmax + (size_t)l * 6 * K,
+                  P.zmin + (size_t)l * 6 * K, bmn, bmx);
+    for (int s = 0; s < 6; ++s)
+      for (int k = 0; k < K; ++k) {
+        bnd[((size_t)l * 2 + 0) * 6 * K + s * K + k] = bmn[s][k];
+        bnd[((size_t)l * 2 + 1) * 6 * K + s * K + k] = bmx[s][k];
+      }
+  }
+}
+
+// Forward of S1 (every cell of every level).
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s1_fwd_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  const size_t n = io.NC;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    const In<double> in{io, l, g};
+    stage1<double>(in, grid, k, [&](int f, double v) { io.W[f * io.NC + c] = v; });
+  }
+}
+
+// Forward of S2 (a work item per cell and flux).
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s2_fwd_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  const size_t n = io.NC * 24;
+  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = w % io.NC;
+    const int j = (int)(w / io.NC);
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    const In<double> in{io, l, g};
+    io.W[(W_F + j) * io.NC + c] = stage2<double>(in, grid, k, j);
+  }
+}
+
+// Forward of S3.
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s3_fwd_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    const In<double> in{io, l, g};
+    stage3<double>(
+        in, grid, k, [&](int f, double v) { io.W[f * io.NC + c] = v; }, [](int, double) {}, [](int, double) {});
+  }
+}
+
+// Adjoint of S4: seeds from the caller's output adjoints.
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Consts C, TapeMem tm) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  stage_smem(io.P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  tape_bind_s(tm);
+  LeafLog lg;
+  for (size_t c = tape().slot; c < io.NC; c += tape().nslot) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    tape_begin(lg);
+    const In<RVar> in{io, l, g, &lg};
+    RVar outs[NSF];
+    int it = 0;
+    const int rc = stage4<RVar>(in, C, grid, fm, k, [&](int f, const RVar& v) { outs[f] = v; }, &it);
+    if (rc) record_err(io.P.status, rc, k, g, l, it);
+    if (stage_overflow(io, lg, k, g, l)) continue;
+    tape_clear_adj();
+    for (int f = 0; f < NSF; ++f)
+      if (f != SF_RVX && f != SF_RVY && f != SF_RVZ && f != SF_RW && f != SF_GPREC) seed(outs[f], io.SB[f * io.NC + c]);
+    tape_reverse();
+    scatter(io, lg);
+  }
+}
+
+// Adjoint of S3: seeds from S4's adjoints (WB) and the caller's output
+// adjoints of rhogvx/y/z, rhogw, GPREC and the surface outputs.
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s3_kernel(StageIO io, TapeMem tm) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  tape_bind_s(tm);
+  LeafLog lg;
+  const double* SC = io.SB + (size_t)NSF * io.NC;   // [NSC][lall][gall]
+  const size_t ncol = (size_t)io.L.lall * io.L.G;
+  for (size_t c = tape().slot; c < io.NC; c += tape().nslot) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    tape_begin(lg);
+    const In<RVar> in{io, l, g, &lg};
+    RVar wo[NWF - W_RHOG_N];
+    RVar fo[NSF];
+    RVar co[NSC];
+    stage3<RVar>(
+        in, grid, k, [&](int f, const RVar& v) { wo[f - W_RHOG_N] = v; }, [&](int f, const RVar& v) { fo[f] = v; },
+        [&](int f, const RVar& v) { co[f] = v; });
+    if (stage_overflow(io, lg, k, g, l)) continue;
+    tape_clear_adj();
+    for (int f = W_RHOG_N; f < NWF; ++f) seed(wo[f - W_RHOG_N], io.WB[f * io.NC + c]);
+    seed(fo[SF_RVX], io.SB[SF_RVX * io.NC + c]);
+    seed(fo[SF_RVY], io.SB[SF_RVY * io.NC + c]);
+    seed(fo[SF_RVZ], io.SB[SF_RVZ * io.NC + c]);
+    seed(fo[SF_RW], io.SB[SF_RW * io.NC + c]);
+    if (k >= io.P.kmin && k <= io.P.kmax) seed(fo[SF_GPREC], io.SB[SF_GPREC * io.NC + c]);
+    if (k == io.P.kmin)
+      for (int f = 0; f < NSC; ++f) seed(co[f], SC[f * ncol + io.L.c(l, g)]);
+    tape_reverse();
+    scatter(io, lg);
+  }
+}
+
+// Adjoint of S2 (a work item per cell and flux).
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s2_kernel(StageIO io, TapeMem tm) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  tape_bind_s(tm);
+  LeafLog lg;
+  const size_t n = io.NC * 24;
+  for (size_t w = tape().slot; w < n; w += tape().nslot) {
+    const size_t c = w % io.NC;
+    const int j = (int)(w / io.NC);
+    const double gF = io.WB[(W_F + j) * io.NC + c];
+    if (gF == 0.0) continue;
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    tape_begin(lg);
+    const In<RVar> in{io, l, g, &lg};
+    const RVar F = stage2<RVar>(in, grid, k, j);
+    if (stage_overflow(io, lg, k, g, l)) continue;
+    tape_clear_adj();
+    seed(F, gF);
+    tape_reverse();
+    scatter(io, lg);
+  }
+}
+
+// Adjoint of S1: seeds from S2's and S3's adjoints (WB).
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s1_kernel(StageIO io, TapeMem tm) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  tape_bind_s(tm);
+  LeafLog lg;
+  for (size_t c = tape().slot; c < io.NC; c += tape().nslot) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    tape_begin(lg);
+    const In<RVar> in{io, l, g, &lg};
+    RVar o[W_F];
+    stage1<RVar>(in, grid, k, [&](int f, const RVar& v) { o[f] = v; });
+    if (stage_overflow(io, lg, k, g, l)) continue;
+    tape_clear_adj();
+    for (int f = 0; f < W_F; ++f) seed(o[f], io.WB[f * io.NC + c]);
+    tape_reverse();
+    scatter(io, lg);
+  }
+}
+
+// Copies the caller's output adjoints of the column phase into the seed
+// buffer and clears them there (input adjoints are then added in place).
+__global__ void adj_seed_kernel(StageIO io) {
+  const LayS& L = io.L;
+  double* SB = const_cast<double*>(io.SB);
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % L.G), k = (int)((c / L.G) % L.K), l = (int)(c / ((size_t)L.G * L.K));
+    auto take = [&](int f, int a, size_t i) {
+      SB[f * io.NC + c] = io.xb.a[a][i];
+      io.xb.a[a][i] = 0.0;
+    };
+    take(SF_RHOG, A_rhog, c);
+    take(SF_RHOGE, A_rhoge, c);
+    take(SF_RVX, A_rhogvx, c);
+    take(SF_RVY, A_rhogvy, c);
+    take(SF_RVZ, A_rhogvz, c);
+    take(SF_RW, A_rhogw, c);
+    take(SF_RHO, A_rho, c);
+    take(SF_TEM, A_tem, c);
+    take(SF_PRE, A_pre, c);
+    take(SF_QD, A_qd, c);
+    take(SF_GPREC, A_GPREC, c);
+    for (int n = 0; n < 6; ++n) {
+      take(SF_RQ + n, A_rhogq, L.t(l, n, k, g));
+      take(SF_Q + n, A_q, L.t(l, n, k, g));
+    }
+    io.xb.a[A_re_solid][c] = 0.0;
+    io.xb.a[A_GDCLW][c] = 0.0;
+    io.xb.a[A_GDCFRC][c] = 0.0;
+    // outputs of the cell phase (interior levels): their adjoints go to YB
+    const bool interior = (k >= io.P.kmin && k <= io.P.kmax);
+    io.YB[YS_RE * io.NC + c] = interior ? io.xb.a[A_re_liquid][c] : 0.0;
+    io.YB[YS_RECLD * io.NC + c] = interior ? io.xb.a[A_re_cld][c] : 0.0;
+    io.xb.a[A_re_liquid][c] = 0.0;
+    io.xb.a[A_re_cld][c] = 0.0;
+    if (k == io.P.kmax) {
+      // rwtop = sw rctop + (1 - sw) UNDEF with sw from tctop (TagUpdateCLD)
+      const size_t ic = L.c(l, g);
+      const double sw = (0.5 + copysign(0.5, io.Y[YS_TCTOP * io.NC + c] - TEM00));
+      io.YB[YS_RCTOP * io.NC + c] = io.xb.a[A_rctop][ic] + sw * io.xb.a[A_rwtop][ic];
+      io.YB[YS_TCTOP * io.NC + c] = io.xb.a[A_tctop][ic];
+    }
+    if (k == 0) {
+      const size_t ncol = (size_t)L.lall * L.G;
+      double* SC = SB + (size_t)NSF * io.NC;
+      const size_t ic = L.c(l, g);
+      auto takec = [&](int f, int a, size_t i) {
+        SC[f * ncol + ic] = io.xb.a[a][i];
+        io.xb.a[a][i] = 0.0;
+      };
+      takec(SC_PRECIP0, A_precip, L.p(0, l, g));
+      takec(SC_PRECIP1, A_precip, L.p(1, l, g));
+      takec(SC_LH, A_precip_lh_heat, ic);
+      takec(SC_RHOE, A_precip_rhoe, ic);
+      takec(SC_RHOPHI, A_precip_rhophi, ic);
+      takec(SC_RHOKIN, A_precip_rhokin, ic);
+      io.xb.a[A_ISO1][L.p(0, l, g)] = 0.0;
+      io.xb.a[A_ISO1][L.p(1, l, g)] = 0.0;
+      io.xb.a[A_ISO2][L.p(0, l, g)] = 0.0;
+      io.xb.a[A_ISO2][L.p(1, l, g)] = 0.0;
+    }
+  }
+}
+
+// Clears the caller's adjoints of the cloud-top outputs (read by the seed
+// kernel at the top interior level).
+__global__ void adj_seed_columns_kernel(StageIO io) {
+  const size_t ncol = (size_t)io.L.lall * io.L.G;
+  for (size_t ic = (size_t)blockIdx.x * blockDim.x + threadIdx.x; ic < ncol; ic += (size_t)gridDim.x * blockDim.x) {
+    io.xb.a[A_rctop][ic] = 0.0;
+    io.xb.a[A_rwtop][ic] = 0.0;
+    io.xb.a[A_tctop][ic] = 0.0;
+  }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+size_t adj_stage_work_doubles(int lall, int kall, int gall) {
+  const size_t NC = (size_t)lall * kall * gall;
+  return 2 * (size_t)NWF * NC + (size_t)NSF * NC + (size_t)NSC * lall * gall;
+}
+size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 6 * kall; }
+int adj_stage_tape_cap() { return 512; }
+int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
+
+// The column phase's adjoint: its forward S1..S3 from the state x and the cell
+// phase's outputs Y, then the adjoints S4..S1 into YB (zeroed here first) and
+// xb.  work: adj_stage_work_doubles doubles; bnd: adj_stage_bound_ints ints;
+// tm: adj_stage_slots() slots of adj_stage_tape_cap() entries.
+cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
+                                     const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
+                                     cudaStream_t stream) {
+  StageIO io;
+  io.P = P;
+  io.L = LayS{P.kall, P.gall, P.lall};
+  io.NC = (size_t)P.lall * P.kall * P.gall;
+  io.x = x;
+  io.xb = xb;
+  io.Y = Y;
+  io.YB = YB;
+  io.W = work;
+  io.WB = work + (size_t)NWF * io.NC;
+  io.SB = work + 2 * (size_t)NWF * io.NC;
+  io.bnd = bnd;
+  const int blocks = tm.nslot / STAGE_THREADS;
+  cudaError_t e;
+  if ((e = cudaMemsetAsync(io.WB, 0, sizeof(double) * NWF * io.NC, stream)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(YB, 0, sizeof(double) * ny * io.NC, stream)) != cudaSuccess) return e;
+  adj_bounds_kernel<<<P.lall, 32, 0, stream>>>(P, bnd);
+  adj_s1_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  adj_s2_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  adj_seed_kernel<<<152 * 4, 256, 0, stream>>>(io);
+  adj_seed_columns_kernel<<<64, 256, 0, stream>>>(io);
+  adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
+  adj_s3_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  return cudaGetLastError();
+}
+
+}  // namespace nsw6

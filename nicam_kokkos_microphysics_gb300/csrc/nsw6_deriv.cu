@@ -340,10 +340,13 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_adj_column_kernel(Problem P, 
   }
 }
 
+// done[cell] (may be null): set once a cell's adjoint has been added; cells
+// already done are skipped, so that a launch repeated with a longer tape after
+// an overflow adds each cell once.
 __global__ void __launch_bounds__(AD_THREADS) nsw6_adj_cell_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
                                                                    const double* YB, TapeMem tm,
                                                                    const double* params, double* pbar,
-                                                                   int* tape_max) {
+                                                                   int* tape_max, int* done) {
   __shared__ double tab[FM_TABLE_DOUBLES];
   __shared__ double red[7][AD_THREADS];
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
@@ -358,6 +361,7 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_adj_cell_kernel(Problem P, Co
   Tape& t = tape();
   double pacc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (long long c = t.slot; c < ncell; c += t.nslot) {
+    if (done && done[c]) continue;
     const int g = (int)(c % P.gall);
     const int k = P.kmin + (int)((c / P.gall) % nint);
     const int l = (int)(c / ((long long)P.gall * nint));
@@ -406,6 +410,7 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_adj_cell_kernel(Problem P, Co
     add(in.q0, A_q, L.t(l, 0, k, g));
     for (int n = 0; n < 6; ++n) add(in.rhogq[n], A_rhogq, L.t(l, n, k, g));
     for (int j = 0; j < 7; ++j) pacc[j] += adj_of(p[j]);
+    if (done) done[c] = 1;
   }
   for (int j = 0; j < 7; ++j) red[j][threadIdx.x] = pacc[j];
   __syncthreads();
@@ -444,10 +449,10 @@ cudaError_t launch_adj_column(const Problem& P, const Consts& C, const ArgPtrs& 
 }
 
 cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
-                            const TapeMem& tm, const double* params, double* pbar, int* tape_max,
+                            const TapeMem& tm, const double* params, double* pbar, int* tape_max, int* done,
                             cudaStream_t stream) {
   nsw6_adj_cell_kernel<<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, YB, tm, params, pbar,
-                                                                         tape_max);
+                                                                         tape_max, done);
   return cudaGetLastError();
 }
 

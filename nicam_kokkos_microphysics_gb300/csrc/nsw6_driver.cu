@@ -28,8 +28,15 @@ cudaError_t launch_adj_cellfwd(const Problem& P, const Consts& C, const ArgPtrs&
 cudaError_t launch_adj_column(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* Y,
                               double* YB, const TapeMem& tm, int* tape_max, cudaStream_t stream);
 cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
-                            const TapeMem& tm, const double* params, double* pbar, int* tape_max,
+                            const TapeMem& tm, const double* params, double* pbar, int* tape_max, int* done,
                             cudaStream_t stream);
+cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
+                                     const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
+                                     cudaStream_t stream);
+size_t adj_stage_work_doubles(int lall, int kall, int gall);
+size_t adj_stage_bound_ints(int lall, int kall);
+int adj_stage_tape_cap();
+int adj_stage_slots();
 int adj_nfields();
 constexpr int DERIV_MAX_KALL = 48;   // KA of nsw6_column_step.cuh
 constexpr int DERIV_THREADS = 128;   // AD_THREADS of nsw6_ad.cuh
@@ -66,6 +73,11 @@ struct nsw6_handle {
   size_t tape_bytes = 0;
   TapeMem ctape{};       // cell-adjoint tapes
   size_t ctape_bytes = 0;
+  TapeMem stape{};       // tapes of the staged column adjoint
+  size_t stape_bytes = 0;
+  double* d_swork = nullptr;   // work fields, their adjoints and the seeds of the staged column adjoint
+  int* d_sbnd = nullptr;       // flux bounds of the staged column adjoint
+  int* d_done = nullptr;       // per-cell flags of the cell adjoint
   double* d_Y = nullptr;   // cell-phase outputs and their adjoints [2][nfields][lall_max][kall][gall]
   // captured step graph of mp_driver_steps and what it was captured for
   cudaStream_t cap_stream = nullptr;
@@ -667,6 +679,10 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_tmax);
   cudaFree(h->tape.pa);
   cudaFree(h->ctape.pa);
+  cudaFree(h->stape.pa);
+  cudaFree(h->d_swork);
+  cudaFree(h->d_sbnd);
+  cudaFree(h->d_done);
   cudaFree(h->d_Y);
   for (auto& tri : h->ev)
     for (auto& e : tri)
@@ -1038,41 +1054,60 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
     long long s = ((n + DERIV_THREADS - 1) / DERIV_THREADS) * DERIV_THREADS;
     return (int)(s > maxs ? maxs : s);
   };
-  const int ncol_slots = round_slots((long long)lall * h->gall, ADJ_COL_SLOTS);
-  const int ncell_slots = round_slots((long long)lall * (h->kall - 2) * h->gall, ADJ_CELL_SLOTS);
-  if (launch_adj_cellfwd(P, h->C, x, Y, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
-  // sizing passes: the longest tape of each stage
-  int tcol = 0, tcell = 0;
-  TapeMem cnt{};
-  cnt.count_only = 1;
-  cnt.nslot = ncol_slots;
-  if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-      launch_adj_column(P, h->C, x, xb, Y, YB, cnt, h->d_tmax, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(&tcol, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
-    return NSW6_ERR_CUDA;
-  cnt.nslot = ncell_slots;
-  if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-      launch_adj_cell(P, h->C, x, xb, YB, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(&tcell, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-      cudaStreamSynchronize(h->stream) != cudaSuccess)
-    return NSW6_ERR_CUDA;
-  if ((rc = ensure_tape(h->tape, h->tape_bytes, ncol_slots, tcol)) != NSW6_OK) return rc;
-  if ((rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, tcell)) != NSW6_OK) return rc;
-  h->tape.count_only = 0;
-  h->ctape.count_only = 0;
+  const long long ncell = (long long)lall * (h->kall - 2) * h->gall;
+  const int ncell_slots = round_slots(ncell, ADJ_CELL_SLOTS);
+  // buffers of the staged column adjoint and the per-cell flags, sized for lall_max
+  if (!h->d_swork) {
+    if (cudaMalloc(&h->d_swork, sizeof(double) * adj_stage_work_doubles(h->lall_max, h->kall, h->gall)) !=
+            cudaSuccess ||
+        cudaMalloc(&h->d_sbnd, sizeof(int) * adj_stage_bound_ints(h->lall_max, h->kall)) != cudaSuccess ||
+        cudaMalloc(&h->d_done, sizeof(int) * (size_t)h->lall_max * h->kall * h->gall) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+  }
+  if ((rc = ensure_tape(h->stape, h->stape_bytes, adj_stage_slots(), adj_stage_tape_cap())) != NSW6_OK) return rc;
+  h->stape.count_only = 0;
   double pb[8] = {};
-  int t1 = 0, t2 = 0;
-  if (cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
-      cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-      launch_adj_column(P, h->C, x, xb, Y, YB, h->tape, h->d_tmax, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(&t1, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-      cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-      launch_adj_cell(P, h->C, x, xb, YB, h->ctape, h->d_dparam, h->d_pbar, h->d_tmax, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(&t2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-      cudaMemcpyAsync(pb, h->d_pbar, sizeof(double) * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+  // the cell phase's outputs, then the column phase's adjoint (level-parallel stages)
+  if (launch_adj_cellfwd(P, h->C, x, Y, h->stream) != cudaSuccess ||
+      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->stream) !=
+          cudaSuccess ||
+      cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
+      cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  // the cell phase's adjoint: a tape as long as the longest cell's record
+  // (measured once, then kept; a longer record makes the launch repeat for the
+  // cells that did not fit)
+  for (int attempt = 0; attempt < 3; ++attempt) {
+    if (!h->ctape.pa || attempt > 0) {
+      int tcell = 0;
+      TapeMem cnt{};
+      cnt.count_only = 1;
+      cnt.nslot = ncell_slots;
+      if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+          launch_adj_cell(P, h->C, x, xb, YB, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->d_done, h->stream) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(&tcell, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+          cudaStreamSynchronize(h->stream) != cudaSuccess)
+        return NSW6_ERR_CUDA;
+      if ((rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, tcell + tcell / 4 + 64)) != NSW6_OK) return rc;
+    }
+    h->ctape.count_only = 0;
+    if (h->ctape.nslot != ncell_slots &&
+        (rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, h->ctape.cap)) != NSW6_OK)
+      return rc;
+    int t2 = 0;
+    if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+        launch_adj_cell(P, h->C, x, xb, YB, h->ctape, h->d_dparam, h->d_pbar, h->d_tmax, h->d_done, h->stream) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(&t2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+    if (t2 <= h->ctape.cap) break;
+    if (attempt == 2) return NSW6_ERR_UNSUPPORTED;
+  }
+  if (cudaMemcpyAsync(pb, h->d_pbar, sizeof(double) * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
       cudaStreamSynchronize(h->stream) != cudaSuccess)
     return NSW6_ERR_CUDA;
-  if (t1 > h->tape.cap || t2 > h->ctape.cap) return NSW6_ERR_UNSUPPORTED;
   if (dparams)
     for (int i = 0; i < 7; ++i) dparams[i] += pb[i];
   return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
