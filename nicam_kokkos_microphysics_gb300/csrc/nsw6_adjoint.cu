@@ -592,34 +592,101 @@ __device__ __forceinline__ bool stage_overflow(const StageIO& io, const LeafLog&
 }
 
 // ------------------------------------------------------------------ kernels
-__global__ void __launch_bounds__(STAGE_THREADS) adj_bounds_kernel(Problem P, int* bnd) {
-  __shared__ double grid[GF_COUNT * MAX_KALL];
-  for (int c = threadIdx.x; c < GF_COUNT * P.kall; c += blockDim.x) grid[c] = P.grid[c];
-  __syncthreads();
-  const int l = blockIdx.x;
+// Flux bounds kcell_min / kcell_max of every region, row and level from the
+// departure-distance extrema (mod_vadv1d.cpp:316-353), one thread each, as
+// the column kernel forms them.
+__global__ void adj_bounds_kernel(Problem P, int* bnd) {
   const int K = P.kall;
-  if (threadIdx.x == 0) {
-    int bmn[6][KA], bmx[6][KA];
-    column_bounds(grid + GF_GZH * K, grid + GF_GZSHIFT * K, K, P.kmin, P.kmax, P.zmax + (size_t)l * 6 * K,
-                  P.zmin + (size_t)l * 6 * K, bmn, bmx);
-    for (int s = 0; s < 6; ++s)
-      for (int k = 0; k < K; ++k) {
-        bnd[((size_t)l * 2 + 0) * 6 * K + s * K + k] = bmn[s][k];
-        bnd[((size_t)l * 2 + 1) * 6 * K + s * K + k] = bmx[s][k];
+  const int n = P.lall * 6 * K;
+  const double* gzh = P.grid + GF_GZH * K;
+  const double* gzs = P.grid + GF_GZSHIFT * K;
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const int k = e % K, s = (e / K) % 6, l = e / (6 * K);
+    const int half = s / 3;
+    const int mkmin = half ? P.kmin + 1 : P.kmin;
+    const double* zh = half ? gzs : gzh;
+    int lo = k, hi = k;
+    if (k >= mkmin && k <= P.kmax) {
+      const unsigned long long kx = P.zmax[e], kn = P.zmin[e];
+      double zzmax = DBL_MIN, zzmin = DBL_MIN;
+      if (kx != 0ull) {
+        const double v = key_value(kx);
+        zzmax = v > zzmax ? v : zzmax;
       }
+      if (kn != ~0ull) {
+        const double v = key_value(kn);
+        zzmin = v < zzmin ? v : zzmin;
+      }
+      if (zzmax > 0.0) {
+        for (int k2 = k; k2 >= mkmin; --k2)
+          if ((zh[k2] <= zh[k] - zzmax) && (zh[k2 + 1] > zh[k] - zzmax)) {
+            lo = k2;
+            break;
+          }
+      }
+      if (zzmin < 0.0) {
+        for (int k2 = k; k2 <= P.kmax; ++k2)
+          if ((zh[k2] <= zh[k] - zzmin) && (zh[k2 + 1] > zh[k] - zzmin)) {
+            hi = k2;
+            break;
+          }
+      }
+    }
+    bnd[((size_t)l * 2 + 0) * 6 * K + s * K + k] = lo;
+    bnd[((size_t)l * 2 + 1) * 6 * K + s * K + k] = hi;
   }
 }
 
-// Forward of S1 (every cell of every level).
+// Forward of S1.  A block is STAGE_THREADS columns of one level of one region
+// (grid: columns, levels, regions), so that the per-level extrema of the
+// departure distances over the region (vadv1d_prep, mod_vadv1d.cpp:316-353)
+// reduce within the block: one 64-bit atomic per block and row, on
+// order-preserving keys (exact, independent of the order of the atomics).
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_fwd_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
+  __shared__ unsigned long long red[2][6][STAGE_THREADS / 32];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
-  const size_t n = io.NC;
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+  const int g = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y, l = blockIdx.z;
+  const bool valid = g < io.L.G;
+  double z[6] = {0, 0, 0, 0, 0, 0};
+  if (valid) {
+    const size_t c = io.L.f(l, k, g);
     const In<double> in{io, l, g};
-    stage1<double>(in, grid, k, [&](int f, double v) { io.W[f * io.NC + c] = v; });
+    stage1<double>(in, grid, k, [&](int f, double v) {
+      io.W[f * io.NC + c] = v;
+      if (f < 6) z[f] = v;
+    });
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int r = 0; r < 6; ++r) {
+    const int mkmin = r < 3 ? io.P.kmin : io.P.kmin + 1;
+    const bool in_range = valid && k >= mkmin && k <= io.P.kmax && z[r] == z[r];   // NaN never wins
+    unsigned long long kmx = in_range ? order_key(z[r]) : 0ull;
+    unsigned long long kmn = in_range ? order_key(z[r]) : ~0ull;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long a = __shfl_xor_sync(0xffffffffu, kmx, o);
+      const unsigned long long b = __shfl_xor_sync(0xffffffffu, kmn, o);
+      kmx = a > kmx ? a : kmx;
+      kmn = b < kmn ? b : kmn;
+    }
+    if (lane == 0) {
+      red[0][r][wid] = kmx;
+      red[1][r][wid] = kmn;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    const int r = threadIdx.x;
+    unsigned long long kmx = 0ull, kmn = ~0ull;
+    for (int w = 0; w < (int)blockDim.x / 32; ++w) {
+      kmx = red[0][r][w] > kmx ? red[0][r][w] : kmx;
+      kmn = red[1][r][w] < kmn ? red[1][r][w] : kmn;
+    }
+    const size_t e = ((size_t)l * 6 + r) * io.P.kall + k;
+    if (kmx != 0ull) atomicMax(&io.P.zmax[e], kmx);
+    if (kmn != ~0ull) atomicMin(&io.P.zmin[e], kmn);
   }
 }
 
@@ -841,11 +908,12 @@ size_t adj_stage_work_doubles(int lall, int kall, int gall) {
 }
 size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 6 * kall; }
 int adj_stage_tape_cap() { return 512; }
-int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
+int adj_stage_slots() { return 152 * 8 * STAGE_THREADS; }
 
 // The column phase's adjoint: its forward S1..S3 from the state x and the cell
-// phase's outputs Y, then the adjoints S4..S1 into YB (zeroed here first) and
-// xb.  work: adj_stage_work_doubles doubles; bnd: adj_stage_bound_ints ints;
+// phase's outputs Y (S1 also forms the region extrema of the departure
+// distances in P.zmax / P.zmin, and from them the flux bounds), then the
+// adjoints S4..S1 into YB (zeroed here first) and xb.  work: adj_stage_work_doubles doubles; bnd: adj_stage_bound_ints ints;
 // tm: adj_stage_slots() slots of adj_stage_tape_cap() entries.
 cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
@@ -866,8 +934,12 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   cudaError_t e;
   if ((e = cudaMemsetAsync(io.WB, 0, sizeof(double) * NWF * io.NC, stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(YB, 0, sizeof(double) * ny * io.NC, stream)) != cudaSuccess) return e;
-  adj_bounds_kernel<<<P.lall, 32, 0, stream>>>(P, bnd);
-  adj_s1_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+  adj_s1_fwd_kernel<<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(
+      io);
+  adj_bounds_kernel<<<(int)((nkey + 127) / 128), 128, 0, stream>>>(P, bnd);
   adj_s2_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_seed_kernel<<<152 * 4, 256, 0, stream>>>(io);

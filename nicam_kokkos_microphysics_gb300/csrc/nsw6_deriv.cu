@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_adj_column_kernel(Problem P, 
 // done[cell] (may be null): set once a cell's adjoint has been added; cells
 // already done are skipped, so that a launch repeated with a longer tape after
 // an overflow adds each cell once.
-__global__ void __launch_bounds__(AD_THREADS) nsw6_adj_cell_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
+__global__ void __launch_bounds__(AD_THREADS, 3) nsw6_adj_cell_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
                                                                    const double* YB, TapeMem tm,
                                                                    const double* params, double* pbar,
                                                                    int* tape_max, int* done) {

@@ -41,7 +41,7 @@ int adj_nfields();
 constexpr int DERIV_MAX_KALL = 48;   // KA of nsw6_column_step.cuh
 constexpr int DERIV_THREADS = 128;   // AD_THREADS of nsw6_ad.cuh
 constexpr int ADJ_COL_SLOTS = 8192;    // threads of the column adjoint (each with its own tape)
-constexpr int ADJ_CELL_SLOTS = 32768;  // threads of the cell adjoint
+constexpr int ADJ_CELL_SLOTS = 152 * 3 * 128;  // threads of the cell adjoint (3 resident blocks per SM)
 cudaError_t launch_math(int fn, const double* x, const double* y, double* out, int n, const double* fmtab,
                         cudaStream_t stream);
 }
@@ -1030,8 +1030,6 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
                       double dt, double ct) {
   (void)ct;
   int rc = deriv_check(h, lall, args, aargs);
-  if (rc != NSW6_OK) return rc;
-  rc = deriv_prepass(h, lall, args, dt);
   if (rc != NSW6_OK) return rc;
   Problem P;
   rc = fill_problem(h, lall, args, dt, P);
