@@ -181,12 +181,11 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_tlm_kernel(Problem P, Consts 
 }
 
 // ------------------------------------------------------------------ adjoint in stages
-// The adjoint step runs in three kernels so that the cell physics, which is
-// local to a cell, is differentiated with one thread per cell:
+// The adjoint step differentiates every part with one thread per cell:
 //   1. nsw6_adj_cellfwd_kernel  (per cell)    the FP64 cell phase, its outputs Y;
-//   2. nsw6_adj_column_kernel   (per column)  the adjoint of the column phase
-//      around Y: adjoints of the step's inputs it reads directly (into xb) and
-//      of the cell phase's outputs (YB);
+//   2. the column phase's adjoint around Y in level-parallel stages
+//      (nsw6_adjoint.cu): adjoints of the step's inputs it reads directly
+//      (into xb) and of the cell phase's outputs (YB);
 //   3. nsw6_adj_cell_kernel     (per cell)    the adjoint of the cell phase:
 //      adjoints of the cell inputs (into xb) and of the parameters.
 // Y / YB layout: [ADJ_NF][lall][kall][gall], fields below.
@@ -243,101 +242,6 @@ __device__ __forceinline__ void tape_bind(const TapeMem& tm) {
   t.slot = blockIdx.x * blockDim.x + threadIdx.x;
   t.cap = tm.cap;
   t.count_only = tm.count_only;
-}
-
-__global__ void __launch_bounds__(AD_THREADS) nsw6_adj_column_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
-                                                                     const double* Y, double* YB, TapeMem tm,
-                                                                     int* tape_max) {
-  __shared__ double grid[GF_COUNT * KA];
-  __shared__ double tab[FM_TABLE_DOUBLES];
-  stage(P, grid, tab);
-  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
-  const Lay L{P.kall, P.gall, P.lall};
-  const size_t NC = (size_t)P.lall * P.kall * P.gall;
-  tape_bind(tm);
-  Tape& t = tape();
-  const int ncol = P.lall * P.gall;
-  for (int col = t.slot; col < ncol; col += t.nslot) {
-    const int l = col / P.gall, g = col % P.gall;
-    t.n = 0;
-    t.overflow = 0;
-    ColState<RVar> s;
-    ColWork<RVar> w;
-    // direct inputs and the halo levels from x; interior state from the cell phase's outputs Y
-    for_inputs(s, L, l, g, [&](int a, size_t i, RVar& d) { d = leaf(x.a[a][i]); });
-    for (int k = P.kmin; k <= P.kmax; ++k) {
-      const size_t i = L.f(l, k, g);
-      s.rhog[k] = leaf(Y[Y_RHOG * NC + i]);
-      s.rhoge[k] = leaf(Y[Y_RHOGE * NC + i]);
-      s.tem[k] = leaf(Y[Y_TEM * NC + i]);
-      for (int n = 0; n < 6; ++n) s.rhogq[n][k] = leaf(Y[(Y_RHOGQ + n) * NC + i]);
-      for (int n = 1; n < 6; ++n) s.q[n][k] = leaf(Y[(Y_Q + n - 1) * NC + i]);
-      for (int v = 0; v < 3; ++v) w.vt[v][k] = leaf(Y[(Y_VT + v) * NC + i]);
-    }
-    for (int v = 0; v < 3; ++v) {
-      w.vt[v][0] = RVar(0.0);
-      w.vt[v][P.kall - 1] = RVar(0.0);
-    }
-    ColState<RVar> s_in = s;
-    ColWork<RVar> w_in;
-    for (int v = 0; v < 3; ++v)
-      for (int k = 0; k < P.kall; ++k) w_in.vt[v][k] = w.vt[v][k];
-    // outputs of the cell phase only: constants here, their adjoints go to YB
-    for (int k = 0; k < P.kall; ++k) {
-      s.re_liquid[k] = RVar(0.0);
-      s.re_cld[k] = RVar(0.0);
-    }
-    s.rctop = s.tctop = s.rwtop = RVar(0.0);
-    int bmn[6][KA], bmx[6][KA];
-    column_bounds(grid + GF_GZH * P.kall, grid + GF_GZSHIFT * P.kall, P.kall, P.kmin, P.kmax,
-                  P.zmax + (size_t)l * 6 * P.kall, P.zmin + (size_t)l * 6 * P.kall, bmn, bmx);
-    int err = 0, ek = 0, eit = 0;
-    column_transport_phase<RVar>(C, fm, grid, P.kall, P.dt, P.hdt2, P.sdt3, P.itelim, bmn, bmx, s, w, &err, &ek,
-                                 &eit);
-    if (err) record_error_d(P.status, err, ek, g, l, eit);
-    atomicMax(tape_max, t.overflow ? t.cap + 1 : t.n);
-    if (t.overflow || t.count_only) continue;
-    for (int e = 0; e < t.n; ++e) t.adj[(size_t)e * t.nslot + t.slot] = 0.0;
-    // output adjoints of the cell phase's own outputs, passed on to the cell adjoint
-    const size_t ic = L.c(l, g);
-    for (int k = P.kmin; k <= P.kmax; ++k) {
-      const size_t i = L.f(l, k, g);
-      YB[Y_RE * NC + i] = xb.a[A_re_liquid][i];
-      YB[Y_RECLD * NC + i] = xb.a[A_re_cld][i];
-      YB[Y_RCTOP * NC + i] = 0.0;
-      YB[Y_TCTOP * NC + i] = 0.0;
-    }
-    {
-      // rwtop = sw rctop + (1 - sw) UNDEF with sw from tctop (TagUpdateCLD)
-      const size_t i = L.f(l, P.kmax, g);
-      const double sw = (0.5 + copysign(0.5, Y[Y_TCTOP * NC + i] - TEM00));
-      YB[Y_RCTOP * NC + i] = xb.a[A_rctop][ic] + sw * xb.a[A_rwtop][ic];
-      YB[Y_TCTOP * NC + i] = xb.a[A_tctop][ic];
-    }
-    for_outputs(s, L, l, g, [&](int a, size_t i, RVar& d) {
-      if (d.id >= 0) adj_of(d) += xb.a[a][i];
-    });
-    tape_reverse();
-    for_outputs(s, L, l, g, [&](int a, size_t i, RVar&) { xb.a[a][i] = 0.0; });
-    // interior state and fall speeds: to YB; everything else (direct inputs,
-    // halo levels, the caller's q[QV]): added to xb
-    for (int k = P.kmin; k <= P.kmax; ++k) {
-      const size_t i = L.f(l, k, g);
-      auto put = [&](int f, RVar& d) {
-        YB[f * NC + i] = d.id >= 0 ? adj_of(d) : 0.0;
-        d.id = -1;   // not added to xb below
-      };
-      put(Y_RHOG, s_in.rhog[k]);
-      put(Y_RHOGE, s_in.rhoge[k]);
-      put(Y_TEM, s_in.tem[k]);
-      for (int n = 0; n < 6; ++n) put(Y_RHOGQ + n, s_in.rhogq[n][k]);
-      for (int n = 1; n < 6; ++n) put(Y_Q + n - 1, s_in.q[n][k]);
-      for (int v = 0; v < 3; ++v) put(Y_VT + v, w_in.vt[v][k]);
-    }
-    for_inputs(s_in, L, l, g, [&](int a, size_t i, RVar& d) {
-      if (d.id >= 0) xb.a[a][i] += adj_of(d);
-    });
-  }
 }
 
 // done[cell] (may be null): set once a cell's adjoint has been added; cells
@@ -439,12 +343,6 @@ constexpr int ADJ_NFIELDS = ADJ_NF;
 
 cudaError_t launch_adj_cellfwd(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, cudaStream_t stream) {
   nsw6_adj_cellfwd_kernel<<<152 * 4, 256, 0, stream>>>(P, C, x, Y);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_adj_column(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* Y,
-                              double* YB, const TapeMem& tm, int* tape_max, cudaStream_t stream) {
-  nsw6_adj_column_kernel<<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, Y, YB, tm, tape_max);
   return cudaGetLastError();
 }
 

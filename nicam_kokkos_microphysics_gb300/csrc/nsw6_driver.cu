@@ -25,8 +25,6 @@ cudaError_t launch_serial(const Problem& P, const Consts& C, const ArgPtrs& x, c
 cudaError_t launch_tlm(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx, const double* params,
                        const double* dparams, cudaStream_t stream);
 cudaError_t launch_adj_cellfwd(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, cudaStream_t stream);
-cudaError_t launch_adj_column(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* Y,
-                              double* YB, const TapeMem& tm, int* tape_max, cudaStream_t stream);
 cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
                             const TapeMem& tm, const double* params, double* pbar, int* tape_max, int* done,
                             cudaStream_t stream);
@@ -40,7 +38,6 @@ int adj_stage_slots();
 int adj_nfields();
 constexpr int DERIV_MAX_KALL = 48;   // KA of nsw6_column_step.cuh
 constexpr int DERIV_THREADS = 128;   // AD_THREADS of nsw6_ad.cuh
-constexpr int ADJ_COL_SLOTS = 8192;    // threads of the column adjoint (each with its own tape)
 constexpr int ADJ_CELL_SLOTS = 152 * 3 * 128;  // threads of the cell adjoint (3 resident blocks per SM)
 cudaError_t launch_math(int fn, const double* x, const double* y, double* out, int n, const double* fmtab,
                         cudaStream_t stream);
@@ -69,8 +66,6 @@ struct nsw6_handle {
   double* d_dparam = nullptr;    // [16]: params [0,7), tangents [8,15)
   double* d_pbar = nullptr;      // [8]
   int* d_tmax = nullptr;
-  TapeMem tape{};        // column-adjoint tapes
-  size_t tape_bytes = 0;
   TapeMem ctape{};       // cell-adjoint tapes
   size_t ctape_bytes = 0;
   TapeMem stape{};       // tapes of the staged column adjoint
@@ -677,7 +672,6 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_dparam);
   cudaFree(h->d_pbar);
   cudaFree(h->d_tmax);
-  cudaFree(h->tape.pa);
   cudaFree(h->ctape.pa);
   cudaFree(h->stape.pa);
   cudaFree(h->d_swork);
