@@ -86,6 +86,11 @@ struct nsw6_handle {
   // first such call)
   double* d_stage = nullptr;
   size_t stage_count = 0;
+  // copy streams and per-chunk events of the pipelined host-memory path
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaEvent_t* ev_in = nullptr;
+  cudaEvent_t* ev_done = nullptr;
+  cudaEvent_t ev_start = nullptr;
   // kernel timing: a ring of event triples folded into the sums when full
   int timing = 0;
   static constexpr int kRing = 64;
@@ -599,6 +604,86 @@ int run_serial(nsw6_handle* h, int lall, double* const* a, double dt) {
   return finish(h, launch_serial(P, h->C, x, h->stream));
 }
 
+// Host-memory arrays: the regions are independent, so the call runs in
+// chunks of regions over three streams, the copy-in of chunk j+1 and the
+// copy-out of chunk j-1 overlapping the step of chunk j (the H2D and D2H copy
+// engines and the SMs all busy).  Each chunk's step is the batched step on the
+// chunk's regions; the precipitation outputs ([2][lall][gall] in the caller's
+// layout) are staged per chunk as [2][chunk][gall] and copied back in two
+// pieces.  Returns after all copies are done.
+int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
+  const int K = h->kall, G = h->gall;
+  for (int i = 0; i < A_COUNT; ++i)
+    if ((arg_is_read(i) || arg_is_written(i)) && !args[i]) return NSW6_ERR_BAD_ARG;
+  if (h->opts.aerosol_indirect && !args[A_unccn]) return NSW6_ERR_BAD_ARG;
+  double* dev[A_COUNT];
+  int rc = ensure_stage(h, dev);
+  if (rc != NSW6_OK) return rc;
+  if (!h->s_in) {
+    if (cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+    h->ev_in = new cudaEvent_t[h->lall_max]();
+    h->ev_done = new cudaEvent_t[h->lall_max]();
+    for (int i = 0; i < h->lall_max; ++i)
+      if (cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming) != cudaSuccess)
+        return NSW6_ERR_CUDA;
+  }
+  // copies start after the work already queued on the handle's stream
+  if (cudaEventRecord(h->ev_start, h->stream) != cudaSuccess || cudaStreamWaitEvent(h->s_in, h->ev_start, 0) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  const int per = (lall + 4) / 5;   // regions per chunk: about five chunks
+  cudaError_t err = cudaSuccess;
+  int nchunk = 0;
+  for (int l0 = 0; l0 < lall && err == cudaSuccess; l0 += per, ++nchunk) {
+    const int nl = (lall - l0 < per) ? lall - l0 : per;
+    // chunk views: region l0 of every array (the precipitation outputs at
+    // their own [2][nl][gall] block of the staging)
+    double* cdev[A_COUNT];
+    double* chost[A_COUNT];
+    for (int i = 0; i < A_COUNT; ++i) {
+      const size_t e = arg_region_elems(i, K, G);
+      cdev[i] = dev[i] + e * (size_t)l0;
+      chost[i] = args[i] ? args[i] + ((i == A_precip || i == A_ISO1 || i == A_ISO2) ? (size_t)l0 * G : e * l0)
+                         : nullptr;
+    }
+    for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
+      if (!arg_is_read(i) && !(i == A_unccn && h->opts.aerosol_indirect)) continue;
+      err = cudaMemcpyAsync(cdev[i], chost[i], sizeof(double) * arg_region_elems(i, K, G) * nl,
+                            cudaMemcpyHostToDevice, h->s_in);
+    }
+    if (err != cudaSuccess) break;
+    if ((err = cudaEventRecord(h->ev_in[nchunk], h->s_in)) != cudaSuccess) break;
+    if ((err = cudaStreamWaitEvent(h->stream, h->ev_in[nchunk], 0)) != cudaSuccess) break;
+    Problem P;
+    rc = fill_problem(h, nl, cdev, dt, P);
+    if (rc != NSW6_OK) break;
+    if ((err = launch_step(P, h->C, h->stream, nullptr)) != cudaSuccess) break;
+    if ((err = cudaEventRecord(h->ev_done[nchunk], h->stream)) != cudaSuccess) break;
+    if ((err = cudaStreamWaitEvent(h->s_out, h->ev_done[nchunk], 0)) != cudaSuccess) break;
+    for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
+      if (!arg_is_written(i)) continue;
+      if (i == A_precip || i == A_ISO1 || i == A_ISO2) {
+        // [2][nl][G] staged -> rows 0 and 1 of the caller's [2][lall][G]
+        err = cudaMemcpyAsync(chost[i], cdev[i], sizeof(double) * nl * G, cudaMemcpyDeviceToHost, h->s_out);
+        if (err == cudaSuccess)
+          err = cudaMemcpyAsync(chost[i] + (size_t)lall * G, cdev[i] + (size_t)nl * G, sizeof(double) * nl * G,
+                                cudaMemcpyDeviceToHost, h->s_out);
+      } else {
+        err = cudaMemcpyAsync(chost[i], cdev[i], sizeof(double) * arg_region_elems(i, K, G) * nl,
+                              cudaMemcpyDeviceToHost, h->s_out);
+      }
+    }
+  }
+  const cudaError_t se = cudaStreamSynchronize(h->s_out);
+  const cudaError_t si = cudaStreamSynchronize(h->s_in);
+  if (rc != NSW6_OK) return rc;
+  if (err != cudaSuccess || se != cudaSuccess || si != cudaSuccess) return NSW6_ERR_CUDA;
+  return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
+}
+
 int run(nsw6_handle* h, int lall, double* const* a, double dt) {
   if (h->mixed == 2) return run_serial(h, lall, a, dt);
   Problem P;
@@ -668,6 +753,15 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_status);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
+  if (h->s_in) cudaStreamDestroy(h->s_in);
+  if (h->s_out) cudaStreamDestroy(h->s_out);
+  for (int i = 0; h->ev_in && i < h->lall_max; ++i) {
+    if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
+    if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
+  }
+  delete[] h->ev_in;
+  delete[] h->ev_done;
+  if (h->ev_start) cudaEventDestroy(h->ev_start);
   cudaFree(h->d_stage);
   cudaFree(h->d_dparam);
   cudaFree(h->d_pbar);
@@ -885,38 +979,7 @@ int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, dou
   (void)ct;
   if (!h || !args || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
   if (!host) return run(h, lall, args, dt);
-
-  const int K = h->kall, G = h->gall;
-  size_t need = 0;
-  for (int i = 0; i < A_COUNT; ++i) need += arg_region_elems(i, K, G) * (size_t)h->lall_max;
-  if (!h->d_stage) {
-    if (cudaMalloc(&h->d_stage, sizeof(double) * need) != cudaSuccess) return NSW6_ERR_CUDA;
-    h->stage_count = need;
-  }
-  double* dev[A_COUNT];
-  size_t offs = 0;
-  for (int i = 0; i < A_COUNT; ++i) {
-    dev[i] = h->d_stage + offs;
-    offs += arg_region_elems(i, K, G) * (size_t)h->lall_max;
-  }
-  for (int i = 0; i < A_COUNT; ++i) {
-    if ((arg_is_read(i) || arg_is_written(i)) && !args[i]) return NSW6_ERR_BAD_ARG;
-    if (!arg_is_read(i)) continue;
-    const size_t bytes = sizeof(double) * arg_region_elems(i, K, G) * (size_t)lall;
-    if (cudaMemcpyAsync(dev[i], args[i], bytes, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
-      return NSW6_ERR_CUDA;
-  }
-  Problem P;
-  int rc = fill_problem(h, lall, dev, dt, P);
-  if (rc != NSW6_OK) return rc;
-  if (launch_step(P, h->C, h->stream, next_events(h)) != cudaSuccess) return NSW6_ERR_CUDA;
-  for (int i = 0; i < A_COUNT; ++i) {
-    if (!arg_is_written(i)) continue;
-    const size_t bytes = sizeof(double) * arg_region_elems(i, K, G) * (size_t)lall;
-    if (cudaMemcpyAsync(args[i], dev[i], bytes, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
-      return NSW6_ERR_CUDA;
-  }
-  return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
+  return run_host(h, lall, args, dt);
 }
 
 int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int nsteps) {

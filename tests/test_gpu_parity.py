@@ -134,13 +134,16 @@ def test_gpu_batched_equals_per_region():
     drv.close()
 
 
-def test_gpu_host_entry_equals_device_entry():
-    """The host-memory entry point (copies inside the call) gives the device result."""
+@pytest.mark.parametrize("lall,lall_max", [(2, 2), (7, 8)])
+def test_gpu_host_entry_equals_device_entry(lall, lall_max):
+    """The host-memory entry point (copies inside the call, pipelined over
+    chunks of regions; 7 regions give chunks of 2, 2, 2 and 1) gives the
+    device result bit for bit."""
     torch = _torch()
     from nicam_kokkos_microphysics_gb300 import mp_init
-    spec = StateSpec(gall=300, kall=42, lall=2, seed=5, variant="standard")
+    spec = StateSpec(gall=300, kall=42, lall=lall, seed=5, variant="standard")
     st = make_state(spec, out_fill=np.nan)
-    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=2)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=lall_max)
     host = {n: st[n].copy() for n in ARG_NAMES}
     drv.run(host, dt=spec.dt)
     dev = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
