@@ -53,6 +53,10 @@ CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
 # 16900 x 42 region; traffic grows in proportion to cells.
 CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 215.5, "mixed": 172.9}
 COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 379.1, "mixed": 401.0}
+# FP64-pipe activity (fraction of active cycles) of each kernel in the same
+# captures: the hardware-level utilisation of the bound the kernels sit on.
+FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.842, "mixed": 0.747},
+                    "nsw6_column_kernel": {"fp64": 0.673, "mixed": 0.667}}
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (csrc/nsw6_probe.cu) and frozen here.
@@ -530,6 +534,10 @@ def main(argv=None) -> int:
                                "measured cost",
             "op_weights": OP_WEIGHTS,
             "op_weights_this_run": rates["weights"],
+            "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE[names[0]][args.precision],
+            "frac_note": "achieved counts the reference algorithm's FP64 work, so frac > 1 means the kernel does "
+                         "that work in less time than the FP64 pipe needs for it as written; the hardware "
+                         "utilisation is fp64_pipe_active_ncu",
             names[1]: other,
         })
         roofline.update({"work_per_unit": top.get("work_per_interior_cell", top.get("work_per_cell"))})

@@ -263,9 +263,13 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  *   on exit the adjoints of its inputs -- replaced for the arguments the step
  *   both reads and writes, added to for the arguments it only reads, zero for
  *   the arguments it only writes.  dparams[7] (host, may be NULL): the
- *   parameters' adjoint is added to it.  The tapes are sized by a first pass
- *   and kept in the handle (about 32 bytes per recorded operation for up to
- *   8192 columns at a time). */
+ *   parameters' adjoint is added to it.  Every cell is differentiated by its
+ *   own thread: the column phase in four level-parallel stages whose input
+ *   adjoints are added with atomics (so the last bits depend on their order),
+ *   the cell physics per cell.  The first call allocates the tapes and work
+ *   fields and keeps them in the handle: about 2.6 GB of stage tapes, 32 bytes
+ *   per recorded operation of the cell physics for 58,368 cells at a time,
+ *   and about 150 doubles per cell for lall_max regions. */
 int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
                   double dt, double ct);
 int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
