@@ -511,9 +511,86 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     }
     __syncthreads();
 
-    for (int f = 0; f < 6; ++f) {
-      if (MIX && f >= 4) {
-        // momentum fluxes in FP32
+    // flux source: q, e, phi, kin_h, u, v (mod_precip_transport.cpp:776-808)
+    auto source = [&](int f, int c) {
+      const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+      double r = 0.0;
+      if (g < G) {
+        const size_t i = off + (size_t)k * G + g;
+        const double b = F(S_BASE)[c];
+        switch (f) {
+          case 0: r = b; break;
+          case 1: r = b * CVDRY * P.tem[i]; break;
+          case 2: r = b * GRAV * P.z[i]; break;
+          case 3: r = q_n[i - off] * F(S_RGS)[c] * F(S_KINH)[c]; break;
+          case 4: r = b * F(S_VI)[c]; break;
+          default: r = b * F(S_VJ)[c]; break;
+        }
+      }
+      F(S_RHOF)[c] = r;
+    };
+    // flux divergence and surface fluxes (mod_precip_transport.cpp:782-842,
+    // 900-954); the quotients by dt are the correctly rounded ones, formed
+    // from 1/dt
+    auto divergence = [&](int f, int c) {
+      const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+      if (g >= G || k < kmin || k > kmax) return;
+      const double fk = F(S_F)[c], fk1 = F(S_F)[c + COL_TG];
+      const double d = (fk1 - fk) * rdgz[k];
+      switch (f) {
+        case 0:
+          F(dqs_slot)[c] = -d;
+          if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + div_rn(-fk, dt, P.rdt);
+          break;
+        case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - d; break;
+        case 2: F(S_DRHOPHI)[c] = F(S_DRHOPHI)[c] - d; break;
+        case 3: F(S_DKINH)[c] = F(S_DKINH)[c] - d; break;
+        case 4: F(S_DRHOGU)[c] = F(S_DRHOGU)[c] - d; break;
+        default: F(S_DRHOGV)[c] = F(S_DRHOGV)[c] - d; break;
+      }
+      if (k == kmin) {
+        double* acc = S.colacc;
+        const double fdt = div_rn(fk, dt, P.rdt);
+        switch (f) {
+          case 0:
+            if (nq == I_QR) {
+              acc[0 * COL_TG + gx] = acc[0 * COL_TG + gx] - fdt;
+            } else {
+              acc[1 * COL_TG + gx] = acc[1 * COL_TG + gx] - fdt;
+              acc[2 * COL_TG + gx] = acc[2 * COL_TG + gx] + div_rn(fk * LHF0, dt, P.rdt);
+            }
+            break;
+          case 1: acc[3 * COL_TG + gx] = acc[3 * COL_TG + gx] - fdt; break;
+          case 2: acc[4 * COL_TG + gx] = acc[4 * COL_TG + gx] - fdt; break;
+          case 3: acc[5 * COL_TG + gx] = acc[5 * COL_TG + gx] - fdt; break;
+          default: break;
+        }
+      }
+    };
+    // FP64 fluxes (the mixed step integrates the momentum fluxes in FP32
+    // below); the divergence of flux f and the source of flux f + 1 share a
+    // pass
+    const int nf = MIX ? 4 : 6;
+    for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
+    __syncthreads();
+    for (int f = 0; f < nf; ++f) {
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+        double fl = 0.0;
+        if (g < G && k >= kmin && k <= kmax)
+          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[(size_t)k * G + g], bmn_f[k], bmx_f[k]);
+        F(S_F)[c] = fl;
+      }
+      __syncthreads();
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+        divergence(f, c);
+        if (f + 1 < nf) source(f + 1, c);
+      }
+      __syncthreads();
+    }
+    if (MIX) {
+      // momentum fluxes in FP32
+      for (int f = 4; f < 6; ++f) {
         float* rf = FF(S_RHOF);
         float* ff = FF(S_F);
         float* acc = FF(f == 4 ? S_DRHOGU : S_DRHOGV);
@@ -539,71 +616,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
           acc[c] = acc[c] - (ff[c + COL_TG] - ff[c]) * rdgzf[k];
         }
         __syncthreads();
-        continue;
       }
-      // flux source: q, e, phi, kin_h, u, v (mod_precip_transport.cpp:776-808)
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-        double r = 0.0;
-        if (g < G) {
-          const size_t i = off + (size_t)k * G + g;
-          const double b = F(S_BASE)[c];
-          switch (f) {
-            case 0: r = b; break;
-            case 1: r = b * CVDRY * P.tem[i]; break;
-            case 2: r = b * GRAV * P.z[i]; break;
-            case 3: r = q_n[i - off] * F(S_RGS)[c] * F(S_KINH)[c]; break;
-            case 4: r = b * F(S_VI)[c]; break;
-            default: r = b * F(S_VJ)[c]; break;
-          }
-        }
-        F(S_RHOF)[c] = r;
-      }
-      __syncthreads();
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-        double fl = 0.0;
-        if (g < G && k >= kmin && k <= kmax)
-          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[(size_t)k * G + g], bmn_f[k], bmx_f[k]);
-        F(S_F)[c] = fl;
-      }
-      __syncthreads();
-      // flux divergence and surface fluxes (mod_precip_transport.cpp:782-842, 900-954)
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-        if (g >= G || k < kmin || k > kmax) continue;
-        const double fk = F(S_F)[c], fk1 = F(S_F)[c + COL_TG];
-        const double d = (fk1 - fk) * rdgz[k];
-        switch (f) {
-          case 0:
-            F(dqs_slot)[c] = -d;
-            if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + (-fk / dt);
-            break;
-          case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - d; break;
-          case 2: F(S_DRHOPHI)[c] = F(S_DRHOPHI)[c] - d; break;
-          case 3: F(S_DKINH)[c] = F(S_DKINH)[c] - d; break;
-          case 4: F(S_DRHOGU)[c] = F(S_DRHOGU)[c] - d; break;
-          default: F(S_DRHOGV)[c] = F(S_DRHOGV)[c] - d; break;
-        }
-        if (k == kmin) {
-          double* acc = S.colacc;
-          switch (f) {
-            case 0:
-              if (nq == I_QR) {
-                acc[0 * COL_TG + gx] = acc[0 * COL_TG + gx] - fk / dt;
-              } else {
-                acc[1 * COL_TG + gx] = acc[1 * COL_TG + gx] - fk / dt;
-                acc[2 * COL_TG + gx] = acc[2 * COL_TG + gx] + fk * LHF0 / dt;
-              }
-              break;
-            case 1: acc[3 * COL_TG + gx] = acc[3 * COL_TG + gx] - fk / dt; break;
-            case 2: acc[4 * COL_TG + gx] = acc[4 * COL_TG + gx] - fk / dt; break;
-            case 3: acc[5 * COL_TG + gx] = acc[5 * COL_TG + gx] - fk / dt; break;
-            default: break;
-          }
-        }
-      }
-      __syncthreads();
     }
 
     // half levels: departure cells and qh (mod_precip_transport.cpp:845-882)
@@ -755,22 +768,30 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
 
   // ---- KIN2EIN (mod_precip_transport.cpp:991-1011): tmp2 and the vertical
   //      kinetic energy of the updated state
+  //      (and, in the reference configuration's kernel, the metric factors
+  //      W2Cfact of each interior cell for the final pass, in the dead slots
+  //      S_DRHOGW / S_DRHOGV, read after rw)
   for (int c = threadIdx.x; c < ncell && !kin2kin; c += blockDim.x) {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     F(S_DRHOE)[c] = 0.0;
     F(S_DRHOPHI)[c] = 0.0;
     if (g >= G) continue;
     const size_t i = off + (size_t)k * G + g;
+    const bool hk = (k >= kmin + 1 && k <= kmax);
+    const double rw = hk ? (MIX ? P.rhogw[i] : F(S_DRHOGW)[c]) : 0.0;
     if (k >= kmin && k <= kmax) {
       const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
       const double w2c0 = div_rn(cfact[k] * P.gsgam2[i], gh, rgh);
       const double w2c1 = div_rn(dfact[k] * P.gsgam2[i], gh, rgh);
       F(S_DRHOE)[c] = F(S_KINH)[c] + (w2c0 * F(S_KINV)[c + COL_TG] + w2c1 * F(S_KINV)[c]);
+      if (!OPT) {
+        F(S_DRHOGW)[c] = w2c0;
+        F(S_DRHOGV)[c] = w2c1;
+      }
     }
-    if (k >= kmin + 1 && k <= kmax) {
+    if (hk) {
       const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
       const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
-      const double rw = MIX ? P.rhogw[i] : F(S_DRHOGW)[c];
       F(S_DRHOPHI)[c] = 0.5 * (rw * rw) / (c2w0 * F(S_RHOF)[c] + c2w1 * F(S_RHOF)[c - COL_TG]);
     }
   }
@@ -805,9 +826,15 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     if (interior && !kin2kin) {
       const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
       const double tmp_h = div_rn(0.5 * (rvx * rvx + rvy * rvy + rvz * rvz), rhog, rrhog);
-      const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
-      const double w2c0 = div_rn(cfact[k] * P.gsgam2[i], gh, rgh);
-      const double w2c1 = div_rn(dfact[k] * P.gsgam2[i], gh, rgh);
+      double w2c0, w2c1;
+      if (!OPT) {
+        w2c0 = F(S_DRHOGW)[c];
+        w2c1 = F(S_DRHOGV)[c];
+      } else {
+        const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
+        w2c0 = div_rn(cfact[k] * P.gsgam2[i], gh, rgh);
+        w2c1 = div_rn(dfact[k] * P.gsgam2[i], gh, rgh);
+      }
       const double tmp = tmp_h + (w2c0 * F(S_DRHOPHI)[c + COL_TG] + w2c1 * F(S_DRHOPHI)[c]);
       rhoge = rhoge + (F(S_DRHOE)[c] - tmp);
     }
