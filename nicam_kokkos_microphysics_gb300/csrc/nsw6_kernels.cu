@@ -455,9 +455,19 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     S.bmax[c] = bmx;
   }
 
+  // Per-thread values of the half-level metric factors, kept in registers
+  // across the passes: every pass gives a thread the same cells
+  // c = threadIdx.x + j blockDim.x, j < NJ (NJ covers column_threads()).
+  constexpr int NJ = COL_TG == 16 ? 4 : 5;
+  double r_rgsh[NJ], r_c2w0[NJ], r_c2w1[NJ];   // gam2h / gsgam2h and C2Wfact at half level k
+
   // ---- metric factors, kinetic energy, zeroed accumulators
   //      (mod_precip_transport.cpp:715-770, cnvvar_rhogkin_in mod_debug.cpp:269-330)
-  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int c = threadIdx.x + j * blockDim.x;
+    r_rgsh[j] = r_c2w0[j] = r_c2w1[j] = 0.0;
+    if (c >= ncell) continue;
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     for (int s = S_KINH; s <= S_DQG; ++s) F(s)[c] = 0.0;
     if (OPT) F(S_DQI)[c] = 0.0;
@@ -481,6 +491,9 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
       const double rw = P.rhogw[i];
       F(S_KINV)[c] = 0.5 * (rw * rw) / (c2w0 * P.rhog[i] + c2w1 * P.rhog[i - G]);
+      r_c2w0[j] = c2w0;
+      r_c2w1[j] = c2w1;
+      r_rgsh[j] = P.gam2h[i] / P.gsgam2h[i];
     }
   }
   __syncthreads();
@@ -620,12 +633,15 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     }
 
     // half levels: departure cells and qh (mod_precip_transport.cpp:845-882)
-    for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      const int c = threadIdx.x + j * blockDim.x;
+      if (c >= ncell) continue;
       const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
       double qh = 0.0;
       if (g < G && k >= kmin + 1 && k <= kmax) {
         const size_t i = off + (size_t)k * G + g;
-        qh = 0.5 * (q_n[i - off] + q_n[i - off - G]) * (P.gam2h[i] / P.gsgam2h[i]);
+        qh = 0.5 * (q_n[i - off] + q_n[i - off - G]) * r_rgsh[j];
         S.kc[c] = (unsigned char)departure_cell(gzs, zkey + K, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
       }
       F(S_BASE)[c] = qh;
@@ -771,7 +787,10 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   //      (and, in the reference configuration's kernel, the metric factors
   //      W2Cfact of each interior cell for the final pass, in the dead slots
   //      S_DRHOGW / S_DRHOGV, read after rw)
-  for (int c = threadIdx.x; c < ncell && !kin2kin; c += blockDim.x) {
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int c = threadIdx.x + j * blockDim.x;
+    if (c >= ncell || kin2kin) continue;
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     F(S_DRHOE)[c] = 0.0;
     F(S_DRHOPHI)[c] = 0.0;
@@ -789,11 +808,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         F(S_DRHOGV)[c] = w2c1;
       }
     }
-    if (hk) {
-      const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
-      const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
-      F(S_DRHOPHI)[c] = 0.5 * (rw * rw) / (c2w0 * F(S_RHOF)[c] + c2w1 * F(S_RHOF)[c - COL_TG]);
-    }
+    if (hk) F(S_DRHOPHI)[c] = 0.5 * (rw * rw) / (r_c2w0[j] * F(S_RHOF)[c] + r_c2w1[j] * F(S_RHOF)[c - COL_TG]);
   }
   __syncthreads();
 
@@ -1219,6 +1234,8 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   const int tg = column_tile(P.kall);
   dim3 g2((P.gall + tg - 1) / tg, P.lall);
   const int nt = column_threads(P.kall);
+  // every thread of the column kernel keeps at most 4 (tile 16) or 5 (tile 8) cells
+  if ((size_t)nt * (tg == 16 ? 4 : 5) < (size_t)P.kall * tg) return cudaErrorInvalidConfiguration;
   if (tg == 16) {
     if (opt) nsw6_column_kernel<16, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.mixed) nsw6_column_kernel<16, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
