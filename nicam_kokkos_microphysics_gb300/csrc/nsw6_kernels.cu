@@ -868,16 +868,21 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     double qd = 1.0;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) qd = qd - q[n];
-    // THRMDYN_tempre, mod_thrmdyn.cpp:137-180
-    double cvt = 0.0, qdl = 1.0;
+    // THRMDYN_tempre, mod_thrmdyn.cpp:137-180.  Its temperature is replaced
+    // by the saturation adjustment's everywhere and its pressure by the
+    // negative filter's at interior levels: only the halo levels output it.
+    double pre = 0.0;
+    if (!interior) {
+      double cvt = 0.0, qdl = 1.0;
 #pragma unroll
-    for (int n = 1; n <= 5; ++n) {
-      cvt = cvt + q[n] * CVDRY;
-      qdl = qdl - q[n];
+      for (int n = 1; n <= 5; ++n) {
+        cvt = cvt + q[n] * CVDRY;
+        qdl = qdl - q[n];
+      }
+      cvt = cvt + qdl * CVDRY;
+      const double tem0 = ein / cvt;
+      pre = rho * tem0 * (qdl * RDRY + q[I_QV] * RVAP);
     }
-    cvt = cvt + qdl * CVDRY;
-    double tem = ein / cvt;
-    double pre = rho * tem * (qdl * RDRY + q[I_QV] * RVAP);
 
     // SATURATION_adjustment (mod_satadjust.cpp:274-362): ice_adjust = false,
     // or true with the switch (cloud ice joins the adjustment)
@@ -896,9 +901,8 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
 #pragma unroll
     for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
     const double rho_l = rho;
-    tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
+    double tem = mode == 1 ? tres : (ein_moist - q[I_QV] * LHV0) / cvtot;
     if (mode == 1) {
-      tem = tres;
       q[I_QV] = qvres;
       q[I_QC] = qcres;
       if (ice_adj) q[I_QI] = qires;
@@ -935,10 +939,12 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     rq[I_QV] = rhog * q[I_QV];
     rq[I_QC] = rhog * q[I_QC];
     if (ice_adj) rq[I_QI] = rhog * q[I_QI];
-    cvtot = qd * CVDRY;
+    if (!interior) {   // interior levels: rhoge comes from the negative filter below
+      cvtot = qd * CVDRY;
 #pragma unroll
-    for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
-    rhoge = rhog * tem * cvtot;
+      for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+      rhoge = rhog * tem * cvtot;
+    }
 
     // negative_filter (mod_mp_nsw6.cpp:1770-1831), interior levels
     double rhog_o = rhog;
