@@ -478,7 +478,9 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     const size_t i = off + (size_t)k * G + g;
     const size_t ic = (size_t)l * G + g;
     const bool interior = (k >= kmin && k <= kmax);
-    if (interior) F(S_RGS)[c] = P.gam2[i] / P.gsgam2[i];
+    // gam2 / gsgam2 and afact / gsgam2 from one reciprocal, correctly rounded
+    const double rgsg = 1.0 / P.gsgam2[i];
+    if (interior) F(S_RGS)[c] = div_rn(P.gam2[i], P.gsgam2[i], rgsg);
     const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
     F(S_VI)[c] = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
     F(S_VJ)[c] = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
@@ -487,7 +489,7 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
       F(S_KINH)[c] = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / P.rhog[i];
     }
     if (k >= kmin + 1 && k <= kmax) {
-      const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
+      const double c2w0 = div_rn(afact[k], P.gsgam2[i], rgsg) * P.gsgam2h[i];
       const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
       const double rw = P.rhogw[i];
       F(S_KINV)[c] = 0.5 * (rw * rw) / (c2w0 * P.rhog[i] + c2w1 * P.rhog[i - G]);
