@@ -908,7 +908,7 @@ size_t adj_stage_work_doubles(int lall, int kall, int gall) {
 }
 size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 6 * kall; }
 int adj_stage_tape_cap() { return 512; }
-int adj_stage_slots() { return 152 * 8 * STAGE_THREADS; }
+int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
 
 // The column phase's adjoint: its forward S1..S3 from the state x and the cell
 // phase's outputs Y (S1 also forms the region extrema of the departure
