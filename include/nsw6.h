@@ -272,6 +272,12 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  *   and about 150 doubles per cell for lall_max regions. */
 int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
                   double dt, double ct);
+
+/* Implementation of the cell physics' adjoint inside mp_driver_adjoint: 0
+ * (default) the hand-written reverse sweep (no tape); 1 the operations
+ * recorded on a per-cell tape and swept back (the operator-overloading form,
+ * for checking the hand-written one). */
+int nsw6_set_adjoint_mode(nsw6_handle* h, int mode);
 int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
                       double dt, double ct);
 

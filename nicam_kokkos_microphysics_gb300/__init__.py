@@ -160,6 +160,12 @@ class MPDriver:
         m = {"fp64": 0, "mixed": 1, "serial": 2}.get(mode, mode) if isinstance(mode, str) else int(mode)
         _check(self._lib.nsw6_set_precision(self._h, int(m)), self._lib)
 
+    def set_adjoint_mode(self, mode: int | str) -> None:
+        """Cell-physics adjoint of ``adjoint``: 0 / "hand" the hand-written
+        reverse sweep (default), 1 / "tape" the recorded operations."""
+        m = {"hand": 0, "tape": 1}.get(mode, mode) if isinstance(mode, str) else int(mode)
+        _check(self._lib.nsw6_set_adjoint_mode(self._h, int(m)), self._lib)
+
     def set_math(self, mode: int) -> None:
         """0: table-driven exp/log/pow (default), 1: CUDA math library."""
         _check(self._lib.nsw6_set_math(self._h, int(mode)), self._lib)

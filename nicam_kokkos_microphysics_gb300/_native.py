@@ -120,6 +120,7 @@ def load() -> ctypes.CDLL:
     lib.mp_driver_batched.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.mp_driver_mixed.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.nsw6_set_precision.argtypes = [vp, c_int]
+    lib.nsw6_set_adjoint_mode.argtypes = [vp, c_int]
     lib.nsw6_default_options.argtypes = [vp]
     lib.nsw6_default_options.restype = None
     lib.nsw6_set_options.argtypes = [vp, vp]

@@ -34,6 +34,7 @@
 #include <cfloat>
 #include <cuda_runtime.h>
 
+#include "nsw6_cell_adjoint.cuh"
 #include "nsw6_column_step.cuh"
 
 namespace nsw6 {
@@ -899,6 +900,63 @@ __global__ void adj_seed_columns_kernel(StageIO io) {
   }
 }
 
+// The cell phase's adjoint, hand-written (nsw6_cell_adjoint.cuh): one thread
+// per interior cell; output adjoints from YB, input adjoints added to xb (each
+// cell owns its entries here), the parameters' adjoint reduced per block.
+__global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb, const double* YB,
+                                                          double* pbar) {
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  __shared__ double red[7][128];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  __syncthreads();
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const LayS L{P.kall, P.gall, P.lall};
+  const size_t NC = (size_t)P.lall * P.kall * P.gall;
+  const int nint = P.kmax - P.kmin + 1;
+  const long long ncell = (long long)P.lall * nint * P.gall;
+  double pacc[7] = {0, 0, 0, 0, 0, 0, 0};
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(c % P.gall);
+    const int k = P.kmin + (int)((c / P.gall) % nint);
+    const int l = (int)(c / ((long long)P.gall * nint));
+    const size_t i = L.f(l, k, g);
+    CellIn in;
+    in.rhog = x.a[A_rhog][i];
+    in.tem = x.a[A_tem][i];
+    in.gsgam2 = x.a[A_gsgam2][i];
+    in.q0 = x.a[A_q][L.t(l, 0, k, g)];
+    for (int n = 0; n < 6; ++n) in.rhogq[n] = x.a[A_rhogq][L.t(l, n, k, g)];
+    CellBar ob;
+    ob.rhog = YB[YS_RHOG * NC + i];
+    ob.rhoge = YB[YS_RHOGE * NC + i];
+    ob.tem = YB[YS_TEM * NC + i];
+    for (int n = 0; n < 6; ++n) ob.rhogq[n] = YB[(YS_RHOGQ + n) * NC + i];
+    ob.q[0] = 0.0;
+    for (int n = 1; n < 6; ++n) ob.q[n] = YB[(YS_Q + n - 1) * NC + i];
+    ob.Vtr = YB[(YS_VT + 0) * NC + i];
+    ob.Vts = YB[(YS_VT + 1) * NC + i];
+    ob.Vtg = YB[(YS_VT + 2) * NC + i];
+    ob.rceff = YB[YS_RE * NC + i];
+    ob.rceff_cld = YB[YS_RECLD * NC + i];
+    ob.rctop = k == P.kmax ? YB[YS_RCTOP * NC + i] : 0.0;
+    ob.tctop = k == P.kmax ? YB[YS_TCTOP * NC + i] : 0.0;
+    CellInBar ib{};
+    nsw6_cell_adjoint(C, fm, P.dt, P.rdt, in, ob, ib, pacc);
+    xb.a[A_rhog][i] += ib.rhog;
+    xb.a[A_tem][i] += ib.tem;
+    xb.a[A_gsgam2][i] += ib.gsgam2;
+    xb.a[A_q][L.t(l, 0, k, g)] += ib.q0;
+    for (int n = 0; n < 6; ++n) xb.a[A_rhogq][L.t(l, n, k, g)] += ib.rhogq[n];
+  }
+  for (int j = 0; j < 7; ++j) red[j][threadIdx.x] = pacc[j];
+  __syncthreads();
+  if (threadIdx.x < 7) {
+    double sum = 0.0;
+    for (int j = 0; j < (int)blockDim.x; ++j) sum += red[threadIdx.x][j];
+    atomicAdd(&pbar[threadIdx.x], sum);
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
@@ -909,6 +967,12 @@ size_t adj_stage_work_doubles(int lall, int kall, int gall) {
 size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 6 * kall; }
 int adj_stage_tape_cap() { return 512; }
 int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
+
+cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
+                               double* pbar, cudaStream_t stream) {
+  adj_cell_hw_kernel<<<152 * 2, 128, 0, stream>>>(P, C, x, xb, YB, pbar);
+  return cudaGetLastError();
+}
 
 // The column phase's adjoint: its forward S1..S3 from the state x and the cell
 // phase's outputs Y (S1 also forms the region extrema of the departure

@@ -31,6 +31,8 @@ cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x,
 cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
                                      cudaStream_t stream);
+cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
+                               double* pbar, cudaStream_t stream);
 size_t adj_stage_work_doubles(int lall, int kall, int gall);
 size_t adj_stage_bound_ints(int lall, int kall);
 int adj_stage_tape_cap();
@@ -73,6 +75,7 @@ struct nsw6_handle {
   double* d_swork = nullptr;   // work fields, their adjoints and the seeds of the staged column adjoint
   int* d_sbnd = nullptr;       // flux bounds of the staged column adjoint
   int* d_done = nullptr;       // per-cell flags of the cell adjoint
+  int adj_mode = 0;            // cell-phase adjoint: 0 hand-written, 1 recorded tape
   double* d_Y = nullptr;   // cell-phase outputs and their adjoints [2][nfields][lall_max][kall][gall]
   // captured step graph of mp_driver_steps and what it was captured for
   cudaStream_t cap_stream = nullptr;
@@ -846,6 +849,12 @@ int nsw6_set_math(nsw6_handle* h, int mode) {
   return NSW6_OK;
 }
 
+int nsw6_set_adjoint_mode(nsw6_handle* h, int mode) {
+  if (!h || mode < 0 || mode > 1) return NSW6_ERR_BAD_ARG;
+  h->adj_mode = mode;
+  return NSW6_OK;
+}
+
 int nsw6_set_precision(nsw6_handle* h, int mode) {
   if (!h || mode < 0 || mode > 2) return NSW6_ERR_BAD_ARG;
   h->mixed = mode;
@@ -1129,36 +1138,40 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
       cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess)
     return NSW6_ERR_CUDA;
-  // the cell phase's adjoint: a tape as long as the longest cell's record
-  // (measured once, then kept; a longer record makes the launch repeat for the
-  // cells that did not fit)
-  for (int attempt = 0; attempt < 3; ++attempt) {
-    if (!h->ctape.pa || attempt > 0) {
-      int tcell = 0;
-      TapeMem cnt{};
-      cnt.count_only = 1;
-      cnt.nslot = ncell_slots;
+  // the cell phase's adjoint: hand-written, or (adj_mode 1) recorded on a tape
+  // as long as the longest cell's record (measured once, then kept; a longer
+  // record makes the launch repeat for the cells that did not fit)
+  if (h->adj_mode == 0) {
+    if (launch_adj_cell_hw(P, h->C, x, xb, YB, h->d_pbar, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  } else {
+    for (int attempt = 0; attempt < 3; ++attempt) {
+      if (!h->ctape.pa || attempt > 0) {
+        int tcell = 0;
+        TapeMem cnt{};
+        cnt.count_only = 1;
+        cnt.nslot = ncell_slots;
+        if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
+            launch_adj_cell(P, h->C, x, xb, YB, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->d_done, h->stream) !=
+                cudaSuccess ||
+            cudaMemcpyAsync(&tcell, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+            cudaStreamSynchronize(h->stream) != cudaSuccess)
+          return NSW6_ERR_CUDA;
+        if ((rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, tcell + tcell / 4 + 64)) != NSW6_OK) return rc;
+      }
+      h->ctape.count_only = 0;
+      if (h->ctape.nslot != ncell_slots &&
+          (rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, h->ctape.cap)) != NSW6_OK)
+        return rc;
+      int t2 = 0;
       if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-          launch_adj_cell(P, h->C, x, xb, YB, cnt, h->d_dparam, h->d_pbar, h->d_tmax, h->d_done, h->stream) !=
+          launch_adj_cell(P, h->C, x, xb, YB, h->ctape, h->d_dparam, h->d_pbar, h->d_tmax, h->d_done, h->stream) !=
               cudaSuccess ||
-          cudaMemcpyAsync(&tcell, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+          cudaMemcpyAsync(&t2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
           cudaStreamSynchronize(h->stream) != cudaSuccess)
         return NSW6_ERR_CUDA;
-      if ((rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, tcell + tcell / 4 + 64)) != NSW6_OK) return rc;
+      if (t2 <= h->ctape.cap) break;
+      if (attempt == 2) return NSW6_ERR_UNSUPPORTED;
     }
-    h->ctape.count_only = 0;
-    if (h->ctape.nslot != ncell_slots &&
-        (rc = ensure_tape(h->ctape, h->ctape_bytes, ncell_slots, h->ctape.cap)) != NSW6_OK)
-      return rc;
-    int t2 = 0;
-    if (cudaMemsetAsync(h->d_tmax, 0, sizeof(int), h->stream) != cudaSuccess ||
-        launch_adj_cell(P, h->C, x, xb, YB, h->ctape, h->d_dparam, h->d_pbar, h->d_tmax, h->d_done, h->stream) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(&t2, h->d_tmax, sizeof(int), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-        cudaStreamSynchronize(h->stream) != cudaSuccess)
-      return NSW6_ERR_CUDA;
-    if (t2 <= h->ctape.cap) break;
-    if (attempt == 2) return NSW6_ERR_UNSUPPORTED;
   }
   if (cudaMemcpyAsync(pb, h->d_pbar, sizeof(double) * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
       cudaStreamSynchronize(h->stream) != cudaSuccess)
