@@ -744,38 +744,138 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Const
   }
 }
 
-// Adjoint of S3: seeds from S4's adjoints (WB) and the caller's output
-// adjoints of rhogvx/y/z, rhogw, GPREC and the surface outputs.
-__global__ void __launch_bounds__(STAGE_THREADS) adj_s3_kernel(StageIO io, TapeMem tm) {
-  __shared__ double grid[GF_COUNT * MAX_KALL];
-  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
-  __syncthreads();
-  tape_bind_s(tm);
-  LeafLog lg;
-  const double* SC = io.SB + (size_t)NSF * io.NC;   // [NSC][lall][gall]
+// Adjoint of S3, hand-written.  S3 is linear in the fluxes and tendencies, so
+// the adjoints of the divergences at a level follow from that level's output
+// adjoints alone; every cell rebuilds them for itself and its neighbours and
+// gathers the adjoint of each of its 24 fluxes (no atomics; written, not
+// added: S3 is their only reader).  The other input adjoints are the cell's
+// own, added where they live; the unit vectors, shared by a column, atomically.
+struct S3Bar {
+  double dq[3], drhoe, drhophi, dkinh, du, dv, dkinv, dw;
+};
+__device__ __forceinline__ S3Bar s3_bars(const StageIO& io, int l, int k, int g) {
+  const size_t c = io.L.f(l, k, g), NC = io.NC;
+  const double B_rhog = io.WB[W_RHOG_N * NC + c], B_rhoge = io.WB[W_RHOGE_N * NC + c];
+  const double B_rvx = io.WB[W_RVX_N * NC + c] + io.SB[SF_RVX * NC + c];
+  const double B_rvy = io.WB[W_RVY_N * NC + c] + io.SB[SF_RVY * NC + c];
+  const double B_rvz = io.WB[W_RVZ_N * NC + c] + io.SB[SF_RVZ * NC + c];
+  const double B_rw = io.WB[W_RW_N * NC + c] + io.SB[SF_RW * NC + c];
+  const size_t ic = io.L.c(l, g);
+  const double z = io.x.a[A_z][c];
+  S3Bar b;
+  const int tr[3] = {I_QR, I_QS, I_QG};
+  for (int t = 0; t < 3; ++t) b.dq[t] = io.WB[(W_RQ_N + tr[t]) * NC + c] + B_rhog - B_rhoge * GRAV * z;
+  b.drhoe = B_rhoge;
+  b.drhophi = B_rhoge;
+  b.dkinh = io.WB[W_KINH_N * NC + c];
+  b.dkinv = io.WB[W_KINV_N * NC + c];
+  b.du = B_rvx * io.x.a[A_ix][ic] + B_rvy * io.x.a[A_iy][ic] + B_rvz * io.x.a[A_iz][ic];
+  b.dv = B_rvx * io.x.a[A_jx][ic] + B_rvy * io.x.a[A_jy][ic] + B_rvz * io.x.a[A_jz][ic];
+  b.dw = B_rw;
+  return b;
+}
+// adjoint of the divergence d_tf (full f < 6, half 6..7) at a level, from its S3Bar
+__device__ __forceinline__ double s3_bd(const S3Bar& b, int t, int f) {
+  switch (f) {
+    case 0: return -b.dq[t];
+    case 1: return -b.drhoe;
+    case 2: return -b.drhophi;
+    case 3: return -b.dkinh;
+    case 4: return -b.du;
+    case 5: return -b.dv;
+    case 6: return -b.dkinv;
+    default: return -b.dw;
+  }
+}
+
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s3_hw_kernel(StageIO io) {
+  const Problem& P = io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const double* rdgz = P.grid + GF_RDGZ * K;
+  const double* rdgzh = P.grid + GF_RDGZH * K;
+  const double* SC = io.SB + (size_t)NSF * io.NC;
   const size_t ncol = (size_t)io.L.lall * io.L.G;
-  for (size_t c = tape().slot; c < io.NC; c += tape().nslot) {
+  const double dt = P.dt;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
     const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
-    tape_begin(lg);
-    const In<RVar> in{io, l, g, &lg};
-    RVar wo[NWF - W_RHOG_N];
-    RVar fo[NSF];
-    RVar co[NSC];
-    stage3<RVar>(
-        in, grid, k, [&](int f, const RVar& v) { wo[f - W_RHOG_N] = v; }, [&](int f, const RVar& v) { fo[f] = v; },
-        [&](int f, const RVar& v) { co[f] = v; });
-    if (stage_overflow(io, lg, k, g, l)) continue;
-    tape_clear_adj();
-    for (int f = W_RHOG_N; f < NWF; ++f) seed(wo[f - W_RHOG_N], io.WB[f * io.NC + c]);
-    seed(fo[SF_RVX], io.SB[SF_RVX * io.NC + c]);
-    seed(fo[SF_RVY], io.SB[SF_RVY * io.NC + c]);
-    seed(fo[SF_RVZ], io.SB[SF_RVZ * io.NC + c]);
-    seed(fo[SF_RW], io.SB[SF_RW * io.NC + c]);
-    if (k >= io.P.kmin && k <= io.P.kmax) seed(fo[SF_GPREC], io.SB[SF_GPREC * io.NC + c]);
-    if (k == io.P.kmin)
-      for (int f = 0; f < NSC; ++f) seed(co[f], SC[f * ncol + io.L.c(l, g)]);
-    tape_reverse();
-    scatter(io, lg);
+    const bool in_k = (k >= kmin && k <= kmax), in_km = (k - 1 >= kmin && k - 1 <= kmax);
+    const bool hk = (k >= kmin + 1 && k <= kmax), hkp = (k + 1 >= kmin + 1 && k + 1 <= kmax);
+    const S3Bar b0 = s3_bars(io, l, k, g);
+    S3Bar bm{}, bp{};
+    if (in_km) bm = s3_bars(io, l, k - 1, g);
+    if (hkp) bp = s3_bars(io, l, k + 1, g);
+    // flux adjoints
+    for (int t = 0; t < 3; ++t) {
+      for (int f = 0; f < 6; ++f) {
+        double bF = 0.0;
+        if (in_km) bF += s3_bd(bm, t, f) * rdgz[k - 1];
+        if (in_k) bF -= s3_bd(b0, t, f) * rdgz[k];
+        io.WB[(W_F + 8 * t + f) * io.NC + c] = bF;
+      }
+      for (int f = 6; f < 8; ++f) {
+        double bF = 0.0;
+        if (hk) bF += s3_bd(b0, t, f) * rdgzh[k];
+        if (hkp) bF -= s3_bd(bp, t, f) * rdgzh[k + 1];
+        io.WB[(W_F + 8 * t + f) * io.NC + c] = bF;
+      }
+    }
+    // GPREC = 0 + (-F_QR,q(k)) / dt at interior levels; the surface outputs at kmin
+    if (in_k) io.WB[(W_F + 0) * io.NC + c] -= io.SB[SF_GPREC * io.NC + c] / dt;
+    if (k == kmin) {
+      const size_t ic = io.L.c(l, g);
+      const double bp0 = SC[SC_PRECIP0 * ncol + ic], bp1 = SC[SC_PRECIP1 * ncol + ic];
+      const double blh = SC[SC_LH * ncol + ic], bre = SC[SC_RHOE * ncol + ic];
+      const double bph = SC[SC_RHOPHI * ncol + ic], bkn = SC[SC_RHOKIN * ncol + ic];
+      double* F = io.WB + (size_t)W_F * io.NC + c;
+      F[(8 * 0 + 0) * io.NC] -= bp0 / dt;
+      for (int t = 1; t < 3; ++t) F[(8 * t + 0) * io.NC] += -bp1 / dt + blh * LHF0 / dt;
+      for (int t = 0; t < 3; ++t) {
+        F[(8 * t + 1) * io.NC] -= bre / dt;
+        F[(8 * t + 2) * io.NC] -= bph / dt;
+        F[(8 * t + 3) * io.NC] -= bkn / dt;
+      }
+    }
+    // the cell's own inputs
+    const size_t NC = io.NC;
+    const double B_rhog = io.WB[W_RHOG_N * NC + c], B_rhoge = io.WB[W_RHOGE_N * NC + c];
+    const double B_rvx = io.WB[W_RVX_N * NC + c] + io.SB[SF_RVX * NC + c];
+    const double B_rvy = io.WB[W_RVY_N * NC + c] + io.SB[SF_RVY * NC + c];
+    const double B_rvz = io.WB[W_RVZ_N * NC + c] + io.SB[SF_RVZ * NC + c];
+    const double B_rw = io.WB[W_RW_N * NC + c] + io.SB[SF_RW * NC + c];
+    if (in_k) {
+      io.YB[YS_RHOG * NC + c] += B_rhog;
+      io.YB[YS_RHOGE * NC + c] += B_rhoge;
+      for (int n = 0; n < 6; ++n) io.YB[(YS_RHOGQ + n) * NC + c] += io.WB[(W_RQ_N + n) * NC + c];
+    } else {
+      io.xb.a[A_rhog][c] += B_rhog;
+      io.xb.a[A_rhoge][c] += B_rhoge;
+      for (int n = 0; n < 6; ++n) io.xb.a[A_rhogq][io.L.t(l, n, k, g)] += io.WB[(W_RQ_N + n) * NC + c];
+    }
+    io.xb.a[A_rhogvx][c] += B_rvx;
+    io.xb.a[A_rhogvy][c] += B_rvy;
+    io.xb.a[A_rhogvz][c] += B_rvz;
+    io.xb.a[A_rhogw][c] += B_rw;
+    io.WB[W_KINH * NC + c] = io.WB[W_KINH_N * NC + c];
+    io.WB[W_KINV * NC + c] = io.WB[W_KINV_N * NC + c];
+    if (in_k) {
+      // the tendencies at this level (forward values) for the products with z and the unit vectors
+      const double* Fw = io.W + (size_t)W_F * NC + c;
+      double dq[3], du = 0.0, dv = 0.0;
+      for (int t = 0; t < 3; ++t) {
+        dq[t] = -((Fw[(8 * t + 0) * NC + io.L.G] - Fw[(8 * t + 0) * NC]) * rdgz[k]);
+        du = du - (Fw[(8 * t + 4) * NC + io.L.G] - Fw[(8 * t + 4) * NC]) * rdgz[k];
+        dv = dv - (Fw[(8 * t + 5) * NC + io.L.G] - Fw[(8 * t + 5) * NC]) * rdgz[k];
+      }
+      const double bz = -B_rhoge * GRAV * (dq[0] + dq[1] + dq[2]);
+      io.xb.a[A_z][c] += bz;
+      const size_t ic = io.L.c(l, g);
+      atomicAdd(&io.xb.a[A_ix][ic], B_rvx * du);
+      atomicAdd(&io.xb.a[A_iy][ic], B_rvy * du);
+      atomicAdd(&io.xb.a[A_iz][ic], B_rvz * du);
+      atomicAdd(&io.xb.a[A_jx][ic], B_rvx * dv);
+      atomicAdd(&io.xb.a[A_jy][ic], B_rvy * dv);
+      atomicAdd(&io.xb.a[A_jz][ic], B_rvz * dv);
+    }
   }
 }
 
@@ -1009,7 +1109,7 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   adj_seed_kernel<<<152 * 4, 256, 0, stream>>>(io);
   adj_seed_columns_kernel<<<64, 256, 0, stream>>>(io);
   adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
-  adj_s3_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  adj_s3_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
   adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
   return cudaGetLastError();
