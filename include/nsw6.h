@@ -273,10 +273,12 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
 int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
                   double dt, double ct);
 
-/* Implementation of the cell physics' adjoint inside mp_driver_adjoint: 0
- * (default) the hand-written reverse sweep (no tape); 1 the operations
- * recorded on a per-cell tape and swept back (the operator-overloading form,
- * for checking the hand-written one). */
+/* Implementation of the adjoints of the cell physics and of the column
+ * phase's last stage (KIN2EIN, thermodynamics, saturation adjustment,
+ * negative filter) inside mp_driver_adjoint: 0 (default) the hand-written
+ * reverse sweeps (no tape); 1 the operations recorded on per-cell tapes and
+ * swept back (the operator-overloading form, for checking the hand-written
+ * ones). */
 int nsw6_set_adjoint_mode(nsw6_handle* h, int mode);
 int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
                       double dt, double ct);

@@ -744,6 +744,391 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Const
   }
 }
 
+// Adjoint of S4, hand-written: the cell's forward (KIN2EIN, thermodynamics,
+// saturation adjustment, negative filter) recomputed as stage4 does, then the
+// reverse sweep.  The Newton temperature is differentiated implicitly at its
+// converged value as satadjust_t does: with F(T) = T cv(T) + qsat(T) LHV0 -
+// Emoist, dT = -dF / F_T at the last iterate.  Adjoints go to S3's outputs at
+// this level and its neighbours and to the metric factors, atomically.
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Consts C) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  stage_smem(io.P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const Problem& P = io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const double* afact = grid + GF_AFACT * K;
+  const double* bfact = grid + GF_BFACT * K;
+  const double* cfact = grid + GF_CFACT * K;
+  const double* dfact = grid + GF_DFACT * K;
+  const size_t NC = io.NC;
+  const size_t G = io.L.G;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    const bool interior = (k >= kmin && k <= kmax);
+    auto W = [&](int f, size_t cc) { return io.W[f * NC + cc]; };
+    auto WBadd = [&](int f, size_t cc, double v) {
+      if (v != 0.0) atomicAdd(&io.WB[f * NC + cc], v);
+    };
+    auto XBadd = [&](int a, size_t i, double v) {
+      if (v != 0.0) atomicAdd(&io.xb.a[a][i], v);
+    };
+    const double* gs = io.x.a[A_gsgam2];
+    const double* gsh = io.x.a[A_gsgam2h];
+    // ------------------------------------------------------------ forward
+    const double rhog = W(W_RHOG_N, c);
+    const double rrhog = 1.0 / rhog;
+    const double rhoge_a = W(W_RHOGE_N, c);
+    const double gsg = gs[c];
+    double rhoge = rhoge_a;
+    // KIN2EIN pieces
+    double gh = 0, w2c0 = 0, w2c1 = 0, kinh = 0, kvp = 0, kv0 = 0, rvx = 0, rvy = 0, rvz = 0, tmp_h = 0;
+    double kvu[2] = {0, 0}, den[2] = {0, 0}, c2a[2] = {0, 0}, c2b[2] = {0, 0}, rwj[2] = {0, 0};
+    bool hv[2] = {false, false};
+    if (interior) {
+      gh = gsh[c + G];
+      const double rgh = 1.0 / gh;
+      w2c0 = div_rn(cfact[k] * gsg, gh, rgh);
+      w2c1 = div_rn(dfact[k] * gsg, gh, rgh);
+      kinh = W(W_KINH_N, c);
+      kvp = W(W_KINV_N, c + G);
+      kv0 = W(W_KINV_N, c);
+      const double tmp2 = kinh + (w2c0 * kvp + w2c1 * kv0);
+      rvx = W(W_RVX_N, c);
+      rvy = W(W_RVY_N, c);
+      rvz = W(W_RVZ_N, c);
+      tmp_h = div_rn(0.5 * (rvx * rvx + rvy * rvy + rvz * rvz), rhog, rrhog);
+      for (int s2 = 0; s2 < 2; ++s2) {   // s2 = 0: level k + 1, 1: level k
+        const int j = k + 1 - s2;
+        const size_t cj = c + G - s2 * G;
+        hv[s2] = (j >= kmin + 1 && j <= kmax);
+        if (!hv[s2]) continue;
+        const double ghj = gsh[cj];
+        c2a[s2] = afact[j] / gs[cj] * ghj;
+        c2b[s2] = bfact[j] / gs[cj - G] * ghj;
+        rwj[s2] = W(W_RW_N, cj);
+        den[s2] = c2a[s2] * W(W_RHOG_N, cj) + c2b[s2] * W(W_RHOG_N, cj - G);
+        kvu[s2] = 0.5 * (rwj[s2] * rwj[s2]) / den[s2];
+      }
+      const double tmp = tmp_h + (w2c0 * kvu[0] + w2c1 * kvu[1]);
+      rhoge = rhoge_a + (tmp2 - tmp);
+    }
+    double rq[6], qo[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) rq[n] = W(W_RQ_N + n, c);
+#pragma unroll
+    for (int n = 0; n < 6; ++n) qo[n] = div_rn(rq[n], rhog, rrhog);
+    const double rho1 = rhog / gsg;
+    const double ein = div_rn(rhoge, rhog, rrhog);
+    double qd = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qd = qd - qo[n];
+    // THRMDYN_tempre (its pressure is an output at the halo levels)
+    double cvt = 0.0, qdl = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) {
+      cvt = cvt + qo[n] * CVDRY;
+      qdl = qdl - qo[n];
+    }
+    cvt = cvt + qdl * CVDRY;
+    const double tem0 = ein / cvt;
+    const double pq0 = qdl * RDRY + qo[0] * RVAP;
+    const double pre0 = rho1 * tem0 * pq0;
+    const double ein_moist = ein + qo[0] * LHV0;
+    const double qsum = qo[0] + qo[1];
+    double q[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) q[n] = qo[n];
+    q[0] = qsum;
+    q[1] = 0.0;
+    double cvtot1 = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cvtot1 = cvtot1 + q[n] * CVDRY;
+    const double tem_p = (ein_moist - q[0] * LHV0) / cvtot1;
+    double tem = tem_p;
+    // saturation adjustment (satadjust_t's iteration, then its implicit derivative pieces)
+    bool sat = false;
+    double ts = 0, qsT = 0, cvT = 0, FT = 0, dqs = 0, qd_l = 0;
+    if (interior) {
+      qd_l = 1.0;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
+      double tv = tem;
+      double rtem = 1.0 / (dmax(tv, TEM_MIN));
+      double psat = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      double qsat = psat / (rho1 * RVAP * tv);
+      if (qsum - qsat > EPS) {
+        double qv[6];
+#pragma unroll
+        for (int n = 0; n < 6; ++n) qv[n] = q[n];
+        bool converged = false;
+        double tprev = tv;
+        int ite;
+        for (ite = 0; ite < P.itelim; ++ite) {
+          tprev = tv;
+          rtem = 1.0 / (dmax(tv, TEM_MIN));
+          psat = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
+          qsat = psat / (rho1 * RVAP * tv);
+          qv[I_QV] = qsat;
+          qv[I_QC] = qsum - qsat;
+          double cv = qd_l * CVDRY;
+#pragma unroll
+          for (int n = 1; n <= 5; ++n) cv = cv + qv[n] * CVDRY;
+          const double emoist_new = tv * cv + qv[I_QV] * LHV0;
+          const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
+          const double demoist_dT = cv + dqsat_dT * LHV0;
+          const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+          tv = tv - dtemp;
+          if (fabs(dtemp) < C.dtemp_criteria) {
+            converged = true;
+            break;
+          }
+          if (tv * 0.0 != 0.0) break;
+        }
+        tem = tv;
+        q[I_QV] = qv[I_QV];
+        q[I_QC] = qv[I_QC];
+        if (converged) {
+          sat = true;
+          ts = tprev;
+          qsT = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - 1.0 / dmax(ts, TEM_MIN))) / (rho1 * RVAP * ts);
+          cvT = qd_l * CVDRY + (qsum - qsT) * CVDRY;
+#pragma unroll
+          for (int n = 2; n <= 5; ++n) cvT = cvT + q[n] * CVDRY;
+          const double rts = 1.0 / ts;
+          dqs = qsT * (C.LovR_liq * rts * rts - rts);
+          FT = cvT - ts * dqs * CVDRY + dqs * LHV0;
+        } else {
+          record_err(P.status, (tv * 0.0 != 0.0) ? 4 : 3, k, g, l, ite);
+        }
+      }
+    }
+    double rq2[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) rq2[n] = rq[n];
+    rq2[I_QV] = rhog * q[I_QV];
+    rq2[I_QC] = rhog * q[I_QC];
+    double cvtot2 = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cvtot2 = cvtot2 + q[n] * CVDRY;
+    // negative filter (interior)
+    bool clip[6] = {false, false, false, false, false, false};
+    double rqf[6], qf[6], d2 = 0, rhog_o = rhog, rho_f = 0, qdf = 0, cva = 0, pq_f = 0;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      rqf[n] = rq2[n];
+      qf[n] = q[n];
+    }
+    if (interior) {
+      double diffq = 0.0;
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) {
+        diffq += rqf[n];
+        clip[n] = rqf[n] < 0.0;
+        rqf[n] = clip[n] ? 0.0 : rqf[n];
+      }
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) diffq -= rqf[n];
+      rqf[0] += diffq;
+      d2 = rqf[0];
+      clip[0] = rqf[0] < 0.0;
+      rqf[0] = clip[0] ? 0.0 : rqf[0];
+      d2 -= rqf[0];
+      rhog_o = rhog * (1.0 - d2);
+      rho_f = rhog_o / gsg;
+      const double rrhog_o = 1.0 / rhog_o;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) qf[n] = div_rn(rqf[n], rhog_o, rrhog_o);
+      qdf = 1.0;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) qdf = qdf - qf[n];
+      cva = qdf * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) cva = cva + qf[n] * CVDRY;
+      pq_f = qdf * RDRY + qf[I_QV] * RVAP;
+    }
+    // ------------------------------------------------------------ reverse
+    const double* SB = io.SB;
+    double b_tem = SB[SF_TEM * NC + c];
+    double b_qd = SB[SF_QD * NC + c];
+    double b_q[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) b_q[n] = SB[(SF_Q + n) * NC + c];
+    double b_rq2[6];
+    double b_rhog = 0.0, b_rho1 = 0.0, b_pre0 = 0.0, b_rhoge2 = 0.0, b_gsg = 0.0;
+    if (interior) {
+      const double B_pre = SB[SF_PRE * NC + c], B_rhoge = SB[SF_RHOGE * NC + c];
+      double b_rhog_o = SB[SF_RHOG * NC + c];
+      // pre = ((rho_f pq_f) tem)
+      b_tem += B_pre * rho_f * pq_f;
+      double b_rho_f = SB[SF_RHO * NC + c] + B_pre * tem * pq_f;
+      const double b_pq = B_pre * tem * rho_f;
+      double b_qdf = b_pq * RDRY;
+      b_q[I_QV] += b_pq * RVAP;
+      // rhoge = (tem rhog_o) cva
+      b_tem += B_rhoge * rhog_o * cva;
+      b_rhog_o += B_rhoge * tem * cva;
+      const double b_cva = B_rhoge * tem * rhog_o;
+      b_qdf += b_cva * CVDRY;
+      double b_qf[6];
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) b_qf[n] = b_q[n] + b_cva * CVDRY - b_qdf;
+      // qf = rqf / rhog_o; rho_f = rhog_o / gsg
+      double b_rqf[6];
+#pragma unroll
+      for (int n = 0; n < 6; ++n) b_rqf[n] = SB[(SF_RQ + n) * NC + c];
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) {
+        b_rqf[n] += b_qf[n] / rhog_o;
+        b_rhog_o -= b_qf[n] * qf[n] / rhog_o;
+      }
+      b_rhog_o += b_rho_f / gsg;
+      b_gsg -= b_rho_f * rho_f / gsg;
+      // rhog_o = rhog (1 - d2)
+      b_rhog += b_rhog_o * (1.0 - d2);
+      const double b_d2 = -b_rhog_o * rhog;
+      const double b_rq0a = (clip[0] ? b_d2 : 0.0) + (clip[0] ? 0.0 : b_rqf[0]);
+      b_rq2[0] = b_rq0a;
+      b_rq2[1] = b_rqf[1];
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) b_rq2[n] = (clip[n] ? b_rq0a : 0.0) + (clip[n] ? 0.0 : b_rqf[n]);
+      // the q outputs are the filter's for n >= 1: their adjoints were taken above
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) b_q[n] = 0.0;
+    } else {
+#pragma unroll
+      for (int n = 0; n < 6; ++n) b_rq2[n] = SB[(SF_RQ + n) * NC + c];
+      b_rhoge2 = SB[SF_RHOGE * NC + c];
+      b_rhog += SB[SF_RHOG * NC + c];
+      b_rho1 += SB[SF_RHO * NC + c];
+      b_pre0 = SB[SF_PRE * NC + c];
+    }
+    // rhoge2 = (rhog tem) cvtot2 (the output at the halo levels)
+    if (b_rhoge2 != 0.0) {
+      b_rhog += b_rhoge2 * tem * cvtot2;
+      b_tem += b_rhoge2 * rhog * cvtot2;
+      const double b_cv2 = b_rhoge2 * rhog * tem;
+      b_qd += b_cv2 * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) b_q[n] += b_cv2 * CVDRY;
+    }
+    // rq2[QV] = rhog q[QV], rq2[QC] = rhog q[QC]; rq2[n >= 2] = rq[n]
+    b_rhog += b_rq2[I_QV] * q[I_QV] + b_rq2[I_QC] * q[I_QC];
+    b_q[I_QV] += b_rq2[I_QV] * rhog;
+    b_q[I_QC] += b_rq2[I_QC] * rhog;
+    double b_rq[6] = {0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int n = 2; n <= 5; ++n) b_rq[n] += b_rq2[n];
+    // saturation adjustment
+    double b_ein_moist = 0.0, b_qsum = 0.0, b_rho_l = 0.0, b_tem_p = 0.0, b_q0p = 0.0;
+    if (sat) {
+      const double b_qc = b_q[I_QC], b_qv = b_q[I_QV];
+      b_qsum += b_qc;
+      const double b_qsI = b_qv - b_qc;
+      double b_qsT = b_qsI;
+      const double b_temI = b_tem + b_qsI * dqs;
+      const double b_F = -b_temI / FT;
+      const double b_cvT = b_F * ts;
+      b_qsT += b_F * LHV0;
+      b_ein_moist -= b_F;
+      const double b_qd_l = b_cvT * CVDRY;
+      b_qsum += b_cvT * CVDRY;
+      b_qsT -= b_cvT * CVDRY;
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) b_q[n] += b_cvT * CVDRY - b_qd_l;
+      b_rho_l -= b_qsT * qsT / rho1;
+    } else {
+      b_tem_p = b_tem;
+      b_q0p = b_q[I_QV];
+    }
+    // tem_p = (ein_moist - qsum LHV0) / cvtot1, cvtot1 = qd CV + sum_{n >= 2} q[n] CV
+    {
+      const double b_num = b_tem_p / cvtot1;
+      const double b_cv1 = -b_tem_p * tem_p / cvtot1;
+      b_ein_moist += b_num;
+      b_qsum -= b_num * LHV0;
+      b_qd += b_cv1 * CVDRY;
+#pragma unroll
+      for (int n = 2; n <= 5; ++n) b_q[n] += b_cv1 * CVDRY;
+    }
+    b_qsum += b_q0p;
+    b_rho1 += b_rho_l;
+    // q[n >= 2] = qo[n]; qsum = qo[0] + qo[1]; ein_moist = ein + qo[0] LHV0
+    double b_qo[6];
+#pragma unroll
+    for (int n = 0; n < 6; ++n) b_qo[n] = (n >= 2) ? b_q[n] : 0.0;
+    b_qo[0] += b_qsum + b_ein_moist * LHV0;
+    b_qo[1] += b_qsum;
+    double b_ein = b_ein_moist;
+    // pre0 = (rho1 tem0) pq0 (halo output)
+    if (b_pre0 != 0.0) {
+      b_rho1 += b_pre0 * tem0 * pq0;
+      const double b_tem0 = b_pre0 * rho1 * pq0;
+      const double b_pq0 = b_pre0 * rho1 * tem0;
+      const double b_qdl0 = b_pq0 * RDRY;
+      b_qo[0] += b_pq0 * RVAP;
+      b_ein += b_tem0 / cvt;
+      const double b_cvt = -b_tem0 * tem0 / cvt;
+      const double b_qdl = b_qdl0 + b_cvt * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) b_qo[n] += b_cvt * CVDRY - b_qdl;
+    }
+    // qd = 1 - sum qo[1..5]
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) b_qo[n] -= b_qd;
+    // ein = rhoge / rhog, rho1 = rhog / gsg, qo = rq / rhog
+    double b_rhoge = b_ein / rhog;
+    b_rhog -= b_ein * ein / rhog;
+    b_rhog += b_rho1 / gsg;
+    b_gsg -= b_rho1 * rho1 / gsg;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      b_rq[n] += b_qo[n] / rhog;
+      b_rhog -= b_qo[n] * qo[n] / rhog;
+    }
+    // KIN2EIN
+    if (interior) {
+      const double b_tmp2 = b_rhoge, b_tmp = -b_rhoge;
+      WBadd(W_KINH_N, c, b_tmp2);
+      WBadd(W_KINV_N, c + G, b_tmp2 * w2c0);
+      WBadd(W_KINV_N, c, b_tmp2 * w2c1);
+      double b_w2c0 = b_tmp2 * kvp + b_tmp * kvu[0];
+      double b_w2c1 = b_tmp2 * kv0 + b_tmp * kvu[1];
+      const double b_tmp_h = b_tmp;
+      const double b_sq = b_tmp_h / rhog;
+      b_rhog -= b_tmp_h * tmp_h / rhog;
+      WBadd(W_RVX_N, c, b_sq * rvx);
+      WBadd(W_RVY_N, c, b_sq * rvy);
+      WBadd(W_RVZ_N, c, b_sq * rvz);
+      for (int s2 = 0; s2 < 2; ++s2) {
+        if (!hv[s2]) continue;
+        const int j = k + 1 - s2;
+        const size_t cj = c + G - s2 * G;
+        const double b_kvu = b_tmp * (s2 == 0 ? w2c0 : w2c1);
+        WBadd(W_RW_N, cj, b_kvu * rwj[s2] / den[s2]);
+        const double b_den = -b_kvu * kvu[s2] / den[s2];
+        WBadd(W_RHOG_N, cj, b_den * c2a[s2]);
+        WBadd(W_RHOG_N, cj - G, b_den * c2b[s2]);
+        const double b_c2a = b_den * W(W_RHOG_N, cj), b_c2b = b_den * W(W_RHOG_N, cj - G);
+        // c2a = (afact / gs(j)) gsh(j), c2b = (bfact / gs(j-1)) gsh(j)
+        XBadd(A_gsgam2h, cj, b_c2a * (afact[j] / gs[cj]) + b_c2b * (bfact[j] / gs[cj - G]));
+        XBadd(A_gsgam2, cj, -b_c2a * c2a[s2] / gs[cj]);
+        XBadd(A_gsgam2, cj - G, -b_c2b * c2b[s2] / gs[cj - G]);
+      }
+      // w2c0 = cfact gsg / gh, w2c1 = dfact gsg / gh
+      b_gsg += (b_w2c0 * cfact[k] + b_w2c1 * dfact[k]) / gh;
+      XBadd(A_gsgam2h, c + G, -(b_w2c0 * w2c0 + b_w2c1 * w2c1) / gh);
+      WBadd(W_RHOGE_N, c, b_rhoge);
+    } else {
+      WBadd(W_RHOGE_N, c, b_rhoge);
+    }
+    WBadd(W_RHOG_N, c, b_rhog);
+#pragma unroll
+    for (int n = 0; n < 6; ++n) WBadd(W_RQ_N + n, c, b_rq[n]);
+    XBadd(A_gsgam2, c, b_gsg);
+  }
+}
+
 // Adjoint of S3, hand-written.  S3 is linear in the fluxes and tendencies, so
 // the adjoints of the divergences at a level follow from that level's output
 // adjoints alone; every cell rebuilds them for itself and its neighbours and
@@ -1081,7 +1466,7 @@ cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs&
 // tm: adj_stage_slots() slots of adj_stage_tape_cap() entries.
 cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
-                                     cudaStream_t stream) {
+                                     int recorded, cudaStream_t stream) {
   StageIO io;
   io.P = P;
   io.L = LayS{P.kall, P.gall, P.lall};
@@ -1108,7 +1493,10 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_seed_kernel<<<152 * 4, 256, 0, stream>>>(io);
   adj_seed_columns_kernel<<<64, 256, 0, stream>>>(io);
-  adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
+  if (recorded)
+    adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
+  else
+    adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);
   adj_s3_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
   adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);

@@ -30,7 +30,7 @@ cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x,
                             cudaStream_t stream);
 cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
-                                     cudaStream_t stream);
+                                     int recorded, cudaStream_t stream);
 cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
                                double* pbar, cudaStream_t stream);
 size_t adj_stage_work_doubles(int lall, int kall, int gall);
@@ -1133,7 +1133,7 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   double pb[8] = {};
   // the cell phase's outputs, then the column phase's adjoint (level-parallel stages)
   if (launch_adj_cellfwd(P, h->C, x, Y, h->stream) != cudaSuccess ||
-      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->stream) !=
+      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->adj_mode, h->stream) !=
           cudaSuccess ||
       cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess)

@@ -89,9 +89,10 @@ def test_adjoint_dot_product():
 
 @pytest.mark.parametrize("variant,seed", [("standard", 31), ("convective", 32), ("cold", 33)])
 def test_hand_written_adjoint_equals_recorded(variant, seed):
-    """The hand-written adjoint of the cell physics gives the input and
-    parameter adjoints of the operation-recording one (the column phase is
-    the same in both; its atomic sums make the last bits order-dependent)."""
+    """The hand-written adjoints of the cell physics and of the column phase's
+    thermodynamic stage give the input and parameter adjoints of the
+    operation-recording ones (the other column stages are the same in both;
+    their atomic sums make the last bits order-dependent)."""
     torch, drv, spec, st, x0 = _setup(1024, 42, 1, seed, variant)
     g = torch.Generator(device="cuda").manual_seed(seed)
     ybar = {n: torch.zeros_like(v) for n, v in x0.items()}
