@@ -1129,6 +1129,222 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
   }
 }
 
+// Adjoint of vadv_zdis_wh at level k: the adjoints of wh(k-1), wh(k), wh(k+1)
+// (bw[0..2]) from that of zdis.  At k == mkmin only wh(k) and wh(k+1) enter.
+__device__ __forceinline__ void zdis_wh_bar(double wm, double w0, double wpp, const double* rdz, const double* rdzs,
+                                            int k, int mkmin, double dt, double hdt2, double sdt3, double bz,
+                                            double* bw) {
+  if (k == mkmin) {
+    // z = (-hdt2 w0) ((wpp - w0) rdz) + dt w0
+    const double a = -hdt2 * w0, b = (wpp - w0) * rdz[mkmin];
+    bw[0] = 0.0;
+    bw[1] = bz * (-hdt2 * b - a * rdz[mkmin] + dt);
+    bw[2] = bz * a * rdz[mkmin];
+    return;
+  }
+  const double rs = rdzs[k];
+  const double r = (wpp - wm) * rs;
+  const double c = 2.0 * rs * ((wpp - w0) * rdz[k] - (w0 - wm) * rdz[k - 1]);
+  // z = (-hdt2 w0) r + dt w0 + (sdt3 w0) (w0 c + r r)
+  const double b_r = bz * (-hdt2 * w0 + sdt3 * w0 * 2.0 * r);
+  const double b_c = bz * sdt3 * w0 * w0;
+  double b_w0 = bz * (-hdt2 * r + dt + sdt3 * (2.0 * w0 * c + r * r));
+  const double b_d = b_c * 2.0 * rs;
+  b_w0 -= b_d * (rdz[k] + rdz[k - 1]);
+  bw[0] = -b_r * rs + b_d * rdz[k - 1];
+  bw[1] = b_w0;
+  bw[2] = b_r * rs + b_d * rdz[k];
+}
+
+// Adjoint of S1, hand-written: the cell's departure distances, kinetic
+// energies and flux sources recomputed as stage1 does, then the reverse
+// sweep.  Only interior cells have non-constant outputs.  Adjoints of values
+// at this cell that no other thread of the launch touches are added in place;
+// those at level k - 1, of the fall speeds at k - 3 .. k + 1 and of the
+// column's unit vectors go by atomics.
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int i = threadIdx.x; i < GF_COUNT * io.P.kall; i += blockDim.x) grid[i] = io.P.grid[i];
+  __syncthreads();
+  const Problem& P = io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const double* rdgz = grid + GF_RDGZ * K;
+  const double* rdgzh = grid + GF_RDGZH * K;
+  const double* rdzs = grid + GF_RDZS * K;
+  const double* rdzsh = grid + GF_RDZSH * K;
+  const double* afact = grid + GF_AFACT * K;
+  const double* bfact = grid + GF_BFACT * K;
+  const size_t NC = io.NC, G = io.L.G;
+  const double dt = P.dt, hdt2 = P.hdt2, sdt3 = P.sdt3;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    if (k < kmin || k > kmax) continue;
+    const bool hk = (k >= kmin + 1);
+    const size_t cc = io.L.c(l, g);
+    const double* const* x = io.x.a;
+    double* const* xb = io.xb.a;
+    auto Y = [&](int f, size_t i) { return io.Y[f * NC + i]; };
+    auto YBadd = [&](int f, size_t i, double v) {
+      if (v != 0.0) atomicAdd(&io.YB[f * NC + i], v);
+    };
+    auto YBown = [&](int f, size_t i, double v) { io.YB[f * NC + i] += v; };
+    auto XBadd = [&](int a, size_t i, double v) {
+      if (v != 0.0) atomicAdd(&xb[a][i], v);
+    };
+    auto XBown = [&](int a, size_t i, double v) { xb[a][i] += v; };
+    auto WB = [&](int f) { return io.WB[f * NC + c]; };
+    // ---------------------------------------------------- departure distances
+    double vt[3][5];
+    for (int t = 0; t < 3; ++t)
+      for (int j = 0; j < 5; ++j) {
+        const int kk = k - 3 + j;
+        vt[t][j] = (kk >= kmin && kk <= kmax) ? Y(YS_VT + t, c + (size_t)(j - 3) * G) : 0.0;
+      }
+    double bvt[3][5] = {};
+    for (int r = 0; r < 6; ++r) {
+      const double bz = WB(W_ZDIS + r);
+      if (bz == 0.0) continue;
+      const int t = r % 3, half = r / 3;
+      const int mkmin = half ? kmin + 1 : kmin;
+      if (k < mkmin) continue;
+      auto col = [&](int j) { return vt[t][j - k + 3]; };
+      auto wp = [&](int j) {
+        if (!half) return col(j);
+        return (j >= kmin + 1 && j <= kmax - 1) ? 0.5 * (col(j) + col(j - 1)) : 0.0;
+      };
+      auto wh = [&](int j) { return vadv_wh<double>(wp, j, mkmin, kmax); };
+      const double wm = k > mkmin ? wh(k - 1) : 0.0;
+      double bw[3];
+      zdis_wh_bar(wm, wh(k), wh(k + 1), half ? rdgzh : rdgz, half ? rdzsh : rdzs, k, mkmin, dt, hdt2, sdt3, bz, bw);
+      auto add_wp = [&](int j, double v) {
+        if (!half) {
+          bvt[t][j - k + 3] += v;
+        } else if (j >= kmin + 1 && j <= kmax - 1) {
+          bvt[t][j - k + 3] += 0.5 * v;
+          bvt[t][j - 1 - k + 3] += 0.5 * v;
+        }
+      };
+      for (int s2 = 0; s2 < 3; ++s2) {
+        const int j = k - 1 + s2;
+        const double v = bw[s2];
+        if (v == 0.0) continue;
+        if (j >= mkmin + 1 && j <= kmax) {
+          add_wp(j - 1, 0.5 * v);
+          add_wp(j, 0.5 * v);
+        } else if (j == mkmin) {
+          add_wp(mkmin, v);
+        } else if (j == mkmin - 1) {
+          add_wp(mkmin - 1, v);
+        } else {
+          add_wp(kmax, v);
+        }
+      }
+    }
+    for (int t = 0; t < 3; ++t)
+      for (int j = 0; j < 5; ++j) {
+        const int kk = k - 3 + j;
+        if (kk >= kmin && kk <= kmax) YBadd(YS_VT + t, c + (size_t)(j - 3) * G, bvt[t][j]);
+      }
+    // ------------------------------------------- metric factors, kinetic energy
+    const size_t ck = c;   // (l, k, g) in the full-level fields
+    const double gam2 = x[A_gam2][ck], gs = x[A_gsgam2][ck];
+    const double rgs = gam2 / gs;
+    const double vx = x[A_vx][ck], vy = x[A_vy][ck], vz = x[A_vz][ck];
+    const double ix = x[A_ix][cc], iy = x[A_iy][cc], iz = x[A_iz][cc];
+    const double jx = x[A_jx][cc], jy = x[A_jy][cc], jz = x[A_jz][cc];
+    const double vi = vx * ix + vy * iy + vz * iz;
+    const double vj = vx * jx + vy * jy + vz * jz;
+    const double rvx = x[A_rhogvx][ck], rvy = x[A_rhogvy][ck], rvz = x[A_rhogvz][ck];
+    const double rhog = Y(YS_RHOG, c);
+    const double kinh = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / rhog;
+    double gh = 0, gsm = 0, c2w0 = 0, c2w1 = 0, rw = 0, rhogm = 0, den = 0, kinv = 0, gam2h = 0, rgsh = 0;
+    if (hk) {
+      gh = x[A_gsgam2h][ck];
+      gsm = x[A_gsgam2][ck - G];
+      c2w0 = afact[k] / gs * gh;
+      c2w1 = bfact[k] / gsm * gh;
+      rw = x[A_rhogw][ck];
+      rhogm = Y(YS_RHOG, c - G);
+      den = c2w0 * rhog + c2w1 * rhogm;
+      kinv = 0.5 * (rw * rw) / den;
+      gam2h = x[A_gam2h][ck];
+      rgsh = gam2h / gh;
+    }
+    const double tem = Y(YS_TEM, c), zz = x[A_z][ck];
+    // ------------------------------------------------------------- sources
+    double b_kinh = WB(W_KINH), b_kinv = WB(W_KINV), b_rgs = 0.0, b_rgsh = 0.0, b_rw = 0.0;
+    double b_tem = 0.0, b_zz = 0.0, b_vi = 0.0, b_vj = 0.0;
+    const int tracer[3] = {I_QR, I_QS, I_QG};
+    for (int t = 0; t < 3; ++t) {
+      const int nq = tracer[t];
+      const double* bs = io.WB + (size_t)(W_RHOF + 8 * t) * NC + c;
+      const double b0 = bs[0], b1 = bs[NC], b2 = bs[2 * NC], b3 = bs[3 * NC], b4 = bs[4 * NC], b5 = bs[5 * NC];
+      const double b6 = hk ? bs[6 * NC] : 0.0, b7 = hk ? bs[7 * NC] : 0.0;
+      const double rq = Y(YS_RHOGQ + nq, c), qn = Y(YS_Q + nq - 1, c);
+      const double base = rq * rgs;
+      const double b_base = b0 + b1 * CVDRY * tem + b2 * GRAV * zz + b4 * vi + b5 * vj;
+      b_tem += b1 * base * CVDRY;
+      b_zz += b2 * base * GRAV;
+      b_vi += b4 * base;
+      b_vj += b5 * base;
+      double b_qn = b3 * rgs * kinh;
+      b_rgs += b3 * qn * kinh + b_base * rq;
+      b_kinh += b3 * qn * rgs;
+      if (hk) {
+        const double qm = Y(YS_Q + nq - 1, c - G);
+        const double qh = 0.5 * (qn + qm) * rgsh;
+        const double b_qh = b6 * kinv + b7 * rw;
+        b_kinv += b6 * qh;
+        b_rw += b7 * qh;
+        b_qn += b_qh * 0.5 * rgsh;
+        YBadd(YS_Q + nq - 1, c - G, b_qh * 0.5 * rgsh);
+        b_rgsh += b_qh * 0.5 * (qn + qm);
+      }
+      YBadd(YS_Q + nq - 1, c, b_qn);
+      YBown(YS_RHOGQ + nq, c, b_base * rgs);
+    }
+    YBown(YS_TEM, c, b_tem);
+    XBown(A_z, ck, b_zz);
+    double b_rhog = 0.0, b_gs = 0.0;
+    if (hk) {
+      // rgsh = gam2h / gsgam2h; kinv = 0.5 rw^2 / (c2w0 rhog(k) + c2w1 rhog(k-1))
+      double b_gh = -b_rgsh * rgsh / gh;
+      XBown(A_gam2h, ck, b_rgsh / gh);
+      b_rw += b_kinv * rw / den;
+      const double b_den = -b_kinv * kinv / den;
+      b_rhog += b_den * c2w0;
+      YBadd(YS_RHOG, c - G, b_den * c2w1);
+      const double b_c2w0 = b_den * rhog, b_c2w1 = b_den * rhogm;
+      b_gh += b_c2w0 * (afact[k] / gs) + b_c2w1 * (bfact[k] / gsm);
+      b_gs -= b_c2w0 * c2w0 / gs;
+      XBadd(A_gsgam2, ck - G, -b_c2w1 * c2w1 / gsm);
+      XBown(A_gsgam2h, ck, b_gh);
+      XBown(A_rhogw, ck, b_rw);
+    }
+    // kinh = 0.5 (rvx^2 + rvy^2 + rvz^2) / rhog
+    const double b_sq = b_kinh / rhog;
+    b_rhog -= b_kinh * kinh / rhog;
+    XBown(A_rhogvx, ck, b_sq * rvx);
+    XBown(A_rhogvy, ck, b_sq * rvy);
+    XBown(A_rhogvz, ck, b_sq * rvz);
+    // vi, vj
+    XBown(A_vx, ck, b_vi * ix + b_vj * jx);
+    XBown(A_vy, ck, b_vi * iy + b_vj * jy);
+    XBown(A_vz, ck, b_vi * iz + b_vj * jz);
+    XBadd(A_ix, cc, b_vi * vx);
+    XBadd(A_iy, cc, b_vi * vy);
+    XBadd(A_iz, cc, b_vi * vz);
+    XBadd(A_jx, cc, b_vj * vx);
+    XBadd(A_jy, cc, b_vj * vy);
+    XBadd(A_jz, cc, b_vj * vz);
+    // rgs = gam2 / gsgam2
+    XBown(A_gam2, ck, b_rgs / gs);
+    b_gs -= b_rgs * rgs / gs;
+    XBadd(A_gsgam2, ck, b_gs);
+    YBadd(YS_RHOG, c, b_rhog);
+  }
+}
+
 // Adjoint of S3, hand-written.  S3 is linear in the fluxes and tendencies, so
 // the adjoints of the divergences at a level follow from that level's output
 // adjoints alone; every cell rebuilds them for itself and its neighbours and
@@ -1499,7 +1715,10 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
     adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);
   adj_s3_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
-  adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  if (recorded)
+    adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  else
+    adj_s1_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io);
   return cudaGetLastError();
 }
 
