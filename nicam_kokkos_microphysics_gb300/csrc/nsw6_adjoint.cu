@@ -782,12 +782,12 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     const double gsg = gs[c];
     double rhoge = rhoge_a;
     // KIN2EIN pieces
-    double gh = 0, w2c0 = 0, w2c1 = 0, kinh = 0, kvp = 0, kv0 = 0, rvx = 0, rvy = 0, rvz = 0, tmp_h = 0;
+    double gh = 0, rgh = 0, w2c0 = 0, w2c1 = 0, kinh = 0, kvp = 0, kv0 = 0, rvx = 0, rvy = 0, rvz = 0, tmp_h = 0;
     double kvu[2] = {0, 0}, den[2] = {0, 0}, c2a[2] = {0, 0}, c2b[2] = {0, 0}, rwj[2] = {0, 0};
     bool hv[2] = {false, false};
     if (interior) {
       gh = gsh[c + G];
-      const double rgh = 1.0 / gh;
+      rgh = 1.0 / gh;
       w2c0 = div_rn(cfact[k] * gsg, gh, rgh);
       w2c1 = div_rn(dfact[k] * gsg, gh, rgh);
       kinh = W(W_KINH_N, c);
@@ -913,7 +913,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     for (int n = 1; n <= 5; ++n) cvtot2 = cvtot2 + q[n] * CVDRY;
     // negative filter (interior)
     bool clip[6] = {false, false, false, false, false, false};
-    double rqf[6], qf[6], d2 = 0, rhog_o = rhog, rho_f = 0, qdf = 0, cva = 0, pq_f = 0;
+    double rqf[6], qf[6], d2 = 0, rhog_o = rhog, rrhog_o = rrhog, rho_f = 0, qdf = 0, cva = 0, pq_f = 0;
 #pragma unroll
     for (int n = 0; n < 6; ++n) {
       rqf[n] = rq2[n];
@@ -936,7 +936,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       d2 -= rqf[0];
       rhog_o = rhog * (1.0 - d2);
       rho_f = rhog_o / gsg;
-      const double rrhog_o = 1.0 / rhog_o;
+      rrhog_o = 1.0 / rhog_o;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qf[n] = div_rn(rqf[n], rhog_o, rrhog_o);
       qdf = 1.0;
@@ -948,6 +948,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       pq_f = qdf * RDRY + qf[I_QV] * RVAP;
     }
     // ------------------------------------------------------------ reverse
+    // (divisions by reciprocals: the adjoint's coefficients need no correct rounding)
+    const double rgsg = 1.0 / gsg;
     const double* SB = io.SB;
     double b_tem = SB[SF_TEM * NC + c];
     double b_qd = SB[SF_QD * NC + c];
@@ -979,11 +981,11 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       for (int n = 0; n < 6; ++n) b_rqf[n] = SB[(SF_RQ + n) * NC + c];
 #pragma unroll
       for (int n = 1; n <= 5; ++n) {
-        b_rqf[n] += b_qf[n] / rhog_o;
-        b_rhog_o -= b_qf[n] * qf[n] / rhog_o;
+        b_rqf[n] += b_qf[n] * rrhog_o;
+        b_rhog_o -= b_qf[n] * qf[n] * rrhog_o;
       }
-      b_rhog_o += b_rho_f / gsg;
-      b_gsg -= b_rho_f * rho_f / gsg;
+      b_rhog_o += b_rho_f * rgsg;
+      b_gsg -= b_rho_f * rho_f * rgsg;
       // rhog_o = rhog (1 - d2)
       b_rhog += b_rhog_o * (1.0 - d2);
       const double b_d2 = -b_rhog_o * rhog;
@@ -1027,7 +1029,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double b_qsI = b_qv - b_qc;
       double b_qsT = b_qsI;
       const double b_temI = b_tem + b_qsI * dqs;
-      const double b_F = -b_temI / FT;
+      const double b_F = -b_temI * (1.0 / FT);
       const double b_cvT = b_F * ts;
       b_qsT += b_F * LHV0;
       b_ein_moist -= b_F;
@@ -1036,15 +1038,16 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       b_qsT -= b_cvT * CVDRY;
 #pragma unroll
       for (int n = 2; n <= 5; ++n) b_q[n] += b_cvT * CVDRY - b_qd_l;
-      b_rho_l -= b_qsT * qsT / rho1;
+      b_rho_l -= b_qsT * qsT * (gsg * rrhog);
     } else {
       b_tem_p = b_tem;
       b_q0p = b_q[I_QV];
     }
     // tem_p = (ein_moist - qsum LHV0) / cvtot1, cvtot1 = qd CV + sum_{n >= 2} q[n] CV
     {
-      const double b_num = b_tem_p / cvtot1;
-      const double b_cv1 = -b_tem_p * tem_p / cvtot1;
+      const double rcv1 = 1.0 / cvtot1;
+      const double b_num = b_tem_p * rcv1;
+      const double b_cv1 = -b_tem_p * tem_p * rcv1;
       b_ein_moist += b_num;
       b_qsum -= b_num * LHV0;
       b_qd += b_cv1 * CVDRY;
@@ -1067,8 +1070,9 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double b_pq0 = b_pre0 * rho1 * tem0;
       const double b_qdl0 = b_pq0 * RDRY;
       b_qo[0] += b_pq0 * RVAP;
-      b_ein += b_tem0 / cvt;
-      const double b_cvt = -b_tem0 * tem0 / cvt;
+      const double rcvt = 1.0 / cvt;
+      b_ein += b_tem0 * rcvt;
+      const double b_cvt = -b_tem0 * tem0 * rcvt;
       const double b_qdl = b_qdl0 + b_cvt * CVDRY;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) b_qo[n] += b_cvt * CVDRY - b_qdl;
@@ -1077,14 +1081,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
 #pragma unroll
     for (int n = 1; n <= 5; ++n) b_qo[n] -= b_qd;
     // ein = rhoge / rhog, rho1 = rhog / gsg, qo = rq / rhog
-    double b_rhoge = b_ein / rhog;
-    b_rhog -= b_ein * ein / rhog;
-    b_rhog += b_rho1 / gsg;
-    b_gsg -= b_rho1 * rho1 / gsg;
+    double b_rhoge = b_ein * rrhog;
+    b_rhog -= b_ein * ein * rrhog;
+    b_rhog += b_rho1 * rgsg;
+    b_gsg -= b_rho1 * rho1 * rgsg;
 #pragma unroll
     for (int n = 0; n < 6; ++n) {
-      b_rq[n] += b_qo[n] / rhog;
-      b_rhog -= b_qo[n] * qo[n] / rhog;
+      b_rq[n] += b_qo[n] * rrhog;
+      b_rhog -= b_qo[n] * qo[n] * rrhog;
     }
     // KIN2EIN
     if (interior) {
@@ -1095,8 +1099,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       double b_w2c0 = b_tmp2 * kvp + b_tmp * kvu[0];
       double b_w2c1 = b_tmp2 * kv0 + b_tmp * kvu[1];
       const double b_tmp_h = b_tmp;
-      const double b_sq = b_tmp_h / rhog;
-      b_rhog -= b_tmp_h * tmp_h / rhog;
+      const double b_sq = b_tmp_h * rrhog;
+      b_rhog -= b_tmp_h * tmp_h * rrhog;
       WBadd(W_RVX_N, c, b_sq * rvx);
       WBadd(W_RVY_N, c, b_sq * rvy);
       WBadd(W_RVZ_N, c, b_sq * rvz);
@@ -1105,19 +1109,21 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
         const int j = k + 1 - s2;
         const size_t cj = c + G - s2 * G;
         const double b_kvu = b_tmp * (s2 == 0 ? w2c0 : w2c1);
-        WBadd(W_RW_N, cj, b_kvu * rwj[s2] / den[s2]);
-        const double b_den = -b_kvu * kvu[s2] / den[s2];
+        const double rden = 1.0 / den[s2];
+        WBadd(W_RW_N, cj, b_kvu * rwj[s2] * rden);
+        const double b_den = -b_kvu * kvu[s2] * rden;
         WBadd(W_RHOG_N, cj, b_den * c2a[s2]);
         WBadd(W_RHOG_N, cj - G, b_den * c2b[s2]);
         const double b_c2a = b_den * W(W_RHOG_N, cj), b_c2b = b_den * W(W_RHOG_N, cj - G);
         // c2a = (afact / gs(j)) gsh(j), c2b = (bfact / gs(j-1)) gsh(j)
-        XBadd(A_gsgam2h, cj, b_c2a * (afact[j] / gs[cj]) + b_c2b * (bfact[j] / gs[cj - G]));
-        XBadd(A_gsgam2, cj, -b_c2a * c2a[s2] / gs[cj]);
-        XBadd(A_gsgam2, cj - G, -b_c2b * c2b[s2] / gs[cj - G]);
+        const double rgj = 1.0 / gs[cj], rgjm = 1.0 / gs[cj - G];
+        XBadd(A_gsgam2h, cj, b_c2a * (afact[j] * rgj) + b_c2b * (bfact[j] * rgjm));
+        XBadd(A_gsgam2, cj, -b_c2a * c2a[s2] * rgj);
+        XBadd(A_gsgam2, cj - G, -b_c2b * c2b[s2] * rgjm);
       }
       // w2c0 = cfact gsg / gh, w2c1 = dfact gsg / gh
-      b_gsg += (b_w2c0 * cfact[k] + b_w2c1 * dfact[k]) / gh;
-      XBadd(A_gsgam2h, c + G, -(b_w2c0 * w2c0 + b_w2c1 * w2c1) / gh);
+      b_gsg += (b_w2c0 * cfact[k] + b_w2c1 * dfact[k]) * rgh;
+      XBadd(A_gsgam2h, c + G, -(b_w2c0 * w2c0 + b_w2c1 * w2c1) * rgh);
       WBadd(W_RHOGE_N, c, b_rhoge);
     } else {
       WBadd(W_RHOGE_N, c, b_rhoge);

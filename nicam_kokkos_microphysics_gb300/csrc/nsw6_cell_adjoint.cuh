@@ -564,8 +564,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   // tem_o = rhoge / rcva
   {
     const double g = ob.tem;
-    b_rhoge += g / rcva;
-    const double b_rcva = -g * tem_o / rcva;
+    const double rr = 1.0 / rcva;
+    b_rhoge += g * rr;
+    const double b_rcva = -g * tem_o * rr;
     b_rhog += b_rcva * cva;
     const double b_cva = b_rcva * rhog;
     // cva = qd2 CV + sum q2 CV
@@ -576,8 +577,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   // q2[n] = rq2[n] / rhog
 #pragma unroll
   for (int n = 1; n <= 5; ++n) {
-    b_rq2[n] += b_q2[n] / rhog;
-    b_rhog -= b_q2[n] * q2[n] / rhog;
+    b_rq2[n] += b_q2[n] * rrhog;
+    b_rhog -= b_q2[n] * q2[n] * rrhog;
   }
   // rhoge = rhoge0 - LHV0 rqt0 dt + LHF0 (rqt3 + rqt4 + rqt5) dt
   double b_rhoge0 = b_rhoge;
@@ -606,9 +607,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     double b_r2_qc = 0.0, b_r2_qr = 0.0, b_r3_qc = 0.0, b_r3_qr = 0.0;
     // rceff = big ? r3 / r2 : 0
     if (big) {
-      const double rc = r3 / r2;
-      const double b_r3 = ob.rceff / r2;
-      const double b_r2 = -ob.rceff * rc / r2;
+      const double rr2 = 1.0 / r2;
+      const double b_r3 = ob.rceff * rr2;
+      const double b_r2 = -ob.rceff * (r3 * rr2) * rr2;
       b_r3_qc += b_r3;
       b_r3_qr += b_r3;
       b_r2_qc += b_r2;
@@ -618,9 +619,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     if (top) b_temp += ob.tctop;
     // rceff_cld = cld ? r3_qc / r2_qc : 0
     if (cld) {
-      const double rcc = r3_qc / r2_qc;
-      b_r3_qc += ob.rceff_cld / r2_qc;
-      b_r2_qc -= ob.rceff_cld * rcc / r2_qc;
+      const double rr2 = 1.0 / r2_qc;
+      b_r3_qc += ob.rceff_cld * rr2;
+      b_r2_qc -= ob.rceff_cld * (r3_qc * rr2) * rr2;
     }
     // r3_qc = (coef_xf dens) qc, r3_qr = (coef_xf dens) qr
     b_qc += b_r3_qc * r3c_a;
@@ -673,8 +674,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
       *bx[j] *= L.fac;
     }
     if (L.ratio) {   // fac = -dq / net
-      b_dq -= b_fac / L.net;
-      const double b_net = b_fac * dq / (L.net * L.net);
+      const double rnet = 1.0 / L.net;
+      b_dq -= b_fac * rnet;
+      const double b_net = b_fac * dq * (rnet * rnet);
       for (int j = 0; j < n; ++j) *bx[j] += sgn[j] * b_net;
     }
   };
@@ -872,8 +874,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
       const double b_dia = b_Di;
       const double b_dis = b_dia * C.Di_a;
       const double b_XMi = b_dis * bsqrt(di_s);
-      b_rhoqi += b_XMi / XNi;
-      b_XNi -= b_XMi * XMi / XNi;
+      const double rXNi = 1.0 / XNi;
+      b_rhoqi += b_XMi * rXNi;
+      b_XNi -= b_XMi * XMi * rXNi;
     }
     // XNi = min(max(5.38e7 pow(rhoqi, 0.75), 1e3), 1e6)
     if (!xn_hi && !xn_lo) {
@@ -905,8 +908,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     b_Cr += b_vr2 * fr;
     b_rho_fact += b_vr2 * C.Cr;
     // Glv = xl / (((LHV0 rKaT) (LovR_liq rtem - 1)) xl + 1)
-    const double b_xl0 = b_Glv / gl6;
-    const double b_gl6 = -b_Glv * Glv / gl6;
+    const double rgl6 = 1.0 / gl6;
+    const double b_xl0 = b_Glv * rgl6;
+    const double b_gl6 = -b_Glv * Glv * rgl6;
     const double b_gl4 = b_gl6 * xl;
     const double b_xl = b_xl0 + b_gl6 * gl4;
     const double b_gl1 = b_gl4 * gl3;
@@ -917,7 +921,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     b_KdD += b_xl * qsatl;
     b_qsatl += b_xl * KdD;
     // rKaT = 1 / (Ka temp)
-    const double b_kat = -b_rKaT_l * rKaT / kat;
+    const double b_kat = -b_rKaT_l * rKaT * rKaT;
     b_Ka += b_kat * temp;
     b_temp += b_kat * Ka;
   }
@@ -929,15 +933,16 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   }
   // Giv = xi / (((LHS0 rKaT) (LovR_ice rtem - 1)) xi + 1)
   {
-    const double b_xi0 = b_Giv / gv6;
-    const double b_gv6 = -b_Giv * Giv / gv6;
+    const double rgv6 = 1.0 / gv6;
+    const double b_xi0 = b_Giv * rgv6;
+    const double b_gv6 = -b_Giv * Giv * rgv6;
     const double b_gv4 = b_gv6 * xi;
     const double b_xi = b_xi0 + b_gv6 * gv4;
     const double b_gv1 = b_gv4 * gv3;
     const double b_gv3 = b_gv4 * gv1;
     b_rtem += b_gv3 * C.LovR_ice;
     const double b_rKaT = b_gv1 * LHS0;
-    const double b_kat = -b_rKaT * rKaT / kat;
+    const double b_kat = -b_rKaT * rKaT * rKaT;
     b_Ka += b_kat * temp;
     b_temp += b_kat * Ka;
     b_KdD += b_xi * qsati;
@@ -945,16 +950,18 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   }
   // rNu = dens / nu0, nu0 = 1.718e-5 + 5.28e-8 temc
   {
-    b_dens += b_rNu / nu0;
-    const double b_nu0 = -b_rNu * rNu / nu0;
+    const double rnu0 = 1.0 / nu0;
+    b_dens += b_rNu * rnu0;
+    const double b_nu0 = -b_rNu * rNu * rnu0;
     b_temc += b_nu0 * 5.28E-8;
   }
   // KdD = ((kd0 PSTD) / pre) dens, kd0 = 2.222e-5 + 1.37e-7 temc
   {
     b_dens += b_KdD * kd2;
     const double b_kd2 = b_KdD * dens;
-    const double b_kd1 = b_kd2 / pre;
-    b_pre -= b_kd2 * kd2 / pre;
+    const double rpre = 1.0 / pre;
+    const double b_kd1 = b_kd2 * rpre;
+    b_pre -= b_kd2 * kd2 * rpre;
     b_temc += b_kd1 * PSTD * 1.37E-7;
   }
   // Ka = 2.428e-2 + 7.47e-5 temc
@@ -1149,8 +1156,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   // snow moments: Vts's RMOMs_Vt = mom5 / mom2; mom_i = exp(logX lb_i + la_i(tems)); MOMs_2 = Xs2
   double b_Xs2 = b_MOMs_2;
   if (snow) {
-    b_mom[5] += b_RMOMs_Vt / mom[2];
-    b_mom[2] -= b_RMOMs_Vt * RMOMs_Vt / mom[2];
+    const double rm2 = 1.0 / mom[2];
+    b_mom[5] += b_RMOMs_Vt * rm2;
+    b_mom[2] -= b_RMOMs_Vt * RMOMs_Vt * rm2;
     double b_logX = 0.0, b_tems = 0.0;
 #pragma unroll
     for (int i = 0; i < 7; ++i) {
@@ -1196,24 +1204,29 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     b_qr += b_a * dens;
   }
   // dq/dt = q / dt
-  b_qv += b_dqv / dt;
-  b_qc += b_dqc / dt;
-  b_qr += b_dqr / dt;
-  b_qi += b_dqi / dt;
-  b_qs += b_dqs / dt;
-  b_qg += b_dqg / dt;
+  {
+    const double rdt = 1.0 / dt;
+    b_qv += b_dqv * rdt;
+    b_qc += b_dqc * rdt;
+    b_qr += b_dqr * rdt;
+    b_qi += b_dqi * rdt;
+    b_qs += b_dqs * rdt;
+    b_qg += b_dqg * rdt;
+  }
   // temc = temp - TEM00; rho_fact = sqrt(DENS00 Rdens); Rdens = 1 / dens
   b_temp += b_temc;
   b_Rdens += b_rho_fact * bsqrt(rho_fact) * DENS00;
-  b_dens -= b_Rdens * Rdens / dens;
+  b_dens -= b_Rdens * Rdens * Rdens;
   // Sliq = qv / max(qsatl, EPS), Sice = qv / max(qsati, EPS)
   {
-    b_qv += b_Sliq / sld;
-    const double b_sld = -b_Sliq * Sliq / sld;
+    const double rsld = 1.0 / sld;
+    b_qv += b_Sliq * rsld;
+    const double b_sld = -b_Sliq * Sliq * rsld;
     double dummy = 0.0;
     bmax(qsatl, EPS, b_sld, b_qsatl, dummy);
-    b_qv += b_Sice / sid;
-    const double b_sid = -b_Sice * Sice / sid;
+    const double rsid = 1.0 / sid;
+    b_qv += b_Sice * rsid;
+    const double b_sid = -b_Sice * Sice * rsid;
     bmax(qsati, EPS, b_sid, b_qsati, dummy);
   }
   // q* = max(qn, 0)
@@ -1228,12 +1241,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   {
     const double b_rdrt = b_qsatl * psatl + b_qsati * psati;
     const double b_psatl = b_qsatl * rdrt, b_psati = b_qsati * rdrt;
-    const double b_drt = -b_rdrt * rdrt / drt;
+    const double b_drt = -b_rdrt * rdrt * rdrt;
     b_dens += b_drt * temp * RVAP;
     b_temp += b_drt * drv;
     b_rtem -= b_psatl * PSAT0 * el * C.LovR_liq + b_psati * PSAT0 * ei * C.LovR_ice;
     // rtem = 1 / max(temp, TEM_MIN)
-    const double b_tmx = -b_rtem * rtem / tmx;
+    const double b_tmx = -b_rtem * rtem * rtem;
     double dummy = 0.0;
     bmax(temp, TEM_MIN, b_tmx, b_temp, dummy);
   }
@@ -1258,11 +1271,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   {
 #pragma unroll
     for (int n = 1; n <= 5; ++n) {
-      b_rq[n] += b_qn[n] / rhog;
-      b_rhog -= b_qn[n] * qn[n] / rhog;
+      b_rq[n] += b_qn[n] * rrhog;
+      b_rhog -= b_qn[n] * qn[n] * rrhog;
     }
-    b_rhog += b_dens / in.gsgam2;
-    ib.gsgam2 += -b_dens * dens / in.gsgam2;
+    const double rgs = 1.0 / in.gsgam2;
+    b_rhog += b_dens * rgs;
+    ib.gsgam2 += -b_dens * dens * rgs;
   }
   // rhog = in.rhog (1 - d2); negative filter
   {
@@ -1281,10 +1295,10 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   // parameters
   pb[0] += b_beta;
   pb[1] += b_qicrt;
-  pb[2] += b_K_vtr * C.K_vtr / C.Cr + b_K_raci * C.K_raci / C.Cr + b_K_iacr * C.K_iacr / C.Cr + b_Cr;
-  pb[3] += b_K_vts * C.K_vts / C.Cs + b_K_sacw * C.K_sacw / C.Cs + b_K_saci * C.K_saci / C.Cs +
-           b_K_vents2 * 0.5 * C.K_vents2 / C.Cs;
-  pb[4] += b_K_vtg * C.K_vtg / C.Cg + b_K_gacw * C.K_gacw / C.Cg + b_Cg;
+  pb[2] += (b_K_vtr * C.K_vtr + b_K_raci * C.K_raci + b_K_iacr * C.K_iacr) * (1.0 / C.Cr) + b_Cr;
+  pb[3] += (b_K_vts * C.K_vts + b_K_sacw * C.K_sacw + b_K_saci * C.K_saci + b_K_vents2 * 0.5 * C.K_vents2) *
+           (1.0 / C.Cs);
+  pb[4] += (b_K_vtg * C.K_vtg + b_K_gacw * C.K_gacw) * (1.0 / C.Cg) + b_Cg;
   pb[5] += b_icenuc;
   pb[6] += b_K_aut * C.K_aut / C.kk_aut;
 }
