@@ -1252,9 +1252,11 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
         if (kk >= kmin && kk <= kmax) YBadd(YS_VT + t, c + (size_t)(j - 3) * G, bvt[t][j]);
       }
     // ------------------------------------------- metric factors, kinetic energy
+    // (recomputed for the partials only, so by reciprocals; no branch reads them)
     const size_t ck = c;   // (l, k, g) in the full-level fields
     const double gam2 = x[A_gam2][ck], gs = x[A_gsgam2][ck];
-    const double rgs = gam2 / gs;
+    const double rgsr = 1.0 / gs;
+    const double rgs = gam2 * rgsr;
     const double vx = x[A_vx][ck], vy = x[A_vy][ck], vz = x[A_vz][ck];
     const double ix = x[A_ix][cc], iy = x[A_iy][cc], iz = x[A_iz][cc];
     const double jx = x[A_jx][cc], jy = x[A_jy][cc], jz = x[A_jz][cc];
@@ -1262,19 +1264,23 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     const double vj = vx * jx + vy * jy + vz * jz;
     const double rvx = x[A_rhogvx][ck], rvy = x[A_rhogvy][ck], rvz = x[A_rhogvz][ck];
     const double rhog = Y(YS_RHOG, c);
-    const double kinh = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / rhog;
-    double gh = 0, gsm = 0, c2w0 = 0, c2w1 = 0, rw = 0, rhogm = 0, den = 0, kinv = 0, gam2h = 0, rgsh = 0;
+    const double rrhog = 1.0 / rhog;
+    const double kinh = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) * rrhog;
+    double gh = 0, rgh = 0, rgsm = 0, rden = 0, gsm = 0, c2w0 = 0, c2w1 = 0, rw = 0, rhogm = 0, den = 0, kinv = 0, gam2h = 0, rgsh = 0;
     if (hk) {
       gh = x[A_gsgam2h][ck];
       gsm = x[A_gsgam2][ck - G];
-      c2w0 = afact[k] / gs * gh;
-      c2w1 = bfact[k] / gsm * gh;
+      rgh = 1.0 / gh;
+      rgsm = 1.0 / gsm;
+      c2w0 = afact[k] * rgsr * gh;
+      c2w1 = bfact[k] * rgsm * gh;
       rw = x[A_rhogw][ck];
       rhogm = Y(YS_RHOG, c - G);
       den = c2w0 * rhog + c2w1 * rhogm;
-      kinv = 0.5 * (rw * rw) / den;
+      rden = 1.0 / den;
+      kinv = 0.5 * (rw * rw) * rden;
       gam2h = x[A_gam2h][ck];
-      rgsh = gam2h / gh;
+      rgsh = gam2h * rgh;
     }
     const double tem = Y(YS_TEM, c), zz = x[A_z][ck];
     // ------------------------------------------------------------- sources
@@ -1314,22 +1320,22 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     double b_rhog = 0.0, b_gs = 0.0;
     if (hk) {
       // rgsh = gam2h / gsgam2h; kinv = 0.5 rw^2 / (c2w0 rhog(k) + c2w1 rhog(k-1))
-      double b_gh = -b_rgsh * rgsh / gh;
-      XBown(A_gam2h, ck, b_rgsh / gh);
-      b_rw += b_kinv * rw / den;
-      const double b_den = -b_kinv * kinv / den;
+      double b_gh = -b_rgsh * rgsh * rgh;
+      XBown(A_gam2h, ck, b_rgsh * rgh);
+      b_rw += b_kinv * rw * rden;
+      const double b_den = -b_kinv * kinv * rden;
       b_rhog += b_den * c2w0;
       YBadd(YS_RHOG, c - G, b_den * c2w1);
       const double b_c2w0 = b_den * rhog, b_c2w1 = b_den * rhogm;
-      b_gh += b_c2w0 * (afact[k] / gs) + b_c2w1 * (bfact[k] / gsm);
-      b_gs -= b_c2w0 * c2w0 / gs;
-      XBadd(A_gsgam2, ck - G, -b_c2w1 * c2w1 / gsm);
+      b_gh += b_c2w0 * (afact[k] * rgsr) + b_c2w1 * (bfact[k] * rgsm);
+      b_gs -= b_c2w0 * c2w0 * rgsr;
+      XBadd(A_gsgam2, ck - G, -b_c2w1 * c2w1 * rgsm);
       XBown(A_gsgam2h, ck, b_gh);
       XBown(A_rhogw, ck, b_rw);
     }
     // kinh = 0.5 (rvx^2 + rvy^2 + rvz^2) / rhog
-    const double b_sq = b_kinh / rhog;
-    b_rhog -= b_kinh * kinh / rhog;
+    const double b_sq = b_kinh * rrhog;
+    b_rhog -= b_kinh * kinh * rrhog;
     XBown(A_rhogvx, ck, b_sq * rvx);
     XBown(A_rhogvy, ck, b_sq * rvy);
     XBown(A_rhogvz, ck, b_sq * rvz);
@@ -1344,8 +1350,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     XBadd(A_jy, cc, b_vj * vy);
     XBadd(A_jz, cc, b_vj * vz);
     // rgs = gam2 / gsgam2
-    XBown(A_gam2, ck, b_rgs / gs);
-    b_gs -= b_rgs * rgs / gs;
+    XBown(A_gam2, ck, b_rgs * rgsr);
+    b_gs -= b_rgs * rgs * rgsr;
     XBadd(A_gsgam2, ck, b_gs);
     YBadd(YS_RHOG, c, b_rhog);
   }
@@ -1508,6 +1514,63 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_kernel(StageIO io, TapeM
     seed(F, gF);
     tape_reverse();
     scatter(io, lg);
+  }
+}
+
+// Adjoint of S2, hand-written: one thread per cell and tracer, for the eight
+// fluxes of the tracer.  A flux is acc = sum_k2 src(k2) c(k2) + src(kc) zdis'
+// where |acc| >= EPS and 0 below; the stored flux tells which (acc is never 0
+// where it is kept).  The departure distances' adjoints of this cell are only
+// written here; the sources' go to the levels the integral spans, by atomics.
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s2_hw_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int i = threadIdx.x; i < GF_COUNT * io.P.kall; i += blockDim.x) grid[i] = io.P.grid[i];
+  __syncthreads();
+  const Problem& P = io.P;
+  const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
+  const size_t NC = io.NC, G = io.L.G;
+  const size_t n = NC * 3;
+  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = w % NC;
+    const int t = (int)(w / NC);
+    const int k = (int)((c / G) % K), l = (int)(c / (G * K));
+    if (k < kmin || k > kmax) continue;
+    const int* bmn = io.bnd + ((size_t)l * 2 + 0) * 6 * K;
+    const int* bmx = io.bnd + ((size_t)l * 2 + 1) * 6 * K;
+    for (int half = 0; half < 2; ++half) {
+      const int mkmin = half ? kmin + 1 : kmin;
+      if (k < mkmin) continue;
+      const int f0 = half ? 6 : 0, f1 = half ? 8 : 6;
+      bool any = false;
+      for (int f = f0; f < f1; ++f)
+        any = any || (io.WB[(W_F + 8 * t + f) * NC + c] != 0.0 && io.W[(W_F + 8 * t + f) * NC + c] != 0.0);
+      if (!any) continue;
+      const int r = half ? 3 + t : t;
+      const int lo = bmn[r * K + k];
+      const int hi = bmx[t * K + k];
+      const double* zh = grid + (half ? GF_GZSHIFT : GF_GZH) * K;
+      const double* dz = grid + (half ? GF_DGZH : GF_DGZ) * K;
+      const double zv = io.W[(W_ZDIS + r) * NC + c];
+      const int kc = departure_cell_t(zh, k, zv, lo, bmx[r * K + k], mkmin, kmax);
+      const bool span = !(lo == k && hi == k);
+      double zd = zv;
+      if (span && hi != kc) zd = zd - (hi > kc ? dz[hi] : -dz[hi]);
+      double b_z = 0.0;
+      for (int f = f0; f < f1; ++f) {
+        const double gF = io.WB[(W_F + 8 * t + f) * NC + c];
+        if (gF == 0.0 || io.W[(W_F + 8 * t + f) * NC + c] == 0.0) continue;
+        const int src = W_RHOF + 8 * t + f;
+        double* bs = io.WB + (size_t)src * NC + (c - (size_t)k * G);   // level 0 of this column
+        if (span)
+          for (int k2 = lo; k2 <= hi; ++k2) {
+            if (k2 == kc) continue;
+            atomicAdd(bs + (size_t)k2 * G, gF * (k2 > kc ? dz[k2] : -dz[k2]));
+          }
+        if (zd != 0.0) atomicAdd(bs + (size_t)kc * G, gF * zd);
+        b_z += gF * io.W[(size_t)src * NC + (c - (size_t)k * G) + (size_t)kc * G];
+      }
+      io.WB[(W_ZDIS + r) * NC + c] += b_z;
+    }
   }
 }
 
@@ -1720,7 +1783,10 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   else
     adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);
   adj_s3_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
-  adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  if (recorded)
+    adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  else
+    adj_s2_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   if (recorded)
     adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
   else
