@@ -37,7 +37,8 @@ typedef enum nsw6_status {
   NSW6_ERR_NOCONV = 3,       /* satadjust Newton hit the iteration limit             */
   NSW6_ERR_NAN = 4,          /* satadjust produced a non-finite temperature          */
   NSW6_ERR_UNSUPPORTED = 5,  /* configuration not implemented                        */
-  NSW6_ERR_TOO_LARGE = 6     /* region larger than mp_driver_noalloc's fixed scratch */
+  NSW6_ERR_TOO_LARGE = 6,    /* region larger than mp_driver_noalloc's fixed scratch */
+  NSW6_ERR_CHECK = 7         /* adjoint mode 2: its forward differs from the step's  */
 } nsw6_status;
 
 /* Tunable NSW6 scheme parameters (GlobalParams, src/mod_mp_nsw6.h:16-123,
@@ -266,19 +267,23 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  *   parameters' adjoint is added to it.  Every cell is differentiated by its
  *   own thread: the column phase in four level-parallel stages whose input
  *   adjoints are added with atomics (so the last bits depend on their order),
- *   the cell physics per cell.  The first call allocates the tapes and work
- *   fields and keeps them in the handle: about 2.6 GB of stage tapes, 32 bytes
- *   per recorded operation of the cell physics for 58,368 cells at a time,
- *   and about 150 doubles per cell for lall_max regions. */
+ *   the cell physics per cell, each by a hand-written reverse sweep.  The
+ *   first call allocates the work fields and keeps them in the handle: about
+ *   150 doubles per cell for lall_max regions (nsw6_set_adjoint_mode 1 adds
+ *   tapes: about 2.6 GB for the stages and 32 bytes per recorded operation of
+ *   the cell physics for 58,368 cells at a time). */
 int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
                   double dt, double ct);
 
-/* Implementation of the adjoints of the cell physics and of the column
- * phase's last stage (KIN2EIN, thermodynamics, saturation adjustment,
- * negative filter) inside mp_driver_adjoint: 0 (default) the hand-written
- * reverse sweeps (no tape); 1 the operations recorded on per-cell tapes and
- * swept back (the operator-overloading form, for checking the hand-written
- * ones). */
+/* Implementation of the adjoint inside mp_driver_adjoint: 0 (default) the
+ * hand-written reverse sweeps (no tape), the cell physics' from a checkpoint
+ * of its costly forward values (49 doubles per cell, kept in the handle);
+ * 1 the operations of the cell physics and of the column stages S1, S2, S4
+ * recorded on per-cell tapes and swept back (the operator-overloading form,
+ * for checking the hand-written ones); 2 as 0, and the hand-written forward
+ * the checkpoint comes from is also checked against the step's cell physics
+ * on every cell: a cell whose outputs differ in any bit ends the call with
+ * NSW6_ERR_CHECK (nsw6_last_error's iters: the first differing output). */
 int nsw6_set_adjoint_mode(nsw6_handle* h, int mode);
 int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
                       double dt, double ct);

@@ -161,9 +161,11 @@ class MPDriver:
         _check(self._lib.nsw6_set_precision(self._h, int(m)), self._lib)
 
     def set_adjoint_mode(self, mode: int | str) -> None:
-        """Cell-physics adjoint of ``adjoint``: 0 / "hand" the hand-written
-        reverse sweep (default), 1 / "tape" the recorded operations."""
-        m = {"hand": 0, "tape": 1}.get(mode, mode) if isinstance(mode, str) else int(mode)
+        """Implementation of ``adjoint``: 0 / "hand" the hand-written reverse
+        sweeps (default), 1 / "tape" the recorded operations, 2 / "check" as
+        "hand" with its forward checked bitwise against the step's cell
+        physics on every cell (a difference raises NSW6_ERR_CHECK)."""
+        m = {"hand": 0, "tape": 1, "check": 2}.get(mode, mode) if isinstance(mode, str) else int(mode)
         _check(self._lib.nsw6_set_adjoint_mode(self._h, int(m)), self._lib)
 
     def set_math(self, mode: int) -> None:

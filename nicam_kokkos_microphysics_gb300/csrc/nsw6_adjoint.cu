@@ -42,7 +42,7 @@ namespace nsw6 {
 // Cell-phase output fields (Y / YB layout of nsw6_deriv.cu).
 enum AdjFieldS {
   YS_RHOG, YS_RHOGE, YS_TEM, YS_RHOGQ, YS_Q = YS_RHOGQ + 6, YS_VT = YS_Q + 5, YS_RE = YS_VT + 3, YS_RECLD,
-  YS_RCTOP, YS_TCTOP
+  YS_RCTOP, YS_TCTOP, ADJ_Y_FIELDS
 };
 
 // Work fields of the staged column adjoint: [NWF][lall][kall][gall].
@@ -833,7 +833,6 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     cvt = cvt + qdl * CVDRY;
     const double tem0 = ein / cvt;
     const double pq0 = qdl * RDRY + qo[0] * RVAP;
-    const double pre0 = rho1 * tem0 * pq0;
     const double ein_moist = ein + qo[0] * LHV0;
     const double qsum = qo[0] + qo[1];
     double q[6];
@@ -1673,8 +1672,80 @@ __global__ void adj_seed_columns_kernel(StageIO io) {
 // The cell phase's adjoint, hand-written (nsw6_cell_adjoint.cuh): one thread
 // per interior cell; output adjoints from YB, input adjoints added to xb (each
 // cell owns its entries here), the parameters' adjoint reduced per block.
+// The cell phase's forward for the adjoint: the outputs Y of every interior
+// cell and the checkpoint of its costly forward values (CELL_CK_SLOTS doubles,
+// slot-major over the cells), both from the hand-written forward.  check: also
+// evaluate nsw6_cell and report a cell whose outputs differ in any bit
+// (status ERR_ADJ_CHECK, iters = the first output field that differs).
+constexpr int ERR_ADJ_CHECK = 7;
+__global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C, ArgPtrs x, double* Y, double* ck,
+                                                            int check) {
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  __syncthreads();
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const LayS L{P.kall, P.gall, P.lall};
+  const size_t NC = (size_t)P.lall * P.kall * P.gall;
+  const int nint = P.kmax - P.kmin + 1;
+  const long long ncell = (long long)P.lall * nint * P.gall;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(c % P.gall);
+    const int k = P.kmin + (int)((c / P.gall) % nint);
+    const int l = (int)(c / ((long long)P.gall * nint));
+    const size_t i = L.f(l, k, g);
+    CellIn in;
+    in.rhog = x.a[A_rhog][i];
+    in.tem = x.a[A_tem][i];
+    in.gsgam2 = x.a[A_gsgam2][i];
+    in.q0 = x.a[A_q][L.t(l, 0, k, g)];
+    for (int n = 0; n < 6; ++n) in.rhogq[n] = x.a[A_rhogq][L.t(l, n, k, g)];
+    CellOut o;
+    CellBar ob{};
+    CellInBar ib{};
+    nsw6_cell_adjoint<CA_SAVE>(C, fm, P.dt, P.rdt, in, ob, ib, nullptr, CellCk{ck + c, (size_t)ncell}, &o);
+    double y[ADJ_Y_FIELDS];
+    y[YS_RHOG] = o.rhog;
+    y[YS_RHOGE] = o.rhoge;
+    y[YS_TEM] = o.tem;
+    for (int n = 0; n < 6; ++n) y[YS_RHOGQ + n] = o.rhogq[n];
+    for (int n = 1; n < 6; ++n) y[YS_Q + n - 1] = o.q[n];
+    y[YS_VT + 0] = o.Vtr;
+    y[YS_VT + 1] = o.Vts;
+    y[YS_VT + 2] = o.Vtg;
+    y[YS_RE] = o.rceff;
+    y[YS_RECLD] = o.rceff_cld;
+    y[YS_RCTOP] = o.rctop;
+    y[YS_TCTOP] = o.tctop;
+    for (int f = 0; f < ADJ_Y_FIELDS; ++f) Y[f * NC + i] = y[f];
+    if (check) {
+      CellOut r;
+      nsw6_cell(C, fm, P.dt, P.rdt, in, r);
+      double z[ADJ_Y_FIELDS];
+      z[YS_RHOG] = r.rhog;
+      z[YS_RHOGE] = r.rhoge;
+      z[YS_TEM] = r.tem;
+      for (int n = 0; n < 6; ++n) z[YS_RHOGQ + n] = r.rhogq[n];
+      for (int n = 1; n < 6; ++n) z[YS_Q + n - 1] = r.q[n];
+      z[YS_VT + 0] = r.Vtr;
+      z[YS_VT + 1] = r.Vts;
+      z[YS_VT + 2] = r.Vtg;
+      z[YS_RE] = r.rceff;
+      z[YS_RECLD] = r.rceff_cld;
+      z[YS_RCTOP] = r.rctop;
+      z[YS_TCTOP] = r.tctop;
+      for (int f = 0; f < ADJ_Y_FIELDS; ++f)
+        if (__double_as_longlong(y[f]) != __double_as_longlong(z[f])) {
+          record_err(P.status, ERR_ADJ_CHECK, k, g, l, f);
+          break;
+        }
+    }
+  }
+}
+
+// The cell phase's adjoint, hand-written, from the checkpoint ck of
+// adj_cell_save_kernel.
 __global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb, const double* YB,
-                                                          double* pbar) {
+                                                          double* pbar, double* ck) {
   __shared__ double tab[FM_TABLE_DOUBLES];
   __shared__ double red[7][128];
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
@@ -1711,7 +1782,7 @@ __global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, Consts C, A
     ob.rctop = k == P.kmax ? YB[YS_RCTOP * NC + i] : 0.0;
     ob.tctop = k == P.kmax ? YB[YS_TCTOP * NC + i] : 0.0;
     CellInBar ib{};
-    nsw6_cell_adjoint(C, fm, P.dt, P.rdt, in, ob, ib, pacc);
+    nsw6_cell_adjoint<CA_LOAD>(C, fm, P.dt, P.rdt, in, ob, ib, pacc, CellCk{ck + c, (size_t)ncell});
     xb.a[A_rhog][i] += ib.rhog;
     xb.a[A_tem][i] += ib.tem;
     xb.a[A_gsgam2][i] += ib.gsgam2;
@@ -1739,8 +1810,16 @@ int adj_stage_tape_cap() { return 512; }
 int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
 
 cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
-                               double* pbar, cudaStream_t stream) {
-  adj_cell_hw_kernel<<<152 * 2, 128, 0, stream>>>(P, C, x, xb, YB, pbar);
+                               double* pbar, double* ck, cudaStream_t stream) {
+  adj_cell_hw_kernel<<<152 * 2, 128, 0, stream>>>(P, C, x, xb, YB, pbar, ck);
+  return cudaGetLastError();
+}
+
+size_t adj_cell_ck_doubles(int lall, int kall, int gall) { return (size_t)CELL_CK_SLOTS * lall * (kall - 2) * gall; }
+
+cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, double* ck, int check,
+                                 cudaStream_t stream) {
+  adj_cell_save_kernel<<<152 * 4, 128, 0, stream>>>(P, C, x, Y, ck, check);
   return cudaGetLastError();
 }
 

@@ -51,8 +51,33 @@ __device__ __forceinline__ void bmax(double a, double b, double g, double& ba, d
 }
 __device__ __forceinline__ double bsqrt(double s) { return s > 0.0 ? 0.5 / s : 0.0; }
 
+// How a call treats the forward's costly values (quotients, square roots,
+// exp / log / pow; CELL_CK_SLOTS of them, each computed at most once):
+//   CA_FULL  computes them, then runs the reverse sweep;
+//   CA_SAVE  computes them and stores them to the cell's checkpoint, writes
+//            the cell outputs (those of nsw6_cell) and returns;
+//   CA_LOAD  reads them from the checkpoint instead, then runs the reverse.
+// The stored values are the computed ones, so every branch takes the same way
+// in all three.
+enum CellAdjMode { CA_FULL = 0, CA_SAVE = 1, CA_LOAD = 2 };
+constexpr int CELL_CK_SLOTS = 49;
+// Slot s of this cell's checkpoint at p[s * stride].
+struct CellCk {
+  double* p;
+  size_t stride;
+};
+template <int MODE>
+__device__ __forceinline__ double ck_keep(const CellCk& ck, int s, double v) {
+  if constexpr (MODE == CA_SAVE) ck.p[(size_t)s * ck.stride] = v;
+  return v;
+}
+// The value of expr (not evaluated under CA_LOAD) at slot s.
+#define NSW6_CK(s, expr) ((MODE == CA_LOAD) ? ck.p[(size_t)(s) * ck.stride] : ck_keep<MODE>(ck, (s), (expr)))
+
+template <int MODE = CA_FULL>
 __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMath& mth, double dt, double rdt,
-                                                  const CellIn& in, const CellBar& ob, CellInBar& ib, double* pb) {
+                                                  const CellIn& in, const CellBar& ob, CellInBar& ib, double* pb,
+                                                  CellCk ck = {nullptr, 0}, CellOut* out = nullptr) {
   const double Z = 0.0, ONE = 1.0;
   // ==================================================================== forward
   // ---- negative_filter, mod_mp_nsw6.cpp:1770-1831
@@ -76,8 +101,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   d2 -= rq[0];
   const double omd = 1.0 - d2;
   const double rhog = in.rhog * omd;
-  const double rrhog = 1.0 / rhog;
-  const double dens = rhog / in.gsgam2;
+  const double rrhog = NSW6_CK(0, 1.0 / rhog);
+  const double dens = NSW6_CK(1, rhog / in.gsgam2);
   double qn[6];
   qn[0] = in.q0;
 #pragma unroll
@@ -97,15 +122,15 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
 
   // ---- psat / qsat
   const double tmx = dmax(temp, TEM_MIN);
-  const double rtem = 1.0 / tmx;
+  const double rtem = NSW6_CK(2, 1.0 / tmx);
   const double al = C.LovR_liq * (C.RTEM00 - rtem);
   const double ai = C.LovR_ice * (C.RTEM00 - rtem);
-  const double el = mth.exp(al), ei = mth.exp(ai);
+  const double el = NSW6_CK(3, mth.exp(al)), ei = NSW6_CK(4, mth.exp(ai));
   const double psatl = PSAT0 * el;
   const double psati = PSAT0 * ei;
   const double drv = dens * RVAP;
   const double drt = drv * temp;
-  const double rdrt = 1.0 / drt;
+  const double rdrt = NSW6_CK(5, 1.0 / drt);
   const double qsatl = psatl * rdrt;
   const double qsati = psati * rdrt;
 
@@ -113,11 +138,11 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   const double qv = dmax(qn[0], Z), qc = dmax(qn[1], Z), qr = dmax(qn[2], Z);
   const double qi = dmax(qn[3], Z), qs = dmax(qn[4], Z), qg = dmax(qn[5], Z);
   const double sld = dmax(qsatl, EPS), sid = dmax(qsati, EPS);
-  const double Sliq = qv / sld;
-  const double Sice = qv / sid;
-  const double Rdens = ONE / dens;
+  const double Sliq = NSW6_CK(6, qv / sld);
+  const double Sice = NSW6_CK(7, qv / sid);
+  const double Rdens = NSW6_CK(8, ONE / dens);
   const double rfa = DENS00 * Rdens;
-  const double rho_fact = sqrt(rfa);
+  const double rho_fact = NSW6_CK(9, sqrt(rfa));
   const double temc = temp - TEM00;
   const bool warm = !(temc < Z);
   const bool d1 = (qr >= 1.0E-4);
@@ -135,9 +160,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   if (rain) {
     r_a = dens * qr;
     r_b = r_a * C.K_rlmdr;
-    r_s1 = sqrt(r_b);
-    RLMDr = sqrt(r_s1);
-    RLMDr_dr = sqrt(RLMDr);
+    r_s1 = NSW6_CK(10, sqrt(r_b));
+    RLMDr = NSW6_CK(11, sqrt(r_s1));
+    RLMDr_dr = NSW6_CK(12, sqrt(RLMDr));
     RLMDr_2 = RLMDr * RLMDr;
     RLMDr_3 = RLMDr_2 * RLMDr;
     RLMDr_1br = RLMDr_2 * RLMDr_2;
@@ -161,7 +186,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   if (snow) {
     tems_sel = temc < -0.1;   // dmin(-0.1, temc) is temc
     tems = tems_sel ? temc : -0.1;
-    logX = mth.log(Xs2);
+    logX = NSW6_CK(13, mth.log(Xs2));
 #pragma unroll
     for (int i = 0; i < 7; ++i) {
       const double* a = C.roh_a + 4 * i;
@@ -169,9 +194,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
       const double la = __fma_rn(__fma_rn(__fma_rn(a[3], tems, a[2]), tems, a[1]), tems, a[0]);
       const double lb = __fma_rn(__fma_rn(__fma_rn(b[3], tems, b[2]), tems, b[1]), tems, b[0]);
       mlb[i] = lb;
-      mom[i] = mth.exp(__fma_rn(logX, lb, la));
+      mom[i] = NSW6_CK(14 + i, mth.exp(__fma_rn(logX, lb, la)));
     }
-    RMOMs_Vt = mom[5] / mom[2];
+    RMOMs_Vt = NSW6_CK(21, mom[5] / mom[2]);
   }
   const double MOMs_0 = mom[0], MOMs_1 = mom[1], MOMs_2 = Xs2;
   const double MOMs_0bs = mom[2], MOMs_1bs = mom[3], MOMs_2bs = mom[4], MOMs_2ds = mom[5];
@@ -184,9 +209,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   if (graupel) {
     g_a = dens * qg;
     g_b = g_a * C.K_rlmdg;
-    g_s1 = sqrt(g_b);
-    RLMDg = sqrt(g_s1);
-    RLMDg_dg = sqrt(RLMDg);
+    g_s1 = NSW6_CK(22, sqrt(g_b));
+    RLMDg = NSW6_CK(23, sqrt(g_s1));
+    RLMDg_dg = NSW6_CK(24, sqrt(RLMDg));
     RLMDg_2 = RLMDg * RLMDg;
     RLMDg_3 = RLMDg_2 * RLMDg;
     RLMDg_3dg = RLMDg_3 * RLMDg_dg;
@@ -206,7 +231,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   const double nm01 = -0.1 * temc;
   const double nmax = dmax(nm01, Z);
   const double nex = 1.33 * (C.ln1000 + nmax);
-  const double nexp = mth.exp(nex);
+  const double nexp = NSW6_CK(25, mth.exp(nex));
   const double qi0a = C.ice_nuc * nexp;
   const double Qi0 = qi0a * Rdens;
   const double pg1 = Qi0 - qi, pg2 = qv - qsati;
@@ -219,7 +244,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   bool esi_exp = false, bet_exp = false;   // Esi_mod / betai took the exponential branch of min
   const bool cold_branch = !(warm && C.Esi >= Z && C.beta_saut >= Z);
   if (cold_branch) {
-    eg = mth.exp(C.gamma_sacr * temc);
+    eg = NSW6_CK(26, mth.exp(C.gamma_sacr * temc));
     const double es = C.Esi * eg;
     esi_exp = es < C.Esi;
     Esi_mod = esi_exp ? es : C.Esi;
@@ -231,7 +256,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   double Pracw = Z, prw_pow = Z;
   const bool prw_on = (qcqr >= 1.0E-12);
   if (prw_on) {
-    prw_pow = mth.pow(qcqr, 1.15);
+    prw_pow = NSW6_CK(27, mth.pow(qcqr, 1.15));
     Pracw = 67.0 * prw_pow;
   }
   const double fr = rho_fact;
@@ -274,7 +299,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   double Praut = Z, aut_pow = Z;
   const bool aut_on = qc > Z;
   if (aut_on) {
-    aut_pow = mth.pow(qc, 2.47);
+    aut_pow = NSW6_CK(28, mth.pow(qc, 2.47));
     Praut = C.K_aut * aut_pow;
   }
   const double saut_a = qi - C.qicrt_saut;
@@ -285,12 +310,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   const double Ka = (2.428E-2 + 7.47E-5 * temc);
   const double kd0 = (2.222E-5 + 1.37E-7 * temc);
   const double kd1 = kd0 * PSTD;
-  const double kd2 = kd1 / pre;
+  const double kd2 = NSW6_CK(29, kd1 / pre);
   const double KdD = kd2 * dens;
   const double nu0 = (1.718E-5 + 5.28E-8 * temc);
-  const double rNu = dens / nu0;
+  const double rNu = NSW6_CK(30, dens / nu0);
   const double kat = Ka * temp;
-  const double rKaT = ONE / kat;
+  const double rKaT = NSW6_CK(31, ONE / kat);
   const double xi = KdD * qsati;
   const double gv1 = LHS0 * rKaT;
   const double gv2 = C.LovR_ice * rtem;
@@ -298,7 +323,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   const double gv4 = gv1 * gv3;
   const double gv5 = gv4 * xi;
   const double gv6 = gv5 + ONE;
-  const double Giv = xi / gv6;
+  const double Giv = NSW6_CK(32, xi / gv6);
   const double gil_a = Ka * temc;
   const double Gil = gil_a * C.rLHF0;
   double Prevp = Z;
@@ -314,12 +339,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     gl4 = gl1 * gl3;
     gl5 = gl4 * xl;
     gl6 = gl5 + ONE;
-    Glv = xl / gl6;
+    Glv = NSW6_CK(33, xl / gl6);
     vr1 = C.K_ventr1 * RLMDr_2;
     vr2 = C.Cr * fr;
     vr3 = vr2 * rNu;
     vr4 = vr3 * RLMDr_5dr;
-    vr5 = sqrt(vr4);
+    vr5 = NSW6_CK(34, sqrt(vr4));
     vr6 = C.K_ventr2 * vr5;
     ventr = vr1 + vr6;
     ev1 = C.K_revp * Rdens;
@@ -337,14 +362,14 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   bool xn_lo = false, xn_hi = false, di_cap = false;
   const bool ice_on = rhoqi > EPS;
   if (ice_on) {
-    xn_pow = mth.pow(rhoqi, 0.75);
+    xn_pow = NSW6_CK(35, mth.pow(rhoqi, 0.75));
     xn_a = 5.38E+7 * xn_pow;
     xn_lo = xn_a < 1.0E+3;             // dmax(xn_a, 1e3) gives 1e3
     const double xm = xn_lo ? 1.0E+3 : xn_a;
     xn_hi = 1.0E+6 < xm;               // dmin(xm, 1e6) gives 1e6
     XNi = xn_hi ? 1.0E+6 : xm;
-    XMi = rhoqi / XNi;
-    di_s = sqrt(XMi);
+    XMi = NSW6_CK(36, rhoqi / XNi);
+    di_s = NSW6_CK(37, sqrt(XMi));
     di_a = C.Di_a * di_s;
     di_cap = C.Di_max < di_a;
     Di = di_cap ? C.Di_max : di_a;
@@ -356,7 +381,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   const bool below40 = (temc + 40.0 < Z);
   double Pihom = below40 ? dqc_dt : Z;
   const double efa = -C.A_frz * temc;
-  const double efe = mth.exp(efa);
+  const double efe = NSW6_CK(38, mth.exp(efa));
   const double efrz = efe - ONE;
   const bool htr_on = (!below40 && !warm);
   const double qc2 = qc * qc;
@@ -365,7 +390,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   double Pimlt = warm ? dqi_dt : Z;
   const double vs1 = 0.65 * MOMs_1;
   const double vs2 = fr * rNu;
-  const double vs3 = sqrt(vs2);
+  const double vs3 = NSW6_CK(39, sqrt(vs2));
   const double vs4 = C.K_vents2 * vs3;
   const double vs5 = vs4 * MOMs_5ds_h;
   const double vents = vs1 + vs5;
@@ -379,7 +404,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   double Psmlt = dmax(sm_f, Z);
   const double vg1 = C.K_ventg1 * RLMDg_2;
   const double vg2 = C.Cg * fr, vg3 = vg2 * rNu, vg4 = vg3 * RLMDg_5dg;
-  const double vg5 = sqrt(vg4);
+  const double vg5 = NSW6_CK(40, sqrt(vg4));
   const double vg6 = C.K_ventg2 * vg5;
   const double ventg = vg1 + vg6;
   const double g1a = C.K_gdep * Rdens, g1b = g1a * sm1, g1c = g1b * Giv;
@@ -442,14 +467,14 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     double net, fac;
     bool scaled, ratio;   // fac != 1; fac is -dq / net (else 1 from min)
   };
-  auto limit = [&](double net, double dq) {
+  auto limit = [&](int slot, double net, double dq) {
     Lim L;
     L.net = net;
     if (net + EPS >= Z) {
       L.fac = ONE;
       L.ratio = false;
     } else {
-      const double r = -dq / net;
+      const double r = NSW6_CK(slot, -dq / net);
       L.ratio = !(ONE < r);
       L.fac = L.ratio ? r : ONE;
     }
@@ -458,21 +483,21 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   };
   // [QC]
   const double QC_in[7] = {Pimlt, Praut, Pracw, Pihom, Pihtr, Psacw, Pgacw};
-  const Lim Lc = limit(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw, dqc_dt);
+  const Lim Lc = limit(41, +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw, dqc_dt);
   if (Lc.scaled) {
     Pimlt *= Lc.fac; Praut *= Lc.fac; Pracw *= Lc.fac; Pihom *= Lc.fac; Pihtr *= Lc.fac; Psacw *= Lc.fac;
     Pgacw *= Lc.fac;
   }
   // [QI]
   const double QI_in[10] = {Pigen, Pidep, Pihom, Pihtr, Pisub, Pimlt, Psaut, Praci_s, Psaci, Praci_g};
-  const Lim Li = limit(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g, dqi_dt);
+  const Lim Li = limit(42, +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g, dqi_dt);
   if (Li.scaled) {
     Pigen *= Li.fac; Pidep *= Li.fac; Pihom *= Li.fac; Pihtr *= Li.fac; Pisub *= Li.fac; Pimlt *= Li.fac;
     Psaut *= Li.fac; Praci_s *= Li.fac; Psaci *= Li.fac; Praci_g *= Li.fac;
   }
   // [QR]
   const double QR_in[11] = {Praut, Pracw, Psmlt, Pgmlt, Prevp, Piacr_s, Psacr_s, Piacr_g, Psacr_g, Pgacr, Pgfrz};
-  const Lim Lr = limit(+Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz,
+  const Lim Lr = limit(43, +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz,
                        dqr_dt);
   if (Lr.scaled) {
     Praut *= Lr.fac; Pracw *= Lr.fac; Psmlt *= Lr.fac; Pgmlt *= Lr.fac; Prevp *= Lr.fac; Piacr_s *= Lr.fac;
@@ -480,21 +505,21 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   }
   // [QV]
   const double QV_in[8] = {Prevp, Pisub, Pssub, Pgsub, Pigen, Pidep, Psdep, Pgdep};
-  const Lim Lv = limit(+Prevp + Pisub + Pssub + Pgsub - Pigen - Pidep - Psdep - Pgdep, dqv_dt);
+  const Lim Lv = limit(44, +Prevp + Pisub + Pssub + Pgsub - Pigen - Pidep - Psdep - Pgdep, dqv_dt);
   if (Lv.scaled) {
     Prevp *= Lv.fac; Pisub *= Lv.fac; Pssub *= Lv.fac; Pgsub *= Lv.fac; Pigen *= Lv.fac; Pidep *= Lv.fac;
     Psdep *= Lv.fac; Pgdep *= Lv.fac;
   }
   // [QS]
   const double QS_in[10] = {Psdep, Psacw, Piacr_s, Psacr_s, Psaut, Praci_s, Psaci, Pssub, Psmlt, Pracs};
-  const Lim Ls = limit(+Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs, dqs_dt);
+  const Lim Ls = limit(45, +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs, dqs_dt);
   if (Ls.scaled) {
     Psdep *= Ls.fac; Psacw *= Ls.fac; Piacr_s *= Ls.fac; Psacr_s *= Ls.fac; Psaut *= Ls.fac; Praci_s *= Ls.fac;
     Psaci *= Ls.fac; Pssub *= Ls.fac; Psmlt *= Ls.fac; Pracs *= Ls.fac;
   }
   // [QG]
   const double QG_in[10] = {Pgdep, Pgacw, Piacr_g, Psacr_g, Pgacr, Pgfrz, Praci_g, Pracs, Pgsub, Pgmlt};
-  const Lim Lg = limit(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt, dqg_dt);
+  const Lim Lg = limit(46, +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt, dqg_dt);
   if (Lg.scaled) {
     Pgdep *= Lg.fac; Pgacw *= Lg.fac; Piacr_g *= Lg.fac; Psacr_g *= Lg.fac; Pgacr *= Lg.fac; Pgfrz *= Lg.fac;
     Praci_g *= Lg.fac; Pracs *= Lg.fac; Pgsub *= Lg.fac; Pgmlt *= Lg.fac;
@@ -523,7 +548,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   const double xf1 = rhoqc * C.K_xf;
   const double xf2 = C.coef_xf * xf1;
   const double xf3 = xf2 + EPS;
-  const double rf_qc = mth.pow(xf3, 0.33333333);
+  const double rf_qc = NSW6_CK(47, mth.pow(xf3, 0.33333333));
   const double rf2 = rf_qc * rf_qc;
   const double r2_qc = C.K_r2c * rf2;
   const double r2_qr = C.K_r2r * RLMDr_3;
@@ -550,7 +575,27 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
 #pragma unroll
   for (int n = 1; n <= 5; ++n) cva = cva + q2[n] * CVDRY;
   const double rcva = rhog * cva;
-  const double tem_o = rhoge / rcva;
+  const double tem_o = NSW6_CK(48, rhoge / rcva);
+  if constexpr (MODE == CA_SAVE) {
+    // the outputs of nsw6_cell (the same operations on the same values)
+    out->Vtr = Vtr;
+    out->Vts = Vts;
+    out->Vtg = Vtg;
+    out->Vti = 0.0;
+    out->rceff = big ? r3 / r2 : Z;
+    out->rctop = top ? out->rceff : UNDEF;
+    out->tctop = top ? temp : UNDEF;
+    out->rceff_cld = cld ? r3_qc / r2_qc : 0.0;
+#pragma unroll
+    for (int n = 0; n < 6; ++n) {
+      out->q[n] = q2[n];
+      out->rhogq[n] = rq2[n];
+    }
+    out->tem = tem_o;
+    out->rhog = rhog;
+    out->rhoge = rhoge;
+    return;
+  }
 
   // ==================================================================== reverse
   // adjoints of the outputs
@@ -1302,5 +1347,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   pb[5] += b_icenuc;
   pb[6] += b_K_aut * C.K_aut / C.kk_aut;
 }
+
+#undef NSW6_CK
 
 }  // namespace nsw6

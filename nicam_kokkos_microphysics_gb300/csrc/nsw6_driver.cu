@@ -32,7 +32,10 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
                                      int recorded, cudaStream_t stream);
 cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
-                               double* pbar, cudaStream_t stream);
+                               double* pbar, double* ck, cudaStream_t stream);
+cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, double* ck, int check,
+                                 cudaStream_t stream);
+size_t adj_cell_ck_doubles(int lall, int kall, int gall);
 size_t adj_stage_work_doubles(int lall, int kall, int gall);
 size_t adj_stage_bound_ints(int lall, int kall);
 int adj_stage_tape_cap();
@@ -75,6 +78,7 @@ struct nsw6_handle {
   double* d_swork = nullptr;   // work fields, their adjoints and the seeds of the staged column adjoint
   int* d_sbnd = nullptr;       // flux bounds of the staged column adjoint
   int* d_done = nullptr;       // per-cell flags of the cell adjoint
+  double* d_cellck = nullptr;  // checkpoint of the cell physics' costly forward values
   int adj_mode = 0;            // cell-phase adjoint: 0 hand-written, 1 recorded tape
   double* d_Y = nullptr;   // cell-phase outputs and their adjoints [2][nfields][lall_max][kall][gall]
   // captured step graph of mp_driver_steps and what it was captured for
@@ -774,6 +778,7 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_swork);
   cudaFree(h->d_sbnd);
   cudaFree(h->d_done);
+  cudaFree(h->d_cellck);
   cudaFree(h->d_Y);
   for (auto& tri : h->ev)
     for (auto& e : tri)
@@ -850,7 +855,7 @@ int nsw6_set_math(nsw6_handle* h, int mode) {
 }
 
 int nsw6_set_adjoint_mode(nsw6_handle* h, int mode) {
-  if (!h || mode < 0 || mode > 1) return NSW6_ERR_BAD_ARG;
+  if (!h || mode < 0 || mode > 2) return NSW6_ERR_BAD_ARG;
   h->adj_mode = mode;
   return NSW6_OK;
 }
@@ -906,6 +911,7 @@ const char* nsw6_strerror(int status) {
     case NSW6_ERR_NOCONV: return "saturation adjustment did not converge";
     case NSW6_ERR_NAN: return "saturation adjustment produced a non-finite temperature";
     case NSW6_ERR_UNSUPPORTED: return "unsupported configuration";
+    case NSW6_ERR_CHECK: return "adjoint self-check: the adjoint's forward differs from the step's";
     case NSW6_ERR_TOO_LARGE:
       return "region too large for mp_driver_noalloc (needs 5 <= kall <= 160 and gall * kall <= 2097152)";
     default: return "unknown status";
@@ -1128,21 +1134,30 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
         cudaMalloc(&h->d_done, sizeof(int) * (size_t)h->lall_max * h->kall * h->gall) != cudaSuccess)
       return NSW6_ERR_CUDA;
   }
-  if ((rc = ensure_tape(h->stape, h->stape_bytes, adj_stage_slots(), adj_stage_tape_cap())) != NSW6_OK) return rc;
+  // the stage tapes serve only the recorded form (adj_mode 1)
+  if (h->adj_mode == 1 &&
+      (rc = ensure_tape(h->stape, h->stape_bytes, adj_stage_slots(), adj_stage_tape_cap())) != NSW6_OK)
+    return rc;
   h->stape.count_only = 0;
   double pb[8] = {};
   // the cell phase's outputs, then the column phase's adjoint (level-parallel stages)
-  if (launch_adj_cellfwd(P, h->C, x, Y, h->stream) != cudaSuccess ||
-      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->adj_mode, h->stream) !=
-          cudaSuccess ||
+  const bool recorded = h->adj_mode == 1;
+  if (!recorded && !h->d_cellck &&
+      cudaMalloc(&h->d_cellck, sizeof(double) * adj_cell_ck_doubles(h->lall_max, h->kall, h->gall)) != cudaSuccess)
+    return NSW6_ERR_CUDA;
+  if ((recorded ? launch_adj_cellfwd(P, h->C, x, Y, h->stream)
+                : launch_adj_cell_save(P, h->C, x, Y, h->d_cellck, h->adj_mode == 2, h->stream)) != cudaSuccess ||
+      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, recorded,
+                               h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
-      cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess)
+      (recorded && cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess))
     return NSW6_ERR_CUDA;
   // the cell phase's adjoint: hand-written, or (adj_mode 1) recorded on a tape
   // as long as the longest cell's record (measured once, then kept; a longer
   // record makes the launch repeat for the cells that did not fit)
-  if (h->adj_mode == 0) {
-    if (launch_adj_cell_hw(P, h->C, x, xb, YB, h->d_pbar, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (!recorded) {
+    if (launch_adj_cell_hw(P, h->C, x, xb, YB, h->d_pbar, h->d_cellck, h->stream) != cudaSuccess)
+      return NSW6_ERR_CUDA;
   } else {
     for (int attempt = 0; attempt < 3; ++attempt) {
       if (!h->ctape.pa || attempt > 0) {

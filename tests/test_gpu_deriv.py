@@ -87,6 +87,34 @@ def test_adjoint_dot_product():
     drv.close()
 
 
+@pytest.mark.parametrize("variant,seed", [("standard", 41), ("convective", 42), ("cold", 43)])
+def test_adjoint_forward_checkpoint_bitwise(variant, seed):
+    """The hand-written forward the cell adjoint's checkpoint comes from gives
+    the step's cell-physics outputs bit for bit on every cell (adjoint mode
+    "check" compares them in the kernel and fails the call otherwise), and the
+    checked adjoint equals the plain one up to the order of its atomic sums
+    (some input adjoints are sums that cancel, so the bound is relative to
+    the field's largest entry)."""
+    torch, drv, spec, st, x0 = _setup(1024, 42, 2, seed, variant)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    ybar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    for n in WRITE_NAMES:
+        ybar[n] = torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64)
+    drv.set_adjoint_mode("check")
+    b2 = _clone(ybar)
+    p2 = drv.adjoint(spec.lall, _clone(x0), b2, dt=spec.dt)
+    drv.set_adjoint_mode("hand")
+    b0 = _clone(ybar)
+    p0 = drv.adjoint(spec.lall, _clone(x0), b0, dt=spec.dt)
+    for n in READ_NAMES:
+        scale = float(b0[n].abs().max())
+        if scale > 0.0:
+            err = float((b2[n] - b0[n]).abs().max()) / scale
+            assert err <= 1e-9, (n, err)
+    assert np.allclose(p2, p0, rtol=1e-9, atol=0.0)
+    drv.close()
+
+
 @pytest.mark.parametrize("variant,seed", [("standard", 31), ("convective", 32), ("cold", 33)])
 def test_hand_written_adjoint_equals_recorded(variant, seed):
     """The hand-written adjoints of the cell physics and of the column phase's
