@@ -961,16 +961,16 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double B_pre = SB[SF_PRE * NC + c], B_rhoge = SB[SF_RHOGE * NC + c];
       double b_rhog_o = SB[SF_RHOG * NC + c];
       // pre = ((rho_f pq_f) tem)
-      b_tem += B_pre * rho_f * pq_f;
+      b_tem = fma(B_pre * rho_f, pq_f, b_tem);
       double b_rho_f = SB[SF_RHO * NC + c] + B_pre * tem * pq_f;
       const double b_pq = B_pre * tem * rho_f;
       double b_qdf = b_pq * RDRY;
-      b_q[I_QV] += b_pq * RVAP;
+      b_q[I_QV] = fma(b_pq, RVAP, b_q[I_QV]);
       // rhoge = (tem rhog_o) cva
-      b_tem += B_rhoge * rhog_o * cva;
-      b_rhog_o += B_rhoge * tem * cva;
+      b_tem = fma(B_rhoge * rhog_o, cva, b_tem);
+      b_rhog_o = fma(B_rhoge * tem, cva, b_rhog_o);
       const double b_cva = B_rhoge * tem * rhog_o;
-      b_qdf += b_cva * CVDRY;
+      b_qdf = fma(b_cva, CVDRY, b_qdf);
       double b_qf[6];
 #pragma unroll
       for (int n = 1; n <= 5; ++n) b_qf[n] = b_q[n] + b_cva * CVDRY - b_qdf;
@@ -980,13 +980,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       for (int n = 0; n < 6; ++n) b_rqf[n] = SB[(SF_RQ + n) * NC + c];
 #pragma unroll
       for (int n = 1; n <= 5; ++n) {
-        b_rqf[n] += b_qf[n] * rrhog_o;
-        b_rhog_o -= b_qf[n] * qf[n] * rrhog_o;
+        b_rqf[n] = fma(b_qf[n], rrhog_o, b_rqf[n]);
+        b_rhog_o = fma(-(b_qf[n] * qf[n]), rrhog_o, b_rhog_o);
       }
-      b_rhog_o += b_rho_f * rgsg;
-      b_gsg -= b_rho_f * rho_f * rgsg;
+      b_rhog_o = fma(b_rho_f, rgsg, b_rhog_o);
+      b_gsg = fma(-(b_rho_f * rho_f), rgsg, b_gsg);
       // rhog_o = rhog (1 - d2)
-      b_rhog += b_rhog_o * (1.0 - d2);
+      b_rhog = fma(b_rhog_o, (1.0 - d2), b_rhog);
       const double b_d2 = -b_rhog_o * rhog;
       const double b_rq0a = (clip[0] ? b_d2 : 0.0) + (clip[0] ? 0.0 : b_rqf[0]);
       b_rq2[0] = b_rq0a;
@@ -1006,17 +1006,17 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     }
     // rhoge2 = (rhog tem) cvtot2 (the output at the halo levels)
     if (b_rhoge2 != 0.0) {
-      b_rhog += b_rhoge2 * tem * cvtot2;
-      b_tem += b_rhoge2 * rhog * cvtot2;
+      b_rhog = fma(b_rhoge2 * tem, cvtot2, b_rhog);
+      b_tem = fma(b_rhoge2 * rhog, cvtot2, b_tem);
       const double b_cv2 = b_rhoge2 * rhog * tem;
-      b_qd += b_cv2 * CVDRY;
+      b_qd = fma(b_cv2, CVDRY, b_qd);
 #pragma unroll
       for (int n = 1; n <= 5; ++n) b_q[n] += b_cv2 * CVDRY;
     }
     // rq2[QV] = rhog q[QV], rq2[QC] = rhog q[QC]; rq2[n >= 2] = rq[n]
     b_rhog += b_rq2[I_QV] * q[I_QV] + b_rq2[I_QC] * q[I_QC];
-    b_q[I_QV] += b_rq2[I_QV] * rhog;
-    b_q[I_QC] += b_rq2[I_QC] * rhog;
+    b_q[I_QV] = fma(b_rq2[I_QV], rhog, b_q[I_QV]);
+    b_q[I_QC] = fma(b_rq2[I_QC], rhog, b_q[I_QC]);
     double b_rq[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
     for (int n = 2; n <= 5; ++n) b_rq[n] += b_rq2[n];
@@ -1030,14 +1030,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double b_temI = b_tem + b_qsI * dqs;
       const double b_F = -b_temI * (1.0 / FT);
       const double b_cvT = b_F * ts;
-      b_qsT += b_F * LHV0;
+      b_qsT = fma(b_F, LHV0, b_qsT);
       b_ein_moist -= b_F;
       const double b_qd_l = b_cvT * CVDRY;
-      b_qsum += b_cvT * CVDRY;
-      b_qsT -= b_cvT * CVDRY;
+      b_qsum = fma(b_cvT, CVDRY, b_qsum);
+      b_qsT = fma(-b_cvT, CVDRY, b_qsT);
 #pragma unroll
       for (int n = 2; n <= 5; ++n) b_q[n] += b_cvT * CVDRY - b_qd_l;
-      b_rho_l -= b_qsT * qsT * (gsg * rrhog);
+      b_rho_l = fma(-(b_qsT * qsT), (gsg * rrhog), b_rho_l);
     } else {
       b_tem_p = b_tem;
       b_q0p = b_q[I_QV];
@@ -1048,8 +1048,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double b_num = b_tem_p * rcv1;
       const double b_cv1 = -b_tem_p * tem_p * rcv1;
       b_ein_moist += b_num;
-      b_qsum -= b_num * LHV0;
-      b_qd += b_cv1 * CVDRY;
+      b_qsum = fma(-b_num, LHV0, b_qsum);
+      b_qd = fma(b_cv1, CVDRY, b_qd);
 #pragma unroll
       for (int n = 2; n <= 5; ++n) b_q[n] += b_cv1 * CVDRY;
     }
@@ -1064,13 +1064,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     double b_ein = b_ein_moist;
     // pre0 = (rho1 tem0) pq0 (halo output)
     if (b_pre0 != 0.0) {
-      b_rho1 += b_pre0 * tem0 * pq0;
+      b_rho1 = fma(b_pre0 * tem0, pq0, b_rho1);
       const double b_tem0 = b_pre0 * rho1 * pq0;
       const double b_pq0 = b_pre0 * rho1 * tem0;
       const double b_qdl0 = b_pq0 * RDRY;
-      b_qo[0] += b_pq0 * RVAP;
+      b_qo[0] = fma(b_pq0, RVAP, b_qo[0]);
       const double rcvt = 1.0 / cvt;
-      b_ein += b_tem0 * rcvt;
+      b_ein = fma(b_tem0, rcvt, b_ein);
       const double b_cvt = -b_tem0 * tem0 * rcvt;
       const double b_qdl = b_qdl0 + b_cvt * CVDRY;
 #pragma unroll
@@ -1081,13 +1081,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     for (int n = 1; n <= 5; ++n) b_qo[n] -= b_qd;
     // ein = rhoge / rhog, rho1 = rhog / gsg, qo = rq / rhog
     double b_rhoge = b_ein * rrhog;
-    b_rhog -= b_ein * ein * rrhog;
-    b_rhog += b_rho1 * rgsg;
-    b_gsg -= b_rho1 * rho1 * rgsg;
+    b_rhog = fma(-(b_ein * ein), rrhog, b_rhog);
+    b_rhog = fma(b_rho1, rgsg, b_rhog);
+    b_gsg = fma(-(b_rho1 * rho1), rgsg, b_gsg);
 #pragma unroll
     for (int n = 0; n < 6; ++n) {
-      b_rq[n] += b_qo[n] * rrhog;
-      b_rhog -= b_qo[n] * qo[n] * rrhog;
+      b_rq[n] = fma(b_qo[n], rrhog, b_rq[n]);
+      b_rhog = fma(-(b_qo[n] * qo[n]), rrhog, b_rhog);
     }
     // KIN2EIN
     if (interior) {
@@ -1099,7 +1099,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       double b_w2c1 = b_tmp2 * kv0 + b_tmp * kvu[1];
       const double b_tmp_h = b_tmp;
       const double b_sq = b_tmp_h * rrhog;
-      b_rhog -= b_tmp_h * tmp_h * rrhog;
+      b_rhog = fma(-(b_tmp_h * tmp_h), rrhog, b_rhog);
       WBadd(W_RVX_N, c, b_sq * rvx);
       WBadd(W_RVY_N, c, b_sq * rvy);
       WBadd(W_RVZ_N, c, b_sq * rvz);
@@ -1121,7 +1121,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
         XBadd(A_gsgam2, cj - G, -b_c2b * c2b[s2] * rgjm);
       }
       // w2c0 = cfact gsg / gh, w2c1 = dfact gsg / gh
-      b_gsg += (b_w2c0 * cfact[k] + b_w2c1 * dfact[k]) * rgh;
+      b_gsg = fma((b_w2c0 * cfact[k] + b_w2c1 * dfact[k]), rgh, b_gsg);
       XBadd(A_gsgam2h, c + G, -(b_w2c0 * w2c0 + b_w2c1 * w2c1) * rgh);
       WBadd(W_RHOGE_N, c, b_rhoge);
     } else {
@@ -1155,7 +1155,7 @@ __device__ __forceinline__ void zdis_wh_bar(double wm, double w0, double wpp, co
   const double b_c = bz * sdt3 * w0 * w0;
   double b_w0 = bz * (-hdt2 * r + dt + sdt3 * (2.0 * w0 * c + r * r));
   const double b_d = b_c * 2.0 * rs;
-  b_w0 -= b_d * (rdz[k] + rdz[k - 1]);
+  b_w0 = fma(-b_d, (rdz[k] + rdz[k - 1]), b_w0);
   bw[0] = -b_r * rs + b_d * rdz[k - 1];
   bw[1] = b_w0;
   bw[2] = b_r * rs + b_d * rdz[k];
@@ -1294,22 +1294,22 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
       const double rq = Y(YS_RHOGQ + nq, c), qn = Y(YS_Q + nq - 1, c);
       const double base = rq * rgs;
       const double b_base = b0 + b1 * CVDRY * tem + b2 * GRAV * zz + b4 * vi + b5 * vj;
-      b_tem += b1 * base * CVDRY;
-      b_zz += b2 * base * GRAV;
-      b_vi += b4 * base;
-      b_vj += b5 * base;
+      b_tem = fma(b1 * base, CVDRY, b_tem);
+      b_zz = fma(b2 * base, GRAV, b_zz);
+      b_vi = fma(b4, base, b_vi);
+      b_vj = fma(b5, base, b_vj);
       double b_qn = b3 * rgs * kinh;
       b_rgs += b3 * qn * kinh + b_base * rq;
-      b_kinh += b3 * qn * rgs;
+      b_kinh = fma(b3 * qn, rgs, b_kinh);
       if (hk) {
         const double qm = Y(YS_Q + nq - 1, c - G);
         const double qh = 0.5 * (qn + qm) * rgsh;
         const double b_qh = b6 * kinv + b7 * rw;
-        b_kinv += b6 * qh;
-        b_rw += b7 * qh;
-        b_qn += b_qh * 0.5 * rgsh;
+        b_kinv = fma(b6, qh, b_kinv);
+        b_rw = fma(b7, qh, b_rw);
+        b_qn = fma(b_qh * 0.5, rgsh, b_qn);
         YBadd(YS_Q + nq - 1, c - G, b_qh * 0.5 * rgsh);
-        b_rgsh += b_qh * 0.5 * (qn + qm);
+        b_rgsh = fma(b_qh * 0.5, (qn + qm), b_rgsh);
       }
       YBadd(YS_Q + nq - 1, c, b_qn);
       YBown(YS_RHOGQ + nq, c, b_base * rgs);
@@ -1321,20 +1321,20 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
       // rgsh = gam2h / gsgam2h; kinv = 0.5 rw^2 / (c2w0 rhog(k) + c2w1 rhog(k-1))
       double b_gh = -b_rgsh * rgsh * rgh;
       XBown(A_gam2h, ck, b_rgsh * rgh);
-      b_rw += b_kinv * rw * rden;
+      b_rw = fma(b_kinv * rw, rden, b_rw);
       const double b_den = -b_kinv * kinv * rden;
-      b_rhog += b_den * c2w0;
+      b_rhog = fma(b_den, c2w0, b_rhog);
       YBadd(YS_RHOG, c - G, b_den * c2w1);
       const double b_c2w0 = b_den * rhog, b_c2w1 = b_den * rhogm;
       b_gh += b_c2w0 * (afact[k] * rgsr) + b_c2w1 * (bfact[k] * rgsm);
-      b_gs -= b_c2w0 * c2w0 * rgsr;
+      b_gs = fma(-(b_c2w0 * c2w0), rgsr, b_gs);
       XBadd(A_gsgam2, ck - G, -b_c2w1 * c2w1 * rgsm);
       XBown(A_gsgam2h, ck, b_gh);
       XBown(A_rhogw, ck, b_rw);
     }
     // kinh = 0.5 (rvx^2 + rvy^2 + rvz^2) / rhog
     const double b_sq = b_kinh * rrhog;
-    b_rhog -= b_kinh * kinh * rrhog;
+    b_rhog = fma(-(b_kinh * kinh), rrhog, b_rhog);
     XBown(A_rhogvx, ck, b_sq * rvx);
     XBown(A_rhogvy, ck, b_sq * rvy);
     XBown(A_rhogvz, ck, b_sq * rvz);
@@ -1350,7 +1350,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     XBadd(A_jz, cc, b_vj * vz);
     // rgs = gam2 / gsgam2
     XBown(A_gam2, ck, b_rgs * rgsr);
-    b_gs -= b_rgs * rgs * rgsr;
+    b_gs = fma(-(b_rgs * rgs), rgsr, b_gs);
     XBadd(A_gsgam2, ck, b_gs);
     YBadd(YS_RHOG, c, b_rhog);
   }
@@ -1566,7 +1566,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_hw_kernel(StageIO io) {
             atomicAdd(bs + (size_t)k2 * G, gF * (k2 > kc ? dz[k2] : -dz[k2]));
           }
         if (zd != 0.0) atomicAdd(bs + (size_t)kc * G, gF * zd);
-        b_z += gF * io.W[(size_t)src * NC + (c - (size_t)k * G) + (size_t)kc * G];
+        b_z = fma(gF, io.W[(size_t)src * NC + (c - (size_t)k * G) + (size_t)kc * G], b_z);
       }
       io.WB[(W_ZDIS + r) * NC + c] += b_z;
     }

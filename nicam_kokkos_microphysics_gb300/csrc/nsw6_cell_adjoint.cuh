@@ -610,9 +610,9 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   {
     const double g = ob.tem;
     const double rr = 1.0 / rcva;
-    b_rhoge += g * rr;
+    b_rhoge = fma(g, rr, b_rhoge);
     const double b_rcva = -g * tem_o * rr;
-    b_rhog += b_rcva * cva;
+    b_rhog = fma(b_rcva, cva, b_rhog);
     const double b_cva = b_rcva * rhog;
     // cva = qd2 CV + sum q2 CV
     const double b_qd2 = b_cva * CVDRY;
@@ -622,28 +622,28 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   // q2[n] = rq2[n] / rhog
 #pragma unroll
   for (int n = 1; n <= 5; ++n) {
-    b_rq2[n] += b_q2[n] * rrhog;
-    b_rhog -= b_q2[n] * q2[n] * rrhog;
+    b_rq2[n] = fma(b_q2[n], rrhog, b_rq2[n]);
+    b_rhog = fma(-(b_q2[n] * q2[n]), rrhog, b_rhog);
   }
   // rhoge = rhoge0 - LHV0 rqt0 dt + LHF0 (rqt3 + rqt4 + rqt5) dt
   double b_rhoge0 = b_rhoge;
   double b_rqt[6] = {0, 0, 0, 0, 0, 0};
-  b_rqt[0] -= b_rhoge * LHV0 * dt;
-  b_rqt[3] += b_rhoge * LHF0 * dt;
-  b_rqt[4] += b_rhoge * LHF0 * dt;
-  b_rqt[5] += b_rhoge * LHF0 * dt;
+  b_rqt[0] = fma(-(b_rhoge * LHV0), dt, b_rqt[0]);
+  b_rqt[3] = fma(b_rhoge * LHF0, dt, b_rqt[3]);
+  b_rqt[4] = fma(b_rhoge * LHF0, dt, b_rqt[4]);
+  b_rqt[5] = fma(b_rhoge * LHF0, dt, b_rqt[5]);
   // rq2 = rq + rqt dt
   double b_rq[6];
 #pragma unroll
   for (int n = 0; n < 6; ++n) {
     b_rq[n] = b_rq2[n];
-    b_rqt[n] += b_rq2[n] * dt;
+    b_rqt[n] = fma(b_rq2[n], dt, b_rqt[n]);
   }
   // rqt = rhog qt
   double b_qt[6];
 #pragma unroll
   for (int n = 0; n < 6; ++n) {
-    b_rhog += b_rqt[n] * qt[n];
+    b_rhog = fma(b_rqt[n], qt[n], b_rhog);
     b_qt[n] = b_rqt[n] * rhog;
   }
   // effective radius and cloud top: adjoints of the dens, qc, qr, RLMDr_3, temp they read
@@ -665,19 +665,19 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     // rceff_cld = cld ? r3_qc / r2_qc : 0
     if (cld) {
       const double rr2 = 1.0 / r2_qc;
-      b_r3_qc += ob.rceff_cld * rr2;
-      b_r2_qc -= ob.rceff_cld * (r3_qc * rr2) * rr2;
+      b_r3_qc = fma(ob.rceff_cld, rr2, b_r3_qc);
+      b_r2_qc = fma(-(ob.rceff_cld * (r3_qc * rr2)), rr2, b_r2_qc);
     }
     // r3_qc = (coef_xf dens) qc, r3_qr = (coef_xf dens) qr
-    b_qc += b_r3_qc * r3c_a;
-    b_qr += b_r3_qr * r3c_a;
-    b_dens += (b_r3_qc * qc + b_r3_qr * qr) * C.coef_xf;
+    b_qc = fma(b_r3_qc, r3c_a, b_qc);
+    b_qr = fma(b_r3_qr, r3c_a, b_qr);
+    b_dens = fma((b_r3_qc * qc + b_r3_qr * qr), C.coef_xf, b_dens);
     // r2_qr = K_r2r RLMDr_3
-    b_RLMDr_3 += b_r2_qr * C.K_r2r;
+    b_RLMDr_3 = fma(b_r2_qr, C.K_r2r, b_RLMDr_3);
     // r2_qc = K_r2c rf^2, rf = pow(xf3, 1/3)
     const double b_rf = b_r2_qc * C.K_r2c * 2.0 * rf_qc;
     const double b_xf3 = (xf3 > 0.0) ? b_rf * 0.33333333 * rf_qc / xf3 : 0.0;
-    b_rhoqc += b_xf3 * C.coef_xf * C.K_xf;
+    b_rhoqc = fma(b_xf3 * C.coef_xf, C.K_xf, b_rhoqc);
   }
   // Vt outputs
   double b_Vtr = ob.Vtr, b_Vts = ob.Vts, b_Vtg = ob.Vtg;
@@ -715,12 +715,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     if (!L.scaled) return;
     double b_fac = 0.0;
     for (int j = 0; j < n; ++j) {
-      b_fac += *bx[j] * xin[j];
+      b_fac = fma(*bx[j], xin[j], b_fac);
       *bx[j] *= L.fac;
     }
     if (L.ratio) {   // fac = -dq / net
       const double rnet = 1.0 / L.net;
-      b_dq -= b_fac * rnet;
+      b_dq = fma(-b_fac, rnet, b_dq);
       const double b_net = b_fac * dq * (rnet * rnet);
       for (int j = 0; j < n; ++j) *bx[j] += sgn[j] * b_net;
     }
@@ -818,100 +818,100 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   double b_K_aut = 0.0;
 
   // Pgfrz = (K_gfrz Rdens) efrz RLMDr_7
-  b_Rdens += bPgfrz * RLMDr_7 * efrz * C.K_gfrz;
-  b_efrz += bPgfrz * RLMDr_7 * gf_a;
-  b_RLMDr_7 += bPgfrz * gf_b;
+  b_Rdens = fma(bPgfrz * RLMDr_7 * efrz, C.K_gfrz, b_Rdens);
+  b_efrz = fma(bPgfrz * RLMDr_7, gf_a, b_efrz);
+  b_RLMDr_7 = fma(bPgfrz, gf_b, b_RLMDr_7);
   // Pgmlt = max(gm_b + sm_c gm_d, 0); gm_b = (g1a Gil) ventg; gm_d = Pgacw + Pgacr
   double b_ventg = 0.0, b_g1a = 0.0, b_sm_c = 0.0;
   {
     double b_f = 0.0, dummy = 0.0;
     bmax(gm_f, Z, bPgmlt, b_f, dummy);
-    b_g1a += b_f * ventg * Gil;
-    b_Gil += b_f * ventg * g1a;
-    b_ventg += b_f * gm_a;
-    b_sm_c += b_f * gm_d;
-    bPgacw += b_f * sm_c;
-    bPgacr += b_f * sm_c;
+    b_g1a = fma(b_f * ventg, Gil, b_g1a);
+    b_Gil = fma(b_f * ventg, g1a, b_Gil);
+    b_ventg = fma(b_f, gm_a, b_ventg);
+    b_sm_c = fma(b_f, gm_d, b_sm_c);
+    bPgacw = fma(b_f, sm_c, bPgacw);
+    bPgacr = fma(b_f, sm_c, bPgacr);
   }
   // Pgdep = sel(sps, tmp3), Pgsub = sel(!sps, -tmp3); tmp3 = (g1a sm1 Giv) ventg
   {
     const double b_t = (sps ? bPgdep : 0.0) - (!sps ? bPgsub : 0.0);
-    b_g1a += b_t * ventg * Giv * sm1;
-    b_Sice += b_t * ventg * Giv * g1a;
-    b_Giv += b_t * ventg * g1b;
-    b_ventg += b_t * g1c;
+    b_g1a = fma(b_t * ventg * Giv, sm1, b_g1a);
+    b_Sice = fma(b_t * ventg * Giv, g1a, b_Sice);
+    b_Giv = fma(b_t * ventg, g1b, b_Giv);
+    b_ventg = fma(b_t, g1c, b_ventg);
   }
   // g1a = K_gdep Rdens
-  b_Rdens += b_g1a * C.K_gdep;
+  b_Rdens = fma(b_g1a, C.K_gdep, b_Rdens);
   // ventg = K_ventg1 RLMDg_2 + K_ventg2 sqrt(Cg fr rNu RLMDg_5dg)
   {
-    b_RLMDg_2 += b_ventg * C.K_ventg1;
+    b_RLMDg_2 = fma(b_ventg, C.K_ventg1, b_RLMDg_2);
     const double b_vg5 = b_ventg * C.K_ventg2;
     const double b_vg4 = b_vg5 * bsqrt(vg5);
-    b_RLMDg_5dg += b_vg4 * vg3;
+    b_RLMDg_5dg = fma(b_vg4, vg3, b_RLMDg_5dg);
     const double b_vg3 = b_vg4 * RLMDg_5dg;
-    b_rNu += b_vg3 * vg2;
+    b_rNu = fma(b_vg3, vg2, b_rNu);
     const double b_vg2 = b_vg3 * rNu;
-    b_Cg += b_vg2 * fr;
-    b_rho_fact += b_vg2 * C.Cg;
+    b_Cg = fma(b_vg2, fr, b_Cg);
+    b_rho_fact = fma(b_vg2, C.Cg, b_rho_fact);
   }
   // Psmlt = max(sm_b + sm_c sm_d, 0); sm_b = (s1a Gil) vents; sm_d = Psacw + Psacr
   double b_vents = 0.0, b_s1a = 0.0;
   {
     double b_f = 0.0, dummy = 0.0;
     bmax(sm_f, Z, bPsmlt, b_f, dummy);
-    b_s1a += b_f * vents * Gil;
-    b_Gil += b_f * vents * s1a;
-    b_vents += b_f * sm_a;
-    b_sm_c += b_f * sm_d;
-    bPsacw += b_f * sm_c;
-    bPsacr += b_f * sm_c;
+    b_s1a = fma(b_f * vents, Gil, b_s1a);
+    b_Gil = fma(b_f * vents, s1a, b_Gil);
+    b_vents = fma(b_f, sm_a, b_vents);
+    b_sm_c = fma(b_f, sm_d, b_sm_c);
+    bPsacw = fma(b_f, sm_c, bPsacw);
+    bPsacr = fma(b_f, sm_c, bPsacr);
   }
   // sm_c = K_clf temc
-  b_temc += b_sm_c * C.K_clf;
+  b_temc = fma(b_sm_c, C.K_clf, b_temc);
   // Psdep / Pssub: tmp2 = (s1a sm1 Giv) vents
   {
     const double b_t = (sps ? bPsdep : 0.0) - (!sps ? bPssub : 0.0);
-    b_s1a += b_t * vents * Giv * sm1;
-    b_Sice += b_t * vents * Giv * s1a;
-    b_Giv += b_t * vents * s1b;
-    b_vents += b_t * s1c;
+    b_s1a = fma(b_t * vents * Giv, sm1, b_s1a);
+    b_Sice = fma(b_t * vents * Giv, s1a, b_Sice);
+    b_Giv = fma(b_t * vents, s1b, b_Giv);
+    b_vents = fma(b_t, s1c, b_vents);
   }
-  b_Rdens += b_s1a * C.K_2pi;
+  b_Rdens = fma(b_s1a, C.K_2pi, b_Rdens);
   // vents = 0.65 MOMs_1 + (K_vents2 sqrt(fr rNu)) MOMs_5ds_h
   {
-    b_mom[1] += b_vents * 0.65;
-    b_mom[6] += b_vents * vs4;
+    b_mom[1] = fma(b_vents, 0.65, b_mom[1]);
+    b_mom[6] = fma(b_vents, vs4, b_mom[6]);
     const double b_vs4 = b_vents * MOMs_5ds_h;
-    b_K_vents2 += b_vs4 * vs3;
+    b_K_vents2 = fma(b_vs4, vs3, b_K_vents2);
     const double b_vs2 = b_vs4 * C.K_vents2 * bsqrt(vs3);
-    b_rho_fact += b_vs2 * rNu;
-    b_rNu += b_vs2 * fr;
+    b_rho_fact = fma(b_vs2, rNu, b_rho_fact);
+    b_rNu = fma(b_vs2, fr, b_rNu);
   }
   // Pimlt = warm ? dqi_dt : 0
   if (warm) b_dqi += bPimlt;
   // Pihtr = htr_on ? (dens qc^2 K_ihtr) efrz : 0
   if (htr_on) {
-    b_efrz += bPihtr * ht2;
+    b_efrz = fma(bPihtr, ht2, b_efrz);
     const double b_ht1 = bPihtr * efrz * C.K_ihtr;
-    b_dens += b_ht1 * qc2;
-    b_qc += b_ht1 * dens * 2.0 * qc;
+    b_dens = fma(b_ht1, qc2, b_dens);
+    b_qc = fma(b_ht1 * dens * 2.0, qc, b_qc);
   }
   // efrz = exp(-A_frz temc) - 1
-  b_temc += b_efrz * efe * (-C.A_frz);
+  b_temc = fma(b_efrz * efe, (-C.A_frz), b_temc);
   // Pihom = below40 ? dqc_dt : 0
   if (below40) b_dqc += bPihom;
   // Pidep / Pisub: tmp1 = (((4 Di) XNi) Rdens sm1) Giv
   {
     const double b_t = (sps ? bPidep : 0.0) - (!sps ? bPisub : 0.0);
-    b_Giv += b_t * t1d;
+    b_Giv = fma(b_t, t1d, b_Giv);
     const double b_t1d = b_t * Giv;
-    b_Sice += b_t1d * t1c;
+    b_Sice = fma(b_t1d, t1c, b_Sice);
     const double b_t1c = b_t1d * sm1;
-    b_Rdens += b_t1c * t1b;
+    b_Rdens = fma(b_t1c, t1b, b_Rdens);
     const double b_t1b = b_t1c * Rdens;
-    b_XNi += b_t1b * t1a;
-    b_Di += b_t1b * XNi * 4.0;
+    b_XNi = fma(b_t1b, t1a, b_XNi);
+    b_Di = fma(b_t1b * XNi, 4.0, b_Di);
   }
   // XNi, Di from rhoqi
   if (ice_on) {
@@ -920,8 +920,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
       const double b_dis = b_dia * C.Di_a;
       const double b_XMi = b_dis * bsqrt(di_s);
       const double rXNi = 1.0 / XNi;
-      b_rhoqi += b_XMi * rXNi;
-      b_XNi -= b_XMi * XMi * rXNi;
+      b_rhoqi = fma(b_XMi, rXNi, b_rhoqi);
+      b_XNi = fma(-(b_XMi * XMi), rXNi, b_XNi);
     }
     // XNi = min(max(5.38e7 pow(rhoqi, 0.75), 1e3), 1e6)
     if (!xn_hi && !xn_lo) {
@@ -930,8 +930,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     }
   }
   if (rqi_on) {
-    b_dens += b_rhoqi * qi;
-    b_qi += b_rhoqi * dens;
+    b_dens = fma(b_rhoqi, qi, b_dens);
+    b_qi = fma(b_rhoqi, dens, b_qi);
   }
   // Prevp = (((K_revp Rdens) (1 - min(Sliq, 1))) Glv) ventr
   if (rain) {
@@ -942,16 +942,16 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     const double b_ev1 = b_ev3 * ev2;
     const double b_ev2 = b_ev3 * ev1;
     if (sl_min) b_Sliq -= b_ev2;
-    b_Rdens += b_ev1 * C.K_revp;
+    b_Rdens = fma(b_ev1, C.K_revp, b_Rdens);
     // ventr = K_ventr1 RLMDr_2 + K_ventr2 sqrt(Cr fr rNu RLMDr_5dr)
-    b_RLMDr_2 += b_ventr * C.K_ventr1;
+    b_RLMDr_2 = fma(b_ventr, C.K_ventr1, b_RLMDr_2);
     const double b_vr4 = b_ventr * C.K_ventr2 * bsqrt(vr5);
-    b_RLMDr_5dr += b_vr4 * vr3;
+    b_RLMDr_5dr = fma(b_vr4, vr3, b_RLMDr_5dr);
     const double b_vr3 = b_vr4 * RLMDr_5dr;
-    b_rNu += b_vr3 * vr2;
+    b_rNu = fma(b_vr3, vr2, b_rNu);
     const double b_vr2 = b_vr3 * rNu;
-    b_Cr += b_vr2 * fr;
-    b_rho_fact += b_vr2 * C.Cr;
+    b_Cr = fma(b_vr2, fr, b_Cr);
+    b_rho_fact = fma(b_vr2, C.Cr, b_rho_fact);
     // Glv = xl / (((LHV0 rKaT) (LovR_liq rtem - 1)) xl + 1)
     const double rgl6 = 1.0 / gl6;
     const double b_xl0 = b_Glv * rgl6;
@@ -960,21 +960,21 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     const double b_xl = b_xl0 + b_gl6 * gl4;
     const double b_gl1 = b_gl4 * gl3;
     const double b_gl3 = b_gl4 * gl1;
-    b_rtem += b_gl3 * C.LovR_liq;
+    b_rtem = fma(b_gl3, C.LovR_liq, b_rtem);
     const double b_rKaT_l = b_gl1 * LHV0;
     // xl = KdD qsatl
-    b_KdD += b_xl * qsatl;
-    b_qsatl += b_xl * KdD;
+    b_KdD = fma(b_xl, qsatl, b_KdD);
+    b_qsatl = fma(b_xl, KdD, b_qsatl);
     // rKaT = 1 / (Ka temp)
     const double b_kat = -b_rKaT_l * rKaT * rKaT;
-    b_Ka += b_kat * temp;
-    b_temp += b_kat * Ka;
+    b_Ka = fma(b_kat, temp, b_Ka);
+    b_temp = fma(b_kat, Ka, b_temp);
   }
   // Gil = (Ka temc) rLHF0
   {
     const double b_gila = b_Gil * C.rLHF0;
-    b_Ka += b_gila * temc;
-    b_temc += b_gila * Ka;
+    b_Ka = fma(b_gila, temc, b_Ka);
+    b_temc = fma(b_gila, Ka, b_temc);
   }
   // Giv = xi / (((LHS0 rKaT) (LovR_ice rtem - 1)) xi + 1)
   {
@@ -985,152 +985,152 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     const double b_xi = b_xi0 + b_gv6 * gv4;
     const double b_gv1 = b_gv4 * gv3;
     const double b_gv3 = b_gv4 * gv1;
-    b_rtem += b_gv3 * C.LovR_ice;
+    b_rtem = fma(b_gv3, C.LovR_ice, b_rtem);
     const double b_rKaT = b_gv1 * LHS0;
     const double b_kat = -b_rKaT * rKaT * rKaT;
-    b_Ka += b_kat * temp;
-    b_temp += b_kat * Ka;
-    b_KdD += b_xi * qsati;
-    b_qsati += b_xi * KdD;
+    b_Ka = fma(b_kat, temp, b_Ka);
+    b_temp = fma(b_kat, Ka, b_temp);
+    b_KdD = fma(b_xi, qsati, b_KdD);
+    b_qsati = fma(b_xi, KdD, b_qsati);
   }
   // rNu = dens / nu0, nu0 = 1.718e-5 + 5.28e-8 temc
   {
     const double rnu0 = 1.0 / nu0;
-    b_dens += b_rNu * rnu0;
+    b_dens = fma(b_rNu, rnu0, b_dens);
     const double b_nu0 = -b_rNu * rNu * rnu0;
-    b_temc += b_nu0 * 5.28E-8;
+    b_temc = fma(b_nu0, 5.28E-8, b_temc);
   }
   // KdD = ((kd0 PSTD) / pre) dens, kd0 = 2.222e-5 + 1.37e-7 temc
   {
-    b_dens += b_KdD * kd2;
+    b_dens = fma(b_KdD, kd2, b_dens);
     const double b_kd2 = b_KdD * dens;
     const double rpre = 1.0 / pre;
     const double b_kd1 = b_kd2 * rpre;
-    b_pre -= b_kd2 * kd2 * rpre;
-    b_temc += b_kd1 * PSTD * 1.37E-7;
+    b_pre = fma(-(b_kd2 * kd2), rpre, b_pre);
+    b_temc = fma(b_kd1 * PSTD, 1.37E-7, b_temc);
   }
   // Ka = 2.428e-2 + 7.47e-5 temc
-  b_temc += b_Ka * 7.47E-5;
+  b_temc = fma(b_Ka, 7.47E-5, b_temc);
   // Psaut = max(betai (qi - qicrt), 0)
   {
     double b_sb = 0.0, dummy = 0.0;
     bmax(saut_b, Z, bPsaut, b_sb, dummy);
-    b_betai += b_sb * saut_a;
+    b_betai = fma(b_sb, saut_a, b_betai);
     const double b_sa = b_sb * betai;
     b_qi += b_sa;
     b_qicrt -= b_sa;
   }
   // Praut = K_aut pow(qc, 2.47)
   if (aut_on) {
-    b_K_aut += bPraut * aut_pow;
+    b_K_aut = fma(bPraut, aut_pow, b_K_aut);
     if (qc > 0.0) b_qc += bPraut * C.K_aut * 2.47 * aut_pow / qc;
   }
   // rhoqc = (dens qc) 1000 (read by the effective radius)
-  b_dens += b_rhoqc * 1000.0 * qc;
-  b_qc += b_rhoqc * 1000.0 * dens;
+  b_dens = fma(b_rhoqc * 1000.0, qc, b_dens);
+  b_qc = fma(b_rhoqc * 1000.0, dens, b_qc);
   // Pracs = (K_racs Rdens) dvrs (2 MOMs_0bs RLMDr_3 + 2 MOMs_1bs RLMDr_2 + MOMs_2bs RLMDr)
   double b_dvrs = 0.0;
   {
     const double b_s = bPracs * racs_kd;
     const double b_kd = bPracs * racs_s;
-    b_dvrs += b_kd * racs_k;
-    b_Rdens += b_kd * dvrs * C.K_racs;
-    b_mom[2] += b_s * RLMDr_3 * 2.0;
-    b_RLMDr_3 += b_s * racs_t1;
-    b_mom[3] += b_s * RLMDr_2 * 2.0;
-    b_RLMDr_2 += b_s * racs_t2;
-    b_mom[4] += b_s * RLMDr;
-    b_RLMDr += b_s * MOMs_2bs;
+    b_dvrs = fma(b_kd, racs_k, b_dvrs);
+    b_Rdens = fma(b_kd * dvrs, C.K_racs, b_Rdens);
+    b_mom[2] = fma(b_s * RLMDr_3, 2.0, b_mom[2]);
+    b_RLMDr_3 = fma(b_s, racs_t1, b_RLMDr_3);
+    b_mom[3] = fma(b_s * RLMDr_2, 2.0, b_mom[3]);
+    b_RLMDr_2 = fma(b_s, racs_t2, b_RLMDr_2);
+    b_mom[4] = fma(b_s, RLMDr, b_mom[4]);
+    b_RLMDr = fma(b_s, MOMs_2bs, b_RLMDr);
   }
   // Pgacr = (K_gacr Rdens) |Vtg - Vtr| (K_g13 RLMDr_1br RLMDg_3 + K_g22 RLMDr_2br RLMDg_2 + GAM_3br RLMDr_3br RLMDg)
   {
     const double b_s = bPgacr * gacr_kd;
     const double b_kd = bPgacr * gacr_s;
     const double b_dv = b_kd * gacr_k;
-    b_Rdens += b_kd * dvgr * C.K_gacr;
+    b_Rdens = fma(b_kd * dvgr, C.K_gacr, b_Rdens);
     const double sgn = dvgr_d < 0.0 ? -1.0 : 1.0;
-    b_Vtg += b_dv * sgn;
-    b_Vtr -= b_dv * sgn;
-    b_RLMDr_1br += b_s * RLMDg_3 * C.K_g13;
-    b_RLMDg_3 += b_s * gacr_t1;
-    b_RLMDr_2br += b_s * RLMDg_2 * C.K_g22;
-    b_RLMDg_2 += b_s * gacr_t2;
-    b_RLMDr_3br += b_s * RLMDg * C.GAM_3br;
-    b_RLMDg += b_s * gacr_t3;
+    b_Vtg = fma(b_dv, sgn, b_Vtg);
+    b_Vtr = fma(-b_dv, sgn, b_Vtr);
+    b_RLMDr_1br = fma(b_s * RLMDg_3, C.K_g13, b_RLMDr_1br);
+    b_RLMDg_3 = fma(b_s, gacr_t1, b_RLMDg_3);
+    b_RLMDr_2br = fma(b_s * RLMDg_2, C.K_g22, b_RLMDr_2br);
+    b_RLMDg_2 = fma(b_s, gacr_t2, b_RLMDg_2);
+    b_RLMDr_3br = fma(b_s * RLMDg, C.GAM_3br, b_RLMDr_3br);
+    b_RLMDg = fma(b_s, gacr_t3, b_RLMDg);
   }
   // Psacr = (K_sacr Rdens) dvrs (GAM_1br RLMDr_1br MOMs_2 + K_2gam2br RLMDr_2br MOMs_1 + GAM_3br RLMDr_3br MOMs_0)
   {
     const double b_s = bPsacr * sacr_kd;
     const double b_kd = bPsacr * sacr_s;
-    b_dvrs += b_kd * sacr_k;
-    b_Rdens += b_kd * dvrs * C.K_sacr;
-    b_RLMDr_1br += b_s * MOMs_2 * C.GAM_1br;
-    b_MOMs_2 += b_s * sacr_t1;
-    b_RLMDr_2br += b_s * MOMs_1 * C.K_2gam2br;
-    b_mom[1] += b_s * sacr_t2;
-    b_RLMDr_3br += b_s * MOMs_0 * C.GAM_3br;
-    b_mom[0] += b_s * sacr_t3;
+    b_dvrs = fma(b_kd, sacr_k, b_dvrs);
+    b_Rdens = fma(b_kd * dvrs, C.K_sacr, b_Rdens);
+    b_RLMDr_1br = fma(b_s * MOMs_2, C.GAM_1br, b_RLMDr_1br);
+    b_MOMs_2 = fma(b_s, sacr_t1, b_MOMs_2);
+    b_RLMDr_2br = fma(b_s * MOMs_1, C.K_2gam2br, b_RLMDr_2br);
+    b_mom[1] = fma(b_s, sacr_t2, b_mom[1]);
+    b_RLMDr_3br = fma(b_s * MOMs_0, C.GAM_3br, b_RLMDr_3br);
+    b_mom[0] = fma(b_s, sacr_t3, b_mom[0]);
   }
   // dvrs = |Vtr - Vts|
   {
     const double sgn = dvrs_d < 0.0 ? -1.0 : 1.0;
-    b_Vtr += b_dvrs * sgn;
-    b_Vts -= b_dvrs * sgn;
+    b_Vtr = fma(b_dvrs, sgn, b_Vtr);
+    b_Vts = fma(-b_dvrs, sgn, b_Vts);
   }
   // Piacr = ((qi K_iacr) RLMDr_6dr) fr
-  b_rho_fact += bPiacr * iacr_b;
+  b_rho_fact = fma(bPiacr, iacr_b, b_rho_fact);
   {
     const double b_b = bPiacr * fr;
-    b_RLMDr_6dr += b_b * iacr_a;
+    b_RLMDr_6dr = fma(b_b, iacr_a, b_RLMDr_6dr);
     const double b_a = b_b * RLMDr_6dr;
-    b_qi += b_a * C.K_iacr;
-    b_K_iacr += b_a * qi;
+    b_qi = fma(b_a, C.K_iacr, b_qi);
+    b_K_iacr = fma(b_a, qi, b_K_iacr);
   }
   // Psaci = (((qi K_saci) Esi_mod) MOMs_2ds) fr
-  b_rho_fact += bPsaci * saci_c;
+  b_rho_fact = fma(bPsaci, saci_c, b_rho_fact);
   {
     const double b_c = bPsaci * fr;
-    b_mom[5] += b_c * saci_b;
+    b_mom[5] = fma(b_c, saci_b, b_mom[5]);
     const double b_b = b_c * MOMs_2ds;
-    b_Esi_mod += b_b * saci_a;
+    b_Esi_mod = fma(b_b, saci_a, b_Esi_mod);
     const double b_a = b_b * Esi_mod;
-    b_qi += b_a * C.K_saci;
-    b_K_saci += b_a * qi;
+    b_qi = fma(b_a, C.K_saci, b_qi);
+    b_K_saci = fma(b_a, qi, b_K_saci);
   }
   // Praci = ((qi K_raci) RLMDr_3dr) fr
-  b_rho_fact += bPraci * raci_b;
+  b_rho_fact = fma(bPraci, raci_b, b_rho_fact);
   {
     const double b_b = bPraci * fr;
-    b_RLMDr_3dr += b_b * raci_a;
+    b_RLMDr_3dr = fma(b_b, raci_a, b_RLMDr_3dr);
     const double b_a = b_b * RLMDr_3dr;
-    b_qi += b_a * C.K_raci;
-    b_K_raci += b_a * qi;
+    b_qi = fma(b_a, C.K_raci, b_qi);
+    b_K_raci = fma(b_a, qi, b_K_raci);
   }
   // Pgacw = ((qc K_gacw) RLMDg_3dg) fr
-  b_rho_fact += bPgacw * gacw_b;
+  b_rho_fact = fma(bPgacw, gacw_b, b_rho_fact);
   {
     const double b_b = bPgacw * fr;
-    b_RLMDg_3dg += b_b * gacw_a;
+    b_RLMDg_3dg = fma(b_b, gacw_a, b_RLMDg_3dg);
     const double b_a = b_b * RLMDg_3dg;
-    b_qc += b_a * C.K_gacw;
-    b_K_gacw += b_a * qc;
+    b_qc = fma(b_a, C.K_gacw, b_qc);
+    b_K_gacw = fma(b_a, qc, b_K_gacw);
   }
   // Psacw = ((qc K_sacw) MOMs_2ds) fr
-  b_rho_fact += bPsacw * sacw_b;
+  b_rho_fact = fma(bPsacw, sacw_b, b_rho_fact);
   {
     const double b_b = bPsacw * fr;
-    b_mom[5] += b_b * sacw_a;
+    b_mom[5] = fma(b_b, sacw_a, b_mom[5]);
     const double b_a = b_b * MOMs_2ds;
-    b_qc += b_a * C.K_sacw;
-    b_K_sacw += b_a * qc;
+    b_qc = fma(b_a, C.K_sacw, b_qc);
+    b_K_sacw = fma(b_a, qc, b_K_sacw);
   }
   // Pracw = 67 pow(qc qr, 1.15)
   if (prw_on) {
     const double b_pow = bPracw0 * 67.0;
     if (qcqr > 0.0) {
       const double b_qcqr = b_pow * 1.15 * prw_pow / qcqr;
-      b_qc += b_qcqr * qr;
-      b_qr += b_qcqr * qc;
+      b_qc = fma(b_qcqr, qr, b_qc);
+      b_qr = fma(b_qcqr, qc, b_qr);
     }
   }
   // Esi_mod = min(Esi, Esi eg), betai = min(beta, beta eg), eg = exp(gamma_sacr temc)
@@ -1138,12 +1138,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     double b_eg = 0.0;
     if (esi_exp) b_eg += b_Esi_mod * C.Esi;
     if (bet_exp) {
-      b_eg += b_betai * C.beta_saut;
-      b_beta += b_betai * eg;
+      b_eg = fma(b_betai, C.beta_saut, b_eg);
+      b_beta = fma(b_betai, eg, b_beta);
     } else {
       b_beta += b_betai;
     }
-    b_temc += b_eg * eg * C.gamma_sacr;
+    b_temc = fma(b_eg * eg, C.gamma_sacr, b_temc);
   } else {
     b_beta += b_betai;
   }
@@ -1158,119 +1158,119 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     b_qv += b_p2;
     b_qsati -= b_p2;
     // Qi0 = (ice_nuc exp(1.33 (ln1000 + max(-0.1 temc, 0)))) Rdens
-    b_Rdens += b_p1 * qi0a;
+    b_Rdens = fma(b_p1, qi0a, b_Rdens);
     const double b_qi0a = b_p1 * Rdens;
-    b_icenuc += b_qi0a * nexp;
+    b_icenuc = fma(b_qi0a, nexp, b_icenuc);
     const double b_nex = b_qi0a * C.ice_nuc * nexp;
     double b_nm01 = 0.0, dummy2 = 0.0;
     bmax(nm01, Z, b_nex * 1.33, b_nm01, dummy2);
-    b_temc += b_nm01 * -0.1;
+    b_temc = fma(b_nm01, -0.1, b_temc);
   }
   // terminal velocities: Vtr = (K_vtr rho_fact) RLMDr_dr etc.
   {
-    b_RLMDr_dr += b_Vtr * vtr_a;
+    b_RLMDr_dr = fma(b_Vtr, vtr_a, b_RLMDr_dr);
     const double b_a = b_Vtr * RLMDr_dr;
-    b_K_vtr += b_a * rho_fact;
-    b_rho_fact += b_a * C.K_vtr;
-    b_RMOMs_Vt += b_Vts * vts_a;
+    b_K_vtr = fma(b_a, rho_fact, b_K_vtr);
+    b_rho_fact = fma(b_a, C.K_vtr, b_rho_fact);
+    b_RMOMs_Vt = fma(b_Vts, vts_a, b_RMOMs_Vt);
     const double b_s = b_Vts * RMOMs_Vt;
-    b_K_vts += b_s * rho_fact;
-    b_rho_fact += b_s * C.K_vts;
-    b_RLMDg_dg += b_Vtg * vtg_a;
+    b_K_vts = fma(b_s, rho_fact, b_K_vts);
+    b_rho_fact = fma(b_s, C.K_vts, b_rho_fact);
+    b_RLMDg_dg = fma(b_Vtg, vtg_a, b_RLMDg_dg);
     const double b_g = b_Vtg * RLMDg_dg;
-    b_K_vtg += b_g * rho_fact;
-    b_rho_fact += b_g * C.K_vtg;
+    b_K_vtg = fma(b_g, rho_fact, b_K_vtg);
+    b_rho_fact = fma(b_g, C.K_vtg, b_rho_fact);
   }
   // graupel slope parameter
   if (graupel) {
-    b_RLMDg_3 += b_RLMDg_5dg * RLMDg_dg * RLMDg_2;
-    b_RLMDg_2 += b_RLMDg_5dg * RLMDg_dg * RLMDg_3;
-    b_RLMDg_dg += b_RLMDg_5dg * g32;
-    b_RLMDg_3 += b_RLMDg_3dg * RLMDg_dg;
-    b_RLMDg_dg += b_RLMDg_3dg * RLMDg_3;
-    b_RLMDg_2 += b_RLMDg_3 * RLMDg;
-    b_RLMDg += b_RLMDg_3 * RLMDg_2;
-    b_RLMDg += b_RLMDg_2 * 2.0 * RLMDg;
-    b_RLMDg += b_RLMDg_dg * bsqrt(RLMDg_dg);
+    b_RLMDg_3 = fma(b_RLMDg_5dg * RLMDg_dg, RLMDg_2, b_RLMDg_3);
+    b_RLMDg_2 = fma(b_RLMDg_5dg * RLMDg_dg, RLMDg_3, b_RLMDg_2);
+    b_RLMDg_dg = fma(b_RLMDg_5dg, g32, b_RLMDg_dg);
+    b_RLMDg_3 = fma(b_RLMDg_3dg, RLMDg_dg, b_RLMDg_3);
+    b_RLMDg_dg = fma(b_RLMDg_3dg, RLMDg_3, b_RLMDg_dg);
+    b_RLMDg_2 = fma(b_RLMDg_3, RLMDg, b_RLMDg_2);
+    b_RLMDg = fma(b_RLMDg_3, RLMDg_2, b_RLMDg);
+    b_RLMDg = fma(b_RLMDg_2 * 2.0, RLMDg, b_RLMDg);
+    b_RLMDg = fma(b_RLMDg_dg, bsqrt(RLMDg_dg), b_RLMDg);
     const double b_s1 = b_RLMDg * bsqrt(RLMDg);
     const double b_b = b_s1 * bsqrt(g_s1);
     const double b_a = b_b * C.K_rlmdg;
-    b_dens += b_a * qg;
-    b_qg += b_a * dens;
+    b_dens = fma(b_a, qg, b_dens);
+    b_qg = fma(b_a, dens, b_qg);
   }
   // snow moments: Vts's RMOMs_Vt = mom5 / mom2; mom_i = exp(logX lb_i + la_i(tems)); MOMs_2 = Xs2
   double b_Xs2 = b_MOMs_2;
   if (snow) {
     const double rm2 = 1.0 / mom[2];
-    b_mom[5] += b_RMOMs_Vt * rm2;
-    b_mom[2] -= b_RMOMs_Vt * RMOMs_Vt * rm2;
+    b_mom[5] = fma(b_RMOMs_Vt, rm2, b_mom[5]);
+    b_mom[2] = fma(-(b_RMOMs_Vt * RMOMs_Vt), rm2, b_mom[2]);
     double b_logX = 0.0, b_tems = 0.0;
 #pragma unroll
     for (int i = 0; i < 7; ++i) {
       const double b_arg = b_mom[i] * mom[i];
-      b_logX += b_arg * mlb[i];
+      b_logX = fma(b_arg, mlb[i], b_logX);
       const double* a = C.roh_a + 4 * i;
       const double* b = C.roh_b + 4 * i;
       // d la / d tems and d lb / d tems of the cubics
       const double dla = __fma_rn(__fma_rn(3.0 * a[3], tems, 2.0 * a[2]), tems, a[1]);
       const double dlb = __fma_rn(__fma_rn(3.0 * b[3], tems, 2.0 * b[2]), tems, b[1]);
-      b_tems += b_arg * (dla + logX * dlb);
+      b_tems = fma(b_arg, (dla + logX * dlb), b_tems);
     }
     b_Xs2 += b_logX / Xs2;
     if (tems_sel) b_temc += b_tems;
   }
   {
     const double b_xsa = b_Xs2 * C.rAs;
-    b_dens += b_xsa * qs;
-    b_qs += b_xsa * dens;
+    b_dens = fma(b_xsa, qs, b_dens);
+    b_qs = fma(b_xsa, dens, b_qs);
   }
   // rain slope parameter
   if (rain) {
-    b_RLMDr_3br += b_RLMDr_6dr * RLMDr_dr;
-    b_RLMDr_dr += b_RLMDr_6dr * RLMDr_3br;
-    b_RLMDr_2br += b_RLMDr_5dr * RLMDr_dr;
-    b_RLMDr_dr += b_RLMDr_5dr * RLMDr_2br;
-    b_RLMDr_3 += b_RLMDr_3dr * RLMDr_dr;
-    b_RLMDr_dr += b_RLMDr_3dr * RLMDr_3;
-    b_RLMDr_3br += b_RLMDr_7 * RLMDr;
-    b_RLMDr += b_RLMDr_7 * RLMDr_3br;
-    b_RLMDr_3 += b_RLMDr_3br * 2.0 * RLMDr_3;
-    b_RLMDr_1br += b_RLMDr_2br * RLMDr;
-    b_RLMDr += b_RLMDr_2br * RLMDr_1br;
-    b_RLMDr_2 += b_RLMDr_1br * 2.0 * RLMDr_2;
-    b_RLMDr_2 += b_RLMDr_3 * RLMDr;
-    b_RLMDr += b_RLMDr_3 * RLMDr_2;
-    b_RLMDr += b_RLMDr_2 * 2.0 * RLMDr;
-    b_RLMDr += b_RLMDr_dr * bsqrt(RLMDr_dr);
+    b_RLMDr_3br = fma(b_RLMDr_6dr, RLMDr_dr, b_RLMDr_3br);
+    b_RLMDr_dr = fma(b_RLMDr_6dr, RLMDr_3br, b_RLMDr_dr);
+    b_RLMDr_2br = fma(b_RLMDr_5dr, RLMDr_dr, b_RLMDr_2br);
+    b_RLMDr_dr = fma(b_RLMDr_5dr, RLMDr_2br, b_RLMDr_dr);
+    b_RLMDr_3 = fma(b_RLMDr_3dr, RLMDr_dr, b_RLMDr_3);
+    b_RLMDr_dr = fma(b_RLMDr_3dr, RLMDr_3, b_RLMDr_dr);
+    b_RLMDr_3br = fma(b_RLMDr_7, RLMDr, b_RLMDr_3br);
+    b_RLMDr = fma(b_RLMDr_7, RLMDr_3br, b_RLMDr);
+    b_RLMDr_3 = fma(b_RLMDr_3br * 2.0, RLMDr_3, b_RLMDr_3);
+    b_RLMDr_1br = fma(b_RLMDr_2br, RLMDr, b_RLMDr_1br);
+    b_RLMDr = fma(b_RLMDr_2br, RLMDr_1br, b_RLMDr);
+    b_RLMDr_2 = fma(b_RLMDr_1br * 2.0, RLMDr_2, b_RLMDr_2);
+    b_RLMDr_2 = fma(b_RLMDr_3, RLMDr, b_RLMDr_2);
+    b_RLMDr = fma(b_RLMDr_3, RLMDr_2, b_RLMDr);
+    b_RLMDr = fma(b_RLMDr_2 * 2.0, RLMDr, b_RLMDr);
+    b_RLMDr = fma(b_RLMDr_dr, bsqrt(RLMDr_dr), b_RLMDr);
     const double b_s1 = b_RLMDr * bsqrt(RLMDr);
     const double b_b = b_s1 * bsqrt(r_s1);
     const double b_a = b_b * C.K_rlmdr;
-    b_dens += b_a * qr;
-    b_qr += b_a * dens;
+    b_dens = fma(b_a, qr, b_dens);
+    b_qr = fma(b_a, dens, b_qr);
   }
   // dq/dt = q / dt
   {
     const double rdt = 1.0 / dt;
-    b_qv += b_dqv * rdt;
-    b_qc += b_dqc * rdt;
-    b_qr += b_dqr * rdt;
-    b_qi += b_dqi * rdt;
-    b_qs += b_dqs * rdt;
-    b_qg += b_dqg * rdt;
+    b_qv = fma(b_dqv, rdt, b_qv);
+    b_qc = fma(b_dqc, rdt, b_qc);
+    b_qr = fma(b_dqr, rdt, b_qr);
+    b_qi = fma(b_dqi, rdt, b_qi);
+    b_qs = fma(b_dqs, rdt, b_qs);
+    b_qg = fma(b_dqg, rdt, b_qg);
   }
   // temc = temp - TEM00; rho_fact = sqrt(DENS00 Rdens); Rdens = 1 / dens
   b_temp += b_temc;
-  b_Rdens += b_rho_fact * bsqrt(rho_fact) * DENS00;
-  b_dens -= b_Rdens * Rdens * Rdens;
+  b_Rdens = fma(b_rho_fact * bsqrt(rho_fact), DENS00, b_Rdens);
+  b_dens = fma(-(b_Rdens * Rdens), Rdens, b_dens);
   // Sliq = qv / max(qsatl, EPS), Sice = qv / max(qsati, EPS)
   {
     const double rsld = 1.0 / sld;
-    b_qv += b_Sliq * rsld;
+    b_qv = fma(b_Sliq, rsld, b_qv);
     const double b_sld = -b_Sliq * Sliq * rsld;
     double dummy = 0.0;
     bmax(qsatl, EPS, b_sld, b_qsatl, dummy);
     const double rsid = 1.0 / sid;
-    b_qv += b_Sice * rsid;
+    b_qv = fma(b_Sice, rsid, b_qv);
     const double b_sid = -b_Sice * Sice * rsid;
     bmax(qsati, EPS, b_sid, b_qsati, dummy);
   }
@@ -1287,8 +1287,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
     const double b_rdrt = b_qsatl * psatl + b_qsati * psati;
     const double b_psatl = b_qsatl * rdrt, b_psati = b_qsati * rdrt;
     const double b_drt = -b_rdrt * rdrt * rdrt;
-    b_dens += b_drt * temp * RVAP;
-    b_temp += b_drt * drv;
+    b_dens = fma(b_drt * temp, RVAP, b_dens);
+    b_temp = fma(b_drt, drv, b_temp);
     b_rtem -= b_psatl * PSAT0 * el * C.LovR_liq + b_psati * PSAT0 * ei * C.LovR_ice;
     // rtem = 1 / max(temp, TEM_MIN)
     const double b_tmx = -b_rtem * rtem * rtem;
@@ -1297,18 +1297,18 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   }
   // pre = (dens (qd RDRY + qn0 RVAP)) temp
   {
-    b_temp += b_pre * dp;
+    b_temp = fma(b_pre, dp, b_temp);
     const double b_dp = b_pre * temp;
-    b_dens += b_dp * pq;
+    b_dens = fma(b_dp, pq, b_dens);
     const double b_pq = b_dp * dens;
     double b_qd = b_pq * RDRY;
-    b_qn[0] += b_pq * RVAP;
+    b_qn[0] = fma(b_pq, RVAP, b_qn[0]);
     // rhoge0 = (temp rhog) cv
     const double b_trh = b_rhoge0 * cv;
     const double b_cv = b_rhoge0 * trh;
-    b_temp += b_trh * rhog;
-    b_rhog += b_trh * temp;
-    b_qd += b_cv * CVDRY;
+    b_temp = fma(b_trh, rhog, b_temp);
+    b_rhog = fma(b_trh, temp, b_rhog);
+    b_qd = fma(b_cv, CVDRY, b_qd);
 #pragma unroll
     for (int n = 1; n <= 5; ++n) b_qn[n] += b_cv * CVDRY - b_qd;
   }
@@ -1316,16 +1316,16 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   {
 #pragma unroll
     for (int n = 1; n <= 5; ++n) {
-      b_rq[n] += b_qn[n] * rrhog;
-      b_rhog -= b_qn[n] * qn[n] * rrhog;
+      b_rq[n] = fma(b_qn[n], rrhog, b_rq[n]);
+      b_rhog = fma(-(b_qn[n] * qn[n]), rrhog, b_rhog);
     }
     const double rgs = 1.0 / in.gsgam2;
-    b_rhog += b_dens * rgs;
-    ib.gsgam2 += -b_dens * dens * rgs;
+    b_rhog = fma(b_dens, rgs, b_rhog);
+    ib.gsgam2 = fma(-b_dens * dens, rgs, ib.gsgam2);
   }
   // rhog = in.rhog (1 - d2); negative filter
   {
-    ib.rhog += b_rhog * omd;
+    ib.rhog = fma(b_rhog, omd, ib.rhog);
     const double b_d2 = -b_rhog * in.rhog;
     // d2 = rq0a - clip(rq0a): d d2 / d rq0a = clip ? 1 : 0; rq[0] = clip(rq0a)
     const double b_rq0a = (clip[0] ? b_d2 : 0.0) + (clip[0] ? 0.0 : b_rq[0]);
