@@ -60,7 +60,7 @@ FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.842, "mixed": 0.747},
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (csrc/nsw6_probe.cu) and frozen here.
-ADJOINT_LAUNCHES = 12   # kernels of one mp_driver_adjoint call once its tapes are sized
+ADJOINT_LAUNCHES = 12   # kernels of one mp_driver_adjoint call (hand-written sweeps)
 OP_WEIGHTS = {"add": 1.0, "mul": 1.0, "cmp": 1.0, "div": 15.0, "sqrt": 15.2, "exp": 30.0, "log": 58.4,
               "pow": 173.8}
 
