@@ -4,6 +4,8 @@
 
 #include <cstdint>
 
+#include "nsw6_fpcmp.cuh"
+
 #ifndef __CUDACC__
 #define __host__
 #define __device__

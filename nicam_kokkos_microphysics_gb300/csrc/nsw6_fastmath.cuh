@@ -22,10 +22,13 @@
 // exp(h)(1 + l), which keeps it within a few units in the last place.
 //
 // The tables (8 KB) are built on the host in extended precision and staged
-// in shared memory by every CTA.
+// in shared memory by every CTA.  The range tests compare bit patterns on the
+// integer pipe (nsw6_fpcmp.cuh), with the IEEE comparisons' results.
 #pragma once
 
 #include <cstdint>
+
+#include "nsw6_fpcmp.cuh"
 
 namespace nsw6 {
 
@@ -41,7 +44,7 @@ struct FastMath {
 
   // exp within about half an ulp; slow path outside (-708, 708).
   __device__ __forceinline__ double exp(double x) const {
-    if (!(fabs(x) < 708.0)) return ::exp(x);
+    if (!fp_abs_lt(x, 708.0)) return ::exp(x);
     const double shift = 6755399441055744.0;               // 1.5 * 2^52
     const double inv = 369.32993046757463;                  // 256 / ln 2
     const double l_hi = 2.7076061740622863e-03;             // ln2/256, high part
@@ -66,11 +69,13 @@ struct FastMath {
   // log(x) as hi + lo (|lo| <= ulp(hi)); slow path for x <= 0, non-normal, inf, nan.
   __device__ __forceinline__ double log_hl(double x, double& lo) const {
     const long long bits = __double_as_longlong(x);
-    if (!(x >= 2.2250738585072014e-308 && x < 1.7976931348623157e308)) {
+    // x normal and finite, positive (the signed bits order the positive doubles)
+    if (!(bits >= 0x0010000000000000ll && bits < 0x7FEFFFFFFFFFFFFFll)) {
       lo = 0.0;
       return ::log(x);
     }
-    if (fabs(x - 1.0) < NEAR1) {  // x - 1 is exact here (Sterbenz)
+    // |x - 1| < NEAR1, i.e. 1 - 2^-7 < x < 1 + 2^-7 (x - 1 is exact there, Sterbenz)
+    if (bits > 0x3FEFC00000000000ll && bits < 0x3FF0200000000000ll) {
       lo = 0.0;
       return log1p_near1(x - 1.0);
     }
@@ -124,7 +129,7 @@ struct FastMath {
 
   // x^y for x >= 0 (the only use here); x == 0 gives 0 for y > 0.
   __device__ __forceinline__ double pow(double x, double y) const {
-    if (x == 0.0) return (y > 0.0) ? 0.0 : ::pow(x, y);
+    if (fp_is_zero(x)) return fp_gt(y, 0.0) ? 0.0 : ::pow(x, y);
     double lo;
     const double hi = log_hl(x, lo);
     const double ph = __dmul_rn(y, hi);

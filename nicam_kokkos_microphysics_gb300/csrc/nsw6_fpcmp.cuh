@@ -1,0 +1,68 @@
+// IEEE-754 double comparisons evaluated on the integer pipe.
+//
+// On GB300 an FP64 compare issues to the FP64 pipe, which completes about two
+// operations per SM per cycle, while the integer pipe completes 64; the NSW6
+// kernels are FP64-pipe bound, so their comparisons (min / max, thresholds,
+// range checks) are computed from the bit patterns instead.  Each function
+// returns exactly what the IEEE comparison returns for every pair of doubles:
+// false when either operand is NaN, -0 equal to +0.
+//
+// For a non-NaN x with bits b (as a signed 64-bit integer), the key
+// b ^ ((b >> 63) & 0x7FF...F) orders the doubles like the reals, except that
+// -0 (key -1) sorts below +0 (key 0); the zero pair is tested separately.
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+
+#ifdef __CUDACC__
+#define NSW6_FP_HD __host__ __device__ __forceinline__
+#else
+#define NSW6_FP_HD inline
+#endif
+
+namespace nsw6 {
+
+constexpr long long FP_ABS = 0x7FFFFFFFFFFFFFFFll;   // all but the sign
+constexpr long long FP_INF = 0x7FF0000000000000ll;   // +inf; larger magnitudes are NaN
+
+NSW6_FP_HD long long fp_bits(double x) {
+#ifdef __CUDA_ARCH__
+  return __double_as_longlong(x);
+#else
+  long long b;
+  std::memcpy(&b, &x, sizeof b);
+  return b;
+#endif
+}
+
+NSW6_FP_HD long long fp_key(long long b) { return b ^ ((b >> 63) & FP_ABS); }
+
+// a < b
+NSW6_FP_HD bool fp_lt(double a, double b) {
+  const long long ia = fp_bits(a), ib = fp_bits(b);
+  const long long ma = ia & FP_ABS, mb = ib & FP_ABS;
+  const bool ordered = (ma <= FP_INF) & (mb <= FP_INF);
+  const bool zeros = (ma | mb) == 0;
+  return ordered & !zeros & (fp_key(ia) < fp_key(ib));
+}
+
+// a <= b
+NSW6_FP_HD bool fp_le(double a, double b) {
+  const long long ia = fp_bits(a), ib = fp_bits(b);
+  const long long ma = ia & FP_ABS, mb = ib & FP_ABS;
+  const bool ordered = (ma <= FP_INF) & (mb <= FP_INF);
+  const bool zeros = (ma | mb) == 0;
+  return ordered & (zeros | (fp_key(ia) <= fp_key(ib)));
+}
+
+NSW6_FP_HD bool fp_gt(double a, double b) { return fp_lt(b, a); }
+NSW6_FP_HD bool fp_ge(double a, double b) { return fp_le(b, a); }
+
+// |x| < c for a constant c > 0 (NaN: false)
+NSW6_FP_HD bool fp_abs_lt(double x, double c) { return (fp_bits(x) & FP_ABS) < fp_bits(c); }
+
+// x == 0 (either zero)
+NSW6_FP_HD bool fp_is_zero(double x) { return (fp_bits(x) & FP_ABS) == 0; }
+
+}  // namespace nsw6
