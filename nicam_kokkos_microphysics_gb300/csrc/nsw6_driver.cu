@@ -641,11 +641,20 @@ int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
   // copies start after the work already queued on the handle's stream
   if (cudaEventRecord(h->ev_start, h->stream) != cudaSuccess || cudaStreamWaitEvent(h->s_in, h->ev_start, 0) != cudaSuccess)
     return NSW6_ERR_CUDA;
-  const int per = (lall + 4) / 5;   // regions per chunk: about five chunks
+  // Chunks of regions: the first chunk's copy in and the last chunk's copy
+  // out are not hidden behind compute, so those two are one region each; the
+  // rest go in about four chunks (larger launches fill the GPU's last wave
+  // better).
+  const int mid = lall > 2 ? (lall - 2 + 3) / 4 : 1;
+  auto chunk_len = [&](int l0) {
+    if (lall <= 2 || l0 == 0 || l0 == lall - 1) return 1;
+    const int left = lall - 1 - l0;   // regions before the last one
+    return left < mid ? left : mid;
+  };
   cudaError_t err = cudaSuccess;
   int nchunk = 0;
-  for (int l0 = 0; l0 < lall && err == cudaSuccess; l0 += per, ++nchunk) {
-    const int nl = (lall - l0 < per) ? lall - l0 : per;
+  for (int l0 = 0, nl = 0; l0 < lall && err == cudaSuccess; l0 += nl, ++nchunk) {
+    nl = chunk_len(l0);
     // chunk views: region l0 of every array (the precipitation outputs at
     // their own [2][nl][gall] block of the staging)
     double* cdev[A_COUNT];
