@@ -41,6 +41,10 @@ constexpr int I_QV = 0, I_QC = 1, I_QR = 2, I_QI = 3, I_QS = 4, I_QG = 5;
 constexpr int CELL_TG = 32;
 constexpr int CELL_THREADS = 256;
 constexpr int MAX_KALL = 160;
+// Above this many levels the cell kernel with the scheme switches reads the
+// grid metrics and the FastMath tables from global memory instead of staging
+// them in shared memory, so that its tile fits at MAX_KALL.
+constexpr int CELL_SMEM_KMAX = 128;
 
 // Scheme constants: mp_nsw6_init (mod_mp_nsw6.cpp:276-434) with the settings it
 // hard-wires, the effective-radius constants of mp_nsw6_new::init

@@ -83,9 +83,15 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
   const size_t off = (size_t)l * KG;
   const size_t offq = (size_t)l * NQ * KG;
   R* vts = reinterpret_cast<R*>(sm);                   // [ntr][K][CELL_TG] fall speeds, tracer order
-  double* grid = sm + cell_vts_doubles<R>(K, NV);      // [GF_COUNT][K]
-  double* tab = grid + GF_COUNT * K;                   // [FM_TABLE_DOUBLES]
-  float* gridf = reinterpret_cast<float*>(tab + FM_TABLE_DOUBLES);  // [4][K], mixed only
+  // grid metrics and FastMath tables: staged in shared memory, or, in the
+  // kernel with the scheme switches for columns deeper than CELL_SMEM_KMAX,
+  // read from global memory (through L1)
+  const bool stage = !OPT || K <= CELL_SMEM_KMAX;
+  double* sgrid = sm + cell_vts_doubles<R>(K, NV);     // [GF_COUNT][K]
+  double* stab = sgrid + (stage ? GF_COUNT * K : 0);   // [FM_TABLE_DOUBLES]
+  const double* grid = stage ? sgrid : P.grid;
+  const double* tab = stage ? stab : P.fmtab;
+  float* gridf = reinterpret_cast<float*>(stab + (stage ? FM_TABLE_DOUBLES : 0));  // [4][K], mixed only
   unsigned short* perm = reinterpret_cast<unsigned short*>(gridf + 4 * K);  // [nlev * CELL_TG], FP64 only
   unsigned char* key = reinterpret_cast<unsigned char*>(perm + (K - 2) * CELL_TG);
   R* whs = reinterpret_cast<R*>(                                          // [K][CELL_TG] half-level velocities
@@ -93,9 +99,11 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
   __shared__ int bucket[33];
 
   for (int c = threadIdx.x; c < NV * K * CELL_TG; c += blockDim.x) vts[c] = R(0.0);
-  for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) grid[c] = P.grid[c];
-  if (!kMixed)
-    for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  if (stage) {
+    for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) sgrid[c] = P.grid[c];
+    if (!kMixed)
+      for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) stab[c] = P.fmtab[c];
+  }
   if (kMixed) {
     const int rows[4] = {GF_RDGZ, GF_RDGZH, GF_RDZS, GF_RDZSH};
     for (int c = threadIdx.x; c < 4 * K; c += blockDim.x) gridf[c] = (float)P.grid[rows[c / K] * K + c % K];
@@ -268,6 +276,11 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
 // Shared-memory field slots, each [K][COL_TG] doubles.
 // S_DQI (the tendency of sedimenting QI) exists in the kernel with the scheme
 // switches only.
+// Above this many levels the column kernel with the scheme switches reads the
+// FastMath tables (8 KB) from global memory (they stay in L1) instead of
+// staging them in shared memory, so that its tile fits at MAX_KALL levels.
+constexpr int COL_FMTAB_SMEM_KMAX = 128;
+
 enum ColSlot {
   S_KINH, S_KINV, S_DRHOE, S_DRHOPHI, S_DKINH, S_DKINV, S_DRHOGU, S_DRHOGV, S_DRHOGW,
   S_DQR, S_DQS, S_DQG, S_RHOF, S_F, S_RGS, S_BASE, S_VI, S_VJ, S_COUNT,
@@ -386,9 +399,11 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
   S.bmin = reinterpret_cast<int*>(S.colacc + 6 * COL_TG);
   S.bmax = S.bmin + NROW_MAX * K;
   S.kc = reinterpret_cast<unsigned char*>(S.bmax + NROW_MAX * K);
-  double* tab = reinterpret_cast<double*>(
+  const bool tab_smem = !OPT || K <= COL_FMTAB_SMEM_KMAX;
+  double* after_kc = reinterpret_cast<double*>(
       (reinterpret_cast<uintptr_t>(S.kc + (size_t)K * COL_TG) + 15) & ~(uintptr_t)15);
-  long long* zkey = reinterpret_cast<long long*>(tab + FM_TABLE_DOUBLES);   // [2][K]: cmp_key of gzh, gzshift
+  const double* tab = tab_smem ? after_kc : P.fmtab;
+  long long* zkey = reinterpret_cast<long long*>(after_kc + (tab_smem ? FM_TABLE_DOUBLES : 0));   // [2][K]: cmp_key of gzh, gzshift
   float* gf = reinterpret_cast<float*>(zkey + 2 * K);   // MIX: dgz, dgzh, rdgz, rdgzh in FP32
   auto F = [&](int slot) { return S.f + (size_t)slot * ncell; };
   // FP32 views of slots (MIX): the flux source and flux of the momentum
@@ -403,7 +418,8 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
     for (int c = threadIdx.x; c < 4 * K; c += blockDim.x) gf[c] = (float)P.grid[rows[c / K] * K + c % K];
   }
   for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) S.colacc[c] = 0.0;
-  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  if (tab_smem)
+    for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) after_kc[c] = P.fmtab[c];
   __syncthreads();
   const M mth = make_math<M>(tab);
   const double* gzh = S.grid + GF_GZH * K;
@@ -1138,8 +1154,9 @@ cudaError_t launch_math(int fn, const double* x, const double* y, double* out, i
 // ------------------------------------------------------------------ launchers
 size_t cell_smem_bytes(int K, bool mixed, bool opt) {
   const size_t vts = mixed ? cell_vts_doubles<float>(K) : cell_vts_doubles<double>(K, opt ? 4 : 3);
+  const size_t staged = (!opt || K <= CELL_SMEM_KMAX) ? (size_t)GF_COUNT * K + FM_TABLE_DOUBLES : 0;
   // fall speeds, grid, tables, the FP32 reciprocal rows, the cell order and keys
-  return sizeof(double) * (vts + (size_t)GF_COUNT * K + FM_TABLE_DOUBLES) + sizeof(float) * 4 * K +
+  return sizeof(double) * (vts + staged) + sizeof(float) * 4 * K +
          (sizeof(unsigned short) + 1) * (size_t)(K - 2) * CELL_TG + 16 +
          (mixed ? sizeof(float) : sizeof(double)) * (size_t)K * CELL_TG;
 }
@@ -1150,7 +1167,8 @@ size_t column_smem_bytes(int K, bool opt) {
   const int TG = column_tile(K);
   const size_t nslot = opt ? S_COUNT_OPT : S_COUNT;
   const size_t nrow = opt ? 8 : 6;
-  return sizeof(double) * (nslot * K * TG + GF_COUNT * K + 6 * TG + FM_TABLE_DOUBLES) +
+  const size_t ntab = (!opt || K <= COL_FMTAB_SMEM_KMAX) ? FM_TABLE_DOUBLES : 0;
+  return sizeof(double) * (nslot * K * TG + GF_COUNT * K + 6 * TG + ntab) +
          sizeof(int) * 2 * nrow * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 4 * K;
 }
 

@@ -40,10 +40,11 @@ CASES = [
     ("convective", 48, 42, 12),
     ("cold", 48, 42, 13),
     ("convective", 40, 12, 14),
+    ("convective", 8, 160, 15),   # the deepest column the build takes (MAX_KALL)
 ]
 
 
-# (name, state variant, seed, switches that differ from the reference defaults)
+# (name, state variant, seed, switches that differ from the reference defaults[, gall, kall])
 OPTION_CASES = [
     ("noroh", "standard", 11, dict(roh2014=0, explicit_icegen=0)),
     ("noroh", "cold", 13, dict(roh2014=0, explicit_icegen=0)),
@@ -55,6 +56,8 @@ OPTION_CASES = [
     ("indir", "standard", 11, dict(aerosol_indirect=1)),
     ("all", "convective", 12, dict(roh2014=0, explicit_icegen=0, kk2000=0, qi_sediment=1, kin2kin=1,
                                    aerosol_indirect=1)),
+    ("all", "convective", 15, dict(roh2014=0, explicit_icegen=0, kk2000=0, qi_sediment=1, kin2kin=1,
+                                   aerosol_indirect=1), 8, 160),
 ]
 
 

@@ -87,7 +87,7 @@ def test_gpu_matches_oracle_full_region(variant, seed):
     assert_parity(got, want, f"{variant} 16900x42")
 
 
-@pytest.mark.parametrize("gall,kall", [(1, 42), (17, 42), (33, 12), (31, 5), (250, 7), (64, 96)])
+@pytest.mark.parametrize("gall,kall", [(1, 42), (17, 42), (33, 12), (31, 5), (250, 7), (64, 96), (24, 160)])
 def test_gpu_ragged_and_small_shapes(gall, kall):
     spec = StateSpec(gall=gall, kall=kall, lall=1, seed=gall * 1000 + kall, variant="convective")
     st = make_state(spec, out_fill=np.nan)
