@@ -97,9 +97,10 @@ typedef struct nsw6_options {
 void nsw6_default_options(nsw6_options* o);
 
 /* Selects the scheme switches for the following calls of the handle.  Any
- * non-default switch runs the FP64 step in the kernels built with the
- * switched branches; with one set, mp_driver_mixed, nsw6_set_precision(h, 1
- * or 2), nsw6_set_math(h, 1), mp_driver_tlm and mp_driver_adjoint return
+ * non-default switch runs the step (FP64, or mixed precision with
+ * mp_driver_mixed / nsw6_set_precision(h, 1)) in the kernels built with the
+ * switched branches; with one set, nsw6_set_precision(h, 2),
+ * nsw6_set_math(h, 1), mp_driver_tlm and mp_driver_adjoint return
  * NSW6_ERR_UNSUPPORTED. */
 int nsw6_set_options(nsw6_handle* h, const nsw6_options* o);
 int nsw6_get_options(const nsw6_handle* h, nsw6_options* o);

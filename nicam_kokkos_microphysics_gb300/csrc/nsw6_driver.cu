@@ -458,7 +458,8 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.mixed = h->mixed;
   P.opt = h->opt_active;
   P.ntr = h->opts.qi_sediment ? 4 : 3;
-  if (h->opt_active && (h->mixed != 0 || h->math_lib != 0)) return NSW6_ERR_UNSUPPORTED;
+  // the switches run in the FP64 and mixed-precision kernels (FastMath)
+  if (h->opt_active && (h->mixed == 2 || h->math_lib != 0)) return NSW6_ERR_UNSUPPORTED;
   if (h->opts.aerosol_indirect && !a[A_unccn]) return NSW6_ERR_BAD_ARG;
   P.unccn = a[A_unccn];
   P.rhog = a[A_rhog];

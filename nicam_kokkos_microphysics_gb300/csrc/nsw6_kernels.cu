@@ -1153,7 +1153,7 @@ cudaError_t launch_math(int fn, const double* x, const double* y, double* out, i
 
 // ------------------------------------------------------------------ launchers
 size_t cell_smem_bytes(int K, bool mixed, bool opt) {
-  const size_t vts = mixed ? cell_vts_doubles<float>(K) : cell_vts_doubles<double>(K, opt ? 4 : 3);
+  const size_t vts = mixed ? cell_vts_doubles<float>(K, opt ? 4 : 3) : cell_vts_doubles<double>(K, opt ? 4 : 3);
   const size_t staged = (!opt || K <= CELL_SMEM_KMAX) ? (size_t)GF_COUNT * K + FM_TABLE_DOUBLES : 0;
   // fall speeds, grid, tables, the FP32 reciprocal rows, the cell order and keys
   return sizeof(double) * (vts + staged) + sizeof(float) * 4 * K +
@@ -1231,7 +1231,10 @@ cudaError_t launch_prepare() {
         raise_smem_limit(nsw6_column_kernel<16, LibMath, false>, optin),
         raise_smem_limit(nsw6_column_kernel<8, LibMath, false>, optin),
         raise_smem_limit(nsw6_column_kernel<16, FastMath, true>, optin),
-        raise_smem_limit(nsw6_column_kernel<8, FastMath, true>, optin)};
+        raise_smem_limit(nsw6_column_kernel<8, FastMath, true>, optin),
+        raise_smem_limit(nsw6_cell_kernel<FloatMath, float, true>, optin),
+        raise_smem_limit(nsw6_column_kernel<16, FastMath, true, true>, optin),
+        raise_smem_limit(nsw6_column_kernel<8, FastMath, true, true>, optin)};
     done = cudaSuccess;
     for (cudaError_t x : r)
       if (x != cudaSuccess) done = x;
@@ -1252,7 +1255,8 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   const size_t s2 = column_smem_bytes(P.kall, opt);
   dim3 g1((P.gall + CELL_TG - 1) / CELL_TG, P.lall);
   if (ev) cudaEventRecord(ev[0], stream);
-  if (opt) nsw6_cell_kernel<FastMath, double, true><<<g1, CELL_THREADS, s1, stream>>>(P, C);
+  if (opt && P.mixed) nsw6_cell_kernel<FloatMath, float, true><<<g1, CELL_THREADS, s1, stream>>>(P, consts_to_float(C));
+  else if (opt) nsw6_cell_kernel<FastMath, double, true><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   else if (P.mixed) nsw6_cell_kernel<FloatMath, float><<<g1, CELL_THREADS, s1, stream>>>(P, consts_to_float(C));
   else if (P.math_lib) nsw6_cell_kernel<LibMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   else nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
@@ -1263,12 +1267,14 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   // every thread of the column kernel keeps at most 4 (tile 16) or 5 (tile 8) cells
   if ((size_t)nt * (tg == 16 ? 4 : 5) < (size_t)P.kall * tg) return cudaErrorInvalidConfiguration;
   if (tg == 16) {
-    if (opt) nsw6_column_kernel<16, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
+    if (opt && P.mixed) nsw6_column_kernel<16, FastMath, true, true><<<g2, nt, s2, stream>>>(P, C);
+    else if (opt) nsw6_column_kernel<16, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.mixed) nsw6_column_kernel<16, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.math_lib) nsw6_column_kernel<16, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
     else nsw6_column_kernel<16, FastMath, false><<<g2, nt, s2, stream>>>(P, C);
   } else {
-    if (opt) nsw6_column_kernel<8, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
+    if (opt && P.mixed) nsw6_column_kernel<8, FastMath, true, true><<<g2, nt, s2, stream>>>(P, C);
+    else if (opt) nsw6_column_kernel<8, FastMath, false, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.mixed) nsw6_column_kernel<8, FastMath, true><<<g2, nt, s2, stream>>>(P, C);
     else if (P.math_lib) nsw6_column_kernel<8, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
     else nsw6_column_kernel<8, FastMath, false><<<g2, nt, s2, stream>>>(P, C);

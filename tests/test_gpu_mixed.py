@@ -32,12 +32,15 @@ def errors(a: np.ndarray, b: np.ndarray) -> tuple[float, float]:
     return float(d.max() / bmax), float((d[sig] / np.abs(b[sig])).mean())
 
 
-def run_both(spec):
+def run_both(spec, options=None):
     torch = _torch()
     from nicam_kokkos_microphysics_gb300 import mp_init
     st = make_state(spec, out_fill=0.0)
     reg = region_view(st, 0)
-    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"])
+    if options and options.get("aerosol_indirect"):
+        # cloud condensation nuclei 1e7 .. 2e9 per m3: both branches of max(unccn 1e-6, Nc_def)
+        reg["unccn"][...] = np.random.default_rng(1000 + spec.seed).uniform(1.0e7, 2.0e9, reg["unccn"].shape)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], options=options)
     a = {n: torch.from_numpy(np.ascontiguousarray(reg[n])).cuda() for n in ARG_NAMES}
     b = {n: t.clone() for n, t in a.items()}
     drv.mp_driver(0, *[a[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
@@ -47,9 +50,32 @@ def run_both(spec):
     return ({n: a[n].cpu().numpy() for n in OUTPUT_NAMES}, {n: b[n].cpu().numpy() for n in OUTPUT_NAMES})
 
 
+OPTION_SETS = {
+    "noroh": dict(roh2014=0, explicit_icegen=0),
+    "berry": dict(kk2000=0),
+    "qi_sediment": dict(qi_sediment=1),
+    "kin2kin": dict(kin2kin=1),
+    "indir": dict(aerosol_indirect=1),
+    "all": dict(roh2014=0, explicit_icegen=0, kk2000=0, qi_sediment=1, kin2kin=1, aerosol_indirect=1),
+}
+
+
 @pytest.mark.parametrize("variant,seed", [("standard", 1001), ("convective", 1002), ("cold", 1003)])
 def test_mixed_within_targets(variant, seed):
-    fp64, mixed = run_both(StateSpec(gall=16900, kall=42, lall=1, seed=seed, variant=variant))
+    check_targets(variant, seed)
+
+
+@pytest.mark.parametrize("name,variant,seed", [("noroh", "cold", 1003), ("berry", "standard", 1001),
+                                               ("qi_sediment", "cold", 1003), ("kin2kin", "convective", 1002),
+                                               ("indir", "standard", 1001), ("all", "convective", 1002)])
+def test_mixed_with_switches_within_targets(name, variant, seed):
+    """The scheme switches in the mixed-precision kernels, against the FP64
+    kernels with the same switches (which the reference pins)."""
+    check_targets(variant, seed, OPTION_SETS[name], label=name)
+
+
+def check_targets(variant, seed, options=None, label=""):
+    fp64, mixed = run_both(StateSpec(gall=16900, kall=42, lall=1, seed=seed, variant=variant), options)
     lines = []
     for n in OUTPUT_NAMES:
         assert np.isfinite(mixed[n]).all(), n
@@ -64,7 +90,7 @@ def test_mixed_within_targets(variant, seed):
         mx, mean = errors(mixed[n], fp64[n])
         lines.append(f"{n} max {mx:.2e} mean {mean:.2e}")
         assert mx <= 1e-5, lines[-1]
-    print(f"\n[{variant}] " + "; ".join(lines))
+    print(f"\n[{variant}{' ' + label if label else ''}] " + "; ".join(lines))
 
 
 def test_mixed_entry_equals_precision_switch():

@@ -85,7 +85,13 @@ def test_gpu_options_reject_unsupported_paths():
     kall, gall = reg["rhog"].shape
     drv = mp_init("NSW6", gall, kall, gz, gzh, options=opts)
     t = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in reg.items()}
-    drv.set_precision("mixed")
+    # the CUDA-libm kernels and the serial (derivative-path) step take no switches
+    drv.set_math(1)
+    with pytest.raises(NSW6Error) as e:
+        drv.mp_driver(0, *[t[n] for n in ARG_NAMES], dt=dt, ct=0.0)
+    assert e.value.code == 5
+    drv.set_math(0)
+    drv.set_precision("serial")
     with pytest.raises(NSW6Error) as e:
         drv.mp_driver(0, *[t[n] for n in ARG_NAMES], dt=dt, ct=0.0)
     assert e.value.code == 5
