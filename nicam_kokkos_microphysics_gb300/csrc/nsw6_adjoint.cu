@@ -19,12 +19,17 @@
 //
 // Each stage is a function of one cell written over the scalar type T, its
 // inputs read through an accessor.  The forward kernels (T = double) store the
-// stage outputs; the adjoint kernels (T = RVar) re-record one cell's stage on a
-// short per-thread tape, seed its outputs with their adjoints, sweep the tape
-// and add the adjoints of its inputs, wherever they live (another level, the
-// cell phase's outputs, the caller's arrays), with atomic additions.  Every
-// cell of every column runs in parallel, where the serial column adjoint gave
-// one thread a whole column.
+// stage outputs.  The adjoint kernels (adj_s*_hw_kernel) recompute one cell's
+// stage and sweep it back statement by statement, adding the adjoints of its
+// inputs wherever they live (another level, the cell phase's outputs, the
+// caller's arrays): with atomics where other threads add to the same place,
+// in place where only the thread does (S3 in gather form, each cell
+// collecting the adjoints of the fluxes it feeds).  Adjoint mode 1 runs the
+// recorded form instead (T = RVar: the stage re-recorded on a short per-thread
+// tape, seeded, swept), which checks the hand-written sweeps.  Every cell of
+// every column runs in parallel.  This file also holds the cell phase's
+// hand-written adjoint kernels (its forward with a checkpoint of the costly
+// values, then the reverse sweep from it; nsw6_cell_adjoint.cuh).
 //
 // The arithmetic is that of the serial column step (nsw6_column_step.cuh),
 // which reproduces the production kernels bit for bit; discrete choices
@@ -719,7 +724,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_fwd_kernel(StageIO io) {
   }
 }
 
-// Adjoint of S4: seeds from the caller's output adjoints.
+// Adjoint of S4, recorded on a tape (adjoint mode 1): seeds from the caller's output adjoints.
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Consts C, TapeMem tm) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   __shared__ double tab[FM_TABLE_DOUBLES];
@@ -1491,7 +1496,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_hw_kernel(StageIO io) {
   }
 }
 
-// Adjoint of S2 (a work item per cell and flux).
+// Adjoint of S2, recorded on a tape (adjoint mode 1): a work item per cell and flux.
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_kernel(StageIO io, TapeMem tm) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
@@ -1573,7 +1578,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_hw_kernel(StageIO io) {
   }
 }
 
-// Adjoint of S1: seeds from S2's and S3's adjoints (WB).
+// Adjoint of S1, recorded on a tape (adjoint mode 1): seeds from S2's and S3's adjoints (WB).
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_kernel(StageIO io, TapeMem tm) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];

@@ -182,12 +182,17 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_tlm_kernel(Problem P, Consts 
 
 // ------------------------------------------------------------------ adjoint in stages
 // The adjoint step differentiates every part with one thread per cell:
-//   1. nsw6_adj_cellfwd_kernel  (per cell)    the FP64 cell phase, its outputs Y;
+//   1. the cell phase's forward (per cell), its outputs Y: in the recorded
+//      form nsw6_adj_cellfwd_kernel below; in the hand-written form (the
+//      default) adj_cell_save_kernel (nsw6_adjoint.cu), which also keeps a
+//      checkpoint of the costly forward values;
 //   2. the column phase's adjoint around Y in level-parallel stages
 //      (nsw6_adjoint.cu): adjoints of the step's inputs it reads directly
 //      (into xb) and of the cell phase's outputs (YB);
-//   3. nsw6_adj_cell_kernel     (per cell)    the adjoint of the cell phase:
-//      adjoints of the cell inputs (into xb) and of the parameters.
+//   3. the adjoint of the cell phase (per cell): adjoints of the cell inputs
+//      (into xb) and of the parameters; recorded on a tape by
+//      nsw6_adj_cell_kernel below, or swept by hand from the checkpoint by
+//      adj_cell_hw_kernel (nsw6_adjoint.cu).
 // Y / YB layout: [ADJ_NF][lall][kall][gall], fields below.
 enum AdjField {
   Y_RHOG, Y_RHOGE, Y_TEM, Y_RHOGQ, Y_Q = Y_RHOGQ + 6,   // Y_Q + n - 1 for q[n], n = 1..5
