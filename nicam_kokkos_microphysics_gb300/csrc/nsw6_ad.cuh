@@ -17,6 +17,8 @@
 // their derivative is the one of the branch taken.
 #pragma once
 
+#include <type_traits>
+
 #include "nsw6_common.cuh"
 #include "nsw6_fastmath.cuh"
 
@@ -208,6 +210,10 @@ struct ADMath {
     const double xv = val(x), yv = val(y);
     const double p = fm.pow(xv, yv);
     if (!(xv > 0.0)) return dep2(p, x, 0.0, y, 0.0);
+    if constexpr (std::is_same<T, Dual>::value) {
+      // a constant exponent (every pow of the scheme): no d/dy term, no log
+      if (y.d == 0.0) return Dual(p, (yv * p / xv) * x.d);
+    }
     return dep2(p, x, yv * p / xv, y, p * fm.log(xv));
   }
 };

@@ -1803,6 +1803,209 @@ __global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, Consts C, A
   }
 }
 
+// ------------------------------------------------------------------ tangent-linear step in stages
+// The same stages in forward mode (T = Dual): every cell of every column in
+// parallel.  StageIO's adjoint arrays hold the tangents here: xb the step's
+// argument tangents (read as inputs, written as outputs), YB the cell
+// outputs' tangents, WB the work fields' tangents.  The values of the work
+// fields and the flux bounds come from the forward kernels above.  The last
+// two stages also write the step's output values: the stage functions make
+// the production kernels' operations on the same values, so they are those
+// kernels' outputs bit for bit (tested against the step).
+template <>
+struct In<Dual> {
+  const StageIO& io;
+  int l, g;
+  __device__ Dual w(int f, int kk) const {
+    const size_t i = f * io.NC + io.L.f(l, kk, g);
+    return Dual(io.W[i], io.WB[i]);
+  }
+  __device__ Dual y(int f, int kk) const {
+    const size_t i = f * io.NC + io.L.f(l, kk, g);
+    return Dual(io.Y[i], io.YB[i]);
+  }
+  __device__ Dual x(int a, size_t i) const { return Dual(io.x.a[a][i], io.xb.a[a][i]); }
+};
+
+// Cell phase in forward mode: the FP64 cell physics over Dual (parameter
+// tangents through the folded constants), its outputs' values into Y and
+// tangents into YB.  The constants (one copy per block) sit in shared memory.
+__global__ void __launch_bounds__(128) tlm_cell_kernel(StageIO io, Consts C, const double* params,
+                                                       const double* dparams) {
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  __shared__ __align__(16) unsigned char ct_raw[sizeof(ConstsT<Dual>)];
+  ConstsT<Dual>& CT = *reinterpret_cast<ConstsT<Dual>*>(ct_raw);
+  const Problem& P = io.P;
+  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  if (threadIdx.x == 0) {
+    Dual p[7];
+    for (int i = 0; i < 7; ++i) p[i] = Dual(params[i], dparams ? dparams[i] : 0.0);
+    consts_with_params(C, p, CT);
+  }
+  __syncthreads();
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const ADMath<Dual> mth{fm};
+  const LayS& L = io.L;
+  const size_t NC = io.NC;
+  const int nint = P.kmax - P.kmin + 1;
+  const long long ncell = (long long)P.lall * nint * P.gall;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
+    const int g = (int)(c % P.gall);
+    const int k = P.kmin + (int)((c / P.gall) % nint);
+    const int l = (int)(c / ((long long)P.gall * nint));
+    const size_t i = L.f(l, k, g);
+    const In<Dual> x{io, l, g};
+    CellInT<Dual> in;
+    in.rhog = x.x(A_rhog, i);
+    in.tem = x.x(A_tem, i);
+    in.gsgam2 = x.x(A_gsgam2, i);
+    in.q0 = x.x(A_q, L.t(l, 0, k, g));
+    for (int n = 0; n < 6; ++n) in.rhogq[n] = x.x(A_rhogq, L.t(l, n, k, g));
+    CellOutT<Dual> o;
+    nsw6_cell<ADMath<Dual>, Dual, Dual>(CT, mth, P.dt, P.rdt, in, o);
+    auto put = [&](int f, const Dual& v) {
+      io.YB[f * NC + i] = v.d;
+      const_cast<double*>(io.Y)[f * NC + i] = v.v;
+    };
+    put(YS_RHOG, o.rhog);
+    put(YS_RHOGE, o.rhoge);
+    put(YS_TEM, o.tem);
+    for (int n = 0; n < 6; ++n) put(YS_RHOGQ + n, o.rhogq[n]);
+    for (int n = 1; n < 6; ++n) put(YS_Q + n - 1, o.q[n]);
+    put(YS_VT + 0, o.Vtr);
+    put(YS_VT + 1, o.Vts);
+    put(YS_VT + 2, o.Vtg);
+    put(YS_RE, o.rceff);
+    put(YS_RECLD, o.rceff_cld);
+    put(YS_RCTOP, o.rctop);
+    put(YS_TCTOP, o.tctop);
+  }
+}
+
+// S1 in forward mode: the work fields' tangents.
+__global__ void __launch_bounds__(STAGE_THREADS) tlm_s1_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    const In<Dual> in{io, l, g};
+    stage1<Dual>(in, grid, k, [&](int f, const Dual& v) { io.WB[f * io.NC + c] = v.d; });
+  }
+}
+
+// S2 in forward mode (a work item per cell and flux).
+__global__ void __launch_bounds__(STAGE_THREADS) tlm_s2_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  const size_t n = io.NC * 24;
+  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
+    const size_t c = w % io.NC;
+    const int j = (int)(w / io.NC);
+    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    const In<Dual> in{io, l, g};
+    io.WB[(W_F + j) * io.NC + c] = stage2<Dual>(in, grid, k, j).d;
+  }
+}
+
+// S3 in forward mode: work-field tangents, and the values and tangents of the
+// step's momentum, GPREC and surface outputs.
+__global__ void __launch_bounds__(STAGE_THREADS) tlm_s3_kernel(StageIO io) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  __syncthreads();
+  const LayS& L = io.L;
+  double* const* x = io.x.a;
+  double* const* dx = io.xb.a;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % L.G), k = (int)((c / L.G) % L.K), l = (int)(c / ((size_t)L.G * L.K));
+    const In<Dual> in{io, l, g};
+    const size_t ic = L.c(l, g);
+    auto out = [&](int a, size_t i, const Dual& v) {
+      x[a][i] = v.v;
+      dx[a][i] = v.d;
+    };
+    // GPREC: from the surface-ward flux at the interior levels, 0 elsewhere
+    if (k < io.P.kmin || k > io.P.kmax) out(A_GPREC, c, Dual(0.0));
+    stage3<Dual>(
+        in, grid, k, [&](int f, const Dual& v) { io.WB[f * io.NC + c] = v.d; },
+        [&](int f, const Dual& v) {
+          const int a = f == SF_RVX ? A_rhogvx : f == SF_RVY ? A_rhogvy : f == SF_RVZ ? A_rhogvz
+                      : f == SF_RW ? A_rhogw : A_GPREC;
+          out(a, c, v);
+        },
+        [&](int f, const Dual& v) {
+          switch (f) {
+            case SC_PRECIP0: out(A_precip, L.p(0, l, g), v); break;
+            case SC_PRECIP1: out(A_precip, L.p(1, l, g), v); break;
+            case SC_LH: out(A_precip_lh_heat, ic, v); break;
+            case SC_RHOE: out(A_precip_rhoe, ic, v); break;
+            case SC_RHOPHI: out(A_precip_rhophi, ic, v); break;
+            default: out(A_precip_rhokin, ic, v); break;
+          }
+        });
+  }
+}
+
+// S4 in forward mode: the values and tangents of the step's state outputs, of
+// the outputs the cell phase gives directly (effective radii, cloud top) and
+// of those the step sets to constants (the mp_driver epilogue,
+// mod_mp_driver.cpp:555-612; zero tangents).
+__global__ void __launch_bounds__(STAGE_THREADS) tlm_s4_kernel(StageIO io, Consts C) {
+  __shared__ double grid[GF_COUNT * MAX_KALL];
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  stage_smem(io.P, grid, tab);
+  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const LayS& L = io.L;
+  const size_t NC = io.NC;
+  double* const* x = io.x.a;
+  double* const* dx = io.xb.a;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
+    const int g = (int)(c % L.G), k = (int)((c / L.G) % L.K), l = (int)(c / ((size_t)L.G * L.K));
+    const In<Dual> in{io, l, g};
+    auto out = [&](int a, size_t i, const Dual& v) {
+      x[a][i] = v.v;
+      dx[a][i] = v.d;
+    };
+    auto y = [&](int f) { return Dual(io.Y[f * NC + c], io.YB[f * NC + c]); };
+    int it = 0;
+    const int rc = stage4<Dual>(in, C, grid, fm, k, [&](int f, const Dual& v) {
+      if (f == SF_RHOG) out(A_rhog, c, v);
+      else if (f == SF_RHOGE) out(A_rhoge, c, v);
+      else if (f == SF_RHO) out(A_rho, c, v);
+      else if (f == SF_TEM) out(A_tem, c, v);
+      else if (f == SF_PRE) out(A_pre, c, v);
+      else if (f == SF_QD) out(A_qd, c, v);
+      else if (f >= SF_RQ && f < SF_RQ + 6) out(A_rhogq, L.t(l, f - SF_RQ, k, g), v);
+      else if (f >= SF_Q && f < SF_Q + 6) out(A_q, L.t(l, f - SF_Q, k, g), v);
+    }, &it);
+    if (rc) record_err(io.P.status, rc, k, g, l, it);
+    const bool interior = (k >= io.P.kmin && k <= io.P.kmax);
+    out(A_re_liquid, c, interior ? y(YS_RE) : Dual(0.0));
+    out(A_re_cld, c, interior ? y(YS_RECLD) : Dual(0.0));
+    out(A_re_solid, c, Dual(20.0E-6));
+    out(A_GDCLW, c, Dual(0.0));
+    out(A_GDCFRC, c, Dual(0.0));
+    if (k == io.P.kmax) {
+      // cloud top (TagUpdateCLD): rwtop = sw rctop + (1 - sw) UNDEF, sw from tctop
+      const size_t ic = L.c(l, g);
+      const Dual rct = y(YS_RCTOP), tct = y(YS_TCTOP);
+      const double sw = (0.5 + copysign(0.5, tct.v - TEM00));
+      out(A_rctop, ic, rct);
+      out(A_tctop, ic, tct);
+      x[A_rwtop][ic] = (sw)*rct.v + (1.0 - sw) * UNDEF;
+      dx[A_rwtop][ic] = sw * rct.d;
+    }
+    if (k == 0) {
+      out(A_ISO1, L.p(0, l, g), Dual(0.0));
+      out(A_ISO1, L.p(1, l, g), Dual(0.0));
+      out(A_ISO2, L.p(0, l, g), Dual(0.0));
+      out(A_ISO2, L.p(1, l, g), Dual(0.0));
+    }
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
@@ -1819,6 +2022,45 @@ cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs&
   adj_cell_hw_kernel<<<152 * 2, 128, 0, stream>>>(P, C, x, xb, YB, pbar, ck);
   return cudaGetLastError();
 }
+
+// The tangent-linear step in stages: the cell phase in forward mode (Y and
+// its tangents), the column phase's forward values and flux bounds, then its
+// stages in forward mode writing the step's outputs into x and their tangents
+// into dx.  Y holds 2 x ADJ_Y_FIELDS fields (values, tangents); work as for
+// the adjoint.
+cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx,
+                              const double* params, const double* dparams, double* Y, double* work, int* bnd,
+                              cudaStream_t stream) {
+  StageIO io;
+  io.P = P;
+  io.L = LayS{P.kall, P.gall, P.lall};
+  io.NC = (size_t)P.lall * P.kall * P.gall;
+  io.x = x;
+  io.xb = dx;
+  io.Y = Y;
+  io.YB = Y + (size_t)ADJ_Y_FIELDS * io.NC;
+  io.W = work;
+  io.WB = work + (size_t)NWF * io.NC;
+  io.SB = nullptr;
+  io.bnd = bnd;
+  cudaError_t e;
+  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+  tlm_cell_kernel<<<152 * 4, 128, 0, stream>>>(io, C, params, dparams);
+  adj_s1_fwd_kernel<<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(
+      io);
+  adj_bounds_kernel<<<(int)((nkey + 127) / 128), 128, 0, stream>>>(P, bnd);
+  adj_s2_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  tlm_s1_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  tlm_s2_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  tlm_s3_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
+  tlm_s4_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);
+  return cudaGetLastError();
+}
+
+int adj_y_fields() { return ADJ_Y_FIELDS; }
 
 size_t adj_cell_ck_doubles(int lall, int kall, int gall) { return (size_t)CELL_CK_SLOTS * lall * (kall - 2) * gall; }
 

@@ -36,6 +36,10 @@ cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs&
 cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, double* ck, int check,
                                  cudaStream_t stream);
 size_t adj_cell_ck_doubles(int lall, int kall, int gall);
+cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx,
+                              const double* params, const double* dparams, double* Y, double* work, int* bnd,
+                              cudaStream_t stream);
+int adj_y_fields();
 size_t adj_stage_work_doubles(int lall, int kall, int gall);
 size_t adj_stage_bound_ints(int lall, int kall);
 int adj_stage_tape_cap();
@@ -586,15 +590,34 @@ int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
   return launch_cell_only(P, h->C, h->stream) == cudaSuccess ? NSW6_OK : NSW6_ERR_CUDA;
 }
 
-int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b) {
+// serial: the call runs the serial column step (one column per thread, at
+// most DERIV_MAX_KALL levels); the staged derivative kernels take any kall.
+int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b, bool serial) {
   if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
-  if (h->kall > DERIV_MAX_KALL || h->opt_active) return NSW6_ERR_UNSUPPORTED;
+  if ((serial && h->kall > DERIV_MAX_KALL) || h->opt_active) return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
     if ((arg_is_read(i) || arg_is_written(i)) && (!a[i] || !b[i])) return NSW6_ERR_BAD_ARG;
   if (!h->d_dparam) {
     if (cudaMalloc(&h->d_dparam, sizeof(double) * 16) != cudaSuccess ||
         cudaMalloc(&h->d_pbar, sizeof(double) * 8) != cudaSuccess ||
         cudaMalloc(&h->d_tmax, sizeof(int)) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+  }
+  return NSW6_OK;
+}
+
+// Cell-phase outputs and their tangents / adjoints (Y), the staged column
+// work fields, flux bounds and per-cell flags, sized for lall_max, kept in the
+// handle.
+int ensure_adj_work(nsw6_handle* h) {
+  if (adj_y_fields() != adj_nfields()) return NSW6_ERR_UNSUPPORTED;   // the two layouts of Y must agree
+  const size_t NC = (size_t)h->lall_max * h->kall * h->gall;
+  if (!h->d_Y && cudaMalloc(&h->d_Y, sizeof(double) * 2 * adj_nfields() * NC) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (!h->d_swork) {
+    if (cudaMalloc(&h->d_swork, sizeof(double) * adj_stage_work_doubles(h->lall_max, h->kall, h->gall)) !=
+            cudaSuccess ||
+        cudaMalloc(&h->d_sbnd, sizeof(int) * adj_stage_bound_ints(h->lall_max, h->kall)) != cudaSuccess ||
+        cudaMalloc(&h->d_done, sizeof(int) * NC) != cudaSuccess)
       return NSW6_ERR_CUDA;
   }
   return NSW6_OK;
@@ -1064,10 +1087,12 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
 int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
                   double dt, double ct) {
   (void)ct;
-  int rc = deriv_check(h, lall, args, targs);
+  // adjoint mode 1: the serial column step over Dual (one column per thread);
+  // otherwise the stages in forward mode, every cell in parallel
+  const bool serial = h && h->adj_mode == 1;
+  int rc = deriv_check(h, lall, args, targs, serial);
   if (rc != NSW6_OK) return rc;
-  rc = deriv_prepass(h, lall, args, dt);
-  if (rc != NSW6_OK) return rc;
+  if (serial && (rc = deriv_prepass(h, lall, args, dt)) != NSW6_OK) return rc;
   Problem P;
   rc = fill_problem(h, lall, args, dt, P);
   if (rc != NSW6_OK) return rc;
@@ -1081,7 +1106,13 @@ int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* 
     x.a[i] = args[i];
     dx.a[i] = targs[i];
   }
-  rc = finish(h, launch_tlm(P, h->C, x, dx, h->d_dparam, h->d_dparam + 8, h->stream));
+  if (serial) {
+    rc = finish(h, launch_tlm(P, h->C, x, dx, h->d_dparam, h->d_dparam + 8, h->stream));
+  } else {
+    if ((rc = ensure_adj_work(h)) != NSW6_OK) return rc;
+    rc = finish(h, launch_tlm_staged(P, h->C, x, dx, h->d_dparam, h->d_dparam + 8, h->d_Y, h->d_swork, h->d_sbnd,
+                                     h->stream));
+  }
   if (!h->sync_check && rc == NSW6_OK && cudaStreamSynchronize(h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
   return rc;
 }
@@ -1111,7 +1142,7 @@ int ensure_tape(TapeMem& t, size_t& bytes, int nslot, int cap) {
 int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* const* aargs, double* dparams,
                       double dt, double ct) {
   (void)ct;
-  int rc = deriv_check(h, lall, args, aargs);
+  int rc = deriv_check(h, lall, args, aargs, false);
   if (rc != NSW6_OK) return rc;
   Problem P;
   rc = fill_problem(h, lall, args, dt, P);
@@ -1124,8 +1155,7 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
     x.a[i] = args[i];
     xb.a[i] = aargs[i];
   }
-  const size_t NC = (size_t)h->lall_max * h->kall * h->gall;
-  if (!h->d_Y && cudaMalloc(&h->d_Y, sizeof(double) * 2 * adj_nfields() * NC) != cudaSuccess) return NSW6_ERR_CUDA;
+  if ((rc = ensure_adj_work(h)) != NSW6_OK) return rc;
   // the all-regions layout of Y for this call's lall
   const size_t NCl = (size_t)lall * h->kall * h->gall;
   double* Y = h->d_Y;
@@ -1136,14 +1166,6 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   };
   const long long ncell = (long long)lall * (h->kall - 2) * h->gall;
   const int ncell_slots = round_slots(ncell, ADJ_CELL_SLOTS);
-  // buffers of the staged column adjoint and the per-cell flags, sized for lall_max
-  if (!h->d_swork) {
-    if (cudaMalloc(&h->d_swork, sizeof(double) * adj_stage_work_doubles(h->lall_max, h->kall, h->gall)) !=
-            cudaSuccess ||
-        cudaMalloc(&h->d_sbnd, sizeof(int) * adj_stage_bound_ints(h->lall_max, h->kall)) != cudaSuccess ||
-        cudaMalloc(&h->d_done, sizeof(int) * (size_t)h->lall_max * h->kall * h->gall) != cudaSuccess)
-      return NSW6_ERR_CUDA;
-  }
   // the stage tapes serve only the recorded form (adj_mode 1)
   if (h->adj_mode == 1 &&
       (rc = ensure_tape(h->stape, h->stape_bytes, adj_stage_slots(), adj_stage_tape_cap())) != NSW6_OK)

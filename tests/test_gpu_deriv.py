@@ -57,8 +57,12 @@ def test_serial_forward_bitwise_equals_production(variant, gall, kall):
     drv.close()
 
 
-def test_adjoint_dot_product():
-    torch, drv, spec, st, x0 = _setup(1024, 42, 1, 77, "convective")
+@pytest.mark.parametrize("gall,kall,lall", [(1024, 42, 1), (192, 160, 2)])
+def test_adjoint_dot_product(gall, kall, lall):
+    """<ybar, J dx> + 0 = <J^T ybar, dx> + <pbar, dp> between the staged
+    tangent-linear and adjoint steps, also on the deepest columns (160 levels,
+    beyond the serial column step's 48)."""
+    torch, drv, spec, st, x0 = _setup(gall, kall, lall, 77, "convective")
     g = torch.Generator(device="cuda").manual_seed(5)
     dx = {n: torch.zeros_like(v) for n, v in x0.items()}
     for n in READ_NAMES:
@@ -76,7 +80,7 @@ def test_adjoint_dot_product():
     bar = _clone(ybar)
     pbar = drv.adjoint(spec.lall, _clone(x0), bar, dt=spec.dt)
     rhs = sum(float((bar[n] * dx[n]).sum()) for n in READ_NAMES) + float(np.dot(pbar, dp))
-    print(f"\ndot-product test: <ybar, J dx> = {lhs:.17e}, <J^T ybar, dx> = {rhs:.17e}, "
+    print(f"\ndot-product test ({gall}x{kall}x{lall}): <ybar, J dx> = {lhs:.17e}, <J^T ybar, dx> = {rhs:.17e}, "
           f"rel diff {abs(lhs - rhs) / abs(lhs):.2e}")
     assert abs(lhs - rhs) <= 1e-11 * abs(lhs)
     # the TLM's forward is the FP64 step
@@ -84,6 +88,34 @@ def test_adjoint_dot_product():
     drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
     for n in OUTPUT_NAMES:
         assert torch.equal(y[n], x[n]), n
+    drv.close()
+
+
+@pytest.mark.parametrize("variant,seed", [("standard", 51), ("convective", 52), ("cold", 53)])
+def test_staged_tlm_equals_serial(variant, seed):
+    """The tangent-linear step in stages (every cell in parallel) gives the
+    serial column step's tangents (adjoint mode 1: one column per thread over
+    Dual) to rounding, and the same output values bit for bit."""
+    torch, drv, spec, st, x0 = _setup(1024, 42, 2, seed, variant)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    dx = {n: torch.zeros_like(v) for n, v in x0.items()}
+    for n in READ_NAMES:
+        dx[n] = 1e-3 * x0[n].abs().mean() * torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64)
+    dp = np.array([1e-5, 1e-7, 1.0, 0.05, 0.5, 1e-13, 10.0])
+    xs, ts = _clone(x0), _clone(dx)
+    drv.tlm(spec.lall, xs, ts, dparams=dp, dt=spec.dt)
+    drv.set_adjoint_mode("tape")
+    xr, tr = _clone(x0), _clone(dx)
+    drv.tlm(spec.lall, xr, tr, dparams=dp, dt=spec.dt)
+    worst = 0.0
+    for n in OUTPUT_NAMES:
+        assert torch.equal(xs[n], xr[n]), n
+    for n in WRITE_NAMES:
+        scale = float(tr[n].abs().max())
+        err = float((ts[n] - tr[n]).abs().max()) / scale if scale > 0 else float(ts[n].abs().max())
+        worst = max(worst, err)
+        assert err <= 1e-9, (n, err)
+    print(f"\nstaged vs serial tangent-linear step ({variant}): worst field {worst:.2e}")
     drv.close()
 
 
