@@ -253,12 +253,17 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  * cells and flux-integral bounds of the sedimentation are held fixed; the
  * saturation-adjustment temperature is differentiated implicitly at its
  * converged value.  Parameters are the seven of nsw6_params in their order
- * (beta_saut, qicrt_saut, Cr, Cs, Cg, ice_nuc, kk_aut).  kall <= 48.
+ * (beta_saut, qicrt_saut, Cr, Cs, Cg, ice_nuc, kk_aut).  Any kall the handle
+ * takes (kall <= 48 with nsw6_set_adjoint_mode 1, whose serial column step
+ * holds a column per thread).
  *
- * mp_driver_tlm: advances `args` by one step (the FP64 step, evaluated one
- *   column per thread) and maps the tangents in `targs` (50 device pointers,
- *   same layouts; on entry dx, on exit dy) : dy = (dM/dx) dx + (dM/dp) dp,
- *   with dparams[7] a host array (NULL: no parameter tangent).
+ * mp_driver_tlm: advances `args` by one step (the FP64 step's outputs bit for
+ *   bit) and maps the tangents in `targs` (50 device pointers, same layouts;
+ *   on entry dx, on exit dy) : dy = (dM/dx) dx + (dM/dp) dp, with dparams[7]
+ *   a host array (NULL: no parameter tangent).  Every cell is evaluated in
+ *   forward mode (value and tangent) by its own thread, in the same
+ *   level-parallel stages as the adjoint; nsw6_set_adjoint_mode 1 selects the
+ *   serial column step over the same arithmetic instead (a check).
  *
  * mp_driver_adjoint: `args` is the state BEFORE the step and is not changed.
  *   `aargs` (50 device pointers): on entry the adjoints of the step's outputs,
@@ -276,12 +281,13 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
 int mp_driver_tlm(nsw6_handle* h, int lall, double* const* args, double* const* targs, const double* dparams,
                   double dt, double ct);
 
-/* Implementation of the adjoint inside mp_driver_adjoint: 0 (default) the
+/* Implementation of mp_driver_adjoint and mp_driver_tlm: 0 (default) the
  * hand-written reverse sweeps (no tape), the cell physics' from a checkpoint
- * of its costly forward values (49 doubles per cell, kept in the handle);
- * 1 the operations of the cell physics and of the column stages S1, S2, S4
- * recorded on per-cell tapes and swept back (the operator-overloading form,
- * for checking the hand-written ones); 2 as 0, and the hand-written forward
+ * of its costly forward values (49 doubles per cell, kept in the handle), and
+ * the staged tangent-linear step; 1 the operations of the cell physics and of
+ * the column stages S1, S2, S4 recorded on per-cell tapes and swept back (the
+ * operator-overloading form, for checking the hand-written ones), and the
+ * tangent-linear step on the serial column step; 2 as 0, and the hand-written forward
  * the checkpoint comes from is also checked against the step's cell physics
  * on every cell: a cell whose outputs differ in any bit ends the call with
  * NSW6_ERR_CHECK (nsw6_last_error's iters: the first differing output). */
