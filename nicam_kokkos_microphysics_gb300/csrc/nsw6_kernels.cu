@@ -364,11 +364,12 @@ __device__ __forceinline__ float flux_integral_f(const float* rhof_col, const fl
   return fabsf(f) >= (float)EPS ? f : 0.0f;
 }
 
-// MIX: the mixed-precision step: the momentum fluxes of the sedimentation (u,
-// v and w, full and half levels) are integrated and accumulated in FP32, and
-// the quotients of the final state use a plain reciprocal; the mass, energy
-// and kinetic-energy fluxes, their sums and the saturation adjustment stay
-// FP64.
+// MIX: the mixed-precision step: every flux of the sedimentation (mass,
+// energy, kinetic energy and momentum, full and half levels) is integrated in
+// FP32 from its FP64 source, the mass, energy and kinetic-energy divergences
+// accumulated in FP64 and the momentum ones in FP32, and the quotients of the
+// final state use a plain reciprocal; the state updates, KIN2EIN, the
+// thermodynamics and the saturation adjustment stay FP64.
 //
 // OPT: the kernel with the scheme switches (FP64): QI sedimentation (4
 // tracers), the KIN2KIN kinetic-energy correction (mod_precip_transport.cpp:
@@ -558,7 +559,8 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
           default: r = b * F(S_VJ)[c]; break;
         }
       }
-      F(S_RHOF)[c] = r;
+      if (MIX) FF(S_RHOF)[c] = (float)r;
+      else F(S_RHOF)[c] = r;
     };
     // flux divergence and surface fluxes (mod_precip_transport.cpp:782-842,
     // 900-954); the quotients by dt are the correctly rounded ones, formed
@@ -598,40 +600,35 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         }
       }
     };
-    // FP64 fluxes (the mixed step integrates the momentum fluxes in FP32
-    // below); the divergence of flux f and the source of flux f + 1 share a
-    // pass
-    const int nf = MIX ? 4 : 6;
-    for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
-    __syncthreads();
-    for (int f = 0; f < nf; ++f) {
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-        const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-        double fl = 0.0;
-        if (g < G && k >= kmin && k <= kmax)
-          fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[(size_t)k * G + g], bmn_f[k], bmx_f[k]);
-        F(S_F)[c] = fl;
-      }
+    // the divergence of flux f and the source of flux f + 1 share a pass
+    if (!MIX) {
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
       __syncthreads();
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-        divergence(f, c);
-        if (f + 1 < nf) source(f + 1, c);
-      }
-      __syncthreads();
-    }
-    if (MIX) {
-      // momentum fluxes in FP32
-      for (int f = 4; f < 6; ++f) {
-        float* rf = FF(S_RHOF);
-        float* ff = FF(S_F);
-        float* acc = FF(f == 4 ? S_DRHOGU : S_DRHOGV);
-        const float* dgzf = gf;
-        const float* rdgzf = gf + 2 * K;
+      for (int f = 0; f < 6; ++f) {
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-          const int gx = c % COL_TG, g = g0 + gx;
-          rf[c] = (g < G) ? (float)(F(S_BASE)[c] * F(f == 4 ? S_VI : S_VJ)[c]) : 0.0f;
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          double fl = 0.0;
+          if (g < G && k >= kmin && k <= kmax)
+            fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[(size_t)k * G + g], bmn_f[k], bmx_f[k]);
+          F(S_F)[c] = fl;
         }
         __syncthreads();
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          divergence(f, c);
+          if (f + 1 < 6) source(f + 1, c);
+        }
+        __syncthreads();
+      }
+    } else {
+      // FP32 integrals and divergences; mass, energy and kinetic-energy
+      // tendencies summed in FP64, momentum ones in FP32
+      const float* rf = FF(S_RHOF);
+      float* ff = FF(S_F);
+      const float* dgzf = gf;
+      const float* rdgzf = gf + 2 * K;
+      for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
+      __syncthreads();
+      for (int f = 0; f < 6; ++f) {
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
           float fl = 0.0f;
@@ -643,8 +640,39 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         __syncthreads();
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-          if (g >= G || k < kmin || k > kmax) continue;
-          acc[c] = acc[c] - (ff[c + COL_TG] - ff[c]) * rdgzf[k];
+          if (g < G && k >= kmin && k <= kmax) {
+            const float d = (ff[c + COL_TG] - ff[c]) * rdgzf[k];
+            switch (f) {
+              case 0:
+                F(dqs_slot)[c] = -(double)d;
+                if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + div_rn(-(double)ff[c], dt, P.rdt);
+                break;
+              case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - (double)d; break;
+              case 2: F(S_DRHOPHI)[c] = F(S_DRHOPHI)[c] - (double)d; break;
+              case 3: F(S_DKINH)[c] = F(S_DKINH)[c] - (double)d; break;
+              case 4: FF(S_DRHOGU)[c] = FF(S_DRHOGU)[c] - d; break;
+              default: FF(S_DRHOGV)[c] = FF(S_DRHOGV)[c] - d; break;
+            }
+            if (k == kmin && f < 4) {
+              double* acc = S.colacc;
+              const double fk = (double)ff[c];
+              const double fdt = div_rn(fk, dt, P.rdt);
+              switch (f) {
+                case 0:
+                  if (nq == I_QR) {
+                    acc[0 * COL_TG + gx] = acc[0 * COL_TG + gx] - fdt;
+                  } else {
+                    acc[1 * COL_TG + gx] = acc[1 * COL_TG + gx] - fdt;
+                    acc[2 * COL_TG + gx] = acc[2 * COL_TG + gx] + div_rn(fk * LHF0, dt, P.rdt);
+                  }
+                  break;
+                case 1: acc[3 * COL_TG + gx] = acc[3 * COL_TG + gx] - fdt; break;
+                case 2: acc[4 * COL_TG + gx] = acc[4 * COL_TG + gx] - fdt; break;
+                default: acc[5 * COL_TG + gx] = acc[5 * COL_TG + gx] - fdt; break;
+              }
+            }
+          }
+          if (f + 1 < 6) source(f + 1, c);
         }
         __syncthreads();
       }
@@ -663,10 +691,39 @@ __global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
         S.kc[c] = (unsigned char)departure_cell(gzs, zkey + K, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
       }
       F(S_BASE)[c] = qh;
-      F(S_RHOF)[c] = qh * F(S_KINV)[c];
+      if (MIX) FF(S_RHOF)[c] = (float)(qh * F(S_KINV)[c]);
+      else F(S_RHOF)[c] = qh * F(S_KINV)[c];
     }
     __syncthreads();
     for (int w = 0; w < 2; ++w) {
+      if (MIX && w == 0) {
+        // vertical kinetic energy in FP32, summed into the FP64 tendency; the
+        // pass also forms the FP32 source of momentum w
+        const float* rf = FF(S_RHOF);
+        float* ff = FF(S_F);
+        const float* dgzhf = gf + K;
+        const float* rdgzhf = gf + 3 * K;
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          float fl = 0.0f;
+          if (g < G && k >= kmin + 1 && k <= kmax)
+            fl = flux_integral_f<COL_TG>(rf + gx, dgzhf, k, S.kc[c], (float)zdis0h[(size_t)k * G + g], bmn_h[k],
+                                         bmx_f[k]);
+          ff[c] = fl;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          double r = 0.0;
+          if (g < G && k >= kmin + 1 && k <= kmax) {
+            F(S_DKINV)[c] = F(S_DKINV)[c] - (double)((ff[c] - ff[c - COL_TG]) * rdgzhf[k]);
+            r = F(S_BASE)[c] * P.rhogw[off + (size_t)k * G + g];
+          }
+          FF(S_RHOF)[c] = (float)r;
+        }
+        __syncthreads();
+        continue;
+      }
       if (MIX && w == 1) {
         // momentum w in FP32 (its source was written as FP32 by the w = 0 pass)
         const float* rf = FF(S_RHOF);
