@@ -18,7 +18,8 @@
 #include "nsw6_fastmath.cuh"
 
 namespace nsw6 {
-cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev);
+cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev,
+                        cudaEvent_t before_column = nullptr);
 cudaError_t launch_cell_only(const Problem& P, const Consts& C, cudaStream_t stream);
 cudaError_t launch_prepare();
 cudaError_t launch_serial(const Problem& P, const Consts& C, const ArgPtrs& x, cudaStream_t stream);
@@ -99,7 +100,8 @@ struct nsw6_handle {
   size_t stage_count = 0;
   // copy streams and per-chunk events of the pipelined host-memory path
   cudaStream_t s_in = nullptr, s_out = nullptr;
-  cudaEvent_t* ev_in = nullptr;
+  cudaEvent_t* ev_in = nullptr;    // a chunk's cell-kernel inputs have arrived
+  cudaEvent_t* ev_in2 = nullptr;   // its remaining inputs have arrived
   cudaEvent_t* ev_done = nullptr;
   cudaEvent_t ev_start = nullptr;
   // kernel timing: a ring of event triples folded into the sums when full
@@ -422,6 +424,16 @@ bool arg_is_read(int a) {
       return false;
   }
 }
+// Arguments the cell kernel reads or writes in place (the host pipeline copies
+// them in before the rest).
+bool cell_phase_arg(int a) {
+  switch (a) {
+    case A_rhog: case A_rhoge: case A_tem: case A_rhogq: case A_q: case A_gsgam2: case A_unccn:
+      return true;
+    default:
+      return false;
+  }
+}
 bool arg_is_written(int a) {
   switch (a) {
     case A_rhog: case A_rhogvx: case A_rhogvy: case A_rhogvz: case A_rhogw: case A_rhoge: case A_rhogq:
@@ -656,9 +668,11 @@ int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
         cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming) != cudaSuccess)
       return NSW6_ERR_CUDA;
     h->ev_in = new cudaEvent_t[h->lall_max]();
+    h->ev_in2 = new cudaEvent_t[h->lall_max]();
     h->ev_done = new cudaEvent_t[h->lall_max]();
     for (int i = 0; i < h->lall_max; ++i)
       if (cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&h->ev_in2[i], cudaEventDisableTiming) != cudaSuccess ||
           cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming) != cudaSuccess)
         return NSW6_ERR_CUDA;
   }
@@ -689,18 +703,24 @@ int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
       chost[i] = args[i] ? args[i] + ((i == A_precip || i == A_ISO1 || i == A_ISO2) ? (size_t)l0 * G : e * l0)
                          : nullptr;
     }
-    for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
-      if (!arg_is_read(i) && !(i == A_unccn && h->opts.aerosol_indirect)) continue;
-      err = cudaMemcpyAsync(cdev[i], chost[i], sizeof(double) * arg_region_elems(i, K, G) * nl,
-                            cudaMemcpyHostToDevice, h->s_in);
+    // inputs in two groups: first what the cell kernel reads or rewrites in
+    // place, then what only the column kernel reads, which arrives while the
+    // cell kernel runs
+    for (int group = 0; group < 2 && err == cudaSuccess; ++group) {
+      for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
+        if (!arg_is_read(i) && !(i == A_unccn && h->opts.aerosol_indirect)) continue;
+        if ((cell_phase_arg(i) ? 0 : 1) != group) continue;
+        err = cudaMemcpyAsync(cdev[i], chost[i], sizeof(double) * arg_region_elems(i, K, G) * nl,
+                              cudaMemcpyHostToDevice, h->s_in);
+      }
+      if (err == cudaSuccess) err = cudaEventRecord(group == 0 ? h->ev_in[nchunk] : h->ev_in2[nchunk], h->s_in);
     }
     if (err != cudaSuccess) break;
-    if ((err = cudaEventRecord(h->ev_in[nchunk], h->s_in)) != cudaSuccess) break;
     if ((err = cudaStreamWaitEvent(h->stream, h->ev_in[nchunk], 0)) != cudaSuccess) break;
     Problem P;
     rc = fill_problem(h, nl, cdev, dt, P);
     if (rc != NSW6_OK) break;
-    if ((err = launch_step(P, h->C, h->stream, nullptr)) != cudaSuccess) break;
+    if ((err = launch_step(P, h->C, h->stream, nullptr, h->ev_in2[nchunk])) != cudaSuccess) break;
     if ((err = cudaEventRecord(h->ev_done[nchunk], h->stream)) != cudaSuccess) break;
     if ((err = cudaStreamWaitEvent(h->s_out, h->ev_done[nchunk], 0)) != cudaSuccess) break;
     for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
@@ -797,9 +817,11 @@ int nsw6_destroy(nsw6_handle* h) {
   if (h->s_out) cudaStreamDestroy(h->s_out);
   for (int i = 0; h->ev_in && i < h->lall_max; ++i) {
     if (h->ev_in[i]) cudaEventDestroy(h->ev_in[i]);
+    if (h->ev_in2[i]) cudaEventDestroy(h->ev_in2[i]);
     if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
   }
   delete[] h->ev_in;
+  delete[] h->ev_in2;
   delete[] h->ev_done;
   if (h->ev_start) cudaEventDestroy(h->ev_start);
   cudaFree(h->d_stage);

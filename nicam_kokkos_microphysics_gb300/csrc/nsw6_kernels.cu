@@ -1299,7 +1299,10 @@ cudaError_t launch_prepare() {
   return done;
 }
 
-cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev) {
+// before_column (may be null): an event the column kernel waits for (inputs
+// that only it reads may still be arriving while the cell kernel runs).
+cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, cudaEvent_t* ev,
+                        cudaEvent_t before_column) {
   const size_t nkey = (size_t)P.lall * 2 * P.ntr * P.kall;
   cudaError_t e = launch_prepare();
   if (e != cudaSuccess) return e;
@@ -1318,6 +1321,7 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   else if (P.math_lib) nsw6_cell_kernel<LibMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   else nsw6_cell_kernel<FastMath, double><<<g1, CELL_THREADS, s1, stream>>>(P, C);
   if (ev) cudaEventRecord(ev[1], stream);
+  if (before_column && (e = cudaStreamWaitEvent(stream, before_column, 0)) != cudaSuccess) return e;
   const int tg = column_tile(P.kall);
   dim3 g2((P.gall + tg - 1) / tg, P.lall);
   const int nt = column_threads(P.kall);
