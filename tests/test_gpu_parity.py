@@ -134,16 +134,25 @@ def test_gpu_batched_equals_per_region():
     drv.close()
 
 
-@pytest.mark.parametrize("lall,lall_max", [(2, 2), (7, 8)])
-def test_gpu_host_entry_equals_device_entry(lall, lall_max):
+ALL_SWITCHES = dict(roh2014=0, explicit_icegen=0, kk2000=0, qi_sediment=1, kin2kin=1, aerosol_indirect=1)
+
+
+@pytest.mark.parametrize("lall,lall_max,precision,options", [
+    (2, 2, "fp64", None), (7, 8, "fp64", None), (7, 7, "mixed", None), (7, 7, "fp64", ALL_SWITCHES),
+    (3, 3, "mixed", ALL_SWITCHES)], ids=["fp64-2", "fp64-7", "mixed-7", "switches-7", "mixed-switches-3"])
+def test_gpu_host_entry_equals_device_entry(lall, lall_max, precision, options):
     """The host-memory entry point (copies inside the call, pipelined over
-    chunks of regions; 7 regions give chunks of 2, 2, 2 and 1) gives the
-    device result bit for bit."""
+    chunks of regions, 7 regions as 1, 2, 2, 1, 1; the cell kernel's inputs,
+    the CCN field among them, copied ahead of the rest) gives the device
+    result bit for bit, in both precisions and with the scheme switches."""
     torch = _torch()
     from nicam_kokkos_microphysics_gb300 import mp_init
-    spec = StateSpec(gall=300, kall=42, lall=lall, seed=5, variant="standard")
+    spec = StateSpec(gall=300, kall=42, lall=lall, seed=5, variant="convective" if options else "standard")
     st = make_state(spec, out_fill=np.nan)
-    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=lall_max)
+    if options:
+        st["unccn"][...] = np.random.default_rng(7).uniform(1.0e7, 2.0e9, st["unccn"].shape)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=lall_max, options=options)
+    drv.set_precision(precision)
     host = {n: st[n].copy() for n in ARG_NAMES}
     drv.run(host, dt=spec.dt)
     dev = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
