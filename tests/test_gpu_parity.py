@@ -219,14 +219,19 @@ def test_gpu_libm_mode_matches_oracle():
     assert_parity(got, want, "libm mode, convective 16900x42")
 
 
-def test_gpu_graph_steps_equal_repeated_calls():
+@pytest.mark.parametrize("precision,options", [("fp64", None), ("mixed", ALL_SWITCHES)], ids=["fp64", "mixed-switches"])
+def test_gpu_graph_steps_equal_repeated_calls(precision, options):
     """mp_driver_steps (one captured CUDA graph replayed) equals repeated
-    mp_driver_batched calls bit for bit, and re-captures for new arrays."""
+    mp_driver_batched calls bit for bit, and re-captures for new arrays and
+    for a change of precision."""
     torch = _torch()
     from nicam_kokkos_microphysics_gb300 import mp_init
     spec = StateSpec(gall=900, kall=42, lall=2, seed=44, variant="convective")
     st = make_state(spec, out_fill=np.nan)
-    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    if options:
+        st["unccn"][...] = np.random.default_rng(9).uniform(1.0e7, 2.0e9, st["unccn"].shape)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall, options=options)
+    drv.set_precision(precision)
     a = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
     b = {n: t.clone() for n, t in a.items()}
     c = {n: t.clone() for n, t in a.items()}
@@ -239,4 +244,11 @@ def test_gpu_graph_steps_equal_repeated_calls():
     for n in OUTPUT_NAMES:
         assert torch.equal(a[n], b[n]), n
         assert torch.equal(a[n], c[n]), n
+    # the other precision on the same arrays: the graph is captured again
+    drv.set_precision("fp64" if precision == "mixed" else "mixed")
+    drv.mp_driver_batched(spec.lall, *[a[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.mp_driver_steps(spec.lall, b, 1, dt=spec.dt)
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        assert torch.equal(a[n], b[n]), n
     drv.close()
