@@ -53,6 +53,7 @@ __device__ __forceinline__ bool operator!=(const Dual& a, const Dual& b) { retur
 
 __device__ __forceinline__ double val(double x) { return x; }
 __device__ __forceinline__ double val(const Dual& x) { return x.v; }
+__device__ __forceinline__ double val_of(const Dual& x) { return x.v; }
 __device__ __forceinline__ Dual with_value(const Dual& x, double v) { return Dual(v, x.d); }
 __device__ __forceinline__ double with_value(double, double v) { return v; }
 // f(x) with value fv and derivative dfdx at x.
@@ -155,6 +156,7 @@ __device__ __forceinline__ bool operator==(const RVar& a, const RVar& b) { retur
 __device__ __forceinline__ bool operator!=(const RVar& a, const RVar& b) { return a.v != b.v; }
 
 __device__ __forceinline__ double val(const RVar& x) { return x.v; }
+__device__ __forceinline__ double val_of(const RVar& x) { return x.v; }
 __device__ __forceinline__ RVar with_value(const RVar& x, double v) { return RVar(v, x.id); }
 __device__ __forceinline__ RVar dep(double fv, const RVar& x, double dfdx) { return record(fv, x.id, dfdx, -1, 0.0); }
 __device__ __forceinline__ RVar dep2(double fv, const RVar& x, double dx, const RVar& y, double dy) {

@@ -1830,6 +1830,7 @@ struct In<Dual> {
 // Cell phase in forward mode: the FP64 cell physics over Dual (parameter
 // tangents through the folded constants), its outputs' values into Y and
 // tangents into YB.  The constants (one copy per block) sit in shared memory.
+template <bool OPT>
 __global__ void __launch_bounds__(128) tlm_cell_kernel(StageIO io, Consts C, const double* params,
                                                        const double* dparams) {
   __shared__ double tab[FM_TABLE_DOUBLES];
@@ -1861,8 +1862,10 @@ __global__ void __launch_bounds__(128) tlm_cell_kernel(StageIO io, Consts C, con
     in.gsgam2 = x.x(A_gsgam2, i);
     in.q0 = x.x(A_q, L.t(l, 0, k, g));
     for (int n = 0; n < 6; ++n) in.rhogq[n] = x.x(A_rhogq, L.t(l, n, k, g));
+    // the CCN field (aerosol switch) is an input without a tangent
+    in.unccn = Dual((OPT && io.x.a[A_unccn]) ? io.x.a[A_unccn][i] : 0.0);
     CellOutT<Dual> o;
-    nsw6_cell<ADMath<Dual>, Dual, Dual>(CT, mth, P.dt, P.rdt, in, o);
+    nsw6_cell<ADMath<Dual>, Dual, Dual, OPT>(CT, mth, P.dt, P.rdt, in, o);
     auto put = [&](int f, const Dual& v) {
       io.YB[f * NC + i] = v.d;
       const_cast<double*>(io.Y)[f * NC + i] = v.v;
@@ -2047,7 +2050,10 @@ cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& 
   const size_t nkey = (size_t)P.lall * 6 * P.kall;
   if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-  tlm_cell_kernel<<<152 * 4, 128, 0, stream>>>(io, C, params, dparams);
+  if (P.opt)
+    tlm_cell_kernel<true><<<152 * 4, 128, 0, stream>>>(io, C, params, dparams);
+  else
+    tlm_cell_kernel<false><<<152 * 4, 128, 0, stream>>>(io, C, params, dparams);
   adj_s1_fwd_kernel<<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(
       io);
   adj_bounds_kernel<<<(int)((nkey + 127) / 128), 128, 0, stream>>>(P, bnd);

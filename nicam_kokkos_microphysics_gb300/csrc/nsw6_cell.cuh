@@ -78,6 +78,8 @@ __device__ __forceinline__ double sqrtR(double x) { return sqrt(x); }
 __device__ __forceinline__ float sqrtR(float x) { return sqrtf(x); }
 __device__ __forceinline__ double fabsR(double x) { return fabs(x); }
 __device__ __forceinline__ float fabsR(float x) { return fabsf(x); }
+__device__ __forceinline__ double val_of(double x) { return x; }   // the value of a scalar (its
+__device__ __forceinline__ float val_of(float x) { return x; }     // derivative types add theirs)
 __device__ __forceinline__ float dmin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float dmax(float a, float b) { return (a < b) ? b : a; }
 // x * f for a switch value f in {0, 1} (the reference's iceflg, delta1,
@@ -375,7 +377,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   if constexpr (OPT) {
     if (!expice && cold && !(temc + R(30.0) < Z)) {
       const R tb = dmin(dmax(temc, R(-30.99)), Z);
-      const int it = int(-tb);
+      const int it = int(-val_of(tb));   // the table row: piecewise constant in tb
       const R fact = -(tb + R(it - 1));
       const R a2 = (ONE - fact) * C.berg_a2[it] + fact * C.berg_a2[it + 1];
       const R ma2 = ONE - a2;

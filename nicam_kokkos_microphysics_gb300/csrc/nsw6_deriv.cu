@@ -199,6 +199,8 @@ enum AdjField {
   Y_VT = Y_Q + 5, Y_RE = Y_VT + 3, Y_RECLD, Y_RCTOP, Y_TCTOP, ADJ_NF
 };
 
+// OPT: the cell physics with the scheme switches (the CCN field a constant input).
+template <bool OPT>
 __global__ void __launch_bounds__(256) nsw6_adj_cellfwd_kernel(Problem P, Consts C, ArgPtrs x, double* Y) {
   __shared__ double tab[FM_TABLE_DOUBLES];
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
@@ -219,8 +221,9 @@ __global__ void __launch_bounds__(256) nsw6_adj_cellfwd_kernel(Problem P, Consts
     in.gsgam2 = x.a[A_gsgam2][i];
     in.q0 = x.a[A_q][L.t(l, 0, k, g)];
     for (int n = 0; n < 6; ++n) in.rhogq[n] = x.a[A_rhogq][L.t(l, n, k, g)];
+    in.unccn = (OPT && x.a[A_unccn]) ? x.a[A_unccn][i] : 0.0;
     CellOut o;
-    nsw6_cell(C, fm, P.dt, P.rdt, in, o);
+    nsw6_cell<FastMath, double, double, OPT>(C, fm, P.dt, P.rdt, in, o);
     Y[Y_RHOG * NC + i] = o.rhog;
     Y[Y_RHOGE * NC + i] = o.rhoge;
     Y[Y_TEM * NC + i] = o.tem;
@@ -252,6 +255,7 @@ __device__ __forceinline__ void tape_bind(const TapeMem& tm) {
 // done[cell] (may be null): set once a cell's adjoint has been added; cells
 // already done are skipped, so that a launch repeated with a longer tape after
 // an overflow adds each cell once.
+template <bool OPT>
 __global__ void __launch_bounds__(AD_THREADS, 3) nsw6_adj_cell_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb,
                                                                    const double* YB, TapeMem tm,
                                                                    const double* params, double* pbar,
@@ -287,8 +291,9 @@ __global__ void __launch_bounds__(AD_THREADS, 3) nsw6_adj_cell_kernel(Problem P,
     in.gsgam2 = leaf(x.a[A_gsgam2][i]);
     in.q0 = leaf(x.a[A_q][L.t(l, 0, k, g)]);
     for (int n = 0; n < 6; ++n) in.rhogq[n] = leaf(x.a[A_rhogq][L.t(l, n, k, g)]);
+    in.unccn = RVar((OPT && x.a[A_unccn]) ? x.a[A_unccn][i] : 0.0);
     CellOutT<RVar> o;
-    nsw6_cell<ADMath<RVar>, RVar, RVar>(CT, mth, P.dt, P.rdt, in, o);
+    nsw6_cell<ADMath<RVar>, RVar, RVar, OPT>(CT, mth, P.dt, P.rdt, in, o);
     atomicMax(tape_max, t.overflow ? t.cap + 1 : t.n);
     if (t.overflow || t.count_only) continue;
     for (int e = 0; e < t.n; ++e) t.adj[(size_t)e * t.nslot + t.slot] = 0.0;
@@ -347,14 +352,21 @@ cudaError_t launch_tlm(const Problem& P, const Consts& C, const ArgPtrs& x, cons
 constexpr int ADJ_NFIELDS = ADJ_NF;
 
 cudaError_t launch_adj_cellfwd(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, cudaStream_t stream) {
-  nsw6_adj_cellfwd_kernel<<<152 * 4, 256, 0, stream>>>(P, C, x, Y);
+  if (P.opt)
+    nsw6_adj_cellfwd_kernel<true><<<152 * 4, 256, 0, stream>>>(P, C, x, Y);
+  else
+    nsw6_adj_cellfwd_kernel<false><<<152 * 4, 256, 0, stream>>>(P, C, x, Y);
   return cudaGetLastError();
 }
 
 cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
                             const TapeMem& tm, const double* params, double* pbar, int* tape_max, int* done,
                             cudaStream_t stream) {
-  nsw6_adj_cell_kernel<<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, YB, tm, params, pbar,
+  if (P.opt)
+    nsw6_adj_cell_kernel<true><<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, YB, tm, params, pbar,
+                                                                         tape_max, done);
+  else
+    nsw6_adj_cell_kernel<false><<<tm.nslot / AD_THREADS, AD_THREADS, 0, stream>>>(P, C, x, xb, YB, tm, params, pbar,
                                                                          tape_max, done);
   return cudaGetLastError();
 }

@@ -603,10 +603,14 @@ int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
 }
 
 // serial: the call runs the serial column step (one column per thread, at
-// most DERIV_MAX_KALL levels); the staged derivative kernels take any kall.
+// most DERIV_MAX_KALL levels); the staged derivative kernels take any kall,
+// and the scheme switches that act in the cell physics only (Berry warm rain,
+// the aerosol effect, the classic snow moments with explicit ice generation).
 int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b, bool serial) {
   if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
-  if ((serial && h->kall > DERIV_MAX_KALL) || h->opt_active) return NSW6_ERR_UNSUPPORTED;
+  const bool cell_only = !h->opts.qi_sediment && !h->opts.kin2kin && h->opts.explicit_icegen;
+  if ((serial && h->kall > DERIV_MAX_KALL) || (h->opt_active && (serial || !cell_only)))
+    return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
     if ((arg_is_read(i) || arg_is_written(i)) && (!a[i] || !b[i])) return NSW6_ERR_BAD_ARG;
   if (!h->d_dparam) {
@@ -1195,13 +1199,15 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   h->stape.count_only = 0;
   double pb[8] = {};
   // the cell phase's outputs, then the column phase's adjoint (level-parallel stages)
-  const bool recorded = h->adj_mode == 1;
+  // the cell phase: hand-written, or recorded (adj_mode 1, and with the scheme
+  // switches, whose cell physics the hand-written sweep does not cover)
+  const bool recorded = h->adj_mode == 1 || h->opt_active;
   if (!recorded && !h->d_cellck &&
       cudaMalloc(&h->d_cellck, sizeof(double) * adj_cell_ck_doubles(h->lall_max, h->kall, h->gall)) != cudaSuccess)
     return NSW6_ERR_CUDA;
   if ((recorded ? launch_adj_cellfwd(P, h->C, x, Y, h->stream)
                 : launch_adj_cell_save(P, h->C, x, Y, h->d_cellck, h->adj_mode == 2, h->stream)) != cudaSuccess ||
-      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, recorded,
+      launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->adj_mode == 1,
                                h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
       (recorded && cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess))

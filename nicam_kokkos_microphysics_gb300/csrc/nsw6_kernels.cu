@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
     in.q0 = P.q[iq];
 #pragma unroll
     for (int n = 0; n < 6; ++n) in.rhogq[n] = P.rhogq[iq + (size_t)n * KG];
-    in.unccn = OPT ? P.unccn[i] : 0.0;
+    in.unccn = (OPT && P.unccn) ? P.unccn[i] : 0.0;   // required only with the aerosol switch
     CellOut o;
     nsw6_cell<M, R, double, OPT>(C, mth, P.dt, P.rdt, in, o);
     P.rhog[i] = o.rhog;

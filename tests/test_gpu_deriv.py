@@ -29,12 +29,20 @@ def _torch():
     return torch
 
 
-def _setup(gall=4096, kall=42, lall=1, seed=2024, variant="standard"):
+# the scheme switches that act in the cell physics only (the derivative
+# entry points take these): Berry warm rain, the aerosol effect, the classic
+# snow moments with explicit ice generation
+CELL_SWITCHES = dict(roh2014=0, explicit_icegen=1, kk2000=0, aerosol_indirect=1)
+
+
+def _setup(gall=4096, kall=42, lall=1, seed=2024, variant="standard", options=None):
     torch = _torch()
     from nicam_kokkos_microphysics_gb300 import mp_init
     spec = StateSpec(gall=gall, kall=kall, lall=lall, seed=seed, variant=variant)
     st = make_state(spec, out_fill=0.0)
-    drv = mp_init("NSW6", gall, kall, st["_gz"], st["_gzh"], lall_max=lall)
+    if options and options.get("aerosol_indirect"):
+        st["unccn"][...] = np.random.default_rng(seed).uniform(1.0e7, 2.0e9, st["unccn"].shape)
+    drv = mp_init("NSW6", gall, kall, st["_gz"], st["_gzh"], lall_max=lall, options=options)
     x0 = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
     return torch, drv, spec, st, x0
 
@@ -57,12 +65,13 @@ def test_serial_forward_bitwise_equals_production(variant, gall, kall):
     drv.close()
 
 
-@pytest.mark.parametrize("gall,kall,lall", [(1024, 42, 1), (192, 160, 2)])
-def test_adjoint_dot_product(gall, kall, lall):
+@pytest.mark.parametrize("gall,kall,lall,options", [(1024, 42, 1, None), (192, 160, 2, None),
+                                                    (1024, 42, 1, CELL_SWITCHES)], ids=["42", "160", "switches"])
+def test_adjoint_dot_product(gall, kall, lall, options):
     """<ybar, J dx> + 0 = <J^T ybar, dx> + <pbar, dp> between the staged
     tangent-linear and adjoint steps, also on the deepest columns (160 levels,
-    beyond the serial column step's 48)."""
-    torch, drv, spec, st, x0 = _setup(gall, kall, lall, 77, "convective")
+    beyond the serial column step's 48) and with the cell-physics switches."""
+    torch, drv, spec, st, x0 = _setup(gall, kall, lall, 77, "convective", options)
     g = torch.Generator(device="cuda").manual_seed(5)
     dx = {n: torch.zeros_like(v) for n, v in x0.items()}
     for n in READ_NAMES:
@@ -200,8 +209,9 @@ def _loss_diff(torch, yp, ym, w):
     return float(((pp - pm) * (pp + pm)).sum() + ((yp["rhogq"][:, 1] - ym["rhogq"][:, 1]) * w[None, :, None]).sum())
 
 
-def test_gradient_against_finite_differences():
-    torch, drv, spec, st, x0 = _setup(4096, 42, 1, 2024, "standard")
+@pytest.mark.parametrize("options", [None, CELL_SWITCHES], ids=["reference", "switches"])
+def test_gradient_against_finite_differences(options):
+    torch, drv, spec, st, x0 = _setup(4096, 42, 1, 2024, "standard", options)
     w = _loss_terms(torch, spec)
 
     def forward(x):
@@ -289,8 +299,8 @@ def test_gradient_against_finite_differences():
         worst = max(worst, err)
         print(f"  d L / d {pn}: adjoint {pbar[i]:+.10e}  FD {a1:+.10e}  rel {err:.1e}")
         assert err <= 1e-6, (pn, pbar[i], a1)
-    print(f"\ngradient vs FD: {checked} components checked, {skipped} next to a switch, {unresolved} below the "
-          f"resolution of the step, worst rel err {worst:.2e}")
+    print(f"\ngradient vs FD ({'switches' if options else 'reference'}): {checked} components checked, {skipped} "
+          f"next to a switch, {unresolved} below the resolution of the step, worst rel err {worst:.2e}")
     assert checked >= 20
     drv.close()
 
