@@ -479,8 +479,18 @@ __device__ int stage4(const In<T>& in, const Consts& C, const double* gr, const 
   cvt = cvt + qdl * CVDRY;
   T tem = ein / cvt;
   T pre = rho * tem * (qdl * RDRY + q[I_QV] * RVAP);
-  const T ein_moist = ein + q[I_QV] * LHV0;
-  const T qsum = q[I_QV] + q[I_QC];
+  // SATURATION_adjustment (mod_satadjust.cpp:274-362); with the switch
+  // explicit_icegen = 0 cloud ice joins it (satadjust_all)
+  const bool ice_adj = P.opt && C.opt_expice == 0.0;
+  T ein_moist, qsum;
+  if (ice_adj) {
+    ein_moist = ein + q[I_QV] * LHV0 - q[I_QI] * LHF0;
+    qsum = q[I_QV] + q[I_QC] + q[I_QI];
+    q[I_QI] = T(0.0);
+  } else {
+    ein_moist = ein + q[I_QV] * LHV0;
+    qsum = q[I_QV] + q[I_QC];
+  }
   q[I_QV] = qsum;
   q[I_QC] = T(0.0);
   T cvtot = qd * CVDRY;
@@ -489,9 +499,12 @@ __device__ int stage4(const In<T>& in, const Consts& C, const double* gr, const 
   const T rho_l = rho;
   tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
   int rc = 0;
-  if (interior) rc = satadjust_t(C, fm, P.itelim, ein_moist, qsum, rho_l, q, tem, iters);
+  if (interior)
+    rc = ice_adj ? satadjust_all_t(C, fm, P.itelim, ein_moist, qsum, rho_l, q, tem, iters)
+                 : satadjust_t(C, fm, P.itelim, ein_moist, qsum, rho_l, q, tem, iters);
   rq[I_QV] = rhog * q[I_QV];
   rq[I_QC] = rhog * q[I_QC];
+  if (ice_adj) rq[I_QI] = rhog * q[I_QI];
   cvtot = qd * CVDRY;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
@@ -2110,7 +2123,9 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_seed_kernel<<<152 * 4, 256, 0, stream>>>(io);
   adj_seed_columns_kernel<<<64, 256, 0, stream>>>(io);
-  if (recorded)
+  // S4 recorded also with the mixed-phase saturation adjustment, which the
+  // hand-written sweep does not cover
+  if (recorded || (P.opt && C.opt_expice == 0.0))
     adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
   else
     adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);

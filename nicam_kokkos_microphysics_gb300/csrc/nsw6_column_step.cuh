@@ -228,6 +228,118 @@ __device__ __forceinline__ int satadjust_t(const Consts& C, const FastMath& fm, 
   return 0;
 }
 
+// The mixed-phase saturation adjustment (satadjust_all, mod_satadjust.cpp:
+// 620-769, with the scheme switch explicit_icegen = 0) of one cell, as the
+// column kernel iterates it: liquid and ice saturation blended by alpha(T)
+// between sat_llimit and sat_ulimit, the excess split into cloud water and
+// cloud ice by alpha.  q[QC] and q[QI] are 0 at entry, qsum = qv + qc + qi
+// and ein_moist carries -qi LHF0.  The derivative is the implicit one at the
+// last iterate ts: F(T) = T cv + qsat LHV0 - qi LHF0 - Emoist, with the
+// outputs linear in T about ts.  Its T-slopes are the exact ones (d qsat / dT
+// = qsat (LovR / T^2 - 1 / T), cv = qd_l + qc + q2 + qi + q4 + q5 in CVdry),
+// not the iteration's approximate ones.
+template <class T>
+__device__ __forceinline__ int satadjust_all_t(const Consts& C, const FastMath& fm, int itelim, const T& ein_moist,
+                                               const T& qsum, const T& rho_l, T* q, T& tem, int* iters) {
+  T qd_l = T(1.0);
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
+  const double UL = C.sat_ulimit, LL = C.sat_llimit;
+  double tv = val(tem);
+  const double qsumv = val(qsum), rhov = val(rho_l), emv = val(ein_moist), qdv = val(qd_l);
+  double qv[6];
+#pragma unroll
+  for (int n = 0; n < 6; ++n) qv[n] = val(q[n]);
+  {
+    const double rtem = 1.0 / (dmax(tv, TEM_MIN));
+    double psat = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
+    const double alpha = dmin(dmax((tv - LL) / (UL - LL), 0.0), 1.0);
+    const double psati = PSAT0 * fm.exp(C.LovR_ice * (C.RTEM00 - rtem));
+    psat = psat * alpha + psati * (1.0 - alpha);
+    const double qsat = psat / (rhov * RVAP * tv);
+    if (!(qsumv - qsat > EPS)) return 0;
+  }
+  bool converged = false;
+  int ite;
+  double tprev = tv, alpha_s = 0.0, dalpha_s = 0.0, psatl_s = 0.0, psati_s = 0.0;
+  for (ite = 0; ite < itelim; ++ite) {
+    tprev = tv;
+    const double alpha = dmin(dmax((tv - LL) / (UL - LL), 0.0), 1.0);
+    const double rtem = 1.0 / (dmax(tv, TEM_MIN));
+    const double psatl = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
+    const double psati = PSAT0 * fm.exp(C.LovR_ice * (C.RTEM00 - rtem));
+    const double psat = psatl * alpha + psati * (1.0 - alpha);
+    const double qsatl = psatl / (rhov * RVAP * tv);
+    const double qsati = psati / (rhov * RVAP * tv);
+    const double qsat = psat / (rhov * RVAP * tv);
+    qv[I_QV] = qsat;
+    qv[I_QC] = (qsumv - qsat) * alpha;
+    qv[I_QI] = (qsumv - qsat) * (1.0 - alpha);
+    double cv = qdv * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cv = cv + qv[n] * CVDRY;
+    const double emoist_new = tv * cv + qv[I_QV] * LHV0 - qv[I_QI] * LHF0;
+    const double dalpha_dT = (!(UL - tv < 0.0) && !(tv - LL < 0.0)) ? 1.0 / (UL - LL) : 0.0;
+    const double t2 = tv * tv;
+    const double dqsatl_dT = (C.LovR_liq / t2) * qsatl;
+    const double dqsati_dT = (C.LovR_ice / t2) * qsati;
+    const double dqsat_dT = qsatl * dalpha_dT + dqsatl_dT * alpha - qsati * dalpha_dT + dqsati_dT * (1.0 - alpha);
+    const double dqc_dT = (qsumv - qsat) * dalpha_dT - dqsat_dT * alpha;
+    const double dqi_dT = -(qsumv - qsat) * dalpha_dT - dqsat_dT * (1.0 - alpha);
+    const double dcv_dT = dqsat_dT * CVDRY + dqc_dT * CVDRY + dqi_dT * CVDRY;
+    const double demoist_dT = tv * dcv_dT + cv + dqsat_dT * LHV0 - dqi_dT * LHF0;
+    const double dtemp = (emoist_new - emv) / demoist_dT;
+    alpha_s = alpha;
+    dalpha_s = dalpha_dT;
+    psatl_s = psatl;
+    psati_s = psati;
+    tv = tv - dtemp;
+    if (fabs(dtemp) < C.dtemp_criteria) {
+      converged = true;
+      break;
+    }
+    if (tv * 0.0 != 0.0) break;
+  }
+  *iters = ite;
+  if (!converged) {
+    tem = T(tv);
+    q[I_QV] = T(qv[I_QV]);
+    q[I_QC] = T(qv[I_QC]);
+    q[I_QI] = T(qv[I_QI]);
+    return (tv * 0.0 != 0.0) ? 4 : 3;
+  }
+  // F at the last iterate with the inputs' derivatives (Tc, alpha and the
+  // saturation pressures held at their values there)
+  const double ts = tprev;
+  const T Tc = T(ts);
+  const T qsT = T(psatl_s * alpha_s + psati_s * (1.0 - alpha_s)) / (rho_l * RVAP * Tc);
+  const T exc = qsum - qsT;
+  const T qcT = exc * alpha_s, qiT = exc * (1.0 - alpha_s);
+  T cvT = qd_l * CVDRY;
+  cvT = cvT + qcT * CVDRY;
+  cvT = cvT + q[2] * CVDRY;
+  cvT = cvT + qiT * CVDRY;
+  cvT = cvT + q[4] * CVDRY;
+  cvT = cvT + q[5] * CVDRY;
+  const T F = Tc * cvT + qsT * LHV0 - qiT * LHF0 - ein_moist;
+  // exact T-slopes at ts
+  const double rts = 1.0 / ts;
+  const double qsl = psatl_s / (rhov * RVAP * ts), qsi = psati_s / (rhov * RVAP * ts);
+  const double dqsl = qsl * (C.LovR_liq * rts * rts - rts), dqsi = qsi * (C.LovR_ice * rts * rts - rts);
+  const double qs_v = val(qsT), exc_v = qsumv - qs_v;
+  const double dqs = dqsl * alpha_s + dqsi * (1.0 - alpha_s) + (qsl - qsi) * dalpha_s;
+  const double dqc = -dqs * alpha_s + exc_v * dalpha_s;
+  const double dqi = -dqs * (1.0 - alpha_s) - exc_v * dalpha_s;
+  const double FT = val(cvT) + ts * (dqc + dqi) * CVDRY + dqs * LHV0 - dqi * LHF0;
+  const T temI = T(ts) - (F - T(val(F))) * (1.0 / FT);
+  const T dT = temI - Tc;
+  q[I_QV] = with_value(qsT + dT * dqs, qv[I_QV]);
+  q[I_QC] = with_value(qcT + dT * dqc, qv[I_QC]);
+  q[I_QI] = with_value(qiT + dT * dqi, qv[I_QI]);
+  tem = with_value(temI, tv);
+  return 0;
+}
+
 // The cell phase of one column: nsw6_cell on every interior level (as
 // nsw6_cell_kernel), leaving the fall speeds in w.vt.
 template <class T, class M>

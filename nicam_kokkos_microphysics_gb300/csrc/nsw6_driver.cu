@@ -604,12 +604,13 @@ int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
 
 // serial: the call runs the serial column step (one column per thread, at
 // most DERIV_MAX_KALL levels); the staged derivative kernels take any kall,
-// and the scheme switches that act in the cell physics only (Berry warm rain,
-// the aerosol effect, the classic snow moments with explicit ice generation).
+// and the scheme switches other than those of the transport (Berry warm rain,
+// the aerosol effect, the classic snow moments, the Bergeron process with the
+// mixed-phase saturation adjustment).
 int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b, bool serial) {
   if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
-  const bool cell_only = !h->opts.qi_sediment && !h->opts.kin2kin && h->opts.explicit_icegen;
-  if ((serial && h->kall > DERIV_MAX_KALL) || (h->opt_active && (serial || !cell_only)))
+  const bool staged_ok = !h->opts.qi_sediment && !h->opts.kin2kin;
+  if ((serial && h->kall > DERIV_MAX_KALL) || (h->opt_active && (serial || !staged_ok)))
     return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
     if ((arg_is_read(i) || arg_is_written(i)) && (!a[i] || !b[i])) return NSW6_ERR_BAD_ARG;
@@ -1192,8 +1193,9 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   };
   const long long ncell = (long long)lall * (h->kall - 2) * h->gall;
   const int ncell_slots = round_slots(ncell, ADJ_CELL_SLOTS);
-  // the stage tapes serve only the recorded form (adj_mode 1)
-  if (h->adj_mode == 1 &&
+  // the stage tapes serve the recorded form (adj_mode 1), and S4 with the
+  // mixed-phase saturation adjustment
+  if ((h->adj_mode == 1 || (h->opt_active && !h->opts.explicit_icegen)) &&
       (rc = ensure_tape(h->stape, h->stape_bytes, adj_stage_slots(), adj_stage_tape_cap())) != NSW6_OK)
     return rc;
   h->stape.count_only = 0;

@@ -96,8 +96,8 @@ def test_gpu_options_reject_unsupported_paths():
         drv.mp_driver(0, *[t[n] for n in ARG_NAMES], dt=dt, ct=0.0)
     assert e.value.code == 5
     drv.set_precision("fp64")
-    # the derivative entry points take only the switches of the cell physics
-    if opts["qi_sediment"] or opts["kin2kin"] or not (opts["roh2014"] or opts["explicit_icegen"]):
+    # the derivative entry points take the switches other than the transport's
+    if opts["qi_sediment"] or opts["kin2kin"]:
         kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
         tb = {n: v.reshape(batched_shape(kinds[n], 1, kall, gall)) for n, v in t.items()}   # one region
         bar = {n: torch.zeros_like(v) for n, v in tb.items()}
