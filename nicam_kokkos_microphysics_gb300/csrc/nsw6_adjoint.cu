@@ -979,16 +979,16 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double B_pre = SB[SF_PRE * NC + c], B_rhoge = SB[SF_RHOGE * NC + c];
       double b_rhog_o = SB[SF_RHOG * NC + c];
       // pre = ((rho_f pq_f) tem)
-      b_tem = fma(B_pre * rho_f, pq_f, b_tem);
+      b_tem += B_pre * rho_f * pq_f;
       double b_rho_f = SB[SF_RHO * NC + c] + B_pre * tem * pq_f;
       const double b_pq = B_pre * tem * rho_f;
       double b_qdf = b_pq * RDRY;
-      b_q[I_QV] = fma(b_pq, RVAP, b_q[I_QV]);
+      b_q[I_QV] += b_pq * RVAP;
       // rhoge = (tem rhog_o) cva
-      b_tem = fma(B_rhoge * rhog_o, cva, b_tem);
-      b_rhog_o = fma(B_rhoge * tem, cva, b_rhog_o);
+      b_tem += B_rhoge * rhog_o * cva;
+      b_rhog_o += B_rhoge * tem * cva;
       const double b_cva = B_rhoge * tem * rhog_o;
-      b_qdf = fma(b_cva, CVDRY, b_qdf);
+      b_qdf += b_cva * CVDRY;
       double b_qf[6];
 #pragma unroll
       for (int n = 1; n <= 5; ++n) b_qf[n] = b_q[n] + b_cva * CVDRY - b_qdf;
@@ -998,13 +998,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       for (int n = 0; n < 6; ++n) b_rqf[n] = SB[(SF_RQ + n) * NC + c];
 #pragma unroll
       for (int n = 1; n <= 5; ++n) {
-        b_rqf[n] = fma(b_qf[n], rrhog_o, b_rqf[n]);
-        b_rhog_o = fma(-(b_qf[n] * qf[n]), rrhog_o, b_rhog_o);
+        b_rqf[n] += b_qf[n] * rrhog_o;
+        b_rhog_o -= b_qf[n] * qf[n] * rrhog_o;
       }
-      b_rhog_o = fma(b_rho_f, rgsg, b_rhog_o);
-      b_gsg = fma(-(b_rho_f * rho_f), rgsg, b_gsg);
+      b_rhog_o += b_rho_f * rgsg;
+      b_gsg -= b_rho_f * rho_f * rgsg;
       // rhog_o = rhog (1 - d2)
-      b_rhog = fma(b_rhog_o, (1.0 - d2), b_rhog);
+      b_rhog += b_rhog_o * (1.0 - d2);
       const double b_d2 = -b_rhog_o * rhog;
       const double b_rq0a = (clip[0] ? b_d2 : 0.0) + (clip[0] ? 0.0 : b_rqf[0]);
       b_rq2[0] = b_rq0a;
@@ -1024,17 +1024,17 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     }
     // rhoge2 = (rhog tem) cvtot2 (the output at the halo levels)
     if (b_rhoge2 != 0.0) {
-      b_rhog = fma(b_rhoge2 * tem, cvtot2, b_rhog);
-      b_tem = fma(b_rhoge2 * rhog, cvtot2, b_tem);
+      b_rhog += b_rhoge2 * tem * cvtot2;
+      b_tem += b_rhoge2 * rhog * cvtot2;
       const double b_cv2 = b_rhoge2 * rhog * tem;
-      b_qd = fma(b_cv2, CVDRY, b_qd);
+      b_qd += b_cv2 * CVDRY;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) b_q[n] += b_cv2 * CVDRY;
     }
     // rq2[QV] = rhog q[QV], rq2[QC] = rhog q[QC]; rq2[n >= 2] = rq[n]
     b_rhog += b_rq2[I_QV] * q[I_QV] + b_rq2[I_QC] * q[I_QC];
-    b_q[I_QV] = fma(b_rq2[I_QV], rhog, b_q[I_QV]);
-    b_q[I_QC] = fma(b_rq2[I_QC], rhog, b_q[I_QC]);
+    b_q[I_QV] += b_rq2[I_QV] * rhog;
+    b_q[I_QC] += b_rq2[I_QC] * rhog;
     double b_rq[6] = {0, 0, 0, 0, 0, 0};
 #pragma unroll
     for (int n = 2; n <= 5; ++n) b_rq[n] += b_rq2[n];
@@ -1048,14 +1048,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double b_temI = b_tem + b_qsI * dqs;
       const double b_F = -b_temI * (1.0 / FT);
       const double b_cvT = b_F * ts;
-      b_qsT = fma(b_F, LHV0, b_qsT);
+      b_qsT += b_F * LHV0;
       b_ein_moist -= b_F;
       const double b_qd_l = b_cvT * CVDRY;
-      b_qsum = fma(b_cvT, CVDRY, b_qsum);
-      b_qsT = fma(-b_cvT, CVDRY, b_qsT);
+      b_qsum += b_cvT * CVDRY;
+      b_qsT -= b_cvT * CVDRY;
 #pragma unroll
       for (int n = 2; n <= 5; ++n) b_q[n] += b_cvT * CVDRY - b_qd_l;
-      b_rho_l = fma(-(b_qsT * qsT), (gsg * rrhog), b_rho_l);
+      b_rho_l -= b_qsT * qsT * (gsg * rrhog);
     } else {
       b_tem_p = b_tem;
       b_q0p = b_q[I_QV];
@@ -1066,8 +1066,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       const double b_num = b_tem_p * rcv1;
       const double b_cv1 = -b_tem_p * tem_p * rcv1;
       b_ein_moist += b_num;
-      b_qsum = fma(-b_num, LHV0, b_qsum);
-      b_qd = fma(b_cv1, CVDRY, b_qd);
+      b_qsum -= b_num * LHV0;
+      b_qd += b_cv1 * CVDRY;
 #pragma unroll
       for (int n = 2; n <= 5; ++n) b_q[n] += b_cv1 * CVDRY;
     }
@@ -1082,13 +1082,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     double b_ein = b_ein_moist;
     // pre0 = (rho1 tem0) pq0 (halo output)
     if (b_pre0 != 0.0) {
-      b_rho1 = fma(b_pre0 * tem0, pq0, b_rho1);
+      b_rho1 += b_pre0 * tem0 * pq0;
       const double b_tem0 = b_pre0 * rho1 * pq0;
       const double b_pq0 = b_pre0 * rho1 * tem0;
       const double b_qdl0 = b_pq0 * RDRY;
-      b_qo[0] = fma(b_pq0, RVAP, b_qo[0]);
+      b_qo[0] += b_pq0 * RVAP;
       const double rcvt = 1.0 / cvt;
-      b_ein = fma(b_tem0, rcvt, b_ein);
+      b_ein += b_tem0 * rcvt;
       const double b_cvt = -b_tem0 * tem0 * rcvt;
       const double b_qdl = b_qdl0 + b_cvt * CVDRY;
 #pragma unroll
@@ -1099,13 +1099,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     for (int n = 1; n <= 5; ++n) b_qo[n] -= b_qd;
     // ein = rhoge / rhog, rho1 = rhog / gsg, qo = rq / rhog
     double b_rhoge = b_ein * rrhog;
-    b_rhog = fma(-(b_ein * ein), rrhog, b_rhog);
-    b_rhog = fma(b_rho1, rgsg, b_rhog);
-    b_gsg = fma(-(b_rho1 * rho1), rgsg, b_gsg);
+    b_rhog -= b_ein * ein * rrhog;
+    b_rhog += b_rho1 * rgsg;
+    b_gsg -= b_rho1 * rho1 * rgsg;
 #pragma unroll
     for (int n = 0; n < 6; ++n) {
-      b_rq[n] = fma(b_qo[n], rrhog, b_rq[n]);
-      b_rhog = fma(-(b_qo[n] * qo[n]), rrhog, b_rhog);
+      b_rq[n] += b_qo[n] * rrhog;
+      b_rhog -= b_qo[n] * qo[n] * rrhog;
     }
     // KIN2EIN
     if (interior) {
@@ -1117,7 +1117,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       double b_w2c1 = b_tmp2 * kv0 + b_tmp * kvu[1];
       const double b_tmp_h = b_tmp;
       const double b_sq = b_tmp_h * rrhog;
-      b_rhog = fma(-(b_tmp_h * tmp_h), rrhog, b_rhog);
+      b_rhog -= b_tmp_h * tmp_h * rrhog;
       WBadd(W_RVX_N, c, b_sq * rvx);
       WBadd(W_RVY_N, c, b_sq * rvy);
       WBadd(W_RVZ_N, c, b_sq * rvz);
@@ -1139,7 +1139,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
         XBadd(A_gsgam2, cj - G, -b_c2b * c2b[s2] * rgjm);
       }
       // w2c0 = cfact gsg / gh, w2c1 = dfact gsg / gh
-      b_gsg = fma((b_w2c0 * cfact[k] + b_w2c1 * dfact[k]), rgh, b_gsg);
+      b_gsg += (b_w2c0 * cfact[k] + b_w2c1 * dfact[k]) * rgh;
       XBadd(A_gsgam2h, c + G, -(b_w2c0 * w2c0 + b_w2c1 * w2c1) * rgh);
       WBadd(W_RHOGE_N, c, b_rhoge);
     } else {
