@@ -356,12 +356,15 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   const R efrz = mth.exp(-C.A_frz * temc) - ONE;
   R Pihtr = (!below40 && !warm) ? densR * (qc * qc) * C.K_ihtr * efrz : Z;
   R Pimlt = warm ? dqi_dt : Z;
-  const R vents = R(0.65) * MOMs_1 + C.K_vents2 * sqrtR(fr * rNu) * MOMs_5ds_h;
+  // ventilation of snow and graupel: without the species their moments /
+  // slope terms are exact zeros and so is the sum (+0, skipped with its root)
+  const R vents = (MOMs_1 == Z && MOMs_5ds_h == Z) ? Z : R(0.65) * MOMs_1 + C.K_vents2 * sqrtR(fr * rNu) * MOMs_5ds_h;
   tmp = C.K_2pi * Rdens * (Sice - ONE) * Giv * vents;
   R Psdep = sel(sps, tmp);
   R Pssub = sel(!sps, -tmp);
   R Psmlt = dmax(C.K_2pi * Rdens * Gil * vents + C.K_clf * temc * (Psacw + Psacr), Z);
-  const R ventg = C.K_ventg1 * RLMDg_2 + C.K_ventg2 * sqrtR(C.Cg * fr * rNu * RLMDg_5dg);
+  const R ventg = (RLMDg_2 == Z && RLMDg_5dg == Z) ? Z
+                                                  : C.K_ventg1 * RLMDg_2 + C.K_ventg2 * sqrtR(C.Cg * fr * rNu * RLMDg_5dg);
   tmp = C.K_gdep * Rdens * (Sice - ONE) * Giv * ventg;
   R Pgdep = sel(sps, tmp);
   R Pgsub = sel(!sps, -tmp);
