@@ -376,7 +376,7 @@ __device__ __forceinline__ float flux_integral_f(const float* rhof_col, const fl
 // 1012-1068) and the mixed-phase saturation adjustment (satadjust_all,
 // mod_satadjust.cpp:620-769).
 template <int COL_TG, class M, bool MIX, bool OPT = false>
-__global__ void __launch_bounds__(256) nsw6_column_kernel(Problem P, Consts C) {
+__global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C) {
   extern __shared__ double smraw[];
   const int G = P.gall, K = P.kall, kmin = P.kmin, kmax = P.kmax;
   constexpr int NSLOT = OPT ? S_COUNT_OPT : S_COUNT;
@@ -1231,10 +1231,10 @@ size_t column_smem_bytes(int K, bool opt) {
 
 int column_threads(int K) {
   const int ncell = K * column_tile(K);
-  const int passes = (ncell + 255) / 256;
+  const int passes = (ncell + 383) / 384;
   int per = (ncell + passes - 1) / passes;
   per = (per + 31) / 32 * 32;
-  return per > 256 ? 256 : per;
+  return per > 384 ? 384 : per;
 }
 
 cudaError_t launch_prepare();
