@@ -899,6 +899,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
   __shared__ int nqueue;
   if (threadIdx.x == 0) nqueue = 0;
   __syncthreads();
+  const float lovr_f = float(C.LovR_liq);
 
   // mode 0: returns true when the cell was queued for the Newton iteration;
   // mode 1: finishes a queued cell with the result (tres, qvres, qcres)
@@ -987,16 +988,45 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       double qd_l = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
-      const double rtem = 1.0 / (dmax(tem, TEM_MIN));
-      double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-      if (ice_adj) {
-        const double alpha =
-            dmin(dmax((tem - C.sat_llimit) / (C.sat_ulimit - C.sat_llimit), 0.0), 1.0);
-        const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
-        psat = psat * alpha + psati * (1.0 - alpha);
+      // The test qsum - qsat(tem) > EPS is first decided in FP32 (liquid
+      // saturation only).  With x = LovR (1/T00 - 1/T) formed as
+      // LovR (T - T00) / (T T00), free of cancellation, the FP32 qsat is within
+      // 4.2e-7 |x| + 6e-7 (relative) of the FP64 one: seven roundings on x,
+      // expf's 2 ulp and five roundings after it.  For |x| <= 80 that is below
+      // 4e-5, so a cell whose distance from the threshold exceeds 1e-4 qsat
+      // (plus the rounding of the FP64 difference) takes the branch the FP64
+      // test takes; the FP64 test decides the cells closer to saturation and
+      // those outside that range, as the reference computes it.  Only the
+      // branch depends on qsat here: a saturated cell's Newton iteration
+      // recomputes it.
+      int sat = -1;
+      if (!ice_adj) {
+        const double tc = dmax(tem, TEM_MIN);
+        const float xf = lovr_f * (float(tc - TEM00) / (float(tc) * float(TEM00)));
+        if (fabsf(xf) <= 80.0f) {
+          const float qsf = (float(PSAT0) * expf(xf)) / (float(rho_l) * float(RVAP) * float(tem));
+          if (qsf > 0.0f && qsf <= 1.0e30f) {
+            const double qs = double(qsf);
+            const double d = qsum - qs;
+            const double m = 1.0e-4 * qs + 1.0e-15 * fabs(qsum);
+            if (d - m > EPS) sat = 1;
+            else if (d + m < EPS) sat = 0;
+          }
+        }
       }
-      const double qsat = psat / (rho_l * RVAP * tem);
-      if (qsum - qsat > EPS) {
+      if (sat < 0) {
+        const double rtem = 1.0 / (dmax(tem, TEM_MIN));
+        double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+        if (ice_adj) {
+          const double alpha =
+              dmin(dmax((tem - C.sat_llimit) / (C.sat_ulimit - C.sat_llimit), 0.0), 1.0);
+          const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
+          psat = psat * alpha + psati * (1.0 - alpha);
+        }
+        const double qsat = psat / (rho_l * RVAP * tem);
+        sat = (qsum - qsat > EPS) ? 1 : 0;
+      }
+      if (sat) {
         const int e = atomicAdd(&nqueue, 1);
         F(QE_TEM)[e] = tem;
         F(QE_EIN)[e] = ein_moist;
