@@ -101,8 +101,7 @@ void nsw6_default_options(nsw6_options* o);
  * mp_driver_mixed / nsw6_set_precision(h, 1)) in the kernels built with the
  * switched branches; with one set, nsw6_set_precision(h, 2) and
  * nsw6_set_math(h, 1) return NSW6_ERR_UNSUPPORTED, and so do mp_driver_tlm
- * and mp_driver_adjoint for the switches of the transport (qi_sediment,
- * kin2kin). */
+ * and mp_driver_adjoint with qi_sediment. */
 int nsw6_set_options(nsw6_handle* h, const nsw6_options* o);
 int nsw6_get_options(const nsw6_handle* h, nsw6_options* o);
 
@@ -256,12 +255,12 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  * converged value.  Parameters are the seven of nsw6_params in their order
  * (beta_saut, qicrt_saut, Cr, Cs, Cg, ice_nuc, kk_aut).  Any kall the handle
  * takes (kall <= 48 with nsw6_set_adjoint_mode 1, whose serial column step
- * holds a column per thread).  Of the scheme switches, all but those of the
- * transport are taken (kk2000 = 0, aerosol_indirect = 1, roh2014 = 0,
- * explicit_icegen = 0 with the mixed-phase saturation adjustment,
- * differentiated implicitly like the liquid one; the adjoint then records the
- * cell physics, and with explicit_icegen = 0 the last column stage, on
- * tapes); qi_sediment and kin2kin give NSW6_ERR_UNSUPPORTED.
+ * holds a column per thread).  Of the scheme switches, all but qi_sediment
+ * are taken (kk2000 = 0, aerosol_indirect = 1, roh2014 = 0, explicit_icegen =
+ * 0 with the mixed-phase saturation adjustment, differentiated implicitly like
+ * the liquid one, kin2kin; the adjoint then records the cell physics, and
+ * with explicit_icegen = 0 or kin2kin the last column stage, on tapes);
+ * qi_sediment gives NSW6_ERR_UNSUPPORTED.
  *
  * mp_driver_tlm: advances `args` by one step (the FP64 step's outputs bit for
  *   bit) and maps the tangents in `targs` (50 device pointers, same layouts;

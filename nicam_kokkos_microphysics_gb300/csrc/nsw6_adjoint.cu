@@ -108,6 +108,7 @@ struct StageIO {
   double* WB;
   const double* SB;     // seeds [NSF][NC] then [NSC][lall][gall]
   const int* bnd;       // flux bounds [lall][2][6][kall]: bmn then bmx
+  int kin2kin;          // the KIN2KIN switch: S4, not S3, gives the final momenta
 };
 
 // Where a leaf's adjoint is added.
@@ -444,11 +445,49 @@ __device__ int stage4(const In<T>& in, const Consts& C, const double* gr, const 
   const double* cfact = gr + GF_CFACT * K;
   const double* dfact = gr + GF_DFACT * K;
   const bool interior = (k >= kmin && k <= kmax);
+  const bool kin2kin = P.opt && C.opt_kin2kin != 0.0;
   const T rhog = in.w(W_RHOG_N, k);
   const T rrhog = 1.0 / rhog;
   T rhoge = in.w(W_RHOGE_N, k);
   const T gsg = xf(in, A_gsgam2, k);
-  if (interior) {
+  if (kin2kin) {
+    // KIN2KIN (mod_precip_transport.cpp:1012-1068) in place of KIN2EIN: the
+    // transported momenta rescaled to carry the transported kinetic energy,
+    // horizontal on [kmin, kmax], vertical on [kmin, kmax + 1]; the other
+    // levels pass through
+    T rvx = in.w(W_RVX_N, k), rvy = in.w(W_RVY_N, k), rvz = in.w(W_RVZ_N, k), rw = in.w(W_RW_N, k);
+    if (k >= kmin && k <= kmax + 1) {
+      if (k <= kmax) {
+        const T kin_h0 = in.w(W_KINH_N, k) / rhog;
+        T vx_t = rvx / rhog, vy_t = rvy / rhog, vz_t = rvz / rhog;
+        const T kin_h = 0.5 * (vx_t * vx_t + vy_t * vy_t + vz_t * vz_t);
+        if (val_of(kin_h) > 1.0E-20) {
+          const T r = sqrtR(fabsR(kin_h0 / kin_h));
+          vx_t = vx_t * r;
+          vy_t = vy_t * r;
+          vz_t = vz_t * r;
+        }
+        rvx = vx_t * rhog;
+        rvy = vy_t * rhog;
+        rvz = vz_t * rhog;
+      }
+      const double* afact = gr + GF_AFACT * K;
+      const double* bfact = gr + GF_BFACT * K;
+      const T gh = xf(in, A_gsgam2h, k);
+      const T c2w0 = afact[k] / gsg * gh;
+      const T c2w1 = bfact[k] / xf(in, A_gsgam2, k - 1) * gh;
+      const T rhogh = c2w0 * rhog + c2w1 * in.w(W_RHOG_N, k - 1);
+      const T kin_v0 = in.w(W_KINV_N, k) / rhogh;
+      T w_t = rw / rhogh;
+      const T kin_v = 0.5 * (w_t * w_t);
+      if (val_of(kin_v) > 1.0E-20) w_t = w_t * sqrtR(fabsR(kin_v0 / kin_v));
+      rw = w_t * rhogh;
+    }
+    fin(SF_RVX, rvx);
+    fin(SF_RVY, rvy);
+    fin(SF_RVZ, rvz);
+    fin(SF_RW, rw);
+  } else if (interior) {
     // KIN2EIN (mod_precip_transport.cpp:991-1011): the transported kinetic
     // energy tmp2 less that of the updated state
     const T gh = xf(in, A_gsgam2h, k + 1), rgh = 1.0 / gh;
@@ -755,10 +794,17 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Const
     if (rc) record_err(io.P.status, rc, k, g, l, it);
     if (stage_overflow(io, lg, k, g, l)) continue;
     tape_clear_adj();
-    for (int f = 0; f < NSF; ++f)
-      if (f != SF_RVX && f != SF_RVY && f != SF_RVZ && f != SF_RW && f != SF_GPREC) seed(outs[f], io.SB[f * io.NC + c]);
+    for (int f = 0; f < NSF; ++f) {
+      const bool momentum = f == SF_RVX || f == SF_RVY || f == SF_RVZ || f == SF_RW;
+      if (f != SF_GPREC && (!momentum || io.kin2kin)) seed(outs[f], io.SB[f * io.NC + c]);
+    }
     tape_reverse();
     scatter(io, lg);
+    if (io.kin2kin) {
+      // consumed here: the S3 sweep adds the momentum seeds only without KIN2KIN
+      double* SB = const_cast<double*>(io.SB);
+      SB[SF_RVX * io.NC + c] = SB[SF_RVY * io.NC + c] = SB[SF_RVZ * io.NC + c] = SB[SF_RW * io.NC + c] = 0.0;
+    }
   }
 }
 
@@ -1947,6 +1993,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s3_kernel(StageIO io) {
     stage3<Dual>(
         in, grid, k, [&](int f, const Dual& v) { io.WB[f * io.NC + c] = v.d; },
         [&](int f, const Dual& v) {
+          if (io.kin2kin && f != SF_GPREC) return;   // S4 gives the momenta
           const int a = f == SF_RVX ? A_rhogvx : f == SF_RVY ? A_rhogvy : f == SF_RVZ ? A_rhogvz
                       : f == SF_RW ? A_rhogw : A_GPREC;
           out(a, c, v);
@@ -1995,6 +2042,10 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s4_kernel(StageIO io, Const
       else if (f == SF_QD) out(A_qd, c, v);
       else if (f >= SF_RQ && f < SF_RQ + 6) out(A_rhogq, L.t(l, f - SF_RQ, k, g), v);
       else if (f >= SF_Q && f < SF_Q + 6) out(A_q, L.t(l, f - SF_Q, k, g), v);
+      else if (f == SF_RVX) out(A_rhogvx, c, v);
+      else if (f == SF_RVY) out(A_rhogvy, c, v);
+      else if (f == SF_RVZ) out(A_rhogvz, c, v);
+      else if (f == SF_RW) out(A_rhogw, c, v);
     }, &it);
     if (rc) record_err(io.P.status, rc, k, g, l, it);
     const bool interior = (k >= io.P.kmin && k <= io.P.kmax);
@@ -2059,6 +2110,7 @@ cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& 
   io.WB = work + (size_t)NWF * io.NC;
   io.SB = nullptr;
   io.bnd = bnd;
+  io.kin2kin = P.opt && C.opt_kin2kin != 0.0;
   cudaError_t e;
   const size_t nkey = (size_t)P.lall * 6 * P.kall;
   if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
@@ -2109,6 +2161,7 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   io.WB = work + (size_t)NWF * io.NC;
   io.SB = work + 2 * (size_t)NWF * io.NC;
   io.bnd = bnd;
+  io.kin2kin = P.opt && C.opt_kin2kin != 0.0;
   const int blocks = tm.nslot / STAGE_THREADS;
   cudaError_t e;
   if ((e = cudaMemsetAsync(io.WB, 0, sizeof(double) * NWF * io.NC, stream)) != cudaSuccess) return e;
@@ -2123,9 +2176,9 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_seed_kernel<<<152 * 4, 256, 0, stream>>>(io);
   adj_seed_columns_kernel<<<64, 256, 0, stream>>>(io);
-  // S4 recorded also with the mixed-phase saturation adjustment, which the
-  // hand-written sweep does not cover
-  if (recorded || (P.opt && C.opt_expice == 0.0))
+  // S4 recorded also with the mixed-phase saturation adjustment and with
+  // KIN2KIN, which the hand-written sweep does not cover
+  if (recorded || (P.opt && C.opt_expice == 0.0) || io.kin2kin)
     adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
   else
     adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);

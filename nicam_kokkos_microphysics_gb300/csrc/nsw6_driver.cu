@@ -604,12 +604,12 @@ int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
 
 // serial: the call runs the serial column step (one column per thread, at
 // most DERIV_MAX_KALL levels); the staged derivative kernels take any kall,
-// and the scheme switches other than those of the transport (Berry warm rain,
-// the aerosol effect, the classic snow moments, the Bergeron process with the
-// mixed-phase saturation adjustment).
+// and every scheme switch but QI sedimentation (Berry warm rain, the aerosol
+// effect, the classic snow moments, the Bergeron process with the mixed-phase
+// saturation adjustment, KIN2KIN).
 int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b, bool serial) {
   if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
-  const bool staged_ok = !h->opts.qi_sediment && !h->opts.kin2kin;
+  const bool staged_ok = !h->opts.qi_sediment;
   if ((serial && h->kall > DERIV_MAX_KALL) || (h->opt_active && (serial || !staged_ok)))
     return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
@@ -1194,8 +1194,8 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   const long long ncell = (long long)lall * (h->kall - 2) * h->gall;
   const int ncell_slots = round_slots(ncell, ADJ_CELL_SLOTS);
   // the stage tapes serve the recorded form (adj_mode 1), and S4 with the
-  // mixed-phase saturation adjustment
-  if ((h->adj_mode == 1 || (h->opt_active && !h->opts.explicit_icegen)) &&
+  // mixed-phase saturation adjustment or KIN2KIN
+  if ((h->adj_mode == 1 || (h->opt_active && (!h->opts.explicit_icegen || h->opts.kin2kin))) &&
       (rc = ensure_tape(h->stape, h->stape_bytes, adj_stage_slots(), adj_stage_tape_cap())) != NSW6_OK)
     return rc;
   h->stape.count_only = 0;

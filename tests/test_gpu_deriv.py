@@ -35,6 +35,8 @@ def _torch():
 CELL_SWITCHES = dict(roh2014=0, explicit_icegen=1, kk2000=0, aerosol_indirect=1)
 # and with the Bergeron process and the mixed-phase saturation adjustment
 ICE_SWITCHES = dict(roh2014=0, explicit_icegen=0, kk2000=0, aerosol_indirect=1)
+# the transport's kinetic-energy correction KIN2KIN in place of KIN2EIN
+KIN2KIN = dict(kin2kin=1)
 
 
 def _setup(gall=4096, kall=42, lall=1, seed=2024, variant="standard", options=None):
@@ -69,8 +71,9 @@ def test_serial_forward_bitwise_equals_production(variant, gall, kall):
 
 @pytest.mark.parametrize("gall,kall,lall,options,variant", [
     (1024, 42, 1, None, "convective"), (192, 160, 2, None, "convective"),
-    (1024, 42, 1, CELL_SWITCHES, "convective"), (1024, 42, 1, ICE_SWITCHES, "cold")],
-    ids=["42", "160", "switches", "ice-switches"])
+    (1024, 42, 1, CELL_SWITCHES, "convective"), (1024, 42, 1, ICE_SWITCHES, "cold"),
+    (1024, 42, 1, KIN2KIN, "convective")],
+    ids=["42", "160", "switches", "ice-switches", "kin2kin"])
 def test_adjoint_dot_product(gall, kall, lall, options, variant):
     """<ybar, J dx> + 0 = <J^T ybar, dx> + <pbar, dp> between the staged
     tangent-linear and adjoint steps, also on the deepest columns (160 levels,
@@ -81,14 +84,17 @@ def test_adjoint_dot_product(gall, kall, lall, options, variant):
     for n in READ_NAMES:
         dx[n] = 1e-3 * x0[n].abs().mean() * torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64)
     dp = np.array([1e-5, 1e-7, 1.0, 0.05, 0.5, 1e-13, 10.0])
+    # output weights: every output, or with KIN2KIN the four momenta alone
+    # (which it changes; the other outputs' terms would dominate the sums)
+    ynames = ("rhogvx", "rhogvy", "rhogvz", "rhogw") if options is KIN2KIN else WRITE_NAMES
     ybar = {n: torch.zeros_like(v) for n, v in x0.items()}
-    for n in WRITE_NAMES:
+    for n in ynames:
         ybar[n] = torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64) / \
             (x0[n].abs().mean() + 1e-30)
     # TLM
     x, t = _clone(x0), _clone(dx)
     drv.tlm(spec.lall, x, t, dparams=dp, dt=spec.dt)
-    lhs = sum(float((ybar[n] * t[n]).sum()) for n in WRITE_NAMES)
+    lhs = sum(float((ybar[n] * t[n]).sum()) for n in ynames)
     # adjoint
     bar = _clone(ybar)
     pbar = drv.adjoint(spec.lall, _clone(x0), bar, dt=spec.dt)
@@ -329,6 +335,92 @@ def test_gradient_against_finite_differences(options, variant):
         assert err <= tol, (pn, pbar[i], a1)
     print(f"\ngradient vs FD ({variant}, {options or 'reference'}): {checked} components checked, {skipped} "
           f"next to a switch, {unresolved} below the resolution of the step, worst rel err {worst:.2e}")
+    assert checked >= 20
+    drv.close()
+
+
+def test_kin2kin_gradient_against_finite_differences():
+    """With KIN2KIN the final momenta are the transported ones rescaled to
+    carry the transported kinetic energy.  The adjoint gradient of a random
+    weighted sum of the four momentum outputs against central differences of
+    the forward step, in columns with falling rain, for the momenta, the
+    density and the rain water, and for the fall-speed parameters."""
+    torch, drv, spec, st, x0 = _setup(1024, 42, 1, 2024, "convective", KIN2KIN)
+    gen = torch.Generator(device="cuda").manual_seed(9)
+    mom = ("rhogvx", "rhogvy", "rhogvz", "rhogw")
+    wts = {n: torch.randn(x0[n].shape, generator=gen, device="cuda", dtype=torch.float64) for n in mom}
+
+    def forward(x):
+        y = _clone(x)
+        drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        return y
+
+    def ldiff(yp, ym):   # L(yp) - L(ym) term by term
+        return float(sum((wts[n] * (yp[n] - ym[n])).sum() for n in mom))
+
+    y0 = forward(x0)
+    bar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    for n in mom:
+        bar[n] = wts[n].clone()
+    pbar = drv.adjoint(spec.lall, _clone(x0), bar, dt=spec.dt)
+    prc = (y0["precip"][0, 0] + y0["precip"][1, 0]).abs().cpu().numpy()
+    cols = np.random.default_rng(4).choice(np.argsort(prc)[-200:], 12, replace=False)
+    fields = (("rhogvx", lambda k, g: (0, k, g), None), ("rhogw", lambda k, g: (0, k, g), None),
+              ("rhog", lambda k, g: (0, k, g), None), ("rhogq", lambda k, g: (0, 2, k, g), 2))
+    checked = skipped = 0
+    worst = 0.0
+    for g in cols:
+        for name, idx, nq in fields:
+            gcol = bar[name][0, :, g] if nq is None else bar[name][0, nq, :, g]
+            k = int(gcol[1:spec.kall - 1].abs().argmax()) + 1
+            ix = idx(k, int(g))
+            x = float(x0[name][ix])
+            adj = float(bar[name][ix])
+            if x == 0.0 or adj == 0.0:
+                continue
+            h = 1e-6 * abs(x)
+
+            def fd(hh, name=name, ix=ix):
+                xp, xm = _clone(x0), _clone(x0)
+                xp[name][ix] += hh
+                xm[name][ix] -= hh
+                return ldiff(forward(xp), forward(xm)) / (2 * hh)
+
+            a1, a2 = fd(h), fd(h / 4)
+            scale = max(abs(a1), abs(adj), 1e-300)
+            if abs(a1 - a2) > 1e-6 * scale:   # a switch flips between the FD points
+                skipped += 1
+                continue
+            checked += 1
+            err = abs(adj - a1) / scale
+            worst = max(worst, err)
+            print(f"  d L / d {name}{ix}: adjoint {adj:+.10e}  FD {a1:+.10e}  rel {err:.1e}")
+            assert err <= 1e-6, (name, ix, adj, a1)
+    base = drv.get_params()
+    for pn in ("Cr", "Cs", "Cg"):
+        i = PARAMS.index(pn)
+        p0 = base[pn]
+        h = 1e-6 * abs(p0)
+
+        def yp(v, pn=pn, p0=p0):
+            drv.set_params(**{pn: v})
+            out = forward(x0)
+            drv.set_params(**{pn: p0})
+            return out
+
+        a1 = ldiff(yp(p0 + h), yp(p0 - h)) / (2 * h)
+        a2 = ldiff(yp(p0 + h / 4), yp(p0 - h / 4)) / (h / 2)
+        scale = max(abs(a1), abs(pbar[i]), 1e-300)
+        if abs(a1 - a2) > 1e-6 * scale:
+            skipped += 1
+            continue
+        checked += 1
+        err = abs(pbar[i] - a1) / scale
+        worst = max(worst, err)
+        print(f"  d L / d {pn}: adjoint {pbar[i]:+.10e}  FD {a1:+.10e}  rel {err:.1e}")
+        assert err <= 1e-6, (pn, pbar[i], a1)
+    print(f"\nKIN2KIN gradient vs FD: {checked} components checked, {skipped} next to a switch, "
+          f"worst rel err {worst:.2e}")
     assert checked >= 20
     drv.close()
 
