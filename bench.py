@@ -52,11 +52,11 @@ CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
 # the column kernel, from ncu captures (--set full) of each kernel on one
 # 16900 x 42 region; traffic grows in proportion to cells.
 CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 215.5, "mixed": 172.9}
-COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 374.9, "mixed": 383.3}
+COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 375.1, "mixed": 383.3}
 # FP64-pipe activity (fraction of active cycles) of each kernel in the same
 # captures: the hardware-level utilisation of the bound the kernels sit on.
 FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.842, "mixed": 0.747},
-                    "nsw6_column_kernel": {"fp64": 0.713, "mixed": 0.679}}
+                    "nsw6_column_kernel": {"fp64": 0.708, "mixed": 0.679}}
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (csrc/nsw6_probe.cu) and frozen here.
