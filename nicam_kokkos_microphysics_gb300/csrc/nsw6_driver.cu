@@ -686,9 +686,11 @@ int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
     return NSW6_ERR_CUDA;
   // Chunks of regions: the first chunk's copy in and the last chunk's copy
   // out are not hidden behind compute, so those two are one region each; the
-  // rest go in about four chunks (larger launches fill the GPU's last wave
-  // better).
-  const int mid = lall > 2 ? (lall - 2 + 3) / 4 : 1;
+  // FP64 step (compute above the copies) takes the rest in about four chunks
+  // (larger launches fill the GPU's last wave better), the mixed-precision
+  // step (copies above the compute) one region at a time, so that each
+  // region's copy out starts as soon as it is done.
+  const int mid = (lall > 2 && h->mixed != 1) ? (lall - 2 + 3) / 4 : 1;
   auto chunk_len = [&](int l0) {
     if (lall <= 2 || l0 == 0 || l0 == lall - 1) return 1;
     const int left = lall - 1 - l0;   // regions before the last one
