@@ -14,7 +14,8 @@
 // same fused multiply-adds, correctly rounded quotients and table-driven
 // transcendentals), so a derivative instance follows the same trajectory as
 // the plain step.  Branches (limiters, switches, min/max) follow the values;
-// their derivative is the one of the branch taken.
+// their derivative is the one of the branch taken, except that a rate clamped
+// at zero (rate_on) is off where its argument is exactly zero.
 #pragma once
 
 #include <type_traits>
@@ -72,6 +73,7 @@ __device__ __forceinline__ Dual sqrtR(const Dual& x) {
 __device__ __forceinline__ Dual fabsR(const Dual& x) { return x.v < 0.0 ? -x : x; }
 __device__ __forceinline__ Dual dmin(const Dual& a, const Dual& b) { return (b < a) ? b : a; }
 __device__ __forceinline__ Dual dmax(const Dual& a, const Dual& b) { return (a < b) ? b : a; }
+__device__ __forceinline__ Dual rate_on(const Dual& x) { return x.v > 0.0 ? x : Dual(dmax(x.v, 0.0)); }
 // The quotient helpers of the FP64 kernels give the correctly rounded a / b.
 __device__ __forceinline__ Dual div_rn(const Dual& a, const Dual& b, const Dual&) { return a / b; }
 __device__ __forceinline__ Dual sel(bool on, const Dual& x) { return on ? x : Dual(copysign(0.0, x.v)); }
@@ -175,6 +177,7 @@ __device__ __forceinline__ RVar sqrtR(const RVar& x) {
 __device__ __forceinline__ RVar fabsR(const RVar& x) { return x.v < 0.0 ? -x : x; }
 __device__ __forceinline__ RVar dmin(const RVar& a, const RVar& b) { return (b < a) ? b : a; }
 __device__ __forceinline__ RVar dmax(const RVar& a, const RVar& b) { return (a < b) ? b : a; }
+__device__ __forceinline__ RVar rate_on(const RVar& x) { return x.v > 0.0 ? x : RVar(dmax(x.v, 0.0)); }
 __device__ __forceinline__ RVar div_rn(const RVar& a, const RVar& b, const RVar&) { return a / b; }
 __device__ __forceinline__ RVar sel(bool on, const RVar& x) { return on ? x : RVar(copysign(0.0, x.v)); }
 __device__ __forceinline__ RVar per_dt(const RVar& q, const RVar& dt, const RVar&) { return q / dt; }

@@ -82,6 +82,14 @@ __device__ __forceinline__ double val_of(double x) { return x; }   // the value 
 __device__ __forceinline__ float val_of(float x) { return x; }     // derivative types add theirs)
 __device__ __forceinline__ float dmin(float a, float b) { return (b < a) ? b : a; }
 __device__ __forceinline__ float dmax(float a, float b) { return (a < b) ? b : a; }
+
+// A process rate clamped at zero, max(x, 0) (Kokkos::max as above).  Its
+// derivative types (nsw6_ad.cuh) treat the rate as off where x is exactly
+// zero: the ice->snow autoconversion max(beta (qi - qicrt), 0) sits there in
+// every cell without ice at the reference threshold qicrt = 0, where the ice
+// limiters hold the rate at zero on both sides of the threshold.
+template <class R>
+__device__ __forceinline__ R rate_on(const R& x) { return dmax(x, R(0)); }
 // x * f for a switch value f in {0, 1} (the reference's iceflg, delta1,
 // delta2, spsati): x, or the zero x * 0 gives (a zero with the sign of x),
 // selected without an FP64 multiplication.
@@ -323,7 +331,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     }
     Praut = Rdens * R(1.67E-5) * rhoqc * rhoqc / (R(5.0) + R(3.66E-2) * Nc / (Dc * rhoqc + R(EPS)));
   }
-  R Psaut = dmax(betai * (qi - C.qicrt_saut), Z);
+  R Psaut = rate_on(betai * (qi - C.qicrt_saut));
 
   // evaporation, sublimation, melting and freezing, :1174-1247
   const R Ka = (R(2.428E-2) + R(7.47E-5) * temc);

@@ -1011,10 +1011,10 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const Consts& C, const FastMat
   }
   // Ka = 2.428e-2 + 7.47e-5 temc
   b_temc = fma(b_Ka, 7.47E-5, b_temc);
-  // Psaut = max(betai (qi - qicrt), 0)
+  // Psaut = max(betai (qi - qicrt), 0), off where its argument is exactly 0
+  // (rate_on: a cell without ice at the threshold qicrt = 0)
   {
-    double b_sb = 0.0, dummy = 0.0;
-    bmax(saut_b, Z, bPsaut, b_sb, dummy);
+    const double b_sb = saut_b > Z ? bPsaut : 0.0;
     b_betai = fma(b_sb, saut_a, b_betai);
     const double b_sa = b_sb * betai;
     b_qi += b_sa;

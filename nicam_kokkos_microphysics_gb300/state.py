@@ -292,18 +292,42 @@ def make_region(rng: np.random.Generator, gall: int, kall: int, variant: str,
     return out
 
 
-def make_state(spec: StateSpec, out_fill: float = np.nan) -> dict[str, np.ndarray]:
+def region_rng(seed: int, l: int) -> np.random.Generator:
+    """The random stream of region l: the seed's PCG64 stream for region 0,
+    its l-th jump (2^127 draws ahead, an independent stream) for region l, so
+    that any subset of regions can be generated on its own."""
+    bitgen = np.random.PCG64(seed)
+    return np.random.Generator(bitgen if l == 0 else bitgen.jumped(l))
+
+
+def shard_regions(lall: int, rank: int, world: int) -> range:
+    """The regions of one rank when `lall` regions are split over `world`
+    ranks: contiguous blocks, the first lall % world ranks one region more.
+    Regions are independent (the only cross-column coupling of the step, the
+    departure-distance extrema, is per region), so every rank steps its block
+    alone and no data moves between ranks."""
+    if not 0 <= rank < world:
+        raise ValueError(f"rank {rank} outside 0..{world - 1}")
+    base, extra = divmod(lall, world)
+    start = rank * base + min(rank, extra)
+    return range(start, start + base + (1 if rank < extra else 0))
+
+
+def make_state(spec: StateSpec, out_fill: float = np.nan, regions=None) -> dict[str, np.ndarray]:
     """All-regions mp_driver arguments, arrays in the batched layout.
 
     Output-only arguments are filled with ``out_fill`` so that a test can
-    check that every output element is written.
+    check that every output element is written.  ``regions`` (default: all
+    ``spec.lall``) selects the regions to generate, in that order; region l
+    is the same array whichever subset it is generated in.
     """
     gz, gzh = vertical_grid(spec.kall)
-    rng = np.random.Generator(np.random.PCG64(spec.seed))
-    regions = [make_region(rng, spec.gall, spec.kall, spec.variant, gz, gzh) for _ in range(spec.lall)]
+    ls = range(spec.lall) if regions is None else list(regions)
+    regions = [make_region(region_rng(spec.seed, l), spec.gall, spec.kall, spec.variant, gz, gzh) for l in ls]
+    lall = len(regions)
     st: dict[str, np.ndarray] = {}
     for name, kind, intent in MP_DRIVER_ARGS:
-        shp = batched_shape(kind, spec.lall, spec.kall, spec.gall)
+        shp = batched_shape(kind, lall, spec.kall, spec.gall)
         if intent == "out":
             st[name] = np.full(shp, out_fill)
             continue
@@ -337,3 +361,13 @@ def store_region(st: dict[str, np.ndarray], l: int, reg: dict[str, np.ndarray]) 
             st[name][:, l] = reg[name]
         else:
             st[name][l] = reg[name]
+
+
+def regions_to_batched(regions: list[dict[str, np.ndarray]]) -> dict[str, np.ndarray]:
+    """Stacks per-region argument sets (per-region layout, as region_view
+    gives them) into the all-regions layout of mp_driver_batched."""
+    out = {}
+    for name, kind, _ in MP_DRIVER_ARGS:
+        axis = 1 if kind == "2g" else 0
+        out[name] = np.ascontiguousarray(np.stack([r[name] for r in regions], axis=axis), dtype=np.float64)
+    return out

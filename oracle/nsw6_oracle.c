@@ -22,6 +22,24 @@
 #define NSW6O_PHASE(n)
 #endif
 
+/* Decision-site markers for the decision-recording build
+ * (oracle/branchsig.cpp), which tags every discrete decision of the step with
+ * the part of the algorithm that takes it; empty otherwise. */
+#ifndef NSW6O_SITE
+#define NSW6O_SITE(n)
+#endif
+enum {
+  SITE_OTHER,      /* thermodynamics, updates, metric factors */
+  SITE_RATES,      /* process rates, slope parameters, fall speeds (TagBigLoop) */
+  SITE_LIMITER,    /* the rate limiters and per-species loss limiters, :1249-1559 */
+  SITE_NEGFILTER,  /* negative_filter */
+  SITE_DEPARTURE,  /* vadv1d_prep: region-wide extrema, flux bounds, departure cells */
+  SITE_FLUXSUM,    /* vadv1d_getflux_new: the flux integral's weights */
+  SITE_EPSFILTER,  /* vadv1d_getflux_new: the |flux| < EPS filter */
+  SITE_NEWTON,     /* SATURATION_adjustment: saturation test and Newton iteration */
+  SITE_DIAG        /* effective radii and cloud top */
+};
+
 #ifdef _OPENMP
 #include <omp.h>
 #define OMP_FOR _Pragma("omp parallel for schedule(static)")
@@ -288,6 +306,7 @@ static void negative_filter(const dims_t* D, double* rhog, double* rhoge, double
                             const double* tem, double* pre, double* q, const double* gsgam2,
                             double* qd_w, double* cv_w) {
   const size_t lo = IX(D->kmin, 0), hi = IX(D->kmax + 1, 0), N = D->N;
+  NSW6O_SITE(SITE_NEGFILTER);
   OMP_FOR
   for (size_t i = lo; i < hi; ++i) {
     double diffq = 0.0;
@@ -317,6 +336,7 @@ static void negative_filter(const dims_t* D, double* rhog, double* rhoge, double
     rhoge[i] = tem[i] * rhog[i] * cv_w[i];
     pre[i] = rho[i] * (qd_w[i] * CONST_Rdry + q[I_QV * N + i] * CONST_Rvap) * tem[i];
   }
+  NSW6O_SITE(SITE_OTHER);
 }
 
 /* SATURATION_psat_liq / _ice, mod_satadjust.cpp:80-106, 133-160 (all k). */
@@ -332,6 +352,7 @@ static void psat_fn(const dims_t* D, const consts_t* c, const double* tem, doubl
 /* Bergeron_param, mod_mp_nsw6.cpp:1834-1890 (interior levels).  The
  * interpolation weight is fact = -(temc + itemc - 1), as in the reference. */
 static void bergeron(const dims_t* D, const double* tem, double* a1, double* a2, double* ma2) {
+  NSW6O_SITE(SITE_RATES);
   static const double a1_tab[32] = {
       0.0001E-7, 0.7939E-7, 0.7841E-6, 0.3369E-5, 0.4336E-5, 0.5285E-5, 0.3728E-5, 0.1852E-5,
       0.2991E-6, 0.4248E-6, 0.7434E-6, 0.1812E-5, 0.4394E-5, 0.9145E-5, 0.1725E-4, 0.3348E-4,
@@ -387,6 +408,7 @@ static void big_loop_cell(const consts_t* c, double dens, double temp, const dou
   const double sw_roh2014 = c->sw_roh2014, ln10 = c->ln10, sw_expice = c->sw_expice;
   const double sw_kk2000 = c->sw_kk2000;
 
+  NSW6O_SITE(SITE_RATES);
   double qv = dmax(qin[0], 0.0), qc = dmax(qin[1], 0.0), qr = dmax(qin[2], 0.0);
   double qi = dmax(qin[3], 0.0), qs = dmax(qin[4], 0.0), qg = dmax(qin[5], 0.0);
 
@@ -605,6 +627,7 @@ static void big_loop_cell(const consts_t* c, double dens, double temp, const dou
   wk[I_Psfi] = qi / dt1;
 
   /* limiters, :1249-1296 */
+  NSW6O_SITE(SITE_LIMITER);
   wk[I_Pigen] = dmin(wk[I_Pigen], wk[I_dqv_dt]) * (wk[I_iceflg]) * sw_expice;
   wk[I_Pidep] = dmin(wk[I_Pidep], wk[I_dqv_dt]) * (wk[I_iceflg]) * sw_expice;
   wk[I_Psdep] = dmin(wk[I_Psdep], wk[I_dqv_dt]) * (wk[I_iceflg]);
@@ -774,6 +797,7 @@ static void big_loop_cell(const consts_t* c, double dens, double temp, const dou
   o->Vt[3] = Vtg;
 
   /* effective radius and cloud top, :1566-1592 */
+  NSW6O_SITE(SITE_DIAG);
   double xf_qc = rhoqc / Nc * 1.0E-9;
   double rf_qc = pow((c->coef_xf * xf_qc + EPS), 0.33333333);
   double r2_qc = c->coef_dgam * (rf_qc * rf_qc) * (Nc * 1.0E+6);
@@ -829,6 +853,7 @@ static void vadv1d_prep(const dims_t* D, int mkmin, int mkmax, const double* dz,
                         double* wh) {
   const int G = D->G, K = D->K;
   NSW6O_PHASE(3);
+  NSW6O_SITE(SITE_DEPARTURE);
   const double dt2 = pow(dt, 2);
   const double dt3 = pow(dt, 3);
   memset(wh, 0, sizeof(double) * D->N);
@@ -910,6 +935,7 @@ static void vadv1d_prep(const dims_t* D, int mkmin, int mkmax, const double* dz,
     if (kcell[i] == 0) kcell[i] = mkmin;
     if (kcell[i] == mkmax + 1) kcell[i] = mkmax;
   }
+  NSW6O_SITE(SITE_OTHER);
 }
 
 /* vadv1d_getflux_new, mod_vadv1d.cpp:393-450.
@@ -924,6 +950,7 @@ static void vadv1d_getflux(const dims_t* D, int mkmin, int mkmax, const double* 
                            const double* zdis0, const int* kcell, const int* kcell_max, const int* kcell_min,
                            double* frhof) {
   const int G = D->G;
+  NSW6O_SITE(SITE_FLUXSUM);
   memset(frhof, 0, sizeof(double) * D->N);
   for (int k = mkmin; k <= mkmax; ++k) {
     OMP_FOR
@@ -951,8 +978,10 @@ static void vadv1d_getflux(const dims_t* D, int mkmin, int mkmax, const double* 
       frhof[i] = f;
     }
   }
+  NSW6O_SITE(SITE_EPSFILTER);
   OMP_FOR
   for (size_t i = 0; i < D->N; ++i) frhof[i] = frhof[i] * (0.5 + copysign(0.5, fabs(frhof[i]) - CONST_EPS));
+  NSW6O_SITE(SITE_OTHER);
 }
 
 /* ------------------------------------------------------------------ driver */
@@ -1045,6 +1074,7 @@ int nsw6o_mp_driver(int gall, int kall, const double* gz_in, const double* gzh_i
       tctop_cld[g] = o.tctop_cld;
     }
   }
+  NSW6O_SITE(SITE_OTHER);
   OMP_FOR
   for (size_t i = IX(kmin, 0); i < IX(kmax + 1, 0); ++i) {  /* TagUpdateRHOGQ, :692-700 */
     for (int nq = 0; nq < 6; ++nq) rhogq[nq * N + i] += drhogq[nq * N + i];
@@ -1082,6 +1112,7 @@ int nsw6o_mp_driver(int gall, int kall, const double* gz_in, const double* gzh_i
 
   /* ---- precip_transport_new, mod_precip_transport.cpp:573-1087 */
   NSW6O_PHASE(2);
+  NSW6O_SITE(SITE_OTHER);
   {
     double *rhogkin = zalloc(N), *rhogkin_h = zalloc(N), *rhogkin_v = zalloc(N);
     double *rhoq = zalloc(N), *rhoeq = zalloc(N), *rhophiq = zalloc(N), *rhokin_h = zalloc(N);
@@ -1288,6 +1319,7 @@ int nsw6o_mp_driver(int gall, int kall, const double* gz_in, const double* gzh_i
 
   /* ---- SATURATION_adjustment (ice_adjust = false), mod_satadjust.cpp:274-362 */
   int rc = 0;
+  NSW6O_SITE(SITE_NEWTON);
   {
     double *ein_moist = zalloc(N), *qsum = zalloc(N), *CVtot = zalloc(N), *rho_l = zalloc(N), *qd_l = zalloc(N);
     for (size_t i = 0; i < N; ++i) {

@@ -90,6 +90,98 @@ def count_ops(reg: dict[str, np.ndarray], gz: np.ndarray, gzh: np.ndarray, dt: f
     return res
 
 
+def build_branchsig(force: bool = False) -> Path:
+    """Decision-recording build (oracle/branchsig.cpp)."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    so = BUILD / "libnsw6_branchsig.so"
+    src = [HERE / "branchsig.cpp", HERE / "nsw6_oracle.c", HERE / "nsw6_oracle.h"]
+    if so.exists() and not force and all(so.stat().st_mtime >= s.stat().st_mtime for s in src):
+        return so
+    subprocess.run(["g++", "-std=c++17", "-O1", "-ffp-contract=off", "-fPIC", "-shared", "-w", f"-I{HERE}",
+                    str(HERE / "branchsig.cpp"), "-o", str(so)], check=True)
+    return so
+
+
+# Sites of the decision record (the enum in nsw6_oracle.c).
+SITES = ["other", "rates", "limiter", "negfilter", "departure", "fluxsum", "epsfilter", "newton", "diag"]
+
+
+def branch_record(reg: dict[str, np.ndarray], gz: np.ndarray, gzh: np.ndarray, dt: float,
+                  params: dict[str, float] | None = None, inplace: bool = False) -> dict[str, np.ndarray]:
+    """The discrete decisions of one step of the reference algorithm on one
+    region, in program order (the region's arrays are stepped in place with
+    ``inplace``, else left unchanged):
+
+      code  uint8   site << 2 | kind << 1 | outcome (kind 1: an integer conversion)
+      val   float64 the compared difference a - b, the sign argument, or the integer
+      mag   float64 the larger magnitude of the compared operands
+
+    Two steps whose records have equal codes (and equal integers) take the
+    same branch everywhere."""
+    lib = _LIBS.get("branchsig")
+    if lib is None:
+        lib = ctypes.CDLL(str(build_branchsig()), mode=os.RTLD_LOCAL)
+        dp = ctypes.POINTER(ctypes.c_double)
+        lib.nsw6o_branch_record.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp, dp, ctypes.POINTER(ctypes.c_void_p),
+                                            ctypes.c_double, ctypes.POINTER(ctypes.c_longlong)]
+        lib.nsw6o_branch_copy.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]
+        _LIBS["branchsig"] = lib
+    dp = ctypes.POINTER(ctypes.c_double)
+    if inplace:
+        work = reg
+        for n, _, _ in MP_DRIVER_ARGS:
+            if work[n].dtype != np.float64 or not work[n].flags.c_contiguous:
+                raise ValueError(f"argument {n}: must be contiguous float64 to be stepped in place")
+    else:
+        work = {n: np.array(reg[n], dtype=np.float64, order="C", copy=True) for n, _, _ in MP_DRIVER_ARGS}
+    kall, gall = work["rhog"].shape
+    par = default_params()
+    par.update(params or {})
+    p = np.array([par[n] for n in PARAM_NAMES])
+    ptrs = (ctypes.c_void_p * len(MP_DRIVER_ARGS))()
+    for i, (name, _, _) in enumerate(MP_DRIVER_ARGS):
+        ptrs[i] = work[name].ctypes.data
+    gz = np.ascontiguousarray(gz, dtype=np.float64)
+    gzh = np.ascontiguousarray(gzh, dtype=np.float64)
+    n = ctypes.c_longlong(0)
+    rc = lib.nsw6o_branch_record(gall, kall, gz.ctypes.data_as(dp), gzh.ctypes.data_as(dp), p.ctypes.data_as(dp),
+                                 ptrs, float(dt), ctypes.byref(n))
+    if rc != 0:
+        raise RuntimeError(f"decision-recording step failed with status {rc}")
+    out = {"code": np.empty(n.value, dtype=np.uint8), "val": np.empty(n.value), "mag": np.empty(n.value)}
+    lib.nsw6o_branch_copy(out["code"].ctypes.data, out["val"].ctypes.data, out["mag"].ctypes.data, n.value)
+    return out
+
+
+def decision_changes(r0: dict[str, np.ndarray], r1: dict[str, np.ndarray], tie_rel: float = 0.0,
+                     tie_abs: float = 0.0) -> dict | None:
+    """Compares two decision records of the same region.  None when the
+    control flow differs (a different number of decisions: a Newton iteration
+    or a search loop ran a different number of times); else, per site, the
+    number of decisions taken differently, the largest |val| and |val| / mag
+    of those decisions in the first record (how far from its switch each one
+    was), how many of them were not ties there (|val| > tie_abs and
+    |val| > tie_rel * mag), and how many sat exactly on their switch there
+    (val == 0: a kink at the point itself)."""
+    if len(r0["code"]) != len(r1["code"]):
+        return None
+    c0, c1 = r0["code"], r1["code"]
+    integer = (c0 & 2) != 0
+    changed = (c0 != c1) | (integer & (r0["val"] != r1["val"]))
+    site = c0 >> 2
+    res = {}
+    for s, name in enumerate(SITES):
+        m = changed & (site == s)
+        v = np.abs(r0["val"][m])
+        mag = r0["mag"][m]
+        rel = v / np.maximum(mag, 1e-300)
+        res[name] = {"changed": int(m.sum()), "max_abs": float(v.max()) if v.size else 0.0,
+                     "max_rel": float(rel.max()) if rel.size else 0.0,
+                     "untied": int(((v > tie_abs) & (v > tie_rel * mag)).sum()),
+                     "exact": int((v == 0.0).sum())}
+    return res
+
+
 _LIBS: dict[str, ctypes.CDLL] = {}
 
 

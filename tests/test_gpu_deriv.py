@@ -339,6 +339,94 @@ def test_gradient_against_finite_differences(options, variant):
     drv.close()
 
 
+def _region_fd_check(torch, reg, gz, gzh, names, dt=60.0):
+    """Adjoint parameter gradients of L on one region against central
+    differences of the production step (relative step 1e-6, and 1e-6 / 4 to
+    show the difference resolves the derivative), and against central
+    differences of the reference algorithm (the oracle) with the same step.
+    Every finite-difference point is certified by the reference's decision
+    record (no switch between p - h and p + h)."""
+    import _fdregions as F
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    from nicam_kokkos_microphysics_gb300.state import regions_to_batched
+    kall, gall = reg["rhog"].shape
+    drv = mp_init("NSW6", gall, kall, gz, gzh, lall_max=1)
+    x0 = {n: torch.from_numpy(v).cuda() for n, v in regions_to_batched([reg]).items()}
+    w = torch.from_numpy(F.loss_weights(gzh)).cuda()
+
+    def forward():
+        y = _clone(x0)
+        drv.mp_driver_batched(1, *[y[n] for n in ARG_NAMES], dt=dt, ct=0.0)
+        return y
+
+    y0 = forward()
+    bar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    bar["precip"] = 2.0 * (y0["precip"][0] + y0["precip"][1]).unsqueeze(0).expand_as(y0["precip"]).contiguous()
+    bar["rhogq"][:, 1] = w[None, :, None].expand(1, kall, gall)
+    pbar = drv.adjoint(1, _clone(x0), bar, dt=dt)
+    wn = F.loss_weights(gzh)
+
+    def oracle_diff(a, b):
+        pa, pb = a["precip"][0] + a["precip"][1], b["precip"][0] + b["precip"][1]
+        return float(((pa - pb) * (pa + pb)).sum() + ((a["rhogq"][1] - b["rhogq"][1]) * wn[:, None]).sum())
+
+    base = drv.get_params()
+    rows = []
+    for pn in names:
+        i = PARAMS.index(pn)
+        p0 = base[pn]
+        h = 1e-6 * abs(p0) if p0 != 0.0 else 1e-9   # the threshold at 0: an absolute 1e-9 kg/kg
+        cert = F.certify(reg, gz, gzh, pn, p0, (h, -h, h / 4, -h / 4), dt)
+        assert cert["ok"], (pn, cert["per_step"])
+
+        def at(v, pn=pn, p0=p0):
+            drv.set_params(**{pn: v})
+            out = forward()
+            drv.set_params(**{pn: p0})
+            return out
+
+        a1 = _loss_diff(torch, at(p0 + h), at(p0 - h), w) / (2 * h)
+        a2 = _loss_diff(torch, at(p0 + h / 4), at(p0 - h / 4), w) / (h / 2)
+        o1 = oracle_diff(F._step(reg, gz, gzh, dt, {pn: p0 + h}), F._step(reg, gz, gzh, dt, {pn: p0 - h})) / (2 * h)
+        scale = max(abs(a1), abs(pbar[i]), 1e-300)
+        err, err_ref, res = abs(pbar[i] - a1) / scale, abs(pbar[i] - o1) / scale, abs(a1 - a2) / scale
+        changed = sum(v.get("changed", 0) for st in cert["per_step"] for k, v in st.items() if isinstance(v, dict))
+        rows.append((pn, pbar[i], a1, o1, err, err_ref, res, changed))
+        print(f"  d L / d {pn:10s}: adjoint {pbar[i]:+.10e}  FD {a1:+.10e}  FD(reference) {o1:+.10e}  "
+              f"rel {err:.1e} / {err_ref:.1e}  (h vs h/4 {res:.1e}; {changed} tie decisions changed)")
+        assert res <= 1e-7, (pn, a1, a2)
+        assert err <= 1e-6, (pn, pbar[i], a1)
+        assert err_ref <= 1e-6, (pn, pbar[i], o1)
+    drv.close()
+    return rows
+
+
+def test_parameter_gradients_against_finite_differences():
+    """All seven NSW6 parameters, with the reference configuration's scheme
+    switches and parameter values: the adjoint gradient of L = sum (precip)^2
+    + sum rhogq[QC] dz against central differences (relative step 1e-6, the
+    threshold qicrt_saut = 0 with an absolute 1e-9) of the production step and
+    of the reference algorithm.  Six parameters act on L through the surface
+    precipitation and are checked on columns that the step leaves without
+    cloud water (the autoconversion rate on the few whose surface rain it
+    feeds most); the ice-nucleation coefficient acts through the cloud water
+    and is checked on cloudy columns (where the cloud water's cancellation
+    noise hides the others' smaller effects).  The
+    finite-difference points are certified switch-free by the reference's
+    decision record (tests/_fdregions.py)."""
+    torch = _torch()
+    import _fdregions as F
+    reg, gz, gzh = F.precipitating_region()
+    rows = _region_fd_check(torch, reg, gz, gzh, ["beta_saut", "qicrt_saut", "Cr", "Cs", "Cg"])
+    reg, gz, gzh = F.autoconversion_region()
+    rows += _region_fd_check(torch, reg, gz, gzh, ["kk_aut"])
+    reg, gz, gzh = F.cloudy_region(ncol=1024)
+    rows += _region_fd_check(torch, reg, gz, gzh, ["ice_nuc"])
+    assert sorted(r[0] for r in rows) == sorted(PARAMS)
+    print(f"\nparameter gradients vs FD: {len(rows)} of 7 checked, worst rel err "
+          f"{max(r[4] for r in rows):.2e} (production step), {max(r[5] for r in rows):.2e} (reference)")
+
+
 def test_kin2kin_gradient_against_finite_differences():
     """With KIN2KIN the final momenta are the transported ones rescaled to
     carry the transported kinetic energy.  The adjoint gradient of a random
@@ -426,36 +514,47 @@ def test_kin2kin_gradient_against_finite_differences():
 
 
 def test_window_gradient_against_finite_differences():
-    """Three-step window with checkpoints: gradient of the accumulated surface
-    precipitation with respect to the initial temperature and vapour and the
-    parameters, against term-wise central differences of the FP64 window."""
-    torch, drv, spec, st, x0 = _setup(512, 42, 1, 99, "convective")
+    """Three-step window with per-step checkpoints (FP64 forward): the gradient
+    of the accumulated surface precipitation J with respect to the initial
+    temperature and vapour and to all seven parameters, against term-wise
+    central differences of the FP64 window (relative step 1e-6; the threshold
+    qicrt_saut = 0 with an absolute 1e-9), on the precipitating region of
+    tests/_fdregions.py.  Every parameter point is certified switch-free over
+    the whole window by the reference's decision records."""
+    torch = _torch()
+    import _fdregions as F
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    from nicam_kokkos_microphysics_gb300.state import regions_to_batched
     from nicam_kokkos_microphysics_gb300.window import window_gradient
-    nsteps = 3
-    res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision="fp64")
+    reg, gz, gzh = F.precipitating_region()
+    kall, gall = reg["rhog"].shape
+    dt, nsteps = 60.0, 3
+    drv = mp_init("NSW6", gall, kall, gz, gzh, lall_max=1)
+    x0 = {n: torch.from_numpy(v).cuda() for n, v in regions_to_batched([reg]).items()}
+    res = window_gradient(drv, 1, x0, nsteps, dt, precision="fp64")
     bar, pbar = res["grad"], res["dparams"]
 
     def precip_series(x):
         y = _clone(x)
         out = []
         for _ in range(nsteps):
-            drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+            drv.mp_driver_batched(1, *[y[n] for n in ARG_NAMES], dt=dt, ct=0.0)
             out.append((y["precip"][0] + y["precip"][1]).clone())
         return out
 
-    def dJ(xp, xm):
-        sp, sm = precip_series(xp), precip_series(xm)
-        return float(sum((a - b).sum() for a, b in zip(sp, sm))) * spec.dt
+    def dJ(sp, sm):
+        return float(sum((a - b).sum() for a, b in zip(sp, sm))) * dt
 
     y1 = _clone(x0)
-    drv.mp_driver_batched(spec.lall, *[y1[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    drv.mp_driver_batched(1, *[y1[n] for n in ARG_NAMES], dt=dt, ct=0.0)
     prc = (y1["precip"][0, 0] + y1["precip"][1, 0]).abs().cpu().numpy()
     rng = np.random.default_rng(8)
     checked = skipped = 0
-    for g in rng.choice(np.argsort(prc)[-64:], 8, replace=False):
+    worst = 0.0
+    for g in rng.choice(np.argsort(prc)[-48:], 8, replace=False):
         for name, nq in (("tem", None), ("q", 0)):
             gcol = bar[name][0, :, g] if nq is None else bar[name][0, nq, :, g]
-            k = int(gcol[1:spec.kall - 1].abs().argmax()) + 1   # the most sensitive level
+            k = int(gcol[1:kall - 1].abs().argmax()) + 1   # the most sensitive level
             ix = (0, k, int(g)) if nq is None else (0, nq, k, int(g))
             h = 1e-6 * abs(float(x0[name][ix]))
             vals = []
@@ -463,17 +562,82 @@ def test_window_gradient_against_finite_differences():
                 xp, xm = _clone(x0), _clone(x0)
                 xp[name][ix] += hh
                 xm[name][ix] -= hh
-                vals.append(dJ(xp, xm) / (2 * hh))
+                vals.append(dJ(precip_series(xp), precip_series(xm)) / (2 * hh))
             adj = float(bar[name][ix])
             scale = max(abs(vals[0]), abs(adj), 1e-300)
-            if abs(vals[0] - vals[1]) > 1e-6 * scale or scale < 1e-25:
+            # a derivative 1e-10 below the field's largest is rounding noise
+            # of the adjoint, not a sensitivity a 1e-6 step resolves
+            if abs(vals[0] - vals[1]) > 1e-6 * scale or scale < 1e-10 * float(bar[name].abs().max()):
                 skipped += 1
                 continue
             checked += 1
             err = abs(adj - vals[0]) / scale
+            worst = max(worst, err)
             print(f"  window dJ/d{name}{ix}: adjoint {adj:+.10e} FD {vals[0]:+.10e} rel {err:.1e}")
             assert err <= 1e-6, (name, ix, adj, vals[0])
-    print(f"\nwindow gradient: {checked} checked, {skipped} next to a switch; J = {res['J']:.6e}; "
-          f"forward {res['t_forward'] * 1e3:.1f} ms, adjoint {res['t_adjoint'] * 1e3:.1f} ms")
-    assert checked >= 6
+    base = drv.get_params()
+    for i, pn in enumerate(PARAMS):
+        p0 = base[pn]
+        h = 1e-6 * abs(p0) if p0 != 0.0 else 1e-9
+        cert = F.certify_window(reg, gz, gzh, pn, p0, (h, -h, h / 4, -h / 4), nsteps, dt)
+        assert cert["ok"], (pn, cert["per_step"])
+
+        def series(v, pn=pn, p0=p0):
+            drv.set_params(**{pn: v})
+            out = precip_series(x0)
+            drv.set_params(**{pn: p0})
+            return out
+
+        a1 = dJ(series(p0 + h), series(p0 - h)) / (2 * h)
+        a2 = dJ(series(p0 + h / 4), series(p0 - h / 4)) / (h / 2)
+        scale = max(abs(a1), abs(pbar[i]), 1e-300)
+        err, resol = abs(pbar[i] - a1) / scale, abs(a1 - a2) / scale
+        worst = max(worst, err)
+        print(f"  window dJ/d{pn:10s}: adjoint {pbar[i]:+.10e} FD {a1:+.10e} rel {err:.1e} (h vs h/4 {resol:.1e})")
+        assert resol <= 1e-7, (pn, a1, a2)
+        assert err <= 1e-6, (pn, pbar[i], a1)
+        checked += 1
+    print(f"\nwindow gradient: {checked} checked (7 parameters), {skipped} state points skipped, "
+          f"worst rel err {worst:.2e}; J = {res['J']:.6e}; forward {res['t_forward'] * 1e3:.1f} ms, "
+          f"adjoint {res['t_adjoint'] * 1e3:.1f} ms")
+    assert checked >= 6 + len(PARAMS)
+    drv.close()
+
+
+def test_window_gradient_mixed_forward_against_fp64_forward():
+    """The configured 12-step window runs the mixed-precision forward with FP64
+    adjoint accumulation.  Its gradient (the adjoint around the mixed
+    forward's checkpoints) against the same window with the FP64 forward, on
+    a 16900-column region, reported per parameter and for the gradient fields
+    of the initial temperature and vapour.  The two are gradients of two
+    trajectories that part by the mixed step's errors (about 1e-6): where a
+    cell of one trajectory sits on the other side of a limiter or threshold
+    switch than in the other, its derivative differs outright, so the
+    parameters that act through such switches (the ice autoconversion rate
+    and threshold) differ by a few per cent, the others by 1e-6 to 1e-4, the
+    fields by a few 1e-3 (relative L2)."""
+    torch, drv, spec, st, x0 = _setup(16900, 42, 1, 1005, "standard")
+    from nicam_kokkos_microphysics_gb300.window import window_gradient
+    r64 = window_gradient(drv, 1, x0, 12, spec.dt, precision="fp64")
+    rmx = window_gradient(drv, 1, x0, 12, spec.dt, precision="mixed")
+    print(f"\n12-step window, J fp64 {r64['J']:.10e} mixed {rmx['J']:.10e} "
+          f"(rel {abs(rmx['J'] - r64['J']) / abs(r64['J']):.2e})")
+    worst = {}
+    for i, pn in enumerate(PARAMS):
+        a, b = rmx["dparams"][i], r64["dparams"][i]
+        rel = abs(a - b) / max(abs(b), 1e-300)
+        worst[pn] = rel
+        print(f"  dJ/d{pn:10s}: fp64 forward {b:+.10e}  mixed forward {a:+.10e}  rel {rel:.2e}")
+    for name, sl in (("tem", (slice(None),)), ("q[QV]", (slice(None), 0))):
+        f = "tem" if name == "tem" else "q"
+        a, b = rmx["grad"][f][sl], r64["grad"][f][sl]
+        l2 = float((a - b).norm() / b.norm())
+        mx = float((a - b).abs().max() / b.abs().max())
+        worst[name] = l2
+        print(f"  dJ/d{name} field: relative L2 difference {l2:.2e}, field-normalised max {mx:.2e}")
+    for pn in ("Cr", "Cs", "Cg", "ice_nuc", "kk_aut"):
+        assert worst[pn] <= 1e-3, (pn, worst[pn])
+    for pn in ("beta_saut", "qicrt_saut"):
+        assert worst[pn] <= 0.1, (pn, worst[pn])
+    assert worst["tem"] <= 1e-2 and worst["q[QV]"] <= 1e-2, worst
     drv.close()
