@@ -15,7 +15,7 @@ from conftest import golden_files
 from nicam_kokkos_microphysics_gb300.state import (ARG_NAMES, MP_DRIVER_ARGS, OUTPUT_NAMES, StateSpec, make_state,
                                                    region_shape, region_view)
 from oracle import restatement
-from _parity import compare, passes, summary
+from _parity import compare, passes, reference_spread, summary, threshold_cells
 
 pytestmark = pytest.mark.gpu
 
@@ -49,11 +49,30 @@ def run_oracle(reg: dict, gz, gzh, dt: float, params: dict | None = None) -> dic
     return want
 
 
-def assert_parity(got: dict, want: dict, label: str):
+SPREAD = reference_spread()
+# The reference's own fma build against its strict build is one sample of its
+# build-to-build spread; on the small deep-column states (a few thousand
+# values, kall 96 and 160) where it has 0 or 12 threshold cells a different
+# but equally valid rounding of the same cancellation residues gives a few
+# more.  The bound is that count plus the fixed allowance of 8 values that the
+# parity criterion gives every state (tests/_parity.py).
+SPREAD_SLACK = 8
+
+
+def assert_parity(got: dict, want: dict, label: str, spread_key: str | None = None):
+    """The parity criterion, the reference's statistic within its bound, and,
+    where the state has a recorded reference spread, no more threshold cells
+    than the reference's own fma build has against its strict build (plus the
+    fixed allowance of 8)."""
     stats = compare(got, want, OUTPUT_NAMES)
-    print(f"\n[{label}]\n" + summary(stats))
-    bad = sorted(n for n, s in stats.items() if s["n_bad"])
+    thr = threshold_cells(stats)
+    ref_thr = SPREAD[spread_key]["threshold_cells"] if spread_key else None
+    print(f"\n[{label}] threshold cells: gpu {thr}, reference fma build {ref_thr}\n" + summary(stats))
+    bad = sorted(n for n, s in stats.items() if s["n_bad"] or not s["statistic_ok"])
     assert passes(stats), f"{label}: fields outside tolerance: {bad}\n" + summary(stats)
+    if spread_key is not None:
+        assert thr <= ref_thr + SPREAD_SLACK, \
+            f"{label}: {thr} threshold cells, the reference's fma build has {ref_thr}"
 
 
 def load_golden(path):
@@ -71,7 +90,7 @@ def load_golden(path):
 def test_gpu_matches_reference_golden(path):
     reg, out, gz, gzh, dt = load_golden(path)
     got = run_gpu(reg, gz, gzh, dt)
-    assert_parity(got, out, path.stem)
+    assert_parity(got, out, path.stem, path.stem)
     for n in OUTPUT_NAMES:
         assert np.isfinite(got[n]).all(), f"{n} not fully written"
 
@@ -84,7 +103,7 @@ def test_gpu_matches_oracle_full_region(variant, seed):
     reg = region_view(st, 0)
     want = run_oracle(reg, st["_gz"], st["_gzh"], spec.dt)
     got = run_gpu(reg, st["_gz"], st["_gzh"], spec.dt)
-    assert_parity(got, want, f"{variant} 16900x42")
+    assert_parity(got, want, f"{variant} 16900x42", f"full_{variant}_{seed}")
 
 
 @pytest.mark.parametrize("gall,kall", [(1, 42), (17, 42), (33, 12), (31, 5), (250, 7), (64, 96), (24, 160)])
@@ -94,7 +113,7 @@ def test_gpu_ragged_and_small_shapes(gall, kall):
     reg = region_view(st, 0)
     want = run_oracle(reg, st["_gz"], st["_gzh"], spec.dt)
     got = run_gpu(reg, st["_gz"], st["_gzh"], spec.dt)
-    assert_parity(got, want, f"{gall}x{kall}")
+    assert_parity(got, want, f"{gall}x{kall}", f"ragged_{gall}x{kall}")
 
 
 def test_gpu_changed_parameters():
@@ -176,7 +195,7 @@ def test_gpu_matches_oracle_on_stepped_states(variant, seed):
     for step in (2, 3):
         got = run_gpu(state, st["_gz"], st["_gzh"], spec.dt)
         want = run_oracle(state, st["_gz"], st["_gzh"], spec.dt)
-        assert_parity(got, want, f"{variant} step {step}")
+        assert_parity(got, want, f"{variant} step {step}", f"stepped_{variant}_{seed}_step{step}")
         state = want
 
 
@@ -233,7 +252,7 @@ def test_gpu_libm_mode_matches_oracle():
     torch.cuda.synchronize()
     got = {k: v.cpu().numpy() for k, v in t.items()}
     drv.close()
-    assert_parity(got, want, "libm mode, convective 16900x42")
+    assert_parity(got, want, "libm mode, convective 16900x42", "full_convective_1002")
 
 
 @pytest.mark.parametrize("precision,options", [("fp64", None), ("mixed", ALL_SWITCHES)], ids=["fp64", "mixed-switches"])
