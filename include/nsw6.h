@@ -155,11 +155,23 @@ int nsw6_last_error(nsw6_handle* h, int* k, int* g, int* l, int* iters);
 
 const char* nsw6_strerror(int status);
 
+/* Row stride, in doubles, of precip, ISO1_precip and ISO2_precip in the
+ * per-region calls mp_driver and mp_driver_mixed: row 1 (snow and graupel)
+ * starts `ld` doubles after row 0 (rain).  The reference harness passes
+ * subview(precip_mp, ALL, l, 0, ALL) of its [2][lall][1][gall] array
+ * (src/main.cpp:37, 220-222), whose rows are lall * gall apart: with
+ * ld = lall * gall the per-region call takes that subview's data pointer as it
+ * is.  0 (the default) means gall, a contiguous [2][gall] array; 0 < ld < gall
+ * is rejected.  The batched, host-memory, multi-step and derivative entry
+ * points keep the all-regions layout [2][lall][gall]. */
+int nsw6_set_precip_stride(nsw6_handle* h, long long ld);
+
 /* One NSW6 step on one region: replaces MP_DRIVER::mp_driver
  * (src/mod_mp_driver.cpp:335-388), same arguments in the same order.
  * 2-D fields are [kall][gall], tracer fields [6][kall][gall] (QV QC QR QI QS
- * QG), precip/ISO1_precip/ISO2_precip [2][gall], precip_rhoe..precip_rhokin
- * and ix..jz [gall], rctop/rwtop/tctop [1][gall].  w, unccn, frhoge_af,
+ * QG), precip/ISO1_precip/ISO2_precip [2][gall] (row 1 gall doubles after row
+ * 0, or as set by nsw6_set_precip_stride), precip_rhoe..precip_rhokin and
+ * ix..jz [gall], rctop/rwtop/tctop [1][gall].  w, unccn, frhoge_af,
  * frhogqv_af, frhoge_rad, rhogqke, zh, ct and CBMFX are accepted and unused,
  * as in the reference. */
 int mp_driver(nsw6_handle* h, int l_region,
@@ -325,9 +337,12 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
  * `stream`, then synchronises it and returns the step's status
  * (NSW6_ERR_NOCONV / NSW6_ERR_NAN as mp_driver).
  *
- * Set-up: the first call on each device looks up the scratch array's device
- * address (cudaGetSymbolAddress, which may load the library's device code);
- * make that first call before any stream capture begins.
+ * Set-up: every call looks up the scratch array's device address on the
+ * current device (cudaGetSymbolAddress; the first call on a device may load
+ * the library's device code there).  The call ends by reading the step's
+ * status back and synchronising `stream`, so it cannot run on a stream that
+ * is being captured into a CUDA graph: it then returns NSW6_ERR_UNSUPPORTED
+ * before issuing anything.
  *
  * Zero state: nothing has to be zero before a call.  Each call writes the grid
  * metrics and fast-math tables into the scratch, resets the status word to 0

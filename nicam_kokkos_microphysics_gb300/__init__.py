@@ -141,6 +141,12 @@ class MPDriver:
         o = _Options(**cur)
         _check(self._lib.nsw6_set_options(self._h, ctypes.byref(o)), self._lib)
 
+    def set_precip_stride(self, ld: int) -> None:
+        """Row stride of precip / ISO1_precip / ISO2_precip in ``mp_driver``
+        (per-region) calls: ``lall * gall`` takes the reference harness's
+        subview of its [2][lall][1][gall] array; 0 restores [2][gall]."""
+        _check(self._lib.nsw6_set_precip_stride(self._h, ctypes.c_longlong(int(ld))), self._lib)
+
     def set_itelim(self, itelim: int) -> None:
         _check(self._lib.nsw6_set_itelim(self._h, int(itelim)), self._lib)
 

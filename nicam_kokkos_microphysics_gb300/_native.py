@@ -69,22 +69,6 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
-PROBE_LIB = LIBDIR / "libnsw6_probe.so"
-
-
-def build_probe(force: bool = False) -> Path:
-    """Throughput probes (FP64 pipe peak and CUDA FP64 function rates) used by bench.py."""
-    src = CSRC / "nsw6_probe.cu"
-    if not force and PROBE_LIB.exists() and PROBE_LIB.stat().st_mtime >= src.stat().st_mtime:
-        return PROBE_LIB
-    LIBDIR.mkdir(parents=True, exist_ok=True)
-    tmp = PROBE_LIB.with_suffix(".so.tmp")
-    subprocess.run([nvcc(), *ARCH, "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-shared", str(src), "-o", str(tmp)],
-                   check=True)
-    os.replace(tmp, PROBE_LIB)
-    return PROBE_LIB
-
-
 _lib: ctypes.CDLL | None = None
 
 
@@ -108,6 +92,7 @@ def load() -> ctypes.CDLL:
     lib.nsw6_set_stream.argtypes = [vp, vp]
     lib.nsw6_set_sync_check.argtypes = [vp, c_int]
     lib.nsw6_set_itelim.argtypes = [vp, c_int]
+    lib.nsw6_set_precip_stride.argtypes = [vp, ctypes.c_longlong]
     lib.nsw6_last_error.argtypes = [vp] + [ctypes.POINTER(c_int)] * 4
     lib.nsw6_set_timing.argtypes = [vp, c_int]
     lib.nsw6_set_math.argtypes = [vp, c_int]

@@ -79,12 +79,13 @@ namespace {
 
 struct LayS {
   int K, G, lall;
+  size_t pld;   // row stride of the [2][..] precipitation arrays
   __device__ __forceinline__ size_t f(int l, int k, int g) const { return ((size_t)l * K + k) * G + g; }
   __device__ __forceinline__ size_t t(int l, int n, int k, int g) const {
     return (((size_t)l * NQ + n) * K + k) * G + g;
   }
   __device__ __forceinline__ size_t c(int l, int g) const { return (size_t)l * G + g; }
-  __device__ __forceinline__ size_t p(int r, int l, int g) const { return ((size_t)r * lall + l) * G + g; }
+  __device__ __forceinline__ size_t p(int r, int l, int g) const { return (size_t)r * pld + (size_t)l * G + g; }
 };
 
 __device__ __forceinline__ void record_err(DevStatus* st, int code, int k, int g, int l, int iters) {
@@ -1748,7 +1749,7 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C,
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
-  const LayS L{P.kall, P.gall, P.lall};
+  const LayS L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
   const long long ncell = (long long)P.lall * nint * P.gall;
@@ -1815,7 +1816,7 @@ __global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, Consts C, A
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
-  const LayS L{P.kall, P.gall, P.lall};
+  const LayS L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
   const long long ncell = (long long)P.lall * nint * P.gall;
@@ -2100,7 +2101,7 @@ cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& 
                               cudaStream_t stream) {
   StageIO io;
   io.P = P;
-  io.L = LayS{P.kall, P.gall, P.lall};
+  io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld};
   io.NC = (size_t)P.lall * P.kall * P.gall;
   io.x = x;
   io.xb = dx;
@@ -2151,7 +2152,7 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
                                      int recorded, cudaStream_t stream) {
   StageIO io;
   io.P = P;
-  io.L = LayS{P.kall, P.gall, P.lall};
+  io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld};
   io.NC = (size_t)P.lall * P.kall * P.gall;
   io.x = x;
   io.xb = xb;

@@ -149,7 +149,8 @@ struct Problem {
   double *rhog, *rhogvx, *rhogvy, *rhogvz, *rhogw, *rhoge, *rhogq;
   const double *vx, *vy, *vz;
   double *rho, *tem, *pre, *q, *qd;
-  double *precip, *iso1, *iso2;          // [2][lall][gall]
+  double *precip, *iso1, *iso2;          // [2][lall][gall]: row 1 starts prec_ld doubles after row 0
+  size_t prec_ld;                        // lall * gall, or the caller's stride (nsw6_set_precip_stride)
   double *precip_rhoe, *precip_lh_heat, *precip_rhophi, *precip_rhokin;   // [lall][gall]
   double *re_liquid, *re_solid, *re_cld;
   double *rctop, *rwtop, *tctop;         // [lall][1][gall]

@@ -26,12 +26,13 @@ __device__ __forceinline__ void record_error_d(DevStatus* st, int code, int k, i
 // Index helpers for the all-regions layout.
 struct Lay {
   int K, G, lall;
+  size_t pld;   // row stride of the [2][..] precipitation arrays
   __device__ __forceinline__ size_t f(int l, int k, int g) const { return ((size_t)l * K + k) * G + g; }
   __device__ __forceinline__ size_t t(int l, int n, int k, int g) const {
     return (((size_t)l * NQ + n) * K + k) * G + g;
   }
   __device__ __forceinline__ size_t c(int l, int g) const { return (size_t)l * G + g; }
-  __device__ __forceinline__ size_t p(int r, int l, int g) const { return ((size_t)r * lall + l) * G + g; }
+  __device__ __forceinline__ size_t p(int r, int l, int g) const { return (size_t)r * pld + (size_t)l * G + g; }
 };
 
 // Visits every (argument, index, state slot) the step reads.
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_serial_kernel(Problem P, Cons
   __shared__ double tab[FM_TABLE_DOUBLES];
   stage(P, grid, tab);
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
-  const Lay L{P.kall, P.gall, P.lall};
+  const Lay L{P.kall, P.gall, P.lall, P.prec_ld};
   const int l = blockIdx.y;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= P.gall) return;
@@ -156,7 +157,7 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_tlm_kernel(Problem P, Consts 
   stage(P, grid, tab);
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
   const ADMath<Dual> mth{fm};
-  const Lay L{P.kall, P.gall, P.lall};
+  const Lay L{P.kall, P.gall, P.lall, P.prec_ld};
   const int l = blockIdx.y;
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= P.gall) return;
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(256) nsw6_adj_cellfwd_kernel(Problem P, Consts
   for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
-  const Lay L{P.kall, P.gall, P.lall};
+  const Lay L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
   const size_t ncell = (size_t)P.lall * nint * P.gall;
@@ -266,7 +267,7 @@ __global__ void __launch_bounds__(AD_THREADS, 3) nsw6_adj_cell_kernel(Problem P,
   __syncthreads();
   const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
   const ADMath<RVar> mth{fm};
-  const Lay L{P.kall, P.gall, P.lall};
+  const Lay L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
   const long long ncell = (long long)P.lall * nint * P.gall;

@@ -72,6 +72,11 @@ struct nsw6_handle {
   int itelim = 100;
   int math_lib = 0;   // 0: table-driven exp/log/pow, 1: CUDA libm
   int mixed = 0;      // 0: plain FP64 step, 1: mixed precision, 2: serial-column FP64 (derivative forward)
+  // row stride (doubles) of precip / ISO1_precip / ISO2_precip in the per-region
+  // calls mp_driver and mp_driver_mixed (0: contiguous [2][gall]); region_call
+  // marks such a call while it runs
+  long long prec_ld = 0;
+  int region_call = 0;
   // derivative kernels: parameters, their adjoint, the tape-size counter and the tapes
   double* d_dparam = nullptr;    // [16]: params [0,7), tangents [8,15)
   double* d_pbar = nullptr;      // [8]
@@ -461,6 +466,7 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.kmin = 1;
   P.kmax = h->kall - 2;
   P.lall = lall;
+  P.prec_ld = (h->region_call && h->prec_ld > 0) ? (size_t)h->prec_ld : (size_t)lall * (size_t)h->gall;
   P.dt = dt;
   P.dt2 = std::pow(dt, 2);
   P.dt3 = std::pow(dt, 3);
@@ -1002,7 +1008,17 @@ int mp_driver(nsw6_handle* h, int l_region, double* rhog, double* rhogvx, double
                         (double*)gsgam2, (double*)gsgam2h, (double*)gam2, (double*)gam2h,
                         (double*)ix, (double*)iy, (double*)iz, (double*)jx, (double*)jy, (double*)jz,
                         (double*)z, (double*)zh, GDCLW, GDCFRC, GPREC, (double*)CBMFX};
-  return run(h, 1, a, dt);
+  if (!h) return NSW6_ERR_BAD_ARG;
+  h->region_call = 1;
+  const int rc = run(h, 1, a, dt);
+  h->region_call = 0;
+  return rc;
+}
+
+int nsw6_set_precip_stride(nsw6_handle* h, long long ld) {
+  if (!h || ld < 0 || (ld > 0 && ld < h->gall)) return NSW6_ERR_BAD_ARG;
+  h->prec_ld = ld;
+  return NSW6_OK;
 }
 
 int mp_driver_mixed(nsw6_handle* h, int l_region, double* rhog, double* rhogvx, double* rhogvy, double* rhogvz,
@@ -1279,20 +1295,13 @@ static_assert(sizeof(DevStatus) <= 32 * sizeof(double), "status slot too small")
 
 static __device__ __align__(256) double g_noalloc_scratch[NA_TOTAL];
 
-constexpr int NA_MAX_DEVICES = 64;
-double* g_noalloc_ptr[NA_MAX_DEVICES] = {};
-
-// Device address of the scratch on the current device, looked up once.
+// Device address of the scratch on the current device.  Looked up on every
+// call (cheap once the module is loaded) rather than cached, so that a device
+// reset or a new context between calls cannot leave a stale address.
 int noalloc_scratch(double** out) {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return NSW6_ERR_CUDA;
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return NSW6_ERR_UNSUPPORTED;
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return NSW6_ERR_CUDA;
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return NSW6_ERR_CUDA;
+  *out = static_cast<double*>(p);
   return NSW6_OK;
 }
 }  // namespace
@@ -1304,6 +1313,11 @@ extern "C" int mp_driver_noalloc(int gall, int kall, const double* gz, const dou
   if (!gz || !gzh || !args) return NSW6_ERR_BAD_ARG;
   if (gall < 1 || kall < 5) return NSW6_ERR_BAD_ARG;
   if (kall > MAX_KALL || (long long)gall * kall > NSW6_NOALLOC_MAX_CELLS) return NSW6_ERR_TOO_LARGE;
+  // The call ends with a synchronising read of the status word, which a
+  // capturing stream does not allow: refuse before issuing anything.
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cap) != cudaSuccess) return NSW6_ERR_CUDA;
+  if (cap != cudaStreamCaptureStatusNone) return NSW6_ERR_UNSUPPORTED;
   double* base = nullptr;
   int rc = noalloc_scratch(&base);
   if (rc != NSW6_OK) return rc;

@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           default: r = b * F(S_VJ)[c]; break;
         }
       }
-      if (MIX) FF(S_RHOF)[c] = (float)r;
+      if (MIX && f >= 3) FF(S_RHOF)[c] = (float)r;
       else F(S_RHOF)[c] = r;
     };
     // flux divergence and surface fluxes (mod_precip_transport.cpp:782-842,
@@ -620,15 +620,32 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
         __syncthreads();
       }
     } else {
-      // FP32 integrals and divergences; mass, energy and kinetic-energy
-      // tendencies summed in FP64, momentum ones in FP32
+      // the mass and energy fluxes (mass, internal and potential energy) as
+      // in the FP64 step; the kinetic-energy and momentum ones as FP32
+      // integrals, the kinetic-energy tendency summed in FP64, the momentum
+      // ones in FP32
       const float* rf = FF(S_RHOF);
       float* ff = FF(S_F);
       const float* dgzf = gf;
       const float* rdgzf = gf + 2 * K;
       for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
       __syncthreads();
-      for (int f = 0; f < 6; ++f) {
+      for (int f = 0; f < 3; ++f) {
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+          double fl = 0.0;
+          if (g < G && k >= kmin && k <= kmax)
+            fl = flux_integral<COL_TG>(F(S_RHOF) + gx, dgz, k, S.kc[c], zdis0[(size_t)k * G + g], bmn_f[k], bmx_f[k]);
+          F(S_F)[c] = fl;
+        }
+        __syncthreads();
+        for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
+          divergence(f, c);
+          source(f + 1, c);
+        }
+        __syncthreads();
+      }
+      for (int f = 3; f < 6; ++f) {
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
           float fl = 0.0f;
@@ -643,34 +660,13 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           if (g < G && k >= kmin && k <= kmax) {
             const float d = (ff[c + COL_TG] - ff[c]) * rdgzf[k];
             switch (f) {
-              case 0:
-                F(dqs_slot)[c] = -(double)d;
-                if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + div_rn(-(double)ff[c], dt, P.rdt);
-                break;
-              case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - (double)d; break;
-              case 2: F(S_DRHOPHI)[c] = F(S_DRHOPHI)[c] - (double)d; break;
               case 3: F(S_DKINH)[c] = F(S_DKINH)[c] - (double)d; break;
               case 4: FF(S_DRHOGU)[c] = FF(S_DRHOGU)[c] - d; break;
               default: FF(S_DRHOGV)[c] = FF(S_DRHOGV)[c] - d; break;
             }
-            if (k == kmin && f < 4) {
-              double* acc = S.colacc;
-              const double fk = (double)ff[c];
-              const double fdt = div_rn(fk, dt, P.rdt);
-              switch (f) {
-                case 0:
-                  if (nq == I_QR) {
-                    acc[0 * COL_TG + gx] = acc[0 * COL_TG + gx] - fdt;
-                  } else {
-                    acc[1 * COL_TG + gx] = acc[1 * COL_TG + gx] - fdt;
-                    acc[2 * COL_TG + gx] = acc[2 * COL_TG + gx] + div_rn(fk * LHF0, dt, P.rdt);
-                  }
-                  break;
-                case 1: acc[3 * COL_TG + gx] = acc[3 * COL_TG + gx] - fdt; break;
-                case 2: acc[4 * COL_TG + gx] = acc[4 * COL_TG + gx] - fdt; break;
-                default: acc[5 * COL_TG + gx] = acc[5 * COL_TG + gx] - fdt; break;
-              }
-            }
+            // the kinetic energy reaching the ground (precip_rhokin)
+            if (k == kmin && f == 3)
+              S.colacc[5 * COL_TG + gx] = S.colacc[5 * COL_TG + gx] - div_rn((double)ff[c], dt, P.rdt);
           }
           if (f + 1 < 6) source(f + 1, c);
         }
@@ -1111,7 +1107,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     final_cell(c, 0, 0.0, 0.0, 0.0, 0.0);
     if (k == kmin) {
       const size_t ic = (size_t)l * G + g;
-      const size_t r0 = (size_t)l * G + g, r1 = ((size_t)P.lall + l) * G + g;
+      const size_t r0 = (size_t)l * G + g, r1 = P.prec_ld + r0;
       const double* acc = S.colacc;
       P.precip[r0] = 0.0 + acc[0 * COL_TG + gx];
       P.precip[r1] = 0.0 + acc[1 * COL_TG + gx];

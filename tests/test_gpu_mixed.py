@@ -113,3 +113,52 @@ def test_mixed_entry_equals_precision_switch():
         assert torch.equal(a[n], b[n]), n
     assert not torch.equal(a["rhogq"], c["rhogq"])
     drv.close()
+
+
+@pytest.mark.parametrize("variant,seed", [("standard", 1021), ("convective", 1022)])
+def test_mixed_conserves_column_water_like_fp64(variant, seed):
+    """Twelve steps of each path from the same state.  The water of a column
+    changes only by what falls out of it: sum_k sum_nq rhogq dz + the
+    accumulated surface precipitation x dt stays at its initial value up to
+    rounding wherever the negative filter removes no vapour (where vapour
+    goes negative the filter takes it from the air, mod_mp_nsw6.cpp:1810-1816).
+    The mixed path keeps the sedimentation's mass and energy flux sums and the
+    water budget of the process rates in FP64, so it closes that budget as
+    tightly as the FP64 path, in as many columns; there its column water and
+    internal energy stay close to the FP64 path's."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    from nicam_kokkos_microphysics_gb300.state import vertical_grid
+    spec = StateSpec(gall=16900, kall=42, lall=1, seed=seed, variant=variant)
+    st = make_state(spec, out_fill=0.0)
+    reg = region_view(st, 0)
+    gz, gzh = vertical_grid(spec.kall)
+    dz = torch.zeros(spec.kall, dtype=torch.float64, device="cuda")
+    dz[1:spec.kall - 1] = torch.from_numpy(np.diff(gzh)[1:spec.kall - 1]).cuda()
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"])
+    res = {}
+    for precision in ("fp64", "mixed"):
+        drv.set_precision(precision)
+        x = {n: torch.from_numpy(np.ascontiguousarray(reg[n])).cuda() for n in ARG_NAMES}
+        w0 = (x["rhogq"].sum(0) * dz[:, None]).sum(0)
+        acc = torch.zeros_like(w0)
+        for _ in range(12):
+            drv.mp_driver(0, *[x[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+            acc += (x["precip"][0] + x["precip"][1]) * spec.dt
+        w = (x["rhogq"].sum(0) * dz[:, None]).sum(0)
+        e = (x["rhoge"] * dz[:, None]).sum(0)
+        res[precision] = ((w - w0 + acc).abs() / w0, w, e)
+    drv.close()
+    c64, w64, e64 = res["fp64"]
+    cmx, wmx, emx = res["mixed"]
+    closed64, closedmx = c64 <= 1e-13, cmx <= 1e-13
+    f64, fmx = float(closed64.double().mean()), float(closedmx.double().mean())
+    both = closed64 & closedmx
+    dw = float(((wmx - w64).abs() / w64)[both].max())
+    de = float(((emx - e64).abs() / e64.abs())[both].max())
+    print(f"\n12 steps, {variant}: water budget closed to 1e-13 in {100 * f64:.2f} % of the columns (FP64), "
+          f"{100 * fmx:.2f} % (mixed); in the columns both close, mixed to {float(cmx[both].max()):.2e} "
+          f"(FP64 {float(c64[both].max()):.2e}), column water mixed vs FP64 {dw:.2e}, column internal energy "
+          f"{de:.2e}")
+    assert f64 > 0.9 and fmx >= f64 - 0.005
+    assert dw <= 1e-6 and de <= 1e-5
