@@ -9,13 +9,19 @@ harness loops over SET_iteration (src/main.cpp:261-319).  The working set
 (about 3 GB) is far larger than the 129 MB L2, so no flush is needed between
 steps.
 
-Metric: cells per second per NSW6 step (gall * kall * lall / step time).
+Metric: cells per second per NSW6 step (gall * kall * lall / step time).  The
+default line also carries the other two parts of the metric: the
+mixed-precision step on the same workload (its rate, end to end, and its
+per-field errors against the FP64 step), the adjoint / forward time ratio of
+one FP64 step (4096 x 42) and of the 12-step checkpointed window (5 regions of
+16900 x 42, forward FP64 and mixed-precision).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
-For N > 1 (torchrun, one process per GPU) every rank steps its own lall
-regions (weak scaling, no collective on the data path); rank 0 prints the
-line with value = all cells / max step time over ranks.
+For N > 1 (torchrun, one process per GPU) the N * lall regions are split into
+one block of lall regions per rank (shard_regions; weak scaling, no collective
+on the data path); rank 0 prints the line with value = all cells / max step
+time over ranks.
 """
 from __future__ import annotations
 
@@ -35,7 +41,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 from nicam_kokkos_microphysics_gb300.state import (ARG_NAMES, MP_DRIVER_ARGS, StateSpec, batched_shape,  # noqa: E402
-                                                   make_state, region_view)
+                                                   make_state, region_view, shard_regions)
 
 METRIC = "cells/sec per NSW6 step (FP64)"
 METRIC_MIXED = "cells/sec per NSW6 step (mixed precision)"
@@ -48,30 +54,34 @@ ALGO_BYTES_PER_CELL = 49 * 8 + 3
 # rhogq(6), q(QV), tem, gsgam2 and writes rhog, rhoge, tem, rhogq(6), q(5),
 # re_liquid, re_cld.
 CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
-# DRAM bytes (read + write) per interior cell of the cell kernel and per cell of
-# the column kernel, from ncu captures (--set full) of each kernel on one
-# 16900 x 42 region; traffic grows in proportion to cells.
-CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 215.5, "mixed": 172.9}
-COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 375.1, "mixed": 383.3}
+# Per launch of each kernel, from ncu captures of one 16900 x 42 region
+# (profiles/fp64_work_16900x42.md; every figure grows in proportion to the
+# cells): DRAM bytes read + written, and the FP64 thread instructions the
+# kernel executes -- DFMA, DADD, DMUL and all instructions of the FP64 pipe
+# (compares, min/max and conversions included) -- per interior cell (cell
+# kernel) or per cell (column kernel).
+CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 215.8, "mixed": 172.4}
+COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 374.6, "mixed": 383.8}
+FP64_EXECUTED = {
+    "nsw6_cell_kernel": {"fp64": {"dfma": 353.9, "dadd": 277.9, "dmul": 273.0, "pipe": 1015.7},
+                         "mixed": {"dfma": 29.0, "dadd": 58.0, "dmul": 46.1, "pipe": 166.9}},
+    "nsw6_column_kernel": {"fp64": {"dfma": 141.3, "dadd": 155.1, "dmul": 155.9, "pipe": 468.8},
+                           "mixed": {"dfma": 102.8, "dadd": 118.3, "dmul": 141.6, "pipe": 417.1}},
+}
 # FP64-pipe activity (fraction of active cycles) of each kernel in the same
-# captures: the hardware-level utilisation of the bound the kernels sit on.
-FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.842, "mixed": 0.747},
-                    "nsw6_column_kernel": {"fp64": 0.708, "mixed": 0.679}}
+# captures (cold, serialised launches).
+FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.841, "mixed": 0.744},
+                    "nsw6_column_kernel": {"fp64": 0.708, "mixed": 0.690}}
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
-# the throughput probe (csrc/nsw6_probe.cu) and frozen here.
-ADJOINT_LAUNCHES = 12   # kernels of one mp_driver_adjoint call (hand-written sweeps)
+# the throughput probe (probe/nsw6_probe.cu) and frozen here.
 OP_WEIGHTS = {"add": 1.0, "mul": 1.0, "cmp": 1.0, "div": 15.0, "sqrt": 15.2, "exp": 30.0, "log": 58.4,
               "pow": 173.8}
+ADJOINT_LAUNCHES = 12   # kernels of one mp_driver_adjoint call (hand-written sweeps)
 
 
 def env_rank():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
-
-
-def rank_seed(seed: int, rank: int) -> int:
-    """Each rank steps its own regions (weak scaling): a distinct state seed."""
-    return seed + 7919 * rank
 
 
 def max_over_ranks(x: float, dist=None, device: str = "cuda") -> float:
@@ -94,6 +104,14 @@ def measured_peaks():
     if p.exists():
         return json.loads(p.read_text()), "measured"
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def workload_config(spec: StateSpec, precision: str, world: int) -> dict:
+    """The `config` of both arms' lines (identical on the same workload)."""
+    return {"workload": f"NSW6 {'mixed-precision' if precision == 'mixed' else 'FP64'} step, gall={spec.gall} "
+                        f"kall={spec.kall} lall={spec.lall} per GPU ({spec.cells} cells), dt={spec.dt}",
+            "variant": spec.variant, "precision": precision, "l2": "working set >> L2 (no flush needed)",
+            "parallelism": f"regions x{world}"}
 
 
 class ClockSampler:
@@ -157,10 +175,10 @@ def fp64_rates():
     counts 2, so weight = 2 x DFMA rate / function rate, less the additions
     and multiplications the probe loop wraps around each call)."""
     import ctypes
-    from nicam_kokkos_microphysics_gb300 import _native
-    if not _native.PROBE_LIB.exists():
+    from probe import build as probe_build
+    if not probe_build.LIB.exists():
         return None
-    lib = ctypes.CDLL(str(_native.PROBE_LIB))
+    lib = ctypes.CDLL(str(probe_build.LIB))
     lib.nsw6_probe_rate.restype = ctypes.c_double
     lib.nsw6_probe_rate.argtypes = [ctypes.c_int, ctypes.c_int]
     r = {n: lib.nsw6_probe_rate(i, it) for i, (n, it) in
@@ -189,9 +207,7 @@ def algorithmic_work(spec: StateSpec, st: dict, weights: dict) -> dict:
         return sum(c[ph][k] * weights[k] for k in c[ph])
 
     return {"cell_per_interior_cell": (work("cell") + work("zdis")) / n_int,
-            "column_per_cell": work("column") / n_all,
-            "counts_per_interior_cell": {k: (c["cell"][k] + c["zdis"][k]) / n_int for k in c["cell"]},
-            "column_counts_per_cell": {k: c["column"][k] / n_all for k in c["column"]}}
+            "column_per_cell": work("column") / n_all}
 
 
 # ----------------------------------------------------------------- CPU side
@@ -201,49 +217,71 @@ def cpu_reference_sample(spec: StateSpec, steps: int, use_port: bool = False):
     Uses the reference's own sources built with the OpenMP Kokkos shim
     (oracle/_ref) when they are available, else the OpenMP build of the C
     restatement.  Returns (cells/s, kind, threads, seconds per step list)."""
-    from oracle import build_ref, restatement
     one = StateSpec(gall=spec.gall, kall=spec.kall, lall=1, seed=spec.seed, variant=spec.variant, dt=spec.dt)
     st = make_state(one, out_fill=0.0)
-    reg = region_view(st, 0)
-    cells = one.gall * one.kall
+    step, kind, threads = _reference_stepper(one, st)
+    regs = [region_view(st, 0)]
+    step(regs)  # warm-up
     times = []
-    if not use_port and build_ref.sources_available():
-        from oracle import ref
-        lib = ref.load(one.gall, one.kall, st["_gz"], st["_gzh"], variant="omp")
-        kind = "reference"
-        threads = os.cpu_count()
-        run = lambda: ref.mp_driver(lib, reg, one.dt)  # noqa: E731
-    else:
-        kind = "port"
-        lib = restatement.load("omp")
-        threads = lib.nsw6o_max_threads()
-        run = lambda: restatement.mp_driver(reg, st["_gz"], st["_gzh"], one.dt, variant="omp")  # noqa: E731
-    run()  # warm-up
     for _ in range(steps):
         t0 = time.perf_counter()
-        run()
+        step(regs)
         times.append(time.perf_counter() - t0)
-    med = statistics.median(times)
-    return cells / med, kind, threads, times
+    return one.gall * one.kall / statistics.median(times), kind, threads, times
+
+
+def _reference_stepper(spec: StateSpec, st: dict):
+    """A function stepping a list of per-region argument sets in place with
+    the reference's CPU build (oracle/_ref, OpenMP shim) or, where the
+    reference sources are absent, the OpenMP build of the C restatement."""
+    from oracle import build_ref, restatement
+    if build_ref.sources_available():
+        from oracle import ref
+        lib = ref.load(spec.gall, spec.kall, st["_gz"], st["_gzh"], variant="omp")
+
+        def step(regs):
+            for r in regs:
+                if ref.mp_driver(lib, r, spec.dt) != 0:
+                    raise RuntimeError("reference step failed")
+        return step, "reference", os.cpu_count()
+    lib = restatement.load("omp")
+
+    def step(regs):
+        for r in regs:
+            rc, status = restatement.mp_driver(r, st["_gz"], st["_gzh"], spec.dt, variant="omp")
+            if rc != 0:
+                raise RuntimeError(f"restatement step failed: {status}")
+    return step, "port", lib.nsw6o_max_threads()
 
 
 def run_reference_arm(args):
+    """The reference's CPU implementation on the GPU arm's workload: every
+    step is one mp_driver call per region over all lall regions (the
+    reference harness's loop, src/main.cpp:261-319), the state evolving in
+    place; W warm-up steps, then the mean of K timed steps."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
     spec = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall, seed=args.seed, variant=args.variant)
-    total = max(args.warmup, 0)
-    v, kind, threads, times = cpu_reference_sample(spec, max(args.steps, 1) + 0 * total)
-    ms = statistics.median(times) * 1e3
+    st = make_state(spec, out_fill=0.0)
+    step, kind, threads = _reference_stepper(spec, st)
+    regs = [region_view(st, l) for l in range(spec.lall)]
+    for _ in range(args.warmup):
+        step(regs)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step(regs)
+    ms = (time.perf_counter() - t0) / args.steps * 1e3
+    v = spec.cells / (ms * 1e-3)
     line = {
         "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded NICAM-like state)",
         "impl": "reference",
-        "config": {"workload": f"NSW6 step, gall={spec.gall} kall={spec.kall}, one region per step "
-                               f"(sample of lall={spec.lall})", "variant": spec.variant},
+        "config": workload_config(spec, "fp64", 1),
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": kind,
-                         "sample": f"{args.steps} steps x 1 region of {spec.gall}x{spec.kall} cells, median"},
+                         "sample": f"all {spec.lall} regions of {spec.gall}x{spec.kall} cells per step, "
+                                   f"{args.warmup} warm-up + {args.steps} timed steps (mean), OpenMP"},
         "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -260,7 +298,6 @@ SPECIES = ["QV", "QC", "QR", "QI", "QS", "QG"]
 
 
 def field_errors(a, b) -> dict:
-    import torch
     d = (a - b).abs()
     bmax = b.abs().max()
     sig = (b.abs() >= 1e-3 * bmax) & (b.abs() > 0)   # a field that is zero everywhere has no relative error
@@ -291,100 +328,199 @@ def mixed_vs_fp64(drv, spec: StateSpec, st0: dict) -> dict:
     return out
 
 
-def run_adjoint_bench(args) -> int:
-    """Adjoint / forward time of one step (mp_driver_adjoint around the state,
-    seeded with the loss sum (precip)^2 + column QC), or, with --window N, of
-    the window gradient of the accumulated surface precipitation (forward in
-    --precision, per-step checkpoints, FP64 adjoint)."""
+# ----------------------------------------------------------------- GPU side
+def time_device_steps(drv, lall: int, dev: dict, dt: float, steps: int, dist=None):
+    """Mean time of `steps` steps on device-resident arrays (CUDA events on the
+    library's stream, a synchronize on both sides), and the mean time of its
+    cell and column kernels (events inside the library)."""
+    import torch
+    args_dev = [dev[n] for n in ARG_NAMES]
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    drv.set_timing(True)
+    drv.read_timing()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        drv.mp_driver_batched(lall, *args_dev, dt=dt, ct=0.0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    t_cell, t_col, n = drv.read_timing()
+    drv.set_timing(False)
+    rc, cell = drv.last_error()
+    if rc != 0:
+        raise RuntimeError(f"timed steps failed with status {rc} at {cell}")
+    return e0.elapsed_time(e1) / steps, t_cell / max(n, 1), t_col / max(n, 1)
+
+
+E2E_READ = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "vx", "vy", "vz", "tem", "q",
+            "gsgam2", "gsgam2h", "gam2", "gam2h", "ix", "iy", "iz", "jx", "jy", "jz", "z"]
+E2E_WRITE = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "rho", "tem", "pre", "q", "qd",
+             "precip", "ISO1_precip", "ISO2_precip", "precip_rhoe", "precip_lh_heat", "precip_rhophi",
+             "precip_rhokin", "re_liquid", "re_solid", "re_cld", "rctop", "rwtop", "tctop", "GDCLW", "GDCFRC",
+             "GPREC"]
+
+
+def time_end_to_end(drv, spec: StateSpec, st: dict, steps: int, world: int, dist=None) -> dict:
+    """The same step through the public host-memory entry point
+    (mp_driver_argv with host = 1, via MPDriver.run on pinned numpy arrays):
+    every step copies the arguments it reads to the device and those it
+    writes back inside the call."""
+    import torch
+    kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
+    host = {}
+    for n in ARG_NAMES:
+        t = torch.empty(st[n].shape, dtype=torch.float64, pin_memory=True)
+        t.numpy()[...] = st[n]
+        host[n] = t.numpy()
+    nbytes = lambda n: int(np.prod(batched_shape(kinds[n], spec.lall, spec.kall, spec.gall))) * 8  # noqa: E731
+    drv.run(host, dt=spec.dt)  # warm-up (allocates the staging buffers)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        drv.run(host, dt=spec.dt)
+    dt_e2e = max_over_ranks((time.perf_counter() - t0) / steps, dist)
+    return {"value": whole_job_rate(spec.cells, world, dt_e2e), "unit": UNIT,
+            "h2d_bytes_per_step": sum(nbytes(n) for n in E2E_READ),
+            "d2h_bytes_per_step": sum(nbytes(n) for n in E2E_WRITE), "ms_per_step": dt_e2e * 1e3}
+
+
+def roofline_of(kernel_ms: dict, spec: StateSpec, precision: str, rates, aw) -> dict:
+    """FP64 roofline of the dominant kernel.  Both kernels are bound by the
+    FP64 pipe, which issues one DFMA, DADD, DMUL, compare, min/max or
+    conversion per thread and slot.  achieved = the FP64-pipe thread
+    instructions the kernel executes per launch (ncu, per cell, times the
+    cells of a launch) / its mean CUDA-event duration, counted at 2 flops each
+    as the peak counts a DFMA; peak = 2 x the DFMA rate the throughput probe
+    measures in this run (MEASURED_PEAKS.json has no FP64 figure); frac is the
+    share of the FP64 pipe's issue rate the kernel uses.  executed_flops
+    counts the arithmetic alone (2 per DFMA, 1 per DADD or DMUL)."""
+    peaks, src = measured_peaks()
+    n_int = spec.gall * (spec.kall - 2) * spec.lall
+    units = {"nsw6_cell_kernel": n_int, "nsw6_column_kernel": spec.cells}
+    traffic = {"nsw6_cell_kernel": CELL_KERNEL_TRAFFIC_PER_CELL[precision] * n_int,
+               "nsw6_column_kernel": COLUMN_KERNEL_TRAFFIC_PER_CELL[precision] * spec.cells}
+    top = max(kernel_ms, key=kernel_ms.get)
+    per = {}
+    for k, ms in kernel_ms.items():
+        d = {"ms": ms, "traffic": traffic[k], "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE[k][precision]}
+        ex = FP64_EXECUTED[k][precision]
+        if rates and ex:
+            d["achieved"] = 2.0 * ex["pipe"] * units[k] / (ms * 1e-3) / 1e12
+            d["frac"] = d["achieved"] / rates["peak_tflops"]
+            flops = (2.0 * ex["dfma"] + ex["dadd"] + ex["dmul"]) * units[k]
+            d["executed_flops_tflops"] = flops / (ms * 1e-3) / 1e12
+            d["executed_flops_frac"] = d["executed_flops_tflops"] / rates["peak_tflops"]
+        if rates and aw:
+            ref_work = aw["cell_per_interior_cell" if k == "nsw6_cell_kernel" else "column_per_cell"] * units[k]
+            d["reference_work_rate_over_fp64_peak"] = ref_work / (ms * 1e-3) / 1e12 / rates["peak_tflops"]
+        per[k] = d
+    hbm_cell = CELL_KERNEL_BYTES_PER_CELL * n_int / (kernel_ms["nsw6_cell_kernel"] * 1e-3) / 1e9
+    out = {"kernel": top, "bound": "fp64", "unit": "TFLOP/s", "achieved": per[top].get("achieved"),
+           "peak": rates["peak_tflops"] if rates else None, "frac": per[top].get("frac"),
+           "traffic": per[top]["traffic"],
+           "executed_flops_tflops": per[top].get("executed_flops_tflops"),
+           "executed_flops_frac": per[top].get("executed_flops_frac"),
+           "peak_source": "measured in this run: FP64 FMA throughput probe, 2 flops per DFMA "
+                          "(MEASURED_PEAKS.json has no FP64 peak)",
+           "work_definition": "FP64-pipe thread instructions the kernel executes (ncu "
+                              "sm__thread_inst_executed_pipe_fp64_pred_on per cell on one 16900 x 42 region, "
+                              "profiles/fp64_work_16900x42.md, times the cells of the launch), 2 flops each",
+           "kernels": per,
+           "hbm": {"cell_kernel_gbs": hbm_cell, "cell_kernel_frac": hbm_cell / peaks["hbm_gbs"],
+                   "peak": peaks["hbm_gbs"], "unit": "GB/s", "peak_source": f"{src} copy bandwidth"}}
+    if aw:
+        out["reference_work"] = {
+            "definition": "the reference algorithm's FP64 operations on this state (oracle op count, integer "
+                          "powers as products) weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by their "
+                          "frozen measured cost; rate / FP64 peak above 1 means the kernel does that work in less "
+                          "time than the FP64 pipe needs for it as written",
+            "per_interior_cell": aw["cell_per_interior_cell"], "column_per_cell": aw["column_per_cell"],
+            "op_weights": OP_WEIGHTS, "op_weights_this_run": rates["weights"] if rates else None}
+    return out
+
+
+def adjoint_ratio(seed: int, variant: str, steps: int, warmup: int) -> dict:
+    """Config 4: adjoint / forward time of one FP64 step on 4096 x 42 (one
+    region), both timed with CUDA events on the library's stream; the adjoint
+    seeded with the loss sum (precip)^2 + column QC."""
+    import torch
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=4096, kall=42, lall=1, seed=seed, variant=variant)
+    st = make_state(spec, out_fill=0.0)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=1)
+    x0 = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
+    kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
+    y = {n: t.clone() for n, t in x0.items()}
+    for _ in range(warmup):
+        drv.mp_driver_batched(1, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(steps):
+        drv.mp_driver_batched(1, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    e1.record()
+    torch.cuda.synchronize()
+    t_fwd = e0.elapsed_time(e1) / steps
+    bar0 = {n: torch.zeros(batched_shape(kinds[n], 1, spec.kall, spec.gall), dtype=torch.float64, device="cuda")
+            for n in ARG_NAMES}
+    seeds = []
+    for _ in range(steps + warmup):
+        b = {n: t.clone() for n, t in bar0.items()}
+        b["precip"].fill_(1.0)
+        b["rhogq"][:, 1] = 1.0
+        seeds.append(b)
+    for b in seeds[:warmup]:
+        drv.adjoint(1, x0, b, dt=spec.dt)
+    torch.cuda.synchronize()
+    e0.record()
+    for b in seeds[warmup:]:
+        drv.adjoint(1, x0, b, dt=spec.dt)
+    e1.record()
+    torch.cuda.synchronize()
+    t_adj = e0.elapsed_time(e1) / steps
+    drv.close()
+    return {"ratio": t_adj / t_fwd, "forward_ms": t_fwd, "adjoint_ms": t_adj,
+            "workload": f"adjoint of one FP64 step, gall={spec.gall} kall={spec.kall} lall=1, dt={spec.dt}",
+            "timing": "CUDA events on the library's stream, both sides", "steps": steps, "warmup": warmup}
+
+
+def window_ratio(seed: int, variant: str, nsteps: int = 12, lall: int = 5) -> dict:
+    """Config 5: gradient of the window-accumulated surface precipitation over
+    `nsteps` steps with per-step checkpoints (FP64 adjoint), against the plain
+    forward window, with the FP64 and with the mixed-precision forward."""
     import torch
     from nicam_kokkos_microphysics_gb300 import mp_init
     from nicam_kokkos_microphysics_gb300.window import window_forward, window_gradient
-    gall = args.gall if args.gall != 16900 or args.window else 4096
-    lall = args.lall if args.window else 1
-    spec = StateSpec(gall=gall, kall=args.kall, lall=lall, seed=args.seed, variant=args.variant)
+    spec = StateSpec(gall=16900, kall=42, lall=lall, seed=seed, variant=variant)
     st = make_state(spec, out_fill=0.0)
     drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
     x0 = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
-    sampler = ClockSampler(0)
-    line = {"n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded NICAM-like state)", "unit": "ratio", "gpu_launches": None}
-    if args.window:
-        for _ in range(max(1, args.warmup // 3)):
-            window_gradient(drv, spec.lall, x0, 2, spec.dt, precision=args.precision)
+    out = {"workload": f"{nsteps}-step window, gall={spec.gall} kall={spec.kall} lall={spec.lall}, dt={spec.dt}, "
+                       f"per-step checkpoints, FP64 adjoint"}
+    for precision in ("fp64", "mixed"):
+        window_gradient(drv, spec.lall, x0, 2, spec.dt, precision=precision)   # warm-up
         torch.cuda.reset_peak_memory_stats()
-        sampler.start()
-        res = window_gradient(drv, spec.lall, x0, args.window, spec.dt, precision=args.precision)
-        clocks = sampler.stop()
-        # forward alone, without checkpoints, for the ratio
+        res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision=precision)
         xs = {n: t.clone() for n, t in x0.items()}
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        window_forward(drv, spec.lall, xs, args.window, spec.dt, args.precision)
+        window_forward(drv, spec.lall, xs, nsteps, spec.dt, precision)
         torch.cuda.synchronize()
         t_plain = time.perf_counter() - t0
-        line.update({
-            "metric": "adjoint/forward time ratio, window gradient of accumulated surface precipitation",
-            "value": res["t_adjoint"] / t_plain, "steps": args.window, "warmup": args.warmup,
-            "ms_per_step": res["t_adjoint"] * 1e3 / args.window,
-            "config": {"workload": f"{args.window}-step window, gall={spec.gall} kall={spec.kall} lall={spec.lall}, "
-                                   f"dt={spec.dt}, forward {args.precision}, FP64 adjoint, per-step checkpoints",
-                       "variant": spec.variant},
-            "forward_ms": t_plain * 1e3, "forward_with_checkpoints_ms": res["t_forward"] * 1e3,
-            "adjoint_ms": res["t_adjoint"] * 1e3, "peak_device_bytes": res["peak_bytes"],
-            "J": res["J"], "dJ_dparams": res["dparams"].tolist(), "clocks": clocks,
-            "gpu_launches": args.window * 2 + args.window * ADJOINT_LAUNCHES,
-        })
-    else:
-        dev = {n: t.clone() for n, t in x0.items()}
-        kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
-        for _ in range(args.warmup):
-            y = {n: t.clone() for n, t in x0.items()}
-            drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
-        y = {n: t.clone() for n, t in x0.items()}
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        for _ in range(args.steps):
-            drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
-        e1.record()
-        torch.cuda.synchronize()
-        t_fwd = e0.elapsed_time(e1) / args.steps
-        bar = {n: torch.zeros(batched_shape(kinds[n], spec.lall, spec.kall, spec.gall), dtype=torch.float64,
-                              device="cuda") for n in ARG_NAMES}
-        drv.adjoint(spec.lall, dev, {n: b.clone() for n, b in bar.items()}, dt=spec.dt)   # warm-up, tape sizing
-        torch.cuda.reset_peak_memory_stats()
-        # the output adjoints of every timed step, prepared beforehand (the
-        # call overwrites them with the input adjoints)
-        seeds = []
-        for _ in range(args.steps):
-            b = {n: t.clone() for n, t in bar.items()}
-            b["precip"].fill_(1.0)
-            b["rhogq"][:, 1] = 1.0
-            seeds.append(b)
-        sampler.start()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for b in seeds:
-            drv.adjoint(spec.lall, dev, b, dt=spec.dt)
-        torch.cuda.synchronize()
-        t_adj = (time.perf_counter() - t0) / args.steps * 1e3
-        clocks = sampler.stop()
-        line.update({
-            "metric": "adjoint/forward time ratio of one NSW6 step", "value": t_adj / t_fwd, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": t_adj,
-            "config": {"workload": f"adjoint of one FP64 step, gall={spec.gall} kall={spec.kall} lall={spec.lall}, "
-                                   f"dt={spec.dt}", "variant": spec.variant},
-            "forward_ms": t_fwd, "adjoint_ms": t_adj, "clocks": clocks,
-            # per call: the cell phase's forward, 3 forward stages, the flux
-            # bounds, 2 seed kernels, 4 adjoint stages and the cell adjoint
-            "gpu_launches": ADJOINT_LAUNCHES * args.steps,
-        })
-    print(json.dumps(line), flush=True)
+        out[f"forward_{precision}"] = {
+            "ratio": res["t_adjoint"] / t_plain, "forward_ms": t_plain * 1e3,
+            "forward_with_checkpoints_ms": res["t_forward"] * 1e3, "adjoint_ms": res["t_adjoint"] * 1e3,
+            "peak_device_bytes": res["peak_bytes"], "J": res["J"]}
     drv.close()
-    return 0
+    return out
 
 
-# ----------------------------------------------------------------- GPU side
 def main(argv=None) -> int:
     ap = argparse.ArgumentParser(description="NSW6 step benchmark")
     ap.add_argument("--gpus", type=int, default=1)
@@ -398,15 +534,12 @@ def main(argv=None) -> int:
     ap.add_argument("--seed", type=int, default=1002)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="FP64 line only: no mixed-precision, adjoint or window sections")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
-                    help="plain FP64 step, or FP32 process rates with FP64 budgets, flux sums and Newton")
-    ap.add_argument("--adjoint", action="store_true",
-                    help="time the adjoint step against the forward step (default workload 4096 x 42, one region)")
-    ap.add_argument("--window", type=int, default=0,
-                    help="with --adjoint: gradient over a window of this many steps with per-step checkpoints")
+                    help="precision of the headline step: plain FP64, or FP32 process rates with FP64 budgets, "
+                         "flux sums and Newton")
     args = ap.parse_args(argv)
-    if args.adjoint:
-        return run_adjoint_bench(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
@@ -422,129 +555,38 @@ def main(argv=None) -> int:
 
     from nicam_kokkos_microphysics_gb300 import mp_init
 
-    spec = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall, seed=rank_seed(args.seed, rank),
-                     variant=args.variant)
-    st = make_state(spec, out_fill=0.0)
+    # this rank's block of the job's world * lall regions
+    job = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall * world, seed=args.seed, variant=args.variant)
+    st = make_state(job, out_fill=0.0, regions=shard_regions(job.lall, rank, world))
+    spec = StateSpec(gall=args.gall, kall=args.kall, lall=args.lall, seed=args.seed, variant=args.variant)
     st0 = {k: v.copy() for k, v in st.items()}
     drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
-    drv.set_precision(args.precision)
-    dev = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
-    args_dev = [dev[n] for n in ARG_NAMES]
     drv.set_sync_check(False)
 
-    def step():
-        drv.mp_driver_batched(spec.lall, *args_dev, dt=spec.dt, ct=0.0)
+    def device_run(precision: str, with_clocks: bool):
+        drv.set_precision(precision)
+        dev = {n: torch.from_numpy(st0[n]).cuda() for n in ARG_NAMES}
+        for _ in range(args.warmup):
+            drv.mp_driver_batched(spec.lall, *[dev[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        rc, cell = drv.last_error()
+        if rc != 0:
+            raise RuntimeError(f"warm-up step failed with status {rc} at {cell}")
+        sampler = ClockSampler(local) if with_clocks else None
+        if sampler:
+            sampler.start()
+            time.sleep(0.3)
+        ms, cell_ms, col_ms = time_device_steps(drv, spec.lall, dev, spec.dt, args.steps, dist)
+        clocks = sampler.stop() if sampler else None
+        del dev
+        return max_over_ranks(ms, dist), {"nsw6_cell_kernel": cell_ms, "nsw6_column_kernel": col_ms}, clocks
 
-    for _ in range(args.warmup):
-        step()
-    rc, cell = drv.last_error()
-    if rc != 0:
-        raise RuntimeError(f"warm-up step failed with status {rc} at {cell}")
+    ms, kernel_ms, clocks = device_run(args.precision, True)
+    value = whole_job_rate(spec.cells, world, ms * 1e-3)
+    e2e = None if args.no_e2e else time_end_to_end(drv, spec, st0, args.steps, world, dist)
 
-    stream = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    sampler = ClockSampler(local)
-    sampler.start()
-    time.sleep(0.3)
-    drv.set_timing(True)
-    drv.read_timing()
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
-    clocks = sampler.stop()
-    t_cell, t_col, nsteps = drv.read_timing()
-    drv.set_timing(False)
-    rc, cell = drv.last_error()
-    if rc != 0:
-        raise RuntimeError(f"timed steps failed with status {rc} at {cell}")
-    ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist)
-    cells_rank = spec.cells
-    value = whole_job_rate(cells_rank, world, ms * 1e-3)
-
-    # ---- end to end through the public API with host (pinned) buffers
-    e2e = None
-    if not args.no_e2e:
-        host = {}
-        for n in ARG_NAMES:
-            t = torch.empty(st[n].shape, dtype=torch.float64, pin_memory=True)
-            t.numpy()[...] = st[n]
-            host[n] = t.numpy()
-        from nicam_kokkos_microphysics_gb300._native import load as _load  # noqa: F401
-        import ctypes
-        kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
-        read_args = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "vx", "vy", "vz", "tem", "q",
-                     "gsgam2", "gsgam2h", "gam2", "gam2h", "ix", "iy", "iz", "jx", "jy", "jz", "z"]
-        write_args = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "rho", "tem", "pre", "q", "qd",
-                      "precip", "ISO1_precip", "ISO2_precip", "precip_rhoe", "precip_lh_heat", "precip_rhophi",
-                      "precip_rhokin", "re_liquid", "re_solid", "re_cld", "rctop", "rwtop", "tctop", "GDCLW",
-                      "GDCFRC", "GPREC"]
-        nbytes = lambda n: int(np.prod(batched_shape(kinds[n], spec.lall, spec.kall, spec.gall))) * 8  # noqa: E731
-        h2d = sum(nbytes(n) for n in read_args)
-        d2h = sum(nbytes(n) for n in write_args)
-        drv.run(host, dt=spec.dt)  # warm-up (allocates the staging buffers)
-        if dist:
-            dist.barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            drv.run(host, dt=spec.dt)
-        dt_e2e = max_over_ranks((time.perf_counter() - t0) / args.steps, dist)
-        e2e = {"value": whole_job_rate(cells_rank, world, dt_e2e), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": dt_e2e * 1e3}
-
-    # ---- mixed precision: error of one step against the FP64 path on the same state
-    mixed_error = None
-    if args.precision == "mixed":
-        mixed_error = mixed_vs_fp64(drv, spec, st0)
-
-    # ---- roofline of the dominant kernel
-    peaks, src = measured_peaks()
-    n_int = spec.gall * (spec.kall - 2) * spec.lall
-    cell_ms = t_cell / max(nsteps, 1)
-    col_ms = t_col / max(nsteps, 1)
-    rates = fp64_rates()
-    hbm_cell = CELL_KERNEL_BYTES_PER_CELL * n_int / (cell_ms * 1e-3) / 1e9
-    hbm = {"cell_kernel_gbs": hbm_cell, "cell_kernel_frac": hbm_cell / peaks["hbm_gbs"], "peak": peaks["hbm_gbs"],
-           "unit": "GB/s", "peak_source": f"{src} copy bandwidth"}
-    roofline = {"cell_kernel_ms": cell_ms, "column_kernel_ms": col_ms, "hbm": hbm}
-    if rates:
-        aw = algorithmic_work(spec, st0, OP_WEIGHTS)
-        cell_flops = aw["cell_per_interior_cell"] * n_int
-        col_flops = aw["column_per_cell"] * spec.cells
-        cell = {"achieved": cell_flops / (cell_ms * 1e-3) / 1e12, "work_per_interior_cell": aw["cell_per_interior_cell"],
-                "traffic": CELL_KERNEL_TRAFFIC_PER_CELL[args.precision] * n_int}
-        col = {"achieved": col_flops / (col_ms * 1e-3) / 1e12, "work_per_cell": aw["column_per_cell"],
-               "traffic": COLUMN_KERNEL_TRAFFIC_PER_CELL[args.precision] * spec.cells}
-        for d in (cell, col):
-            d["frac"] = d["achieved"] / rates["peak_tflops"]
-        top, other, names = (cell, col, ("nsw6_cell_kernel", "nsw6_column_kernel")) if cell_ms >= col_ms else \
-            (col, cell, ("nsw6_column_kernel", "nsw6_cell_kernel"))
-        roofline.update({
-            "kernel": names[0], "bound": "fp64", "achieved": top["achieved"], "peak": rates["peak_tflops"],
-            "unit": "TFLOP/s", "frac": top["frac"], "traffic": top["traffic"],
-            "peak_source": "measured in this run: FP64 FMA throughput probe (MEASURED_PEAKS.json has no FP64 peak)",
-            "work_definition": "FP64 operations of the reference algorithm counted on this state (integer powers "
-                               "as products), weighted add/mul/cmp 1, FMA 2, div/sqrt/exp/log/pow by their frozen "
-                               "measured cost",
-            "op_weights": OP_WEIGHTS,
-            "op_weights_this_run": rates["weights"],
-            "fp64_pipe_active_ncu": FP64_PIPE_ACTIVE[names[0]][args.precision],
-            "frac_note": "achieved counts the reference algorithm's FP64 work, so frac > 1 means the kernel does "
-                         "that work in less time than the FP64 pipe needs for it as written; the hardware "
-                         "utilisation is fp64_pipe_active_ncu",
-            names[1]: other,
-        })
-        roofline.update({"work_per_unit": top.get("work_per_interior_cell", top.get("work_per_cell"))})
-    else:
-        roofline.update({"kernel": "nsw6_cell_kernel", "bound": "hbm", "achieved": hbm_cell,
-                         "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": hbm_cell / peaks["hbm_gbs"],
-                         "traffic": None})
+    rates = fp64_rates() if rank == 0 else None
+    aw = algorithmic_work(spec, st0, OP_WEIGHTS) if rank == 0 else None
+    roofline = roofline_of(kernel_ms, spec, args.precision, rates, aw)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -557,15 +599,28 @@ def main(argv=None) -> int:
         "metric": METRIC_MIXED if mixed else METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic (seeded NICAM-like state)",
-        "config": {"workload": f"NSW6 {'mixed-precision' if mixed else 'FP64'} step, gall={spec.gall} "
-                               f"kall={spec.kall} lall={spec.lall} per GPU ({spec.cells} cells), dt={spec.dt}",
-                   "variant": spec.variant, "precision": args.precision,
-                   "l2": "working set >> L2 (no flush needed)", "parallelism": f"regions x{world}"},
+        "config": workload_config(spec, args.precision, world),
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
         "gpu_launches": 2 * args.steps,
     }
-    if mixed_error is not None:
-        line["mixed_error_vs_fp64"] = mixed_error
+
+    if not args.no_extras and world == 1:
+        # the other parts of the metric, each outside the headline's timed region
+        other = "fp64" if mixed else "mixed"
+        ms2, kernel_ms2, _ = device_run(other, False)
+        sec = {"value": whole_job_rate(spec.cells, world, ms2 * 1e-3), "unit": UNIT, "ms_per_step": ms2,
+               "mixed_speedup_over_fp64": (ms / ms2) if other == "mixed" else (ms2 / ms), "kernel_ms": kernel_ms2,
+               "roofline": roofline_of(kernel_ms2, spec, other, rates, None)}
+        if not args.no_e2e:
+            drv.set_precision(other)
+            sec["e2e"] = time_end_to_end(drv, spec, st0, args.steps, world)
+        sec["error_vs_fp64"] = mixed_vs_fp64(drv, spec, st0)
+        line["mixed" if other == "mixed" else "fp64"] = sec
+        drv.set_precision(args.precision)
+        line["adjoint"] = adjoint_ratio(args.seed, args.variant, args.steps, args.warmup)
+        line["window"] = window_ratio(args.seed, args.variant)
+    elif mixed:
+        line["mixed_error_vs_fp64"] = mixed_vs_fp64(drv, spec, st0)
     if rank == 0:
         print(json.dumps(line), flush=True)
     drv.close()
