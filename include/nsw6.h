@@ -99,9 +99,9 @@ void nsw6_default_options(nsw6_options* o);
 /* Selects the scheme switches for the following calls of the handle.  Any
  * non-default switch runs the step (FP64, or mixed precision with
  * mp_driver_mixed / nsw6_set_precision(h, 1)) in the kernels built with the
- * switched branches; with one set, nsw6_set_precision(h, 2) and
- * nsw6_set_math(h, 1) return NSW6_ERR_UNSUPPORTED, and so do mp_driver_tlm
- * and mp_driver_adjoint with qi_sediment. */
+ * switched branches; with one set, nsw6_set_precision(h, 2),
+ * nsw6_set_math(h, 1) and mp_driver_tlm under nsw6_set_adjoint_mode(h, 1)
+ * (the serial column step) return NSW6_ERR_UNSUPPORTED. */
 int nsw6_set_options(nsw6_handle* h, const nsw6_options* o);
 int nsw6_get_options(const nsw6_handle* h, nsw6_options* o);
 
@@ -267,12 +267,13 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  * converged value.  Parameters are the seven of nsw6_params in their order
  * (beta_saut, qicrt_saut, Cr, Cs, Cg, ice_nuc, kk_aut).  Any kall the handle
  * takes (kall <= 48 with nsw6_set_adjoint_mode 1, whose serial column step
- * holds a column per thread).  Of the scheme switches, all but qi_sediment
- * are taken (kk2000 = 0, aerosol_indirect = 1, roh2014 = 0, explicit_icegen =
- * 0 with the mixed-phase saturation adjustment, differentiated implicitly like
- * the liquid one, kin2kin; the adjoint then records the cell physics, and
- * with explicit_icegen = 0 or kin2kin the last column stage, on tapes);
- * qi_sediment gives NSW6_ERR_UNSUPPORTED.
+ * holds a column per thread, and takes no scheme switch).  Every scheme
+ * switch is taken (kk2000 = 0, aerosol_indirect = 1, roh2014 = 0,
+ * explicit_icegen = 0 with the mixed-phase saturation adjustment,
+ * differentiated implicitly like the liquid one, qi_sediment with cloud ice
+ * as a fourth sedimenting tracer, kin2kin; the adjoint then records the cell
+ * physics, and with explicit_icegen = 0 or kin2kin the last column stage, on
+ * tapes).
  *
  * mp_driver_tlm: advances `args` by one step (the FP64 step's outputs bit for
  *   bit) and maps the tangents in `targs` (50 device pointers, same layouts;

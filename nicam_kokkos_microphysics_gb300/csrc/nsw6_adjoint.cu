@@ -1,14 +1,14 @@
 // Level-parallel adjoint of the column phase of the NSW6 step.
 //
 // The column phase (everything after the per-cell physics: departure
-// distances, the transport of QR, QS, QG, KIN2EIN, thermodynamics, the
+// distances, the transport of QR, (QI,) QS, QG, KIN2EIN, thermodynamics, the
 // saturation adjustment and the closing negative filter) is split at the
 // points where a value computed at one level is read at another, into four
 // per-cell stages:
 //
 //   S1  departure distances (vadv1d_prep, mod_vadv1d.cpp:231-391) from the
-//       fall speeds, the kinetic energies and the 24 flux sources
-//       (mod_precip_transport.cpp:767-900) of one cell;
+//       fall speeds, the kinetic energies and the eight flux sources of each
+//       sedimenting tracer (mod_precip_transport.cpp:767-900) of one cell;
 //   S2  one flux integral of vadv1d_getflux_new (mod_vadv1d.cpp:393-450) of
 //       one cell (a work item per cell and flux);
 //   S3  the flux divergences, surface fluxes and the application of the
@@ -44,19 +44,35 @@
 
 namespace nsw6 {
 
-// Cell-phase output fields (Y / YB layout of nsw6_deriv.cu).
+// Cell-phase output fields (Y / YB layout of nsw6_deriv.cu).  Fall speeds:
+// YS_VT + 0 Vtr, + 1 Vts, + 2 Vtg, + 3 Vti (0 unless QI sediments).
 enum AdjFieldS {
-  YS_RHOG, YS_RHOGE, YS_TEM, YS_RHOGQ, YS_Q = YS_RHOGQ + 6, YS_VT = YS_Q + 5, YS_RE = YS_VT + 3, YS_RECLD,
+  YS_RHOG, YS_RHOGE, YS_TEM, YS_RHOGQ, YS_Q = YS_RHOGQ + 6, YS_VT = YS_Q + 5, YS_RE = YS_VT + 4, YS_RECLD,
   YS_RCTOP, YS_TCTOP, ADJ_Y_FIELDS
 };
 
-// Work fields of the staged column adjoint: [NWF][lall][kall][gall].
+// Sedimenting tracer t of ntr in the transport's order (mod_mp_nsw6.cpp:596-599,
+// mod_precip_transport.cpp:767): QR, QS, QG, or QR, QI, QS, QG when QI
+// sediments ("4WATER"); nq its tracer index, vt its fall speed's Y field.
+struct SedTracer {
+  int nq, vt;
+};
+__device__ __forceinline__ SedTracer sed_tracer(int t, int ntr) {
+  if (t == 0) return {I_QR, YS_VT + 0};
+  if (ntr == 4 && t == 1) return {I_QI, YS_VT + 3};
+  const int u = ntr == 4 ? t - 1 : t;   // 1: QS, 2: QG
+  return {u == 1 ? I_QS : I_QG, YS_VT + u};
+}
+constexpr int MAX_TR = 4;
+
+// Work fields of the staged column adjoint: [NWF][lall][kall][gall], laid out
+// for up to four sedimenting tracers (t < ntr are used).
 enum WorkField {
-  W_ZDIS = 0,                  // 6 departure distances (QR, QS, QG full; QR, QS, QG half)
-  W_KINH = 6, W_KINV,          // kinetic energies of the transport's input state
-  W_RHOF = 8,                  // 24 flux sources, tracer t, flux j: W_RHOF + 8 t + j (j < 6 full, 6..7 half)
-  W_F = W_RHOF + 24,           // 24 fluxes, same order
-  W_RHOG_N = W_F + 24, W_RHOGE_N, W_RVX_N, W_RVY_N, W_RVZ_N, W_RW_N,
+  W_ZDIS = 0,                  // 2 ntr departure distances: row t full, row ntr + t half
+  W_KINH = 2 * MAX_TR, W_KINV, // kinetic energies of the transport's input state
+  W_RHOF,                      // flux sources, tracer t, flux j: W_RHOF + 8 t + j (j < 6 full, 6..7 half)
+  W_F = W_RHOF + 8 * MAX_TR,   // fluxes, same order
+  W_RHOG_N = W_F + 8 * MAX_TR, W_RHOGE_N, W_RVX_N, W_RVY_N, W_RVZ_N, W_RW_N,
   W_RQ_N,                      // 6 tracers
   W_KINH_N = W_RQ_N + 6, W_KINV_N,
   NWF
@@ -108,7 +124,7 @@ struct StageIO {
   double* W;
   double* WB;
   const double* SB;     // seeds [NSF][NC] then [NSC][lall][gall]
-  const int* bnd;       // flux bounds [lall][2][6][kall]: bmn then bmx
+  const int* bnd;       // flux bounds [lall][2][2 MAX_TR][kall]: bmn then bmx, rows as W_ZDIS
   int kin2kin;          // the KIN2KIN switch: S4, not S3, gives the final momenta
 };
 
@@ -211,15 +227,16 @@ __device__ void stage1(const In<T>& in, const double* gr, int k, const O& out) {
   const double* afact = gr + GF_AFACT * K;
   const double* bfact = gr + GF_BFACT * K;
   const bool interior = (k >= kmin && k <= kmax);
+  const int ntr = P.ntr;
   // fall speeds at levels k-3 .. k+1 (zero outside the interior)
-  T vt[3][5];
-  for (int t = 0; t < 3; ++t)
+  T vt[MAX_TR][5];
+  for (int t = 0; t < ntr; ++t)
     for (int j = 0; j < 5; ++j) {
       const int kk = k - 3 + j;
-      vt[t][j] = (interior && kk >= kmin && kk <= kmax) ? in.y(YS_VT + t, kk) : T(0.0);
+      vt[t][j] = (interior && kk >= kmin && kk <= kmax) ? in.y(sed_tracer(t, ntr).vt, kk) : T(0.0);
     }
-  for (int r = 0; r < 6; ++r) {
-    const int t = r % 3, half = r / 3;
+  for (int r = 0; r < 2 * ntr; ++r) {
+    const int t = r % ntr, half = r / ntr;
     const int mkmin = half ? kmin + 1 : kmin;
     T z = T(0.0);
     if (k >= mkmin && k <= kmax) {
@@ -255,14 +272,13 @@ __device__ void stage1(const In<T>& in, const double* gr, int k, const O& out) {
   }
   out(W_KINH, kinh);
   out(W_KINV, kinv);
-  // flux sources of QR, QS, QG (mod_precip_transport.cpp:776-808, 864-882)
-  const int tracer[3] = {I_QR, I_QS, I_QG};
+  // flux sources of the sedimenting tracers (mod_precip_transport.cpp:776-808, 864-882)
   const T tem = interior ? st_tem(in, k) : T(0.0);
   const T zz = interior ? xf(in, A_z, k) : T(0.0);
   T rgsh = T(0.0);
   if (hk) rgsh = xf(in, A_gam2h, k) / xf(in, A_gsgam2h, k);
-  for (int t = 0; t < 3; ++t) {
-    const int nq = tracer[t];
+  for (int t = 0; t < ntr; ++t) {
+    const int nq = sed_tracer(t, ntr).nq;
     T base = T(0.0), qn = T(0.0);
     if (interior) {
       base = st_rhogq(in, nq, k) * rgs;
@@ -293,9 +309,9 @@ __device__ T stage2(const In<T>& in, const double* gr, int k, int j) {
   const bool full = f < 6;
   const int mkmin = full ? kmin : kmin + 1;
   if (k < mkmin || k > kmax) return T(0.0);
-  const int r = full ? t : 3 + t;
-  const int* bmn = in.io.bnd + ((size_t)in.l * 2 + 0) * 6 * K;
-  const int* bmx = in.io.bnd + ((size_t)in.l * 2 + 1) * 6 * K;
+  const int r = full ? t : P.ntr + t;
+  const int* bmn = in.io.bnd + ((size_t)in.l * 2 + 0) * 2 * MAX_TR * K;
+  const int* bmx = in.io.bnd + ((size_t)in.l * 2 + 1) * 2 * MAX_TR * K;
   // the integral's range: the half levels use the full-level kcell_max
   // (mod_precip_transport.cpp:890, 892)
   const int lo = bmn[r * K + k];
@@ -329,12 +345,12 @@ __device__ void stage3(const In<T>& in, const double* gr, int k, const O& o, con
   const double dt = P.dt;
   const bool interior = (k >= kmin && k <= kmax);
   const bool hk = (k >= kmin + 1 && k <= kmax);
-  T dq[3] = {T(0.0), T(0.0), T(0.0)};
+  const int ntr = P.ntr;
+  T dq[MAX_TR] = {T(0.0), T(0.0), T(0.0), T(0.0)};
   T drhoe = T(0.0), drhophi = T(0.0), dkinh = T(0.0), dkinv = T(0.0), du = T(0.0), dv = T(0.0), dw = T(0.0);
   T acc[6] = {T(0.0), T(0.0), T(0.0), T(0.0), T(0.0), T(0.0)};
-  const int tracer[3] = {I_QR, I_QS, I_QG};
-  for (int t = 0; t < 3; ++t) {
-    const int nq = tracer[t];
+  for (int t = 0; t < ntr; ++t) {
+    const int nq = sed_tracer(t, ntr).nq;
     if (interior) {
       for (int f = 0; f < 6; ++f) {
         const T fk = in.w(W_F + 8 * t + f, k), fk1 = in.w(W_F + 8 * t + f, k + 1);
@@ -409,13 +425,21 @@ __device__ void stage3(const In<T>& in, const double* gr, int k, const O& o, con
   o(W_RQ_N + I_QR, st_rhogq(in, I_QR, k) + dq[0]);
   rhog = rhog + dq[0];
   rhoge = rhoge - dq[0] * GRAV * zz;
-  o(W_RQ_N + I_QI, st_rhogq(in, I_QI, k) + 0.0);
-  o(W_RQ_N + I_QS, st_rhogq(in, I_QS, k) + dq[1]);
-  rhog = rhog + dq[1];
-  rhoge = rhoge - dq[1] * GRAV * zz;
-  o(W_RQ_N + I_QG, st_rhogq(in, I_QG, k) + dq[2]);
-  rhog = rhog + dq[2];
-  rhoge = rhoge - dq[2] * GRAV * zz;
+  // (tracers in order QV..QG; QI adds an exact zero unless it sediments)
+  const int ts = ntr - 2, tg = ntr - 1;   // QS, QG
+  if (ntr == 4) {
+    o(W_RQ_N + I_QI, st_rhogq(in, I_QI, k) + dq[1]);
+    rhog = rhog + dq[1];
+    rhoge = rhoge - dq[1] * GRAV * zz;
+  } else {
+    o(W_RQ_N + I_QI, st_rhogq(in, I_QI, k) + 0.0);
+  }
+  o(W_RQ_N + I_QS, st_rhogq(in, I_QS, k) + dq[ts]);
+  rhog = rhog + dq[ts];
+  rhoge = rhoge - dq[ts] * GRAV * zz;
+  o(W_RQ_N + I_QG, st_rhogq(in, I_QG, k) + dq[tg]);
+  rhog = rhog + dq[tg];
+  rhoge = rhoge - dq[tg] * GRAV * zz;
   o(W_RHOG_N, rhog);
   o(W_RHOGE_N, rhoge);
 }
@@ -656,12 +680,13 @@ __device__ __forceinline__ bool stage_overflow(const StageIO& io, const LeafLog&
 // the column kernel forms them.
 __global__ void adj_bounds_kernel(Problem P, int* bnd) {
   const int K = P.kall;
-  const int n = P.lall * 6 * K;
+  const int nrow = 2 * P.ntr;
+  const int n = P.lall * nrow * K;
   const double* gzh = P.grid + GF_GZH * K;
   const double* gzs = P.grid + GF_GZSHIFT * K;
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
-    const int k = e % K, s = (e / K) % 6, l = e / (6 * K);
-    const int half = s / 3;
+    const int k = e % K, s = (e / K) % nrow, l = e / (nrow * K);
+    const int half = s / P.ntr;
     const int mkmin = half ? P.kmin + 1 : P.kmin;
     const double* zh = half ? gzs : gzh;
     int lo = k, hi = k;
@@ -691,8 +716,8 @@ __global__ void adj_bounds_kernel(Problem P, int* bnd) {
           }
       }
     }
-    bnd[((size_t)l * 2 + 0) * 6 * K + s * K + k] = lo;
-    bnd[((size_t)l * 2 + 1) * 6 * K + s * K + k] = hi;
+    bnd[((size_t)l * 2 + 0) * 2 * MAX_TR * K + s * K + k] = lo;
+    bnd[((size_t)l * 2 + 1) * 2 * MAX_TR * K + s * K + k] = hi;
   }
 }
 
@@ -703,23 +728,24 @@ __global__ void adj_bounds_kernel(Problem P, int* bnd) {
 // order-preserving keys (exact, independent of the order of the atomics).
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_fwd_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
-  __shared__ unsigned long long red[2][6][STAGE_THREADS / 32];
+  __shared__ unsigned long long red[2][2 * MAX_TR][STAGE_THREADS / 32];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
   const int g = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y, l = blockIdx.z;
   const bool valid = g < io.L.G;
-  double z[6] = {0, 0, 0, 0, 0, 0};
+  const int nrow = 2 * io.P.ntr;
+  double z[2 * MAX_TR] = {0, 0, 0, 0, 0, 0, 0, 0};
   if (valid) {
     const size_t c = io.L.f(l, k, g);
     const In<double> in{io, l, g};
     stage1<double>(in, grid, k, [&](int f, double v) {
       io.W[f * io.NC + c] = v;
-      if (f < 6) z[f] = v;
+      if (f < nrow) z[f] = v;
     });
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int r = 0; r < 6; ++r) {
-    const int mkmin = r < 3 ? io.P.kmin : io.P.kmin + 1;
+  for (int r = 0; r < nrow; ++r) {
+    const int mkmin = r < io.P.ntr ? io.P.kmin : io.P.kmin + 1;
     const bool in_range = valid && k >= mkmin && k <= io.P.kmax && z[r] == z[r];   // NaN never wins
     unsigned long long kmx = in_range ? order_key(z[r]) : 0ull;
     unsigned long long kmn = in_range ? order_key(z[r]) : ~0ull;
@@ -736,14 +762,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_fwd_kernel(StageIO io) {
     }
   }
   __syncthreads();
-  if (threadIdx.x < 6) {
+  if (threadIdx.x < nrow) {
     const int r = threadIdx.x;
     unsigned long long kmx = 0ull, kmn = ~0ull;
     for (int w = 0; w < (int)blockDim.x / 32; ++w) {
       kmx = red[0][r][w] > kmx ? red[0][r][w] : kmx;
       kmn = red[1][r][w] < kmn ? red[1][r][w] : kmn;
     }
-    const size_t e = ((size_t)l * 6 + r) * io.P.kall + k;
+    const size_t e = ((size_t)l * nrow + r) * io.P.kall + k;
     if (kmx != 0ull) atomicMax(&io.P.zmax[e], kmx);
     if (kmn != ~0ull) atomicMin(&io.P.zmin[e], kmn);
   }
@@ -754,7 +780,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_fwd_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
-  const size_t n = io.NC * 24;
+  const size_t n = io.NC * 8 * io.P.ntr;
   for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
     const size_t c = w % io.NC;
     const int j = (int)(w / io.NC);
@@ -1264,17 +1290,18 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     auto XBown = [&](int a, size_t i, double v) { xb[a][i] += v; };
     auto WB = [&](int f) { return io.WB[f * NC + c]; };
     // ---------------------------------------------------- departure distances
-    double vt[3][5];
-    for (int t = 0; t < 3; ++t)
+    const int ntr = P.ntr;
+    double vt[MAX_TR][5];
+    for (int t = 0; t < ntr; ++t)
       for (int j = 0; j < 5; ++j) {
         const int kk = k - 3 + j;
-        vt[t][j] = (kk >= kmin && kk <= kmax) ? Y(YS_VT + t, c + (size_t)(j - 3) * G) : 0.0;
+        vt[t][j] = (kk >= kmin && kk <= kmax) ? Y(sed_tracer(t, ntr).vt, c + (size_t)(j - 3) * G) : 0.0;
       }
-    double bvt[3][5] = {};
-    for (int r = 0; r < 6; ++r) {
+    double bvt[MAX_TR][5] = {};
+    for (int r = 0; r < 2 * ntr; ++r) {
       const double bz = WB(W_ZDIS + r);
       if (bz == 0.0) continue;
-      const int t = r % 3, half = r / 3;
+      const int t = r % ntr, half = r / ntr;
       const int mkmin = half ? kmin + 1 : kmin;
       if (k < mkmin) continue;
       auto col = [&](int j) { return vt[t][j - k + 3]; };
@@ -1310,10 +1337,10 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
         }
       }
     }
-    for (int t = 0; t < 3; ++t)
+    for (int t = 0; t < ntr; ++t)
       for (int j = 0; j < 5; ++j) {
         const int kk = k - 3 + j;
-        if (kk >= kmin && kk <= kmax) YBadd(YS_VT + t, c + (size_t)(j - 3) * G, bvt[t][j]);
+        if (kk >= kmin && kk <= kmax) YBadd(sed_tracer(t, ntr).vt, c + (size_t)(j - 3) * G, bvt[t][j]);
       }
     // ------------------------------------------- metric factors, kinetic energy
     // (recomputed for the partials only, so by reciprocals; no branch reads them)
@@ -1350,9 +1377,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     // ------------------------------------------------------------- sources
     double b_kinh = WB(W_KINH), b_kinv = WB(W_KINV), b_rgs = 0.0, b_rgsh = 0.0, b_rw = 0.0;
     double b_tem = 0.0, b_zz = 0.0, b_vi = 0.0, b_vj = 0.0;
-    const int tracer[3] = {I_QR, I_QS, I_QG};
-    for (int t = 0; t < 3; ++t) {
-      const int nq = tracer[t];
+    for (int t = 0; t < ntr; ++t) {
+      const int nq = sed_tracer(t, ntr).nq;
       const double* bs = io.WB + (size_t)(W_RHOF + 8 * t) * NC + c;
       const double b0 = bs[0], b1 = bs[NC], b2 = bs[2 * NC], b3 = bs[3 * NC], b4 = bs[4 * NC], b5 = bs[5 * NC];
       const double b6 = hk ? bs[6 * NC] : 0.0, b7 = hk ? bs[7 * NC] : 0.0;
@@ -1424,11 +1450,11 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
 // Adjoint of S3, hand-written.  S3 is linear in the fluxes and tendencies, so
 // the adjoints of the divergences at a level follow from that level's output
 // adjoints alone; every cell rebuilds them for itself and its neighbours and
-// gathers the adjoint of each of its 24 fluxes (no atomics; written, not
+// gathers the adjoint of each of its 8 ntr fluxes (no atomics; written, not
 // added: S3 is their only reader).  The other input adjoints are the cell's
 // own, added where they live; the unit vectors, shared by a column, atomically.
 struct S3Bar {
-  double dq[3], drhoe, drhophi, dkinh, du, dv, dkinv, dw;
+  double dq[MAX_TR], drhoe, drhophi, dkinh, du, dv, dkinv, dw;
 };
 __device__ __forceinline__ S3Bar s3_bars(const StageIO& io, int l, int k, int g) {
   const size_t c = io.L.f(l, k, g), NC = io.NC;
@@ -1440,8 +1466,8 @@ __device__ __forceinline__ S3Bar s3_bars(const StageIO& io, int l, int k, int g)
   const size_t ic = io.L.c(l, g);
   const double z = io.x.a[A_z][c];
   S3Bar b;
-  const int tr[3] = {I_QR, I_QS, I_QG};
-  for (int t = 0; t < 3; ++t) b.dq[t] = io.WB[(W_RQ_N + tr[t]) * NC + c] + B_rhog - B_rhoge * GRAV * z;
+  for (int t = 0; t < io.P.ntr; ++t)
+    b.dq[t] = io.WB[(W_RQ_N + sed_tracer(t, io.P.ntr).nq) * NC + c] + B_rhog - B_rhoge * GRAV * z;
   b.drhoe = B_rhoge;
   b.drhophi = B_rhoge;
   b.dkinh = io.WB[W_KINH_N * NC + c];
@@ -1482,7 +1508,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_hw_kernel(StageIO io) {
     if (in_km) bm = s3_bars(io, l, k - 1, g);
     if (hkp) bp = s3_bars(io, l, k + 1, g);
     // flux adjoints
-    for (int t = 0; t < 3; ++t) {
+    const int ntr = P.ntr;
+    for (int t = 0; t < ntr; ++t) {
       for (int f = 0; f < 6; ++f) {
         double bF = 0.0;
         if (in_km) bF += s3_bd(bm, t, f) * rdgz[k - 1];
@@ -1505,8 +1532,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_hw_kernel(StageIO io) {
       const double bph = SC[SC_RHOPHI * ncol + ic], bkn = SC[SC_RHOKIN * ncol + ic];
       double* F = io.WB + (size_t)W_F * io.NC + c;
       F[(8 * 0 + 0) * io.NC] -= bp0 / dt;
-      for (int t = 1; t < 3; ++t) F[(8 * t + 0) * io.NC] += -bp1 / dt + blh * LHF0 / dt;
-      for (int t = 0; t < 3; ++t) {
+      for (int t = 1; t < ntr; ++t) F[(8 * t + 0) * io.NC] += -bp1 / dt + blh * LHF0 / dt;
+      for (int t = 0; t < ntr; ++t) {
         F[(8 * t + 1) * io.NC] -= bre / dt;
         F[(8 * t + 2) * io.NC] -= bph / dt;
         F[(8 * t + 3) * io.NC] -= bkn / dt;
@@ -1537,13 +1564,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_hw_kernel(StageIO io) {
     if (in_k) {
       // the tendencies at this level (forward values) for the products with z and the unit vectors
       const double* Fw = io.W + (size_t)W_F * NC + c;
-      double dq[3], du = 0.0, dv = 0.0;
-      for (int t = 0; t < 3; ++t) {
-        dq[t] = -((Fw[(8 * t + 0) * NC + io.L.G] - Fw[(8 * t + 0) * NC]) * rdgz[k]);
+      double dqsum = 0.0, du = 0.0, dv = 0.0;
+      for (int t = 0; t < ntr; ++t) {
+        dqsum -= (Fw[(8 * t + 0) * NC + io.L.G] - Fw[(8 * t + 0) * NC]) * rdgz[k];
         du = du - (Fw[(8 * t + 4) * NC + io.L.G] - Fw[(8 * t + 4) * NC]) * rdgz[k];
         dv = dv - (Fw[(8 * t + 5) * NC + io.L.G] - Fw[(8 * t + 5) * NC]) * rdgz[k];
       }
-      const double bz = -B_rhoge * GRAV * (dq[0] + dq[1] + dq[2]);
+      const double bz = -B_rhoge * GRAV * dqsum;
       io.xb.a[A_z][c] += bz;
       const size_t ic = io.L.c(l, g);
       atomicAdd(&io.xb.a[A_ix][ic], B_rvx * du);
@@ -1563,7 +1590,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_kernel(StageIO io, TapeM
   __syncthreads();
   tape_bind_s(tm);
   LeafLog lg;
-  const size_t n = io.NC * 24;
+  const size_t n = io.NC * 8 * io.P.ntr;
   for (size_t w = tape().slot; w < n; w += tape().nslot) {
     const size_t c = w % io.NC;
     const int j = (int)(w / io.NC);
@@ -1593,14 +1620,15 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_hw_kernel(StageIO io) {
   const Problem& P = io.P;
   const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
   const size_t NC = io.NC, G = io.L.G;
-  const size_t n = NC * 3;
+  const int ntr = P.ntr;
+  const size_t n = NC * ntr;
   for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
     const size_t c = w % NC;
     const int t = (int)(w / NC);
     const int k = (int)((c / G) % K), l = (int)(c / (G * K));
     if (k < kmin || k > kmax) continue;
-    const int* bmn = io.bnd + ((size_t)l * 2 + 0) * 6 * K;
-    const int* bmx = io.bnd + ((size_t)l * 2 + 1) * 6 * K;
+    const int* bmn = io.bnd + ((size_t)l * 2 + 0) * 2 * MAX_TR * K;
+    const int* bmx = io.bnd + ((size_t)l * 2 + 1) * 2 * MAX_TR * K;
     for (int half = 0; half < 2; ++half) {
       const int mkmin = half ? kmin + 1 : kmin;
       if (k < mkmin) continue;
@@ -1609,7 +1637,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_hw_kernel(StageIO io) {
       for (int f = f0; f < f1; ++f)
         any = any || (io.WB[(W_F + 8 * t + f) * NC + c] != 0.0 && io.W[(W_F + 8 * t + f) * NC + c] != 0.0);
       if (!any) continue;
-      const int r = half ? 3 + t : t;
+      const int r = half ? ntr + t : t;
       const int lo = bmn[r * K + k];
       const int hi = bmx[t * K + k];
       const double* zh = grid + (half ? GF_GZSHIFT : GF_GZH) * K;
@@ -1777,6 +1805,7 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C,
     y[YS_VT + 0] = o.Vtr;
     y[YS_VT + 1] = o.Vts;
     y[YS_VT + 2] = o.Vtg;
+    y[YS_VT + 3] = 0.0;   // QI does not sediment in this (switch-free) cell phase
     y[YS_RE] = o.rceff;
     y[YS_RECLD] = o.rceff_cld;
     y[YS_RCTOP] = o.rctop;
@@ -1794,6 +1823,7 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C,
       z[YS_VT + 0] = r.Vtr;
       z[YS_VT + 1] = r.Vts;
       z[YS_VT + 2] = r.Vtg;
+      z[YS_VT + 3] = 0.0;
       z[YS_RE] = r.rceff;
       z[YS_RECLD] = r.rceff_cld;
       z[YS_RCTOP] = r.rctop;
@@ -1938,6 +1968,7 @@ __global__ void __launch_bounds__(128) tlm_cell_kernel(StageIO io, Consts C, con
     put(YS_VT + 0, o.Vtr);
     put(YS_VT + 1, o.Vts);
     put(YS_VT + 2, o.Vtg);
+    put(YS_VT + 3, o.Vti);
     put(YS_RE, o.rceff);
     put(YS_RECLD, o.rceff_cld);
     put(YS_RCTOP, o.rctop);
@@ -1962,7 +1993,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s2_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
-  const size_t n = io.NC * 24;
+  const size_t n = io.NC * 8 * io.P.ntr;
   for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
     const size_t c = w % io.NC;
     const int j = (int)(w / io.NC);
@@ -2081,7 +2112,7 @@ size_t adj_stage_work_doubles(int lall, int kall, int gall) {
   const size_t NC = (size_t)lall * kall * gall;
   return 2 * (size_t)NWF * NC + (size_t)NSF * NC + (size_t)NSC * lall * gall;
 }
-size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 6 * kall; }
+size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 2 * MAX_TR * kall; }
 int adj_stage_tape_cap() { return 512; }
 int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
 
@@ -2113,7 +2144,7 @@ cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& 
   io.bnd = bnd;
   io.kin2kin = P.opt && C.opt_kin2kin != 0.0;
   cudaError_t e;
-  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  const size_t nkey = (size_t)P.lall * 2 * P.ntr * P.kall;
   if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
   if (P.opt)
@@ -2167,7 +2198,7 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   cudaError_t e;
   if ((e = cudaMemsetAsync(io.WB, 0, sizeof(double) * NWF * io.NC, stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(YB, 0, sizeof(double) * ny * io.NC, stream)) != cudaSuccess) return e;
-  const size_t nkey = (size_t)P.lall * 6 * P.kall;
+  const size_t nkey = (size_t)P.lall * 2 * P.ntr * P.kall;
   if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
   adj_s1_fwd_kernel<<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(

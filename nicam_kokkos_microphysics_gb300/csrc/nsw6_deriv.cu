@@ -197,7 +197,8 @@ __global__ void __launch_bounds__(AD_THREADS) nsw6_tlm_kernel(Problem P, Consts 
 // Y / YB layout: [ADJ_NF][lall][kall][gall], fields below.
 enum AdjField {
   Y_RHOG, Y_RHOGE, Y_TEM, Y_RHOGQ, Y_Q = Y_RHOGQ + 6,   // Y_Q + n - 1 for q[n], n = 1..5
-  Y_VT = Y_Q + 5, Y_RE = Y_VT + 3, Y_RECLD, Y_RCTOP, Y_TCTOP, ADJ_NF
+  Y_VT = Y_Q + 5,   // fall speeds: Y_VT + 0 Vtr, + 1 Vts, + 2 Vtg, + 3 Vti (0 unless QI sediments)
+  Y_RE = Y_VT + 4, Y_RECLD, Y_RCTOP, Y_TCTOP, ADJ_NF
 };
 
 // OPT: the cell physics with the scheme switches (the CCN field a constant input).
@@ -233,6 +234,7 @@ __global__ void __launch_bounds__(256) nsw6_adj_cellfwd_kernel(Problem P, Consts
     Y[(Y_VT + 0) * NC + i] = o.Vtr;
     Y[(Y_VT + 1) * NC + i] = o.Vts;
     Y[(Y_VT + 2) * NC + i] = o.Vtg;
+    Y[(Y_VT + 3) * NC + i] = o.Vti;
     Y[Y_RE * NC + i] = o.rceff;
     Y[Y_RECLD * NC + i] = o.rceff_cld;
     Y[Y_RCTOP * NC + i] = o.rctop;
@@ -309,6 +311,7 @@ __global__ void __launch_bounds__(AD_THREADS, 3) nsw6_adj_cell_kernel(Problem P,
     seed(o.Vtr, Y_VT + 0);
     seed(o.Vts, Y_VT + 1);
     seed(o.Vtg, Y_VT + 2);
+    seed(o.Vti, Y_VT + 3);
     seed(o.rceff, Y_RE);
     seed(o.rceff_cld, Y_RECLD);
     if (k == P.kmax) {

@@ -609,15 +609,13 @@ int deriv_prepass(nsw6_handle* h, int lall, double* const* a, double dt) {
 }
 
 // serial: the call runs the serial column step (one column per thread, at
-// most DERIV_MAX_KALL levels); the staged derivative kernels take any kall,
-// and every scheme switch but QI sedimentation (Berry warm rain, the aerosol
+// most DERIV_MAX_KALL levels, no scheme switch); the staged derivative
+// kernels take any kall and every scheme switch (Berry warm rain, the aerosol
 // effect, the classic snow moments, the Bergeron process with the mixed-phase
-// saturation adjustment, KIN2KIN).
+// saturation adjustment, QI sedimentation, KIN2KIN).
 int deriv_check(nsw6_handle* h, int lall, double* const* a, double* const* b, bool serial) {
   if (!h || !a || !b || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
-  const bool staged_ok = !h->opts.qi_sediment;
-  if ((serial && h->kall > DERIV_MAX_KALL) || (h->opt_active && (serial || !staged_ok)))
-    return NSW6_ERR_UNSUPPORTED;
+  if ((serial && h->kall > DERIV_MAX_KALL) || (h->opt_active && serial)) return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
     if ((arg_is_read(i) || arg_is_written(i)) && (!a[i] || !b[i])) return NSW6_ERR_BAD_ARG;
   if (!h->d_dparam) {

@@ -37,6 +37,10 @@ CELL_SWITCHES = dict(roh2014=0, explicit_icegen=1, kk2000=0, aerosol_indirect=1)
 ICE_SWITCHES = dict(roh2014=0, explicit_icegen=0, kk2000=0, aerosol_indirect=1)
 # the transport's kinetic-energy correction KIN2KIN in place of KIN2EIN
 KIN2KIN = dict(kin2kin=1)
+# cloud ice sediments as a fourth tracer ("4WATER")
+QI_SEDIMENT = dict(qi_sediment=1)
+# every switch off its default at once
+ALL_SWITCHES = dict(roh2014=0, explicit_icegen=0, kk2000=0, qi_sediment=1, kin2kin=1, aerosol_indirect=1)
 
 
 def _setup(gall=4096, kall=42, lall=1, seed=2024, variant="standard", options=None):
@@ -72,12 +76,14 @@ def test_serial_forward_bitwise_equals_production(variant, gall, kall):
 @pytest.mark.parametrize("gall,kall,lall,options,variant", [
     (1024, 42, 1, None, "convective"), (192, 160, 2, None, "convective"),
     (1024, 42, 1, CELL_SWITCHES, "convective"), (1024, 42, 1, ICE_SWITCHES, "cold"),
-    (1024, 42, 1, KIN2KIN, "convective")],
-    ids=["42", "160", "switches", "ice-switches", "kin2kin"])
+    (1024, 42, 1, KIN2KIN, "convective"), (1024, 42, 2, QI_SEDIMENT, "cold"),
+    (192, 160, 1, QI_SEDIMENT, "cold"), (1024, 42, 1, ALL_SWITCHES, "cold")],
+    ids=["42", "160", "switches", "ice-switches", "kin2kin", "qi-sediment", "qi-sediment-160", "all-switches"])
 def test_adjoint_dot_product(gall, kall, lall, options, variant):
     """<ybar, J dx> + 0 = <J^T ybar, dx> + <pbar, dp> between the staged
     tangent-linear and adjoint steps, also on the deepest columns (160 levels,
-    beyond the serial column step's 48) and with the cell-physics switches."""
+    beyond the serial column step's 48), with the cell-physics switches and
+    with cloud ice sedimenting as a fourth tracer."""
     torch, drv, spec, st, x0 = _setup(gall, kall, lall, 77, variant, options)
     g = torch.Generator(device="cuda").manual_seed(5)
     dx = {n: torch.zeros_like(v) for n, v in x0.items()}
@@ -166,13 +172,16 @@ def test_adjoint_forward_checkpoint_bitwise(variant, seed):
     drv.close()
 
 
-@pytest.mark.parametrize("variant,seed", [("standard", 31), ("convective", 32), ("cold", 33)])
-def test_hand_written_adjoint_equals_recorded(variant, seed):
-    """The hand-written adjoints of the cell physics and of the column phase's
-    thermodynamic stage give the input and parameter adjoints of the
-    operation-recording ones (the other column stages are the same in both;
-    their atomic sums make the last bits order-dependent)."""
-    torch, drv, spec, st, x0 = _setup(1024, 42, 1, seed, variant)
+@pytest.mark.parametrize("variant,seed,options", [("standard", 31, None), ("convective", 32, None), ("cold", 33, None),
+                                                  ("cold", 34, QI_SEDIMENT)],
+                         ids=["standard", "convective", "cold", "qi-sediment"])
+def test_hand_written_adjoint_equals_recorded(variant, seed, options):
+    """The hand-written adjoints of the cell physics and of the column
+    phase's stages give the input and parameter adjoints of the
+    operation-recording ones (their atomic sums make the last bits
+    order-dependent); with QI sedimenting, those of the transport's four
+    tracers."""
+    torch, drv, spec, st, x0 = _setup(1024, 42, 1, seed, variant, options)
     g = torch.Generator(device="cuda").manual_seed(seed)
     ybar = {n: torch.zeros_like(v) for n, v in x0.items()}
     for n in WRITE_NAMES:
@@ -510,6 +519,90 @@ def test_kin2kin_gradient_against_finite_differences():
     print(f"\nKIN2KIN gradient vs FD: {checked} components checked, {skipped} next to a switch, "
           f"worst rel err {worst:.2e}")
     assert checked >= 20
+    drv.close()
+
+
+def _fd_ladder(fd, x):
+    """Central differences fd(h) at h = 1e-3 .. 1e-6 of |x|: the value at the
+    smaller step of the two neighbouring steps that agree best, and their
+    relative disagreement."""
+    vals = [fd(r * x) for r in (1e-3, 1e-4, 1e-5, 1e-6)]
+    gaps = [abs(vals[i] - vals[i + 1]) / max(abs(vals[i + 1]), 1e-300) for i in range(3)]
+    i = int(np.argmin(gaps))
+    return vals[i + 1], gaps[i]
+
+
+def test_qi_sediment_gradient_against_finite_differences():
+    """With cloud ice sedimenting ("4WATER", mod_mp_nsw6.cpp:596-599) the
+    transport carries QI as a fourth tracer with the fall speed
+    Vti = -3.29 (rho qi)^0.16 (mod_mp_nsw6.cpp:1073-1075), and its surface
+    flux joins the solid precipitation.  The adjoint gradient of a random
+    weighted sum of the cloud-ice output and of the solid surface
+    precipitation against central differences of the forward step, in the
+    columns with the most ice, for the ice and snow contents, the temperature
+    and the density."""
+    torch, drv, spec, st, x0 = _setup(1024, 42, 1, 2024, "cold", QI_SEDIMENT)
+    gen = torch.Generator(device="cuda").manual_seed(12)
+    wq = torch.randn(x0["rhogq"][:, 3].shape, generator=gen, device="cuda", dtype=torch.float64)
+    wp = torch.randn(x0["precip"][1].shape, generator=gen, device="cuda", dtype=torch.float64)
+    # the two terms of comparable size
+    sq = float(x0["rhogq"][:, 3].abs().mean())
+
+    def forward(x):
+        y = _clone(x)
+        drv.mp_driver_batched(spec.lall, *[y[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+        return y
+
+    y0 = forward(x0)
+    sp = sq / max(float(y0["precip"][1].abs().mean()), 1e-300)
+
+    def ldiff(yp, ym):   # L(yp) - L(ym) term by term
+        return float((wq * (yp["rhogq"][:, 3] - ym["rhogq"][:, 3])).sum() +
+                     sp * (wp * (yp["precip"][1] - ym["precip"][1])).sum())
+
+    bar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    bar["rhogq"][:, 3] = wq
+    bar["precip"][1] = sp * wp
+    drv.adjoint(spec.lall, _clone(x0), bar, dt=spec.dt)
+    ice = x0["rhogq"][0, 3].sum(dim=0).cpu().numpy()
+    cols = np.random.default_rng(6).choice(np.argsort(ice)[-200:], 12, replace=False)
+    fields = (("rhogq", lambda k, g: (0, 3, k, g), 3), ("rhogq", lambda k, g: (0, 4, k, g), 4),
+              ("tem", lambda k, g: (0, k, g), None), ("rhog", lambda k, g: (0, k, g), None))
+    checked = skipped = 0
+    worst = 0.0
+    for g in cols:
+        for name, idx, nq in fields:
+            gcol = bar[name][0, :, g] if nq is None else bar[name][0, nq, :, g]
+            k = int(gcol[1:spec.kall - 1].abs().argmax()) + 1
+            ix = idx(k, int(g))
+            x = float(x0[name][ix])
+            adj = float(bar[name][ix])
+            if x == 0.0 or adj == 0.0:
+                continue
+
+            def fd(hh, name=name, ix=ix):
+                xp, xm = _clone(x0), _clone(x0)
+                xp[name][ix] += hh
+                xm[name][ix] -= hh
+                return ldiff(forward(xp), forward(xm)) / (2 * hh)
+
+            # a ladder of steps (relative 1e-3 .. 1e-6): where the input is
+            # weakly coupled to the loss, the small steps drown in the
+            # rounding of the outputs, the large ones in the curvature; the
+            # estimate is the pair of neighbouring steps that agree best
+            a1, spread = _fd_ladder(fd, abs(x))
+            scale = max(abs(a1), abs(adj), 1e-300)
+            if spread > 1e-7:   # no two steps agree: a switch flips between the FD points
+                skipped += 1
+                continue
+            checked += 1
+            err = abs(adj - a1) / scale
+            worst = max(worst, err)
+            print(f"  d L / d {name}{ix}: adjoint {adj:+.10e}  FD {a1:+.10e}  rel {err:.1e}")
+            assert err <= 1e-6, (name, ix, adj, a1)
+    print(f"\nQI sedimentation gradient vs FD: {checked} components checked, {skipped} next to a switch, "
+          f"worst rel err {worst:.2e}")
+    assert checked >= 24
     drv.close()
 
 

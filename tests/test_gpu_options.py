@@ -96,17 +96,17 @@ def test_gpu_options_reject_unsupported_paths():
         drv.mp_driver(0, *[t[n] for n in ARG_NAMES], dt=dt, ct=0.0)
     assert e.value.code == 5
     drv.set_precision("fp64")
-    # the derivative entry points take every switch but QI sedimentation
-    drv.set_options(qi_sediment=1)
+    # the serial tangent-linear step (adjoint mode "tape": one column per
+    # thread) takes no switch; the staged derivative steps take them all
     kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
     tb = {n: v.reshape(batched_shape(kinds[n], 1, kall, gall)) for n, v in t.items()}   # one region
     bar = {n: torch.zeros_like(v) for n, v in tb.items()}
-    with pytest.raises(NSW6Error) as e:
-        drv.adjoint(1, tb, bar, dt=dt)
-    assert e.value.code == 5
+    drv.set_options(qi_sediment=1)
+    drv.set_adjoint_mode("tape")
     with pytest.raises(NSW6Error) as e:
         drv.tlm(1, tb, bar, dt=dt)
     assert e.value.code == 5
+    drv.set_adjoint_mode("hand")
     with pytest.raises(KeyError):
         drv.set_options(no_such_switch=1)
     with pytest.raises(NSW6Error):
