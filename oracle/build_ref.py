@@ -24,7 +24,9 @@ Variants:
           precip_transport_type, PRCIP_TRN_ECORRECT) can all be flipped; with
           the defaults it computes exactly what strict computes.
 
-When the reference tree is absent (on a machine that only received the
+The reference tree is found at ``--reference-root`` (or the environment
+variable NSW6_REFERENCE_ROOT), else in a checkout named ``reference`` beside
+this repository.  When it is absent (on a machine that only received the
 repository), the copy already in ``oracle/_ref/src`` is used if present.
 Everything written goes to ``oracle/_ref/`` only.
 """
@@ -41,7 +43,8 @@ import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
-REF_ROOT = Path(os.environ.get("NSW6_REFERENCE_ROOT", "/root/reference"))
+# the reference checkout: NSW6_REFERENCE_ROOT, else "reference" beside this repository
+REF_ROOT = Path(os.environ.get("NSW6_REFERENCE_ROOT") or HERE.parent.parent / "reference")
 OUT = HERE / "_ref"
 SRC_COPY = OUT / "src"
 SHIM = HERE / "kokkos_shim"
@@ -178,7 +181,12 @@ def main(argv=None) -> int:
     ap.add_argument("--kall", type=int, required=True)
     ap.add_argument("--variant", choices=sorted(VARIANT_FLAGS), default="strict")
     ap.add_argument("--force", action="store_true")
+    ap.add_argument("--reference-root", type=Path, default=None,
+                    help="the reference checkout (default: NSW6_REFERENCE_ROOT, else ../reference)")
     a = ap.parse_args(argv)
+    if a.reference_root is not None:
+        global REF_ROOT
+        REF_ROOT = a.reference_root
     print(build(a.gall, a.kall, a.variant, force=a.force))
     return 0
 
