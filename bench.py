@@ -492,8 +492,11 @@ def adjoint_ratio(seed: int, variant: str, steps: int, warmup: int) -> dict:
 
 def window_ratio(seed: int, variant: str, nsteps: int = 12, lall: int = 5) -> dict:
     """Config 5: gradient of the window-accumulated surface precipitation over
-    `nsteps` steps with per-step checkpoints (FP64 adjoint), against the plain
-    forward window, with the FP64 and with the mixed-precision forward."""
+    `nsteps` steps with per-step checkpoints, against the plain forward window:
+    the FP64 window (FP64 forward and adjoint), the mixed-precision window
+    (mixed forward; its adjoint linearises the mixed step with FP32 rate
+    adjoints and FP64 budgets, column stages and accumulation) and, beside it,
+    the mixed forward with the FP64 adjoint."""
     import torch
     from nicam_kokkos_microphysics_gb300 import mp_init
     from nicam_kokkos_microphysics_gb300.window import window_forward, window_gradient
@@ -502,18 +505,19 @@ def window_ratio(seed: int, variant: str, nsteps: int = 12, lall: int = 5) -> di
     drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
     x0 = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
     out = {"workload": f"{nsteps}-step window, gall={spec.gall} kall={spec.kall} lall={spec.lall}, dt={spec.dt}, "
-                       f"per-step checkpoints, FP64 adjoint"}
-    for precision in ("fp64", "mixed"):
-        window_gradient(drv, spec.lall, x0, 2, spec.dt, precision=precision)   # warm-up
+                       f"per-step checkpoints, adjoint accumulation in FP64"}
+    for precision, adjoint, key in (("fp64", "fp64", "forward_fp64"), ("mixed", "mixed", "forward_mixed"),
+                                    ("mixed", "fp64", "forward_mixed_adjoint_fp64")):
+        window_gradient(drv, spec.lall, x0, 2, spec.dt, precision=precision, adjoint=adjoint)   # warm-up
         torch.cuda.reset_peak_memory_stats()
-        res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision=precision)
+        res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision=precision, adjoint=adjoint)
         xs = {n: t.clone() for n, t in x0.items()}
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         window_forward(drv, spec.lall, xs, nsteps, spec.dt, precision)
         torch.cuda.synchronize()
         t_plain = time.perf_counter() - t0
-        out[f"forward_{precision}"] = {
+        out[key] = {
             "ratio": res["t_adjoint"] / t_plain, "forward_ms": t_plain * 1e3,
             "forward_with_checkpoints_ms": res["t_forward"] * 1e3, "adjoint_ms": res["t_adjoint"] * 1e3,
             "peak_device_bytes": res["peak_bytes"], "J": res["J"]}

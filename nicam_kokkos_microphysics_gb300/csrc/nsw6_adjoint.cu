@@ -1765,18 +1765,39 @@ __global__ void adj_seed_columns_kernel(StageIO io) {
 // The cell phase's adjoint, hand-written (nsw6_cell_adjoint.cuh): one thread
 // per interior cell; output adjoints from YB, input adjoints added to xb (each
 // cell owns its entries here), the parameters' adjoint reduced per block.
+// R = double: the FP64 cell physics (table-driven exp / log / pow); R = float:
+// the mixed-precision one (FP32 rates with the CUDA FP32 math functions, FP64
+// budgets), as the step's cell kernel evaluates them.
+template <class R>
+struct CellMath;
+template <>
+struct CellMath<double> {
+  using M = FastMath;
+  __device__ static M make(const double* tab) {
+    return FastMath{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  }
+};
+template <>
+struct CellMath<float> {
+  using M = FloatMath;
+  __device__ static M make(const double*) { return FloatMath{}; }
+};
+
 // The cell phase's forward for the adjoint: the outputs Y of every interior
 // cell and the checkpoint of its costly forward values (CELL_CK_SLOTS doubles,
 // slot-major over the cells), both from the hand-written forward.  check: also
 // evaluate nsw6_cell and report a cell whose outputs differ in any bit
 // (status ERR_ADJ_CHECK, iters = the first output field that differs).
 constexpr int ERR_ADJ_CHECK = 7;
-__global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C, ArgPtrs x, double* Y, double* ck,
+template <class R>
+__global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, ConstsT<R> C, ArgPtrs x, double* Y, double* ck,
                                                             int check) {
   __shared__ double tab[FM_TABLE_DOUBLES];
-  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
-  __syncthreads();
-  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  if constexpr (sizeof(R) == sizeof(double)) {
+    for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+    __syncthreads();
+  }
+  const auto fm = CellMath<R>::make(tab);
   const LayS L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
@@ -1813,7 +1834,7 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C,
     for (int f = 0; f < ADJ_Y_FIELDS; ++f) Y[f * NC + i] = y[f];
     if (check) {
       CellOut r;
-      nsw6_cell(C, fm, P.dt, P.rdt, in, r);
+      nsw6_cell<typename CellMath<R>::M, R, double>(C, fm, P.dt, P.rdt, in, r);
       double z[ADJ_Y_FIELDS];
       z[YS_RHOG] = r.rhog;
       z[YS_RHOGE] = r.rhoge;
@@ -1839,13 +1860,15 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, Consts C,
 
 // The cell phase's adjoint, hand-written, from the checkpoint ck of
 // adj_cell_save_kernel.
-__global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, Consts C, ArgPtrs x, ArgPtrs xb, const double* YB,
-                                                          double* pbar, double* ck) {
+template <class R>
+__global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, ConstsT<R> C, ArgPtrs x, ArgPtrs xb,
+                                                          const double* YB, double* pbar, double* ck) {
   __shared__ double tab[FM_TABLE_DOUBLES];
   __shared__ double red[7][128];
-  for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
+  if constexpr (sizeof(R) == sizeof(double))
+    for (int c = threadIdx.x; c < FM_TABLE_DOUBLES; c += blockDim.x) tab[c] = P.fmtab[c];
   __syncthreads();
-  const FastMath fm{tab, tab + FM_EXP_N, tab + 2 * FM_EXP_N, tab + 2 * FM_EXP_N + FM_LOG_N};
+  const auto fm = CellMath<R>::make(tab);
   const LayS L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
@@ -2116,9 +2139,13 @@ size_t adj_stage_bound_ints(int lall, int kall) { return (size_t)lall * 2 * 2 * 
 int adj_stage_tape_cap() { return 512; }
 int adj_stage_slots() { return 152 * 4 * STAGE_THREADS; }
 
+// mixed: the cell phase of the mixed-precision step (FP32 rates).
 cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
-                               double* pbar, double* ck, cudaStream_t stream) {
-  adj_cell_hw_kernel<<<152 * 2, 128, 0, stream>>>(P, C, x, xb, YB, pbar, ck);
+                               double* pbar, double* ck, int mixed, cudaStream_t stream) {
+  if (mixed)
+    adj_cell_hw_kernel<float><<<152 * 2, 128, 0, stream>>>(P, consts_to_float(C), x, xb, YB, pbar, ck);
+  else
+    adj_cell_hw_kernel<double><<<152 * 2, 128, 0, stream>>>(P, C, x, xb, YB, pbar, ck);
   return cudaGetLastError();
 }
 
@@ -2168,8 +2195,11 @@ int adj_y_fields() { return ADJ_Y_FIELDS; }
 size_t adj_cell_ck_doubles(int lall, int kall, int gall) { return (size_t)CELL_CK_SLOTS * lall * (kall - 2) * gall; }
 
 cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, double* ck, int check,
-                                 cudaStream_t stream) {
-  adj_cell_save_kernel<<<152 * 4, 128, 0, stream>>>(P, C, x, Y, ck, check);
+                                 int mixed, cudaStream_t stream) {
+  if (mixed)
+    adj_cell_save_kernel<float><<<152 * 4, 128, 0, stream>>>(P, consts_to_float(C), x, Y, ck, check);
+  else
+    adj_cell_save_kernel<double><<<152 * 4, 128, 0, stream>>>(P, C, x, Y, ck, check);
   return cudaGetLastError();
 }
 

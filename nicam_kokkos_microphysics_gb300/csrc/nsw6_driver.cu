@@ -33,9 +33,9 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
                                      int recorded, cudaStream_t stream);
 cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
-                               double* pbar, double* ck, cudaStream_t stream);
+                               double* pbar, double* ck, int mixed, cudaStream_t stream);
 cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, double* ck, int check,
-                                 cudaStream_t stream);
+                                 int mixed, cudaStream_t stream);
 size_t adj_cell_ck_doubles(int lall, int kall, int gall);
 cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& dx,
                               const double* params, const double* dparams, double* Y, double* work, int* bnd,
@@ -1220,11 +1220,15 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   // the cell phase: hand-written, or recorded (adj_mode 1, and with the scheme
   // switches, whose cell physics the hand-written sweep does not cover)
   const bool recorded = h->adj_mode == 1 || h->opt_active;
+  // with the mixed-precision step selected, the hand-written cell phase
+  // linearises that step's cell physics (FP32 rates, FP64 budgets)
+  const int mixed_cell = h->mixed == 1 ? 1 : 0;
   if (!recorded && !h->d_cellck &&
       cudaMalloc(&h->d_cellck, sizeof(double) * adj_cell_ck_doubles(h->lall_max, h->kall, h->gall)) != cudaSuccess)
     return NSW6_ERR_CUDA;
   if ((recorded ? launch_adj_cellfwd(P, h->C, x, Y, h->stream)
-                : launch_adj_cell_save(P, h->C, x, Y, h->d_cellck, h->adj_mode == 2, h->stream)) != cudaSuccess ||
+                : launch_adj_cell_save(P, h->C, x, Y, h->d_cellck, h->adj_mode == 2, mixed_cell, h->stream)) !=
+          cudaSuccess ||
       launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->adj_mode == 1,
                                h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
@@ -1234,7 +1238,7 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   // as long as the longest cell's record (measured once, then kept; a longer
   // record makes the launch repeat for the cells that did not fit)
   if (!recorded) {
-    if (launch_adj_cell_hw(P, h->C, x, xb, YB, h->d_pbar, h->d_cellck, h->stream) != cudaSuccess)
+    if (launch_adj_cell_hw(P, h->C, x, xb, YB, h->d_pbar, h->d_cellck, mixed_cell, h->stream) != cudaSuccess)
       return NSW6_ERR_CUDA;
   } else {
     for (int attempt = 0; attempt < 3; ++attempt) {

@@ -4,9 +4,12 @@ The forward pass runs ``nsteps`` steps (FP64 or the mixed-precision step) and
 keeps, before every step, a copy of the fields the step changes (the
 checkpoint); the fields it only reads are shared by all steps.  The backward
 pass walks the window in reverse: for step n it recomputes the step from its
-checkpoint inside ``mp_driver_adjoint`` (FP64 derivatives around that state),
-so device memory holds nsteps checkpoints and one step's tapes, not nsteps
-tapes.
+checkpoint inside ``mp_driver_adjoint`` and sweeps it back, so device memory
+holds nsteps checkpoints and one step's work arrays, not nsteps tapes.  With
+the mixed-precision forward the backward linearises the same step: its cell
+physics with FP32 rates and FP32 rate adjoints, FP64 budgets, column stages
+and accumulation of the state and parameter adjoints (``adjoint="fp64"``
+linearises the FP64 step around the mixed trajectory's states instead).
 
 The adjoint convention of mp_driver_adjoint makes the chaining direct: on
 return the adjoint arrays of the fields a step both reads and writes hold the
@@ -46,10 +49,13 @@ def window_forward(drv, lall: int, state: dict, nsteps: int, dt: float, precisio
     return float(J)
 
 
-def window_gradient(drv, lall: int, state0: dict, nsteps: int, dt: float, precision: str = "fp64") -> dict:
+def window_gradient(drv, lall: int, state0: dict, nsteps: int, dt: float, precision: str = "fp64",
+                    adjoint: str | None = None) -> dict:
     """Gradient of J over the window with respect to the initial state and the
-    seven parameters.  Returns {"J", "grad" (adjoints keyed by ARG_NAMES),
-    "dparams" (7), "t_forward", "t_adjoint", "peak_bytes"}."""
+    seven parameters; ``adjoint`` is the precision of the step the backward
+    linearises (default: that of the forward).  Returns {"J", "grad"
+    (adjoints keyed by ARG_NAMES), "dparams" (7), "t_forward", "t_adjoint",
+    "peak_bytes"}."""
     import torch
     kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
     free0 = torch.cuda.mem_get_info()[0]
@@ -72,6 +78,7 @@ def window_gradient(drv, lall: int, state0: dict, nsteps: int, dt: float, precis
            for n in ARG_NAMES}
     dparams = np.zeros(7)
     x = {n: state0[n].clone() for n in ARG_NAMES}
+    drv.set_precision(adjoint or precision)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for n in reversed(range(nsteps)):
@@ -82,5 +89,6 @@ def window_gradient(drv, lall: int, state0: dict, nsteps: int, dt: float, precis
         track()
     torch.cuda.synchronize()
     t_adj = time.perf_counter() - t0
+    drv.set_precision("fp64")
     track()
     return {"J": J, "grad": bar, "dparams": dparams, "t_forward": t_fwd, "t_adjoint": t_adj, "peak_bytes": peak}

@@ -208,6 +208,57 @@ def test_hand_written_adjoint_equals_recorded(variant, seed, options):
     drv.close()
 
 
+@pytest.mark.parametrize("variant,seed", [("standard", 61), ("convective", 62), ("cold", 63)])
+def test_mixed_adjoint_against_fp64_adjoint(variant, seed):
+    """With the mixed-precision step selected, the adjoint's cell phase
+    linearises that step's cell physics (FP32 rates and rate adjoints, FP64
+    budgets; the column stages are FP64 in both): its forward reproduces the
+    mixed-precision cell kernel bit for bit on every cell (adjoint mode
+    "check"), and its input and parameter adjoints agree with those of the
+    FP64 adjoint to the FP32 rounding of the rates.  Output seeds are random,
+    scaled by each output's mean.  The adjoints with respect to tracer
+    contents that are zero are compared apart: there a flux bound of the
+    transport, set by the region's extreme departure distance and so by the
+    last bits of a fall speed, decides whether an empty layer's (zero) source
+    enters a flux integral, which changes that entry's adjoint and nothing
+    else."""
+    torch, drv, spec, st, x0 = _setup(4096, 42, 1, seed, variant)
+    y0 = _clone(x0)
+    drv.mp_driver_batched(spec.lall, *[y0[n] for n in ARG_NAMES], dt=spec.dt, ct=0.0)
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    ybar = {n: torch.zeros_like(v) for n, v in x0.items()}
+    for n in WRITE_NAMES:
+        scale = float(y0[n].abs().mean())
+        if scale > 0.0:
+            ybar[n] = torch.randn(x0[n].shape, generator=g, device="cuda", dtype=torch.float64) / scale
+    b64 = _clone(ybar)
+    p64 = drv.adjoint(spec.lall, _clone(x0), b64, dt=spec.dt)
+    drv.set_precision("mixed")
+    drv.set_adjoint_mode("check")
+    b32 = _clone(ybar)
+    p32 = drv.adjoint(spec.lall, _clone(x0), b32, dt=spec.dt)
+    drv.set_adjoint_mode("hand")
+    drv.set_precision("fp64")
+
+    def rel(a, b):
+        ref = float(torch.linalg.vector_norm(b))
+        return float(torch.linalg.vector_norm(a - b)) / ref if ref > 0 else 0.0
+
+    present = x0["rhogq"] > 0.0
+    errs = {n: rel(b32[n], b64[n]) for n in READ_NAMES if n != "rhogq"}
+    errs["rhogq (present)"] = rel(b32["rhogq"][present], b64["rhogq"][present])
+    empty = rel(b32["rhogq"][~present], b64["rhogq"][~present])
+    perr = np.abs(p32 - p64) / np.maximum(np.abs(p64), 1e-300)
+    print(f"\nmixed vs FP64 adjoint ({variant}), relative 2-norm: "
+          + ", ".join(f"{n} {e:.1e}" for n, e in errs.items())
+          + f"; rhogq (empty) {empty:.1e}; parameters " + ", ".join(f"{v:.1e}" for v in perr))
+    assert max(errs.values()) <= 1e-4, errs
+    # a parameter's adjoint is a sum over every cell with terms of both
+    # signs, so the FP32 rounding of the rates shows more in it
+    assert np.all(perr <= 1e-3), perr
+    drv.close()
+
+
 def _loss_terms(torch, spec):
     gz, gzh = vertical_grid(spec.kall)
     dgz = torch.tensor(np.diff(gzh, append=gzh[-1] + (gzh[-1] - gzh[-2])), dtype=torch.float64, device="cuda")
