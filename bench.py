@@ -502,14 +502,22 @@ def window_ratio(seed: int, variant: str, nsteps: int = 12, lall: int = 5) -> di
     from nicam_kokkos_microphysics_gb300.window import window_forward, window_gradient
     spec = StateSpec(gall=16900, kall=42, lall=lall, seed=seed, variant=variant)
     st = make_state(spec, out_fill=0.0)
-    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
     x0 = {n: torch.from_numpy(st[n]).cuda() for n in ARG_NAMES}
     out = {"workload": f"{nsteps}-step window, gall={spec.gall} kall={spec.kall} lall={spec.lall}, dt={spec.dt}, "
-                       f"per-step checkpoints, adjoint accumulation in FP64"}
+                       f"per-step checkpoints, adjoint accumulation in FP64",
+           "peak_device_bytes": "device memory in use at the window's peak beyond that before the handle was "
+                                "created: the handle's workspaces, the checkpoints and the adjoint arrays"}
     for precision, adjoint, key in (("fp64", "fp64", "forward_fp64"), ("mixed", "mixed", "forward_mixed"),
                                     ("mixed", "fp64", "forward_mixed_adjoint_fp64")):
-        window_gradient(drv, spec.lall, x0, 2, spec.dt, precision=precision, adjoint=adjoint)   # warm-up
-        torch.cuda.reset_peak_memory_stats()
+        # a handle per case, so that each peak includes the workspaces its calls allocate
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        free0 = torch.cuda.mem_get_info()[0]
+        drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+        res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision=precision, adjoint=adjoint,
+                              free0=free0)
+        peak = res["peak_bytes"]
+        torch.cuda.empty_cache()
         res = window_gradient(drv, spec.lall, x0, nsteps, spec.dt, precision=precision, adjoint=adjoint)
         xs = {n: t.clone() for n, t in x0.items()}
         torch.cuda.synchronize()
@@ -520,8 +528,8 @@ def window_ratio(seed: int, variant: str, nsteps: int = 12, lall: int = 5) -> di
         out[key] = {
             "ratio": res["t_adjoint"] / t_plain, "forward_ms": t_plain * 1e3,
             "forward_with_checkpoints_ms": res["t_forward"] * 1e3, "adjoint_ms": res["t_adjoint"] * 1e3,
-            "peak_device_bytes": res["peak_bytes"], "J": res["J"]}
-    drv.close()
+            "peak_device_bytes": peak, "J": res["J"]}
+        drv.close()
     return out
 
 
@@ -543,11 +551,21 @@ def main(argv=None) -> int:
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
                     help="precision of the headline step: plain FP64, or FP32 process rates with FP64 budgets, "
                          "flux sums and Newton")
+    ap.add_argument("--only", choices=["adjoint", "window"], default=None,
+                    help="run one section alone and print its JSON (for profiling): the adjoint of one FP64 step "
+                         "on 4096 x 42, or the checkpointed window (--window-steps steps on --lall regions)")
+    ap.add_argument("--window-steps", type=int, default=12)
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference_arm(args)
+    if args.only == "adjoint":
+        print(json.dumps(adjoint_ratio(args.seed, args.variant, args.steps, args.warmup)), flush=True)
+        return 0
+    if args.only == "window":
+        print(json.dumps(window_ratio(args.seed, args.variant, args.window_steps, args.lall)), flush=True)
+        return 0
 
     import torch
     rank, world, local = env_rank()

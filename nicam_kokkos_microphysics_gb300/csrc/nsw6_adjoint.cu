@@ -1816,7 +1816,7 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, ConstsT<R
     CellOut o;
     CellBar ob{};
     CellInBar ib{};
-    nsw6_cell_adjoint<CA_SAVE>(C, fm, P.dt, P.rdt, in, ob, ib, nullptr, CellCk{ck + c, (size_t)ncell}, &o);
+    nsw6_cell_adjoint<CA_SAVE>(C, fm, P.dt, P.rdt, in, ob, ib, nullptr, CellCk{ck, (size_t)ncell, (size_t)c}, &o);
     double y[ADJ_Y_FIELDS];
     y[YS_RHOG] = o.rhog;
     y[YS_RHOGE] = o.rhoge;
@@ -1900,7 +1900,7 @@ __global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, ConstsT<R> 
     ob.rctop = k == P.kmax ? YB[YS_RCTOP * NC + i] : 0.0;
     ob.tctop = k == P.kmax ? YB[YS_TCTOP * NC + i] : 0.0;
     CellInBar ib{};
-    nsw6_cell_adjoint<CA_LOAD>(C, fm, P.dt, P.rdt, in, ob, ib, pacc, CellCk{ck + c, (size_t)ncell});
+    nsw6_cell_adjoint<CA_LOAD>(C, fm, P.dt, P.rdt, in, ob, ib, pacc, CellCk{ck, (size_t)ncell, (size_t)c});
     xb.a[A_rhog][i] += ib.rhog;
     xb.a[A_tem][i] += ib.tem;
     xb.a[A_gsgam2][i] += ib.gsgam2;

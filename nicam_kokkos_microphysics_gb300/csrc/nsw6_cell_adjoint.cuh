@@ -69,30 +69,40 @@ __device__ __forceinline__ float bsqrt(float s) { return s > 0.0f ? 0.5f / s : 0
 //   CA_SAVE  computes them and stores them to the cell's checkpoint, writes
 //            the cell outputs (those of nsw6_cell) and returns;
 //   CA_LOAD  reads them from the checkpoint instead, then runs the reverse.
-// The stored values are the computed ones (an FP32 value is stored exactly in
-// its double slot), so every branch takes the same way in all three.
+// The stored values are the computed ones, so every branch takes the same way
+// in all three.
 enum CellAdjMode { CA_FULL = 0, CA_SAVE = 1, CA_LOAD = 2 };
 constexpr int CELL_CK_SLOTS = 49;
-// Slot s of this cell's checkpoint at p[s * stride].
+// The checkpoint of cell c: slot s at element c + s * stride of the buffer p
+// viewed as an array of the rate precision R (the buffer holds CELL_CK_SLOTS
+// doubles per cell; the mixed-precision step's FP32 slots use its first half).
 struct CellCk {
   double* p;
-  size_t stride;
+  size_t stride, c;
 };
-template <int MODE, class T>
-__device__ __forceinline__ T ck_keep(const CellCk& ck, int s, T v) {
-  if constexpr (MODE == CA_SAVE) ck.p[(size_t)s * ck.stride] = (double)v;
-  return v;
+// The value f() of slot s (of type T; not evaluated under CA_LOAD).  The few
+// FP64 slots of the mixed-precision step (1 / rhog, rhog / gsgam2, the
+// temperature) are recomputed in all three modes instead.
+template <int MODE, class R, class T, class F>
+__device__ __forceinline__ T ck_val(const CellCk& ck, int s, const F& f) {
+  if constexpr (sizeof(T) != sizeof(R)) {
+    return f();
+  } else {
+    T* p = reinterpret_cast<T*>(ck.p) + ck.c + (size_t)s * ck.stride;
+    if constexpr (MODE == CA_LOAD) return *p;
+    const T v = f();
+    if constexpr (MODE == CA_SAVE) *p = v;
+    return v;
+  }
 }
-// The value of expr (of type T; not evaluated under CA_LOAD) at slot s.
-#define NSW6_CK(T, s, expr) \
-  ((MODE == CA_LOAD) ? (T)ck.p[(size_t)(s) * ck.stride] : ck_keep<MODE, T>(ck, (s), (expr)))
+#define NSW6_CK(T, s, expr) ck_val<MODE, R, T>(ck, (s), [&]() -> T { return (expr); })
 
 // R = double with FastMath (the FP64 step) or R = float with FloatMath (the
 // mixed-precision step).
 template <int MODE = CA_FULL, class R = double, class M = FastMath>
 __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& mth, double dt, double rdt,
                                                   const CellIn& in, const CellBar& ob, CellInBar& ib, double* pb,
-                                                  CellCk ck = {nullptr, 0}, CellOut* out = nullptr) {
+                                                  CellCk ck = {nullptr, 0, 0}, CellOut* out = nullptr) {
   using D = double;
   constexpr bool kMixed = sizeof(R) == sizeof(float);
   const R Z = R(0.0), ONE = R(1.0);

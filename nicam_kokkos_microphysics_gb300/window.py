@@ -50,15 +50,17 @@ def window_forward(drv, lall: int, state: dict, nsteps: int, dt: float, precisio
 
 
 def window_gradient(drv, lall: int, state0: dict, nsteps: int, dt: float, precision: str = "fp64",
-                    adjoint: str | None = None) -> dict:
+                    adjoint: str | None = None, free0: int | None = None) -> dict:
     """Gradient of J over the window with respect to the initial state and the
     seven parameters; ``adjoint`` is the precision of the step the backward
     linearises (default: that of the forward).  Returns {"J", "grad"
     (adjoints keyed by ARG_NAMES), "dparams" (7), "t_forward", "t_adjoint",
-    "peak_bytes"}."""
+    "peak_bytes" (the most device memory in use beyond ``free0``, the free
+    device memory to measure from; default: that at the call)}."""
     import torch
     kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
-    free0 = torch.cuda.mem_get_info()[0]
+    if free0 is None:
+        free0 = torch.cuda.mem_get_info()[0]
     peak = 0
 
     def track():

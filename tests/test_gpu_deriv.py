@@ -752,10 +752,12 @@ def test_window_gradient_against_finite_differences():
 
 def test_window_gradient_mixed_forward_against_fp64_forward():
     """The configured 12-step window runs the mixed-precision forward with FP64
-    adjoint accumulation.  Its gradient (the adjoint around the mixed
-    forward's checkpoints) against the same window with the FP64 forward, on
-    a 16900-column region, reported per parameter and for the gradient fields
-    of the initial temperature and vapour.  The two are gradients of two
+    adjoint accumulation.  Its gradient (the adjoint of the mixed step around
+    the mixed forward's checkpoints: FP32 rate adjoints, FP64 budgets, column
+    stages and accumulation), and the same window's with the FP64 adjoint
+    around the same checkpoints, against the window with the FP64 forward,
+    on a 16900-column region, reported per parameter and for the gradient
+    fields of the initial temperature and vapour.  They are gradients of
     trajectories that part by the mixed step's errors (about 1e-6): where a
     cell of one trajectory sits on the other side of a limiter or threshold
     switch than in the other, its derivative differs outright, so the
@@ -765,25 +767,26 @@ def test_window_gradient_mixed_forward_against_fp64_forward():
     torch, drv, spec, st, x0 = _setup(16900, 42, 1, 1005, "standard")
     from nicam_kokkos_microphysics_gb300.window import window_gradient
     r64 = window_gradient(drv, 1, x0, 12, spec.dt, precision="fp64")
-    rmx = window_gradient(drv, 1, x0, 12, spec.dt, precision="mixed")
-    print(f"\n12-step window, J fp64 {r64['J']:.10e} mixed {rmx['J']:.10e} "
-          f"(rel {abs(rmx['J'] - r64['J']) / abs(r64['J']):.2e})")
-    worst = {}
-    for i, pn in enumerate(PARAMS):
-        a, b = rmx["dparams"][i], r64["dparams"][i]
-        rel = abs(a - b) / max(abs(b), 1e-300)
-        worst[pn] = rel
-        print(f"  dJ/d{pn:10s}: fp64 forward {b:+.10e}  mixed forward {a:+.10e}  rel {rel:.2e}")
-    for name, sl in (("tem", (slice(None),)), ("q[QV]", (slice(None), 0))):
-        f = "tem" if name == "tem" else "q"
-        a, b = rmx["grad"][f][sl], r64["grad"][f][sl]
-        l2 = float((a - b).norm() / b.norm())
-        mx = float((a - b).abs().max() / b.abs().max())
-        worst[name] = l2
-        print(f"  dJ/d{name} field: relative L2 difference {l2:.2e}, field-normalised max {mx:.2e}")
-    for pn in ("Cr", "Cs", "Cg", "ice_nuc", "kk_aut"):
-        assert worst[pn] <= 1e-3, (pn, worst[pn])
-    for pn in ("beta_saut", "qicrt_saut"):
-        assert worst[pn] <= 0.1, (pn, worst[pn])
-    assert worst["tem"] <= 1e-2 and worst["q[QV]"] <= 1e-2, worst
+    for adjoint in ("mixed", "fp64"):
+        rmx = window_gradient(drv, 1, x0, 12, spec.dt, precision="mixed", adjoint=adjoint)
+        print(f"\n12-step window, {adjoint} adjoint: J fp64 {r64['J']:.10e} mixed {rmx['J']:.10e} "
+              f"(rel {abs(rmx['J'] - r64['J']) / abs(r64['J']):.2e})")
+        worst = {}
+        for i, pn in enumerate(PARAMS):
+            a, b = rmx["dparams"][i], r64["dparams"][i]
+            rel = abs(a - b) / max(abs(b), 1e-300)
+            worst[pn] = rel
+            print(f"  dJ/d{pn:10s}: fp64 forward {b:+.10e}  mixed forward {a:+.10e}  rel {rel:.2e}")
+        for name, sl in (("tem", (slice(None),)), ("q[QV]", (slice(None), 0))):
+            f = "tem" if name == "tem" else "q"
+            a, b = rmx["grad"][f][sl], r64["grad"][f][sl]
+            l2 = float((a - b).norm() / b.norm())
+            mx = float((a - b).abs().max() / b.abs().max())
+            worst[name] = l2
+            print(f"  dJ/d{name} field: relative L2 difference {l2:.2e}, field-normalised max {mx:.2e}")
+        for pn in ("Cr", "Cs", "Cg", "ice_nuc", "kk_aut"):
+            assert worst[pn] <= 1e-3, (adjoint, pn, worst[pn])
+        for pn in ("beta_saut", "qicrt_saut"):
+            assert worst[pn] <= 0.1, (adjoint, pn, worst[pn])
+        assert worst["tem"] <= 1e-2 and worst["q[QV]"] <= 1e-2, (adjoint, worst)
     drv.close()
