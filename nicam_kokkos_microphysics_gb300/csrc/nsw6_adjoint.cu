@@ -216,8 +216,12 @@ __device__ __forceinline__ T xc(const In<T>& in, int a) {
 
 // ------------------------------------------------------------------ stages
 // S1: departure distances, kinetic energies and flux sources of cell (l, k, g).
-template <class T, class O>
-__device__ void stage1(const In<T>& in, const double* gr, int k, const O& out) {
+// MIX (T = double): the departure distances of the mixed-precision step, in
+// FP32 from the FP32 reciprocal rows grf (rdgz, rdgzh, rdzs, rdzsh) as its
+// cell kernel forms them, so that the flux bounds and departure cells are the
+// mixed step's.
+template <class T, bool MIX = false, class O>
+__device__ void stage1(const In<T>& in, const double* gr, int k, const O& out, const float* grf = nullptr) {
   const Problem& P = in.io.P;
   const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
   const double* rdgz = gr + GF_RDGZ * K;
@@ -235,10 +239,31 @@ __device__ void stage1(const In<T>& in, const double* gr, int k, const O& out) {
       const int kk = k - 3 + j;
       vt[t][j] = (interior && kk >= kmin && kk <= kmax) ? in.y(sed_tracer(t, ntr).vt, kk) : T(0.0);
     }
+  float vtf[MIX ? MAX_TR : 1][5];
+  if constexpr (MIX)
+    for (int t = 0; t < ntr; ++t)
+      for (int j = 0; j < 5; ++j) vtf[t][j] = float(vt[t][j]);
   for (int r = 0; r < 2 * ntr; ++r) {
     const int t = r % ntr, half = r / ntr;
     const int mkmin = half ? kmin + 1 : kmin;
     T z = T(0.0);
+    if constexpr (MIX) {
+      if (k >= mkmin && k <= kmax) {
+        auto col = [&](int j) { return vtf[t][j - k + 3]; };
+        const float dtf = float(P.dt), hdt2f = float(P.hdt2), sdt3f = float(P.sdt3);
+        float zf;
+        if (!half) {
+          auto wp = [&](int j) { return col(j); };
+          zf = vadv_zdis<float>(wp, grf, grf + 2 * K, k, mkmin, kmax, dtf, hdt2f, sdt3f);
+        } else {
+          auto wp = [&](int j) { return (j >= kmin + 1 && j <= kmax - 1) ? 0.5f * (col(j) + col(j - 1)) : 0.0f; };
+          zf = vadv_zdis<float>(wp, grf + K, grf + 3 * K, k, mkmin, kmax, dtf, hdt2f, sdt3f);
+        }
+        z = T(double(zf));
+      }
+      out(W_ZDIS + r, z);
+      continue;
+    }
     if (k >= mkmin && k <= kmax) {
       auto col = [&](int j) { return vt[t][j - k + 3]; };
       if (!half) {
@@ -726,10 +751,17 @@ __global__ void adj_bounds_kernel(Problem P, int* bnd) {
 // departure distances over the region (vadv1d_prep, mod_vadv1d.cpp:316-353)
 // reduce within the block: one 64-bit atomic per block and row, on
 // order-preserving keys (exact, independent of the order of the atomics).
+template <bool MIX>
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_fwd_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
+  __shared__ float grf[MIX ? 4 * MAX_KALL : 1];   // MIX: rdgz, rdgzh, rdzs, rdzsh in FP32
   __shared__ unsigned long long red[2][2 * MAX_TR][STAGE_THREADS / 32];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
+  if constexpr (MIX) {
+    const int rows[4] = {GF_RDGZ, GF_RDGZH, GF_RDZS, GF_RDZSH};
+    for (int c = threadIdx.x; c < 4 * io.P.kall; c += blockDim.x)
+      grf[c] = (float)io.P.grid[rows[c / io.P.kall] * io.P.kall + c % io.P.kall];
+  }
   __syncthreads();
   const int g = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y, l = blockIdx.z;
   const bool valid = g < io.L.G;
@@ -738,10 +770,13 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_fwd_kernel(StageIO io) {
   if (valid) {
     const size_t c = io.L.f(l, k, g);
     const In<double> in{io, l, g};
-    stage1<double>(in, grid, k, [&](int f, double v) {
-      io.W[f * io.NC + c] = v;
-      if (f < nrow) z[f] = v;
-    });
+    stage1<double, MIX>(
+        in, grid, k,
+        [&](int f, double v) {
+          io.W[f * io.NC + c] = v;
+          if (f < nrow) z[f] = v;
+        },
+        grf);
   }
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   for (int r = 0; r < nrow; ++r) {
@@ -1227,26 +1262,26 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
 
 // Adjoint of vadv_zdis_wh at level k: the adjoints of wh(k-1), wh(k), wh(k+1)
 // (bw[0..2]) from that of zdis.  At k == mkmin only wh(k) and wh(k+1) enter.
-__device__ __forceinline__ void zdis_wh_bar(double wm, double w0, double wpp, const double* rdz, const double* rdzs,
-                                            int k, int mkmin, double dt, double hdt2, double sdt3, double bz,
-                                            double* bw) {
+template <class R>
+__device__ __forceinline__ void zdis_wh_bar(R wm, R w0, R wpp, const R* rdz, const R* rdzs, int k, int mkmin, R dt,
+                                            R hdt2, R sdt3, R bz, R* bw) {
   if (k == mkmin) {
     // z = (-hdt2 w0) ((wpp - w0) rdz) + dt w0
-    const double a = -hdt2 * w0, b = (wpp - w0) * rdz[mkmin];
-    bw[0] = 0.0;
+    const R a = -hdt2 * w0, b = (wpp - w0) * rdz[mkmin];
+    bw[0] = R(0.0);
     bw[1] = bz * (-hdt2 * b - a * rdz[mkmin] + dt);
     bw[2] = bz * a * rdz[mkmin];
     return;
   }
-  const double rs = rdzs[k];
-  const double r = (wpp - wm) * rs;
-  const double c = 2.0 * rs * ((wpp - w0) * rdz[k] - (w0 - wm) * rdz[k - 1]);
+  const R rs = rdzs[k];
+  const R r = (wpp - wm) * rs;
+  const R c = R(2.0) * rs * ((wpp - w0) * rdz[k] - (w0 - wm) * rdz[k - 1]);
   // z = (-hdt2 w0) r + dt w0 + (sdt3 w0) (w0 c + r r)
-  const double b_r = bz * (-hdt2 * w0 + sdt3 * w0 * 2.0 * r);
-  const double b_c = bz * sdt3 * w0 * w0;
-  double b_w0 = bz * (-hdt2 * r + dt + sdt3 * (2.0 * w0 * c + r * r));
-  const double b_d = b_c * 2.0 * rs;
-  b_w0 = fma(-b_d, (rdz[k] + rdz[k - 1]), b_w0);
+  const R b_r = bz * (-hdt2 * w0 + sdt3 * w0 * R(2.0) * r);
+  const R b_c = bz * sdt3 * w0 * w0;
+  R b_w0 = bz * (-hdt2 * r + dt + sdt3 * (R(2.0) * w0 * c + r * r));
+  const R b_d = b_c * R(2.0) * rs;
+  b_w0 = fmaR(-b_d, (rdz[k] + rdz[k - 1]), b_w0);
   bw[0] = -b_r * rs + b_d * rdz[k - 1];
   bw[1] = b_w0;
   bw[2] = b_r * rs + b_d * rdz[k];
@@ -1258,9 +1293,18 @@ __device__ __forceinline__ void zdis_wh_bar(double wm, double w0, double wpp, co
 // at this cell that no other thread of the launch touches are added in place;
 // those at level k - 1, of the fall speeds at k - 3 .. k + 1 and of the
 // column's unit vectors go by atomics.
+// MIX: the departure distances are the mixed step's (FP32, stage1): their
+// adjoint coefficients in FP32 at the FP32 values, times the FP64 adjoint.
+template <bool MIX>
 __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
+  __shared__ float grf[MIX ? 4 * MAX_KALL : 1];   // MIX: rdgz, rdgzh, rdzs, rdzsh in FP32
   for (int i = threadIdx.x; i < GF_COUNT * io.P.kall; i += blockDim.x) grid[i] = io.P.grid[i];
+  if constexpr (MIX) {
+    const int rows[4] = {GF_RDGZ, GF_RDGZH, GF_RDZS, GF_RDZSH};
+    for (int c = threadIdx.x; c < 4 * io.P.kall; c += blockDim.x)
+      grf[c] = (float)io.P.grid[rows[c / io.P.kall] * io.P.kall + c % io.P.kall];
+  }
   __syncthreads();
   const Problem& P = io.P;
   const int K = P.kall, kmin = P.kmin, kmax = P.kmax;
@@ -1304,15 +1348,30 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
       const int t = r % ntr, half = r / ntr;
       const int mkmin = half ? kmin + 1 : kmin;
       if (k < mkmin) continue;
-      auto col = [&](int j) { return vt[t][j - k + 3]; };
-      auto wp = [&](int j) {
-        if (!half) return col(j);
-        return (j >= kmin + 1 && j <= kmax - 1) ? 0.5 * (col(j) + col(j - 1)) : 0.0;
-      };
-      auto wh = [&](int j) { return vadv_wh<double>(wp, j, mkmin, kmax); };
-      const double wm = k > mkmin ? wh(k - 1) : 0.0;
       double bw[3];
-      zdis_wh_bar(wm, wh(k), wh(k + 1), half ? rdgzh : rdgz, half ? rdzsh : rdzs, k, mkmin, dt, hdt2, sdt3, bz, bw);
+      if constexpr (MIX) {
+        auto col = [&](int j) { return float(vt[t][j - k + 3]); };
+        auto wp = [&](int j) {
+          if (!half) return col(j);
+          return (j >= kmin + 1 && j <= kmax - 1) ? 0.5f * (col(j) + col(j - 1)) : 0.0f;
+        };
+        auto wh = [&](int j) { return vadv_wh<float>(wp, j, mkmin, kmax); };
+        const float wm = k > mkmin ? wh(k - 1) : 0.0f;
+        float cw[3];
+        zdis_wh_bar<float>(wm, wh(k), wh(k + 1), grf + (half ? K : 0), grf + (half ? 3 * K : 2 * K), k, mkmin,
+                           float(dt), float(hdt2), float(sdt3), 1.0f, cw);
+        for (int i = 0; i < 3; ++i) bw[i] = bz * double(cw[i]);
+      } else {
+        auto col = [&](int j) { return vt[t][j - k + 3]; };
+        auto wp = [&](int j) {
+          if (!half) return col(j);
+          return (j >= kmin + 1 && j <= kmax - 1) ? 0.5 * (col(j) + col(j - 1)) : 0.0;
+        };
+        auto wh = [&](int j) { return vadv_wh<double>(wp, j, mkmin, kmax); };
+        const double wm = k > mkmin ? wh(k - 1) : 0.0;
+        zdis_wh_bar<double>(wm, wh(k), wh(k + 1), half ? rdgzh : rdgz, half ? rdzsh : rdzs, k, mkmin, dt, hdt2,
+                            sdt3, bz, bw);
+      }
       auto add_wp = [&](int j, double v) {
         if (!half) {
           bvt[t][j - k + 3] += v;
@@ -2178,7 +2237,7 @@ cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& 
     tlm_cell_kernel<true><<<152 * 4, 128, 0, stream>>>(io, C, params, dparams);
   else
     tlm_cell_kernel<false><<<152 * 4, 128, 0, stream>>>(io, C, params, dparams);
-  adj_s1_fwd_kernel<<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(
+  adj_s1_fwd_kernel<false><<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(
       io);
   adj_bounds_kernel<<<(int)((nkey + 127) / 128), 128, 0, stream>>>(P, bnd);
   adj_s2_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
@@ -2208,9 +2267,12 @@ cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtr
 // distances in P.zmax / P.zmin, and from them the flux bounds), then the
 // adjoints S4..S1 into YB (zeroed here first) and xb.  work: adj_stage_work_doubles doubles; bnd: adj_stage_bound_ints ints;
 // tm: adj_stage_slots() slots of adj_stage_tape_cap() entries.
+// mixed (not with recorded): the departure distances of the mixed-precision
+// step (FP32), whose bounds and departure cells the stages then hold.
 cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
-                                     int recorded, cudaStream_t stream) {
+                                     int recorded, int mixed, cudaStream_t stream) {
+  if (recorded && mixed) return cudaErrorInvalidValue;
   StageIO io;
   io.P = P;
   io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld};
@@ -2231,8 +2293,11 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   const size_t nkey = (size_t)P.lall * 2 * P.ntr * P.kall;
   if ((e = cudaMemsetAsync(P.zmax, 0x00, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
   if ((e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream)) != cudaSuccess) return e;
-  adj_s1_fwd_kernel<<<dim3((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall), STAGE_THREADS, 0, stream>>>(
-      io);
+  const dim3 s1grid((P.gall + STAGE_THREADS - 1) / STAGE_THREADS, P.kall, P.lall);
+  if (mixed)
+    adj_s1_fwd_kernel<true><<<s1grid, STAGE_THREADS, 0, stream>>>(io);
+  else
+    adj_s1_fwd_kernel<false><<<s1grid, STAGE_THREADS, 0, stream>>>(io);
   adj_bounds_kernel<<<(int)((nkey + 127) / 128), 128, 0, stream>>>(P, bnd);
   adj_s2_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   adj_s3_fwd_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
@@ -2251,8 +2316,10 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
     adj_s2_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   if (recorded)
     adj_s1_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
+  else if (mixed)
+    adj_s1_hw_kernel<true><<<152 * 4, STAGE_THREADS, 0, stream>>>(io);
   else
-    adj_s1_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io);
+    adj_s1_hw_kernel<false><<<152 * 4, STAGE_THREADS, 0, stream>>>(io);
   return cudaGetLastError();
 }
 

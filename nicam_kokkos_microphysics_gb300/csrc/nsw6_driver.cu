@@ -31,7 +31,7 @@ cudaError_t launch_adj_cell(const Problem& P, const Consts& C, const ArgPtrs& x,
                             cudaStream_t stream);
 cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb,
                                      const double* Y, double* YB, int ny, double* work, int* bnd, const TapeMem& tm,
-                                     int recorded, cudaStream_t stream);
+                                     int recorded, int mixed, cudaStream_t stream);
 cudaError_t launch_adj_cell_hw(const Problem& P, const Consts& C, const ArgPtrs& x, const ArgPtrs& xb, const double* YB,
                                double* pbar, double* ck, int mixed, cudaStream_t stream);
 cudaError_t launch_adj_cell_save(const Problem& P, const Consts& C, const ArgPtrs& x, double* Y, double* ck, int check,
@@ -1220,9 +1220,10 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
   // the cell phase: hand-written, or recorded (adj_mode 1, and with the scheme
   // switches, whose cell physics the hand-written sweep does not cover)
   const bool recorded = h->adj_mode == 1 || h->opt_active;
-  // with the mixed-precision step selected, the hand-written cell phase
-  // linearises that step's cell physics (FP32 rates, FP64 budgets)
-  const int mixed_cell = h->mixed == 1 ? 1 : 0;
+  // with the mixed-precision step selected, the hand-written adjoint
+  // linearises that step: its cell physics (FP32 rates, FP64 budgets) and its
+  // FP32 departure distances
+  const int mixed_cell = (h->mixed == 1 && !recorded) ? 1 : 0;
   if (!recorded && !h->d_cellck &&
       cudaMalloc(&h->d_cellck, sizeof(double) * adj_cell_ck_doubles(h->lall_max, h->kall, h->gall)) != cudaSuccess)
     return NSW6_ERR_CUDA;
@@ -1230,7 +1231,7 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
                 : launch_adj_cell_save(P, h->C, x, Y, h->d_cellck, h->adj_mode == 2, mixed_cell, h->stream)) !=
           cudaSuccess ||
       launch_adj_column_staged(P, h->C, x, xb, Y, YB, adj_nfields(), h->d_swork, h->d_sbnd, h->stape, h->adj_mode == 1,
-                               h->stream) != cudaSuccess ||
+                               mixed_cell, h->stream) != cudaSuccess ||
       cudaMemsetAsync(h->d_pbar, 0, sizeof(double) * 8, h->stream) != cudaSuccess ||
       (recorded && cudaMemsetAsync(h->d_done, 0, sizeof(int) * (size_t)ncell, h->stream) != cudaSuccess))
     return NSW6_ERR_CUDA;
