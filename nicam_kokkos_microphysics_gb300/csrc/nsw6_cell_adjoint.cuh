@@ -75,27 +75,29 @@ enum CellAdjMode { CA_FULL = 0, CA_SAVE = 1, CA_LOAD = 2 };
 constexpr int CELL_CK_SLOTS = 49;
 // The checkpoint of cell c: slot s at element c + s * stride of the buffer p
 // viewed as an array of the rate precision R (the buffer holds CELL_CK_SLOTS
-// doubles per cell; the mixed-precision step's FP32 slots use its first half).
+// doubles per cell).  The mixed-precision step's FP32 slots use its first
+// half; its three FP64 slots (0: 1 / rhog, 1: rhog / gsgam2, 48: the
+// temperature) sit as doubles at rows CK_MIXED_D, + 1, + 2 of the second.
 struct CellCk {
   double* p;
   size_t stride, c;
 };
-// The value f() of slot s (of type T; not evaluated under CA_LOAD).  The few
-// FP64 slots of the mixed-precision step (1 / rhog, rhog / gsgam2, the
-// temperature) are recomputed in all three modes instead.
-template <int MODE, class R, class T, class F>
-__device__ __forceinline__ T ck_val(const CellCk& ck, int s, const F& f) {
-  if constexpr (sizeof(T) != sizeof(R)) {
-    return f();
-  } else {
-    T* p = reinterpret_cast<T*>(ck.p) + ck.c + (size_t)s * ck.stride;
-    if constexpr (MODE == CA_LOAD) return *p;
-    const T v = f();
-    if constexpr (MODE == CA_SAVE) *p = v;
-    return v;
-  }
+constexpr int CK_MIXED_D = (CELL_CK_SLOTS + 1) / 2;
+// Where slot s (of type T) of the cell lives.
+template <class R, class T>
+__device__ __forceinline__ T* ck_ptr(const CellCk& ck, int s) {
+  if constexpr (sizeof(T) != sizeof(R))
+    return reinterpret_cast<T*>(ck.p) + ck.c + (size_t)(CK_MIXED_D + (s == 0 ? 0 : s == 1 ? 1 : 2)) * ck.stride;
+  else
+    return reinterpret_cast<T*>(ck.p) + ck.c + (size_t)s * ck.stride;
 }
-#define NSW6_CK(T, s, expr) ck_val<MODE, R, T>(ck, (s), [&]() -> T { return (expr); })
+template <int MODE, class R, class T>
+__device__ __forceinline__ T ck_keep(const CellCk& ck, int s, T v) {
+  if constexpr (MODE == CA_SAVE) *ck_ptr<R, T>(ck, s) = v;
+  return v;
+}
+// The value of expr (of type T; not evaluated under CA_LOAD) at slot s.
+#define NSW6_CK(T, s, expr) ((MODE == CA_LOAD) ? *ck_ptr<R, T>(ck, (s)) : ck_keep<MODE, R, T>(ck, (s), (T)(expr)))
 
 // R = double with FastMath (the FP64 step) or R = float with FloatMath (the
 // mixed-precision step).
@@ -705,10 +707,16 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // so that large output adjoints cannot overflow FP32.
   D sc = 1.0, isc = 1.0;
   if constexpr (kMixed) {
-    D m = fmax(fmax(fabs(ob.Vtr), fabs(ob.Vts)), fmax(fabs(ob.Vtg), fmax(fabs(ob.rceff), fabs(ob.rceff_cld))));
+    // the largest biased exponent among them, on the integer pipe
+    auto ebits = [](double v) { return (unsigned long long)__double_as_longlong(v) & 0x7ff0000000000000ull; };
+    unsigned long long me = ebits(ob.Vtr);
+    me = max(me, ebits(ob.Vts));
+    me = max(me, ebits(ob.Vtg));
+    me = max(me, ebits(ob.rceff));
+    me = max(me, ebits(ob.rceff_cld));
 #pragma unroll
-    for (int n = 0; n < 6; ++n) m = fmax(m, fabs(b_qtD[n]));
-    const int ex = (int)((__double_as_longlong(m) >> 52) & 0x7ff);   // biased exponent of m
+    for (int n = 0; n < 6; ++n) me = max(me, ebits(b_qtD[n]));
+    const int ex = (int)(me >> 52);   // biased exponent of the largest
     if (ex >= 1 && ex <= 2045) {
       sc = __longlong_as_double((long long)(2046 - ex) << 52);   // 2^(1023 - ex)
       isc = __longlong_as_double((long long)ex << 52);           // 2^(ex - 1023)
@@ -1412,7 +1420,23 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   }
   ib.tem += b_tempD;
   ib.q0 += b_qn[0];
-  // parameters (their adjoints scaled back as above)
+  // parameters (their adjoints scaled back as above); in the mixed step each
+  // cell's contribution is formed in FP32 and accumulated in FP64
+  if constexpr (kMixed) {
+    const R p2 = (b_K_vtr * C.K_vtr + b_K_raci * C.K_raci + b_K_iacr * C.K_iacr) / C.Cr + b_Cr;
+    const R p3 = (b_K_vts * C.K_vts + b_K_sacw * C.K_sacw + b_K_saci * C.K_saci + b_K_vents2 * R(0.5) * C.K_vents2) /
+                 C.Cs;
+    const R p4 = (b_K_vtg * C.K_vtg + b_K_gacw * C.K_gacw) / C.Cg + b_Cg;
+    const R p6 = b_K_aut * C.K_aut / C.kk_aut;
+    pb[0] += D(b_beta) * isc;
+    pb[1] += D(b_qicrt) * isc;
+    pb[2] += D(p2) * isc;
+    pb[3] += D(p3) * isc;
+    pb[4] += D(p4) * isc;
+    pb[5] += D(b_icenuc) * isc;
+    pb[6] += D(p6) * isc;
+    return;
+  }
   pb[0] += D(b_beta) * isc;
   pb[1] += D(b_qicrt) * isc;
   pb[2] += ((D(b_K_vtr) * D(C.K_vtr) + D(b_K_raci) * D(C.K_raci) + D(b_K_iacr) * D(C.K_iacr)) * (1.0 / D(C.Cr)) +
