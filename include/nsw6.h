@@ -293,9 +293,10 @@ int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, do
  *   adjoints are added with atomics (so the last bits depend on their order),
  *   the cell physics per cell, each by a hand-written reverse sweep.  With
  *   nsw6_set_precision(h, 1) (the mixed-precision step) the cell physics is
- *   that step's: FP32 rates and FP32 rate adjoints, FP64 budgets; the column
- *   stages and the accumulation of the state and parameter adjoints stay
- *   FP64 (the 12-step window with a mixed forward uses this); any other
+ *   that step's: FP32 rates and FP32 rate adjoints, FP64 budgets, and the
+ *   step's FP32 departure distances; the other column stages and the
+ *   accumulation of the state and parameter adjoints stay FP64 (the 12-step
+ *   window with a mixed forward uses this); any other
  *   precision, a scheme switch or nsw6_set_adjoint_mode 1 linearise the FP64
  *   step.  The first call allocates the work fields and keeps them in the
  *   handle: about 300 doubles per cell for lall_max regions (nsw6_set_adjoint_mode 1 adds
