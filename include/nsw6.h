@@ -37,7 +37,8 @@ typedef enum nsw6_status {
   NSW6_ERR_NOCONV = 3,       /* satadjust Newton hit the iteration limit             */
   NSW6_ERR_NAN = 4,          /* satadjust produced a non-finite temperature          */
   NSW6_ERR_UNSUPPORTED = 5,  /* configuration not implemented                        */
-  NSW6_ERR_TOO_LARGE = 6,    /* region larger than mp_driver_noalloc's fixed scratch */
+  NSW6_ERR_TOO_LARGE = 6,    /* region larger than mp_driver_noalloc's fixed scratch,
+                                or gall kall lall_max >= 2^32 at nsw6_create          */
   NSW6_ERR_CHECK = 7         /* adjoint mode 2: its forward differs from the step's  */
 } nsw6_status;
 
@@ -64,7 +65,8 @@ void nsw6_default_params(nsw6_params* p);
  * per batched call.  gz/gzh are the full-level and interface heights [kall]
  * in HOST memory (the contents of GRD_gz.dat / GRD_gzh.dat read by
  * GRD_Input_vgrid, mod_debug.cpp:189-195).  Allocates all device workspace;
- * no later call allocates.  Uses the current CUDA device. */
+ * no later call allocates.  Uses the current CUDA device.  Returns
+ * NSW6_ERR_TOO_LARGE when gall * kall * lall_max >= 2^32. */
 int nsw6_create(nsw6_handle** h, int gall, int kall, int lall_max, const double* gz, const double* gzh);
 int nsw6_destroy(nsw6_handle* h);
 
@@ -332,7 +334,7 @@ int mp_driver_adjoint(nsw6_handle* h, int lall, double* const* args, double* con
  * cannot create an nsw6_handle, which allocates its workspace.
  *
  * The workspace is a fixed file-scope device array inside the library (about
- * 100 MB, present on every device the library is loaded on).  Limits: kall in
+ * 110 MB, present on every device the library is loaded on).  Limits: kall in
  * [5, 160] and gall * kall <= NSW6_NOALLOC_MAX_CELLS; larger regions return
  * NSW6_ERR_TOO_LARGE before anything is issued.
  *

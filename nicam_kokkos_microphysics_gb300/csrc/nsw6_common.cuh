@@ -166,6 +166,8 @@ struct Problem {
   double* zdis;                // [lall][2 ntr][kall][gall]: zdis0 per tracer, then zdis0h per tracer
   unsigned long long* zmax;    // [lall][2 ntr][kall] ordered keys, reset to 0
   unsigned long long* zmin;    // [lall][2 ntr][kall] ordered keys, reset to ~0
+  unsigned* satq;              // [1 + lall kall gall]: count (reset to 0), then the saturated cells'
+                               // indices l kall gall + k gall + g, for nsw6_satadj_kernel
   DevStatus* status;
 };
 

@@ -66,6 +66,7 @@ struct nsw6_handle {
   double* d_zdis = nullptr;
   unsigned long long* d_zmax = nullptr;
   unsigned long long* d_zmin = nullptr;
+  unsigned* d_satq = nullptr;   // count and list of the saturated cells of a step
   DevStatus* d_status = nullptr;
   cudaStream_t stream = nullptr;
   int sync_check = 1;
@@ -529,6 +530,7 @@ int fill_problem(nsw6_handle* h, int lall, double* const* a, double dt, Problem&
   P.zdis = h->d_zdis;
   P.zmax = h->d_zmax;
   P.zmin = h->d_zmin;
+  P.satq = h->d_satq;
   P.status = h->d_status;
   return NSW6_OK;
 }
@@ -780,6 +782,8 @@ void nsw6_default_params(nsw6_params* p) {
 
 int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const double* gz, const double* gzh) {
   if (!out || gall < 1 || kall < 5 || kall > MAX_KALL || lall_max < 1 || !gz || !gzh) return NSW6_ERR_BAD_ARG;
+  // the saturated cells of a step are listed by 32-bit cell index
+  if ((unsigned long long)gall * kall * lall_max >= 0xFFFFFFFFull) return NSW6_ERR_TOO_LARGE;
   *out = nullptr;
   nsw6_handle* h = new (std::nothrow) nsw6_handle();
   if (!h) return NSW6_ERR_BAD_ARG;
@@ -800,6 +804,7 @@ int nsw6_create(nsw6_handle** out, int gall, int kall, int lall_max, const doubl
             cudaMalloc(&h->d_zdis, sizeof(double) * 8 * KG * lall_max) == cudaSuccess &&
             cudaMalloc(&h->d_zmax, sizeof(unsigned long long) * nkey) == cudaSuccess &&
             cudaMalloc(&h->d_zmin, sizeof(unsigned long long) * nkey) == cudaSuccess &&
+            cudaMalloc(&h->d_satq, sizeof(unsigned) * (1 + KG * lall_max)) == cudaSuccess &&
             cudaMalloc(&h->d_status, sizeof(DevStatus)) == cudaSuccess &&
             cudaMalloc(&h->d_fmtab, sizeof(double) * FM_TABLE_DOUBLES) == cudaSuccess &&
             cudaMemcpy(h->d_fmtab, htab, sizeof(double) * FM_TABLE_DOUBLES, cudaMemcpyHostToDevice) == cudaSuccess &&
@@ -821,6 +826,7 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_zdis);
   cudaFree(h->d_zmax);
   cudaFree(h->d_zmin);
+  cudaFree(h->d_satq);
   cudaFree(h->d_status);
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
@@ -1291,7 +1297,8 @@ constexpr size_t NA_ZMIN = NA_ZMAX + 6 * MAX_KALL;                // [6][MAX_KAL
 constexpr size_t NA_GRID = NA_ZMIN + 6 * MAX_KALL;                // [GF_COUNT][MAX_KALL]
 constexpr size_t NA_FMTAB = NA_GRID + (size_t)GF_COUNT * MAX_KALL; // [FM_TABLE_DOUBLES]
 constexpr size_t NA_ZDIS = ((NA_FMTAB + FM_TABLE_DOUBLES + 31) / 32) * 32;  // [6][kall][gall]
-constexpr size_t NA_TOTAL = NA_ZDIS + 6 * (size_t)NSW6_NOALLOC_MAX_CELLS;
+constexpr size_t NA_SATQ = NA_ZDIS + 6 * (size_t)NSW6_NOALLOC_MAX_CELLS;  // [1 + cells] uint32
+constexpr size_t NA_TOTAL = NA_SATQ + ((size_t)NSW6_NOALLOC_MAX_CELLS + 2) / 2;
 static_assert(NA_ZMAX % 32 == 0 && NA_ZMIN % 32 == 0 && NA_GRID % 32 == 0 && NA_FMTAB % 32 == 0,
               "scratch slots must stay 256-byte aligned");
 static_assert(sizeof(DevStatus) <= 32 * sizeof(double), "status slot too small");
@@ -1338,6 +1345,7 @@ extern "C" int mp_driver_noalloc(int gall, int kall, const double* gz, const dou
   h.d_zdis = base + NA_ZDIS;
   h.d_zmax = reinterpret_cast<unsigned long long*>(base + NA_ZMAX);
   h.d_zmin = reinterpret_cast<unsigned long long*>(base + NA_ZMIN);
+  h.d_satq = reinterpret_cast<unsigned*>(base + NA_SATQ);
   h.d_status = reinterpret_cast<DevStatus*>(base + NA_STATUS);
   h.stream = static_cast<cudaStream_t>(stream);
 

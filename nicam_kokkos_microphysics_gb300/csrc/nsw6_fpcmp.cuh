@@ -62,7 +62,26 @@ NSW6_FP_HD bool fp_ge(double a, double b) { return fp_le(b, a); }
 // |x| < c for a constant c > 0 (NaN: false)
 NSW6_FP_HD bool fp_abs_lt(double x, double c) { return (fp_bits(x) & FP_ABS) < fp_bits(c); }
 
+// x < c for a constant c > 0: every negative x and -0 below it, a positive x
+// by its bits (NaN: false)
+NSW6_FP_HD bool fp_lt_pos(double x, double c) {
+  const long long b = fp_bits(x);
+  return ((b & FP_ABS) <= FP_INF) & (b < fp_bits(c));
+}
+
+// max(x, c) as Kokkos::max, (x < c) ? c : x, for a constant c > 0
+NSW6_FP_HD double fp_max_pos(double x, double c) { return fp_lt_pos(x, c) ? c : x; }
+
 // x == 0 (either zero)
 NSW6_FP_HD bool fp_is_zero(double x) { return (fp_bits(x) & FP_ABS) == 0; }
+
+// x is +-inf or NaN (x * 0 != 0)
+NSW6_FP_HD bool fp_not_finite(double x) { return (fp_bits(x) & FP_ABS) >= FP_INF; }
+
+// x is a positive normal number (not zero, subnormal, infinite or NaN)
+NSW6_FP_HD bool fp_pos_normal(double x) {
+  const long long b = fp_bits(x);
+  return (b >= 0x0010000000000000ll) & (b < FP_INF);
+}
 
 }  // namespace nsw6

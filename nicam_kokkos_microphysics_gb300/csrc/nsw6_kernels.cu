@@ -364,6 +364,274 @@ __device__ __forceinline__ float flux_integral_f(const float* rhof_col, const fl
   return fabsf(f) >= (float)EPS ? f : 0.0f;
 }
 
+// Newton iteration of the saturation adjustment of one saturated cell:
+// satadjust_liq (mod_satadjust.cpp:771-896, the iteration :840-880) or, with
+// the switch, satadjust_all (:620-769, the iteration :686-754).  q holds the
+// cell's specific humidities with q[QV] = qsum and q[QC] (and q[QI] with
+// satadjust_all) = 0; the iteration leaves the adjusted ones there and
+// returns the temperature.  Its range, convergence and finiteness tests run
+// on the integer pipe (nsw6_fpcmp.cuh).
+template <class M>
+__device__ __forceinline__ double satadjust_newton(const Problem& P, const Consts& C, const M& mth, bool ice_adj,
+                                                   double tem, double ein_moist, double qsum, double rho_l,
+                                                   double qd_l, double* q, int k, int g, int l) {
+  bool converged = false;
+  int ite;
+  if (ice_adj) {
+    // satadjust_all, mod_satadjust.cpp:686-754 (CPovR = CVovR = 0, all CVW = CVdry)
+    const double UL = C.sat_ulimit, LL = C.sat_llimit;
+    for (ite = 0; ite < P.itelim; ++ite) {
+      const double alpha = dmin(dmax((tem - LL) / (UL - LL), 0.0), 1.0);
+      const double rtem = 1.0 / fp_max_pos(tem, TEM_MIN);
+      const double psatl = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
+      const double psat = psatl * alpha + psati * (1.0 - alpha);
+      const double qsatl = psatl / (rho_l * RVAP * tem);
+      const double qsati = psati / (rho_l * RVAP * tem);
+      const double qsat = psat / (rho_l * RVAP * tem);
+      q[I_QV] = qsat;
+      q[I_QC] = (qsum - qsat) * alpha;
+      q[I_QI] = (qsum - qsat) * (1.0 - alpha);
+      double cv = qd_l * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
+      const double emoist_new = tem * cv + q[I_QV] * LHV0 - q[I_QI] * LHF0;
+      const double dalpha_dT = (!(UL - tem < 0.0) && !(tem - LL < 0.0)) ? 1.0 / (UL - LL) : 0.0;
+      const double t2 = tem * tem;
+      const double dqsatl_dT = (C.LovR_liq / t2) * qsatl;
+      const double dqsati_dT = (C.LovR_ice / t2) * qsati;
+      const double dqsat_dT = qsatl * dalpha_dT + dqsatl_dT * alpha - qsati * dalpha_dT + dqsati_dT * (1.0 - alpha);
+      const double dqc_dT = (qsum - qsat) * dalpha_dT - dqsat_dT * alpha;
+      const double dqi_dT = -(qsum - qsat) * dalpha_dT - dqsat_dT * (1.0 - alpha);
+      const double dcv_dT = dqsat_dT * CVDRY + dqc_dT * CVDRY + dqi_dT * CVDRY;
+      const double demoist_dT = tem * dcv_dT + cv + dqsat_dT * LHV0 - dqi_dT * LHF0;
+      const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+      tem = tem - dtemp;
+      if (fp_abs_lt(dtemp, C.dtemp_criteria)) {
+        converged = true;
+        break;
+      }
+      if (fp_not_finite(tem)) break;
+    }
+  } else {
+    for (ite = 0; ite < P.itelim; ++ite) {
+      const double rtem = 1.0 / fp_max_pos(tem, TEM_MIN);
+      const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      const double qsat = psat / (rho_l * RVAP * tem);
+      q[I_QV] = qsat;
+      q[I_QC] = qsum - qsat;
+      double cv = qd_l * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
+      const double emoist_new = tem * cv + q[I_QV] * LHV0;
+      // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
+      // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
+      const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
+      const double demoist_dT = cv + dqsat_dT * LHV0;
+      const double dtemp = (emoist_new - ein_moist) / demoist_dT;
+      tem = tem - dtemp;
+      if (fp_abs_lt(dtemp, C.dtemp_criteria)) {
+        converged = true;
+        break;
+      }
+      if (fp_not_finite(tem)) break;
+    }
+  }
+  if (!converged) record_error(P.status, fp_not_finite(tem) ? ERR_NAN : ERR_NOCONV, k, g, l, ite);
+  return tem;
+}
+
+// The final state of one cell after the transport and KIN2EIN: thermodynamics,
+// saturation adjustment, negative filter and outputs (mod_mp_driver.cpp:
+// 555-612 with mod_thrmdyn.cpp, mod_satadjust.cpp:274-362 and
+// mod_mp_nsw6.cpp:1770-1831).  rhog, its reciprocal and rhoge (after KIN2EIN)
+// are the cell's; the rest comes from the state arrays.  With newton = false
+// (the column kernel) a saturated interior cell is left as it is and true is
+// returned, for nsw6_satadj_kernel; every other cell is finished.  With
+// newton = true (that kernel) the cell is saturated: the same values are
+// formed, the Newton iteration runs and the cell is finished.
+template <class M, bool MIX, bool OPT>
+__device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, const M& mth, bool ice_adj, float lovr_f,
+                                           size_t i, size_t iq, size_t KG, bool interior, double rhog, double rrhog,
+                                           double rhoge, bool newton, int k, int g, int l) {
+  double rq[6], q[6];
+#pragma unroll
+  for (int n = 0; n < 6; ++n) rq[n] = P.rhogq[iq + (size_t)n * KG];
+  // These quotients must be correctly rounded: the saturation adjustment
+  // forms qc = qsum - qsat from them, a difference of nearly equal numbers
+  // in which one unit in the last place of qsum is already a relative error
+  // of 1e-11 when qc is small.
+#pragma unroll
+  for (int n = 0; n < 6; ++n) q[n] = MIX ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
+  const double gsg = P.gsgam2[i];
+  double rho = rhog / gsg;
+  const double ein = MIX ? rhoge * rrhog : div_rn(rhoge, rhog, rrhog);
+  double qd = 1.0;
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) qd = qd - q[n];
+  // THRMDYN_tempre, mod_thrmdyn.cpp:137-180.  Its temperature is replaced
+  // by the saturation adjustment's everywhere and its pressure by the
+  // negative filter's at interior levels: only the halo levels output it.
+  double pre = 0.0;
+  if (!interior) {
+    double cvt = 0.0, qdl = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) {
+      cvt = cvt + q[n] * CVDRY;
+      qdl = qdl - q[n];
+    }
+    cvt = cvt + qdl * CVDRY;
+    const double tem0 = ein / cvt;
+    pre = rho * tem0 * (qdl * RDRY + q[I_QV] * RVAP);
+  }
+
+  // SATURATION_adjustment (mod_satadjust.cpp:274-362): ice_adjust = false,
+  // or true with the switch (cloud ice joins the adjustment)
+  double ein_moist, qsum;
+  if (ice_adj) {
+    ein_moist = ein + q[I_QV] * LHV0 - q[I_QI] * LHF0;
+    qsum = q[I_QV] + q[I_QC] + q[I_QI];
+    q[I_QI] = 0.0;
+  } else {
+    ein_moist = ein + q[I_QV] * LHV0;
+    qsum = q[I_QV] + q[I_QC];
+  }
+  q[I_QV] = qsum;
+  q[I_QC] = 0.0;
+  double cvtot = qd * CVDRY;
+#pragma unroll
+  for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+  const double rho_l = rho;
+  double tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
+  if (interior) {
+    // satadjust_liq (mod_satadjust.cpp:771-896) or satadjust_all
+    // (:620-769)
+    double qd_l = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
+    if (newton) {
+      tem = satadjust_newton(P, C, mth, ice_adj, tem, ein_moist, qsum, rho_l, qd_l, q, k, g, l);
+    } else {
+    // is the cell saturated?
+    // The test qsum - qsat(tem) > EPS is first decided in FP32 (liquid
+    // saturation only), from three conversions (T, rho, qsum): an FP64
+    // compare or conversion costs as much of the FP64 pipe as an FMA.
+    // x = LovR (1/T00 - 1/T) is formed as LovR (Tf - T00f) / (Tf T00f): the
+    // difference is exact, so x carries seven roundings (4.2e-7 |x|) and the
+    // conversions of T and T00 (LovR u (1/T00 + 1/T) <= 7.2e-6 for |x| <= 80,
+    // u = 2^-24); with expf's 2 ulp and eight roundings after it the FP32
+    // qsat is within 4.2e-5 (relative) of the FP64 one.  qsum rounds by u.
+    // So qsum_f > 1.0001 qsat_f means qsum > (1 + 5.7e-5) qsat, and with
+    // qsat_f >= 1e-11 the FP64 difference exceeds EPS; qsum_f < 0.9999 qsat_f
+    // means qsum < qsat.  The FP64 test decides the cells in between and
+    // outside those ranges, as the reference computes it.  Only the branch
+    // depends on qsat here: a saturated cell's Newton iteration recomputes it.
+    int sat = -1;
+    if (!ice_adj) {
+      const float tf = float(tem);
+      const float tcf = (tf < float(TEM_MIN)) ? float(TEM_MIN) : tf;   // float(max(tem, TEM_MIN))
+      const float xf = lovr_f * ((tcf - float(TEM00)) / (tcf * float(TEM00)));
+      if (fabsf(xf) <= 80.0f) {
+        const float qsf = (float(PSAT0) * expf(xf)) / (float(rho_l) * float(RVAP) * tf);
+        if (qsf >= 1.0e-11f && qsf <= 1.0e30f) {
+          const float qq = float(qsum);
+          if (qq > qsf * 1.0001f) sat = 1;
+          else if (qq < qsf * 0.9999f) sat = 0;
+        }
+      }
+    }
+    if (sat < 0) {
+      const double rtem = 1.0 / fp_max_pos(tem, TEM_MIN);
+      double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
+      if (ice_adj) {
+        const double alpha =
+            dmin(dmax((tem - C.sat_llimit) / (C.sat_ulimit - C.sat_llimit), 0.0), 1.0);
+        const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
+        psat = psat * alpha + psati * (1.0 - alpha);
+      }
+      const double qsat = psat / (rho_l * RVAP * tem);
+      sat = (qsum - qsat > EPS) ? 1 : 0;
+    }
+    if (sat) return true;
+    }
+  }
+  rq[I_QV] = rhog * q[I_QV];
+  rq[I_QC] = rhog * q[I_QC];
+  if (ice_adj) rq[I_QI] = rhog * q[I_QI];
+  if (!interior) {   // interior levels: rhoge comes from the negative filter below
+    cvtot = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+    rhoge = rhog * tem * cvtot;
+  }
+
+  // negative_filter (mod_mp_nsw6.cpp:1770-1831), interior levels
+  double rhog_o = rhog;
+  if (interior) {
+    double diffq = 0.0;
+    unsigned clamped = 0;   // bit n: rq[n] was negative and is now zero
+#pragma unroll
+    for (int n = 2; n <= 5; ++n) {
+      diffq += rq[n];
+      if (rq[n] < 0.0) clamped |= 1u << n;   // rq[n] = max(rq[n], 0)
+      rq[n] = dmax(rq[n], 0.0);
+    }
+#pragma unroll
+    for (int n = 2; n <= 5; ++n) diffq -= rq[n];
+    rq[I_QV] += diffq;
+    diffq = rq[I_QV];
+    rq[I_QV] = dmax(rq[I_QV], 0.0);
+    diffq -= rq[I_QV];
+    if (fp_is_zero(diffq) && fp_pos_normal(rhog)) {
+      // Nothing removed: rhog (1 - diffq) is rhog exactly, and so are
+      // rho = rhog / gsg and the reciprocal formed above.  The quotients of
+      // the tracers the filter left as they were are those formed above
+      // (QR, QS, QG; QI unless the adjustment set it), and an unsaturated
+      // cell's cloud water is +0 = (rhog 0) / rhog.
+      const unsigned same = (0x34u | (ice_adj && newton ? 0u : 0x08u) | (newton ? 0u : 0x02u)) & ~clamped;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n)
+        if (!((same >> n) & 1u)) q[n] = MIX ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
+    } else {
+      rhog_o = rhog * (1.0 - diffq);
+      rho = rhog_o / gsg;
+      const double rrhog_o = 1.0 / rhog_o;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) q[n] = MIX ? rq[n] * rrhog_o : div_rn(rq[n], rhog_o, rrhog_o);
+    }
+    double qdf = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
+    double cva = qdf * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
+    rhoge = tem * rhog_o * cva;
+    pre = rho * (qdf * RDRY + q[I_QV] * RVAP) * tem;
+  }
+
+  P.rhog[i] = rhog_o;
+  P.rhoge[i] = rhoge;
+#pragma unroll
+  for (int n = 0; n < 6; ++n) {
+    P.rhogq[iq + (size_t)n * KG] = rq[n];
+    P.q[iq + (size_t)n * KG] = q[n];
+  }
+  P.rho[i] = rho;
+  P.tem[i] = tem;
+  P.pre[i] = pre;
+  P.qd[i] = qd;
+  // mp_driver epilogue (mod_mp_driver.cpp:555-612, MP_DIV_NUM = 1)
+  P.re_solid[i] = 20.0E-6;
+  P.GDCLW[i] = 0.0;
+  P.GDCFRC[i] = 0.0;
+  if (!interior) {
+    P.GPREC[i] = 0.0;
+    P.re_liquid[i] = 0.0;
+    P.re_cld[i] = 0.0;
+  }
+  return false;
+}
+
 // MIX: the mixed-precision step: every flux of the sedimentation (mass,
 // energy, kinetic energy and momentum, full and half levels) is integrated in
 // FP32 from its FP64 source, the mass, energy and kinetic-energy divergences
@@ -885,24 +1153,21 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
 
   // ---- per cell: KIN2EIN, final thermodynamics, saturation adjustment,
   //      negative filter, outputs.  The saturation-adjustment Newton
-  //      iteration runs only in saturated cells; to keep warps full they are
-  //      queued (pass A), iterated together (pass B) and finished (pass C),
-  //      the queue living in slots that are dead by now.  Pass C recomputes
-  //      the cell's state exactly as pass A did and takes the Newton result.
-  const int QE_TEM = S_KINH, QE_EIN = S_KINV, QE_QSUM = S_DKINH, QE_RHOL = S_DKINV, QE_QDL = S_DQR;
-  const int QE_Q2 = S_DQS, QE_Q3 = S_DQG, QE_Q4 = S_F, QE_Q5 = S_RGS, QE_C = S_BASE;
-  const int QE_TOUT = S_VI, QE_QV = S_VJ, QE_QC = S_DRHOGU, QE_QI = S_DRHOGV;
+  //      iteration runs only in saturated cells, a few percent of them; a
+  //      tile's would share one warp, which issues one FP64 instruction per
+  //      64 cycles where the SM issues one per 19.  So the saturated cells are
+  //      left as they are (rhoge after KIN2EIN stored), listed, and finished
+  //      by nsw6_satadj_kernel, whose warps are full and fill every SM.
   __shared__ int nqueue;
+  __shared__ unsigned qbase;
   if (threadIdx.x == 0) nqueue = 0;
   __syncthreads();
   const float lovr_f = float(C.LovR_liq);
-
-  // mode 0: returns true when the cell was queued for the Newton iteration;
-  // mode 1: finishes a queued cell with the result (tres, qvres, qcres)
-  auto final_cell = [&](int c, int mode, double tres, double qvres, double qcres, double qires) -> bool {
+  int* qcell = reinterpret_cast<int*>(F(S_BASE));   // the tile's saturated cells (S_BASE is dead by now)
+  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    if (g >= G) continue;
     const size_t i = off + (size_t)k * G + g;
-    const size_t iq = offq + (size_t)k * G + g;
     const bool interior = (k >= kmin && k <= kmax);
     const double rhog = F(S_RHOF)[c];
     // Quotients by a shared denominator are formed from one reciprocal with a
@@ -924,187 +1189,11 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       }
       const double tmp = tmp_h + (w2c0 * F(S_DRHOPHI)[c + COL_TG] + w2c1 * F(S_DRHOPHI)[c]);
       rhoge = rhoge + (F(S_DRHOE)[c] - tmp);
+      P.rhoge[i] = rhoge;   // a saturated cell's adjustment starts from here (final_cell overwrites the rest)
     }
-    double rq[6], q[6];
-#pragma unroll
-    for (int n = 0; n < 6; ++n) rq[n] = P.rhogq[iq + (size_t)n * KG];
-    // These quotients must be correctly rounded: the saturation adjustment
-    // forms qc = qsum - qsat from them, a difference of nearly equal numbers
-    // in which one unit in the last place of qsum is already a relative error
-    // of 1e-11 when qc is small.
-#pragma unroll
-    for (int n = 0; n < 6; ++n) q[n] = MIX ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
-    const double gsg = P.gsgam2[i];
-    double rho = rhog / gsg;
-    const double ein = MIX ? rhoge * rrhog : div_rn(rhoge, rhog, rrhog);
-    double qd = 1.0;
-#pragma unroll
-    for (int n = 1; n <= 5; ++n) qd = qd - q[n];
-    // THRMDYN_tempre, mod_thrmdyn.cpp:137-180.  Its temperature is replaced
-    // by the saturation adjustment's everywhere and its pressure by the
-    // negative filter's at interior levels: only the halo levels output it.
-    double pre = 0.0;
-    if (!interior) {
-      double cvt = 0.0, qdl = 1.0;
-#pragma unroll
-      for (int n = 1; n <= 5; ++n) {
-        cvt = cvt + q[n] * CVDRY;
-        qdl = qdl - q[n];
-      }
-      cvt = cvt + qdl * CVDRY;
-      const double tem0 = ein / cvt;
-      pre = rho * tem0 * (qdl * RDRY + q[I_QV] * RVAP);
-    }
-
-    // SATURATION_adjustment (mod_satadjust.cpp:274-362): ice_adjust = false,
-    // or true with the switch (cloud ice joins the adjustment)
-    double ein_moist, qsum;
-    if (ice_adj) {
-      ein_moist = ein + q[I_QV] * LHV0 - q[I_QI] * LHF0;
-      qsum = q[I_QV] + q[I_QC] + q[I_QI];
-      q[I_QI] = 0.0;
-    } else {
-      ein_moist = ein + q[I_QV] * LHV0;
-      qsum = q[I_QV] + q[I_QC];
-    }
-    q[I_QV] = qsum;
-    q[I_QC] = 0.0;
-    double cvtot = qd * CVDRY;
-#pragma unroll
-    for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
-    const double rho_l = rho;
-    double tem = mode == 1 ? tres : (ein_moist - q[I_QV] * LHV0) / cvtot;
-    if (mode == 1) {
-      q[I_QV] = qvres;
-      q[I_QC] = qcres;
-      if (ice_adj) q[I_QI] = qires;
-    } else if (interior) {
-      // satadjust_liq (mod_satadjust.cpp:771-896) or satadjust_all
-      // (:620-769): is the cell saturated?
-      double qd_l = 1.0;
-#pragma unroll
-      for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
-      // The test qsum - qsat(tem) > EPS is first decided in FP32 (liquid
-      // saturation only).  With x = LovR (1/T00 - 1/T) formed as
-      // LovR (T - T00) / (T T00), free of cancellation, the FP32 qsat is within
-      // 4.2e-7 |x| + 6e-7 (relative) of the FP64 one: seven roundings on x,
-      // expf's 2 ulp and five roundings after it.  For |x| <= 80 that is below
-      // 4e-5, so a cell whose distance from the threshold exceeds 1e-4 qsat
-      // (plus the rounding of the FP64 difference) takes the branch the FP64
-      // test takes; the FP64 test decides the cells closer to saturation and
-      // those outside that range, as the reference computes it.  Only the
-      // branch depends on qsat here: a saturated cell's Newton iteration
-      // recomputes it.
-      int sat = -1;
-      if (!ice_adj) {
-        const double tc = dmax(tem, TEM_MIN);
-        const float xf = lovr_f * (float(tc - TEM00) / (float(tc) * float(TEM00)));
-        if (fabsf(xf) <= 80.0f) {
-          const float qsf = (float(PSAT0) * expf(xf)) / (float(rho_l) * float(RVAP) * float(tem));
-          if (qsf > 0.0f && qsf <= 1.0e30f) {
-            const double qs = double(qsf);
-            const double d = qsum - qs;
-            const double m = 1.0e-4 * qs + 1.0e-15 * fabs(qsum);
-            if (d - m > EPS) sat = 1;
-            else if (d + m < EPS) sat = 0;
-          }
-        }
-      }
-      if (sat < 0) {
-        const double rtem = 1.0 / (dmax(tem, TEM_MIN));
-        double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-        if (ice_adj) {
-          const double alpha =
-              dmin(dmax((tem - C.sat_llimit) / (C.sat_ulimit - C.sat_llimit), 0.0), 1.0);
-          const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
-          psat = psat * alpha + psati * (1.0 - alpha);
-        }
-        const double qsat = psat / (rho_l * RVAP * tem);
-        sat = (qsum - qsat > EPS) ? 1 : 0;
-      }
-      if (sat) {
-        const int e = atomicAdd(&nqueue, 1);
-        F(QE_TEM)[e] = tem;
-        F(QE_EIN)[e] = ein_moist;
-        F(QE_QSUM)[e] = qsum;
-        F(QE_RHOL)[e] = rho_l;
-        F(QE_QDL)[e] = qd_l;
-        F(QE_Q2)[e] = q[2];
-        F(QE_Q3)[e] = q[3];
-        F(QE_Q4)[e] = q[4];
-        F(QE_Q5)[e] = q[5];
-        F(QE_C)[e] = (double)c;
-        return true;
-      }
-    }
-    rq[I_QV] = rhog * q[I_QV];
-    rq[I_QC] = rhog * q[I_QC];
-    if (ice_adj) rq[I_QI] = rhog * q[I_QI];
-    if (!interior) {   // interior levels: rhoge comes from the negative filter below
-      cvtot = qd * CVDRY;
-#pragma unroll
-      for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
-      rhoge = rhog * tem * cvtot;
-    }
-
-    // negative_filter (mod_mp_nsw6.cpp:1770-1831), interior levels
-    double rhog_o = rhog;
-    if (interior) {
-      double diffq = 0.0;
-#pragma unroll
-      for (int n = 2; n <= 5; ++n) {
-        diffq += rq[n];
-        rq[n] = dmax(rq[n], 0.0);
-      }
-#pragma unroll
-      for (int n = 2; n <= 5; ++n) diffq -= rq[n];
-      rq[I_QV] += diffq;
-      diffq = rq[I_QV];
-      rq[I_QV] = dmax(rq[I_QV], 0.0);
-      diffq -= rq[I_QV];
-      rhog_o = rhog * (1.0 - diffq);
-      rho = rhog_o / gsg;
-      const double rrhog_o = 1.0 / rhog_o;
-#pragma unroll
-      for (int n = 1; n <= 5; ++n) q[n] = MIX ? rq[n] * rrhog_o : div_rn(rq[n], rhog_o, rrhog_o);
-      double qdf = 1.0;
-#pragma unroll
-      for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
-      double cva = qdf * CVDRY;
-#pragma unroll
-      for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
-      rhoge = tem * rhog_o * cva;
-      pre = rho * (qdf * RDRY + q[I_QV] * RVAP) * tem;
-    }
-
-    P.rhog[i] = rhog_o;
-    P.rhoge[i] = rhoge;
-#pragma unroll
-    for (int n = 0; n < 6; ++n) {
-      P.rhogq[iq + (size_t)n * KG] = rq[n];
-      P.q[iq + (size_t)n * KG] = q[n];
-    }
-    P.rho[i] = rho;
-    P.tem[i] = tem;
-    P.pre[i] = pre;
-    P.qd[i] = qd;
-    // mp_driver epilogue (mod_mp_driver.cpp:555-612, MP_DIV_NUM = 1)
-    P.re_solid[i] = 20.0E-6;
-    P.GDCLW[i] = 0.0;
-    P.GDCFRC[i] = 0.0;
-    if (!interior) {
-      P.GPREC[i] = 0.0;
-      P.re_liquid[i] = 0.0;
-      P.re_cld[i] = 0.0;
-    }
-    return false;
-  };
-
-  // pass A: every cell; saturated interior cells are queued
-  for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
-    const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-    if (g >= G) continue;
-    final_cell(c, 0, 0.0, 0.0, 0.0, 0.0);
+    if (final_cell<M, MIX, OPT>(P, C, mth, ice_adj, lovr_f, i, offq + (size_t)k * G + g, KG, interior, rhog, rrhog,
+                                rhoge, false, k, g, l))
+      qcell[atomicAdd(&nqueue, 1)] = c;
     if (k == kmin) {
       const size_t ic = (size_t)l * G + g;
       const size_t r0 = (size_t)l * G + g, r1 = P.prec_ld + r0;
@@ -1122,95 +1211,44 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     }
   }
   __syncthreads();
-
-  // pass B: the Newton iteration of the queued cells, warps full
-  const int nq = nqueue;
-  for (int e = threadIdx.x; e < nq; e += blockDim.x) {
-    double tem = F(QE_TEM)[e];
-    const double ein_moist = F(QE_EIN)[e], qsum = F(QE_QSUM)[e], rho_l = F(QE_RHOL)[e], qd_l = F(QE_QDL)[e];
-    double q[6];
-    q[0] = qsum;
-    q[1] = 0.0;
-    q[2] = F(QE_Q2)[e];
-    q[3] = F(QE_Q3)[e];
-    q[4] = F(QE_Q4)[e];
-    q[5] = F(QE_Q5)[e];
-    bool converged = false;
-    int ite;
-    if (ice_adj) {
-      // satadjust_all, mod_satadjust.cpp:686-754 (CPovR = CVovR = 0, all CVW = CVdry)
-      const double UL = C.sat_ulimit, LL = C.sat_llimit;
-      for (ite = 0; ite < P.itelim; ++ite) {
-        const double alpha = dmin(dmax((tem - LL) / (UL - LL), 0.0), 1.0);
-        const double rtem = 1.0 / (dmax(tem, TEM_MIN));
-        const double psatl = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-        const double psati = PSAT0 * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
-        const double psat = psatl * alpha + psati * (1.0 - alpha);
-        const double qsatl = psatl / (rho_l * RVAP * tem);
-        const double qsati = psati / (rho_l * RVAP * tem);
-        const double qsat = psat / (rho_l * RVAP * tem);
-        q[I_QV] = qsat;
-        q[I_QC] = (qsum - qsat) * alpha;
-        q[I_QI] = (qsum - qsat) * (1.0 - alpha);
-        double cv = qd_l * CVDRY;
-#pragma unroll
-        for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
-        const double emoist_new = tem * cv + q[I_QV] * LHV0 - q[I_QI] * LHF0;
-        const double dalpha_dT = (!(UL - tem < 0.0) && !(tem - LL < 0.0)) ? 1.0 / (UL - LL) : 0.0;
-        const double t2 = tem * tem;
-        const double dqsatl_dT = (C.LovR_liq / t2) * qsatl;
-        const double dqsati_dT = (C.LovR_ice / t2) * qsati;
-        const double dqsat_dT = qsatl * dalpha_dT + dqsatl_dT * alpha - qsati * dalpha_dT + dqsati_dT * (1.0 - alpha);
-        const double dqc_dT = (qsum - qsat) * dalpha_dT - dqsat_dT * alpha;
-        const double dqi_dT = -(qsum - qsat) * dalpha_dT - dqsat_dT * (1.0 - alpha);
-        const double dcv_dT = dqsat_dT * CVDRY + dqc_dT * CVDRY + dqi_dT * CVDRY;
-        const double demoist_dT = tem * dcv_dT + cv + dqsat_dT * LHV0 - dqi_dT * LHF0;
-        const double dtemp = (emoist_new - ein_moist) / demoist_dT;
-        tem = tem - dtemp;
-        if (fabs(dtemp) < C.dtemp_criteria) {
-          converged = true;
-          break;
-        }
-        if (tem * 0.0 != 0.0) break;
-      }
-    } else {
-      for (ite = 0; ite < P.itelim; ++ite) {
-        const double rtem = 1.0 / (dmax(tem, TEM_MIN));
-        const double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
-        const double qsat = psat / (rho_l * RVAP * tem);
-        q[I_QV] = qsat;
-        q[I_QC] = qsum - qsat;
-        double cv = qd_l * CVDRY;
-#pragma unroll
-        for (int n = 1; n <= 5; ++n) cv = cv + q[n] * CVDRY;
-        const double emoist_new = tem * cv + q[I_QV] * LHV0;
-        // dqsat/dT = (LovR/T^2 + CVovR/T) qsat with CVovR = 0, and
-        // dCVtot/dT = dqsat/dT (CVW(QV) - CVW(QC)) = 0 (all CVW = CVdry)
-        const double dqsat_dT = C.LovR_liq * rtem * rtem * qsat;
-        const double demoist_dT = cv + dqsat_dT * LHV0;
-        const double dtemp = (emoist_new - ein_moist) / demoist_dT;
-        tem = tem - dtemp;
-        if (fabs(dtemp) < C.dtemp_criteria) {
-          converged = true;
-          break;
-        }
-        if (tem * 0.0 != 0.0) break;
-      }
-    }
-    if (!converged) {
-      const int c = (int)F(QE_C)[e];
-      record_error(P.status, (tem * 0.0 != 0.0) ? ERR_NAN : ERR_NOCONV, c / COL_TG, g0 + c % COL_TG, l, ite);
-    }
-    F(QE_TOUT)[e] = tem;
-    F(QE_QV)[e] = q[I_QV];
-    F(QE_QC)[e] = q[I_QC];
-    if (ice_adj) F(QE_QI)[e] = q[I_QI];
-  }
+  // the tile's saturated cells join the list (satq[0] counts them)
+  if (threadIdx.x == 0) qbase = nqueue > 0 ? atomicAdd(P.satq, (unsigned)nqueue) : 0u;
   __syncthreads();
+  for (int e = threadIdx.x; e < nqueue; e += blockDim.x) {
+    const int c = qcell[e];
+    P.satq[1 + qbase + e] = (unsigned)(off + (size_t)(c / COL_TG) * G + g0 + c % COL_TG);
+  }
+}
 
-  // pass C: finish the queued cells
-  for (int e = threadIdx.x; e < nq; e += blockDim.x)
-    final_cell((int)F(QE_C)[e], 1, F(QE_TOUT)[e], F(QE_QV)[e], F(QE_QC)[e], ice_adj ? F(QE_QI)[e] : 0.0);
+// ------------------------------------------------------------------ kernel 3
+// The saturated cells the column kernel listed (P.satq): the cell's state
+// after KIN2EIN is formed again exactly as there, the saturation-adjustment
+// Newton iteration runs and the cell is finished (final_cell).  One thread per
+// cell, grid-stride over the list, whose length only the device knows.
+constexpr int SAT_THREADS = 128;
+constexpr int SAT_BLOCKS = 152 * 8;
+
+template <class M, bool MIX, bool OPT>
+__global__ void __launch_bounds__(SAT_THREADS) nsw6_satadj_kernel(Problem P, Consts C) {
+  __shared__ double tab[FM_TABLE_DOUBLES];
+  const unsigned n = P.satq[0];
+  if (n == 0) return;
+  for (int t = threadIdx.x; t < FM_TABLE_DOUBLES; t += blockDim.x) tab[t] = P.fmtab[t];
+  __syncthreads();
+  const M mth = make_math<M>(tab);
+  const int G = P.gall;
+  const size_t KG = (size_t)P.kall * G;
+  const bool ice_adj = OPT && C.opt_expice == 0.0;
+  const float lovr_f = float(C.LovR_liq);
+  for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x) {
+    const size_t i = P.satq[1 + e];
+    const int l = (int)(i / KG);
+    const size_t r = i - (size_t)l * KG;
+    const int k = (int)(r / G), g = (int)(r - (size_t)k * G);
+    const double rhog = P.rhog[i];
+    final_cell<M, MIX, OPT>(P, C, mth, ice_adj, lovr_f, i, (size_t)l * NQ * KG + r, KG, true, rhog, 1.0 / rhog,
+                            P.rhoge[i], true, k, g, l);
+  }
 }
 
 // ------------------------------------------------------------------ math check
@@ -1336,6 +1374,8 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(P.zmin, 0xff, nkey * sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(P.satq, 0, sizeof(unsigned), stream);
+  if (e != cudaSuccess) return e;
   const bool opt = P.opt != 0;
   const size_t s1 = cell_smem_bytes(P.kall, P.mixed != 0, opt);
   const size_t s2 = column_smem_bytes(P.kall, opt);
@@ -1366,6 +1406,11 @@ cudaError_t launch_step(const Problem& P, const Consts& C, cudaStream_t stream, 
     else if (P.math_lib) nsw6_column_kernel<8, LibMath, false><<<g2, nt, s2, stream>>>(P, C);
     else nsw6_column_kernel<8, FastMath, false><<<g2, nt, s2, stream>>>(P, C);
   }
+  if (opt && P.mixed) nsw6_satadj_kernel<FastMath, true, true><<<SAT_BLOCKS, SAT_THREADS, 0, stream>>>(P, C);
+  else if (opt) nsw6_satadj_kernel<FastMath, false, true><<<SAT_BLOCKS, SAT_THREADS, 0, stream>>>(P, C);
+  else if (P.mixed) nsw6_satadj_kernel<FastMath, true, false><<<SAT_BLOCKS, SAT_THREADS, 0, stream>>>(P, C);
+  else if (P.math_lib) nsw6_satadj_kernel<LibMath, false, false><<<SAT_BLOCKS, SAT_THREADS, 0, stream>>>(P, C);
+  else nsw6_satadj_kernel<FastMath, false, false><<<SAT_BLOCKS, SAT_THREADS, 0, stream>>>(P, C);
   if (ev) cudaEventRecord(ev[2], stream);
   return cudaGetLastError();
 }
