@@ -101,6 +101,19 @@ __device__ __forceinline__ float sel(bool on, float x) { return on ? x : copysig
 __device__ __forceinline__ double per_dt(double q, double dt, double rdt) { return div_rn(q, dt, rdt); }
 __device__ __forceinline__ float per_dt(float q, float, float rdt) { return q * rdt; }
 
+// fac == 1 and x >= 0 in the limiters: for doubles from the bit patterns, on
+// the integer pipe (an FP64 comparison takes an FP64-pipe slot, as an FMA
+// does), with the IEEE comparisons' results for every double.
+__device__ __forceinline__ bool is_one(double x) { return fp_bits(x) == 0x3FF0000000000000ll; }
+__device__ __forceinline__ bool is_nonneg(double x) {   // +0 .. +inf, or -0
+  const long long b = fp_bits(x);
+  return (b >= 0 && b <= FP_INF) || b == -0x7FFFFFFFFFFFFFFFll - 1;
+}
+template <class T>
+__device__ __forceinline__ bool is_one(const T& x) { return x == T(1.0); }
+template <class T>
+__device__ __forceinline__ bool is_nonneg(const T& x) { return x >= T(0.0); }
+
 // R = double: the plain FP64 step.  R = float (the mixed path): saturation
 // values, process rates, limiters, tendencies, fall speeds and effective radii
 // in FP32; the negative filter, the tracer and internal-energy budgets
@@ -444,82 +457,104 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   // loss limiters, :1298-1477: fac = 1 when production >= loss - EPS,
   // else min(-dq/dt / net, 1) (the reference's (net - fac_sw) is net there)
   auto limiter = [&](R net, R dq) {
-    return (net + R(EPS) >= Z) ? ONE : dmin(-dq / net, ONE);
+    return is_nonneg(net + R(EPS)) ? ONE : dmin(-dq / net, ONE);
   };
-  // scaling by fac = 1 is exact and skipped
-  R fac;
+  // Scaling by fac = 1 is exact and skipped.  The tendencies below are the
+  // nets the limiters form (same terms, same order) where no later scaling
+  // changed their rates.  lc .. lg: the QC, QI, QR, QV, QS, QG limiter scaled
+  // its rates.
+  bool lc, li, lr, lv, ls, lg;
+  R fac, net_c, net_i, net_r, net_s, net_g;
   if constexpr (!OPT) {
-    fac = limiter(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw, dqc_dt);  // [QC]
-    if (fac != ONE) {
+    net_c = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;  // [QC]
+    fac = limiter(net_c, dqc_dt);
+    lc = !is_one(fac);
+    if (lc) {
       Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Pgacw *= fac;
     }
-    fac = limiter(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g, dqi_dt);  // [QI]
-    if (fac != ONE) {
+    net_i = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;  // [QI]
+    fac = limiter(net_i, dqi_dt);
+    li = !is_one(fac);
+    if (li) {
       Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
       Praci_s *= fac; Psaci *= fac; Praci_g *= fac;
     }
   } else {
-    fac = limiter(+Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Psfw - Pgacw, dqc_dt);  // [QC]
-    if (fac != ONE) {
+    net_c = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Psfw - Pgacw;  // [QC]
+    fac = limiter(net_c, dqc_dt);
+    lc = !is_one(fac);
+    if (lc) {
       Pimlt *= fac; Praut *= fac; Pracw *= fac; Pihom *= fac; Pihtr *= fac; Psacw *= fac; Psfw *= fac; Pgacw *= fac;
     }
-    fac = limiter(+Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Psfi - Praci_g - Pgaci,
-                  dqi_dt);  // [QI]
-    if (fac != ONE) {
+    net_i = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Psfi - Praci_g - Pgaci;  // [QI]
+    fac = limiter(net_i, dqi_dt);
+    li = !is_one(fac);
+    if (li) {
       Pigen *= fac; Pidep *= fac; Pihom *= fac; Pihtr *= fac; Pisub *= fac; Pimlt *= fac; Psaut *= fac;
       Praci_s *= fac; Psaci *= fac; Psfi *= fac; Praci_g *= fac; Pgaci *= fac;
     }
   }
-  fac = limiter(+Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz,
-                dqr_dt);  // [QR]
-  if (fac != ONE) {
+  net_r = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;  // [QR]
+  fac = limiter(net_r, dqr_dt);
+  lr = !is_one(fac);
+  if (lr) {
     Praut *= fac; Pracw *= fac; Psmlt *= fac; Pgmlt *= fac; Prevp *= fac; Piacr_s *= fac; Psacr_s *= fac;
     Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac;
   }
   fac = limiter(+Prevp + Pisub + Pssub + Pgsub - Pigen - Pidep - Psdep - Pgdep, dqv_dt);  // [QV]
-  if (fac != ONE) {
+  lv = !is_one(fac);
+  if (lv) {
     Prevp *= fac; Pisub *= fac; Pssub *= fac; Pgsub *= fac; Pigen *= fac; Pidep *= fac; Psdep *= fac; Pgdep *= fac;
   }
   if constexpr (!OPT) {
-    fac = limiter(+Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs, dqs_dt);  // [QS]
-    if (fac != ONE) {
+    net_s = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;  // [QS]
+    fac = limiter(net_s, dqs_dt);
+    ls = !is_one(fac);
+    if (ls) {
       Psdep *= fac; Psacw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac; Psaci *= fac;
       Pssub *= fac; Psmlt *= fac; Pracs *= fac;
     }
-    fac = limiter(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt, dqg_dt);  // [QG]
-    if (fac != ONE) {
+    net_g = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;  // [QG]
+    fac = limiter(net_g, dqg_dt);
+    lg = !is_one(fac);
+    if (lg) {
       Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
       Pracs *= fac; Pgsub *= fac; Pgmlt *= fac;
     }
   } else {
-    fac = limiter(+Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs -
-                      Pgacs,
-                  dqs_dt);  // [QS]
-    if (fac != ONE) {
+    net_s = +Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs - Pgacs;
+    fac = limiter(net_s, dqs_dt);  // [QS]
+    ls = !is_one(fac);
+    if (ls) {
       Psdep *= fac; Psacw *= fac; Psfw *= fac; Piacr_s *= fac; Psacr_s *= fac; Psaut *= fac; Praci_s *= fac;
       Psaci *= fac; Psfi *= fac; Pssub *= fac; Psmlt *= fac; Pracs *= fac; Pgacs *= fac;
     }
-    fac = limiter(+Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt,
-                  dqg_dt);  // [QG]
-    if (fac != ONE) {
+    net_g = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt;
+    fac = limiter(net_g, dqg_dt);  // [QG]
+    lg = !is_one(fac);
+    if (lg) {
       Pgdep *= fac; Pgacw *= fac; Piacr_g *= fac; Psacr_g *= fac; Pgacr *= fac; Pgfrz *= fac; Praci_g *= fac;
       Pgaci *= fac; Pracs *= fac; Pgacs *= fac; Pgsub *= fac; Pgmlt *= fac;
     }
   }
 
-  // tendencies, :1479-1559
-  R qc_t, qr_t, qi_t, qs_t, qg_t;
-  qr_t = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;
+  // tendencies, :1479-1559.  A species' net above stands unless a limiter at
+  // or after it scaled one of its rates: QC's by QC, QI, QR, QS, QG; QI's by
+  // QI, QV, QS, QG; QR's by QR, QV, QS, QG; QS's by QS, QG; QG's by QG.
+  R qc_t = net_c, qr_t = net_r, qi_t = net_i, qs_t = net_s, qg_t = net_g;
+  if (lr | lv | ls | lg) qr_t = +Praut + Pracw + Psmlt + Pgmlt - Prevp - Piacr_s - Psacr_s - Piacr_g - Psacr_g - Pgacr - Pgfrz;
   if constexpr (!OPT) {
-    qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;
-    qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;
-    qs_t = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
-    qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
+    if (lc | li | lr | ls | lg) qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Pgacw;
+    if (li | lv | ls | lg) qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Praci_g;
+    if (ls | lg) qs_t = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
+    if (lg) qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
   } else {
-    qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Psfw - Pgacw;
-    qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Psfi - Praci_g - Pgaci;
-    qs_t = +Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs - Pgacs;
-    qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt;
+    if (lc | li | lr | ls | lg) qc_t = +Pimlt - Praut - Pracw - Pihom - Pihtr - Psacw - Psfw - Pgacw;
+    if (li | lv | ls | lg)
+      qi_t = +Pigen + Pidep + Pihom + Pihtr - Pisub - Pimlt - Psaut - Praci_s - Psaci - Psfi - Praci_g - Pgaci;
+    if (ls | lg)
+      qs_t = +Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs - Pgacs;
+    if (lg) qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt;
   }
   qc_t = dmax(qc_t, -dqc_dt);
   qr_t = dmax(qr_t, -dqr_dt);

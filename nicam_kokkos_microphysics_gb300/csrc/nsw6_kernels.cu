@@ -253,8 +253,9 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
       P.zdis[((size_t)l * nrow + s) * KG + (size_t)k * G + g] = z;
     }
     // NaN never wins the reference's comparisons, so it is left out
-    unsigned long long kmx = (valid && z == z) ? order_key(z) : 0ull;
-    unsigned long long kmn = (valid && z == z) ? order_key(z) : ~0ull;
+    const bool use = valid && !is_nan_bits(z);
+    unsigned long long kmx = use ? order_key(z) : 0ull;
+    unsigned long long kmn = use ? order_key(z) : ~0ull;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const unsigned long long a = __shfl_xor_sync(0xffffffffu, kmx, o);
