@@ -114,6 +114,59 @@ __device__ __forceinline__ bool is_one(const T& x) { return x == T(1.0); }
 template <class T>
 __device__ __forceinline__ bool is_nonneg(const T& x) { return x >= T(0.0); }
 
+// Comparisons with constants (c > 0 normal, in lt_negc c < 0) and the
+// min / max they select, for doubles from the bit patterns on the integer pipe,
+// with the IEEE results for every double (false with NaN; -0 == +0); the
+// other types compare natively.
+__device__ __forceinline__ bool lt_z(double x) {   // x < 0
+  return (unsigned long long)fp_bits(x) - 0x8000000000000001ull < 0x7FF0000000000000ull;
+}
+__device__ __forceinline__ bool gt_z(double x) {   // x > 0
+  const long long b = fp_bits(x);
+  return b > 0 && b <= FP_INF;
+}
+__device__ __forceinline__ bool ge_c(double x, double c) {
+  const long long b = fp_bits(x);
+  return b >= fp_bits(c) && b <= FP_INF;
+}
+__device__ __forceinline__ bool gt_c(double x, double c) {
+  const long long b = fp_bits(x);
+  return b > fp_bits(c) && b <= FP_INF;
+}
+__device__ __forceinline__ bool le_c(double x, double c) {
+  const long long b = fp_bits(x);
+  return b <= fp_bits(c) && (b & FP_ABS) <= FP_INF;
+}
+__device__ __forceinline__ bool lt_negc(double x, double c) {
+  const long long b = fp_bits(x), m = b & FP_ABS;
+  return b < 0 && m > (fp_bits(c) & FP_ABS) && m <= FP_INF;
+}
+__device__ __forceinline__ double maxz(double x) { return lt_z(x) ? 0.0 : x; }                // max(x, 0)
+__device__ __forceinline__ double maxc(double x, double c) { return fp_lt_pos(x, c) ? c : x; }   // max(x, c)
+__device__ __forceinline__ double minc(double x, double c) { return gt_c(x, c) ? c : x; }       // min(x, c)
+template <class T>
+__device__ __forceinline__ bool lt_z(const T& x) { return x < T(0.0); }
+template <class T>
+__device__ __forceinline__ bool gt_z(const T& x) { return x > T(0.0); }
+template <class T>
+__device__ __forceinline__ bool ge_c(const T& x, const T& c) { return x >= c; }
+template <class T>
+__device__ __forceinline__ bool gt_c(const T& x, const T& c) { return x > c; }
+template <class T>
+__device__ __forceinline__ bool le_c(const T& x, const T& c) { return x <= c; }
+template <class T>
+__device__ __forceinline__ bool lt_negc(const T& x, const T& c) { return x < c; }
+template <class T>
+__device__ __forceinline__ T maxz(const T& x) { return dmax(x, T(0.0)); }
+__device__ __forceinline__ bool is_zero(double x) { return fp_is_zero(x); }
+template <class T>
+__device__ __forceinline__ bool is_zero(const T& x) { return x == T(0.0); }
+__device__ __forceinline__ double rate_on(double x) { return maxz(x); }
+template <class T>
+__device__ __forceinline__ T maxc(const T& x, const T& c) { return dmax(x, c); }
+template <class T>
+__device__ __forceinline__ T minc(const T& x, const T& c) { return dmin(x, c); }
+
 // R = double: the plain FP64 step.  R = float (the mixed path): saturation
 // values, process rates, limiters, tendencies, fall speeds and effective radii
 // in FP32; the negative filter, the tracer and internal-energy budgets
@@ -135,13 +188,13 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
 #pragma unroll
   for (int n = 2; n <= 5; ++n) {
     diffq += rq[n];
-    rq[n] = dmax(rq[n], D(0.0));
+    rq[n] = maxz(rq[n]);
   }
 #pragma unroll
   for (int n = 2; n <= 5; ++n) diffq -= rq[n];
   rq[I_QV] += diffq;
   diffq = rq[I_QV];
-  rq[I_QV] = dmax(rq[I_QV], D(0.0));
+  rq[I_QV] = maxz(rq[I_QV]);
   diffq -= rq[I_QV];
   const D rhog = in.rhog * (1.0 - diffq);
   const D rrhog = 1.0 / rhog;
@@ -162,7 +215,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
 
   // ---- psat / qsat (CPovR = 0 under EIN_TYPE "SIMPLE": the power term is 1)
   const R tempR = R(temp), densR = R(dens);
-  const R rtem = R(1.0) / dmax(tempR, R(TEM_MIN));
+  const R rtem = R(1.0) / maxc(tempR, R(TEM_MIN));
   const R psatl = R(PSAT0) * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
   const R psati = R(PSAT0) * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
   const R rdrt = R(1.0) / (densR * R(RVAP) * tempR);
@@ -171,17 +224,17 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
 
   // ---- TagBigLoop, mod_mp_nsw6.cpp:902-1594
   const R Z = R(0.0), ONE = R(1.0);
-  const R qv = dmax(R(qn[0]), Z), qc = dmax(R(qn[1]), Z), qr = dmax(R(qn[2]), Z);
-  const R qi = dmax(R(qn[3]), Z), qs = dmax(R(qn[4]), Z), qg = dmax(R(qn[5]), Z);
-  const R Sliq = qv / dmax(qsatl, R(EPS));
-  const R Sice = qv / dmax(qsati, R(EPS));
+  const R qv = maxz(R(qn[0])), qc = maxz(R(qn[1])), qr = maxz(R(qn[2]));
+  const R qi = maxz(R(qn[3])), qs = maxz(R(qn[4])), qg = maxz(R(qn[5]));
+  const R Sliq = qv / maxc(qsatl, R(EPS));
+  const R Sice = qv / maxc(qsati, R(EPS));
   const R Rdens = ONE / densR;
   const R rho_fact = sqrtR(R(DENS00) * Rdens);
   const R temc = tempR - R(TEM00);
-  const bool warm = !(temc < Z);  // iceflg = 0.5 - copysign(0.5, temc) == 0
-  const bool d1 = (qr >= R(1.0E-4));                          // delta1
-  const bool d2 = (R(1.0E-4) >= qr && R(1.0E-4) >= qs);       // delta2
-  const bool sps = (Sice >= ONE);                              // spsati
+  const bool warm = !lt_z(temc);  // iceflg = 0.5 - copysign(0.5, temc) == 0
+  const bool d1 = ge_c(qr, R(1.0E-4));                          // delta1
+  const bool d2 = le_c(qr, R(1.0E-4)) && le_c(qs, R(1.0E-4));       // delta2
+  const bool sps = ge_c(Sice, ONE);                              // spsati
   const R dqv_dt = per_dt(qv, dtR, rdtR), dqc_dt = per_dt(qc, dtR, rdtR), dqr_dt = per_dt(qr, dtR, rdtR);
   const R dqi_dt = per_dt(qi, dtR, rdtR), dqs_dt = per_dt(qs, dtR, rdtR), dqg_dt = per_dt(qg, dtR, rdtR);
 
@@ -191,7 +244,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   // The cell kernel groups cells by species so that whole warps skip them.
 
   // rain slope parameter, :953-967
-  const bool rain = (qr >= R(1.0E-12));
+  const bool rain = ge_c(qr, R(1.0E-12));
   R RLMDr = Z, RLMDr_dr = Z, RLMDr_2 = Z, RLMDr_3 = Z, RLMDr_1br = Z, RLMDr_2br = Z, RLMDr_3br = Z, RLMDr_7 = Z;
   R RLMDr_3dr = Z, RLMDr_5dr = Z, RLMDr_6dr = Z;
   if (rain) {
@@ -213,7 +266,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   // polynomials in tems whose coefficients per moment are folded on the host.
   const R Xs2 = densR * qs * C.rAs;
   const bool roh = !OPT || C.opt_roh != Z;
-  const bool snow = roh && (Xs2 >= R(1.0E-12));
+  const bool snow = roh && ge_c(Xs2, R(1.0E-12));
   R mom[7] = {Z, Z, Z, Z, Z, Z, Z};  // MOMs_0, _1, _0bs, _1bs, _2bs, _2ds (= nm 2.25), _5ds_h
   R RMOMs_Vt = Z;
   R MOMs_2 = Xs2;
@@ -222,7 +275,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     // RLMDs = (dens qs / (As N0s GAM_1bs))^(1/4) and integer powers as products
     if (!roh) {
       MOMs_2 = Z;
-      if (qs >= R(1.0E-12)) {
+      if (ge_c(qs, R(1.0E-12))) {
         const R s1 = sqrtR(sqrtR(densR * qs * C.K_rlmds));
         const R ds = sqrtR(sqrtR(s1));
         const R s2 = s1 * s1, s3 = s2 * s1, s4 = s2 * s2, s5 = s4 * s1, s6 = s3 * s3;
@@ -239,7 +292,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     }
   }
   if (snow) {
-    const R tems = dmin(R(-0.1), temc);
+    const R tems = lt_negc(temc, R(-0.1)) ? temc : R(-0.1);   // min(-0.1, temc)
     const R logX = mth.log(Xs2);
 #pragma unroll
     for (int i = 0; i < 7; ++i) {
@@ -256,7 +309,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   const R MOMs_5ds_h = mom[6];
 
   // graupel slope parameter, :1059-1066
-  const bool graupel = (qg >= R(1.0E-12));
+  const bool graupel = ge_c(qg, R(1.0E-12));
   R RLMDg = Z, RLMDg_dg = Z, RLMDg_2 = Z, RLMDg_3 = Z, RLMDg_3dg = Z, RLMDg_5dg = Z;
   if (graupel) {
     RLMDg = sqrtR(sqrtR(densR * qg * C.K_rlmdg));
@@ -284,15 +337,15 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
 
   // nucleation, :1080-1085: Ni0 = max(exp(-0.1 temc), 1) * 1000 and
   // Qi0 = ice_nuc * Ni0^1.33 / dens, with log(Ni0) = ln 1000 + max(-0.1 temc, 0)
-  const R Qi0 = C.ice_nuc * mth.exp(R(1.33) * (C.ln1000 + dmax(R(-0.1) * temc, Z))) * Rdens;
-  R Pigen = dmax(dmin(Qi0 - qi, qv - qsati), Z) * rdtR;
+  const R Qi0 = C.ice_nuc * mth.exp(R(1.33) * (C.ln1000 + maxz(R(-0.1) * temc))) * Rdens;
+  R Pigen = maxz(dmin(Qi0 - qi, qv - qsati)) * rdtR;
 
   // accretion, :1087-1145
   // Esi_mod and betai, :1089, :1162: min(E, E exp(0.06 temc)) is E when temc >= 0
   // (exp >= 1 there) and E >= 0; both use the same exponential when
   // gamma_sacr == gamma_saut (both 6e-2 in this configuration).
   R Esi_mod = C.Esi, betai = C.beta_saut;
-  if (!(warm && C.Esi >= Z && C.beta_saut >= Z)) {
+  if (!(warm && is_nonneg(C.Esi) && is_nonneg(C.beta_saut))) {
     const R eg = mth.exp(C.gamma_sacr * temc);
     const R eb = (C.gamma_saut == C.gamma_sacr) ? eg : mth.exp(C.gamma_saut * temc);
     Esi_mod = dmin(C.Esi, C.Esi * eg);
@@ -303,7 +356,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   const R qcqr = qc * qr;
   R Pracw = Z;
   if (kk) {
-    if (qcqr >= R(1.0E-12)) Pracw = R(67.0) * mth.pow(qcqr, R(1.15));
+    if (ge_c(qcqr, R(1.0E-12))) Pracw = R(67.0) * mth.pow(qcqr, R(1.15));
   } else {
     Pracw = qc * C.K_raci * RLMDr_3dr * fr;   // Pracw_orig (Erw = Eri = 1)
   }
@@ -335,7 +388,7 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     if constexpr (OPT) {
       if (C.opt_indir != Z) K_aut = C.kk_aut * mth.pow(Nc, R(-1.79));
     }
-    if (qc > Z) Praut = K_aut * mth.pow(qc, R(2.47));
+    if (gt_z(qc)) Praut = K_aut * mth.pow(qc, R(2.47));
   } else {
     // Berry (1968), :1145-1147
     R Dc = C.Dc_berry;
@@ -359,37 +412,37 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     const R xl = KdD * qsatl;
     const R Glv = xl / (R(LHV0) * rKaT * (C.LovR_liq * rtem - ONE) * xl + ONE);
     const R ventr = C.K_ventr1 * RLMDr_2 + C.K_ventr2 * sqrtR(C.Cr * fr * rNu * RLMDr_5dr);
-    Prevp = C.K_revp * Rdens * (ONE - dmin(Sliq, ONE)) * Glv * ventr;
+    Prevp = C.K_revp * Rdens * (ONE - minc(Sliq, ONE)) * Glv * ventr;
   }
-  const R rhoqi = dmax(densR * qi, R(EPS));
+  const R rhoqi = maxc(densR * qi, R(EPS));
   // with no ice, rhoqi = EPS and XNi, Di take the constant values folded on the host
   R XNi = C.XNi_eps, Di = C.Di_eps;
-  if (rhoqi > R(EPS)) {
-    XNi = dmin(dmax(R(5.38E+7) * mth.pow(rhoqi, R(0.75)), R(1.0E+3)), R(1.0E+6));
+  if (gt_c(rhoqi, R(EPS))) {
+    XNi = minc(maxc(R(5.38E+7) * mth.pow(rhoqi, R(0.75)), R(1.0E+3)), R(1.0E+6));
     const R XMi = rhoqi / XNi;
-    Di = dmin(C.Di_a * sqrtR(XMi), C.Di_max);
+    Di = minc(C.Di_a * sqrtR(XMi), C.Di_max);
   }
   R tmp = R(4.0) * Di * XNi * Rdens * (Sice - ONE) * Giv;
   R Pidep = sel(sps, tmp);
   R Pisub = sel(!sps, -tmp);
-  const bool below40 = (temc + R(40.0) < Z);
+  const bool below40 = lt_z(temc + R(40.0));
   R Pihom = below40 ? dqc_dt : Z;
   const R efrz = mth.exp(-C.A_frz * temc) - ONE;
   R Pihtr = (!below40 && !warm) ? densR * (qc * qc) * C.K_ihtr * efrz : Z;
   R Pimlt = warm ? dqi_dt : Z;
   // ventilation of snow and graupel: without the species their moments /
   // slope terms are exact zeros and so is the sum (+0, skipped with its root)
-  const R vents = (MOMs_1 == Z && MOMs_5ds_h == Z) ? Z : R(0.65) * MOMs_1 + C.K_vents2 * sqrtR(fr * rNu) * MOMs_5ds_h;
+  const R vents = (is_zero(MOMs_1) && is_zero(MOMs_5ds_h)) ? Z : R(0.65) * MOMs_1 + C.K_vents2 * sqrtR(fr * rNu) * MOMs_5ds_h;
   tmp = C.K_2pi * Rdens * (Sice - ONE) * Giv * vents;
   R Psdep = sel(sps, tmp);
   R Pssub = sel(!sps, -tmp);
-  R Psmlt = dmax(C.K_2pi * Rdens * Gil * vents + C.K_clf * temc * (Psacw + Psacr), Z);
-  const R ventg = (RLMDg_2 == Z && RLMDg_5dg == Z) ? Z
+  R Psmlt = maxz(C.K_2pi * Rdens * Gil * vents + C.K_clf * temc * (Psacw + Psacr));
+  const R ventg = (is_zero(RLMDg_2) && is_zero(RLMDg_5dg)) ? Z
                                                   : C.K_ventg1 * RLMDg_2 + C.K_ventg2 * sqrtR(C.Cg * fr * rNu * RLMDg_5dg);
   tmp = C.K_gdep * Rdens * (Sice - ONE) * Giv * ventg;
   R Pgdep = sel(sps, tmp);
   R Pgsub = sel(!sps, -tmp);
-  R Pgmlt = dmax(C.K_gdep * Rdens * Gil * ventg + C.K_clf * temc * (Pgacw + Pgacr), Z);
+  R Pgmlt = maxz(C.K_gdep * Rdens * Gil * ventg + C.K_clf * temc * (Pgacw + Pgacr));
   R Pgfrz = C.K_gfrz * Rdens * efrz * RLMDr_7;
 
   // Bergeron process (:1239-1247) with Bergeron_param (:1834-1890); it
@@ -605,13 +658,13 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
     const R r3_qc = C.coef_xf * densR * qc;
     const R r3_qr = C.coef_xf * densR * qr;
     const R r2 = r2_qc + r2_qr;
-    const bool big = (r2 >= r2_min);
+    const bool big = ge_c(r2, r2_min);
     const R rceff = big ? (r3_qc + r3_qr) / r2 : Z;
-    const bool top = !big && ((qc + qr) >= q_min);
+    const bool top = !big && ge_c(qc + qr, q_min);
     o.rceff = D(rceff);
     o.rctop = top ? D(rceff) : D(UNDEF);
     o.tctop = top ? temp : D(UNDEF);
-    o.rceff_cld = (r2_qc >= r2_min) ? D(r3_qc / r2_qc) : D(0.0);
+    o.rceff_cld = ge_c(r2_qc, r2_min) ? D(r3_qc / r2_qc) : D(0.0);
   }
 
   // ---- TagUpdateRHOGQ / RHOGE / MassConc / TEM, mod_mp_nsw6.cpp:692-744
