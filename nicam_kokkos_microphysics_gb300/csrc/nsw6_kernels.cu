@@ -127,9 +127,9 @@ __global__ void __launch_bounds__(CELL_THREADS, 2) nsw6_cell_kernel(Problem P, C
       int kk = 32;   // columns past the region's end go last
       if (g < G) {
         const size_t iq = offq + (size_t)k * G + g;
-        kk = (P.rhogq[iq + (size_t)I_QS * KG] > 0.0 ? 16 : 0) | (P.rhogq[iq + (size_t)I_QR * KG] > 0.0 ? 8 : 0) |
-             (P.rhogq[iq + (size_t)I_QG * KG] > 0.0 ? 4 : 0) | (P.rhogq[iq + (size_t)I_QI * KG] > 0.0 ? 2 : 0) |
-             (P.rhogq[iq + (size_t)I_QC * KG] > 0.0 ? 1 : 0);
+        kk = (gt_z(P.rhogq[iq + (size_t)I_QS * KG]) ? 16 : 0) | (gt_z(P.rhogq[iq + (size_t)I_QR * KG]) ? 8 : 0) |
+             (gt_z(P.rhogq[iq + (size_t)I_QG * KG]) ? 4 : 0) | (gt_z(P.rhogq[iq + (size_t)I_QI * KG]) ? 2 : 0) |
+             (gt_z(P.rhogq[iq + (size_t)I_QC * KG]) ? 1 : 0);
       }
       key[c] = (unsigned char)kk;
       atomicAdd(&bucket[kk], 1);
@@ -499,9 +499,12 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
   }
   q[I_QV] = qsum;
   q[I_QC] = 0.0;
+  // q[QC] (and q[QI] in satadjust_all) is +0 now: its terms leave the sums
+  // below as they are (no partial sum is -0), so they are not formed
   double cvtot = qd * CVDRY;
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) cvtot = cvtot + q[n] * CVDRY;
+  for (int n = 2; n <= 5; ++n)
+    if (n != I_QI || !ice_adj) cvtot = cvtot + q[n] * CVDRY;
   const double rho_l = rho;
   double tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
   if (interior) {
@@ -509,7 +512,8 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
     // (:620-769)
     double qd_l = 1.0;
 #pragma unroll
-    for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
+    for (int n = 2; n <= 5; ++n)
+      if (n != I_QI || !ice_adj) qd_l = qd_l - q[n];
     if (newton) {
       tem = satadjust_newton(P, C, mth, ice_adj, tem, ein_moist, qsum, rho_l, qd_l, q, k, g, l);
     } else {
@@ -574,15 +578,16 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
 #pragma unroll
     for (int n = 2; n <= 5; ++n) {
       diffq += rq[n];
-      if (rq[n] < 0.0) clamped |= 1u << n;   // rq[n] = max(rq[n], 0)
-      rq[n] = dmax(rq[n], 0.0);
+      if (lt_z(rq[n])) clamped |= 1u << n;
+      rq[n] = maxz(rq[n]);
     }
 #pragma unroll
     for (int n = 2; n <= 5; ++n) diffq -= rq[n];
     rq[I_QV] += diffq;
     diffq = rq[I_QV];
-    rq[I_QV] = dmax(rq[I_QV], 0.0);
+    rq[I_QV] = maxz(rq[I_QV]);
     diffq -= rq[I_QV];
+    double qdf, cva;
     if (fp_is_zero(diffq) && fp_pos_normal(rhog)) {
       // Nothing removed: rhog (1 - diffq) is rhog exactly, and so are
       // rho = rhog / gsg and the reciprocal formed above.  The quotients of
@@ -593,19 +598,29 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
 #pragma unroll
       for (int n = 1; n <= 5; ++n)
         if (!((same >> n) & 1u)) q[n] = MIX ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
+      // an unsaturated cell's q[QC] (and q[QI] in satadjust_all) is still +0
+      const unsigned zero = newton ? 0u : (ice_adj ? 0x0Au : 0x02u);
+      qdf = 1.0;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n)
+        if (!((zero >> n) & 1u)) qdf = qdf - q[n];
+      cva = qdf * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n)
+        if (!((zero >> n) & 1u)) cva = cva + q[n] * CVDRY;
     } else {
       rhog_o = rhog * (1.0 - diffq);
       rho = rhog_o / gsg;
       const double rrhog_o = 1.0 / rhog_o;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) q[n] = MIX ? rq[n] * rrhog_o : div_rn(rq[n], rhog_o, rrhog_o);
+      qdf = 1.0;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
+      cva = qdf * CVDRY;
+#pragma unroll
+      for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
     }
-    double qdf = 1.0;
-#pragma unroll
-    for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
-    double cva = qdf * CVDRY;
-#pragma unroll
-    for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
     rhoge = tem * rhog_o * cva;
     pre = rho * (qdf * RDRY + q[I_QV] * RVAP) * tem;
   }
@@ -764,9 +779,13 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const size_t i = off + (size_t)k * G + g;
     const size_t ic = (size_t)l * G + g;
     const bool interior = (k >= kmin && k <= kmax);
-    // gam2 / gsgam2 and afact / gsgam2 from one reciprocal, correctly rounded
-    const double rgsg = 1.0 / P.gsgam2[i];
-    if (interior) F(S_RGS)[c] = div_rn(P.gam2[i], P.gsgam2[i], rgsg);
+    // gam2 / gsgam2, afact / gsgam2 and (below) the level above's bfact /
+    // gsgam2 from one reciprocal, correctly rounded; the reciprocal waits in
+    // S_BASE (free until the transport) for that level
+    const double gsg = P.gsgam2[i];
+    const double rgsg = 1.0 / gsg;
+    F(S_BASE)[c] = rgsg;
+    if (interior) F(S_RGS)[c] = div_rn(P.gam2[i], gsg, rgsg);
     const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
     F(S_VI)[c] = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
     F(S_VJ)[c] = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
@@ -775,14 +794,23 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       F(S_KINH)[c] = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / P.rhog[i];
     }
     if (k >= kmin + 1 && k <= kmax) {
-      const double c2w0 = div_rn(afact[k], P.gsgam2[i], rgsg) * P.gsgam2h[i];
-      const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
-      const double rw = P.rhogw[i];
-      F(S_KINV)[c] = 0.5 * (rw * rw) / (c2w0 * P.rhog[i] + c2w1 * P.rhog[i - G]);
-      r_c2w0[j] = c2w0;
-      r_c2w1[j] = c2w1;
+      r_c2w0[j] = div_rn(afact[k], gsg, rgsg) * P.gsgam2h[i];
       r_rgsh[j] = P.gam2h[i] / P.gsgam2h[i];
     }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < NJ; ++j) {
+    const int c = threadIdx.x + j * blockDim.x;
+    if (c >= ncell) continue;
+    const int k = c / COL_TG, g = g0 + c % COL_TG;
+    if (g >= G || k < kmin + 1 || k > kmax) continue;
+    const size_t i = off + (size_t)k * G + g;
+    const double c2w0 = r_c2w0[j];
+    const double c2w1 = div_rn(bfact[k], P.gsgam2[i - G], F(S_BASE)[c - COL_TG]) * P.gsgam2h[i];
+    const double rw = P.rhogw[i];
+    F(S_KINV)[c] = 0.5 * (rw * rw) / (c2w0 * P.rhog[i] + c2w1 * P.rhog[i - G]);
+    r_c2w1[j] = c2w1;
   }
   __syncthreads();
 
