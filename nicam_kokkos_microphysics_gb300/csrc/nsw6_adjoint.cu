@@ -906,6 +906,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     const double rrhog = 1.0 / rhog;
     const double rhoge_a = W(W_RHOGE_N, c);
     const double gsg = gs[c];
+    const double rgsg = 1.0 / gsg;   // the reciprocals of gsgam2 at k - 1, k, k + 1 serve both sweeps
+    double rg_up = 0.0, rg_dn = 0.0;
     double rhoge = rhoge_a;
     // KIN2EIN pieces
     double gh = 0, rgh = 0, w2c0 = 0, w2c1 = 0, kinh = 0, kvp = 0, kv0 = 0, rvx = 0, rvy = 0, rvz = 0, tmp_h = 0;
@@ -930,8 +932,12 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
         hv[s2] = (j >= kmin + 1 && j <= kmax);
         if (!hv[s2]) continue;
         const double ghj = gsh[cj];
-        c2a[s2] = afact[j] / gs[cj] * ghj;
-        c2b[s2] = bfact[j] / gs[cj - G] * ghj;
+        // afact / gs(j) and bfact / gs(j-1), correctly rounded, from the reciprocals
+        if (s2 == 0) rg_up = 1.0 / gs[cj];
+        else rg_dn = 1.0 / gs[cj - G];
+        const double rgj = s2 == 0 ? rg_up : rgsg, rgjm = s2 == 0 ? rgsg : rg_dn;
+        c2a[s2] = div_rn(afact[j], gs[cj], rgj) * ghj;
+        c2b[s2] = div_rn(bfact[j], gs[cj - G], rgjm) * ghj;
         rwj[s2] = W(W_RW_N, cj);
         den[s2] = c2a[s2] * W(W_RHOG_N, cj) + c2b[s2] * W(W_RHOG_N, cj - G);
         kvu[s2] = 0.5 * (rwj[s2] * rwj[s2]) / den[s2];
@@ -979,21 +985,26 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
       double tv = tem;
-      double rtem = 1.0 / (dmax(tv, TEM_MIN));
-      double psat = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
-      double qsat = psat / (rho1 * RVAP * tv);
-      if (qsum - qsat > EPS) {
+      // the test decided in FP32 where its margin allows (sat_screen_liq)
+      int sc = sat_screen_liq(tv, rho1, qsum, float(C.LovR_liq));
+      if (sc < 0) {
+        const double rtem0 = 1.0 / fp_max_pos(tv, TEM_MIN);
+        const double psat0 = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem0));
+        sc = (qsum - psat0 / (rho1 * RVAP * tv) > EPS) ? 1 : 0;
+      }
+      if (sc) {
         double qv[6];
 #pragma unroll
         for (int n = 0; n < 6; ++n) qv[n] = q[n];
         bool converged = false;
-        double tprev = tv;
+        double tprev = tv, qs_last = 0.0;
         int ite;
         for (ite = 0; ite < P.itelim; ++ite) {
           tprev = tv;
-          rtem = 1.0 / (dmax(tv, TEM_MIN));
-          psat = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
-          qsat = psat / (rho1 * RVAP * tv);
+          const double rtem = 1.0 / fp_max_pos(tv, TEM_MIN);
+          const double psat = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem));
+          const double qsat = psat / (rho1 * RVAP * tv);
+          qs_last = qsat;
           qv[I_QV] = qsat;
           qv[I_QC] = qsum - qsat;
           double cv = qd_l * CVDRY;
@@ -1004,11 +1015,11 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
           const double demoist_dT = cv + dqsat_dT * LHV0;
           const double dtemp = (emoist_new - ein_moist) / demoist_dT;
           tv = tv - dtemp;
-          if (fabs(dtemp) < C.dtemp_criteria) {
+          if (fp_abs_lt(dtemp, C.dtemp_criteria)) {
             converged = true;
             break;
           }
-          if (tv * 0.0 != 0.0) break;
+          if (fp_not_finite(tv)) break;
         }
         tem = tv;
         q[I_QV] = qv[I_QV];
@@ -1016,7 +1027,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
         if (converged) {
           sat = true;
           ts = tprev;
-          qsT = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - 1.0 / dmax(ts, TEM_MIN))) / (rho1 * RVAP * ts);
+          qsT = qs_last;   // qsat at the last iterate ts, as the iteration formed it
           cvT = qd_l * CVDRY + (qsum - qsT) * CVDRY;
 #pragma unroll
           for (int n = 2; n <= 5; ++n) cvT = cvT + q[n] * CVDRY;
@@ -1024,7 +1035,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
           dqs = qsT * (C.LovR_liq * rts * rts - rts);
           FT = cvT - ts * dqs * CVDRY + dqs * LHV0;
         } else {
-          record_err(P.status, (tv * 0.0 != 0.0) ? 4 : 3, k, g, l, ite);
+          record_err(P.status, fp_not_finite(tv) ? 4 : 3, k, g, l, ite);
         }
       }
     }
@@ -1049,21 +1060,31 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
 #pragma unroll
       for (int n = 2; n <= 5; ++n) {
         diffq += rqf[n];
-        clip[n] = rqf[n] < 0.0;
+        clip[n] = lt_z(rqf[n]);
         rqf[n] = clip[n] ? 0.0 : rqf[n];
       }
 #pragma unroll
       for (int n = 2; n <= 5; ++n) diffq -= rqf[n];
       rqf[0] += diffq;
       d2 = rqf[0];
-      clip[0] = rqf[0] < 0.0;
+      clip[0] = lt_z(rqf[0]);
       rqf[0] = clip[0] ? 0.0 : rqf[0];
       d2 -= rqf[0];
-      rhog_o = rhog * (1.0 - d2);
-      rho_f = rhog_o / gsg;
-      rrhog_o = 1.0 / rhog_o;
+      if (fp_is_zero(d2) && fp_pos_normal(rhog)) {
+        // nothing removed: rhog (1 - d2) = rhog exactly, rho_f = rho1 and the
+        // reciprocal as above, and the quotients of the tracers the filter left
+        // as they were are q's (q[QC] is +0 unless the iteration ran)
+        rho_f = rho1;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n) qf[n] = div_rn(rqf[n], rhog_o, rrhog_o);
+        for (int n = 1; n <= 5; ++n)
+          if (n == I_QC ? fp_bits(q[I_QC]) != 0 : clip[n]) qf[n] = div_rn(rqf[n], rhog, rrhog);
+      } else {
+        rhog_o = rhog * (1.0 - d2);
+        rho_f = rhog_o / gsg;
+        rrhog_o = 1.0 / rhog_o;
+#pragma unroll
+        for (int n = 1; n <= 5; ++n) qf[n] = div_rn(rqf[n], rhog_o, rrhog_o);
+      }
       qdf = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qdf = qdf - qf[n];
@@ -1074,7 +1095,6 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     }
     // ------------------------------------------------------------ reverse
     // (divisions by reciprocals: the adjoint's coefficients need no correct rounding)
-    const double rgsg = 1.0 / gsg;
     const double* SB = io.SB;
     double b_tem = SB[SF_TEM * NC + c];
     double b_qd = SB[SF_QD * NC + c];
@@ -1241,7 +1261,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
         WBadd(W_RHOG_N, cj - G, b_den * c2b[s2]);
         const double b_c2a = b_den * W(W_RHOG_N, cj), b_c2b = b_den * W(W_RHOG_N, cj - G);
         // c2a = (afact / gs(j)) gsh(j), c2b = (bfact / gs(j-1)) gsh(j)
-        const double rgj = 1.0 / gs[cj], rgjm = 1.0 / gs[cj - G];
+        const double rgj = s2 == 0 ? rg_up : rgsg, rgjm = s2 == 0 ? rgsg : rg_dn;
         XBadd(A_gsgam2h, cj, b_c2a * (afact[j] * rgj) + b_c2b * (bfact[j] * rgjm));
         XBadd(A_gsgam2, cj, -b_c2a * c2a[s2] * rgj);
         XBadd(A_gsgam2, cj - G, -b_c2b * c2b[s2] * rgjm);

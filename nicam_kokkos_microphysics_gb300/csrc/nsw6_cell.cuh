@@ -167,6 +167,33 @@ __device__ __forceinline__ T maxc(const T& x, const T& c) { return dmax(x, c); }
 template <class T>
 __device__ __forceinline__ T minc(const T& x, const T& c) { return dmin(x, c); }
 
+// The liquid saturation test qsum - qsat(T) > EPS of the saturation
+// adjustment (mod_satadjust.cpp:771-896), decided in FP32 where its margin
+// allows: 1 saturated, 0 not, -1 left to the FP64 test.  Three conversions
+// (T, rho, qsum): an FP64 compare or conversion costs as much of the FP64
+// pipe as an FMA.  x = LovR (1/T00 - 1/T) is formed as LovR (Tf - T00f) /
+// (Tf T00f): the difference is exact, so x carries seven roundings
+// (4.2e-7 |x|) and the conversions of T and T00 (LovR u (1/T00 + 1/T) <=
+// 7.2e-6 for |x| <= 80, u = 2^-24); with expf's 2 ulp and eight roundings
+// after it the FP32 qsat is within 4.2e-5 (relative) of the FP64 one, and
+// qsum rounds by u.  So qsum_f > 1.0001 qsat_f means qsum > (1 + 5.7e-5) qsat,
+// and with qsat_f >= 1e-11 the FP64 difference exceeds EPS; qsum_f <
+// 0.9999 qsat_f means qsum < qsat.  Cells in between and outside those ranges
+// (and NaNs) are left to the FP64 test, as the reference computes it.
+// lovr_f = float(LovR_liq).
+__device__ __forceinline__ int sat_screen_liq(double tem, double rho, double qsum, float lovr_f) {
+  const float tf = float(tem);
+  const float tcf = (tf < float(TEM_MIN)) ? float(TEM_MIN) : tf;   // float(max(tem, TEM_MIN))
+  const float xf = lovr_f * ((tcf - float(TEM00)) / (tcf * float(TEM00)));
+  if (!(fabsf(xf) <= 80.0f)) return -1;
+  const float qsf = (float(PSAT0) * expf(xf)) / (float(rho) * float(RVAP) * tf);
+  if (!(qsf >= 1.0e-11f && qsf <= 1.0e30f)) return -1;
+  const float qq = float(qsum);
+  if (qq > qsf * 1.0001f) return 1;
+  if (qq < qsf * 0.9999f) return 0;
+  return -1;
+}
+
 // R = double: the plain FP64 step.  R = float (the mixed path): saturation
 // values, process rates, limiters, tendencies, fall speeds and effective radii
 // in FP32; the negative filter, the tracer and internal-energy budgets

@@ -519,32 +519,8 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
     } else {
     // is the cell saturated?
     // The test qsum - qsat(tem) > EPS is first decided in FP32 (liquid
-    // saturation only), from three conversions (T, rho, qsum): an FP64
-    // compare or conversion costs as much of the FP64 pipe as an FMA.
-    // x = LovR (1/T00 - 1/T) is formed as LovR (Tf - T00f) / (Tf T00f): the
-    // difference is exact, so x carries seven roundings (4.2e-7 |x|) and the
-    // conversions of T and T00 (LovR u (1/T00 + 1/T) <= 7.2e-6 for |x| <= 80,
-    // u = 2^-24); with expf's 2 ulp and eight roundings after it the FP32
-    // qsat is within 4.2e-5 (relative) of the FP64 one.  qsum rounds by u.
-    // So qsum_f > 1.0001 qsat_f means qsum > (1 + 5.7e-5) qsat, and with
-    // qsat_f >= 1e-11 the FP64 difference exceeds EPS; qsum_f < 0.9999 qsat_f
-    // means qsum < qsat.  The FP64 test decides the cells in between and
-    // outside those ranges, as the reference computes it.  Only the branch
-    // depends on qsat here: a saturated cell's Newton iteration recomputes it.
-    int sat = -1;
-    if (!ice_adj) {
-      const float tf = float(tem);
-      const float tcf = (tf < float(TEM_MIN)) ? float(TEM_MIN) : tf;   // float(max(tem, TEM_MIN))
-      const float xf = lovr_f * ((tcf - float(TEM00)) / (tcf * float(TEM00)));
-      if (fabsf(xf) <= 80.0f) {
-        const float qsf = (float(PSAT0) * expf(xf)) / (float(rho_l) * float(RVAP) * tf);
-        if (qsf >= 1.0e-11f && qsf <= 1.0e30f) {
-          const float qq = float(qsum);
-          if (qq > qsf * 1.0001f) sat = 1;
-          else if (qq < qsf * 0.9999f) sat = 0;
-        }
-      }
-    }
+    // saturation only, sat_screen_liq); the FP64 test decides the rest.
+    int sat = ice_adj ? -1 : sat_screen_liq(tem, rho_l, qsum, lovr_f);
     if (sat < 0) {
       const double rtem = 1.0 / fp_max_pos(tem, TEM_MIN);
       double psat = PSAT0 * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
