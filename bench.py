@@ -59,19 +59,23 @@ CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
 # cells): DRAM bytes read + written, and the FP64 thread instructions the
 # kernel executes -- DFMA, DADD, DMUL and all instructions of the FP64 pipe
 # (compares, min/max and conversions included) -- per interior cell (cell
-# kernel) or per cell (column kernel).
-CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 215.8, "mixed": 172.4}
-COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 374.6, "mixed": 383.8}
+# kernel) or per cell (column phase).  The column phase is nsw6_column_kernel
+# and nsw6_satadj_kernel (the saturated cells), timed together as one
+# interval; its figures are the two kernels' sums.
+CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 214.8, "mixed": 172.4}
+COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 379.6 + 30.1, "mixed": 399.1 + 30.1}
 FP64_EXECUTED = {
-    "nsw6_cell_kernel": {"fp64": {"dfma": 353.9, "dadd": 277.9, "dmul": 273.0, "pipe": 1015.7},
-                         "mixed": {"dfma": 29.0, "dadd": 58.0, "dmul": 46.1, "pipe": 166.9}},
-    "nsw6_column_kernel": {"fp64": {"dfma": 141.3, "dadd": 155.1, "dmul": 155.9, "pipe": 468.8},
-                           "mixed": {"dfma": 102.8, "dadd": 118.3, "dmul": 141.6, "pipe": 417.1}},
+    "nsw6_cell_kernel": {"fp64": {"dfma": 353.9, "dadd": 246.8, "dmul": 273.0, "pipe": 919.5},
+                         "mixed": {"dfma": 29.0, "dadd": 64.0, "dmul": 46.0, "pipe": 161.9}},
+    "nsw6_column_kernel": {"fp64": {"dfma": 113.8 + 9.9, "dadd": 141.5 + 6.0, "dmul": 144.8 + 5.4,
+                                    "pipe": 407.1 + 21.6},
+                           "mixed": {"dfma": 77.9 + 9.0, "dadd": 104.6 + 6.0, "dmul": 130.6 + 5.4,
+                                     "pipe": 358.0 + 20.7}},
 }
 # FP64-pipe activity (fraction of active cycles) of each kernel in the same
-# captures (cold, serialised launches).
-FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.841, "mixed": 0.744},
-                    "nsw6_column_kernel": {"fp64": 0.708, "mixed": 0.690}}
+# captures (cold, serialised launches; the column kernel alone).
+FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.840, "mixed": 0.742},
+                    "nsw6_column_kernel": {"fp64": 0.735, "mixed": 0.716}}
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (probe/nsw6_probe.cu) and frozen here.
@@ -432,6 +436,8 @@ def roofline_of(kernel_ms: dict, spec: StateSpec, precision: str, rates, aw) -> 
                               "sm__thread_inst_executed_pipe_fp64_pred_on per cell on one 16900 x 42 region, "
                               "profiles/fp64_work_16900x42.md, times the cells of the launch), 2 flops each",
            "kernels": per,
+           "column_phase": "nsw6_column_kernel above times the column phase: nsw6_column_kernel and "
+                           "nsw6_satadj_kernel (the saturated cells' Newton iteration), one CUDA-event interval",
            "hbm": {"cell_kernel_gbs": hbm_cell, "cell_kernel_frac": hbm_cell / peaks["hbm_gbs"],
                    "peak": peaks["hbm_gbs"], "unit": "GB/s", "peak_source": f"{src} copy bandwidth"}}
     if aw:
@@ -623,7 +629,7 @@ def main(argv=None) -> int:
         "vs_baseline": None, "dtype": "f32+f64" if mixed else "f64", "data": "synthetic (seeded NICAM-like state)",
         "config": workload_config(spec, args.precision, world),
         "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
-        "gpu_launches": 2 * args.steps,
+        "gpu_launches": 3 * args.steps,   # per step: nsw6_cell_kernel, nsw6_column_kernel, nsw6_satadj_kernel
     }
 
     if not args.no_extras and world == 1:
