@@ -894,10 +894,10 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     const bool interior = (k >= kmin && k <= kmax);
     auto W = [&](int f, size_t cc) { return io.W[f * NC + cc]; };
     auto WBadd = [&](int f, size_t cc, double v) {
-      if (v != 0.0) atomicAdd(&io.WB[f * NC + cc], v);
+      if (!fp_is_zero(v)) atomicAdd(&io.WB[f * NC + cc], v);
     };
     auto XBadd = [&](int a, size_t i, double v) {
-      if (v != 0.0) atomicAdd(&io.xb.a[a][i], v);
+      if (!fp_is_zero(v)) atomicAdd(&io.xb.a[a][i], v);
     };
     const double* gs = io.x.a[A_gsgam2];
     const double* gsh = io.x.a[A_gsgam2h];
@@ -1151,7 +1151,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
       b_pre0 = SB[SF_PRE * NC + c];
     }
     // rhoge2 = (rhog tem) cvtot2 (the output at the halo levels)
-    if (b_rhoge2 != 0.0) {
+    if (!fp_is_zero(b_rhoge2)) {
       b_rhog += b_rhoge2 * tem * cvtot2;
       b_tem += b_rhoge2 * rhog * cvtot2;
       const double b_cv2 = b_rhoge2 * rhog * tem;
@@ -1209,7 +1209,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     b_qo[1] += b_qsum;
     double b_ein = b_ein_moist;
     // pre0 = (rho1 tem0) pq0 (halo output)
-    if (b_pre0 != 0.0) {
+    if (!fp_is_zero(b_pre0)) {
       b_rho1 += b_pre0 * tem0 * pq0;
       const double b_tem0 = b_pre0 * rho1 * pq0;
       const double b_pq0 = b_pre0 * rho1 * tem0;
@@ -1345,11 +1345,11 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     double* const* xb = io.xb.a;
     auto Y = [&](int f, size_t i) { return io.Y[f * NC + i]; };
     auto YBadd = [&](int f, size_t i, double v) {
-      if (v != 0.0) atomicAdd(&io.YB[f * NC + i], v);
+      if (!fp_is_zero(v)) atomicAdd(&io.YB[f * NC + i], v);
     };
     auto YBown = [&](int f, size_t i, double v) { io.YB[f * NC + i] += v; };
     auto XBadd = [&](int a, size_t i, double v) {
-      if (v != 0.0) atomicAdd(&xb[a][i], v);
+      if (!fp_is_zero(v)) atomicAdd(&xb[a][i], v);
     };
     auto XBown = [&](int a, size_t i, double v) { xb[a][i] += v; };
     auto WB = [&](int f) { return io.WB[f * NC + c]; };
@@ -1364,7 +1364,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
     double bvt[MAX_TR][5] = {};
     for (int r = 0; r < 2 * ntr; ++r) {
       const double bz = WB(W_ZDIS + r);
-      if (bz == 0.0) continue;
+      if (fp_is_zero(bz)) continue;
       const int t = r % ntr, half = r / ntr;
       const int mkmin = half ? kmin + 1 : kmin;
       if (k < mkmin) continue;
@@ -1403,7 +1403,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
       for (int s2 = 0; s2 < 3; ++s2) {
         const int j = k - 1 + s2;
         const double v = bw[s2];
-        if (v == 0.0) continue;
+        if (fp_is_zero(v)) continue;
         if (j >= mkmin + 1 && j <= kmax) {
           add_wp(j - 1, 0.5 * v);
           add_wp(j, 0.5 * v);

@@ -141,6 +141,7 @@ __device__ __forceinline__ bool lt_negc(double x, double c) {
   const long long b = fp_bits(x), m = b & FP_ABS;
   return b < 0 && m > (fp_bits(c) & FP_ABS) && m <= FP_INF;
 }
+__device__ __forceinline__ bool lt_c(double x, double c) { return fp_lt_pos(x, c); }
 __device__ __forceinline__ double maxz(double x) { return lt_z(x) ? 0.0 : x; }                // max(x, 0)
 __device__ __forceinline__ double maxc(double x, double c) { return fp_lt_pos(x, c) ? c : x; }   // max(x, c)
 __device__ __forceinline__ double minc(double x, double c) { return gt_c(x, c) ? c : x; }       // min(x, c)
@@ -156,6 +157,8 @@ template <class T>
 __device__ __forceinline__ bool le_c(const T& x, const T& c) { return x <= c; }
 template <class T>
 __device__ __forceinline__ bool lt_negc(const T& x, const T& c) { return x < c; }
+template <class T>
+__device__ __forceinline__ bool lt_c(const T& x, const T& c) { return x < c; }
 template <class T>
 __device__ __forceinline__ T maxz(const T& x) { return dmax(x, T(0.0)); }
 __device__ __forceinline__ bool is_zero(double x) { return fp_is_zero(x); }

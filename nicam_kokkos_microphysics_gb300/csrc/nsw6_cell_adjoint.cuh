@@ -59,6 +59,18 @@ __device__ __forceinline__ void bmax(T a, T b, T g, T& ba, T& bb) {
   if (a < b) bb += g;
   else ba += g;
 }
+// d(max(a, 0)) and d(max(a, c)) for a constant c > 0: the comparisons of
+// bmax with the integer-pipe forms of nsw6_cell.cuh
+template <class T>
+__device__ __forceinline__ void bmaxz(T a, T g, T& ba, T& bb) {
+  if (lt_z(a)) bb += g;
+  else ba += g;
+}
+template <class T>
+__device__ __forceinline__ void bmaxc(T a, T c, T g, T& ba, T& bb) {
+  if (lt_c(a, c)) bb += g;
+  else ba += g;
+}
 // d sqrt(x) / dx from s = sqrt(x)
 __device__ __forceinline__ double bsqrt(double s) { return s > 0.0 ? 0.5 / s : 0.0; }
 __device__ __forceinline__ float bsqrt(float s) { return s > 0.0f ? 0.5f / s : 0.0f; }
@@ -119,14 +131,14 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
 #pragma unroll
   for (int n = 2; n <= 5; ++n) {
     diffq += rq[n];
-    clip[n] = rq[n] < 0.0;
+    clip[n] = lt_z(rq[n]);
     rq[n] = clip[n] ? 0.0 : rq[n];
   }
 #pragma unroll
   for (int n = 2; n <= 5; ++n) diffq -= rq[n];
   rq[0] += diffq;
   D d2 = rq[0];
-  clip[0] = rq[0] < 0.0;
+  clip[0] = lt_z(rq[0]);
   rq[0] = clip[0] ? 0.0 : rq[0];
   d2 -= rq[0];
   const D omd = 1.0 - d2;
@@ -152,7 +164,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
 
   // ---- psat / qsat (rate precision from here to the tendencies)
   const R tempR = R(temp), densR = R(dens);
-  const R tmx = dmax(tempR, R(TEM_MIN));
+  const R tmx = maxc(tempR, R(TEM_MIN));
   const R rtem = NSW6_CK(R, 2, ONE / tmx);
   const R al = C.LovR_liq * (C.RTEM00 - rtem);
   const R ai = C.LovR_ice * (C.RTEM00 - rtem);
@@ -166,24 +178,24 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R qsati = psati * rdrt;
 
   // ---- TagBigLoop
-  const R qv = dmax(R(qn[0]), Z), qc = dmax(R(qn[1]), Z), qr = dmax(R(qn[2]), Z);
-  const R qi = dmax(R(qn[3]), Z), qs = dmax(R(qn[4]), Z), qg = dmax(R(qn[5]), Z);
-  const R sld = dmax(qsatl, R(EPS)), sid = dmax(qsati, R(EPS));
+  const R qv = maxz(R(qn[0])), qc = maxz(R(qn[1])), qr = maxz(R(qn[2]));
+  const R qi = maxz(R(qn[3])), qs = maxz(R(qn[4])), qg = maxz(R(qn[5]));
+  const R sld = maxc(qsatl, R(EPS)), sid = maxc(qsati, R(EPS));
   const R Sliq = NSW6_CK(R, 6, qv / sld);
   const R Sice = NSW6_CK(R, 7, qv / sid);
   const R Rdens = NSW6_CK(R, 8, ONE / densR);
   const R rfa = R(DENS00) * Rdens;
   const R rho_fact = NSW6_CK(R, 9, sqrtR(rfa));
   const R temc = tempR - R(TEM00);
-  const bool warm = !(temc < Z);
-  const bool d1 = (qr >= R(1.0E-4));
-  const bool d2b = (R(1.0E-4) >= qr && R(1.0E-4) >= qs);
-  const bool sps = (Sice >= ONE);
+  const bool warm = !lt_z(temc);
+  const bool d1 = ge_c(qr, R(1.0E-4));
+  const bool d2b = le_c(qr, R(1.0E-4)) && le_c(qs, R(1.0E-4));
+  const bool sps = ge_c(Sice, ONE);
   const R dqv_dt = per_dt(qv, dtR, rdtR), dqc_dt = per_dt(qc, dtR, rdtR), dqr_dt = per_dt(qr, dtR, rdtR);
   const R dqi_dt = per_dt(qi, dtR, rdtR), dqs_dt = per_dt(qs, dtR, rdtR), dqg_dt = per_dt(qg, dtR, rdtR);
 
   // rain slope parameter
-  const bool rain = (qr >= R(1.0E-12));
+  const bool rain = ge_c(qr, R(1.0E-12));
   R r_a = Z, r_b = Z;   // dens qr, (dens qr) K_rlmdr
   R r_s1 = Z;           // sqrt(r_b)
   R RLMDr = Z, RLMDr_dr = Z, RLMDr_2 = Z, RLMDr_3 = Z, RLMDr_1br = Z, RLMDr_2br = Z, RLMDr_3br = Z, RLMDr_7 = Z;
@@ -208,14 +220,14 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // Roh and Satoh (2014) snow moments
   const R xs_a = densR * qs;
   const R Xs2 = xs_a * C.rAs;
-  const bool snow = (Xs2 >= R(1.0E-12));
+  const bool snow = ge_c(Xs2, R(1.0E-12));
   R mom[7] = {Z, Z, Z, Z, Z, Z, Z};
   R mlb[7] = {Z, Z, Z, Z, Z, Z, Z};   // b of each moment (d mom / d logX = mom b)
   R RMOMs_Vt = Z, logX = Z;
   R tems = Z;
   bool tems_sel = false;   // tems = temc (else the constant -0.1)
   if (snow) {
-    tems_sel = temc < R(-0.1);   // dmin(-0.1, temc) is temc
+    tems_sel = lt_negc(temc, R(-0.1));   // dmin(-0.1, temc) is temc
     tems = tems_sel ? temc : R(-0.1);
     logX = NSW6_CK(R, 13, mth.log(Xs2));
 #pragma unroll
@@ -234,7 +246,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R MOMs_5ds_h = mom[6];
 
   // graupel slope parameter
-  const bool graupel = (qg >= R(1.0E-12));
+  const bool graupel = ge_c(qg, R(1.0E-12));
   R g_a = Z, g_b = Z, g_s1 = Z;
   R RLMDg = Z, RLMDg_dg = Z, RLMDg_2 = Z, RLMDg_3 = Z, RLMDg_3dg = Z, RLMDg_5dg = Z, g32 = Z;
   if (graupel) {
@@ -260,20 +272,20 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
 
   // nucleation
   const R nm01 = R(-0.1) * temc;
-  const R nmax = dmax(nm01, Z);
+  const R nmax = maxz(nm01);
   const R nex = R(1.33) * (C.ln1000 + nmax);
   const R nexp = NSW6_CK(R, 25, mth.exp(nex));
   const R qi0a = C.ice_nuc * nexp;
   const R Qi0 = qi0a * Rdens;
   const R pg1 = Qi0 - qi, pg2 = qv - qsati;
   const R pgmin = dmin(pg1, pg2);
-  const R pgmax = dmax(pgmin, Z);
+  const R pgmax = maxz(pgmin);
   R Pigen = pgmax * rdtR;
 
   // accretion
   R Esi_mod = C.Esi, betai = C.beta_saut, eg = Z;
   bool esi_exp = false, bet_exp = false;   // Esi_mod / betai took the exponential branch of min
-  const bool cold_branch = !(warm && C.Esi >= Z && C.beta_saut >= Z);
+  const bool cold_branch = !(warm && is_nonneg(C.Esi) && is_nonneg(C.beta_saut));
   if (cold_branch) {
     eg = NSW6_CK(R, 26, mth.exp(C.gamma_sacr * temc));
     const R es = C.Esi * eg;
@@ -285,7 +297,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   }
   const R qcqr = qc * qr;
   R Pracw = Z, prw_pow = Z;
-  const bool prw_on = (qcqr >= R(1.0E-12));
+  const bool prw_on = ge_c(qcqr, R(1.0E-12));
   if (prw_on) {
     prw_pow = NSW6_CK(R, 27, mth.pow(qcqr, R(1.15)));
     Pracw = R(67.0) * prw_pow;
@@ -328,14 +340,14 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R rhoqc_a = densR * qc;
   const R rhoqc = rhoqc_a * R(1000.0);
   R Praut = Z, aut_pow = Z;
-  const bool aut_on = qc > Z;
+  const bool aut_on = gt_z(qc);
   if (aut_on) {
     aut_pow = NSW6_CK(R, 28, mth.pow(qc, R(2.47)));
     Praut = C.K_aut * aut_pow;
   }
   const R saut_a = qi - C.qicrt_saut;
   const R saut_b = betai * saut_a;
-  R Psaut = dmax(saut_b, Z);
+  R Psaut = maxz(saut_b);
 
   // evaporation, sublimation, melting and freezing
   const R Ka = (R(2.428E-2) + R(7.47E-5) * temc);
@@ -379,37 +391,37 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     vr6 = C.K_ventr2 * vr5;
     ventr = vr1 + vr6;
     ev1 = C.K_revp * Rdens;
-    sl_min = !(ONE < Sliq);   // dmin(Sliq, 1) = Sliq when !(1 < Sliq)
+    sl_min = !gt_c(Sliq, ONE);   // dmin(Sliq, 1) = Sliq when !(1 < Sliq)
     ev2 = ONE - (sl_min ? Sliq : ONE);
     ev3 = ev1 * ev2;
     ev4 = ev3 * Glv;
     Prevp = ev4 * ventr;
   }
   const R rhoqi_a = densR * qi;
-  const bool rqi_on = !(rhoqi_a < R(EPS));   // dmax(dens qi, EPS) = dens qi
+  const bool rqi_on = !lt_c(rhoqi_a, R(EPS));   // dmax(dens qi, EPS) = dens qi
   const R rhoqi = rqi_on ? rhoqi_a : R(EPS);
   R XNi = C.XNi_eps, Di = C.Di_eps;
   R xn_pow = Z, xn_a = Z, XMi = Z, di_s = Z, di_a = Z;
   bool xn_lo = false, xn_hi = false, di_cap = false;
-  const bool ice_on = rhoqi > R(EPS);
+  const bool ice_on = gt_c(rhoqi, R(EPS));
   if (ice_on) {
     xn_pow = NSW6_CK(R, 35, mth.pow(rhoqi, R(0.75)));
     xn_a = R(5.38E+7) * xn_pow;
-    xn_lo = xn_a < R(1.0E+3);             // dmax(xn_a, 1e3) gives 1e3
+    xn_lo = lt_c(xn_a, R(1.0E+3));             // dmax(xn_a, 1e3) gives 1e3
     const R xm = xn_lo ? R(1.0E+3) : xn_a;
-    xn_hi = R(1.0E+6) < xm;               // dmin(xm, 1e6) gives 1e6
+    xn_hi = gt_c(xm, R(1.0E+6));               // dmin(xm, 1e6) gives 1e6
     XNi = xn_hi ? R(1.0E+6) : xm;
     XMi = NSW6_CK(R, 36, rhoqi / XNi);
     di_s = NSW6_CK(R, 37, sqrtR(XMi));
     di_a = C.Di_a * di_s;
-    di_cap = C.Di_max < di_a;
+    di_cap = gt_c(di_a, C.Di_max);
     Di = di_cap ? C.Di_max : di_a;
   }
   const R t1a = R(4.0) * Di, t1b = t1a * XNi, t1c = t1b * Rdens, sm1 = Sice - ONE, t1d = t1c * sm1;
   const R tmp1 = t1d * Giv;
   R Pidep = sel(sps, tmp1);
   R Pisub = sel(!sps, -tmp1);
-  const bool below40 = (temc + R(40.0) < Z);
+  const bool below40 = lt_z(temc + R(40.0));
   R Pihom = below40 ? dqc_dt : Z;
   const R efa = -C.A_frz * temc;
   const R efe = NSW6_CK(R, 38, mth.exp(efa));
@@ -432,7 +444,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R sm_a = s1a * Gil, sm_b = sm_a * vents;
   const R sm_c = C.K_clf * temc, sm_d = Psacw + Psacr, sm_e = sm_c * sm_d;
   const R sm_f = sm_b + sm_e;
-  R Psmlt = dmax(sm_f, Z);
+  R Psmlt = maxz(sm_f);
   const R vg1 = C.K_ventg1 * RLMDg_2;
   const R vg2 = C.Cg * fr, vg3 = vg2 * rNu, vg4 = vg3 * RLMDg_5dg;
   const R vg5 = NSW6_CK(R, 40, sqrtR(vg4));
@@ -445,7 +457,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R gm_a = g1a * Gil, gm_b = gm_a * ventg;
   const R gm_d = Pgacw + Pgacr, gm_e = sm_c * gm_d;
   const R gm_f = gm_b + gm_e;
-  R Pgmlt = dmax(gm_f, Z);
+  R Pgmlt = maxz(gm_f);
   const R gf_a = C.K_gfrz * Rdens, gf_b = gf_a * efrz;
   R Pgfrz = gf_b * RLMDr_7;
 
@@ -501,12 +513,12 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   auto limit = [&](int slot, R net, R dq) {
     Lim L;
     L.net = net;
-    if (net + R(EPS) >= Z) {
+    if (is_nonneg(net + R(EPS))) {
       L.fac = ONE;
       L.ratio = false;
     } else {
       const R r = NSW6_CK(R, slot, -dq / net);
-      L.ratio = !(ONE < r);
+      L.ratio = !gt_c(r, ONE);
       L.fac = L.ratio ? r : ONE;
     }
     L.scaled = L.fac != ONE;
@@ -601,10 +613,10 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R r3c_a = C.coef_xf * densR, r3_qc = r3c_a * qc;
   const R r3_qr = r3c_a * qr;
   const R r2 = r2_qc + r2_qr;
-  const bool big = (r2 >= R(1.0E-10));
+  const bool big = ge_c(r2, R(1.0E-10));
   const R r3 = r3_qc + r3_qr;
-  const bool top = !big && ((qc + qr) >= R(1.0E-5));
-  const bool cld = (r2_qc >= R(1.0E-10));
+  const bool top = !big && ge_c(qc + qr, R(1.0E-5));
+  const bool cld = ge_c(r2_qc, R(1.0E-10));
   // updates (FP64)
   const D rhoge1 = rhoge0 - LHV0 * drq[0];
   const D rhoge2 = rhoge1 + LHF0 * drq[3];
@@ -756,7 +768,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     b_RLMDr_3 = fmaR(b_r2_qr, C.K_r2r, b_RLMDr_3);
     // r2_qc = K_r2c rf^2, rf = pow(xf3, 1/3)
     const R b_rf = b_r2_qc * C.K_r2c * R(2.0) * rf_qc;
-    const R b_xf3 = (xf3 > Z) ? b_rf * R(0.33333333) * rf_qc / xf3 : Z;
+    const R b_xf3 = gt_z(xf3) ? b_rf * R(0.33333333) * rf_qc / xf3 : Z;
     b_rhoqc = fmaR(b_xf3 * C.coef_xf, C.K_xf, b_rhoqc);
   }
   // Vt outputs
@@ -904,7 +916,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   R b_ventg = Z, b_g1a = Z, b_sm_c = Z;
   {
     R b_f = Z, dummy = Z;
-    bmax(gm_f, Z, bPgmlt, b_f, dummy);
+    bmaxz(gm_f, bPgmlt, b_f, dummy);
     b_g1a = fmaR(b_f * ventg, Gil, b_g1a);
     b_Gil = fmaR(b_f * ventg, g1a, b_Gil);
     b_ventg = fmaR(b_f, gm_a, b_ventg);
@@ -938,7 +950,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   R b_vents = Z, b_s1a = Z;
   {
     R b_f = Z, dummy = Z;
-    bmax(sm_f, Z, bPsmlt, b_f, dummy);
+    bmaxz(sm_f, bPsmlt, b_f, dummy);
     b_s1a = fmaR(b_f * vents, Gil, b_s1a);
     b_Gil = fmaR(b_f * vents, s1a, b_Gil);
     b_vents = fmaR(b_f, sm_a, b_vents);
@@ -1005,7 +1017,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     // XNi = min(max(5.38e7 pow(rhoqi, 0.75), 1e3), 1e6)
     if (!xn_hi && !xn_lo) {
       const R b_pow = b_XNi * R(5.38E+7);
-      if (rhoqi > Z) b_rhoqi += b_pow * R(0.75) * xn_pow / rhoqi;
+      if (gt_z(rhoqi)) b_rhoqi += b_pow * R(0.75) * xn_pow / rhoqi;
     }
   }
   if (rqi_on) {
@@ -1093,7 +1105,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // Psaut = max(betai (qi - qicrt), 0), off where its argument is exactly 0
   // (rate_on: a cell without ice at the threshold qicrt = 0)
   {
-    const R b_sb = saut_b > Z ? bPsaut : Z;
+    const R b_sb = gt_z(saut_b) ? bPsaut : Z;
     b_betai = fmaR(b_sb, saut_a, b_betai);
     const R b_sa = b_sb * betai;
     b_qi += b_sa;
@@ -1102,7 +1114,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // Praut = K_aut pow(qc, 2.47)
   if (aut_on) {
     b_K_aut = fmaR(bPraut, aut_pow, b_K_aut);
-    if (qc > Z) b_qc += bPraut * C.K_aut * R(2.47) * aut_pow / qc;
+    if (gt_z(qc)) b_qc += bPraut * C.K_aut * R(2.47) * aut_pow / qc;
   }
   // rhoqc = (dens qc) 1000 (read by the effective radius)
   b_dens = fmaR(b_rhoqc * R(1000.0), qc, b_dens);
@@ -1127,7 +1139,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     const R b_kd = bPgacr * gacr_s;
     const R b_dv = b_kd * gacr_k;
     b_Rdens = fmaR(b_kd * dvgr, C.K_gacr, b_Rdens);
-    const R sgn = dvgr_d < Z ? -ONE : ONE;
+    const R sgn = lt_z(dvgr_d) ? -ONE : ONE;
     b_Vtg = fmaR(b_dv, sgn, b_Vtg);
     b_Vtr = fmaR(-b_dv, sgn, b_Vtr);
     b_RLMDr_1br = fmaR(b_s * RLMDg_3, C.K_g13, b_RLMDr_1br);
@@ -1152,7 +1164,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   }
   // dvrs = |Vtr - Vts|
   {
-    const R sgn = dvrs_d < Z ? -ONE : ONE;
+    const R sgn = lt_z(dvrs_d) ? -ONE : ONE;
     b_Vtr = fmaR(b_dvrs, sgn, b_Vtr);
     b_Vts = fmaR(-b_dvrs, sgn, b_Vts);
   }
@@ -1206,7 +1218,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // Pracw = 67 pow(qc qr, 1.15)
   if (prw_on) {
     const R b_pow = bPracw0 * R(67.0);
-    if (qcqr > Z) {
+    if (gt_z(qcqr)) {
       const R b_qcqr = b_pow * R(1.15) * prw_pow / qcqr;
       b_qc = fmaR(b_qcqr, qr, b_qc);
       b_qr = fmaR(b_qcqr, qc, b_qr);
@@ -1230,7 +1242,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   {
     const R b_max = bPigen * rdtR;
     R b_min = Z, dummy = Z;
-    bmax(pgmin, Z, b_max, b_min, dummy);
+    bmaxz(pgmin, b_max, b_min, dummy);
     R b_p1 = Z, b_p2 = Z;
     bmin(pg1, pg2, b_min, b_p1, b_p2);
     b_qi -= b_p1;
@@ -1242,7 +1254,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     b_icenuc = fmaR(b_qi0a, nexp, b_icenuc);
     const R b_nex = b_qi0a * C.ice_nuc * nexp;
     R b_nm01 = Z, dummy2 = Z;
-    bmax(nm01, Z, b_nex * R(1.33), b_nm01, dummy2);
+    bmaxz(nm01, b_nex * R(1.33), b_nm01, dummy2);
     b_temc = fmaR(b_nm01, R(-0.1), b_temc);
   }
   // terminal velocities: Vtr = (K_vtr rho_fact) RLMDr_dr etc.
@@ -1344,11 +1356,11 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     b_qv = fmaR(b_Sliq, rsld, b_qv);
     const R b_sld = -b_Sliq * Sliq * rsld;
     R dummy = Z;
-    bmax(qsatl, R(EPS), b_sld, b_qsatl, dummy);
+    bmaxc(qsatl, R(EPS), b_sld, b_qsatl, dummy);
     const R rsid = ONE / sid;
     b_qv = fmaR(b_Sice, rsid, b_qv);
     const R b_sid = -b_Sice * Sice * rsid;
-    bmax(qsati, R(EPS), b_sid, b_qsati, dummy);
+    bmaxc(qsati, R(EPS), b_sid, b_qsati, dummy);
   }
   // q* = max(qn, 0) (compared in the rate precision, as the forward does)
   D b_qn[6] = {0, 0, 0, 0, 0, 0};
@@ -1357,7 +1369,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
 #pragma unroll
     for (int n = 0; n < 6; ++n) {
       R b = Z, dummy = Z;
-      bmax(R(qn[n]), Z, bq[n], b, dummy);
+      bmaxz(R(qn[n]), bq[n], b, dummy);
       b_qn[n] = D(b) * isc;
     }
   }
@@ -1372,7 +1384,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     // rtem = 1 / max(temp, TEM_MIN)
     const R b_tmx = -b_rtem * rtem * rtem;
     R dummy = Z;
-    bmax(tempR, R(TEM_MIN), b_tmx, b_temp, dummy);
+    bmaxc(tempR, R(TEM_MIN), b_tmx, b_temp, dummy);
   }
   // ---- FP64 from here: pre = (dens (qd RDRY + qn0 RVAP)) temp
   D b_densD = D(b_dens) * isc;
