@@ -142,6 +142,23 @@ __device__ __forceinline__ bool lt_negc(double x, double c) {
   return b < 0 && m > (fp_bits(c) & FP_ABS) && m <= FP_INF;
 }
 __device__ __forceinline__ bool lt_c(double x, double c) { return fp_lt_pos(x, c); }
+// min(p, d) as Kokkos::min, (d < p) ? d : p, for a d that is not negative
+// (the limiters' d = max(q, 0) / dt with dt > 0, which the API enforces: +-0,
+// positive, or NaN): d < p exactly when p is positive and not NaN and d's
+// magnitude bits are below p's (a NaN d never is).
+__device__ __forceinline__ bool lt_nn(double d, double p) {   // d < p
+  const long long bp = fp_bits(p);
+  return bp > 0 && bp <= FP_INF && (fp_bits(d) & FP_ABS) < bp;
+}
+__device__ __forceinline__ double min_nn(double p, double d) { return lt_nn(d, p) ? d : p; }
+// a < b for a b that is not positive (b = -d of the limiters: -+0, negative,
+// or NaN): a must be negative, not NaN, and of larger magnitude; max(a, b) as
+// Kokkos::max, (a < b) ? b : a
+__device__ __forceinline__ bool lt_np(double a, double b) {
+  const long long ba = fp_bits(a), ma = ba & FP_ABS;
+  return ba < 0 && ma > (fp_bits(b) & FP_ABS) && ma <= FP_INF;
+}
+__device__ __forceinline__ double max_np(double a, double b) { return lt_np(a, b) ? b : a; }
 __device__ __forceinline__ double maxz(double x) { return lt_z(x) ? 0.0 : x; }                // max(x, 0)
 __device__ __forceinline__ double maxc(double x, double c) { return fp_lt_pos(x, c) ? c : x; }   // max(x, c)
 __device__ __forceinline__ double minc(double x, double c) { return gt_c(x, c) ? c : x; }       // min(x, c)
@@ -169,6 +186,14 @@ template <class T>
 __device__ __forceinline__ T maxc(const T& x, const T& c) { return dmax(x, c); }
 template <class T>
 __device__ __forceinline__ T minc(const T& x, const T& c) { return dmin(x, c); }
+template <class T>
+__device__ __forceinline__ bool lt_nn(const T& d, const T& p) { return d < p; }
+template <class T>
+__device__ __forceinline__ T min_nn(const T& p, const T& d) { return dmin(p, d); }
+template <class T>
+__device__ __forceinline__ bool lt_np(const T& a, const T& b) { return a < b; }
+template <class T>
+__device__ __forceinline__ T max_np(const T& a, const T& b) { return dmax(a, b); }
 
 // The liquid saturation test qsum - qsat(T) > EPS of the saturation
 // adjustment (mod_satadjust.cpp:771-896), decided in FP32 where its margin
@@ -497,38 +522,38 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   }
 
   // limiters, :1249-1296 (iceflg selects; sw_expice = 1 unless OPT; Pgaut = 0)
-  Pigen = sel(cold && expice, dmin(Pigen, dqv_dt));
-  Pidep = sel(cold && expice, dmin(Pidep, dqv_dt));
-  Psdep = sel(cold, dmin(Psdep, dqv_dt));
-  Pgdep = sel(cold, dmin(Pgdep, dqv_dt));
+  Pigen = sel(cold && expice, min_nn(Pigen, dqv_dt));
+  Pidep = sel(cold && expice, min_nn(Pidep, dqv_dt));
+  Psdep = sel(cold, min_nn(Psdep, dqv_dt));
+  Pgdep = sel(cold, min_nn(Pgdep, dqv_dt));
   Pracw = Pracw + sel(warm, Psacw) + sel(warm, Pgacw);
-  Praut = dmin(Praut, dqc_dt);
-  Pracw = dmin(Pracw, dqc_dt);
-  Pihom = sel(cold && expice, dmin(Pihom, dqc_dt));
-  Pihtr = sel(cold && expice, dmin(Pihtr, dqc_dt));
-  Psacw = sel(cold, dmin(Psacw, dqc_dt));
-  if constexpr (OPT) Psfw = sel(cold, dmin(Psfw, dqc_dt));
-  Pgacw = sel(cold, dmin(Pgacw, dqc_dt));
-  Prevp = dmin(Prevp, dqr_dt);
-  Piacr = sel(cold, dmin(Piacr, dqr_dt));
-  Psacr = sel(cold, dmin(Psacr, dqr_dt));
-  Pgacr = sel(cold, dmin(Pgacr, dqr_dt));
-  Pgfrz = sel(cold, dmin(Pgfrz, dqr_dt));
-  Pisub = sel(cold && expice, dmin(Pisub, dqi_dt));
-  Pimlt = sel(warm && expice, dmin(Pimlt, dqi_dt));
-  Psaut = sel(cold, dmin(Psaut, dqi_dt));
-  Praci = sel(cold, dmin(Praci, dqi_dt));
-  Psaci = sel(cold, dmin(Psaci, dqi_dt));
+  Praut = min_nn(Praut, dqc_dt);
+  Pracw = min_nn(Pracw, dqc_dt);
+  Pihom = sel(cold && expice, min_nn(Pihom, dqc_dt));
+  Pihtr = sel(cold && expice, min_nn(Pihtr, dqc_dt));
+  Psacw = sel(cold, min_nn(Psacw, dqc_dt));
+  if constexpr (OPT) Psfw = sel(cold, min_nn(Psfw, dqc_dt));
+  Pgacw = sel(cold, min_nn(Pgacw, dqc_dt));
+  Prevp = min_nn(Prevp, dqr_dt);
+  Piacr = sel(cold, min_nn(Piacr, dqr_dt));
+  Psacr = sel(cold, min_nn(Psacr, dqr_dt));
+  Pgacr = sel(cold, min_nn(Pgacr, dqr_dt));
+  Pgfrz = sel(cold, min_nn(Pgfrz, dqr_dt));
+  Pisub = sel(cold && expice, min_nn(Pisub, dqi_dt));
+  Pimlt = sel(warm && expice, min_nn(Pimlt, dqi_dt));
+  Psaut = sel(cold, min_nn(Psaut, dqi_dt));
+  Praci = sel(cold, min_nn(Praci, dqi_dt));
+  Psaci = sel(cold, min_nn(Psaci, dqi_dt));
   if constexpr (OPT) {
-    Psfi = sel(cold, dmin(Psfi, dqi_dt));
-    Pgaci = sel(cold, dmin(Pgaci, dqi_dt));
+    Psfi = sel(cold, min_nn(Psfi, dqi_dt));
+    Pgaci = sel(cold, min_nn(Pgaci, dqi_dt));
   }
-  Pssub = sel(cold, dmin(Pssub, dqs_dt));
-  Psmlt = sel(warm, dmin(Psmlt, dqs_dt));
-  Pracs = sel(cold, dmin(Pracs, dqs_dt));
-  if constexpr (OPT) Pgacs = dmin(Pgacs, dqs_dt);
-  Pgsub = sel(cold, dmin(Pgsub, dqg_dt));
-  Pgmlt = sel(warm, dmin(Pgmlt, dqg_dt));
+  Pssub = sel(cold, min_nn(Pssub, dqs_dt));
+  Psmlt = sel(warm, min_nn(Psmlt, dqs_dt));
+  Pracs = sel(cold, min_nn(Pracs, dqs_dt));
+  if constexpr (OPT) Pgacs = min_nn(Pgacs, dqs_dt);
+  Pgsub = sel(cold, min_nn(Pgsub, dqg_dt));
+  Pgmlt = sel(warm, min_nn(Pgmlt, dqg_dt));
   R Piacr_s = sel(!d1, Piacr);
   R Piacr_g = sel(d1, Piacr);
   R Praci_s = sel(!d1, Praci);
@@ -639,11 +664,11 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
       qs_t = +Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs - Pgacs;
     if (lg) qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt;
   }
-  qc_t = dmax(qc_t, -dqc_dt);
-  qr_t = dmax(qr_t, -dqr_dt);
-  qi_t = dmax(qi_t, -dqi_dt);
-  qs_t = dmax(qs_t, -dqs_dt);
-  qg_t = dmax(qg_t, -dqg_dt);
+  qc_t = max_np(qc_t, -dqc_dt);
+  qr_t = max_np(qr_t, -dqr_dt);
+  qi_t = max_np(qi_t, -dqi_dt);
+  qs_t = max_np(qs_t, -dqs_dt);
+  qg_t = max_np(qg_t, -dqg_dt);
   const R qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
   D drq[6];
   drq[0] = rhog * D(qv_t) * dt;

@@ -464,38 +464,38 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // limiters (:1249-1296); each records which operand of min it took
   const bool cold = !warm;
   const R Pigen0 = Pigen, Pidep0 = Pidep, Psdep0 = Psdep, Pgdep0 = Pgdep;
-  Pigen = sel(cold, dmin(Pigen, dqv_dt));
-  Pidep = sel(cold, dmin(Pidep, dqv_dt));
-  Psdep = sel(cold, dmin(Psdep, dqv_dt));
-  Pgdep = sel(cold, dmin(Pgdep, dqv_dt));
+  Pigen = sel(cold, min_nn(Pigen, dqv_dt));
+  Pidep = sel(cold, min_nn(Pidep, dqv_dt));
+  Psdep = sel(cold, min_nn(Psdep, dqv_dt));
+  Pgdep = sel(cold, min_nn(Pgdep, dqv_dt));
   const R Pracw_a = Pracw + sel(warm, Psacw);
   const R Pracw_b = Pracw_a + sel(warm, Pgacw);
   const R Praut0 = Praut, Pracw0 = Pracw_b, Pihom0 = Pihom, Pihtr0 = Pihtr, Psacw0 = Psacw, Pgacw0 = Pgacw;
-  Praut = dmin(Praut, dqc_dt);
-  Pracw = dmin(Pracw_b, dqc_dt);
-  Pihom = sel(cold, dmin(Pihom, dqc_dt));
-  Pihtr = sel(cold, dmin(Pihtr, dqc_dt));
-  Psacw = sel(cold, dmin(Psacw, dqc_dt));
-  Pgacw = sel(cold, dmin(Pgacw, dqc_dt));
+  Praut = min_nn(Praut, dqc_dt);
+  Pracw = min_nn(Pracw_b, dqc_dt);
+  Pihom = sel(cold, min_nn(Pihom, dqc_dt));
+  Pihtr = sel(cold, min_nn(Pihtr, dqc_dt));
+  Psacw = sel(cold, min_nn(Psacw, dqc_dt));
+  Pgacw = sel(cold, min_nn(Pgacw, dqc_dt));
   const R Prevp0 = Prevp, Piacr0 = Piacr, Psacr0 = Psacr, Pgacr0 = Pgacr, Pgfrz0 = Pgfrz;
-  Prevp = dmin(Prevp, dqr_dt);
-  Piacr = sel(cold, dmin(Piacr, dqr_dt));
-  Psacr = sel(cold, dmin(Psacr, dqr_dt));
-  Pgacr = sel(cold, dmin(Pgacr, dqr_dt));
-  Pgfrz = sel(cold, dmin(Pgfrz, dqr_dt));
+  Prevp = min_nn(Prevp, dqr_dt);
+  Piacr = sel(cold, min_nn(Piacr, dqr_dt));
+  Psacr = sel(cold, min_nn(Psacr, dqr_dt));
+  Pgacr = sel(cold, min_nn(Pgacr, dqr_dt));
+  Pgfrz = sel(cold, min_nn(Pgfrz, dqr_dt));
   const R Pisub0 = Pisub, Pimlt0 = Pimlt, Psaut0 = Psaut, Praci0 = Praci, Psaci0 = Psaci;
-  Pisub = sel(cold, dmin(Pisub, dqi_dt));
-  Pimlt = sel(warm, dmin(Pimlt, dqi_dt));
-  Psaut = sel(cold, dmin(Psaut, dqi_dt));
-  Praci = sel(cold, dmin(Praci, dqi_dt));
-  Psaci = sel(cold, dmin(Psaci, dqi_dt));
+  Pisub = sel(cold, min_nn(Pisub, dqi_dt));
+  Pimlt = sel(warm, min_nn(Pimlt, dqi_dt));
+  Psaut = sel(cold, min_nn(Psaut, dqi_dt));
+  Praci = sel(cold, min_nn(Praci, dqi_dt));
+  Psaci = sel(cold, min_nn(Psaci, dqi_dt));
   const R Pssub0 = Pssub, Psmlt0 = Psmlt, Pracs0 = Pracs;
-  Pssub = sel(cold, dmin(Pssub, dqs_dt));
-  Psmlt = sel(warm, dmin(Psmlt, dqs_dt));
-  Pracs = sel(cold, dmin(Pracs, dqs_dt));
+  Pssub = sel(cold, min_nn(Pssub, dqs_dt));
+  Psmlt = sel(warm, min_nn(Psmlt, dqs_dt));
+  Pracs = sel(cold, min_nn(Pracs, dqs_dt));
   const R Pgsub0 = Pgsub, Pgmlt0 = Pgmlt;
-  Pgsub = sel(cold, dmin(Pgsub, dqg_dt));
-  Pgmlt = sel(warm, dmin(Pgmlt, dqg_dt));
+  Pgsub = sel(cold, min_nn(Pgsub, dqg_dt));
+  Pgmlt = sel(warm, min_nn(Pgmlt, dqg_dt));
   R Piacr_s = sel(!d1, Piacr);
   R Piacr_g = sel(d1, Piacr);
   R Praci_s = sel(!d1, Praci);
@@ -575,8 +575,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R qs_t0 = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
   const R qg_t0 = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
   // qx_t = max(qx_t0, -dqx_dt): true when the tendency itself is kept
-  const bool kc_ = !(qc_t0 < -dqc_dt), kr_ = !(qr_t0 < -dqr_dt), ki_ = !(qi_t0 < -dqi_dt);
-  const bool ks_ = !(qs_t0 < -dqs_dt), kg_ = !(qg_t0 < -dqg_dt);
+  const bool kc_ = !lt_np(qc_t0, -dqc_dt), kr_ = !lt_np(qr_t0, -dqr_dt), ki_ = !lt_np(qi_t0, -dqi_dt);
+  const bool ks_ = !lt_np(qs_t0, -dqs_dt), kg_ = !lt_np(qg_t0, -dqg_dt);
   const R qc_t = kc_ ? qc_t0 : -dqc_dt, qr_t = kr_ ? qr_t0 : -dqr_dt, qi_t = ki_ ? qi_t0 : -dqi_dt;
   const R qs_t = ks_ ? qs_t0 : -dqs_dt, qg_t = kg_ ? qg_t0 : -dqg_dt;
   const R qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
@@ -861,7 +861,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
     }
     const R g = bx;
     bx = Z;
-    bmin(x0, dq, g, bx, b_dq);
+    if (lt_nn(dq, x0)) b_dq += g;   // bmin(x0, dq, ...) with dq = max(q, 0) / dt, not negative
+    else bx += g;
   };
   unmin(warm, Pgmlt0, dqg_dt, bPgmlt, b_dqg);
   unmin(cold, Pgsub0, dqg_dt, bPgsub, b_dqg);
