@@ -96,6 +96,14 @@ namespace {
 struct LayS {
   int K, G, lall;
   size_t pld;   // row stride of the [2][..] precipitation arrays
+  FastDiv dG, dK;   // by G and by K: the cell index splits on 32 bits (lall kall gall < 2^32, nsw6_create)
+  // c = (l K + k) G + g -> l, k, g
+  __device__ __forceinline__ void split(size_t c, int& l, int& k, int& g) const {
+    const unsigned ci = (unsigned)c, q = dG.div(ci), q2 = dK.div(q);
+    g = (int)(ci - q * (unsigned)G);
+    k = (int)(q - q2 * (unsigned)K);
+    l = (int)q2;
+  }
   __device__ __forceinline__ size_t f(int l, int k, int g) const { return ((size_t)l * K + k) * G + g; }
   __device__ __forceinline__ size_t t(int l, int n, int k, int g) const {
     return (((size_t)l * NQ + n) * K + k) * G + g;
@@ -815,14 +823,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_fwd_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
-  const size_t n = io.NC * 8 * io.P.ntr;
-  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
-    const size_t c = w % io.NC;
-    const int j = (int)(w / io.NC);
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
-    const In<double> in{io, l, g};
-    io.W[(W_F + j) * io.NC + c] = stage2<double>(in, grid, k, j);
-  }
+  const int nj = 8 * io.P.ntr;
+  for (int j = 0; j < nj; ++j)
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
+      int g, k, l;
+      io.L.split(c, l, k, g);
+      const In<double> in{io, l, g};
+      io.W[(W_F + j) * io.NC + c] = stage2<double>(in, grid, k, j);
+    }
 }
 
 // Forward of S3.
@@ -831,7 +839,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_fwd_kernel(StageIO io) {
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     const In<double> in{io, l, g};
     stage3<double>(
         in, grid, k, [&](int f, double v) { io.W[f * io.NC + c] = v; }, [](int, double) {}, [](int, double) {});
@@ -847,7 +856,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Const
   tape_bind_s(tm);
   LeafLog lg;
   for (size_t c = tape().slot; c < io.NC; c += tape().nslot) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     tape_begin(lg);
     const In<RVar> in{io, l, g, &lg};
     RVar outs[NSF];
@@ -890,7 +900,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
   const size_t NC = io.NC;
   const size_t G = io.L.G;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     const bool interior = (k >= kmin && k <= kmax);
     auto W = [&](int f, size_t cc) { return io.W[f * NC + cc]; };
     auto WBadd = [&](int f, size_t cc, double v) {
@@ -1337,7 +1348,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_hw_kernel(StageIO io) {
   const size_t NC = io.NC, G = io.L.G;
   const double dt = P.dt, hdt2 = P.hdt2, sdt3 = P.sdt3;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     if (k < kmin || k > kmax) continue;
     const bool hk = (k >= kmin + 1);
     const size_t cc = io.L.c(l, g);
@@ -1579,7 +1591,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s3_hw_kernel(StageIO io) {
   const size_t ncol = (size_t)io.L.lall * io.L.G;
   const double dt = P.dt;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     const bool in_k = (k >= kmin && k <= kmax), in_km = (k - 1 >= kmin && k - 1 <= kmax);
     const bool hk = (k >= kmin + 1 && k <= kmax), hkp = (k + 1 >= kmin + 1 && k + 1 <= kmax);
     const S3Bar b0 = s3_bars(io, l, k, g);
@@ -1675,7 +1688,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s2_kernel(StageIO io, TapeM
     const int j = (int)(w / io.NC);
     const double gF = io.WB[(W_F + j) * io.NC + c];
     if (gF == 0.0) continue;
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     tape_begin(lg);
     const In<RVar> in{io, l, g, &lg};
     const RVar F = stage2<RVar>(in, grid, k, j);
@@ -1753,7 +1767,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s1_kernel(StageIO io, TapeM
   tape_bind_s(tm);
   LeafLog lg;
   for (size_t c = tape().slot; c < io.NC; c += tape().nslot) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     tape_begin(lg);
     const In<RVar> in{io, l, g, &lg};
     RVar o[W_F];
@@ -1772,7 +1787,8 @@ __global__ void adj_seed_kernel(StageIO io) {
   const LayS& L = io.L;
   double* SB = const_cast<double*>(io.SB);
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % L.G), k = (int)((c / L.G) % L.K), l = (int)(c / ((size_t)L.G * L.K));
+    int g, k, l;
+    L.split(c, l, k, g);
     auto take = [&](int f, int a, size_t i) {
       SB[f * io.NC + c] = io.xb.a[a][i];
       io.xb.a[a][i] = 0.0;
@@ -1880,11 +1896,13 @@ __global__ void __launch_bounds__(128) adj_cell_save_kernel(Problem P, ConstsT<R
   const LayS L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
+  const FastDiv dg = FastDiv::make((unsigned)P.gall), dn = FastDiv::make((unsigned)nint);
   const long long ncell = (long long)P.lall * nint * P.gall;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(c % P.gall);
-    const int k = P.kmin + (int)((c / P.gall) % nint);
-    const int l = (int)(c / ((long long)P.gall * nint));
+    const unsigned ci = (unsigned)c, q = dg.div(ci), q2 = dn.div(q);   // ncell < 2^32
+    const int g = (int)(ci - q * (unsigned)P.gall);
+    const int k = P.kmin + (int)(q - q2 * (unsigned)nint);
+    const int l = (int)q2;
     const size_t i = L.f(l, k, g);
     CellIn in;
     in.rhog = x.a[A_rhog][i];
@@ -1951,12 +1969,14 @@ __global__ void __launch_bounds__(128) adj_cell_hw_kernel(Problem P, ConstsT<R> 
   const LayS L{P.kall, P.gall, P.lall, P.prec_ld};
   const size_t NC = (size_t)P.lall * P.kall * P.gall;
   const int nint = P.kmax - P.kmin + 1;
+  const FastDiv dg = FastDiv::make((unsigned)P.gall), dn = FastDiv::make((unsigned)nint);
   const long long ncell = (long long)P.lall * nint * P.gall;
   double pacc[7] = {0, 0, 0, 0, 0, 0, 0};
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(c % P.gall);
-    const int k = P.kmin + (int)((c / P.gall) % nint);
-    const int l = (int)(c / ((long long)P.gall * nint));
+    const unsigned ci = (unsigned)c, q = dg.div(ci), q2 = dn.div(q);   // ncell < 2^32
+    const int g = (int)(ci - q * (unsigned)P.gall);
+    const int k = P.kmin + (int)(q - q2 * (unsigned)nint);
+    const int l = (int)q2;
     const size_t i = L.f(l, k, g);
     CellIn in;
     in.rhog = x.a[A_rhog][i];
@@ -2041,11 +2061,13 @@ __global__ void __launch_bounds__(128) tlm_cell_kernel(StageIO io, Consts C, con
   const LayS& L = io.L;
   const size_t NC = io.NC;
   const int nint = P.kmax - P.kmin + 1;
+  const FastDiv dg = FastDiv::make((unsigned)P.gall), dn = FastDiv::make((unsigned)nint);
   const long long ncell = (long long)P.lall * nint * P.gall;
   for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell; c += (long long)gridDim.x * blockDim.x) {
-    const int g = (int)(c % P.gall);
-    const int k = P.kmin + (int)((c / P.gall) % nint);
-    const int l = (int)(c / ((long long)P.gall * nint));
+    const unsigned ci = (unsigned)c, q = dg.div(ci), q2 = dn.div(q);   // ncell < 2^32
+    const int g = (int)(ci - q * (unsigned)P.gall);
+    const int k = P.kmin + (int)(q - q2 * (unsigned)nint);
+    const int l = (int)q2;
     const size_t i = L.f(l, k, g);
     const In<Dual> x{io, l, g};
     CellInT<Dual> in;
@@ -2084,7 +2106,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s1_kernel(StageIO io) {
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
+    int g, k, l;
+    io.L.split(c, l, k, g);
     const In<Dual> in{io, l, g};
     stage1<Dual>(in, grid, k, [&](int f, const Dual& v) { io.WB[f * io.NC + c] = v.d; });
   }
@@ -2095,14 +2118,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s2_kernel(StageIO io) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   for (int c = threadIdx.x; c < GF_COUNT * io.P.kall; c += blockDim.x) grid[c] = io.P.grid[c];
   __syncthreads();
-  const size_t n = io.NC * 8 * io.P.ntr;
-  for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (size_t)gridDim.x * blockDim.x) {
-    const size_t c = w % io.NC;
-    const int j = (int)(w / io.NC);
-    const int g = (int)(c % io.L.G), k = (int)((c / io.L.G) % io.L.K), l = (int)(c / ((size_t)io.L.G * io.L.K));
-    const In<Dual> in{io, l, g};
-    io.WB[(W_F + j) * io.NC + c] = stage2<Dual>(in, grid, k, j).d;
-  }
+  const int nj = 8 * io.P.ntr;
+  for (int j = 0; j < nj; ++j)
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
+      int g, k, l;
+      io.L.split(c, l, k, g);
+      const In<Dual> in{io, l, g};
+      io.WB[(W_F + j) * io.NC + c] = stage2<Dual>(in, grid, k, j).d;
+    }
 }
 
 // S3 in forward mode: work-field tangents, and the values and tangents of the
@@ -2115,7 +2138,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s3_kernel(StageIO io) {
   double* const* x = io.x.a;
   double* const* dx = io.xb.a;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < io.NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % L.G), k = (int)((c / L.G) % L.K), l = (int)(c / ((size_t)L.G * L.K));
+    int g, k, l;
+    L.split(c, l, k, g);
     const In<Dual> in{io, l, g};
     const size_t ic = L.c(l, g);
     auto out = [&](int a, size_t i, const Dual& v) {
@@ -2159,7 +2183,8 @@ __global__ void __launch_bounds__(STAGE_THREADS) tlm_s4_kernel(StageIO io, Const
   double* const* x = io.x.a;
   double* const* dx = io.xb.a;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
-    const int g = (int)(c % L.G), k = (int)((c / L.G) % L.K), l = (int)(c / ((size_t)L.G * L.K));
+    int g, k, l;
+    L.split(c, l, k, g);
     const In<Dual> in{io, l, g};
     auto out = [&](int a, size_t i, const Dual& v) {
       x[a][i] = v.v;
@@ -2238,7 +2263,7 @@ cudaError_t launch_tlm_staged(const Problem& P, const Consts& C, const ArgPtrs& 
                               cudaStream_t stream) {
   StageIO io;
   io.P = P;
-  io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld};
+  io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld, FastDiv::make((unsigned)P.gall), FastDiv::make((unsigned)P.kall)};
   io.NC = (size_t)P.lall * P.kall * P.gall;
   io.x = x;
   io.xb = dx;
@@ -2295,7 +2320,7 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   if (recorded && mixed) return cudaErrorInvalidValue;
   StageIO io;
   io.P = P;
-  io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld};
+  io.L = LayS{P.kall, P.gall, P.lall, P.prec_ld, FastDiv::make((unsigned)P.gall), FastDiv::make((unsigned)P.kall)};
   io.NC = (size_t)P.lall * P.kall * P.gall;
   io.x = x;
   io.xb = xb;

@@ -131,6 +131,32 @@ struct DevStatus {
   int k, g, l, iters;
 };
 
+// Quotient of a 32-bit unsigned n by a divisor d >= 1 fixed for a launch,
+// by a multiplication (Granlund and Montgomery, "Division by invariant
+// integers using multiplication", PLDI 1994, Theorem 4.2): with
+// s = ceil(log2 d) and M = floor(2^(32+s) / d) + 1, 2^(32+s) < M d <=
+// 2^(32+s) + 2^s, so floor(n M / 2^(32+s)) = floor(n / d) for every n < 2^32.
+// M has 33 bits: m = M - 2^32 is kept and n M / 2^32 = umulhi(n, m) + n.
+// (A 64-bit division is a long instruction sequence with conversions, which
+// the FP64-bound kernels pay for.)
+struct FastDiv {
+  unsigned d, m, s;
+  __host__ __device__ static FastDiv make(unsigned d) {
+    FastDiv f{d, 0u, 0u};
+    while ((1ull << f.s) < d) ++f.s;
+    f.m = (unsigned)(((1ull << 32) * ((1ull << f.s) - d)) / d + 1ull);
+    return f;
+  }
+  __host__ __device__ __forceinline__ unsigned div(unsigned n) const {
+#ifdef __CUDA_ARCH__
+    const unsigned long long hi = __umulhi(n, m);
+#else
+    const unsigned long long hi = ((unsigned long long)n * m) >> 32;
+#endif
+    return (unsigned)((hi + n) >> s);
+  }
+};
+
 // Problem description handed to the kernels.  Array pointers follow the
 // all-regions layout; per-region calls use lall = 1.
 struct Problem {
