@@ -106,9 +106,18 @@ struct nsw6_handle {
   size_t stage_count = 0;
   // copy streams and per-chunk events of the pipelined host-memory path
   cudaStream_t s_in = nullptr, s_out = nullptr;
+  // captured host-memory pipeline (all arguments in pinned memory) and what it
+  // was captured for
+  cudaGraphExec_t hgraph = nullptr;
+  double* hgraph_args[A_COUNT] = {};
+  int hgraph_lall = 0, hgraph_mixed = -1, hgraph_math = -1, hgraph_itelim = 0;
+  double hgraph_dt = 0.0;
+  nsw6_params hgraph_params{};
+  nsw6_options hgraph_opts{};
   cudaEvent_t* ev_in = nullptr;    // a chunk's cell-kernel inputs have arrived
   cudaEvent_t* ev_in2 = nullptr;   // its remaining inputs have arrived
   cudaEvent_t* ev_done = nullptr;
+  cudaEvent_t ev_join_in = nullptr, ev_join_out = nullptr;   // the copy streams' ends
   cudaEvent_t ev_start = nullptr;
   // kernel timing: a ring of event triples folded into the sums when full
   int timing = 0;
@@ -665,31 +674,15 @@ int run_serial(nsw6_handle* h, int lall, double* const* a, double dt) {
 // chunk's regions; the precipitation outputs ([2][lall][gall] in the caller's
 // layout) are staged per chunk as [2][chunk][gall] and copied back in two
 // pieces.  Returns after all copies are done.
-int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
+// Enqueues the host-memory step as a pipeline of chunks of regions: copies in
+// on s_in, the step on cs, copies out on s_out, from an event recorded on cs;
+// cs ends waiting for both copy streams.  rc: a fill_problem error.
+cudaError_t enqueue_host(nsw6_handle* h, int lall, double* const* args, double* const* dev, double dt, cudaStream_t cs,
+                         int& rc) {
   const int K = h->kall, G = h->gall;
-  for (int i = 0; i < A_COUNT; ++i)
-    if ((arg_is_read(i) || arg_is_written(i)) && !args[i]) return NSW6_ERR_BAD_ARG;
-  if (h->opts.aerosol_indirect && !args[A_unccn]) return NSW6_ERR_BAD_ARG;
-  double* dev[A_COUNT];
-  int rc = ensure_stage(h, dev);
-  if (rc != NSW6_OK) return rc;
-  if (!h->s_in) {
-    if (cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming) != cudaSuccess)
-      return NSW6_ERR_CUDA;
-    h->ev_in = new cudaEvent_t[h->lall_max]();
-    h->ev_in2 = new cudaEvent_t[h->lall_max]();
-    h->ev_done = new cudaEvent_t[h->lall_max]();
-    for (int i = 0; i < h->lall_max; ++i)
-      if (cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
-          cudaEventCreateWithFlags(&h->ev_in2[i], cudaEventDisableTiming) != cudaSuccess ||
-          cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming) != cudaSuccess)
-        return NSW6_ERR_CUDA;
-  }
-  // copies start after the work already queued on the handle's stream
-  if (cudaEventRecord(h->ev_start, h->stream) != cudaSuccess || cudaStreamWaitEvent(h->s_in, h->ev_start, 0) != cudaSuccess)
-    return NSW6_ERR_CUDA;
+  rc = NSW6_OK;
+  if (cudaEventRecord(h->ev_start, cs) != cudaSuccess || cudaStreamWaitEvent(h->s_in, h->ev_start, 0) != cudaSuccess)
+    return cudaErrorUnknown;
   // Chunks of regions: the first chunk's copy in and the last chunk's copy
   // out are not hidden behind compute, so those two are one region each; the
   // FP64 step (compute above the copies) takes the rest in about four chunks
@@ -729,12 +722,12 @@ int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
       if (err == cudaSuccess) err = cudaEventRecord(group == 0 ? h->ev_in[nchunk] : h->ev_in2[nchunk], h->s_in);
     }
     if (err != cudaSuccess) break;
-    if ((err = cudaStreamWaitEvent(h->stream, h->ev_in[nchunk], 0)) != cudaSuccess) break;
+    if ((err = cudaStreamWaitEvent(cs, h->ev_in[nchunk], 0)) != cudaSuccess) break;
     Problem P;
     rc = fill_problem(h, nl, cdev, dt, P);
     if (rc != NSW6_OK) break;
-    if ((err = launch_step(P, h->C, h->stream, nullptr, h->ev_in2[nchunk])) != cudaSuccess) break;
-    if ((err = cudaEventRecord(h->ev_done[nchunk], h->stream)) != cudaSuccess) break;
+    if ((err = launch_step(P, h->C, cs, nullptr, h->ev_in2[nchunk])) != cudaSuccess) break;
+    if ((err = cudaEventRecord(h->ev_done[nchunk], cs)) != cudaSuccess) break;
     if ((err = cudaStreamWaitEvent(h->s_out, h->ev_done[nchunk], 0)) != cudaSuccess) break;
     for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
       if (!arg_is_written(i)) continue;
@@ -750,10 +743,105 @@ int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
       }
     }
   }
-  const cudaError_t se = cudaStreamSynchronize(h->s_out);
-  const cudaError_t si = cudaStreamSynchronize(h->s_in);
+  // cs waits for the last copies out (and the copy-in stream, which ended before them)
+  if (err == cudaSuccess && rc == NSW6_OK) {
+    if ((err = cudaEventRecord(h->ev_join_out, h->s_out)) == cudaSuccess &&
+        (err = cudaEventRecord(h->ev_join_in, h->s_in)) == cudaSuccess &&
+        (err = cudaStreamWaitEvent(cs, h->ev_join_out, 0)) == cudaSuccess)
+      err = cudaStreamWaitEvent(cs, h->ev_join_in, 0);
+  }
+  return err;
+}
+
+// True when every argument the host entry copies is in page-locked memory
+// (a stream capture takes copies from page-locked memory only).
+bool host_args_pinned(nsw6_handle* h, double* const* args) {
+  for (int i = 0; i < A_COUNT; ++i) {
+    if (!args[i] || !(arg_is_read(i) || arg_is_written(i) || (i == A_unccn && h->opts.aerosol_indirect))) continue;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, args[i]) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    if (at.type != cudaMemoryTypeHost) return false;
+  }
+  return true;
+}
+
+int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
+  for (int i = 0; i < A_COUNT; ++i)
+    if ((arg_is_read(i) || arg_is_written(i)) && !args[i]) return NSW6_ERR_BAD_ARG;
+  if (h->opts.aerosol_indirect && !args[A_unccn]) return NSW6_ERR_BAD_ARG;
+  if (!(dt > 0.0) || !std::isfinite(dt)) return NSW6_ERR_BAD_ARG;
+  double* dev[A_COUNT];
+  int rc = ensure_stage(h, dev);
   if (rc != NSW6_OK) return rc;
-  if (err != cudaSuccess || se != cudaSuccess || si != cudaSuccess) return NSW6_ERR_CUDA;
+  if (!h->s_in) {
+    if (cudaStreamCreateWithFlags(&h->s_in, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->s_out, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_start, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join_in, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->ev_join_out, cudaEventDisableTiming) != cudaSuccess)
+      return NSW6_ERR_CUDA;
+    h->ev_in = new cudaEvent_t[h->lall_max]();
+    h->ev_in2 = new cudaEvent_t[h->lall_max]();
+    h->ev_done = new cudaEvent_t[h->lall_max]();
+    for (int i = 0; i < h->lall_max; ++i)
+      if (cudaEventCreateWithFlags(&h->ev_in[i], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&h->ev_in2[i], cudaEventDisableTiming) != cudaSuccess ||
+          cudaEventCreateWithFlags(&h->ev_done[i], cudaEventDisableTiming) != cudaSuccess)
+        return NSW6_ERR_CUDA;
+  }
+  if (launch_prepare() != cudaSuccess) return NSW6_ERR_CUDA;
+  // With the arguments in page-locked memory the pipeline (some 400 copies and
+  // launches) is captured once into a CUDA graph and replayed: one launch a
+  // step, so that a host thread descheduled while it issues the work does
+  // not leave the copy engines and the SMs waiting.  It is re-captured when
+  // the arrays, lall, dt, the parameters, the switches or the precision change.
+  if (host_args_pinned(h, args)) {
+    bool same = h->hgraph && h->hgraph_lall == lall && h->hgraph_dt == dt && h->hgraph_mixed == h->mixed &&
+                h->hgraph_math == h->math_lib && h->hgraph_itelim == h->itelim &&
+                std::memcmp(&h->hgraph_params, &h->params, sizeof(nsw6_params)) == 0 &&
+                std::memcmp(&h->hgraph_opts, &h->opts, sizeof(nsw6_options)) == 0;
+    for (int i = 0; same && i < A_COUNT; ++i) same = h->hgraph_args[i] == args[i];
+    if (!same) {
+      if (h->hgraph) {
+        cudaGraphExecDestroy(h->hgraph);
+        h->hgraph = nullptr;
+      }
+      if (!h->cap_stream && cudaStreamCreateWithFlags(&h->cap_stream, cudaStreamNonBlocking) != cudaSuccess)
+        return NSW6_ERR_CUDA;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(h->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return NSW6_ERR_CUDA;
+      const cudaError_t qe = enqueue_host(h, lall, args, dev, dt, h->cap_stream, rc);
+      const cudaError_t ce = cudaStreamEndCapture(h->cap_stream, &g);
+      if (rc != NSW6_OK || qe != cudaSuccess || ce != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        cudaGetLastError();
+        return rc != NSW6_OK ? rc : NSW6_ERR_CUDA;
+      }
+      const cudaError_t ie = cudaGraphInstantiate(&h->hgraph, g, 0);
+      cudaGraphDestroy(g);
+      if (ie != cudaSuccess) {
+        h->hgraph = nullptr;
+        return NSW6_ERR_CUDA;
+      }
+      for (int i = 0; i < A_COUNT; ++i) h->hgraph_args[i] = args[i];
+      h->hgraph_lall = lall;
+      h->hgraph_dt = dt;
+      h->hgraph_mixed = h->mixed;
+      h->hgraph_math = h->math_lib;
+      h->hgraph_itelim = h->itelim;
+      h->hgraph_params = h->params;
+      h->hgraph_opts = h->opts;
+    }
+    if (cudaGraphLaunch(h->hgraph, h->stream) != cudaSuccess) return NSW6_ERR_CUDA;
+    return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
+  }
+  const cudaError_t err = enqueue_host(h, lall, args, dev, dt, h->stream, rc);
+  const cudaError_t se = cudaStreamSynchronize(h->stream);
+  if (rc != NSW6_OK) return rc;
+  if (err != cudaSuccess || se != cudaSuccess) return NSW6_ERR_CUDA;
   return nsw6_last_error(h, nullptr, nullptr, nullptr, nullptr);
 }
 
@@ -829,6 +917,7 @@ int nsw6_destroy(nsw6_handle* h) {
   cudaFree(h->d_satq);
   cudaFree(h->d_status);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->hgraph) cudaGraphExecDestroy(h->hgraph);
   if (h->cap_stream) cudaStreamDestroy(h->cap_stream);
   if (h->s_in) cudaStreamDestroy(h->s_in);
   if (h->s_out) cudaStreamDestroy(h->s_out);
@@ -841,6 +930,8 @@ int nsw6_destroy(nsw6_handle* h) {
   delete[] h->ev_in2;
   delete[] h->ev_done;
   if (h->ev_start) cudaEventDestroy(h->ev_start);
+  if (h->ev_join_in) cudaEventDestroy(h->ev_join_in);
+  if (h->ev_join_out) cudaEventDestroy(h->ev_join_out);
   cudaFree(h->d_stage);
   cudaFree(h->d_dparam);
   cudaFree(h->d_pbar);

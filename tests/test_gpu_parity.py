@@ -182,6 +182,45 @@ def test_gpu_host_entry_equals_device_entry(lall, lall_max, precision, options):
     drv.close()
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gpu_host_entry_pinned_graph(precision):
+    """With the arguments in page-locked memory the host entry captures its
+    pipeline into a CUDA graph once and replays it: two steps in the same
+    arrays (capture, then replay on the new contents) and one in a second set
+    of arrays (a new capture) equal the device entry bit for bit."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=300, kall=42, lall=5, seed=9, variant="standard")
+    st = make_state(spec, out_fill=np.nan)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall)
+    drv.set_precision(precision)
+
+    def pinned():
+        out = {}
+        for n in ARG_NAMES:
+            t = torch.empty(st[n].shape, dtype=torch.float64, pin_memory=True)
+            t.numpy()[...] = st[n]
+            out[n] = t.numpy()
+        return out
+
+    host = pinned()
+    dev = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    for step in range(2):
+        drv.run(host, dt=spec.dt)
+        drv.run(dev, dt=spec.dt)
+        torch.cuda.synchronize()
+        for n in OUTPUT_NAMES:
+            assert np.array_equal(host[n].view(np.int64), dev[n].cpu().numpy().view(np.int64)), (n, step)
+    host2 = pinned()
+    dev2 = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    drv.run(host2, dt=spec.dt)
+    drv.run(dev2, dt=spec.dt)
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        assert np.array_equal(host2[n].view(np.int64), dev2[n].cpu().numpy().view(np.int64)), n
+    drv.close()
+
+
 @pytest.mark.parametrize("variant,seed", [("standard", 1011), ("convective", 1012)])
 def test_gpu_matches_oracle_on_stepped_states(variant, seed):
     """Steps two and three of a run, each from the oracle's own state after the
