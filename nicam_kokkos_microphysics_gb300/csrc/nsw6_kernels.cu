@@ -915,6 +915,12 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           divergence(f, c);
           source(f + 1, c);
+          if (f == 2) {
+            // the FP32 departure distance of the three FP32 fluxes, converted once,
+            // in the upper half of the slot whose lower half now holds FP32 sources
+            const int k = c / COL_TG, g = g0 + c % COL_TG;
+            if (g < G && k >= kmin && k <= kmax) FF(S_RHOF)[ncell + c] = (float)zdis0[(size_t)k * G + g];
+          }
         }
         __syncthreads();
       }
@@ -923,8 +929,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
           float fl = 0.0f;
           if (g < G && k >= kmin && k <= kmax)
-            fl = flux_integral_f<COL_TG>(rf + gx, dgzf, k, S.kc[c], (float)zdis0[(size_t)k * G + g], bmn_f[k],
-                                         bmx_f[k]);
+            fl = flux_integral_f<COL_TG>(rf + gx, dgzf, k, S.kc[c], rf[ncell + c], bmn_f[k], bmx_f[k]);
           ff[c] = fl;
         }
         __syncthreads();
@@ -960,8 +965,13 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
         S.kc[c] = (unsigned char)departure_cell(gzs, zkey + K, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
       }
       F(S_BASE)[c] = qh;
-      if (MIX) FF(S_RHOF)[c] = (float)(qh * F(S_KINV)[c]);
-      else F(S_RHOF)[c] = qh * F(S_KINV)[c];
+      if (MIX) {
+        FF(S_RHOF)[c] = (float)(qh * F(S_KINV)[c]);
+        // the half levels' FP32 departure distance, converted once (upper half)
+        if (g < G && k >= kmin + 1 && k <= kmax) FF(S_RHOF)[ncell + c] = (float)zdis0h[(size_t)k * G + g];
+      } else {
+        F(S_RHOF)[c] = qh * F(S_KINV)[c];
+      }
     }
     __syncthreads();
     for (int w = 0; w < 2; ++w) {
@@ -976,8 +986,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
           float fl = 0.0f;
           if (g < G && k >= kmin + 1 && k <= kmax)
-            fl = flux_integral_f<COL_TG>(rf + gx, dgzhf, k, S.kc[c], (float)zdis0h[(size_t)k * G + g], bmn_h[k],
-                                         bmx_f[k]);
+            fl = flux_integral_f<COL_TG>(rf + gx, dgzhf, k, S.kc[c], rf[ncell + c], bmn_h[k], bmx_f[k]);
           ff[c] = fl;
         }
         __syncthreads();
@@ -1004,8 +1013,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
           float fl = 0.0f;
           if (g < G && k >= kmin + 1 && k <= kmax)
-            fl = flux_integral_f<COL_TG>(rf + gx, dgzhf, k, S.kc[c], (float)zdis0h[(size_t)k * G + g], bmn_h[k],
-                                         bmx_f[k]);
+            fl = flux_integral_f<COL_TG>(rf + gx, dgzhf, k, S.kc[c], rf[ncell + c], bmn_h[k], bmx_f[k]);
           ff[c] = fl;
         }
         __syncthreads();
