@@ -737,6 +737,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
   // c = threadIdx.x + j blockDim.x, j < NJ (NJ covers column_threads()).
   constexpr int NJ = COL_TG == 16 ? 4 : 5;
   double r_rgsh[NJ], r_c2w0[NJ], r_c2w1[NJ];   // gam2h / gsgam2h and C2Wfact at half level k
+  float r_rgshf[NJ];                           // MIX: gam2h / gsgam2h in FP32 (it scales FP32 sources only)
 
   // ---- metric factors, kinetic energy, zeroed accumulators
   //      (mod_precip_transport.cpp:715-770, cnvvar_rhogkin_in mod_debug.cpp:269-330)
@@ -744,6 +745,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
   for (int j = 0; j < NJ; ++j) {
     const int c = threadIdx.x + j * blockDim.x;
     r_rgsh[j] = r_c2w0[j] = r_c2w1[j] = 0.0;
+    r_rgshf[j] = 0.0f;
     if (c >= ncell) continue;
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
     for (int s = S_KINH; s <= S_DQG; ++s) F(s)[c] = 0.0;
@@ -771,7 +773,8 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     }
     if (k >= kmin + 1 && k <= kmax) {
       r_c2w0[j] = div_rn(afact[k], gsg, rgsg) * P.gsgam2h[i];
-      r_rgsh[j] = P.gam2h[i] / P.gsgam2h[i];
+      if (MIX) r_rgshf[j] = float(P.gam2h[i]) / float(P.gsgam2h[i]);
+      else r_rgsh[j] = P.gam2h[i] / P.gsgam2h[i];
     }
   }
   __syncthreads();
@@ -958,18 +961,22 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       const int c = threadIdx.x + j * blockDim.x;
       if (c >= ncell) continue;
       const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-      double qh = 0.0;
-      if (g < G && k >= kmin + 1 && k <= kmax) {
-        const size_t i = off + (size_t)k * G + g;
-        qh = 0.5 * (q_n[i - off] + q_n[i - off - G]) * r_rgsh[j];
-        S.kc[c] = (unsigned char)departure_cell(gzs, zkey + K, k, zdis0h[i - off], bmn_h[k], bmx_h[k], kmin + 1, kmax);
-      }
-      F(S_BASE)[c] = qh;
+      const bool hv = g < G && k >= kmin + 1 && k <= kmax;
+      if (hv)
+        S.kc[c] = (unsigned char)departure_cell(gzs, zkey + K, k, zdis0h[(size_t)k * G + g], bmn_h[k], bmx_h[k], kmin + 1,
+                                                kmax);
       if (MIX) {
-        FF(S_RHOF)[c] = (float)(qh * F(S_KINV)[c]);
+        // qh scales the FP32 sources of the two half-level fluxes only: FP32
+        float qh = 0.0f;
+        if (hv) qh = 0.5f * (float(q_n[(size_t)k * G + g]) + float(q_n[(size_t)(k - 1) * G + g])) * r_rgshf[j];
+        FF(S_BASE)[c] = qh;
+        FF(S_RHOF)[c] = qh * float(F(S_KINV)[c]);
         // the half levels' FP32 departure distance, converted once (upper half)
-        if (g < G && k >= kmin + 1 && k <= kmax) FF(S_RHOF)[ncell + c] = (float)zdis0h[(size_t)k * G + g];
+        if (hv) FF(S_RHOF)[ncell + c] = (float)zdis0h[(size_t)k * G + g];
       } else {
+        double qh = 0.0;
+        if (hv) qh = 0.5 * (q_n[(size_t)k * G + g] + q_n[(size_t)(k - 1) * G + g]) * r_rgsh[j];
+        F(S_BASE)[c] = qh;
         F(S_RHOF)[c] = qh * F(S_KINV)[c];
       }
     }
@@ -992,12 +999,12 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
         __syncthreads();
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-          double r = 0.0;
+          float r = 0.0f;
           if (g < G && k >= kmin + 1 && k <= kmax) {
             F(S_DKINV)[c] = F(S_DKINV)[c] - (double)((ff[c] - ff[c - COL_TG]) * rdgzhf[k]);
-            r = F(S_BASE)[c] * P.rhogw[off + (size_t)k * G + g];
+            r = FF(S_BASE)[c] * float(P.rhogw[off + (size_t)k * G + g]);
           }
-          FF(S_RHOF)[c] = (float)r;
+          FF(S_RHOF)[c] = r;
         }
         __syncthreads();
         continue;
