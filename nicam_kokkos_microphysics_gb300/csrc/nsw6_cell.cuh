@@ -159,6 +159,9 @@ __device__ __forceinline__ bool lt_np(double a, double b) {
   return ba < 0 && ma > (fp_bits(b) & FP_ABS) && ma <= FP_INF;
 }
 __device__ __forceinline__ double max_np(double a, double b) { return lt_np(a, b) ? b : a; }
+// x + 0.0 without the FP64 pipe: -0 becomes +0, every other value stays
+// (a NaN keeps its payload, where the addition would give the canonical NaN)
+__device__ __forceinline__ double plus_zero(double x) { return fp_bits(x) == -0x7FFFFFFFFFFFFFFFll - 1 ? 0.0 : x; }
 __device__ __forceinline__ double maxz(double x) { return lt_z(x) ? 0.0 : x; }                // max(x, 0)
 __device__ __forceinline__ double maxc(double x, double c) { return fp_lt_pos(x, c) ? c : x; }   // max(x, c)
 __device__ __forceinline__ double minc(double x, double c) { return gt_c(x, c) ? c : x; }       // min(x, c)

@@ -849,7 +849,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       switch (f) {
         case 0:
           F(dqs_slot)[c] = -d;
-          if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = 0.0 + div_rn(-fk, dt, P.rdt);
+          if (nq == I_QR) P.GPREC[off + (size_t)k * G + g] = plus_zero(div_rn(-fk, dt, P.rdt));
           break;
         case 1: F(S_DRHOE)[c] = F(S_DRHOE)[c] - d; break;
         case 2: F(S_DRHOPHI)[c] = F(S_DRHOPHI)[c] - d; break;
@@ -1078,11 +1078,11 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const double rw = P.rhogw[i] + (MIX ? (double)FF(S_DRHOGW)[c] : F(S_DRHOGW)[c]);
     P.rhogw[i] = rw;
     if (!MIX) F(S_DRHOGW)[c] = rw;   // MIX: the FP32 view of this slot is still being read
-    // tracers in order QV..QG; QV, QC and QI add exact zeros
+    // tracers in order QV..QG; QV, QC and QI add exact zeros (plus_zero: the addition of +0 on the integer pipe)
     double rhog = P.rhog[i];
     const double zz = P.z[i];
-    P.rhogq[iq + (size_t)I_QV * KG] = P.rhogq[iq + (size_t)I_QV * KG] + 0.0;
-    P.rhogq[iq + (size_t)I_QC * KG] = P.rhogq[iq + (size_t)I_QC * KG] + 0.0;
+    P.rhogq[iq + (size_t)I_QV * KG] = plus_zero(P.rhogq[iq + (size_t)I_QV * KG]);
+    P.rhogq[iq + (size_t)I_QC * KG] = plus_zero(P.rhogq[iq + (size_t)I_QC * KG]);
     P.rhogq[iq + (size_t)I_QR * KG] = P.rhogq[iq + (size_t)I_QR * KG] + dqr;
     rhog = rhog + dqr;
     rhoge = rhoge - dqr * GRAV * zz;
@@ -1092,7 +1092,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       rhog = rhog + dqi;
       rhoge = rhoge - dqi * GRAV * zz;
     } else {
-      P.rhogq[iq + (size_t)I_QI * KG] = P.rhogq[iq + (size_t)I_QI * KG] + 0.0;
+      P.rhogq[iq + (size_t)I_QI * KG] = plus_zero(P.rhogq[iq + (size_t)I_QI * KG]);
     }
     P.rhogq[iq + (size_t)I_QS * KG] = P.rhogq[iq + (size_t)I_QS * KG] + dqs;
     rhog = rhog + dqs;
@@ -1218,16 +1218,16 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       const size_t ic = (size_t)l * G + g;
       const size_t r0 = (size_t)l * G + g, r1 = P.prec_ld + r0;
       const double* acc = S.colacc;
-      P.precip[r0] = 0.0 + acc[0 * COL_TG + gx];
-      P.precip[r1] = 0.0 + acc[1 * COL_TG + gx];
+      P.precip[r0] = plus_zero(acc[0 * COL_TG + gx]);
+      P.precip[r1] = plus_zero(acc[1 * COL_TG + gx]);
       P.iso1[r0] = 0.0;
       P.iso1[r1] = 0.0;
       P.iso2[r0] = 0.0;
       P.iso2[r1] = 0.0;
-      P.precip_lh_heat[ic] = 0.0 + acc[2 * COL_TG + gx];
-      P.precip_rhoe[ic] = 0.0 + acc[3 * COL_TG + gx];
-      P.precip_rhophi[ic] = 0.0 + acc[4 * COL_TG + gx];
-      P.precip_rhokin[ic] = 0.0 + acc[5 * COL_TG + gx];
+      P.precip_lh_heat[ic] = plus_zero(acc[2 * COL_TG + gx]);
+      P.precip_rhoe[ic] = plus_zero(acc[3 * COL_TG + gx]);
+      P.precip_rhophi[ic] = plus_zero(acc[4 * COL_TG + gx]);
+      P.precip_rhokin[ic] = plus_zero(acc[5 * COL_TG + gx]);
     }
   }
   __syncthreads();
