@@ -886,7 +886,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_kernel(StageIO io, Const
 // converged value as satadjust_t does: with F(T) = T cv(T) + qsat(T) LHV0 -
 // Emoist, dT = -dF / F_T at the last iterate.  Adjoints go to S3's outputs at
 // this level and its neighbours and to the metric factors, atomically.
-__global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Consts C) {
+__global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Consts C, int pass) {
   __shared__ double grid[GF_COUNT * MAX_KALL];
   __shared__ double tab[FM_TABLE_DOUBLES];
   stage_smem(io.P, grid, tab);
@@ -899,7 +899,7 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
   const double* dfact = grid + GF_DFACT * K;
   const size_t NC = io.NC;
   const size_t G = io.L.G;
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x) {
+  auto cell = [&](const size_t c, const bool first) {
     int g, k, l;
     io.L.split(c, l, k, g);
     const bool interior = (k >= kmin && k <= kmax);
@@ -991,18 +991,36 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
     // saturation adjustment (satadjust_t's iteration, then its implicit derivative pieces)
     bool sat = false;
     double ts = 0, qsT = 0, cvT = 0, FT = 0, dqs = 0, qd_l = 0;
+    int sc = 0;
     if (interior) {
       qd_l = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qd_l = qd_l - q[n];
-      double tv = tem;
       // the test decided in FP32 where its margin allows (sat_screen_liq)
-      int sc = sat_screen_liq(tv, rho1, qsum, float(C.LovR_liq));
+      sc = sat_screen_liq(tem, rho1, qsum, float(C.LovR_liq));
       if (sc < 0) {
-        const double rtem0 = 1.0 / fp_max_pos(tv, TEM_MIN);
+        const double rtem0 = 1.0 / fp_max_pos(tem, TEM_MIN);
         const double psat0 = PSAT0 * fm.exp(C.LovR_liq * (C.RTEM00 - rtem0));
-        sc = (qsum - psat0 / (rho1 * RVAP * tv) > EPS) ? 1 : 0;
+        sc = (qsum - psat0 / (rho1 * RVAP * tem) > EPS) ? 1 : 0;
       }
+    }
+    if (first) {
+      // A saturated cell goes to the list of the second pass, whose warps it
+      // fills: here its Newton iteration would hold its level's whole warp.
+      // One atomic per warp on the list's count.
+      const unsigned m = __activemask();
+      const unsigned b = __ballot_sync(m, sc != 0);
+      if (b) {
+        const int lane = threadIdx.x & 31, leader = __ffs(m) - 1;
+        unsigned base = 0u;
+        if (lane == leader) base = atomicAdd(io.P.satq, (unsigned)__popc(b));
+        base = __shfl_sync(m, base, leader);
+        if (sc) io.P.satq[1 + base + __popc(b & ((1u << lane) - 1u))] = (unsigned)c;
+      }
+      if (sc) return;
+    }
+    if (interior) {
+      double tv = tem;
       if (sc) {
         double qv[6];
 #pragma unroll
@@ -1288,6 +1306,14 @@ __global__ void __launch_bounds__(STAGE_THREADS) adj_s4_hw_kernel(StageIO io, Co
 #pragma unroll
     for (int n = 0; n < 6; ++n) WBadd(W_RQ_N + n, c, b_rq[n]);
     XBadd(A_gsgam2, c, b_gsg);
+  };
+  if (pass == 0) {
+    for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < NC; c += (size_t)gridDim.x * blockDim.x)
+      cell(c, true);
+  } else {
+    const unsigned n = io.P.satq[0];
+    for (unsigned e = blockIdx.x * blockDim.x + threadIdx.x; e < n; e += gridDim.x * blockDim.x)
+      cell(io.P.satq[1 + e], false);
   }
 }
 
@@ -2350,10 +2376,14 @@ cudaError_t launch_adj_column_staged(const Problem& P, const Consts& C, const Ar
   adj_seed_columns_kernel<<<64, 256, 0, stream>>>(io);
   // S4 recorded also with the mixed-phase saturation adjustment and with
   // KIN2KIN, which the hand-written sweep does not cover
-  if (recorded || (P.opt && C.opt_expice == 0.0) || io.kin2kin)
+  if (recorded || (P.opt && C.opt_expice == 0.0) || io.kin2kin) {
     adj_s4_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, C, tm);
-  else
-    adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C);
+  } else {
+    // first pass: the unsaturated cells, the saturated ones listed; second: those
+    if ((e = cudaMemsetAsync(P.satq, 0, sizeof(unsigned), stream)) != cudaSuccess) return e;
+    adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C, 0);
+    adj_s4_hw_kernel<<<152 * 4, STAGE_THREADS, 0, stream>>>(io, C, 1);
+  }
   adj_s3_hw_kernel<<<152 * 8, STAGE_THREADS, 0, stream>>>(io);
   if (recorded)
     adj_s2_kernel<<<blocks, STAGE_THREADS, 0, stream>>>(io, tm);
