@@ -808,12 +808,18 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const double* rhogq_n = P.rhogq + offq + (size_t)nq * KG;
     const double* q_n = P.q + offq + (size_t)nq * KG;
 
-    // departure cells (full levels) and rhoq = rhogq * rgs
+    // departure cells (full levels) and rhoq = rhogq * rgs, which is also
+    // the source of the first flux (the mass flux)
     for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
       const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-      if (g >= G) continue;
+      if (g >= G) {
+        F(S_RHOF)[c] = 0.0;
+        continue;
+      }
       const size_t i = (size_t)k * G + g;
-      F(S_BASE)[c] = rhogq_n[i] * F(S_RGS)[c];
+      const double b = rhogq_n[i] * F(S_RGS)[c];
+      F(S_BASE)[c] = b;
+      F(S_RHOF)[c] = b;
       if (k >= kmin && k <= kmax)
         S.kc[c] = (unsigned char)departure_cell(gzh, zkey, k, zdis0[i], bmn_f[k], bmx_f[k], kmin, kmax);
     }
@@ -876,10 +882,9 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
         }
       }
     };
-    // the divergence of flux f and the source of flux f + 1 share a pass
+    // the divergence of flux f and the source of flux f + 1 share a pass (the
+    // source of flux 0 is rhoq, written above)
     if (!MIX) {
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
-      __syncthreads();
       for (int f = 0; f < 6; ++f) {
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
@@ -904,8 +909,6 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       float* ff = FF(S_F);
       const float* dgzf = gf;
       const float* rdgzf = gf + 2 * K;
-      for (int c = threadIdx.x; c < ncell; c += blockDim.x) source(0, c);
-      __syncthreads();
       for (int f = 0; f < 3; ++f) {
         for (int c = threadIdx.x; c < ncell; c += blockDim.x) {
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
