@@ -151,14 +151,16 @@ __device__ __forceinline__ bool lt_nn(double d, double p) {   // d < p
   return bp > 0 && bp <= FP_INF && (fp_bits(d) & FP_ABS) < bp;
 }
 __device__ __forceinline__ double min_nn(double p, double d) { return lt_nn(d, p) ? d : p; }
-// a < b for a b that is not positive (b = -d of the limiters: -+0, negative,
-// or NaN): a must be negative, not NaN, and of larger magnitude; max(a, b) as
-// Kokkos::max, (a < b) ? b : a
-__device__ __forceinline__ bool lt_np(double a, double b) {
+// a < -d for a d that is not negative (the limiters' d again): a must be
+// negative, not NaN, and of larger magnitude; max(a, -d) as Kokkos::max,
+// (a < -d) ? -d : a, with -d formed by flipping the sign bit
+__device__ __forceinline__ bool lt_nd(double a, double d) {
   const long long ba = fp_bits(a), ma = ba & FP_ABS;
-  return ba < 0 && ma > (fp_bits(b) & FP_ABS) && ma <= FP_INF;
+  return ba < 0 && ma > (fp_bits(d) & FP_ABS) && ma <= FP_INF;
 }
-__device__ __forceinline__ double max_np(double a, double b) { return lt_np(a, b) ? b : a; }
+__device__ __forceinline__ double max_nd(double a, double d) {
+  return lt_nd(a, d) ? __longlong_as_double(fp_bits(d) ^ (-0x7FFFFFFFFFFFFFFFll - 1)) : a;
+}
 // x + 0.0 without the FP64 pipe: -0 becomes +0, every other value stays
 // (a NaN keeps its payload, where the addition would give the canonical NaN)
 __device__ __forceinline__ double plus_zero(double x) { return fp_bits(x) == -0x7FFFFFFFFFFFFFFFll - 1 ? 0.0 : x; }
@@ -194,9 +196,9 @@ __device__ __forceinline__ bool lt_nn(const T& d, const T& p) { return d < p; }
 template <class T>
 __device__ __forceinline__ T min_nn(const T& p, const T& d) { return dmin(p, d); }
 template <class T>
-__device__ __forceinline__ bool lt_np(const T& a, const T& b) { return a < b; }
+__device__ __forceinline__ bool lt_nd(const T& a, const T& d) { return a < -d; }
 template <class T>
-__device__ __forceinline__ T max_np(const T& a, const T& b) { return dmax(a, b); }
+__device__ __forceinline__ T max_nd(const T& a, const T& d) { return dmax(a, -d); }
 
 // The liquid saturation test qsum - qsat(T) > EPS of the saturation
 // adjustment (mod_satadjust.cpp:771-896), decided in FP32 where its margin
@@ -667,11 +669,11 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
       qs_t = +Psdep + Psacw + Psfw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci + Psfi - Pssub - Psmlt - Pracs - Pgacs;
     if (lg) qg_t = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pgaci + Pracs + Pgacs - Pgsub - Pgmlt;
   }
-  qc_t = max_np(qc_t, -dqc_dt);
-  qr_t = max_np(qr_t, -dqr_dt);
-  qi_t = max_np(qi_t, -dqi_dt);
-  qs_t = max_np(qs_t, -dqs_dt);
-  qg_t = max_np(qg_t, -dqg_dt);
+  qc_t = max_nd(qc_t, dqc_dt);
+  qr_t = max_nd(qr_t, dqr_dt);
+  qi_t = max_nd(qi_t, dqi_dt);
+  qs_t = max_nd(qs_t, dqs_dt);
+  qg_t = max_nd(qg_t, dqg_dt);
   const R qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
   D drq[6];
   drq[0] = rhog * D(qv_t) * dt;

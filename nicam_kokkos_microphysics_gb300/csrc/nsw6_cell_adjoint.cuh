@@ -575,8 +575,8 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const R qs_t0 = +Psdep + Psacw + Piacr_s + Psacr_s + Psaut + Praci_s + Psaci - Pssub - Psmlt - Pracs;
   const R qg_t0 = +Pgdep + Pgacw + Piacr_g + Psacr_g + Pgacr + Pgfrz + Praci_g + Pracs - Pgsub - Pgmlt;
   // qx_t = max(qx_t0, -dqx_dt): true when the tendency itself is kept
-  const bool kc_ = !lt_np(qc_t0, -dqc_dt), kr_ = !lt_np(qr_t0, -dqr_dt), ki_ = !lt_np(qi_t0, -dqi_dt);
-  const bool ks_ = !lt_np(qs_t0, -dqs_dt), kg_ = !lt_np(qg_t0, -dqg_dt);
+  const bool kc_ = !lt_nd(qc_t0, dqc_dt), kr_ = !lt_nd(qr_t0, dqr_dt), ki_ = !lt_nd(qi_t0, dqi_dt);
+  const bool ks_ = !lt_nd(qs_t0, dqs_dt), kg_ = !lt_nd(qg_t0, dqg_dt);
   const R qc_t = kc_ ? qc_t0 : -dqc_dt, qr_t = kr_ ? qr_t0 : -dqr_dt, qi_t = ki_ ? qi_t0 : -dqi_dt;
   const R qs_t = ks_ ? qs_t0 : -dqs_dt, qg_t = kg_ ? qg_t0 : -dqg_dt;
   const R qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
