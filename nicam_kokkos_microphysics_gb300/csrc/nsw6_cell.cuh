@@ -101,72 +101,15 @@ __device__ __forceinline__ float sel(bool on, float x) { return on ? x : copysig
 __device__ __forceinline__ double per_dt(double q, double dt, double rdt) { return div_rn(q, dt, rdt); }
 __device__ __forceinline__ float per_dt(float q, float, float rdt) { return q * rdt; }
 
-// fac == 1 and x >= 0 in the limiters: for doubles from the bit patterns, on
-// the integer pipe (an FP64 comparison takes an FP64-pipe slot, as an FMA
-// does), with the IEEE comparisons' results for every double.
-__device__ __forceinline__ bool is_one(double x) { return fp_bits(x) == 0x3FF0000000000000ll; }
-__device__ __forceinline__ bool is_nonneg(double x) {   // +0 .. +inf, or -0
-  const long long b = fp_bits(x);
-  return (b >= 0 && b <= FP_INF) || b == -0x7FFFFFFFFFFFFFFFll - 1;
-}
+// The comparisons of the cell physics with constants and the min / max they
+// select: for doubles the integer-pipe forms of nsw6_fpcmp.cuh (an FP64
+// comparison takes an FP64-pipe slot, as an FMA does); the other types compare
+// natively (FP32 comparisons are cheap, the derivative types compare values).
 template <class T>
 __device__ __forceinline__ bool is_one(const T& x) { return x == T(1.0); }
 template <class T>
 __device__ __forceinline__ bool is_nonneg(const T& x) { return x >= T(0.0); }
 
-// Comparisons with constants (c > 0 normal, in lt_negc c < 0) and the
-// min / max they select, for doubles from the bit patterns on the integer pipe,
-// with the IEEE results for every double (false with NaN; -0 == +0); the
-// other types compare natively.
-__device__ __forceinline__ bool lt_z(double x) {   // x < 0
-  return (unsigned long long)fp_bits(x) - 0x8000000000000001ull < 0x7FF0000000000000ull;
-}
-__device__ __forceinline__ bool gt_z(double x) {   // x > 0
-  const long long b = fp_bits(x);
-  return b > 0 && b <= FP_INF;
-}
-__device__ __forceinline__ bool ge_c(double x, double c) {
-  const long long b = fp_bits(x);
-  return b >= fp_bits(c) && b <= FP_INF;
-}
-__device__ __forceinline__ bool gt_c(double x, double c) {
-  const long long b = fp_bits(x);
-  return b > fp_bits(c) && b <= FP_INF;
-}
-__device__ __forceinline__ bool le_c(double x, double c) {
-  const long long b = fp_bits(x);
-  return b <= fp_bits(c) && (b & FP_ABS) <= FP_INF;
-}
-__device__ __forceinline__ bool lt_negc(double x, double c) {
-  const long long b = fp_bits(x), m = b & FP_ABS;
-  return b < 0 && m > (fp_bits(c) & FP_ABS) && m <= FP_INF;
-}
-__device__ __forceinline__ bool lt_c(double x, double c) { return fp_lt_pos(x, c); }
-// min(p, d) as Kokkos::min, (d < p) ? d : p, for a d that is not negative
-// (the limiters' d = max(q, 0) / dt with dt > 0, which the API enforces: +-0,
-// positive, or NaN): d < p exactly when p is positive and not NaN and d's
-// magnitude bits are below p's (a NaN d never is).
-__device__ __forceinline__ bool lt_nn(double d, double p) {   // d < p
-  const long long bp = fp_bits(p);
-  return bp > 0 && bp <= FP_INF && (fp_bits(d) & FP_ABS) < bp;
-}
-__device__ __forceinline__ double min_nn(double p, double d) { return lt_nn(d, p) ? d : p; }
-// a < -d for a d that is not negative (the limiters' d again): a must be
-// negative, not NaN, and of larger magnitude; max(a, -d) as Kokkos::max,
-// (a < -d) ? -d : a, with -d formed by flipping the sign bit
-__device__ __forceinline__ bool lt_nd(double a, double d) {
-  const long long ba = fp_bits(a), ma = ba & FP_ABS;
-  return ba < 0 && ma > (fp_bits(d) & FP_ABS) && ma <= FP_INF;
-}
-__device__ __forceinline__ double max_nd(double a, double d) {
-  return lt_nd(a, d) ? __longlong_as_double(fp_bits(d) ^ (-0x7FFFFFFFFFFFFFFFll - 1)) : a;
-}
-// x + 0.0 without the FP64 pipe: -0 becomes +0, every other value stays
-// (a NaN keeps its payload, where the addition would give the canonical NaN)
-__device__ __forceinline__ double plus_zero(double x) { return fp_bits(x) == -0x7FFFFFFFFFFFFFFFll - 1 ? 0.0 : x; }
-__device__ __forceinline__ double maxz(double x) { return lt_z(x) ? 0.0 : x; }                // max(x, 0)
-__device__ __forceinline__ double maxc(double x, double c) { return fp_lt_pos(x, c) ? c : x; }   // max(x, c)
-__device__ __forceinline__ double minc(double x, double c) { return gt_c(x, c) ? c : x; }       // min(x, c)
 template <class T>
 __device__ __forceinline__ bool lt_z(const T& x) { return x < T(0.0); }
 template <class T>
@@ -183,7 +126,6 @@ template <class T>
 __device__ __forceinline__ bool lt_c(const T& x, const T& c) { return x < c; }
 template <class T>
 __device__ __forceinline__ T maxz(const T& x) { return dmax(x, T(0.0)); }
-__device__ __forceinline__ bool is_zero(double x) { return fp_is_zero(x); }
 template <class T>
 __device__ __forceinline__ bool is_zero(const T& x) { return x == T(0.0); }
 __device__ __forceinline__ double rate_on(double x) { return maxz(x); }

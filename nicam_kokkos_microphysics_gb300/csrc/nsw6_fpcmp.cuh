@@ -84,4 +84,76 @@ NSW6_FP_HD bool fp_pos_normal(double x) {
   return (b >= 0x0010000000000000ll) & (b < FP_INF);
 }
 
+// ---- comparisons with constants and the min / max they select (the cell
+// physics' thresholds, clamps and limiters).  c: a positive normal constant
+// (lt_negc: a negative one).  Each returns what the IEEE comparison (and the
+// Kokkos::min / max select, (b < a) ? b : a and (a < b) ? b : a) returns.
+
+NSW6_FP_HD double fp_from_bits(long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double(b);
+#else
+  double x;
+  std::memcpy(&x, &b, sizeof x);
+  return x;
+#endif
+}
+
+constexpr long long FP_SIGN = -0x7FFFFFFFFFFFFFFFll - 1;   // the sign bit; -0
+
+NSW6_FP_HD bool is_one(double x) { return fp_bits(x) == 0x3FF0000000000000ll; }        // x == 1
+NSW6_FP_HD bool is_nonneg(double x) {                                                    // x >= 0
+  const long long b = fp_bits(x);
+  return (b >= 0 && b <= FP_INF) || b == FP_SIGN;
+}
+NSW6_FP_HD bool is_zero(double x) { return fp_is_zero(x); }                              // x == 0
+NSW6_FP_HD bool lt_z(double x) {                                                         // x < 0
+  return (unsigned long long)fp_bits(x) - 0x8000000000000001ull < 0x7FF0000000000000ull;
+}
+NSW6_FP_HD bool gt_z(double x) {                                                         // x > 0
+  const long long b = fp_bits(x);
+  return b > 0 && b <= FP_INF;
+}
+NSW6_FP_HD bool ge_c(double x, double c) {                                               // x >= c
+  const long long b = fp_bits(x);
+  return b >= fp_bits(c) && b <= FP_INF;
+}
+NSW6_FP_HD bool gt_c(double x, double c) {                                               // x > c
+  const long long b = fp_bits(x);
+  return b > fp_bits(c) && b <= FP_INF;
+}
+NSW6_FP_HD bool le_c(double x, double c) {                                               // x <= c
+  const long long b = fp_bits(x);
+  return b <= fp_bits(c) && (b & FP_ABS) <= FP_INF;
+}
+NSW6_FP_HD bool lt_c(double x, double c) { return fp_lt_pos(x, c); }                     // x < c
+NSW6_FP_HD bool lt_negc(double x, double c) {                                            // x < c, c < 0
+  const long long b = fp_bits(x), m = b & FP_ABS;
+  return b < 0 && m > (fp_bits(c) & FP_ABS) && m <= FP_INF;
+}
+NSW6_FP_HD double maxz(double x) { return lt_z(x) ? 0.0 : x; }                          // max(x, 0)
+NSW6_FP_HD double maxc(double x, double c) { return fp_lt_pos(x, c) ? c : x; }          // max(x, c)
+NSW6_FP_HD double minc(double x, double c) { return gt_c(x, c) ? c : x; }               // min(x, c)
+
+// The limiters' d = max(q, 0) / dt (dt > 0, which the API enforces) is not
+// negative: +-0, positive, +inf or NaN.  d < p exactly when p is positive and
+// not NaN and d's magnitude bits are below p's; a < -d exactly when a is
+// negative, not NaN and of larger magnitude.
+NSW6_FP_HD bool lt_nn(double d, double p) {                                             // d < p
+  const long long bp = fp_bits(p);
+  return bp > 0 && bp <= FP_INF && (fp_bits(d) & FP_ABS) < bp;
+}
+NSW6_FP_HD double min_nn(double p, double d) { return lt_nn(d, p) ? d : p; }            // min(p, d)
+NSW6_FP_HD bool lt_nd(double a, double d) {                                             // a < -d
+  const long long ba = fp_bits(a), ma = ba & FP_ABS;
+  return ba < 0 && ma > (fp_bits(d) & FP_ABS) && ma <= FP_INF;
+}
+NSW6_FP_HD double max_nd(double a, double d) {                                          // max(a, -d)
+  return lt_nd(a, d) ? fp_from_bits(fp_bits(d) ^ FP_SIGN) : a;
+}
+
+// x + 0.0: -0 becomes +0, every other value stays (a NaN keeps its payload,
+// where an FP64 addition gives the canonical NaN)
+NSW6_FP_HD double plus_zero(double x) { return fp_bits(x) == FP_SIGN ? 0.0 : x; }
+
 }  // namespace nsw6

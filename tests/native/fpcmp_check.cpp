@@ -19,6 +19,15 @@ static double from_bits(unsigned long long b) {
   return x;
 }
 
+static unsigned long long bits(double x) {
+  unsigned long long b;
+  std::memcpy(&b, &x, sizeof b);
+  return b;
+}
+
+// the same double (bit for bit), or both NaN
+static bool same(double x, double y) { return bits(x) == bits(y) || (std::isnan(x) && std::isnan(y)); }
+
 static long long check(double a, double b) {
   long long bad = 0;
   bad += fp_lt(a, b) != (a < b);
@@ -28,6 +37,33 @@ static long long check(double a, double b) {
   bad += fp_is_zero(a) != (a == 0.0);
   for (double c : {708.0, 1.0e-12, 0.0078125, 1.0e300})
     bad += fp_abs_lt(a, c) != (std::fabs(a) < c);
+  // the cell physics' comparisons with constants and the selects they make
+  bad += lt_z(a) != (a < 0.0);
+  bad += gt_z(a) != (a > 0.0);
+  bad += is_one(a) != (a == 1.0);
+  bad += is_nonneg(a) != (a >= 0.0);
+  bad += is_zero(a) != (a == 0.0);
+  bad += !same(maxz(a), (a < 0.0) ? 0.0 : a);
+  bad += bits(plus_zero(a)) != bits(a + 0.0) && !std::isnan(a);
+  for (double c : {1.0e-12, 1.0e-10, 1.0e-8, 1.0e-5, 1.0e-4, 2.220446e-16, 1.0, 10.0, 1.0e3, 1.0e6, 1.75e-4}) {
+    bad += ge_c(a, c) != (a >= c);
+    bad += gt_c(a, c) != (a > c);
+    bad += le_c(a, c) != (a <= c);
+    bad += lt_c(a, c) != (a < c);
+    bad += fp_lt_pos(a, c) != (a < c);
+    bad += !same(maxc(a, c), (a < c) ? c : a);
+    bad += !same(minc(a, c), (c < a) ? c : a);
+  }
+  for (double c : {-0.1, -30.99, -1.0e-300})
+    bad += lt_negc(a, c) != (a < c);
+  // a limiter bound d = max(q, 0) / dt is not negative: b with its sign cleared
+  double d = std::fabs(b);
+  for (int s = 0; s < 2; ++s, d = std::isnan(b) ? -std::fabs(b) : (d == 0.0 ? -0.0 : d)) {
+    bad += lt_nn(d, a) != (d < a);
+    bad += !same(min_nn(a, d), (d < a) ? d : a);
+    bad += lt_nd(a, d) != (a < -d);
+    bad += !same(max_nd(a, d), (a < -d) ? -d : a);
+  }
   return bad;
 }
 

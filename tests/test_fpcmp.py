@@ -2,7 +2,10 @@
 return what the IEEE comparisons return for every pair tried: the special
 values pairwise (zeros, subnormals, infinities, NaNs of both signs) and four
 million random and nearby pairs (tests/native/fpcmp_check.cpp, built with the
-host compiler)."""
+host compiler).  That covers the general comparisons, the cell physics'
+comparisons with constants and the min / max selects they make (the same
+double bit for bit, or both NaN), the limiters' forms for a bound that is not
+negative, and the addition of +0."""
 import shutil
 import subprocess
 from pathlib import Path
