@@ -245,13 +245,18 @@ int mp_driver_batched(nsw6_handle* h, int lall,
  * of pointers in the reference order (args[0] = rhog ... args[49] = CBMFX).
  * When `host` is non-zero the pointers are HOST memory: the call copies the
  * inputs to device workspace, runs the step and copies the outputs back
- * (synchronous).  This is the entry point a ctypes/cffi/FFI binding uses. */
+ * (synchronous), pipelined by region so copies overlap the kernels.  When all
+ * 50 arrays are page-locked (cudaHostAlloc / cudaHostRegister) the pipeline is
+ * captured into a CUDA graph on the first call and replayed on later calls
+ * (re-captured when the arrays, lall, dt, parameters or settings change);
+ * pageable arrays take the direct path.  Both give the device entry's result
+ * bit for bit.  This is the entry point a ctypes/cffi/FFI binding uses. */
 int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int host);
 
 /* nsteps consecutive steps of mp_driver_argv (device pointers) on the same
  * arrays, the state evolving in place as in the reference harness's
- * SET_iteration loop (src/main.cpp:261-319).  The step (two memsets and the
- * two kernels) is captured once into a CUDA graph on a stream of the handle
+ * SET_iteration loop (src/main.cpp:261-319).  The step (three memsets and the
+ * three kernels) is captured once into a CUDA graph on a stream of the handle
  * and replayed nsteps times on the handle's stream; the graph is kept and
  * re-captured when the arrays, lall, dt, the parameters or the precision /
  * math / itelim settings change.  The status word is checked once, after the
