@@ -351,6 +351,18 @@ __device__ __forceinline__ double flux_integral(const double* rhof_col, const do
   return (ab >= EPS_BITS && ab <= 0x7ff0000000000000LL) ? f : 0.0;
 }
 
+// Kinetic energies of the mixed step (FP32): horizontal, 0.5 |rhog v|^2 / rhog
+// of a cell, and vertical, 0.5 rhogw^2 / (c2w0 rhog(k) + c2w1 rhog(k-1)) of a
+// half level (mod_precip_transport.cpp:744-766, 991-1011).  The same functions
+// form the energies before and after the transport, so a column the transport
+// leaves unchanged gets a zero KIN2EIN correction, as in the FP64 step.
+__device__ __forceinline__ float kin_h_f(float rvx, float rvy, float rvz, float rhog) {
+  return __fdiv_rn(0.5f * __fmaf_rn(rvx, rvx, __fmaf_rn(rvy, rvy, __fmul_rn(rvz, rvz))), rhog);
+}
+__device__ __forceinline__ float kin_v_f(float rw, float c2w0, float c2w1, float rhog, float rhog_below) {
+  return __fdiv_rn(0.5f * __fmul_rn(rw, rw), __fmaf_rn(c2w0, rhog, __fmul_rn(c2w1, rhog_below)));
+}
+
 // FP32 flux integral of the mixed path (momentum fluxes), same form.
 template <int TG>
 __device__ __forceinline__ float flux_integral_f(const float* rhof_col, const float* dz, int k, int kc, float zdis0,
@@ -665,18 +677,21 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       (reinterpret_cast<uintptr_t>(S.kc + (size_t)K * COL_TG) + 15) & ~(uintptr_t)15);
   const double* tab = tab_smem ? after_kc : P.fmtab;
   long long* zkey = reinterpret_cast<long long*>(after_kc + (tab_smem ? FM_TABLE_DOUBLES : 0));   // [2][K]: cmp_key of gzh, gzshift
-  float* gf = reinterpret_cast<float*>(zkey + 2 * K);   // MIX: dgz, dgzh, rdgz, rdgzh in FP32
+  // MIX: dgz, dgzh, rdgz, rdgzh, afact, bfact, cfact, dfact in FP32
+  float* gf = reinterpret_cast<float*>(zkey + 2 * K);
   auto F = [&](int slot) { return S.f + (size_t)slot * ncell; };
-  // FP32 views of slots (MIX): the flux source and flux of the momentum
-  // passes, and the momentum accumulators
+  // FP32 views of slots (MIX): the flux source and flux of the FP32 passes,
+  // the momentum accumulators and the kinetic energies.  A slot's FP32 view
+  // has two halves, [0, ncell) and [ncell, 2 ncell); the thread of cell c
+  // owns entries c and ncell + c of each.
   auto FF = [&](int slot) { return reinterpret_cast<float*>(S.f + (size_t)slot * ncell); };
 
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) S.grid[c] = P.grid[c];
   for (int c = threadIdx.x; c < 2 * K; c += blockDim.x)
     zkey[c] = cmp_key(P.grid[(c < K ? GF_GZH : GF_GZSHIFT) * K + c % K]);
   if (MIX) {
-    const int rows[4] = {GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH};
-    for (int c = threadIdx.x; c < 4 * K; c += blockDim.x) gf[c] = (float)P.grid[rows[c / K] * K + c % K];
+    const int rows[8] = {GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH, GF_AFACT, GF_BFACT, GF_CFACT, GF_DFACT};
+    for (int c = threadIdx.x; c < 8 * K; c += blockDim.x) gf[c] = (float)P.grid[rows[c / K] * K + c % K];
   }
   for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) S.colacc[c] = 0.0;
   if (tab_smem)
@@ -737,22 +752,46 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
   // c = threadIdx.x + j blockDim.x, j < NJ (NJ covers column_threads()).
   constexpr int NJ = COL_TG == 16 ? 4 : 5;
   double r_rgsh[NJ], r_c2w0[NJ], r_c2w1[NJ];   // gam2h / gsgam2h and C2Wfact at half level k
-  float r_rgshf[NJ];                           // MIX: gam2h / gsgam2h in FP32 (it scales FP32 sources only)
+  // MIX: gam2h / gsgam2h (it scales FP32 sources only) and C2Wfact (they
+  // scale the FP32 vertical kinetic energies only) in FP32
+  float r_rgshf[NJ], r_c2w0f[NJ], r_c2w1f[NJ];
+  const float* aff = gf + 4 * K;   // MIX: afact, bfact, cfact, dfact in FP32
+  const float* bff = gf + 5 * K;
+  const float* cff = gf + 6 * K;
+  const float* dff = gf + 7 * K;
 
   // ---- metric factors, kinetic energy, zeroed accumulators
   //      (mod_precip_transport.cpp:715-770, cnvvar_rhogkin_in mod_debug.cpp:269-330)
+  // MIX keeps these FP32 values in the FP32 halves of slots it uses as FP32:
+  //   S_KINH: kinetic energy (horizontal) | rhog (before, then after the transport)
+  //   S_KINV: kinetic energy (vertical)   | gam2 / gsgam2 of the cell
+  //   S_DKINH: its tendency               | rhoq of the tracer being transported
+  //   S_DKINV: its tendency               | rhogw of the half level (before)
+  //   S_VI, S_VJ: the velocity components | gsgam2h, gsgam2 of the cell
 #pragma unroll
   for (int j = 0; j < NJ; ++j) {
     const int c = threadIdx.x + j * blockDim.x;
     r_rgsh[j] = r_c2w0[j] = r_c2w1[j] = 0.0;
-    r_rgshf[j] = 0.0f;
+    r_rgshf[j] = r_c2w0f[j] = r_c2w1f[j] = 0.0f;
     if (c >= ncell) continue;
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
-    for (int s = S_KINH; s <= S_DQG; ++s) F(s)[c] = 0.0;
+    for (int s = S_KINH; s <= S_DQG; ++s) {
+      if (MIX && (s == S_KINH || s == S_KINV || s == S_DKINH || s == S_DKINV)) {
+        FF(s)[c] = 0.0f;
+        FF(s)[ncell + c] = 0.0f;
+      } else {
+        F(s)[c] = 0.0;
+      }
+    }
     if (OPT) F(S_DQI)[c] = 0.0;
     F(S_RGS)[c] = 0.0;
-    F(S_VI)[c] = 0.0;
-    F(S_VJ)[c] = 0.0;
+    if (MIX) {
+      FF(S_VI)[c] = FF(S_VI)[ncell + c] = 0.0f;
+      FF(S_VJ)[c] = FF(S_VJ)[ncell + c] = 0.0f;
+    } else {
+      F(S_VI)[c] = 0.0;
+      F(S_VJ)[c] = 0.0;
+    }
     if (g >= G) continue;
     const size_t i = off + (size_t)k * G + g;
     const size_t ic = (size_t)l * G + g;
@@ -762,19 +801,38 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     // S_BASE (free until the transport) for that level
     const double gsg = P.gsgam2[i];
     const double rgsg = 1.0 / gsg;
-    F(S_BASE)[c] = rgsg;
+    if (!MIX) F(S_BASE)[c] = rgsg;
     if (interior) F(S_RGS)[c] = div_rn(P.gam2[i], gsg, rgsg);
     const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
-    F(S_VI)[c] = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
-    F(S_VJ)[c] = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
+    const double vi = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
+    const double vj = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
+    if (MIX) {
+      // the velocity components scale FP32 momentum sources only
+      FF(S_VI)[c] = (float)vi;
+      FF(S_VJ)[c] = (float)vj;
+      const float gsgf = (float)gsg, ghf = (float)P.gsgam2h[i], rhogf = (float)P.rhog[i];
+      FF(S_VI)[ncell + c] = ghf;
+      FF(S_VJ)[ncell + c] = gsgf;
+      FF(S_KINH)[ncell + c] = rhogf;
+      if (interior) {
+        FF(S_KINV)[ncell + c] = (float)F(S_RGS)[c];
+        FF(S_KINH)[c] = kin_h_f((float)P.rhogvx[i], (float)P.rhogvy[i], (float)P.rhogvz[i], rhogf);
+      }
+      if (k >= kmin + 1 && k <= kmax) {
+        r_c2w0f[j] = __fmul_rn(__fdiv_rn(aff[k], gsgf), ghf);
+        r_rgshf[j] = __fdiv_rn((float)P.gam2h[i], ghf);
+      }
+      continue;
+    }
+    F(S_VI)[c] = vi;
+    F(S_VJ)[c] = vj;
     if (interior) {
       const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
       F(S_KINH)[c] = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / P.rhog[i];
     }
     if (k >= kmin + 1 && k <= kmax) {
       r_c2w0[j] = div_rn(afact[k], gsg, rgsg) * P.gsgam2h[i];
-      if (MIX) r_rgshf[j] = float(P.gam2h[i]) / float(P.gsgam2h[i]);
-      else r_rgsh[j] = P.gam2h[i] / P.gsgam2h[i];
+      r_rgsh[j] = P.gam2h[i] / P.gsgam2h[i];
     }
   }
   __syncthreads();
@@ -785,6 +843,14 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const int k = c / COL_TG, g = g0 + c % COL_TG;
     if (g >= G || k < kmin + 1 || k > kmax) continue;
     const size_t i = off + (size_t)k * G + g;
+    if (MIX) {
+      const float c2w1 = __fmul_rn(__fdiv_rn(bff[k], FF(S_VJ)[ncell + c - COL_TG]), FF(S_VI)[ncell + c]);
+      const float rw = (float)P.rhogw[i];
+      FF(S_DKINV)[ncell + c] = rw;
+      FF(S_KINV)[c] = kin_v_f(rw, r_c2w0f[j], c2w1, FF(S_KINH)[ncell + c], FF(S_KINH)[ncell + c - COL_TG]);
+      r_c2w1f[j] = c2w1;
+      continue;
+    }
     const double c2w0 = r_c2w0[j];
     const double c2w1 = div_rn(bfact[k], P.gsgam2[i - G], F(S_BASE)[c - COL_TG]) * P.gsgam2h[i];
     const double rw = P.rhogw[i];
@@ -828,6 +894,21 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     // flux source: q, e, phi, kin_h, u, v (mod_precip_transport.cpp:776-808)
     auto source = [&](int f, int c) {
       const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+      if (MIX && f >= 3) {
+        // FP32 sources of the kinetic-energy and momentum fluxes; rhoq in FP32
+        // is formed once, with the first of them
+        float r = 0.0f;
+        if (g < G) {
+          if (f == 3) {
+            FF(S_DKINH)[ncell + c] = (float)F(S_BASE)[c];
+            r = __fmul_rn(__fmul_rn((float)q_n[(size_t)k * G + g], FF(S_KINV)[ncell + c]), FF(S_KINH)[c]);
+          } else {
+            r = __fmul_rn(FF(S_DKINH)[ncell + c], f == 4 ? FF(S_VI)[c] : FF(S_VJ)[c]);
+          }
+        }
+        FF(S_RHOF)[c] = r;
+        return;
+      }
       double r = 0.0;
       if (g < G) {
         const size_t i = off + (size_t)k * G + g;
@@ -841,8 +922,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           default: r = b * F(S_VJ)[c]; break;
         }
       }
-      if (MIX && f >= 3) FF(S_RHOF)[c] = (float)r;
-      else F(S_RHOF)[c] = r;
+      F(S_RHOF)[c] = r;
     };
     // flux divergence and surface fluxes (mod_precip_transport.cpp:782-842,
     // 900-954); the quotients by dt are the correctly rounded ones, formed
@@ -902,9 +982,8 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       }
     } else {
       // the mass and energy fluxes (mass, internal and potential energy) as
-      // in the FP64 step; the kinetic-energy and momentum ones as FP32
-      // integrals, the kinetic-energy tendency summed in FP64, the momentum
-      // ones in FP32
+      // in the FP64 step; the kinetic-energy and momentum ones, their sources
+      // and tendencies in FP32
       const float* rf = FF(S_RHOF);
       float* ff = FF(S_F);
       const float* dgzf = gf;
@@ -944,7 +1023,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           if (g < G && k >= kmin && k <= kmax) {
             const float d = (ff[c + COL_TG] - ff[c]) * rdgzf[k];
             switch (f) {
-              case 3: F(S_DKINH)[c] = F(S_DKINH)[c] - (double)d; break;
+              case 3: FF(S_DKINH)[c] = FF(S_DKINH)[c] - d; break;
               case 4: FF(S_DRHOGU)[c] = FF(S_DRHOGU)[c] - d; break;
               default: FF(S_DRHOGV)[c] = FF(S_DRHOGV)[c] - d; break;
             }
@@ -973,7 +1052,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
         float qh = 0.0f;
         if (hv) qh = 0.5f * (float(q_n[(size_t)k * G + g]) + float(q_n[(size_t)(k - 1) * G + g])) * r_rgshf[j];
         FF(S_BASE)[c] = qh;
-        FF(S_RHOF)[c] = qh * float(F(S_KINV)[c]);
+        FF(S_RHOF)[c] = __fmul_rn(qh, FF(S_KINV)[c]);
         // the half levels' FP32 departure distance, converted once (upper half)
         if (hv) FF(S_RHOF)[ncell + c] = (float)zdis0h[(size_t)k * G + g];
       } else {
@@ -986,8 +1065,8 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     __syncthreads();
     for (int w = 0; w < 2; ++w) {
       if (MIX && w == 0) {
-        // vertical kinetic energy in FP32, summed into the FP64 tendency; the
-        // pass also forms the FP32 source of momentum w
+        // vertical kinetic energy in FP32 and its FP32 tendency; the pass also
+        // forms the FP32 source of momentum w
         const float* rf = FF(S_RHOF);
         float* ff = FF(S_F);
         const float* dgzhf = gf + K;
@@ -1004,8 +1083,8 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
           const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
           float r = 0.0f;
           if (g < G && k >= kmin + 1 && k <= kmax) {
-            F(S_DKINV)[c] = F(S_DKINV)[c] - (double)((ff[c] - ff[c - COL_TG]) * rdgzhf[k]);
-            r = FF(S_BASE)[c] * float(P.rhogw[off + (size_t)k * G + g]);
+            FF(S_DKINV)[c] = FF(S_DKINV)[c] - (ff[c] - ff[c - COL_TG]) * rdgzhf[k];
+            r = FF(S_BASE)[c] * FF(S_DKINV)[ncell + c];   // rhogw before the transport, in FP32
           }
           FF(S_RHOF)[c] = r;
         }
@@ -1071,8 +1150,13 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const size_t iq = offq + (size_t)k * G + g;
     const double dqr = F(S_DQR)[c], dqs = F(S_DQS)[c], dqg = F(S_DQG)[c];
     double rhoge = P.rhoge[i] + F(S_DRHOE)[c] + F(S_DRHOPHI)[c];
-    F(S_KINH)[c] = F(S_KINH)[c] + F(S_DKINH)[c];
-    F(S_KINV)[c] = F(S_KINV)[c] + F(S_DKINV)[c];
+    if (MIX) {
+      FF(S_KINH)[c] = FF(S_KINH)[c] + FF(S_DKINH)[c];
+      FF(S_KINV)[c] = FF(S_KINV)[c] + FF(S_DKINV)[c];
+    } else {
+      F(S_KINH)[c] = F(S_KINH)[c] + F(S_DKINH)[c];
+      F(S_KINV)[c] = F(S_KINV)[c] + F(S_DKINV)[c];
+    }
     const double du = MIX ? (double)FF(S_DRHOGU)[c] : F(S_DRHOGU)[c];
     const double dv = MIX ? (double)FF(S_DRHOGV)[c] : F(S_DRHOGV)[c];
     P.rhogvx[i] = P.rhogvx[i] + du * P.ix[ic] + dv * P.jx[ic];
@@ -1106,6 +1190,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     P.rhog[i] = rhog;
     P.rhoge[i] = rhoge;
     F(S_RHOF)[c] = rhog;
+    if (MIX) FF(S_KINH)[ncell + c] = (float)rhog;   // rhog after the transport, for the FP32 kinetic energies
   }
   __syncthreads();
 
@@ -1120,7 +1205,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       const size_t i = off + (size_t)k * G + g;
       const double rhog = F(S_RHOF)[c];
       if (k <= kmax) {
-        const double kin_h0 = F(S_KINH)[c] / rhog;
+        const double kin_h0 = (MIX ? (double)FF(S_KINH)[c] : F(S_KINH)[c]) / rhog;
         double vx_t = P.rhogvx[i] / rhog, vy_t = P.rhogvy[i] / rhog, vz_t = P.rhogvz[i] / rhog;
         const double kin_h = 0.5 * (vx_t * vx_t + vy_t * vy_t + vz_t * vz_t);
         if (kin_h > 1.0E-20) {
@@ -1136,7 +1221,7 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       const double c2w0 = afact[k] / P.gsgam2[i] * P.gsgam2h[i];
       const double c2w1 = bfact[k] / P.gsgam2[i - G] * P.gsgam2h[i];
       const double rhogh = c2w0 * rhog + c2w1 * F(S_RHOF)[c - COL_TG];
-      const double kin_v0 = F(S_KINV)[c] / rhogh;
+      const double kin_v0 = (MIX ? (double)FF(S_KINV)[c] : F(S_KINV)[c]) / rhogh;
       double w_t = P.rhogw[i] / rhogh;
       const double kin_v = 0.5 * (w_t * w_t);
       if (kin_v > 1.0E-20) w_t = w_t * sqrt(fabs(kin_v0 / kin_v));
@@ -1154,12 +1239,31 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const int c = threadIdx.x + j * blockDim.x;
     if (c >= ncell || kin2kin) continue;
     const int k = c / COL_TG, gx = c % COL_TG, g = g0 + gx;
+    if (MIX) {
+      // FP32: the change of the vertical kinetic energy of half level k by
+      // the transport, (KINV + its tendency) - the energy of the updated
+      // state, in the FP32 half of S_DRHOPHI (zero where there is none), and
+      // W2Cfact of the interior cells in the two halves of S_DRHOE
+      float dkv = 0.0f;
+      if (g < G && k >= kmin + 1 && k <= kmax) {
+        const size_t i = off + (size_t)k * G + g;
+        dkv = FF(S_KINV)[c] - kin_v_f((float)P.rhogw[i], r_c2w0f[j], r_c2w1f[j], FF(S_KINH)[ncell + c],
+                                      FF(S_KINH)[ncell + c - COL_TG]);
+      }
+      FF(S_DRHOPHI)[c] = dkv;
+      if (g < G && k >= kmin && k <= kmax) {
+        const float gsgf = FF(S_VJ)[ncell + c], ghu = FF(S_VI)[ncell + c + COL_TG];
+        FF(S_DRHOE)[c] = __fdiv_rn(__fmul_rn(cff[k], gsgf), ghu);
+        FF(S_DRHOE)[ncell + c] = __fdiv_rn(__fmul_rn(dff[k], gsgf), ghu);
+      }
+      continue;
+    }
     F(S_DRHOE)[c] = 0.0;
     F(S_DRHOPHI)[c] = 0.0;
     if (g >= G) continue;
     const size_t i = off + (size_t)k * G + g;
     const bool hk = (k >= kmin + 1 && k <= kmax);
-    const double rw = hk ? (MIX ? P.rhogw[i] : F(S_DRHOGW)[c]) : 0.0;
+    const double rw = hk ? F(S_DRHOGW)[c] : 0.0;
     if (k >= kmin && k <= kmax) {
       const double gh = P.gsgam2h[i + G], rgh = 1.0 / gh;
       const double w2c0 = div_rn(cfact[k] * P.gsgam2[i], gh, rgh);
@@ -1198,7 +1302,17 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     // divisions, at a third of the cost.
     const double rrhog = 1.0 / rhog;
     double rhoge = P.rhoge[i];
-    if (interior && !kin2kin) {
+    if (MIX && interior && !kin2kin) {
+      // FP32 kinetic energies: the horizontal energy after the transport
+      // against before (with its tendency), the vertical energies' changes
+      // weighted by W2Cfact; their sum enters the FP64 internal energy
+      const float kh = kin_h_f((float)P.rhogvx[i], (float)P.rhogvy[i], (float)P.rhogvz[i], FF(S_KINH)[ncell + c]);
+      const float dke = (FF(S_KINH)[c] - kh) +
+                        __fmaf_rn(FF(S_DRHOE)[c], FF(S_DRHOPHI)[c + COL_TG],
+                                  __fmul_rn(FF(S_DRHOE)[ncell + c], FF(S_DRHOPHI)[c]));
+      rhoge = rhoge + (double)dke;
+      P.rhoge[i] = rhoge;   // a saturated cell's adjustment starts from here (final_cell overwrites the rest)
+    } else if (interior && !kin2kin) {
       const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
       const double tmp_h = div_rn(0.5 * (rvx * rvx + rvy * rvy + rvz * rvz), rhog, rrhog);
       double w2c0, w2c1;
@@ -1313,7 +1427,7 @@ size_t column_smem_bytes(int K, bool opt) {
   const size_t nrow = opt ? 8 : 6;
   const size_t ntab = (!opt || K <= COL_FMTAB_SMEM_KMAX) ? FM_TABLE_DOUBLES : 0;
   return sizeof(double) * (nslot * K * TG + GF_COUNT * K + 6 * TG + ntab) +
-         sizeof(int) * 2 * nrow * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 4 * K;
+         sizeof(int) * 2 * nrow * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 8 * K;
 }
 
 int column_threads(int K) {
