@@ -361,27 +361,19 @@ def time_device_steps(drv, lall: int, dev: dict, dt: float, steps: int, dist=Non
     return e0.elapsed_time(e1) / steps, t_cell / max(n, 1), t_col / max(n, 1)
 
 
-E2E_READ = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "vx", "vy", "vz", "tem", "q",
-            "gsgam2", "gsgam2h", "gam2", "gam2h", "ix", "iy", "iz", "jx", "jy", "jz", "z"]
-E2E_WRITE = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "rho", "tem", "pre", "q", "qd",
-             "precip", "ISO1_precip", "ISO2_precip", "precip_rhoe", "precip_lh_heat", "precip_rhophi",
-             "precip_rhokin", "re_liquid", "re_solid", "re_cld", "rctop", "rwtop", "tctop", "GDCLW", "GDCFRC",
-             "GPREC"]
-
-
 def time_end_to_end(drv, spec: StateSpec, st: dict, steps: int, world: int, dist=None) -> dict:
     """The same step through the public host-memory entry point
     (mp_driver_argv with host = 1, via MPDriver.run on pinned numpy arrays):
-    every step copies the arguments it reads to the device and those it
-    writes back inside the call."""
+    every step copies what it reads of the arguments to the device and the
+    arguments it writes back inside the call; the byte counts are the
+    library's own (nsw6_host_copy_bytes)."""
     import torch
-    kinds = {n: k for n, k, _ in MP_DRIVER_ARGS}
     host = {}
     for n in ARG_NAMES:
         t = torch.empty(st[n].shape, dtype=torch.float64, pin_memory=True)
         t.numpy()[...] = st[n]
         host[n] = t.numpy()
-    nbytes = lambda n: int(np.prod(batched_shape(kinds[n], spec.lall, spec.kall, spec.gall))) * 8  # noqa: E731
+    h2d, d2h = drv.host_copy_bytes(spec.lall)
     drv.run(host, dt=spec.dt)  # warm-up (allocates the staging buffers)
     if dist:
         dist.barrier()
@@ -390,8 +382,7 @@ def time_end_to_end(drv, spec: StateSpec, st: dict, steps: int, world: int, dist
         drv.run(host, dt=spec.dt)
     dt_e2e = max_over_ranks((time.perf_counter() - t0) / steps, dist)
     return {"value": whole_job_rate(spec.cells, world, dt_e2e), "unit": UNIT,
-            "h2d_bytes_per_step": sum(nbytes(n) for n in E2E_READ),
-            "d2h_bytes_per_step": sum(nbytes(n) for n in E2E_WRITE), "ms_per_step": dt_e2e * 1e3}
+            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "ms_per_step": dt_e2e * 1e3}
 
 
 def roofline_of(kernel_ms: dict, spec: StateSpec, precision: str, rates, aw) -> dict:

@@ -253,6 +253,14 @@ int mp_driver_batched(nsw6_handle* h, int lall,
  * bit for bit.  This is the entry point a ctypes/cffi/FFI binding uses. */
 int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int host);
 
+/* Bytes one mp_driver_argv(host = 1) call on lall regions copies to the
+ * device and back with the handle's current settings.  Every argument the
+ * step reads is copied in whole except q, of which only QV is read (QC..QG
+ * are formed from rhogq), and rhoge, of which only the two halo levels are
+ * read (the interior levels' are formed from tem, rhog and q); every argument
+ * it writes is copied back whole.  No counterpart in the reference. */
+int nsw6_host_copy_bytes(const nsw6_handle* h, int lall, unsigned long long* h2d, unsigned long long* d2h);
+
 /* nsteps consecutive steps of mp_driver_argv (device pointers) on the same
  * arrays, the state evolving in place as in the reference harness's
  * SET_iteration loop (src/main.cpp:261-319).  The step (three memsets and the

@@ -196,6 +196,13 @@ class MPDriver:
         _check(self._lib.nsw6_read_timing(self._h, t, 2, ctypes.byref(n)), self._lib)
         return t[0], t[1], n.value
 
+    def host_copy_bytes(self, lall: int | None = None) -> tuple[int, int]:
+        """(bytes in, bytes out) that one host-memory call on lall (default lall_max) regions copies."""
+        h2d, d2h = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+        n = self.lall_max if lall is None else lall
+        _check(self._lib.nsw6_host_copy_bytes(self._h, n, ctypes.byref(h2d), ctypes.byref(d2h)), self._lib)
+        return h2d.value, d2h.value
+
     def last_error(self) -> tuple[int, tuple[int, int, int, int]]:
         k, g, l, it = (ctypes.c_int() for _ in range(4))
         rc = self._lib.nsw6_last_error(self._h, ctypes.byref(k), ctypes.byref(g), ctypes.byref(l), ctypes.byref(it))

@@ -101,6 +101,8 @@ def load() -> ctypes.CDLL:
     lib.nsw6_strerror.argtypes = [c_int]
     lib.nsw6_strerror.restype = ctypes.c_char_p
     lib.mp_driver_argv.argtypes = [vp, c_int, ctypes.POINTER(vp), c_double, c_double, c_int]
+    lib.nsw6_host_copy_bytes.argtypes = [vp, c_int, ctypes.POINTER(ctypes.c_ulonglong),
+                                         ctypes.POINTER(ctypes.c_ulonglong)]
     lib.mp_driver.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.mp_driver_batched.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4
     lib.mp_driver_mixed.argtypes = [vp, c_int] + [vp] * 46 + [c_double, c_double] + [vp] * 4

@@ -4,8 +4,9 @@
 // 335-613) and the set-up routines the reference runs through globals:
 // GRD_Setup (mod_debug.cpp:92-187), SATURATION_Setup (mod_satadjust.cpp:24-47)
 // and mp_nsw6_init (mod_mp_nsw6.cpp:276-434).  All device memory a step needs
-// is allocated in nsw6_create; a step enqueues two memsets and two kernels.
+// is allocated in nsw6_create; a step enqueues three memsets and three kernels.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -677,6 +678,20 @@ int run_serial(nsw6_handle* h, int lall, double* const* a, double dt) {
 // Enqueues the host-memory step as a pipeline of chunks of regions: copies in
 // on s_in, the step on cs, copies out on s_out, from an event recorded on cs;
 // cs ends waiting for both copy streams.  rc: a fill_problem error.
+// Doubles of argument i the host entry copies in for nl regions: every
+// argument the step reads, whole, except two it reads in part.  Of q only QV
+// is read (the cell kernel's input; QC..QG of every level are formed from
+// rhogq), of rhoge only the two halo levels (the cell kernel forms the
+// interior levels' from tem, rhog and q before anything reads them).  The
+// device staging keeps whatever the skipped parts held; nothing reads them.
+size_t host_in_doubles(const nsw6_handle* h, int i, int nl) {
+  const size_t K = h->kall, G = h->gall;
+  if (!arg_is_read(i) && !(i == A_unccn && h->opts.aerosol_indirect)) return 0;
+  if (i == A_q) return K * G * (size_t)nl;
+  if (i == A_rhoge) return 2 * G * (size_t)nl;
+  return arg_region_elems(i, (int)K, (int)G) * (size_t)nl;
+}
+
 cudaError_t enqueue_host(nsw6_handle* h, int lall, double* const* args, double* const* dev, double dt, cudaStream_t cs,
                          int& rc) {
   const int K = h->kall, G = h->gall;
@@ -711,13 +726,33 @@ cudaError_t enqueue_host(nsw6_handle* h, int lall, double* const* args, double* 
     }
     // inputs in two groups: first what the cell kernel reads or rewrites in
     // place, then what only the column kernel reads, which arrives while the
-    // cell kernel runs
+    // cell kernel runs; of q and rhoge only the parts the step reads
+    // (host_in_doubles)
     for (int group = 0; group < 2 && err == cudaSuccess; ++group) {
       for (int i = 0; i < A_COUNT && err == cudaSuccess; ++i) {
-        if (!arg_is_read(i) && !(i == A_unccn && h->opts.aerosol_indirect)) continue;
+        if (host_in_doubles(h, i, 1) == 0) continue;
         if ((cell_phase_arg(i) ? 0 : 1) != group) continue;
-        err = cudaMemcpyAsync(cdev[i], chost[i], sizeof(double) * arg_region_elems(i, K, G) * nl,
-                              cudaMemcpyHostToDevice, h->s_in);
+        const size_t e = arg_region_elems(i, K, G);
+        // nl blocks of n doubles, one per region, e doubles apart: one 2D copy
+        // (its pitch is limited to 2^31 - 1 bytes), else one copy per region
+        auto copy_blocks = [&](size_t o, size_t n) {
+          if (sizeof(double) * e <= (size_t)INT_MAX)
+            return cudaMemcpy2DAsync(cdev[i] + o, sizeof(double) * e, chost[i] + o, sizeof(double) * e,
+                                     sizeof(double) * n, nl, cudaMemcpyHostToDevice, h->s_in);
+          cudaError_t ce = cudaSuccess;
+          for (int r = 0; r < nl && ce == cudaSuccess; ++r)
+            ce = cudaMemcpyAsync(cdev[i] + o + e * r, chost[i] + o + e * r, sizeof(double) * n,
+                                 cudaMemcpyHostToDevice, h->s_in);
+          return ce;
+        };
+        if (i == A_q) {
+          err = copy_blocks(0, (size_t)K * G);   // q[QV] of each region
+        } else if (i == A_rhoge) {
+          err = copy_blocks(0, G);               // levels 0 and K-1 of each region
+          if (err == cudaSuccess) err = copy_blocks((size_t)(K - 1) * G, G);
+        } else {
+          err = cudaMemcpyAsync(cdev[i], chost[i], sizeof(double) * e * nl, cudaMemcpyHostToDevice, h->s_in);
+        }
       }
       if (err == cudaSuccess) err = cudaEventRecord(group == 0 ? h->ev_in[nchunk] : h->ev_in2[nchunk], h->s_in);
     }
@@ -1168,6 +1203,18 @@ int mp_driver_argv(nsw6_handle* h, int lall, double* const* args, double dt, dou
   if (!h || !args || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
   if (!host) return run(h, lall, args, dt);
   return run_host(h, lall, args, dt);
+}
+
+int nsw6_host_copy_bytes(const nsw6_handle* h, int lall, unsigned long long* h2d, unsigned long long* d2h) {
+  if (!h || lall < 1 || lall > h->lall_max) return NSW6_ERR_BAD_ARG;
+  unsigned long long in = 0, out = 0;
+  for (int i = 0; i < A_COUNT; ++i) {
+    in += sizeof(double) * host_in_doubles(h, i, lall);
+    if (arg_is_written(i)) out += sizeof(double) * arg_region_elems(i, h->kall, h->gall) * (size_t)lall;
+  }
+  if (h2d) *h2d = in;
+  if (d2h) *d2h = out;
+  return NSW6_OK;
 }
 
 int mp_driver_steps(nsw6_handle* h, int lall, double* const* args, double dt, double ct, int nsteps) {

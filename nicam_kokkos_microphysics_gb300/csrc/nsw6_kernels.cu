@@ -1,6 +1,7 @@
 // GB300 (sm_103a) kernels of one NSW6 microphysics step, FP64.
 //
-// Two kernels per step (plus two memsets of the extrema buffers):
+// Three kernels per step (plus three memsets: the extrema buffers and the
+// saturated-cell list's count):
 //
 //  nsw6_cell_kernel    one CTA = CELL_TG columns x all interior levels of one
 //                      region.  Per cell: negative filter, saturation values,
@@ -15,8 +16,12 @@
 //                      shared memory.  Departure cells, the 24 flux integrals of
 //                      vadv1d_getflux_new, the transport tendencies, surface
 //                      precipitation, the KIN2EIN energy correction, the final
-//                      thermodynamic state, the saturation adjustment (Newton
-//                      on T) and the closing negative filter.
+//                      thermodynamic state and the closing negative filter; the
+//                      cells the saturation adjustment finds saturated are
+//                      listed instead.
+//
+//  nsw6_satadj_kernel  one thread per listed cell: its Newton iteration on T
+//                      (the saturation adjustment) and its final state.
 //
 // The only coupling between columns, the per-level max/min of the departure
 // distance over a region (mod_vadv1d.cpp:316-353), is what separates the two

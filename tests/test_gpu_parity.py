@@ -182,6 +182,49 @@ def test_gpu_host_entry_equals_device_entry(lall, lall_max, precision, options):
     drv.close()
 
 
+@pytest.mark.parametrize("precision,options", [("fp64", None), ("mixed", None),
+                                               ("fp64", {"qi_sediment": 1, "kin2kin": 1, "roh2014": 0})])
+def test_gpu_unread_input_parts(precision, options):
+    """The step reads q only at QV (QC..QG are formed from rhogq) and rhoge
+    only at the two halo levels (the interior levels' are formed from tem,
+    rhog and q), so the host entry copies only those parts
+    (nsw6_host_copy_bytes).  NaN in the unread parts changes no output of
+    either entry, bit for bit."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import mp_init
+    spec = StateSpec(gall=300, kall=42, lall=3, seed=11, variant="convective")
+    st = make_state(spec, out_fill=np.nan)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"], lall_max=spec.lall, options=options)
+    drv.set_precision(precision)
+    K, G, L = spec.kall, spec.gall, spec.lall
+    full = {n: (st[n].size * 8) for n in ARG_NAMES}
+    read = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhogq", "vx", "vy", "vz", "tem", "gsgam2", "gsgam2h",
+            "gam2", "gam2h", "ix", "iy", "iz", "jx", "jy", "jz", "z"]
+    written = ["rhog", "rhogvx", "rhogvy", "rhogvz", "rhogw", "rhoge", "rhogq", "rho", "tem", "pre", "q", "qd",
+               "precip", "ISO1_precip", "ISO2_precip", "precip_rhoe", "precip_lh_heat", "precip_rhophi",
+               "precip_rhokin", "re_liquid", "re_solid", "re_cld", "rctop", "rwtop", "tctop", "GDCLW", "GDCFRC",
+               "GPREC"]
+    want_h2d = sum(full[n] for n in read) + 8 * L * K * G + 8 * L * 2 * G   # + q[QV] + rhoge's halo levels
+    assert drv.host_copy_bytes(L) == (want_h2d, sum(full[n] for n in written))
+
+    clean = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    drv.run(clean, dt=spec.dt)
+    dirty = {n: st[n].copy() for n in ARG_NAMES}
+    assert dirty["q"].shape == (L, 6, K, G) and dirty["rhoge"].shape == (L, K, G)
+    dirty["q"][:, 1:] = np.nan
+    dirty["rhoge"][:, 1:K - 1] = np.nan
+    dev = {n: torch.from_numpy(dirty[n].copy()).cuda() for n in ARG_NAMES}
+    drv.run(dev, dt=spec.dt)
+    host = {n: dirty[n].copy() for n in ARG_NAMES}
+    drv.run(host, dt=spec.dt)
+    torch.cuda.synchronize()
+    for n in OUTPUT_NAMES:
+        want = clean[n].cpu().numpy().view(np.int64)
+        assert np.array_equal(dev[n].cpu().numpy().view(np.int64), want), ("device", n)
+        assert np.array_equal(host[n].view(np.int64), want), ("host", n)
+    drv.close()
+
+
 def test_gpu_all_saturated_state_matches_oracle():
     """Every interior cell supersaturated (vapour at 1.5 qsat): after the cell
     physics about 40 % of the interior cells are still saturated (the oracle
