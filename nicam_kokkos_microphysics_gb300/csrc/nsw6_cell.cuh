@@ -200,23 +200,39 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   diffq -= rq[I_QV];
   const D rhog = in.rhog * (1.0 - diffq);
   const D rrhog = 1.0 / rhog;
-  const D dens = rhog / in.gsgam2;
   D qn[6];
   qn[0] = in.q0;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) qn[n] = kMixed ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
-  D qd = D(1.0);
-#pragma unroll
-  for (int n = 1; n <= 5; ++n) qd = qd - qn[n];
-  D cv = qd * CVDRY;
-#pragma unroll
-  for (int n = 1; n <= 5; ++n) cv = cv + qn[n] * CVDRY;
   const D temp = in.tem;
-  D rhoge = temp * rhog * cv;
-  const R pre = R(dens * (qd * RDRY + qn[0] * RVAP) * temp);
+  D rhoge;
+  R pre, densR;
+  if constexpr (kMixed) {
+    // The internal energy rhog cv T in FP64 with cv = CVdry: under the
+    // "SIMPLE" internal energy every CVW is CVdry, so the reference's
+    // qd CVdry + sum q CVW is CVdry up to its roundings.  Density and
+    // pressure scale FP32 rates only: FP32.
+    rhoge = temp * rhog * CVDRY;
+    densR = R(rhog) / R(in.gsgam2);
+    R qdR = R(1.0);
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qdR = qdR - R(qn[n]);
+    pre = densR * (qdR * R(RDRY) + R(qn[0]) * R(RVAP)) * R(temp);
+  } else {
+    const D dens = rhog / in.gsgam2;
+    D qd = D(1.0);
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qd = qd - qn[n];
+    D cv = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cv = cv + qn[n] * CVDRY;
+    rhoge = temp * rhog * cv;
+    pre = R(dens * (qd * RDRY + qn[0] * RVAP) * temp);
+    densR = R(dens);
+  }
 
   // ---- psat / qsat (CPovR = 0 under EIN_TYPE "SIMPLE": the power term is 1)
-  const R tempR = R(temp), densR = R(dens);
+  const R tempR = R(temp);
   const R rtem = R(1.0) / maxc(tempR, R(TEM_MIN));
   const R psatl = R(PSAT0) * mth.exp(C.LovR_liq * (C.RTEM00 - rtem));
   const R psati = R(PSAT0) * mth.exp(C.LovR_ice * (C.RTEM00 - rtem));
@@ -618,26 +634,30 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   qg_t = max_nd(qg_t, dqg_dt);
   const R qv_t = -(qc_t + qr_t + qi_t + qs_t + qg_t);
   D drq[6];
-  drq[0] = rhog * D(qv_t) * dt;
-  drq[1] = rhog * D(qc_t) * dt;
-  drq[2] = rhog * D(qr_t) * dt;
-  drq[3] = rhog * D(qi_t) * dt;
-  drq[4] = rhog * D(qs_t) * dt;
-  drq[5] = rhog * D(qg_t) * dt;
-  if (kMixed) {
-    // A species whose loss reached its whole content leaves exactly nothing
-    // (the FP64 path leaves a rounding residue of the same size as the
-    // reference's; FP32 rates would leave one 10^9 times larger), and the
-    // vapour takes the balance so that total water stays exact.
+  if constexpr (kMixed) {
+    // The tracer changes rhog q_t dt of the FP32 rates, formed in FP32 and
+    // added to the FP64 budgets.  A species whose loss reached its whole
+    // content leaves exactly nothing (the FP64 path leaves a rounding residue
+    // of the same size as the reference's; FP32 rates would leave one 10^9
+    // times larger), and the vapour takes the balance so that total water
+    // stays exact.
+    const R rgdt = R(rhog * dt);
     const R qt[6] = {qv_t, qc_t, qr_t, qi_t, qs_t, qg_t};
     const R lim[6] = {dqv_dt, dqc_dt, dqr_dt, dqi_dt, dqs_dt, dqg_dt};
     D sum = D(0.0);
 #pragma unroll
     for (int n = 1; n <= 5; ++n) {
-      if (qt[n] <= -lim[n] && lim[n] > Z) drq[n] = -rq[n];
+      drq[n] = (qt[n] <= -lim[n] && lim[n] > Z) ? -rq[n] : D(qt[n] * rgdt);
       sum += drq[n];
     }
     drq[0] = -sum;
+  } else {
+    drq[0] = rhog * D(qv_t) * dt;
+    drq[1] = rhog * D(qc_t) * dt;
+    drq[2] = rhog * D(qr_t) * dt;
+    drq[3] = rhog * D(qi_t) * dt;
+    drq[4] = rhog * D(qs_t) * dt;
+    drq[5] = rhog * D(qg_t) * dt;
   }
   o.Vtr = D(Vtr);
   o.Vts = D(Vts);
@@ -674,15 +694,22 @@ __device__ __forceinline__ void nsw6_cell(const ConstsT<R>& C, const M& mth, dou
   for (int n = 0; n < 6; ++n) rq[n] += drq[n];
   rhoge = rhoge - LHV0 * drq[I_QV] + LHF0 * drq[I_QI] + LHF0 * drq[I_QS] + LHF0 * drq[I_QG];
   o.q[0] = qn[0];
+  if constexpr (kMixed) {
+    // q from the shared reciprocal, T = rhoge / (rhog CVdry) (cv = CVdry as above)
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) o.q[n] = div_rn(rq[n], rhog, rrhog);
-  D qd2 = D(1.0);
+    for (int n = 1; n <= 5; ++n) o.q[n] = rq[n] * rrhog;
+    o.tem = rhoge * rrhog * (1.0 / CVDRY);
+  } else {
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) qd2 = qd2 - o.q[n];
-  D cva = qd2 * CVDRY;
+    for (int n = 1; n <= 5; ++n) o.q[n] = div_rn(rq[n], rhog, rrhog);
+    D qd2 = D(1.0);
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) cva = cva + o.q[n] * CVDRY;
-  o.tem = rhoge / (rhog * cva);
+    for (int n = 1; n <= 5; ++n) qd2 = qd2 - o.q[n];
+    D cva = qd2 * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cva = cva + o.q[n] * CVDRY;
+    o.tem = rhoge / (rhog * cva);
+  }
   o.rhog = rhog;
   o.rhoge = rhoge;
 #pragma unroll

@@ -144,26 +144,42 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const D omd = 1.0 - d2;
   const D rhog = in.rhog * omd;
   const D rrhog = NSW6_CK(D, 0, 1.0 / rhog);
-  const D dens = NSW6_CK(D, 1, rhog / in.gsgam2);
   D qn[6];
   qn[0] = in.q0;
 #pragma unroll
   for (int n = 1; n <= 5; ++n) qn[n] = kMixed ? rq[n] * rrhog : div_rn(rq[n], rhog, rrhog);
-  D qd = 1.0;
-#pragma unroll
-  for (int n = 1; n <= 5; ++n) qd = qd - qn[n];
-  D cv = qd * CVDRY;
-#pragma unroll
-  for (int n = 1; n <= 5; ++n) cv = cv + qn[n] * CVDRY;
   const D temp = in.tem;
   const D trh = temp * rhog;
-  const D rhoge0 = trh * cv;
-  const D pq = qd * RDRY + qn[0] * RVAP;
-  const D dp = dens * pq;
-  const R pre = R(dp * temp);
+  D dens, rhoge0, cv = CVDRY, pq = 0.0, dp = 0.0;
+  R pre, densR, pqR = Z, dpR = Z;
+  if constexpr (kMixed) {
+    // as nsw6_cell: cv = CVdry (every CVW is CVdry), density and pressure in FP32
+    rhoge0 = trh * CVDRY;
+    densR = NSW6_CK(R, 1, R(rhog) / R(in.gsgam2));
+    dens = D(densR);
+    R qdR = ONE;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qdR = qdR - R(qn[n]);
+    pqR = qdR * R(RDRY) + R(qn[0]) * R(RVAP);
+    dpR = densR * pqR;
+    pre = dpR * R(temp);
+  } else {
+    dens = NSW6_CK(D, 1, rhog / in.gsgam2);
+    D qd = 1.0;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) qd = qd - qn[n];
+    cv = qd * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cv = cv + qn[n] * CVDRY;
+    rhoge0 = trh * cv;
+    pq = qd * RDRY + qn[0] * RVAP;
+    dp = dens * pq;
+    pre = R(dp * temp);
+    densR = R(dens);
+  }
 
   // ---- psat / qsat (rate precision from here to the tendencies)
-  const R tempR = R(temp), densR = R(dens);
+  const R tempR = R(temp);
   const R tmx = maxc(tempR, R(TEM_MIN));
   const R rtem = NSW6_CK(R, 2, ONE / tmx);
   const R al = C.LovR_liq * (C.RTEM00 - rtem);
@@ -586,18 +602,21 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   // and the vapour takes the balance (nsw6_cell)
   D drq[6];
   bool exh[6] = {false, false, false, false, false, false};
-#pragma unroll
-  for (int n = 0; n < 6; ++n) drq[n] = rhog * D(qt[n]) * dt;
   if constexpr (kMixed) {
+    // formed in FP32 as in nsw6_cell: qt (rhog dt)
+    const R rgdt = R(rhog * dt);
     const R lim[6] = {dqv_dt, dqc_dt, dqr_dt, dqi_dt, dqs_dt, dqg_dt};
     D sum = 0.0;
 #pragma unroll
     for (int n = 1; n <= 5; ++n) {
       exh[n] = qt[n] <= -lim[n] && lim[n] > Z;
-      if (exh[n]) drq[n] = -rq[n];
+      drq[n] = exh[n] ? -rq[n] : D(qt[n] * rgdt);
       sum += drq[n];
     }
     drq[0] = -sum;
+  } else {
+#pragma unroll
+    for (int n = 0; n < 6; ++n) drq[n] = rhog * D(qt[n]) * dt;
   }
   D rq2[6];
 #pragma unroll
@@ -624,16 +643,24 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   const D rhoge = rhoge3 + LHF0 * drq[5];
   D q2[6];
   q2[0] = qn[0];
+  D cva = CVDRY, rcva = 0.0, tem_o;
+  if constexpr (kMixed) {
+    // as nsw6_cell: q from the reciprocal, T = rhoge / (rhog CVdry)
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) q2[n] = div_rn(rq2[n], rhog, rrhog);
-  D qd2 = 1.0;
+    for (int n = 1; n <= 5; ++n) q2[n] = rq2[n] * rrhog;
+    tem_o = NSW6_CK(D, 48, rhoge * rrhog * (1.0 / CVDRY));
+  } else {
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) qd2 = qd2 - q2[n];
-  D cva = qd2 * CVDRY;
+    for (int n = 1; n <= 5; ++n) q2[n] = div_rn(rq2[n], rhog, rrhog);
+    D qd2 = 1.0;
 #pragma unroll
-  for (int n = 1; n <= 5; ++n) cva = cva + q2[n] * CVDRY;
-  const D rcva = rhog * cva;
-  const D tem_o = NSW6_CK(D, 48, rhoge / rcva);
+    for (int n = 1; n <= 5; ++n) qd2 = qd2 - q2[n];
+    cva = qd2 * CVDRY;
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) cva = cva + q2[n] * CVDRY;
+    rcva = rhog * cva;
+    tem_o = NSW6_CK(D, 48, rhoge / rcva);
+  }
   if constexpr (MODE == CA_SAVE) {
     // the outputs of nsw6_cell (the same operations on the same values)
     out->Vtr = D(Vtr);
@@ -664,18 +691,23 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   D b_q2[6];
 #pragma unroll
   for (int n = 0; n < 6; ++n) b_q2[n] = ob.q[n];
-  // tem_o = rhoge / rcva
+  // tem_o = rhoge / rcva (mixed: (rhoge / rhog) / CVdry)
   {
     const D g = ob.tem;
-    const D rr = 1.0 / rcva;
-    b_rhoge = fma(g, rr, b_rhoge);
-    const D b_rcva = -g * tem_o * rr;
-    b_rhog = fma(b_rcva, cva, b_rhog);
-    const D b_cva = b_rcva * rhog;
-    // cva = qd2 CV + sum q2 CV
-    const D b_qd2 = b_cva * CVDRY;
+    if constexpr (kMixed) {
+      b_rhoge = fma(g, rrhog * (1.0 / CVDRY), b_rhoge);
+      b_rhog = fma(-g * tem_o, rrhog, b_rhog);
+    } else {
+      const D rr = 1.0 / rcva;
+      b_rhoge = fma(g, rr, b_rhoge);
+      const D b_rcva = -g * tem_o * rr;
+      b_rhog = fma(b_rcva, cva, b_rhog);
+      const D b_cva = b_rcva * rhog;
+      // cva = qd2 CV + sum q2 CV
+      const D b_qd2 = b_cva * CVDRY;
 #pragma unroll
-    for (int n = 1; n <= 5; ++n) b_q2[n] += b_cva * CVDRY - b_qd2;
+      for (int n = 1; n <= 5; ++n) b_q2[n] += b_cva * CVDRY - b_qd2;
+    }
   }
   // q2[n] = rq2[n] / rhog
 #pragma unroll
@@ -1391,7 +1423,22 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
   D b_densD = D(b_dens) * isc;
   b_tempD += D(b_temp) * isc;
   D b_rhogD = b_rhog;
-  {
+  if constexpr (kMixed) {
+    // pre = (densR pq) temp, pq = qd RDRY + qn0 RVAP, qd = 1 - sum qn (FP32)
+    const R tR = R(temp);
+    b_tempD = fma(D(b_pre * dpR), isc, b_tempD);
+    const R b_dp = b_pre * tR;
+    b_densD = fma(D(b_dp * pqR), isc, b_densD);
+    const R b_pq = b_dp * densR;
+    const D b_qd = D(b_pq * R(RDRY)) * isc;
+    b_qn[0] = fma(D(b_pq * R(RVAP)), isc, b_qn[0]);
+#pragma unroll
+    for (int n = 1; n <= 5; ++n) b_qn[n] -= b_qd;
+    // rhoge0 = (temp rhog) CVdry
+    const D b_trh = b_rhoge0 * CVDRY;
+    b_tempD = fma(b_trh, rhog, b_tempD);
+    b_rhogD = fma(b_trh, temp, b_rhogD);
+  } else {
     const D b_preD = D(b_pre) * isc;
     b_tempD = fma(b_preD, dp, b_tempD);
     const D b_dp = b_preD * temp;
@@ -1408,7 +1455,7 @@ __device__ __forceinline__ void nsw6_cell_adjoint(const ConstsT<R>& C, const M& 
 #pragma unroll
     for (int n = 1; n <= 5; ++n) b_qn[n] += b_cv * CVDRY - b_qd;
   }
-  // qn[n] = rq[n] / rhog (n >= 1); dens = rhog / gsgam2
+  // qn[n] = rq[n] / rhog (n >= 1); dens = rhog / gsgam2 (mixed: in FP32, the same partials)
   {
 #pragma unroll
     for (int n = 1; n <= 5; ++n) {
