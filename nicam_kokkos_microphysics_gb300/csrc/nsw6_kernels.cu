@@ -518,10 +518,12 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
   q[I_QC] = 0.0;
   // q[QC] (and q[QI] in satadjust_all) is +0 now: its terms leave the sums
   // below as they are (no partial sum is -0), so they are not formed
-  double cvtot = qd * CVDRY;
+  // MIX: every CVW is CVdry, so the sum is formed first and scaled once
+  double cvtot = MIX ? qd : qd * CVDRY;
 #pragma unroll
   for (int n = 2; n <= 5; ++n)
-    if (n != I_QI || !ice_adj) cvtot = cvtot + q[n] * CVDRY;
+    if (n != I_QI || !ice_adj) cvtot = MIX ? cvtot + q[n] : cvtot + q[n] * CVDRY;
+  if (MIX) cvtot = cvtot * CVDRY;
   const double rho_l = rho;
   double tem = (ein_moist - q[I_QV] * LHV0) / cvtot;
   if (interior) {
@@ -597,10 +599,13 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
 #pragma unroll
       for (int n = 1; n <= 5; ++n)
         if (!((zero >> n) & 1u)) qdf = qdf - q[n];
-      cva = qdf * CVDRY;
+      cva = CVDRY;   // MIX: qdf CVdry + sum q CVdry is CVdry up to roundings
+      if (!MIX) {
+        cva = qdf * CVDRY;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n)
-        if (!((zero >> n) & 1u)) cva = cva + q[n] * CVDRY;
+        for (int n = 1; n <= 5; ++n)
+          if (!((zero >> n) & 1u)) cva = cva + q[n] * CVDRY;
+      }
     } else {
       rhog_o = rhog * (1.0 - diffq);
       rho = rhog_o / gsg;
@@ -610,9 +615,12 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
       qdf = 1.0;
 #pragma unroll
       for (int n = 1; n <= 5; ++n) qdf = qdf - q[n];
-      cva = qdf * CVDRY;
+      cva = CVDRY;
+      if (!MIX) {
+        cva = qdf * CVDRY;
 #pragma unroll
-      for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
+        for (int n = 1; n <= 5; ++n) cva = cva + q[n] * CVDRY;
+      }
     }
     rhoge = tem * rhog_o * cva;
     pre = rho * (qdf * RDRY + q[I_QV] * RVAP) * tem;
@@ -694,9 +702,17 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
   for (int c = threadIdx.x; c < GF_COUNT * K; c += blockDim.x) S.grid[c] = P.grid[c];
   for (int c = threadIdx.x; c < 2 * K; c += blockDim.x)
     zkey[c] = cmp_key(P.grid[(c < K ? GF_GZH : GF_GZSHIFT) * K + c % K]);
+  // MIX: the tile's unit vectors ix, iy, iz, jx, jy, jz in FP32 ([6][COL_TG]);
+  // they meet FP32 values only (the velocity components, the momentum tendencies)
+  float* uvf = gf + 8 * K;
   if (MIX) {
     const int rows[8] = {GF_DGZ, GF_DGZH, GF_RDGZ, GF_RDGZH, GF_AFACT, GF_BFACT, GF_CFACT, GF_DFACT};
     for (int c = threadIdx.x; c < 8 * K; c += blockDim.x) gf[c] = (float)P.grid[rows[c / K] * K + c % K];
+    for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) {
+      const int a = c / COL_TG, g = g0 + c % COL_TG;
+      const double* u = a == 0 ? P.ix : a == 1 ? P.iy : a == 2 ? P.iz : a == 3 ? P.jx : a == 4 ? P.jy : P.jz;
+      uvf[c] = g < G ? (float)u[(size_t)l * G + g] : 0.0f;
+    }
   }
   for (int c = threadIdx.x; c < 6 * COL_TG; c += blockDim.x) S.colacc[c] = 0.0;
   if (tab_smem)
@@ -808,13 +824,12 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
     const double rgsg = 1.0 / gsg;
     if (!MIX) F(S_BASE)[c] = rgsg;
     if (interior) F(S_RGS)[c] = div_rn(P.gam2[i], gsg, rgsg);
-    const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
-    const double vi = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
-    const double vj = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
     if (MIX) {
-      // the velocity components scale FP32 momentum sources only
-      FF(S_VI)[c] = (float)vi;
-      FF(S_VJ)[c] = (float)vj;
+      // the velocity components scale FP32 momentum sources only: FP32
+      const float vx = (float)P.vx[i], vy = (float)P.vy[i], vz = (float)P.vz[i];
+      FF(S_VI)[c] = __fmaf_rn(vz, uvf[2 * COL_TG + gx], __fmaf_rn(vy, uvf[1 * COL_TG + gx], __fmul_rn(vx, uvf[gx])));
+      FF(S_VJ)[c] =
+          __fmaf_rn(vz, uvf[5 * COL_TG + gx], __fmaf_rn(vy, uvf[4 * COL_TG + gx], __fmul_rn(vx, uvf[3 * COL_TG + gx])));
       const float gsgf = (float)gsg, ghf = (float)P.gsgam2h[i], rhogf = (float)P.rhog[i];
       FF(S_VI)[ncell + c] = ghf;
       FF(S_VJ)[ncell + c] = gsgf;
@@ -829,8 +844,9 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       }
       continue;
     }
-    F(S_VI)[c] = vi;
-    F(S_VJ)[c] = vj;
+    const double vx = P.vx[i], vy = P.vy[i], vz = P.vz[i];
+    F(S_VI)[c] = vx * P.ix[ic] + vy * P.iy[ic] + vz * P.iz[ic];
+    F(S_VJ)[c] = vx * P.jx[ic] + vy * P.jy[ic] + vz * P.jz[ic];
     if (interior) {
       const double rvx = P.rhogvx[i], rvy = P.rhogvy[i], rvz = P.rhogvz[i];
       F(S_KINH)[c] = 0.5 * (rvx * rvx + rvy * rvy + rvz * rvz) / P.rhog[i];
@@ -1162,11 +1178,18 @@ __global__ void __launch_bounds__(384, 2) nsw6_column_kernel(Problem P, Consts C
       F(S_KINH)[c] = F(S_KINH)[c] + F(S_DKINH)[c];
       F(S_KINV)[c] = F(S_KINV)[c] + F(S_DKINV)[c];
     }
-    const double du = MIX ? (double)FF(S_DRHOGU)[c] : F(S_DRHOGU)[c];
-    const double dv = MIX ? (double)FF(S_DRHOGV)[c] : F(S_DRHOGV)[c];
-    P.rhogvx[i] = P.rhogvx[i] + du * P.ix[ic] + dv * P.jx[ic];
-    P.rhogvy[i] = P.rhogvy[i] + du * P.iy[ic] + dv * P.jy[ic];
-    P.rhogvz[i] = P.rhogvz[i] + du * P.iz[ic] + dv * P.jz[ic];
+    if (MIX) {
+      // the FP32 momentum tendencies along the FP32 unit vectors, added to the FP64 state
+      const float du = FF(S_DRHOGU)[c], dv = FF(S_DRHOGV)[c];
+      P.rhogvx[i] = P.rhogvx[i] + (double)__fmaf_rn(dv, uvf[3 * COL_TG + gx], __fmul_rn(du, uvf[gx]));
+      P.rhogvy[i] = P.rhogvy[i] + (double)__fmaf_rn(dv, uvf[4 * COL_TG + gx], __fmul_rn(du, uvf[1 * COL_TG + gx]));
+      P.rhogvz[i] = P.rhogvz[i] + (double)__fmaf_rn(dv, uvf[5 * COL_TG + gx], __fmul_rn(du, uvf[2 * COL_TG + gx]));
+    } else {
+      const double du = F(S_DRHOGU)[c], dv = F(S_DRHOGV)[c];
+      P.rhogvx[i] = P.rhogvx[i] + du * P.ix[ic] + dv * P.jx[ic];
+      P.rhogvy[i] = P.rhogvy[i] + du * P.iy[ic] + dv * P.jy[ic];
+      P.rhogvz[i] = P.rhogvz[i] + du * P.iz[ic] + dv * P.jz[ic];
+    }
     const double rw = P.rhogw[i] + (MIX ? (double)FF(S_DRHOGW)[c] : F(S_DRHOGW)[c]);
     P.rhogw[i] = rw;
     if (!MIX) F(S_DRHOGW)[c] = rw;   // MIX: the FP32 view of this slot is still being read
@@ -1432,7 +1455,8 @@ size_t column_smem_bytes(int K, bool opt) {
   const size_t nrow = opt ? 8 : 6;
   const size_t ntab = (!opt || K <= COL_FMTAB_SMEM_KMAX) ? FM_TABLE_DOUBLES : 0;
   return sizeof(double) * (nslot * K * TG + GF_COUNT * K + 6 * TG + ntab) +
-         sizeof(int) * 2 * nrow * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 8 * K;
+         sizeof(int) * 2 * nrow * K + (size_t)K * TG + 16 + sizeof(long long) * 2 * K + sizeof(float) * 8 * K +
+         sizeof(float) * 6 * TG;
 }
 
 int column_threads(int K) {
