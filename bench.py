@@ -63,19 +63,19 @@ CELL_KERNEL_BYTES_PER_CELL = (10 + 17) * 8
 # and nsw6_satadj_kernel (the saturated cells), timed together as one
 # interval; its figures are the two kernels' sums.
 CELL_KERNEL_TRAFFIC_PER_CELL = {"fp64": 229.0, "mixed": 172.4}
-COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 379.8 + 30.0, "mixed": 394.1 + 30.1}
+COLUMN_KERNEL_TRAFFIC_PER_CELL = {"fp64": 379.8 + 30.0, "mixed": 386.4 + 30.0}
 FP64_EXECUTED = {
     "nsw6_cell_kernel": {"fp64": {"dfma": 353.9, "dadd": 258.8, "dmul": 273.0, "pipe": 901.5},
                          "mixed": {"dfma": 5.0, "dadd": 43.0, "dmul": 20.1, "pipe": 91.9}},
     "nsw6_column_kernel": {"fp64": {"dfma": 113.8 + 9.9, "dadd": 137.4 + 6.0, "dmul": 144.8 + 5.4,
                                     "pipe": 403.0 + 21.6},
-                           "mixed": {"dfma": 37.3 + 9.0, "dadd": 79.7 + 6.0, "dmul": 76.2 + 5.4,
-                                     "pipe": 237.3 + 20.7}},
+                           "mixed": {"dfma": 37.3 + 9.0, "dadd": 69.0 + 5.8, "dmul": 55.8 + 6.2,
+                                     "pipe": 208.5 + 21.4}},
 }
 # FP64-pipe activity (fraction of active cycles) of each kernel in the same
 # captures (cold, serialised launches; the column kernel alone).
-FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.839, "mixed": 0.657},
-                    "nsw6_column_kernel": {"fp64": 0.732, "mixed": 0.626}}
+FP64_PIPE_ACTIVE = {"nsw6_cell_kernel": {"fp64": 0.839, "mixed": 0.656},
+                    "nsw6_column_kernel": {"fp64": 0.732, "mixed": 0.585}}
 # FP64 op weights in flop equivalents (an FMA counts 2): the cost of CUDA's FP64
 # divide, sqrt, exp, log and pow relative to DFMA, measured once on a GB300 with
 # the throughput probe (probe/nsw6_probe.cu) and frozen here.
