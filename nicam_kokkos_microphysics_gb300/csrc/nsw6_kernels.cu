@@ -649,14 +649,16 @@ __device__ __forceinline__ bool final_cell(const Problem& P, const Consts& C, co
   return false;
 }
 
-// MIX: the mixed-precision step: every flux of the sedimentation (mass,
-// energy, kinetic energy and momentum, full and half levels) is integrated in
-// FP32 from its FP64 source, the mass, energy and kinetic-energy divergences
-// accumulated in FP64 and the momentum ones in FP32, and the quotients of the
-// final state use a plain reciprocal; the state updates, KIN2EIN, the
-// thermodynamics and the saturation adjustment stay FP64.
+// MIX: the mixed-precision step: the mass and energy fluxes of the
+// sedimentation (mass, internal and potential energy) are integrated and their
+// divergences summed in FP64 as in the FP64 step; the kinetic-energy and
+// momentum fluxes, their sources, the kinetic energies, their tendencies and
+// the KIN2EIN correction are FP32; the quotients of the final state use a
+// plain reciprocal and its cv sums are lean (every CVW is CVdry); the state
+// updates, the internal-energy budget, the thermodynamics and the saturation
+// adjustment stay FP64.
 //
-// OPT: the kernel with the scheme switches (FP64): QI sedimentation (4
+// OPT: the kernel with the scheme switches (either precision): QI sedimentation (4
 // tracers), the KIN2KIN kinetic-energy correction (mod_precip_transport.cpp:
 // 1012-1068) and the mixed-phase saturation adjustment (satadjust_all,
 // mod_satadjust.cpp:620-769).
