@@ -88,8 +88,9 @@ constexpr int CELL_CK_SLOTS = 49;
 // The checkpoint of cell c: slot s at element c + s * stride of the buffer p
 // viewed as an array of the rate precision R (the buffer holds CELL_CK_SLOTS
 // doubles per cell).  The mixed-precision step's FP32 slots use its first
-// half; its three FP64 slots (0: 1 / rhog, 1: rhog / gsgam2, 48: the
-// temperature) sit as doubles at rows CK_MIXED_D, + 1, + 2 of the second.
+// half (slot 1, the density, is FP32 there); its FP64 slots (0: 1 / rhog,
+// 48: the temperature) sit as doubles at rows CK_MIXED_D and CK_MIXED_D + 2 of
+// the second.
 struct CellCk {
   double* p;
   size_t stride, c;
