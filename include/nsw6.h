@@ -137,8 +137,10 @@ int nsw6_eval_math(nsw6_handle* h, int fn, const double* x, const double* y, dou
  * energy budgets, the flux sums of the transport and the saturation-
  * adjustment Newton iteration with its vapour pressure stay FP64; 2 the FP64
  * step evaluated one column per thread by the code the tangent-linear and
- * adjoint kernels are built from (bitwise equal to 0; for checking them).  No
- * counterpart in the reference (FP64 only). */
+ * adjoint kernels are built from (bitwise equal to 0; for checking them;
+ * device arrays only: mp_driver_argv with host = 1 returns
+ * NSW6_ERR_UNSUPPORTED in this mode).  No counterpart in the reference (FP64
+ * only). */
 int nsw6_set_precision(nsw6_handle* h, int mode);
 
 /* Per-kernel timing with CUDA events recorded on the handle's stream around

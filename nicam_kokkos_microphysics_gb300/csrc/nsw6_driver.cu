@@ -804,6 +804,9 @@ bool host_args_pinned(nsw6_handle* h, double* const* args) {
 }
 
 int run_host(nsw6_handle* h, int lall, double* const* args, double dt) {
+  // precision 2, the serial check path, runs on device arrays only (its
+  // pre-pass uses the staging buffers this entry copies into)
+  if (h->mixed == 2) return NSW6_ERR_UNSUPPORTED;
   for (int i = 0; i < A_COUNT; ++i)
     if ((arg_is_read(i) || arg_is_written(i)) && !args[i]) return NSW6_ERR_BAD_ARG;
   if (h->opts.aerosol_indirect && !args[A_unccn]) return NSW6_ERR_BAD_ARG;

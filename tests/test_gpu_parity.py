@@ -225,6 +225,29 @@ def test_gpu_unread_input_parts(precision, options):
     drv.close()
 
 
+def test_gpu_host_entry_rejects_serial_precision():
+    """Precision 2, the serial check path, takes device arrays only: the
+    host entry refuses it (NSW6_ERR_UNSUPPORTED) instead of running another
+    step, and the handle still runs the device entry afterwards."""
+    torch = _torch()
+    from nicam_kokkos_microphysics_gb300 import NSW6Error, mp_init
+    spec = StateSpec(gall=40, kall=42, lall=1, seed=13, variant="standard")
+    st = make_state(spec, out_fill=np.nan)
+    drv = mp_init("NSW6", spec.gall, spec.kall, st["_gz"], st["_gzh"])
+    drv.set_precision("serial")
+    host = {n: st[n].copy() for n in ARG_NAMES}
+    with pytest.raises(NSW6Error) as err:
+        drv.run(host, dt=spec.dt)
+    assert err.value.code == 5
+    for n in OUTPUT_NAMES:
+        assert np.array_equal(host[n], st[n], equal_nan=True), n
+    dev = {n: torch.from_numpy(st[n].copy()).cuda() for n in ARG_NAMES}
+    drv.run(dev, dt=spec.dt)
+    torch.cuda.synchronize()
+    assert np.isfinite(dev["rhog"].cpu().numpy()).all()
+    drv.close()
+
+
 def test_gpu_all_saturated_state_matches_oracle():
     """Every interior cell supersaturated (vapour at 1.5 qsat): after the cell
     physics about 40 % of the interior cells are still saturated (the oracle
