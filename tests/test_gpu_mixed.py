@@ -74,8 +74,15 @@ def test_mixed_with_switches_within_targets(name, variant, seed):
     check_targets(variant, seed, OPTION_SETS[name], label=name)
 
 
-def check_targets(variant, seed, options=None, label=""):
-    fp64, mixed = run_both(StateSpec(gall=16900, kall=42, lall=1, seed=seed, variant=variant), options)
+@pytest.mark.parametrize("kall", [96, 160])
+def test_mixed_deep_columns_within_targets(kall):
+    """Deep columns: above 64 levels the column kernel runs its 8-column tile
+    (its FP32 halves, unit vectors and metric rows sized by that tile)."""
+    check_targets("convective", 1100 + kall, label=f"kall {kall}", gall=2000, kall=kall)
+
+
+def check_targets(variant, seed, options=None, label="", gall=16900, kall=42):
+    fp64, mixed = run_both(StateSpec(gall=gall, kall=kall, lall=1, seed=seed, variant=variant), options)
     lines = []
     for n in OUTPUT_NAMES:
         assert np.isfinite(mixed[n]).all(), n
